@@ -1,0 +1,359 @@
+"""Benchmark: path-traced Msamples/s of the plain path tracer on the 1M-triangle seeded scene
+at 1920x1080, 64 samples per pixel, 8 bounces (one step = one Renderer.render_to_target
+over the whole image), on N GB300s (one replica per GPU: the path does not shard across
+GPUs, every rank renders its own full frame; scaling is weak).
+
+Prints one JSON line (rank 0).  `value` is the device-resident throughput (scene, BVH and
+target already in HBM), `e2e` the same metric through Renderer.render_to_texture with the
+target downloaded to pinned host memory every step.  `roofline` relates the integrate
+kernel's algorithmic bytes (BVH nodes, triangle records, instance records, hit shading
+data; counted by the instrumented kernel on the same frame) to its CUDA-event duration and
+the measured HBM copy bandwidth.  `cpu_baseline` times the CPU oracle on a bounded sample
+of the same frame.
+
+--impl reference times the reference path tracer's CPU restatement (the oracle: the
+reference itself is Rust + Vulkan/GLSL and cannot run on this machine) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Msamples/s at 1080p, plain path tracer"
+UNIT = "Msamples/s"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--spp", type=int, default=64)
+    p.add_argument("--depth", type=int, default=8)
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--instances", type=int, default=64)
+    p.add_argument("--freq", type=int, default=28)
+    p.add_argument("--lights", type=int, default=1000)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the cpu_baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- distributed helpers
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(path.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch() -> float | None:
+    """dram__bytes_read.sum + dram__bytes_write.sum of one integrate launch of this workload,
+    from the committed ncu summary (profiles/integrate_icosphere_field_1080p.md)."""
+    f = ROOT / "profiles" / "integrate_icosphere_field_1080p.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_per_launch_bytes:\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+# ---------------------------------------------------------------- workload
+def make_workload(a):
+    from tinytrace_gb300 import scenes
+
+    return scenes.icosphere_workload(extent=(a.width, a.height), spp=a.spp, depth=a.depth,
+                                     instances=a.instances, freq=a.freq, lights=a.lights)
+
+
+def cpu_baseline(w, arrays, target_seconds: float) -> dict:
+    """The oracle (a scalar C++ restatement, OpenMP over pixels on every host core) on a
+    band of rows of the same frame at 1 sample per pixel."""
+    from oracle import oracle
+    from tinytrace_gb300.renderer import Config, make_constants
+
+    cfg = Config(bounce_count=w.config.bounce_count, sample_count=1, tonemap=w.config.tonemap,
+                 light_sampling=w.config.light_sampling)
+    t0 = time.perf_counter()
+    orc = oracle.OracleScene(arrays)
+    build_s = time.perf_counter() - t0
+    c = make_constants(w.camera, w.extent, cfg, 0, 0)
+    W, H = w.extent
+    target = np.zeros((H, W, 4), np.float32)
+    # calibrate on a thin band, then size the band for ~target_seconds
+    y0 = H // 2 - 4
+    t0 = time.perf_counter()
+    orc.render(c, target, rows=(y0, y0 + 8))
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rows = int(max(8, min(H, 8 * target_seconds / dt)))
+    y0 = max(0, H // 2 - rows // 2)
+    t0 = time.perf_counter()
+    orc.render(c, target, rows=(y0, y0 + rows))
+    dt = time.perf_counter() - t0
+    samples = rows * W
+    return {"value": samples / dt / 1e6, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{rows} rows x {W} px of the {W}x{H} frame at 1 spp, depth {cfg.bounce_count} "
+                      f"({samples} samples, {dt:.1f} s; BVH build {build_s:.1f} s excluded)"}
+
+
+def run_reference(a, dist: Dist):
+    if dist.rank != 0:
+        return
+    from tinytrace_gb300.renderer import SceneArrays
+
+    w = make_workload(a)
+    arrays = SceneArrays(w.scene)
+    per_step = max(2.0, min(20.0, 60.0 / max(1, a.steps + a.warmup)))
+    for _ in range(min(a.warmup, 1)):
+        cpu_baseline(w, arrays, per_step / 4)
+    vals = []
+    last = None
+    for _ in range(a.steps):
+        last = cpu_baseline(w, arrays, per_step)
+        vals.append(last["value"])
+    v = statistics.median(vals)
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded generator)", "impl": "reference",
+           "config": {"workload": w.name, "triangles": arrays.triangle_count, "resolution": list(w.extent),
+                      "spp": w.config.sample_count, "depth": w.config.bounce_count},
+           "cpu_baseline": {**last, "value": v},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "reference arm = the reference path tracer restated on the CPU (oracle/); the reference "
+                   "itself (Rust + Vulkan ray queries) cannot run on this machine"}
+    print(json.dumps(out))
+
+
+def run_ours(a, dist: Dist):
+    import ctypes
+
+    from tinytrace_gb300 import native
+    from tinytrace_gb300.native import check
+    from tinytrace_gb300.renderer import Renderer
+
+    device = dist.local_rank
+    w = make_workload(a)
+    r = Renderer(w.extent, device=device)
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    r.set_config(w.config)
+    lib, ctx = r.context.lib, r.context.handle
+    stats = r.context.scene_stats(r.scene)
+    W, H = w.extent
+    spp = w.config.sample_count
+    samples_per_step = W * H * spp
+
+    def step():
+        check(lib.tt_flush_l2(ctx))
+        r.render_to_target()
+        r.present()
+
+    for _ in range(a.warmup):
+        step()
+    check(lib.tt_synchronize(ctx))
+    dist.barrier()
+    clocks = ClockSampler(device)
+    clocks.start()
+    check(lib.tt_synchronize(ctx))
+    check(lib.tt_event_record(ctx, 0))
+    kernel_ns = []
+    for _ in range(a.steps):
+        step()
+        kernel_ns.append(r.timings().integrate * 1e9)  # synchronises; integrate-kernel events
+    check(lib.tt_event_record(ctx, 1))
+    ms = ctypes.c_float()
+    check(lib.tt_event_elapsed_ms(ctx, 0, 1, ctypes.byref(ms)))
+    check(lib.tt_synchronize(ctx))
+    clk = clocks.stop()
+    dist.barrier()
+    total_s = dist.max(ms.value / 1e3)
+    value = samples_per_step * a.steps * dist.world / total_s / 1e6
+
+    # end to end through the public API: render_to_texture into pinned host memory
+    host = ctypes.c_void_p()
+    nbytes = W * H * 16
+    check(lib.tt_host_alloc(nbytes, ctypes.byref(host)))
+    out = np.ctypeslib.as_array((ctypes.c_float * (W * H * 4)).from_address(host.value)).reshape(H, W, 4)
+    e2e_steps = max(1, min(a.steps, 3))
+    r.render_to_target()
+    r.context.download(r.render_target, W, H, out)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        check(lib.tt_flush_l2(ctx))
+        r.render_to_target()  # 368-byte Constants host -> device with the launch
+        r.context.download(r.render_target, W, H, out)  # W*H*16 bytes device -> host, synchronous
+        r.present()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    check(lib.tt_host_free(host))
+    e2e = samples_per_step * e2e_steps * dist.world / e2e_s / 1e6
+
+    # roofline accounting: counters of the instrumented kernel on the same frame
+    cnt = native.TraversalCounters()
+    c = r.constants()
+    check(lib.tt_render_counted(ctx, r.scene, native.ptr(c), r.render_target, ctypes.byref(cnt)))
+    node_bytes = (cnt.blas_nodes + cnt.tlas_nodes) * 64
+    tri_bytes = cnt.triangles * 48
+    inst_bytes = cnt.instances * 64
+    hit_bytes = cnt.hits * (208 + 12 + 18 + 24 + 304)
+    target_bytes = W * H * 16 * 2
+    alg_bytes = node_bytes + tri_bytes + inst_bytes + hit_bytes + target_bytes
+    kernel_s = statistics.mean(kernel_ns) / 1e9
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / kernel_s / 1e9
+
+    out_line = None
+    if dist.rank == 0:
+        cpu = None
+        if not a.no_cpu_baseline:
+            cpu = cpu_baseline(w, r.scene_arrays, a.cpu_seconds)
+        traffic = ncu_traffic_per_launch()
+        out_line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": total_s * 1e3 / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+            "config": {"workload": w.name, "triangles": int(stats.triangle_count),
+                       "instances": int(stats.instance_count), "emissive_triangles": int(stats.emissive_count),
+                       "resolution": [W, H], "spp": spp, "depth": w.config.bounce_count,
+                       "light_sampling": "next_event_estimation",
+                       "l2": "flushed before every step (512 MiB memset, inside the timed region)",
+                       "parallelism": f"replicas x{dist.world}"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 368, "d2h_bytes_per_step": nbytes,
+                    "steps": e2e_steps},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": traffic, "kernel": "integrate_kernel",
+                         "kernel_ms": kernel_s * 1e3,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "node_fetch_bytes_per_launch": node_bytes,
+                         "node_fetch_frac": node_bytes / kernel_s / 1e9 / peak},
+            "counters": {"rays": cnt.rays, "blas_nodes": cnt.blas_nodes, "tlas_nodes": cnt.tlas_nodes,
+                         "triangles": cnt.triangles, "instances": cnt.instances, "hits": cnt.hits},
+            "scene": {"blas_nodes": int(stats.blas_nodes), "tlas_nodes": int(stats.tlas_nodes),
+                      "blas_levels": int(stats.blas_levels), "tlas_levels": int(stats.tlas_levels),
+                      "device_bytes": int(stats.device_bytes), "build_ms": None},
+            "clocks": clk,
+            "gpu_launches": a.steps,
+            "cpu_baseline": cpu,
+        }
+        t = native.Timings()
+        check(lib.tt_timings_get(ctx, ctypes.byref(t)))
+        out_line["scene"]["build_ms"] = t.scene_build_ns / 1e6
+    r.close()
+    if out_line is not None:
+        print(json.dumps(out_line))
+
+
+def main():
+    a = parse_args()
+    dist = Dist()
+    try:
+        if a.impl == "reference":
+            run_reference(a, dist)
+        else:
+            run_ours(a, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

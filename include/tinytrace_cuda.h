@@ -1,0 +1,240 @@
+/*
+ * tinytrace_cuda.h — C ABI of libtinytrace_cuda.so, the GB300 (sm_103a) replacement for the
+ * part of tinytrace_backend::Context that the tinytrace rendering hot path uses.
+ *
+ * The reference renderer (crate `tinytrace`) drives a Vulkan backend; the calls it makes on
+ * the hot path are listed beside each entry point as "replaces: <file>:<line>" (paths are
+ * relative to the reference project root).  The Rust `Renderer`, `Scene`, `Camera` and
+ * `Config` keep their signatures; a thin FFI crate maps them onto these functions.
+ *
+ * Conventions
+ *   - Every function returns a status (TT_OK == 0) except tt_last_error / tt_abi_version.
+ *     The message of the last failure on the calling thread is returned by tt_last_error().
+ *   - Host arrays are borrowed for the duration of the call only.
+ *   - Device resources are owned by the context and named by opaque 64-bit handles
+ *     {lifetime:8, epoch:24, index:32}; a handle whose lifetime was cleared since it was
+ *     created is rejected with TT_ERR_BAD_HANDLE (the reference panics instead,
+ *     crates/tinytrace_backend/src/lib.rs:231-233).
+ *   - A context is used by one thread at a time and owns one CUDA stream.
+ *   - All structs are plain C with the byte layout of the reference's #[repr(C)] types.
+ */
+#ifndef TINYTRACE_CUDA_H
+#define TINYTRACE_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TT_ABI_VERSION 1
+
+/* status codes */
+#define TT_OK 0
+#define TT_ERR_INVALID_ARGUMENT 1
+#define TT_ERR_OOM 2
+#define TT_ERR_BAD_HANDLE 3
+#define TT_ERR_DEVICE 4
+#define TT_ERR_TIMEOUT 5
+#define TT_ERR_OVERFLOW 6
+#define TT_ERR_UNSUPPORTED 7
+#define TT_ERR_NO_DEVICE 8
+
+/* resource lifetimes: crates/tinytrace_backend/src/lib.rs:61-73 */
+#define TT_LIFETIME_STATIC 0
+#define TT_LIFETIME_SURFACE 1
+#define TT_LIFETIME_SCENE 2
+#define TT_LIFETIME_FRAME 3
+#define TT_LIFETIME_RENDERER 4
+
+/* light sampling: src/config.rs:3-12, src/includes/constants.glsl:4-6 */
+#define TT_LIGHT_SAMPLING_ON_HIT 1
+#define TT_LIGHT_SAMPLING_NEXT_EVENT_ESTIMATION 2
+
+/* tonemap output formats (the swapchain write of src/post_process/display.glsl:11 made headless) */
+#define TT_FORMAT_RGBA32F 0
+#define TT_FORMAT_RGBA8_UNORM 1
+
+/* trace flags */
+#define TT_TRACE_CULL_BACK_FACES 1u
+
+typedef struct tt_context tt_context;
+typedef uint64_t tt_handle;
+
+/* src/includes/constants.glsl:8-15 == src/lib.rs:234-250 (368 bytes, column-major mat4) */
+typedef struct tt_constants {
+    float view[16], proj[16], proj_view[16], inverse_view[16], inverse_proj[16];
+    float camera_position[4];
+    uint32_t frame_index, accumulated_frame_count, sample_count, bounce_count;
+    uint32_t screen_size[2];
+    uint32_t tonemap;
+    uint32_t light_sampling;
+} tt_constants;
+
+/* src/material/material.glsl:10-38 == src/asset/material.rs:203-231 (192 bytes) */
+typedef struct tt_material_constants {
+    float base_color[4], specular_color[4], transmission_color[4], coat_color[4], fuzz_color[4],
+        emission_color[4], geometry_normal[4];
+    float base_weight, base_metalness, base_diffuse_roughness, specular_weight,
+        specular_roughness, specular_roughness_anisotropy, specular_ior, specular_rotation,
+        transmission_weight, transmission_depth, coat_weight, coat_roughness,
+        coat_roughness_anisotropy, coat_ior, coat_darkening, coat_rotation, fuzz_weight,
+        fuzz_roughness, emission_luminance, geometry_opacity;
+} tt_material_constants;
+
+/* src/asset/material.rs:268-274 ProcessedMaterial (304 bytes); texture index u32::MAX = none */
+typedef struct tt_material {
+    tt_material_constants constants;
+    uint32_t textures[27];
+    uint32_t padding;
+} tt_material;
+
+/* src/asset/mod.rs:44-47 ProcessedVertex (8 bytes): f16 uv[2] + packed tangent frame */
+typedef struct tt_vertex {
+    uint16_t texture_coordinates[2];
+    uint32_t tangent_frame;
+} tt_vertex;
+
+/* src/asset/mod.rs:49-64 ProcessedMesh (32 bytes) */
+typedef struct tt_mesh {
+    float bounding_sphere_center[3];
+    float bounding_sphere_radius;
+    uint32_t vertex_offset, vertex_count, index_offset, index_count;
+} tt_mesh;
+
+/* src/scene.rs:236-246 Instance (208 bytes) */
+typedef struct tt_instance {
+    float transform[16], inverse_transform[16], normal_transform[16];
+    uint32_t vertex_offset, index_offset, material_index, mesh_index;
+} tt_instance;
+
+/* src/asset/mod.rs:68-73 EmissiveTriangle (36 bytes) */
+typedef struct tt_emissive_triangle {
+    int16_t positions[3][3];
+    uint16_t hash;
+    uint16_t texture_coordinates[3][2];
+    uint32_t instance_index;
+} tt_emissive_triangle;
+
+/* The arrays of asset::Scene (src/asset/mod.rs:77-86) plus the flattened instances and
+ * emissive triangles that Scene::new derives from the node tree (src/scene.rs:29-64). */
+typedef struct tt_scene_desc {
+    const int16_t* positions; /* position_count x [i16; 3], snorm16 */
+    uint64_t position_count;
+    const uint32_t* indices;
+    uint64_t index_count;
+    const tt_vertex* vertices;
+    uint64_t vertex_count;
+    const tt_material* materials;
+    uint32_t material_count;
+    uint32_t mesh_count;
+    const tt_mesh* meshes;
+    const tt_instance* instances;
+    uint32_t instance_count;
+    uint32_t emissive_triangle_count;
+    const tt_emissive_triangle* emissive_triangles;
+} tt_scene_desc;
+
+/* src/lib.rs:228-232 Timings, in nanoseconds of device time */
+typedef struct tt_timings {
+    uint64_t integrate_ns;
+    uint64_t post_process_ns;
+    uint64_t scene_build_ns;
+} tt_timings;
+
+typedef struct tt_scene_stats {
+    uint64_t triangle_count, instance_count, emissive_count;
+    uint64_t blas_nodes, tlas_nodes, blas_levels, tlas_levels;
+    uint64_t device_bytes;
+    uint64_t max_stack;
+} tt_scene_stats;
+
+/* Traversal counters from the instrumented render (roofline accounting). */
+typedef struct tt_traversal_counters {
+    uint64_t rays, blas_nodes, tlas_nodes, triangles, instances, hits;
+} tt_traversal_counters;
+
+/* ---------------------------------------------------------------- context */
+int32_t tt_abi_version(void);
+const char* tt_last_error(void);
+/* replaces: crates/tinytrace_backend/src/lib.rs:171-213 Context::new(None) */
+int32_t tt_context_create(int32_t device, tt_context** out);
+int32_t tt_context_destroy(tt_context* ctx);
+/* replaces: crates/tinytrace_backend/src/lib.rs:268-270 Context::frame_index */
+int32_t tt_frame_index(tt_context* ctx, uint64_t* out);
+/* replaces the frame advance of crates/tinytrace_backend/src/lib.rs:393-410 Context::present
+ * (headless: there is no swapchain to present) */
+int32_t tt_advance_frame(tt_context* ctx);
+/* replaces: crates/tinytrace_backend/src/lib.rs:253-255 clear_resources_with_lifetime */
+int32_t tt_clear_lifetime(tt_context* ctx, uint32_t lifetime);
+/* replaces: crates/tinytrace_backend/src/lib.rs:293-300 wait_until_idle */
+int32_t tt_synchronize(tt_context* ctx);
+
+/* ---------------------------------------------------------------- images */
+/* replaces: src/lib.rs:213-226 create_render_target (create_image, Rgba32Float) */
+int32_t tt_image_create(tt_context* ctx, uint32_t lifetime, uint32_t width, uint32_t height,
+                        tt_handle* out);
+/* replaces: crates/tinytrace_backend/src/copy.rs:102-163 write_images (RGBA32F, tightly packed) */
+int32_t tt_image_write(tt_context* ctx, tt_handle image, const float* host, uint64_t bytes);
+/* replaces: crates/tinytrace_backend/src/copy.rs:183-264 download (RGBA32F, tightly packed) */
+int32_t tt_image_download(tt_context* ctx, tt_handle image, float* host, uint64_t bytes);
+
+/* ---------------------------------------------------------------- scene */
+/* replaces: src/scene.rs:28-186 Scene::new — buffer creation and upload
+ * (crates/tinytrace_backend/src/copy.rs:62-100) and the BLAS/TLAS builds
+ * (crates/tinytrace_backend/src/resource.rs:728-880, 891-1085), which become a GPU LBVH. */
+int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* desc, tt_handle* out);
+int32_t tt_scene_stats_get(tt_context* ctx, tt_handle scene, tt_scene_stats* out);
+/* BVH arrays for node-for-node comparison: blas nodes (64 B each), triangle records
+ * (48 B each), tlas nodes (64 B each).  Sizes in bytes must match tt_scene_stats. */
+int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint64_t blas_bytes,
+                              void* tris, uint64_t tri_bytes, void* tlas, uint64_t tlas_bytes);
+
+/* ---------------------------------------------------------------- rendering */
+/* replaces: src/integrate/mod.rs:39-61 Integrator::integrate (dispatch of integrate.glsl)
+ * with the timestamps of src/lib.rs:149,157 */
+int32_t tt_render(tt_context* ctx, tt_handle scene, const tt_constants* constants,
+                  tt_handle target);
+/* Same render with traversal counters (an instrumented kernel; slower). */
+int32_t tt_render_counted(tt_context* ctx, tt_handle scene, const tt_constants* constants,
+                          tt_handle target, tt_traversal_counters* out);
+/* replaces: src/post_process/mod.rs:42-57 PostProcess::run (display.glsl) writing a host
+ * buffer instead of a swapchain image; format TT_FORMAT_*. */
+int32_t tt_tonemap(tt_context* ctx, tt_handle image, const tt_constants* constants,
+                   uint32_t format, void* host_out, uint64_t bytes);
+/* replaces: src/lib.rs:167-178 Renderer::timings */
+int32_t tt_timings_get(tt_context* ctx, tt_timings* out);
+
+/* ---------------------------------------------------------------- parity entry points */
+/* replaces: src/material/test.rs:112-151 BdsfSampler::sample.  samples: n x 8 floats
+ * (wi xyz, generator state bits, wo xyz, 0); results: n x 8 floats (bsdf rgb, pdf,
+ * generator state after bsdf_prepare, probability of the diffuse, metal, specular lobes). */
+int32_t tt_bsdf_eval_batch(tt_context* ctx, const tt_material_constants* material,
+                           const float* samples, uint32_t n, float* results);
+/* bsdf_prepare + bsdf_sample (src/material/bsdf.glsl:115-120,163-203).  samples: n x 4
+ * (wi xyz, state bits); results: n x 12 (bsdf rgb, pdf, wo xyz, lobe, state bits, 0, 0, 0). */
+int32_t tt_bsdf_sample_batch(tt_context* ctx, const tt_material_constants* material,
+                             const float* samples, uint32_t n, float* results);
+/* Closest-hit ray queries (src/integrate/integrate.glsl:112-127, 168-185).  rays: n x 8
+ * floats (origin xyz, tmin, direction xyz, tmax); hits: n x 8 words (hit, t, u, v bits,
+ * instance, primitive, 0, 0).  flags: TT_TRACE_*. */
+int32_t tt_trace_batch(tt_context* ctx, tt_handle scene, const float* rays, uint32_t n,
+                       uint32_t flags, uint32_t* hits);
+/* Device elementary functions (0 sin, 1 cos, 2 exp, 3 log, 4 acos) for accuracy tests. */
+int32_t tt_math_batch(tt_context* ctx, int32_t which, const float* x, uint64_t n, float* y);
+
+/* ---------------------------------------------------------------- measurement helpers */
+/* Write a buffer larger than L2 on the context stream. */
+int32_t tt_flush_l2(tt_context* ctx);
+/* Record event `slot` (0..15) on the context stream / elapsed ms between two slots. */
+int32_t tt_event_record(tt_context* ctx, uint32_t slot);
+int32_t tt_event_elapsed_ms(tt_context* ctx, uint32_t start_slot, uint32_t end_slot, float* ms);
+/* Pinned host memory for end-to-end copies (cudaMallocHost / cudaFreeHost). */
+int32_t tt_host_alloc(uint64_t bytes, void** out);
+int32_t tt_host_free(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TINYTRACE_CUDA_H */

@@ -1,0 +1,406 @@
+// TEST INFRASTRUCTURE — the CPU oracle for the tinytrace rendering hot path.
+// Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may load this
+// library; it is the checker, never the thing measured as the product or shipped.
+//
+// A CPU restatement of the reference path tracer (src/integrate/integrate.glsl), its
+// OpenPBR BSDF (src/material/*.glsl), emissive-triangle light sampling
+// (src/includes/scene.glsl:114-136) and the neutral tonemap
+// (src/post_process/tonemap.glsl:17-26, display.glsl:6-12), plus the project's LBVH.
+// Parity status: the reference's own tests hold no golden vectors for any of this
+// (src/material/test.rs asserts nothing), and the reference cannot run here (no Rust
+// toolchain, no Vulkan), so this oracle is "parity unpinned" against the reference; it is
+// pinned by analytic checks in tests/ (reciprocity, energy, furnace, convergence).
+//
+// Exported with a C ABI for ctypes.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "ref_bsdf.h"
+#include "ref_bvh.h"
+
+using namespace ref;
+
+namespace {
+
+constexpr float EXTENSION_TMIN = 1.0e-3f, EXTENSION_TMAX = 1000.0f;  // integrate.glsl:116-117
+constexpr float SHADOW_TMIN = 1.0e-3f, SHADOW_TMAX = 10000.0f;       // integrate.glsl:170-171
+
+struct OracleScene {
+    std::vector<int16_t> positions;
+    std::vector<uint32_t> indices;
+    std::vector<Vertex> vertices;
+    std::vector<Material> materials;
+    std::vector<Mesh> meshes;
+    std::vector<Instance> instances;
+    std::vector<EmissiveTriangle> emissive;
+    SceneBvh bvh;
+    bool use_bvh = true;
+    Geometry geom() const {
+        return Geometry{positions.data(), indices.data(), instances.data(),
+                        (uint32_t)instances.size(), meshes.data(), (uint32_t)meshes.size()};
+    }
+    SceneView view() const {
+        return SceneView{positions.data(), indices.data(), vertices.data(), materials.data(),
+                         instances.data(), emissive.data(), (uint32_t)emissive.size()};
+    }
+};
+
+Hit trace(const OracleScene& s, v3 o, v3 d, float tmin, float tmax, bool cull) {
+    Geometry g = s.geom();
+    return s.use_bvh ? trace_bvh(g, s.bvh, o, d, tmin, tmax, cull)
+                     : trace_brute(g, o, d, tmin, tmax, cull);
+}
+
+struct Ray {
+    v3 direction, origin;
+};
+
+// integrate.glsl:17-20
+v3 camera_ray_direction(const Constants& c, v2 ndc) {
+    v4 vsp = mat4_mul(c.inverse_proj, v4{-ndc.x, -ndc.y, 1.0f, 1.0f});
+    v4 w = mat4_mul(c.inverse_view, v4{vsp.x, vsp.y, vsp.z, 0.0f});
+    return normalize(v3{w.x, w.y, w.z});
+}
+
+struct RayHit {
+    v3 world_position;
+    Basis tangent_space;
+    v2 uv;
+    uint32_t instance_index, material_index;
+};
+
+// integrate.glsl:22-110 (ray differentials are skipped: they only select texture mips and
+// scenes handed to this oracle carry no textures).
+RayHit get_ray_hit(const OracleScene& s, const Hit& h) {
+    RayHit hit;
+    const Instance& in = s.instances[h.instance];
+    hit.instance_index = h.instance;
+    hit.material_index = in.material_index;
+    uint32_t base = 3u * h.prim + in.index_offset;
+    uint32_t ti[3];
+    v3 pos[3];
+    for (int k = 0; k < 3; ++k) {
+        ti[k] = s.indices[base + k] + in.vertex_offset;
+        pos[k] = mat43_point(in.transform, dequantize_snorm3(&s.positions[3u * ti[k]]));
+    }
+    const Vertex* tv[3] = {&s.vertices[ti[0]], &s.vertices[ti[1]], &s.vertices[ti[2]]};
+    v3 bary = v3{0.0f, h.u, h.v};
+    bary.x = 1.0f - bary.y - bary.z;
+    TangentFrame tf[3];
+    for (int k = 0; k < 3; ++k) tf[k] = decode_tangent_frame(tv[k]->tangent_frame);
+    hit.tangent_space.normal =
+        normalize(mat3_vec(in.normal_transform, interp3(bary, tf[0].normal, tf[1].normal, tf[2].normal)));
+    hit.tangent_space.tangent = normalize(
+        mat3_vec(in.normal_transform, interp3(bary, tf[0].tangent, tf[1].tangent, tf[2].tangent)));
+    float bs = signf(tf[0].bitangent_sign * bary.x + tf[1].bitangent_sign * bary.y +
+                     tf[2].bitangent_sign * bary.z);
+    hit.tangent_space.bitangent =
+        normalize(bs * cross(hit.tangent_space.normal, hit.tangent_space.tangent));
+    hit.uv = interp2(bary, uv_of(tv[0]->uv), uv_of(tv[1]->uv), uv_of(tv[2]->uv));
+    hit.world_position = bary.x * pos[0] + bary.y * pos[1] + bary.z * pos[2];
+    return hit;
+}
+
+// integrate.glsl:148-154 (constant materials)
+v3 material_emissive(const Material& m) {
+    return xyz(m.constants.emission_color) * m.constants.emission_luminance;
+}
+
+// integrate.glsl:156-193
+v3 direct_light_contribution(const OracleScene& s, v3 position, v3 wi, const Basis& basis,
+                             const MaterialConstants& mat, const Lobes& lobes, Generator& g) {
+    SceneView sv = s.view();
+    DirectLightSample ls = sample_random_light(sv, g);
+    v3 to_light = ls.position - position;
+    v3 wo = transform_from_basis(basis, to_light);
+    float d2 = length_squared(to_light);
+    Ray ray{to_light / std::sqrt(d2), position};
+    float density = (1.0f / ls.area) * d2 / saturate(dot(-ray.direction, ls.normal)) *
+                    ls.light_probability;
+    Hit h = trace(s, ray.origin, ray.direction, SHADOW_TMIN, SHADOW_TMAX, false);
+    if (!h.hit) return splat3(0.0f);
+    if (h.instance != ls.instance) return splat3(0.0f);
+    uint32_t tri = h.prim + s.instances[h.instance].index_offset / 3u;
+    if (tri % 0xffffu != ls.hash) return splat3(0.0f);
+    const Material& lm = s.materials[s.instances[ls.instance].material_index];
+    v3 emissive = material_emissive(lm);
+    float bd = 0.0f;
+    v3 bsdf = bsdf_evaluate(mat, lobes, wi, wo, bd);
+    return bsdf * emissive * std::fabs(cos_theta(wo)) / fmx(density, PDF_EPSILON);
+}
+
+// integrate.glsl:195-201
+Basis create_surface_basis(const Basis& ts, v3 n) {
+    Basis b;
+    b.normal = transform_to_basis(ts, n);
+    b.tangent = gram_schmidt(b.normal, ts.tangent);
+    b.bitangent = normalize(cross(b.normal, b.tangent));
+    return b;
+}
+
+struct PathState {
+    v3 accumulated, throughput;
+    Generator generator;
+    v2 ndc;
+    float mip_level;
+    Ray ray;
+};
+
+// integrate.glsl:270-321
+bool next_path_segment(const OracleScene& s, const Constants& c, PathState& ps, uint32_t bounce) {
+    Hit h = trace(s, ps.ray.origin, ps.ray.direction, EXTENSION_TMIN, EXTENSION_TMAX, true);
+    if (!h.hit) {
+        ps.accumulated += splat3(1.0f) * ps.throughput;
+        return false;
+    }
+    RayHit hit = get_ray_hit(s, h);
+    const Material& material = s.materials[hit.material_index];
+    const MaterialConstants& mc = material.constants;
+    Basis basis = create_surface_basis(hit.tangent_space, xyz(mc.geometry_normal));
+    v3 wi = transform_from_basis(basis, -ps.ray.direction);
+    Lobes lobes = bsdf_prepare(mc, wi, ps.generator);
+    bool nee = c.light_sampling == LIGHT_SAMPLING_NEXT_EVENT_ESTIMATION && !s.emissive.empty() &&
+               mc.specular_roughness > 0.15f;
+    if (nee) {
+        v3 direct = direct_light_contribution(s, hit.world_position, wi, basis, mc, lobes,
+                                              ps.generator);
+        ps.accumulated += ps.throughput * direct;
+    }
+    if (bounce == 0 || !nee) {
+        v3 emissive = material_emissive(material);
+        ps.accumulated += emissive * ps.throughput;
+    }
+    float density = 1.0f;
+    v3 wo = splat3(0.0f);
+    int lobe = 0;
+    v3 bsdf = bsdf_sample(mc, lobes, wi, ps.generator, wo, density, lobe);
+    ps.ray.direction = transform_to_basis(basis, wo);
+    ps.ray.origin = hit.world_position;
+    ps.throughput *= bsdf / fmx(density, PDF_EPSILON) * std::fabs(cos_theta(wo));
+    return true;
+}
+
+// integrate.glsl:323-347 for one pixel.
+v3 render_pixel(const OracleScene& s, const Constants& c, uint32_t px, uint32_t py) {
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    Generator g = init_generator_from_pixel(px, py, W, c.frame_index);
+    v3 acc = splat3(0.0f);
+    for (uint32_t si = 0; si < c.sample_count; ++si) {
+        float ox = random_float(g);
+        float oy = random_float(g);
+        v2 off = v2{ox - 0.5f, oy - 0.5f};
+        v2 ndc = v2{(((float)px + off.x) / (float)W) * 2.0f - 1.0f,
+                    (((float)py + off.y) / (float)H) * 2.0f - 1.0f};
+        Ray ray{camera_ray_direction(c, ndc), xyz(c.camera_position)};
+        PathState ps{splat3(0.0f), splat3(1.0f), g, ndc, 1.0f, ray};
+        for (uint32_t b = 0; b < c.bounce_count; ++b)
+            if (!next_path_segment(s, c, ps, b)) break;
+        acc += ps.accumulated;
+    }
+    return acc / (float)c.sample_count;
+}
+
+// tonemap.glsl:1-26
+v3 neutral_tonemap(v3 col) {
+    v3 y = v3{0.2126f * col.x + 0.7152f * col.y + 0.0722f * col.z,
+              -0.1146f * col.x + -0.3854f * col.y + 0.5f * col.z,
+              0.5f * col.x + -0.4542f * col.y + -0.0458f * col.z};
+    float bt = 1.0f - texp(-(std::sqrt(y.y * y.y + y.z * y.z) * 2.4f));
+    float desat = fmx((bt - 0.7f) * 0.8f, 0.0f);
+    desat *= desat;
+    v3 desat_color = mix3(col, splat3(y.x), desat);
+    float tm_lum = 1.0f - texp(-y.x);
+    float lum = 0.2126f * col.x + 0.7152f * col.y + 0.0722f * col.z;
+    v3 tm0 = col * fmx(0.0f, tm_lum / fmx(1e-5f, lum));
+    v3 tm1 = v3{1.0f - texp(-desat_color.x), 1.0f - texp(-desat_color.y),
+                1.0f - texp(-desat_color.z)};
+    return mix3(tm0, tm1, bt * bt) * 0.97f;
+}
+
+template <class T>
+void copy_in(std::vector<T>& dst, const void* src, uint64_t count) {
+    dst.resize(count);
+    if (count) std::memcpy(dst.data(), src, count * sizeof(T));
+}
+
+}  // namespace
+
+extern "C" {
+
+// Layout of tt_scene_desc (include/tinytrace_cuda.h): pointers + counts.
+struct OracleSceneDesc {
+    const int16_t* positions;
+    uint64_t position_count;
+    const uint32_t* indices;
+    uint64_t index_count;
+    const Vertex* vertices;
+    uint64_t vertex_count;
+    const Material* materials;
+    uint32_t material_count;
+    uint32_t mesh_count;
+    const Mesh* meshes;
+    const Instance* instances;
+    uint32_t instance_count;
+    uint32_t emissive_count;
+    const EmissiveTriangle* emissive;
+};
+
+void* oracle_scene_create(const OracleSceneDesc* d, int use_bvh, int leaf_max) {
+    OracleScene* s = new OracleScene();
+    copy_in(s->positions, d->positions, d->position_count * 3u);
+    copy_in(s->indices, d->indices, d->index_count);
+    copy_in(s->vertices, d->vertices, d->vertex_count);
+    copy_in(s->materials, d->materials, d->material_count);
+    copy_in(s->meshes, d->meshes, d->mesh_count);
+    copy_in(s->instances, d->instances, d->instance_count);
+    copy_in(s->emissive, d->emissive, d->emissive_count);
+    s->use_bvh = use_bvh != 0;
+    if (s->use_bvh) s->bvh = build_scene_bvh(s->geom(), leaf_max);
+    return s;
+}
+
+void oracle_scene_destroy(void* p) { delete static_cast<OracleScene*>(p); }
+
+// BVH arrays for node-for-node comparison with the GPU build.
+void oracle_scene_bvh_info(void* p, uint64_t* out /* blas_nodes, tris, tlas_nodes, blas_levels, tlas_levels */) {
+    OracleScene* s = static_cast<OracleScene*>(p);
+    out[0] = s->bvh.blas.size();
+    out[1] = s->bvh.tris.size();
+    out[2] = s->bvh.tlas.size();
+    out[3] = (uint64_t)s->bvh.blas_levels;
+    out[4] = (uint64_t)s->bvh.tlas_levels;
+}
+void oracle_scene_bvh_copy(void* p, void* blas, void* tris, void* tlas) {
+    OracleScene* s = static_cast<OracleScene*>(p);
+    if (blas) std::memcpy(blas, s->bvh.blas.data(), s->bvh.blas.size() * sizeof(Node4));
+    if (tris) std::memcpy(tris, s->bvh.tris.data(), s->bvh.tris.size() * sizeof(TriRecord));
+    if (tlas) std::memcpy(tlas, s->bvh.tlas.data(), s->bvh.tlas.size() * sizeof(Node4));
+}
+
+// rays: n x 8 floats (origin xyz, tmin, direction xyz, tmax); hits: n x 8 words
+// (hit, t, u, v, instance, prim, 0, 0).  flags bit0 = cull back faces, bit1 = brute force.
+void oracle_trace_batch(void* p, const float* rays, uint32_t n, uint32_t flags, uint32_t* hits,
+                        int threads) {
+    OracleScene* s = static_cast<OracleScene*>(p);
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const float* r = rays + 8 * i;
+        v3 o{r[0], r[1], r[2]}, d{r[4], r[5], r[6]};
+        bool cull = flags & 1u;
+        Geometry g = s->geom();
+        Hit h = (flags & 2u) || !s->use_bvh ? trace_brute(g, o, d, r[3], r[7], cull)
+                                            : trace_bvh(g, s->bvh, o, d, r[3], r[7], cull);
+        uint32_t* out = hits + 8 * i;
+        out[0] = (uint32_t)h.hit;
+        out[1] = h.hit ? fbits(h.t) : 0u;
+        out[2] = h.hit ? fbits(h.u) : 0u;
+        out[3] = h.hit ? fbits(h.v) : 0u;
+        out[4] = h.hit ? h.instance : 0u;
+        out[5] = h.hit ? h.prim : 0u;
+        out[6] = 0u;
+        out[7] = 0u;
+    }
+}
+
+// Renders rows [y0, y1) into `target` (W*H RGBA32F, read for accumulation).
+void oracle_render(void* p, const Constants* c, float* target, uint32_t y0, uint32_t y1,
+                   uint32_t x0, uint32_t x1, int threads) {
+    OracleScene* s = static_cast<OracleScene*>(p);
+    uint32_t W = c->screen_size[0];
+    int64_t cols = (int64_t)x1 - x0;
+    int64_t total = ((int64_t)y1 - y0) * cols;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int64_t k = 0; k < total; ++k) {
+        uint32_t py = y0 + (uint32_t)(k / cols), px = x0 + (uint32_t)(k % cols);
+        v3 acc = render_pixel(*s, *c, px, py);
+        float* t = target + 4ull * ((uint64_t)py * W + px);
+        if (c->accumulated_frame_count != 0) {
+            v3 prev = v3{t[0], t[1], t[2]};
+            acc = (prev * (float)(c->accumulated_frame_count - 1u) + acc) /
+                  (float)c->accumulated_frame_count;
+        }
+        t[0] = acc.x;
+        t[1] = acc.y;
+        t[2] = acc.z;
+        t[3] = 1.0f;
+    }
+}
+
+// display.glsl:6-12 on n RGBA32F pixels -> RGBA32F.
+void oracle_tonemap(const float* in, uint64_t n, int tonemap, float* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        v3 col{in[4 * i], in[4 * i + 1], in[4 * i + 2]};
+        if (tonemap) col = neutral_tonemap(col);
+        out[4 * i] = col.x;
+        out[4 * i + 1] = col.y;
+        out[4 * i + 2] = col.z;
+        out[4 * i + 3] = 1.0f;
+    }
+}
+
+// material/test.rs harness: per sample, bsdf_prepare with Generator(seed) then
+// bsdf_evaluate(wi, wo).  samples: n x 8 floats (wi xyz, seed bits, wo xyz, 0);
+// results: n x 8 floats (bsdf rgb, pdf, lobe probabilities 0..3) — see tt_bsdf_eval_batch.
+void oracle_bsdf_eval_batch(const MaterialConstants* m, const float* samples, uint32_t n,
+                            float* results) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* sm = samples + 8 * i;
+        Generator g{fbits(sm[3])};
+        v3 wi{sm[0], sm[1], sm[2]}, wo{sm[4], sm[5], sm[6]};
+        Lobes l = bsdf_prepare(*m, wi, g);
+        float pdf = 0.0f;
+        v3 b = bsdf_evaluate(*m, l, wi, wo, pdf);
+        float* r = results + 8 * i;
+        r[0] = b.x; r[1] = b.y; r[2] = b.z; r[3] = pdf;
+        r[4] = bitsf(g.state); r[5] = l.probs[5]; r[6] = l.probs[2]; r[7] = l.probs[3];
+    }
+}
+
+// bsdf_prepare + bsdf_sample.  samples: n x 4 (wi xyz, seed bits); results: n x 12
+// (bsdf rgb, pdf, wo xyz, lobe, final state bits, 0, 0, 0).
+void oracle_bsdf_sample_batch(const MaterialConstants* m, const float* samples, uint32_t n,
+                              float* results) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* sm = samples + 4 * i;
+        Generator g{fbits(sm[3])};
+        v3 wi{sm[0], sm[1], sm[2]};
+        Lobes l = bsdf_prepare(*m, wi, g);
+        v3 wo = splat3(0.0f);
+        float pdf = 0.0f;
+        int lobe = 0;
+        v3 b = bsdf_sample(*m, l, wi, g, wo, pdf, lobe);
+        float* r = results + 12 * i;
+        r[0] = b.x; r[1] = b.y; r[2] = b.z; r[3] = pdf;
+        r[4] = wo.x; r[5] = wo.y; r[6] = wo.z; r[7] = (float)lobe;
+        r[8] = bitsf(g.state); r[9] = 0.0f; r[10] = 0.0f; r[11] = 0.0f;
+    }
+}
+
+// Elementary functions, for accuracy tests against libm.
+void oracle_math(int which, const float* x, uint64_t n, float* y) {
+    for (uint64_t i = 0; i < n; ++i) {
+        switch (which) {
+            case 0: y[i] = tsin(x[i]); break;
+            case 1: y[i] = tcos(x[i]); break;
+            case 2: y[i] = texp(x[i]); break;
+            case 3: y[i] = tlog(x[i]); break;
+            case 4: y[i] = tacos(x[i]); break;
+            default: y[i] = 0.0f;
+        }
+    }
+}
+
+int oracle_abi_version(void) { return 1; }
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+"""TEST INFRASTRUCTURE — ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may import this module;
+it is the checker for the CUDA path, never the thing measured or shipped.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_P = ctypes.c_void_p
+
+
+class OracleSceneDesc(ctypes.Structure):
+    _fields_ = [("positions", _P), ("position_count", ctypes.c_uint64), ("indices", _P),
+                ("index_count", ctypes.c_uint64), ("vertices", _P), ("vertex_count", ctypes.c_uint64),
+                ("materials", _P), ("material_count", ctypes.c_uint32), ("mesh_count", ctypes.c_uint32),
+                ("meshes", _P), ("instances", _P), ("instance_count", ctypes.c_uint32),
+                ("emissive_count", ctypes.c_uint32), ("emissive", _P)]
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        lib = ctypes.CDLL(str(path))
+        lib.oracle_scene_create.restype = _P
+        lib.oracle_scene_create.argtypes = [ctypes.POINTER(OracleSceneDesc), ctypes.c_int, ctypes.c_int]
+        lib.oracle_scene_destroy.argtypes = [_P]
+        lib.oracle_scene_bvh_info.argtypes = [_P, _P]
+        lib.oracle_scene_bvh_copy.argtypes = [_P, _P, _P, _P]
+        lib.oracle_trace_batch.argtypes = [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_int]
+        lib.oracle_render.argtypes = [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.c_uint32, ctypes.c_int]
+        lib.oracle_tonemap.argtypes = [_P, ctypes.c_uint64, ctypes.c_int, _P]
+        lib.oracle_bsdf_eval_batch.argtypes = [_P, _P, ctypes.c_uint32, _P]
+        lib.oracle_bsdf_sample_batch.argtypes = [_P, _P, ctypes.c_uint32, _P]
+        lib.oracle_math.argtypes = [ctypes.c_int, _P, ctypes.c_uint64, _P]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleScene:
+    """CPU restatement of the scene (brute-force or LBVH ray queries)."""
+
+    def __init__(self, arrays, use_bvh: bool = True, leaf_max: int = 3):
+        self.arrays = arrays  # keeps the borrowed arrays alive
+        d = OracleSceneDesc(_p(arrays.positions), len(arrays.positions), _p(arrays.indices), len(arrays.indices),
+                            _p(arrays.vertices), len(arrays.vertices), _p(arrays.materials), len(arrays.materials),
+                            len(arrays.meshes), _p(arrays.meshes), _p(arrays.instances), len(arrays.instances),
+                            len(arrays.emissive), _p(arrays.emissive))
+        self.lib = load()
+        self.handle = self.lib.oracle_scene_create(ctypes.byref(d), 1 if use_bvh else 0, leaf_max)
+
+    def __del__(self):
+        try:
+            self.lib.oracle_scene_destroy(self.handle)
+        except Exception:
+            pass
+
+    def bvh(self):
+        from tinytrace_gb300.native import NODE4_DTYPE, TRI_RECORD_DTYPE
+
+        info = np.zeros(5, np.uint64)
+        self.lib.oracle_scene_bvh_info(self.handle, _p(info))
+        blas = np.zeros(int(info[0]), NODE4_DTYPE)
+        tris = np.zeros(int(info[1]), TRI_RECORD_DTYPE)
+        tlas = np.zeros(int(info[2]), NODE4_DTYPE)
+        self.lib.oracle_scene_bvh_copy(self.handle, _p(blas), _p(tris), _p(tlas))
+        return blas, tris, tlas, int(info[3]), int(info[4])
+
+    def trace(self, rays: np.ndarray, cull: bool, brute: bool = False, threads: int = 0) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        hits = np.zeros((len(rays), 8), np.uint32)
+        flags = (1 if cull else 0) | (2 if brute else 0)
+        self.lib.oracle_trace_batch(self.handle, _p(rays), len(rays), flags, _p(hits), threads)
+        return hits
+
+    def render(self, constants: np.ndarray, target: np.ndarray | None = None, rows=None, cols=None,
+               threads: int = 0) -> np.ndarray:
+        w, h = (int(x) for x in constants["screen_size"])
+        if target is None:
+            target = np.zeros((h, w, 4), np.float32)
+        y0, y1 = rows if rows is not None else (0, h)
+        x0, x1 = cols if cols is not None else (0, w)
+        c = np.ascontiguousarray(constants)
+        self.lib.oracle_render(self.handle, _p(c), _p(target), y0, y1, x0, x1, threads)
+        return target
+
+
+def tonemap(image: np.ndarray, enabled: bool = True) -> np.ndarray:
+    img = np.ascontiguousarray(image, np.float32)
+    out = np.zeros_like(img)
+    load().oracle_tonemap(_p(img), img.size // 4, 1 if enabled else 0, _p(out))
+    return out
+
+
+def bsdf_eval(material_constants: np.ndarray, samples: np.ndarray) -> np.ndarray:
+    s = np.ascontiguousarray(samples, np.float32).reshape(-1, 8)
+    out = np.zeros((len(s), 8), np.float32)
+    m = np.ascontiguousarray(material_constants)
+    load().oracle_bsdf_eval_batch(_p(m), _p(s), len(s), _p(out))
+    return out
+
+
+def bsdf_sample(material_constants: np.ndarray, samples: np.ndarray) -> np.ndarray:
+    s = np.ascontiguousarray(samples, np.float32).reshape(-1, 4)
+    out = np.zeros((len(s), 12), np.float32)
+    m = np.ascontiguousarray(material_constants)
+    load().oracle_bsdf_sample_batch(_p(m), _p(s), len(s), _p(out))
+    return out
+
+
+def math(which: int, x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.zeros_like(x)
+    load().oracle_math(which, _p(x), x.size, _p(y))
+    return y

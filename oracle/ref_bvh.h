@@ -1,0 +1,623 @@
+// TEST INFRASTRUCTURE — the CPU oracle for the tinytrace rendering hot path (the checker,
+// never the product; only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg
+// may load it).
+//
+// Ray queries without RT cores.  The reference delegates acceleration-structure build and
+// traversal to the Vulkan driver (src/scene.rs:130-171, src/integrate/integrate.glsl:112-127,
+// 168-185), so there is no reference source for this part: this header states the
+// semantics the GPU implementation must reproduce and restates the project's LBVH build on
+// the CPU so that the GPU build can be compared node for node.
+//
+// Ray-query semantics (the reference's GL_EXT_ray_query use):
+//   * instances are intersected in object space: o' = inverse_transform * (o, 1),
+//     d' = mat3(inverse_transform) * d; the ray parameter t is shared across instances;
+//   * object-space vertices are the dequantised snorm16 positions, value / 32767;
+//   * triangle test: watertight ray/triangle intersection (Woop, Benthin & Wald, JCGT 2013)
+//     with its double-precision fallback when an edge function is exactly zero;
+//     barycentrics (u, v) = (V/det, W/det) so that hit = (1-u-v) p0 + u p1 + v p2;
+//   * front faces are those whose geometric normal cross(p1-p0, p2-p0) faces the ray origin
+//     (det > 0); gl_RayFlagsCullBackFacingTrianglesEXT keeps only front faces;
+//   * a hit counts when tmin <= t <= tmax; the closest hit is the smallest t, ties broken by
+//     the smaller (instance, primitive) pair, so the result does not depend on traversal order.
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "ref_scene.h"
+
+namespace ref {
+
+struct Aabb {
+    v3 lo, hi;
+};
+inline Aabb aabb_empty() {
+    return Aabb{splat3(INFINITY), splat3(-INFINITY)};
+}
+inline Aabb aabb_union(const Aabb& a, const Aabb& b) {
+    return Aabb{v3{fmn(a.lo.x, b.lo.x), fmn(a.lo.y, b.lo.y), fmn(a.lo.z, b.lo.z)},
+                v3{fmx(a.hi.x, b.hi.x), fmx(a.hi.y, b.hi.y), fmx(a.hi.z, b.hi.z)}};
+}
+inline Aabb aabb_point(Aabb a, v3 p) { return aabb_union(a, Aabb{p, p}); }
+// Box coordinates and centroids are canonicalised (-0 -> +0) so that min/max are unambiguous.
+inline float canon(float v) { return v + 0.0f; }
+inline v3 canon3(v3 v) { return v3{canon(v.x), canon(v.y), canon(v.z)}; }
+inline Aabb canon_box(Aabb b) { return Aabb{canon3(b.lo), canon3(b.hi)}; }
+// Half surface area: ex*ey + ey*ez + ez*ex.
+inline float aabb_half_area(const Aabb& a) {
+    v3 e = a.hi - a.lo;
+    return e.x * e.y + e.y * e.z + e.z * e.x;
+}
+
+// ---------------------------------------------------------------- BVH4 node (64 bytes)
+struct Node4 {
+    float origin[3];
+    uint8_t exp[3];  // biased exponent of the per-axis scale 2^(exp-127)
+    uint8_t count;   // number of children (0..4)
+    uint32_t child[4];
+    uint8_t qlo[3][4];
+    uint8_t qhi[3][4];
+    uint32_t pad[2];
+};
+static_assert(sizeof(Node4) == 64, "Node4 is 64 bytes");
+constexpr uint32_t CHILD_LEAF = 0x80000000u;
+inline uint32_t leaf_ref(uint32_t first, uint32_t count) {
+    return CHILD_LEAF | ((count - 1u) << 27) | first;
+}
+inline uint32_t leaf_first(uint32_t ref) { return ref & 0x07ffffffu; }
+inline uint32_t leaf_count(uint32_t ref) { return ((ref >> 27) & 0xfu) + 1u; }
+
+// BLAS triangle record (48 bytes): v0.xyz + primitive index bits, v1.xyz, v2.xyz.
+struct TriRecord {
+    float v0[3];
+    uint32_t prim;
+    float v1[3];
+    uint32_t mesh;
+    float v2[3];
+    uint32_t pad;
+};
+static_assert(sizeof(TriRecord) == 48, "TriRecord is 48 bytes");
+
+// ---------------------------------------------------------------- LBVH build
+inline uint32_t expand_bits10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+inline uint32_t quantize_axis(float c, float lo, float hi) {
+    float ext = hi - lo;
+    if (!(ext > 0.0f)) return 0u;
+    float f = (c - lo) / ext;
+    float s = fmn(fmx(f * 1024.0f, 0.0f), 1023.0f);
+    return (uint32_t)s;
+}
+inline uint32_t morton30(v3 c, v3 lo, v3 hi) {
+    uint32_t x = quantize_axis(c.x, lo.x, hi.x);
+    uint32_t y = quantize_axis(c.y, lo.y, hi.y);
+    uint32_t z = quantize_axis(c.z, lo.z, hi.z);
+    return (expand_bits10(x) << 2) | (expand_bits10(y) << 1) | expand_bits10(z);
+}
+inline int clz64(uint64_t v) { return v == 0 ? 64 : __builtin_clzll(v); }
+inline int clz32(uint32_t v) { return v == 0 ? 32 : __builtin_clz(v); }
+
+struct BinaryTree {
+    // internal nodes [0, n-1), leaves referenced as n-1 + leaf index in `left/right`.
+    int n = 0;
+    std::vector<int> left, right, first, last;  // per internal node
+    std::vector<Aabb> ibox;                     // per internal node
+    std::vector<Aabb> lbox;                     // per leaf (sorted order)
+};
+
+struct BvhBuild {
+    std::vector<Node4> nodes;
+    std::vector<uint32_t> order;  // sorted position -> primitive index
+    std::vector<uint32_t> segment_root_kind;  // 0 empty, 1 ok
+    int levels = 0;
+};
+
+// Karras (2012) common-prefix function with the index tie-break for duplicate keys.
+inline int karras_delta(const std::vector<uint64_t>& k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    if (k[i] != k[j]) return clz64(k[i] ^ k[j]);
+    return 64 + clz32((uint32_t)i ^ (uint32_t)j);
+}
+
+// Quantise the children of a node (the node box is the union of the child boxes).
+inline void quantize_node(Node4& nd, const Aabb& pbox, const Aabb* cbox, int count) {
+    const float* pmin = &pbox.lo.x;
+    const float* pmax = &pbox.hi.x;
+    for (int a = 0; a < 3; ++a) {
+        double ext = (double)pmax[a] - (double)pmin[a];
+        int e = -126;
+        if (ext > 0.0) {
+            int ex;
+            std::frexp(ext / 255.0, &ex);
+            e = ex < -126 ? -126 : (ex > 127 ? 127 : ex);
+        }
+        double scale = std::ldexp(1.0, e);
+        nd.origin[a] = pmin[a];
+        nd.exp[a] = (uint8_t)(e + 127);
+        for (int c = 0; c < 4; ++c) {
+            if (c < count) {
+                const float* cmin = &cbox[c].lo.x;
+                const float* cmax = &cbox[c].hi.x;
+                double lo = std::floor(((double)cmin[a] - (double)pmin[a]) / scale);
+                double hi = std::ceil(((double)cmax[a] - (double)pmin[a]) / scale);
+                lo = lo < 0.0 ? 0.0 : (lo > 255.0 ? 255.0 : lo);
+                hi = hi < 0.0 ? 0.0 : (hi > 255.0 ? 255.0 : hi);
+                nd.qlo[a][c] = (uint8_t)lo;
+                nd.qhi[a][c] = (uint8_t)hi;
+            } else {
+                nd.qlo[a][c] = 255;
+                nd.qhi[a][c] = 0;
+            }
+        }
+    }
+}
+
+// Build BVH4s over primitives grouped in segments (one BVH root per segment, node index =
+// segment index).  `segment` must be non-decreasing in primitive order.  `leaf_max` bounds
+// the primitives per leaf child; `leaf_by_prim` stores the primitive index instead of the
+// sorted position in leaf references (used for the instance level, where leaf_max == 1).
+inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<uint32_t>& segment,
+                           uint32_t segment_count, int leaf_max, bool leaf_by_prim) {
+    BvhBuild out;
+    const int n = (int)prim_box.size();
+    // 1. centroid bounds per segment
+    std::vector<Aabb> cb(segment_count, aabb_empty());
+    std::vector<v3> cent(n);
+    for (int i = 0; i < n; ++i) {
+        cent[i] = canon3((prim_box[i].lo + prim_box[i].hi) * 0.5f);
+        cb[segment[i]] = aabb_point(cb[segment[i]], cent[i]);
+    }
+    // 2. keys, 3. stable sort
+    std::vector<uint64_t> key(n);
+    for (int i = 0; i < n; ++i) {
+        const Aabb& b = cb[segment[i]];
+        key[i] = ((uint64_t)segment[i] << 30) | morton30(cent[i], b.lo, b.hi);
+    }
+    std::vector<uint32_t> order(n);
+    for (int i = 0; i < n; ++i) order[i] = (uint32_t)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+    std::vector<uint64_t> sk(n);
+    for (int i = 0; i < n; ++i) sk[i] = key[order[i]];
+    // 4. Karras hierarchy
+    BinaryTree t;
+    t.n = n;
+    int ni = n > 1 ? n - 1 : 0;
+    t.left.assign(ni, 0);
+    t.right.assign(ni, 0);
+    t.first.assign(ni, 0);
+    t.last.assign(ni, 0);
+    for (int i = 0; i < ni; ++i) {
+        int d = (karras_delta(sk, n, i, i + 1) - karras_delta(sk, n, i, i - 1)) >= 0 ? 1 : -1;
+        int dmin = karras_delta(sk, n, i, i - d);
+        int lmax = 2;
+        while (karras_delta(sk, n, i, i + lmax * d) > dmin) lmax *= 2;
+        int l = 0;
+        for (int tt = lmax / 2; tt >= 1; tt /= 2)
+            if (karras_delta(sk, n, i, i + (l + tt) * d) > dmin) l += tt;
+        int j = i + l * d;
+        int dnode = karras_delta(sk, n, i, j);
+        int s = 0;
+        for (int div = 2;; div *= 2) {
+            int tt = (l + div - 1) / div;
+            if (karras_delta(sk, n, i, i + (s + tt) * d) > dnode) s += tt;
+            if (tt == 1) break;
+        }
+        int gamma = i + s * d + std::min(d, 0);
+        int lo = std::min(i, j), hi = std::max(i, j);
+        t.left[i] = (lo == gamma) ? (ni + gamma) : gamma;
+        t.right[i] = (hi == gamma + 1) ? (ni + gamma + 1) : (gamma + 1);
+        t.first[i] = lo;
+        t.last[i] = hi;
+    }
+    // 5. boxes (bottom-up; exact min/max, so any order gives the same result)
+    t.lbox.resize(n);
+    for (int i = 0; i < n; ++i) t.lbox[i] = prim_box[order[i]];
+    t.ibox.assign(ni, aabb_empty());
+    std::vector<Aabb> memo(ni);
+    std::vector<char> done(ni, 0);
+    // iterative post-order
+    {
+        std::vector<int> st;
+        if (ni > 0) st.push_back(0);
+        while (!st.empty()) {
+            int v = st.back();
+            int l = t.left[v], r = t.right[v];
+            bool ready = true;
+            if (l < ni && !done[l]) { st.push_back(l); ready = false; }
+            if (r < ni && !done[r]) { st.push_back(r); ready = false; }
+            if (!ready) continue;
+            st.pop_back();
+            Aabb bl = l < ni ? t.ibox[l] : t.lbox[l - ni];
+            Aabb br = r < ni ? t.ibox[r] : t.lbox[r - ni];
+            t.ibox[v] = aabb_union(bl, br);
+            done[v] = 1;
+        }
+    }
+    auto is_leaf = [&](int r) { return r >= ni; };
+    auto nfirst = [&](int r) { return is_leaf(r) ? r - ni : t.first[r]; };
+    auto ncount = [&](int r) { return is_leaf(r) ? 1 : t.last[r] - t.first[r] + 1; };
+    auto nbox = [&](int r) { return is_leaf(r) ? t.lbox[r - ni] : t.ibox[r]; };
+    // 6. segment roots: the node whose range equals the segment's sorted range
+    std::vector<int> seg_first(segment_count, 0), seg_count(segment_count, 0);
+    for (int i = 0; i < n; ++i) seg_count[segment[i]]++;
+    for (uint32_t s = 1; s < segment_count; ++s) seg_first[s] = seg_first[s - 1] + seg_count[s - 1];
+    std::vector<int> level;  // binary node refs of the current BVH4 level (-1 = empty)
+    for (uint32_t s = 0; s < segment_count; ++s) {
+        int a = seg_first[s], b = a + seg_count[s] - 1;
+        if (seg_count[s] == 0) level.push_back(-1);
+        else if (seg_count[s] == 1) level.push_back(ni + a);
+        else if (t.first[a] == a && t.last[a] == b) level.push_back(a);
+        else level.push_back(b);
+    }
+    // 7. collapse to BVH4, level by level
+    while (!level.empty()) {
+        out.levels++;
+        std::vector<int> next;
+        size_t base = out.nodes.size();
+        size_t next_base = base + level.size();
+        out.nodes.resize(base + level.size());
+        for (size_t li = 0; li < level.size(); ++li) {
+            Node4& nd = out.nodes[base + li];
+            std::memset(&nd, 0, sizeof(nd));
+            int r = level[li];
+            int ch[4];
+            int cnt = 0;
+            if (r < 0) {
+                cnt = 0;
+            } else if (is_leaf(r) || ncount(r) <= leaf_max) {
+                ch[0] = r;
+                cnt = 1;
+            } else {
+                ch[0] = t.left[r];
+                ch[1] = t.right[r];
+                cnt = 2;
+                while (cnt < 4) {
+                    int best = -1;
+                    float best_area = -1.0f;
+                    for (int c = 0; c < cnt; ++c) {
+                        if (is_leaf(ch[c]) || ncount(ch[c]) <= leaf_max) continue;
+                        float a = aabb_half_area(nbox(ch[c]));
+                        if (best < 0 || a > best_area) {
+                            best = c;
+                            best_area = a;
+                        }
+                    }
+                    if (best < 0) break;
+                    int v = ch[best];
+                    for (int c = cnt; c > best + 1; --c) ch[c] = ch[c - 1];
+                    ch[best] = t.left[v];
+                    ch[best + 1] = t.right[v];
+                    cnt++;
+                }
+            }
+            nd.count = (uint8_t)cnt;
+            Aabb cbx[4];
+            for (int c = 0; c < cnt; ++c) {
+                int v = ch[c];
+                cbx[c] = nbox(v);
+                if (is_leaf(v) || ncount(v) <= leaf_max) {
+                    uint32_t f = (uint32_t)nfirst(v);
+                    uint32_t k = (uint32_t)ncount(v);
+                    nd.child[c] = leaf_by_prim ? leaf_ref(order[f], 1u) : leaf_ref(f, k);
+                } else {
+                    nd.child[c] = (uint32_t)(next_base + next.size());
+                    next.push_back(v);
+                }
+            }
+            for (int c = cnt; c < 4; ++c) nd.child[c] = 0xffffffffu;
+            Aabb pb = cnt > 0 ? nbox(r) : Aabb{splat3(0.0f), splat3(0.0f)};
+            quantize_node(nd, pb, cbx, cnt);
+        }
+        level.swap(next);
+    }
+    out.order = order;
+    return out;
+}
+
+// ---------------------------------------------------------------- ray queries
+struct Hit {
+    int hit;
+    float t, u, v;
+    uint32_t instance, prim;
+};
+
+struct RayPre {
+    v3 o, d;
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+inline float comp(v3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+inline RayPre ray_precompute(v3 o, v3 d) {
+    RayPre r;
+    r.o = o;
+    r.d = d;
+    int kz = 0;
+    if (std::fabs(d.y) > std::fabs(d.x)) kz = 1;
+    if (std::fabs(d.z) > std::fabs(comp(d, kz))) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (comp(d, kz) < 0.0f) std::swap(kx, ky);
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.sx = comp(d, kx) / comp(d, kz);
+    r.sy = comp(d, ky) / comp(d, kz);
+    r.sz = 1.0f / comp(d, kz);
+    return r;
+}
+// Watertight ray/triangle test. Returns true and (t, u, v) on a hit within [tmin, tmax].
+inline bool intersect_triangle(const RayPre& r, v3 p0, v3 p1, v3 p2, bool cull_back, float tmin,
+                               float tmax, float& t_out, float& u_out, float& v_out) {
+    v3 A = p0 - r.o, B = p1 - r.o, C = p2 - r.o;
+    float Ax = comp(A, r.kx) - r.sx * comp(A, r.kz);
+    float Ay = comp(A, r.ky) - r.sy * comp(A, r.kz);
+    float Bx = comp(B, r.kx) - r.sx * comp(B, r.kz);
+    float By = comp(B, r.ky) - r.sy * comp(B, r.kz);
+    float Cx = comp(C, r.kx) - r.sx * comp(C, r.kz);
+    float Cy = comp(C, r.ky) - r.sy * comp(C, r.kz);
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if (cull_back) {
+        if (U < 0.0f || V < 0.0f || W < 0.0f) return false;
+    } else {
+        if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    }
+    float det = U + V + W;
+    if (det == 0.0f) return false;
+    float Az = r.sz * comp(A, r.kz);
+    float Bz = r.sz * comp(B, r.kz);
+    float Cz = r.sz * comp(C, r.kz);
+    float T = U * Az + V * Bz + W * Cz;
+    float rcp = 1.0f / det;
+    float t = T * rcp;
+    if (!(t >= tmin && t <= tmax)) return false;
+    t_out = t;
+    u_out = V * rcp;
+    v_out = W * rcp;
+    return true;
+}
+inline bool closer(float t, uint32_t inst, uint32_t prim, const Hit& best) {
+    if (!best.hit) return true;
+    if (t < best.t) return true;
+    if (t > best.t) return false;
+    if (inst != best.instance) return inst < best.instance;
+    return prim < best.prim;
+}
+inline bool finite3(v3 d) { return std::isfinite(d.x) && std::isfinite(d.y) && std::isfinite(d.z); }
+
+// Scene geometry as seen by the ray queries.
+struct Geometry {
+    const int16_t* positions;
+    const uint32_t* indices;
+    const Instance* instances;
+    uint32_t instance_count;
+    const Mesh* meshes;
+    uint32_t mesh_count;
+};
+inline void triangle_object(const Geometry& g, const Instance& in, uint32_t prim, v3& p0, v3& p1,
+                            v3& p2) {
+    uint32_t base = in.index_offset + 3u * prim;
+    p0 = dequantize_snorm3(g.positions + 3u * (in.vertex_offset + g.indices[base + 0]));
+    p1 = dequantize_snorm3(g.positions + 3u * (in.vertex_offset + g.indices[base + 1]));
+    p2 = dequantize_snorm3(g.positions + 3u * (in.vertex_offset + g.indices[base + 2]));
+}
+inline void object_ray(const Instance& in, v3 o, v3 d, v3& oo, v3& od) {
+    oo = mat43_point(in.inverse_transform, o);
+    od = mat3_vec(in.inverse_transform, d);
+}
+
+// Brute force closest hit over every triangle of every instance.
+inline Hit trace_brute(const Geometry& g, v3 o, v3 d, float tmin, float tmax, bool cull_back) {
+    Hit best{0, 0.0f, 0.0f, 0.0f, 0u, 0u};
+    if (!finite3(d)) return best;
+    for (uint32_t i = 0; i < g.instance_count; ++i) {
+        const Instance& in = g.instances[i];
+        const Mesh& m = g.meshes[in.mesh_index];
+        v3 oo, od;
+        object_ray(in, o, d, oo, od);
+        RayPre r = ray_precompute(oo, od);
+        uint32_t tris = m.index_count / 3u;
+        for (uint32_t p = 0; p < tris; ++p) {
+            v3 p0, p1, p2;
+            triangle_object(g, in, p, p0, p1, p2);
+            float t, u, v;
+            if (!intersect_triangle(r, p0, p1, p2, cull_back, tmin, tmax, t, u, v)) continue;
+            if (closer(t, i, p, best)) best = Hit{1, t, u, v, i, p};
+        }
+    }
+    return best;
+}
+
+// Conservative slab test of one quantised node against a ray; writes entry distances and
+// returns a child mask.  Bounds are widened by 2^-20 of the terms' magnitudes so that float
+// rounding never culls a box the ray enters.
+struct NodeRay {
+    v3 o, inv;
+};
+inline float safe_inv(float d) {
+    float a = std::fabs(d) < 1e-20f ? (d < 0.0f ? -1e-20f : 1e-20f) : d;
+    return 1.0f / a;
+}
+inline int node_hits(const Node4& nd, const NodeRay& r, float tmin, float tbest, float* tnear) {
+    float A[3], Blo[3], Bhi[3];
+    const float o[3] = {r.o.x, r.o.y, r.o.z};
+    const float inv[3] = {r.inv.x, r.inv.y, r.inv.z};
+    for (int a = 0; a < 3; ++a) {
+        float scale = bitsf((uint32_t)nd.exp[a] << 23);
+        A[a] = scale * inv[a];
+        float B = (nd.origin[a] - o[a]) * inv[a];
+        float M = std::fmaf(256.0f, std::fabs(A[a]), std::fabs(B)) * 9.5367431640625e-07f;
+        float s = inv[a] >= 0.0f ? M : -M;
+        Blo[a] = B - s;
+        Bhi[a] = B + s;
+    }
+    int mask = 0;
+    for (int c = 0; c < nd.count; ++c) {
+        float tn = tmin, tf = tbest;
+        for (int a = 0; a < 3; ++a) {
+            float t0 = std::fmaf((float)nd.qlo[a][c], A[a], Blo[a]);
+            float t1 = std::fmaf((float)nd.qhi[a][c], A[a], Bhi[a]);
+            tn = fmx(tn, fmn(t0, t1));
+            tf = fmn(tf, fmx(t0, t1));
+        }
+        if (tn <= tf) {
+            mask |= 1 << c;
+            tnear[c] = tn;
+        }
+    }
+    return mask;
+}
+
+struct SceneBvh {
+    std::vector<Node4> blas;   // node index == mesh index for BLAS roots
+    std::vector<TriRecord> tris;
+    std::vector<Node4> tlas;   // root = 0
+    int blas_levels = 0, tlas_levels = 0;
+};
+
+// BLAS over all meshes (segment = mesh) and TLAS over instances (leaf = instance index).
+inline SceneBvh build_scene_bvh(const Geometry& g, int leaf_max) {
+    SceneBvh s;
+    std::vector<Aabb> pbox;
+    std::vector<uint32_t> seg;
+    std::vector<TriRecord> recs;
+    for (uint32_t m = 0; m < g.mesh_count; ++m) {
+        const Mesh& me = g.meshes[m];
+        uint32_t tris = me.index_count / 3u;
+        for (uint32_t p = 0; p < tris; ++p) {
+            uint32_t base = me.index_offset + 3u * p;
+            v3 q[3];
+            for (int k = 0; k < 3; ++k)
+                q[k] = dequantize_snorm3(g.positions + 3u * (me.vertex_offset + g.indices[base + k]));
+            Aabb b = aabb_point(aabb_point(Aabb{q[0], q[0]}, q[1]), q[2]);
+            pbox.push_back(canon_box(b));
+            seg.push_back(m);
+            TriRecord tr;
+            tr.v0[0] = q[0].x; tr.v0[1] = q[0].y; tr.v0[2] = q[0].z;
+            tr.v1[0] = q[1].x; tr.v1[1] = q[1].y; tr.v1[2] = q[1].z;
+            tr.v2[0] = q[2].x; tr.v2[1] = q[2].y; tr.v2[2] = q[2].z;
+            tr.prim = p;
+            tr.mesh = m;
+            tr.pad = 0;
+            recs.push_back(tr);
+        }
+    }
+    BvhBuild b = build_bvh4(pbox, seg, g.mesh_count, leaf_max, false);
+    s.blas = b.nodes;
+    s.blas_levels = b.levels;
+    s.tris.resize(recs.size());
+    for (size_t i = 0; i < recs.size(); ++i) s.tris[i] = recs[b.order[i]];
+    // instance level: world box = box of the 8 transformed corners of the mesh box
+    std::vector<Aabb> mesh_box(g.mesh_count, aabb_empty());
+    for (size_t i = 0; i < pbox.size(); ++i) mesh_box[seg[i]] = aabb_union(mesh_box[seg[i]], pbox[i]);
+    std::vector<Aabb> ibox;
+    std::vector<uint32_t> iseg;
+    std::vector<uint32_t> ids;
+    for (uint32_t i = 0; i < g.instance_count; ++i) {
+        const Instance& in = g.instances[i];
+        const Mesh& me = g.meshes[in.mesh_index];
+        if (me.index_count / 3u == 0) continue;
+        const Aabb& mb = mesh_box[in.mesh_index];
+        Aabb wb = aabb_empty();
+        for (int k = 0; k < 8; ++k) {
+            v3 c = v3{(k & 1) ? mb.hi.x : mb.lo.x, (k & 2) ? mb.hi.y : mb.lo.y,
+                      (k & 4) ? mb.hi.z : mb.lo.z};
+            wb = aabb_point(wb, mat43_point(in.transform, c));
+        }
+        ibox.push_back(canon_box(wb));
+        iseg.push_back(0);
+        ids.push_back(i);
+    }
+    BvhBuild tb = build_bvh4(ibox, iseg, 1, 1, true);
+    // leaf references hold positions in `ibox`; map them to instance indices
+    for (Node4& nd : tb.nodes)
+        for (int c = 0; c < nd.count; ++c)
+            if (nd.child[c] & CHILD_LEAF) nd.child[c] = leaf_ref(ids[leaf_first(nd.child[c])], 1u);
+    s.tlas = tb.nodes;
+    s.tlas_levels = tb.levels;
+    return s;
+}
+
+inline void trace_blas(const SceneBvh& s, uint32_t root, uint32_t inst, const RayPre& rp,
+                       const NodeRay& nr, bool cull_back, float tmin, Hit& best, float& tbest) {
+    uint32_t stack[256];
+    int sp = 0;
+    stack[sp++] = root;
+    while (sp > 0) {
+        const Node4& nd = s.blas[stack[--sp]];
+        float tn[4];
+        int mask = node_hits(nd, nr, tmin, tbest, tn);
+        for (int c = 0; c < nd.count; ++c) {
+            if (!(mask & (1 << c))) continue;
+            uint32_t ch = nd.child[c];
+            if (ch & CHILD_LEAF) {
+                uint32_t f = leaf_first(ch), k = leaf_count(ch);
+                for (uint32_t q = f; q < f + k; ++q) {
+                    const TriRecord& tr = s.tris[q];
+                    float t, u, v;
+                    if (!intersect_triangle(rp, v3{tr.v0[0], tr.v0[1], tr.v0[2]},
+                                            v3{tr.v1[0], tr.v1[1], tr.v1[2]},
+                                            v3{tr.v2[0], tr.v2[1], tr.v2[2]}, cull_back, tmin,
+                                            tbest, t, u, v))
+                        continue;
+                    if (closer(t, inst, tr.prim, best)) {
+                        best = Hit{1, t, u, v, inst, tr.prim};
+                        tbest = t;
+                    }
+                }
+            } else {
+                stack[sp++] = ch;
+            }
+        }
+    }
+}
+
+// Closest hit through the two-level BVH.
+inline Hit trace_bvh(const Geometry& g, const SceneBvh& s, v3 o, v3 d, float tmin, float tmax,
+                     bool cull_back) {
+    Hit best{0, 0.0f, 0.0f, 0.0f, 0u, 0u};
+    if (!finite3(d) || s.tlas.empty()) return best;
+    float tbest = tmax;
+    NodeRay wr{o, v3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)}};
+    uint32_t stack[256];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const Node4& nd = s.tlas[stack[--sp]];
+        float tn[4];
+        int mask = node_hits(nd, wr, tmin, tbest, tn);
+        for (int c = 0; c < nd.count; ++c) {
+            if (!(mask & (1 << c))) continue;
+            uint32_t ch = nd.child[c];
+            if (ch & CHILD_LEAF) {
+                uint32_t inst = leaf_first(ch);
+                const Instance& in = g.instances[inst];
+                v3 oo, od;
+                object_ray(in, o, d, oo, od);
+                if (!finite3(od)) continue;
+                RayPre rp = ray_precompute(oo, od);
+                NodeRay nr{oo, v3{safe_inv(od.x), safe_inv(od.y), safe_inv(od.z)}};
+                trace_blas(s, in.mesh_index, inst, rp, nr, cull_back, tmin, best, tbest);
+            } else {
+                stack[sp++] = ch;
+            }
+        }
+    }
+    return best;
+}
+
+}  // namespace ref

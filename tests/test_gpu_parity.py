@@ -1,0 +1,183 @@
+"""CUDA path vs the CPU oracle, bit for bit, through the C ABI (GPU required).
+
+Tolerance: zero.  Every kernel on the path is specified operation by operation (IEEE-754
+single precision, no implicit contraction, project-owned elementary functions), so the GPU
+must reproduce the oracle's bits exactly; only NaN payloads may differ.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import assert_same_bits
+from materials import eval_samples, material_suite, sample_samples
+from oracle import oracle
+from tinytrace_gb300 import native, scenes
+from tinytrace_gb300.native import NODE4_DTYPE, TRI_RECORD_DTYPE, check
+from tinytrace_gb300.renderer import SceneArrays, make_constants
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_math(ctx, which, x):
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.zeros_like(x)
+    check(ctx.lib.tt_math_batch(ctx.handle, which, native.ptr(x), x.size, native.ptr(y)))
+    return y
+
+
+def test_math_bits(gpu_context):
+    rng = np.random.default_rng(0)
+    xs = {
+        0: np.concatenate([rng.uniform(-20, 20, 100000), rng.uniform(0, 2 * np.pi, 100000), [0.0, -0.0, 1e7, 3e7]]),
+        1: np.concatenate([rng.uniform(-20, 20, 100000), rng.uniform(0, 2 * np.pi, 100000)]),
+        2: np.concatenate([rng.uniform(-110, 90, 200000), [0.0, -0.0, 88.7, -87.3, -103.0]]),
+        3: np.concatenate([np.exp(rng.uniform(-100, 88, 200000)), [1e-42, 1.0, 0.0, 2.0]]),
+        4: np.concatenate([rng.uniform(-1, 1, 200000), [-1.0, 1.0, 0.5, -0.5, 0.0]]),
+    }
+    for which, x in xs.items():
+        x = x.astype(np.float32)
+        assert_same_bits(gpu_math(gpu_context, which, x), oracle.math(which, x), f"math {which}")
+
+
+def test_bsdf_eval_bits(gpu_context):
+    rng = np.random.default_rng(1)
+    for i, m in enumerate(material_suite()):
+        s = eval_samples(rng, 4096)
+        out = np.zeros((len(s), 8), np.float32)
+        m = np.ascontiguousarray(m)
+        check(gpu_context.lib.tt_bsdf_eval_batch(gpu_context.handle, native.ptr(m), native.ptr(s), len(s),
+                                                 native.ptr(out)))
+        assert_same_bits(out, oracle.bsdf_eval(m, s), f"bsdf_evaluate material {i}")
+
+
+def test_bsdf_sample_bits(gpu_context):
+    rng = np.random.default_rng(2)
+    for i, m in enumerate(material_suite()):
+        s = sample_samples(rng, 4096)
+        out = np.zeros((len(s), 12), np.float32)
+        m = np.ascontiguousarray(m)
+        check(gpu_context.lib.tt_bsdf_sample_batch(gpu_context.handle, native.ptr(m), native.ptr(s), len(s),
+                                                   native.ptr(out)))
+        assert_same_bits(out, oracle.bsdf_sample(m, s), f"bsdf_sample material {i}")
+
+
+def _gpu_bvh(ctx, scene):
+    st = ctx.scene_stats(scene)
+    blas = np.zeros(st.blas_nodes, NODE4_DTYPE)
+    tris = np.zeros(st.triangle_count, TRI_RECORD_DTYPE)
+    tlas = np.zeros(st.tlas_nodes, NODE4_DTYPE)
+    check(ctx.lib.tt_scene_bvh_download(ctx.handle, scene, native.ptr(blas), blas.nbytes, native.ptr(tris),
+                                        tris.nbytes, native.ptr(tlas), tlas.nbytes))
+    return blas, tris, tlas, st
+
+
+def _small_field():
+    return scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11)
+
+
+@pytest.mark.parametrize("name", ["cornell", "field"])
+def test_bvh_topology_bits(gpu_context, name):
+    scene = scenes.cornell_box() if name == "cornell" else _small_field()
+    arrays = SceneArrays(scene)
+    h = gpu_context.create_scene(arrays)
+    blas, tris, tlas, st = _gpu_bvh(gpu_context, h)
+    ob, ot, otl, bl, tl = oracle.OracleScene(arrays).bvh()
+    assert (st.blas_levels, st.tlas_levels) == (bl, tl)
+    assert blas.tobytes() == ob.tobytes(), "BLAS nodes differ"
+    assert tris.tobytes() == ot.tobytes(), "triangle records differ"
+    assert tlas.tobytes() == otl.tobytes(), "TLAS nodes differ"
+
+
+def _random_rays(rng, n, center, spread):
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = center + rng.uniform(-spread, spread, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 4:7] = d
+    rays[:, 3] = 1e-3
+    rays[:, 7] = rng.choice([1000.0, 10000.0, 3.0], n)
+    return rays
+
+
+@pytest.mark.parametrize("name", ["cornell", "field"])
+def test_closest_hit_matches_brute_force(gpu_context, name):
+    scene = scenes.cornell_box() if name == "cornell" else _small_field()
+    arrays = SceneArrays(scene)
+    h = gpu_context.create_scene(arrays)
+    rng = np.random.default_rng(5)
+    center, spread = ((0, 1, 0), 1.2) if name == "cornell" else ((0, 0, 0), 60.0)
+    rays = _random_rays(rng, 20000, np.array(center), spread)
+    if name == "field":  # aim most rays at instance centres so that the field is actually hit
+        targets = arrays.instances["transform"][:, 12:15]
+        t = targets[rng.integers(0, len(targets), len(rays))] + rng.normal(0, 3.0, (len(rays), 3))
+        d = t - rays[:, 0:3]
+        rays[:15000, 4:7] = (d / np.linalg.norm(d, axis=1, keepdims=True))[:15000]
+    rays[:50, 4:7] = np.nan  # NaN directions never hit
+    orc = oracle.OracleScene(arrays)
+    for cull in (False, True):
+        hits = np.zeros((len(rays), 8), np.uint32)
+        check(gpu_context.lib.tt_trace_batch(gpu_context.handle, h, native.ptr(rays), len(rays),
+                                             1 if cull else 0, native.ptr(hits)))
+        brute = orc.trace(rays, cull=cull, brute=True)
+        bvh = orc.trace(rays, cull=cull, brute=False)
+        assert np.array_equal(bvh, brute), "oracle BVH traversal differs from brute force"
+        assert np.array_equal(hits, brute), f"GPU closest hits differ (cull={cull}): {np.sum(np.any(hits != brute, 1))}"
+        assert hits[:, 0].sum() > len(rays) // 20
+
+
+def _render_pair(ctx, w, frames=1):
+    from tinytrace_gb300.renderer import Renderer
+
+    r = Renderer(w.extent)
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    r.set_config(w.config)
+    orc = oracle.OracleScene(r.scene_arrays)
+    cpu = np.zeros((w.extent[1], w.extent[0], 4), np.float32)
+    for f in range(frames):
+        c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
+        gpu = r.render_to_texture()
+        orc.render(c, cpu)
+        assert_same_bits(gpu, cpu, f"{w.name} frame {f}")
+        r.present()
+    r.close()
+    return gpu
+
+
+def test_render_cornell_c1(gpu_context):
+    img = _render_pair(gpu_context, scenes.cornell_workload())
+    assert img[..., :3].mean() > 0.05
+
+
+def test_render_accumulation(gpu_context):
+    # frames 0 and 1 both overwrite (n = 0 and n = 1), later frames average
+    _render_pair(gpu_context, scenes.cornell_workload(extent=(48, 40), spp=1, depth=3), frames=4)
+
+
+def test_render_field_small(gpu_context):
+    w = scenes.Workload("field_small", _small_field(), scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)),
+                        (96, 54), scenes.Config(bounce_count=8, sample_count=3))
+    _render_pair(gpu_context, w)
+
+
+def test_tonemap_bits(gpu_context):
+    rng = np.random.default_rng(9)
+    img = rng.exponential(1.0, (32, 40, 4)).astype(np.float32)
+    img[0, :4, :3] = [[0, 0, 0], [1e-8, 0, 0], [100, 50, 1], [np.inf, 1, 1]]
+    ctx = gpu_context
+    h = ctx.create_image(native.TT_LIFETIME_FRAME, 40, 32)
+    ctx.write_image(h, img)
+    c = np.zeros((), native.CONSTANTS_DTYPE)
+    for enabled in (1, 0):
+        c["tonemap"] = enabled
+        out = np.zeros((32, 40, 4), np.float32)
+        check(ctx.lib.tt_tonemap(ctx.handle, h, native.ptr(c), native.TT_FORMAT_RGBA32F, native.ptr(out), out.nbytes))
+        assert_same_bits(out, oracle.tonemap(img, bool(enabled)), f"tonemap {enabled}")
+    out8 = np.zeros((32, 40, 4), np.uint8)
+    c["tonemap"] = 1
+    check(ctx.lib.tt_tonemap(ctx.handle, h, native.ptr(c), native.TT_FORMAT_RGBA8_UNORM, native.ptr(out8), out8.nbytes))
+    ref = oracle.tonemap(img, True)
+    exp8 = (np.clip(np.nan_to_num(ref, nan=0.0), 0, 1) * np.float32(255) + np.float32(0.5)).astype(np.uint8)
+    exp8[..., 3] = 255
+    assert np.array_equal(out8, exp8)

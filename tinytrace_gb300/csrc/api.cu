@@ -1,0 +1,644 @@
+// C ABI of libtinytrace_cuda.so (declared in include/tinytrace_cuda.h): contexts, handle
+// pools with lifetimes and epochs, scene upload + LBVH build, rendering, tonemapping and the
+// parity entry points.  Every entry point converts failures into a status code and a
+// thread-local message; nothing throws or aborts across the ABI.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tt_internal.h"
+#include "tt_kernels.h"
+
+namespace tt {
+
+thread_local std::string g_last_error;
+
+void fail(int32_t code, const std::string& message) { throw Error{code, message}; }
+void check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    int32_t code = e == cudaErrorMemoryAllocation ? TT_ERR_OOM
+                   : e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? TT_ERR_NO_DEVICE
+                                                                                 : TT_ERR_DEVICE;
+    fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
+    if (this != &o) {
+        if (ptr) cudaFree(ptr);
+        ptr = o.ptr;
+        bytes = o.bytes;
+        o.ptr = nullptr;
+        o.bytes = 0;
+    }
+    return *this;
+}
+DeviceBuffer::~DeviceBuffer() {
+    if (ptr) cudaFree(ptr);
+}
+void DeviceBuffer::alloc(size_t n) {
+    if (ptr) {
+        cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    size_t b = n == 0 ? 16 : n;
+    check_cuda(cudaMalloc(&ptr, b), "cudaMalloc");
+    bytes = n;
+}
+
+namespace {
+
+constexpr uint32_t KIND_IMAGE = 1, KIND_SCENE = 2;
+constexpr int LIFETIMES = 5;
+constexpr int EVENT_SLOTS = 16;
+constexpr size_t L2_FLUSH_BYTES = 512ull << 20;
+constexpr int BLAS_LEAF_MAX = 3;
+
+struct ImageRes {
+    DeviceBuffer buf;
+    uint32_t width = 0, height = 0;
+};
+
+struct SceneRes {
+    DeviceBuffer positions, indices, vertices, materials, instances, emissive, inst_xform;
+    BvhResult bvh;
+    DevScene dev{};
+    tt_scene_stats stats{};
+};
+
+struct Pool {
+    uint32_t epoch = 1;
+    std::vector<std::unique_ptr<ImageRes>> images;
+    std::vector<std::unique_ptr<SceneRes>> scenes;
+};
+
+}  // namespace
+}  // namespace tt
+
+struct tt_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    tt::Pool pools[tt::LIFETIMES];
+    uint64_t frame_index = 0;
+    cudaEvent_t ev_integrate[2] = {nullptr, nullptr};
+    cudaEvent_t ev_post[2] = {nullptr, nullptr};
+    cudaEvent_t user_events[tt::EVENT_SLOTS] = {};
+    bool integrate_timed = false, post_timed = false;
+    float scene_build_ms = 0.0f;
+    tt::DeviceBuffer err_word, counters, l2_flush;
+    uint32_t* err_host = nullptr;  // pinned
+    bool err_pending = false;
+};
+
+namespace tt {
+namespace {
+
+uint64_t make_handle(uint32_t lifetime, uint32_t kind, uint32_t epoch, uint32_t index) {
+    return ((uint64_t)(lifetime & 0xfu) << 60) | ((uint64_t)(kind & 0xfu) << 56) |
+           ((uint64_t)(epoch & 0xffffffu) << 32) | index;
+}
+
+template <class T>
+T* lookup(tt_context* ctx, tt_handle h, uint32_t kind) {
+    uint32_t lifetime = (uint32_t)(h >> 60) & 0xfu;
+    uint32_t k = (uint32_t)(h >> 56) & 0xfu;
+    uint32_t epoch = (uint32_t)(h >> 32) & 0xffffffu;
+    uint32_t index = (uint32_t)h;
+    if (lifetime >= (uint32_t)LIFETIMES || k != kind) fail(TT_ERR_BAD_HANDLE, "handle of the wrong kind");
+    Pool& p = ctx->pools[lifetime];
+    if ((p.epoch & 0xffffffu) != epoch) fail(TT_ERR_BAD_HANDLE, "stale handle: its lifetime was cleared");
+    if constexpr (std::is_same<T, ImageRes>::value) {
+        if (index >= p.images.size() || !p.images[index]) fail(TT_ERR_BAD_HANDLE, "unknown image handle");
+        return p.images[index].get();
+    } else {
+        if (index >= p.scenes.size() || !p.scenes[index]) fail(TT_ERR_BAD_HANDLE, "unknown scene handle");
+        return p.scenes[index].get();
+    }
+}
+
+void require(bool cond, const char* msg) {
+    if (!cond) fail(TT_ERR_INVALID_ARGUMENT, msg);
+}
+
+void use_device(tt_context* ctx) { check_cuda(cudaSetDevice(ctx->device), "cudaSetDevice"); }
+
+// Reads back the device error word after the stream drained.
+void check_device_errors(tt_context* ctx) {
+    if (!ctx->err_pending) return;
+    ctx->err_pending = false;
+    uint32_t e = *ctx->err_host;
+    if (e & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
+    if (e & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
+}
+void sync(tt_context* ctx) {
+    check_cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    check_device_errors(ctx);
+}
+void arm_error_word(tt_context* ctx) {
+    check_cuda(cudaMemsetAsync(ctx->err_word.ptr, 0, 4, ctx->stream), "memset");
+}
+void fetch_error_word(tt_context* ctx) {
+    check_cuda(cudaMemcpyAsync(ctx->err_host, ctx->err_word.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream),
+               "error word");
+    ctx->err_pending = true;
+}
+
+template <class T>
+void upload(DeviceBuffer& b, const T* host, uint64_t count, cudaStream_t st) {
+    b.alloc(count * sizeof(T));
+    if (count) check_cuda(cudaMemcpyAsync(b.ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+}
+
+// Host-side validation: every index the kernels will follow must be in range.
+void validate_scene(const tt_scene_desc* d) {
+    require(d != nullptr, "scene desc is null");
+    require(d->position_count == 0 || d->positions, "positions pointer is null");
+    require(d->index_count == 0 || d->indices, "indices pointer is null");
+    require(d->vertex_count == 0 || d->vertices, "vertices pointer is null");
+    require(d->material_count == 0 || d->materials, "materials pointer is null");
+    require(d->mesh_count == 0 || d->meshes, "meshes pointer is null");
+    require(d->instance_count == 0 || d->instances, "instances pointer is null");
+    require(d->emissive_triangle_count == 0 || d->emissive_triangles, "emissive pointer is null");
+    require(d->position_count < (1ull << 32) && d->index_count < (1ull << 32) && d->vertex_count < (1ull << 32),
+            "arrays above 2^32 entries are not supported");
+    uint64_t verts = std::min(d->position_count, d->vertex_count);
+    uint64_t tris = 0;
+    for (uint32_t m = 0; m < d->mesh_count; ++m) {
+        const tt_mesh& me = d->meshes[m];
+        uint64_t end = (uint64_t)me.index_offset + me.index_count;
+        require(end <= d->index_count, "mesh index range exceeds the index buffer");
+        uint32_t used = me.index_count / 3u * 3u;
+        for (uint32_t k = 0; k < used; ++k)
+            require((uint64_t)d->indices[me.index_offset + k] + me.vertex_offset < verts,
+                    "mesh index points outside the vertex arrays");
+        tris += me.index_count / 3u;
+    }
+    require(tris < (1ull << 27), "more than 2^27 triangles in one scene");
+    for (uint32_t i = 0; i < d->instance_count; ++i) {
+        const tt_instance& in = d->instances[i];
+        require(in.mesh_index < d->mesh_count, "instance mesh_index out of range");
+        require(in.material_index < d->material_count, "instance material_index out of range");
+        const tt_mesh& me = d->meshes[in.mesh_index];
+        require(in.index_offset == me.index_offset && in.vertex_offset == me.vertex_offset,
+                "instance offsets must equal its mesh's offsets (src/scene.rs:52-53)");
+        for (int k = 0; k < 16; ++k)
+            require(std::isfinite(in.transform[k]) && std::isfinite(in.inverse_transform[k]) &&
+                        std::isfinite(in.normal_transform[k]),
+                    "instance matrices must be finite");
+    }
+    for (uint32_t e = 0; e < d->emissive_triangle_count; ++e)
+        require(d->emissive_triangles[e].instance_index < d->instance_count,
+                "emissive triangle instance_index out of range");
+    for (uint32_t m = 0; m < d->material_count; ++m)
+        for (int t = 0; t < 27; ++t)
+            if (d->materials[m].textures[t] != 0xffffffffu)
+                fail(TT_ERR_UNSUPPORTED, "textured materials are not supported (texture index set)");
+}
+
+template <class F>
+int32_t guarded(F&& f) {
+    try {
+        f();
+        return TT_OK;
+    } catch (const Error& e) {
+        g_last_error = e.message;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return TT_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return TT_ERR_DEVICE;
+    } catch (...) {
+        g_last_error = "unknown failure";
+        return TT_ERR_DEVICE;
+    }
+}
+
+}  // namespace
+}  // namespace tt
+
+using namespace tt;
+
+static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c, tt_handle target, bool counted,
+                        tt_traversal_counters* out) {
+    require(ctx && c, "null argument");
+    use_device(ctx);
+    SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
+    ImageRes* img = lookup<ImageRes>(ctx, target, KIND_IMAGE);
+    require(c->screen_size[0] == img->width && c->screen_size[1] == img->height,
+            "constants.screen_size must equal the target extent");
+    RenderParams p;
+    p.sc = s->dev;
+    p.c = *c;
+    p.target = img->buf.as<float4>();
+    p.err = ctx->err_word.as<uint32_t>();
+    p.counters = ctx->counters.as<unsigned long long>();
+    arm_error_word(ctx);
+    if (counted) check_cuda(cudaMemsetAsync(ctx->counters.ptr, 0, 64, ctx->stream), "memset");
+    check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
+    launch_integrate(p, counted, ctx->stream);
+    check_cuda(cudaGetLastError(), "integrate launch");
+    check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
+    ctx->integrate_timed = true;
+    fetch_error_word(ctx);
+    if (counted) {
+        unsigned long long h[6];
+        check_cuda(cudaMemcpyAsync(h, ctx->counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        sync(ctx);
+        out->rays = h[0];
+        out->blas_nodes = h[1];
+        out->tlas_nodes = h[2];
+        out->triangles = h[3];
+        out->instances = h[4];
+        out->hits = h[5];
+    }
+}
+
+// Copies host data into stream-ordered device scratch, runs `launch`, copies results back.
+template <class L>
+static void batch(tt_context* ctx, const void* in, uint64_t in_bytes, const void* extra, uint64_t extra_bytes,
+                  void* out, uint64_t out_bytes, L&& launch) {
+    use_device(ctx);
+    cudaStream_t st = ctx->stream;
+    void *din = nullptr, *dex = nullptr, *dout = nullptr;
+    check_cuda(cudaMallocAsync(&din, in_bytes ? in_bytes : 16, st), "cudaMallocAsync");
+    check_cuda(cudaMallocAsync(&dout, out_bytes ? out_bytes : 16, st), "cudaMallocAsync");
+    if (extra_bytes) check_cuda(cudaMallocAsync(&dex, extra_bytes, st), "cudaMallocAsync");
+    if (in_bytes) check_cuda(cudaMemcpyAsync(din, in, in_bytes, cudaMemcpyHostToDevice, st), "upload");
+    if (extra_bytes) check_cuda(cudaMemcpyAsync(dex, extra, extra_bytes, cudaMemcpyHostToDevice, st), "upload");
+    launch(din, dex, dout);
+    check_cuda(cudaGetLastError(), "batch launch");
+    if (out_bytes) check_cuda(cudaMemcpyAsync(out, dout, out_bytes, cudaMemcpyDeviceToHost, st), "download");
+    cudaFreeAsync(din, st);
+    cudaFreeAsync(dout, st);
+    if (dex) cudaFreeAsync(dex, st);
+    sync(ctx);
+}
+
+extern "C" {
+
+int32_t tt_abi_version(void) { return TT_ABI_VERSION; }
+const char* tt_last_error(void) { return g_last_error.c_str(); }
+
+int32_t tt_context_create(int32_t device, tt_context** out) {
+    return guarded([&] {
+        require(out != nullptr, "out is null");
+        int count = 0;
+        cudaError_t e = cudaGetDeviceCount(&count);
+        if (e != cudaSuccess || count == 0) fail(TT_ERR_NO_DEVICE, "no CUDA device available");
+        require(device >= 0 && device < count, "device index out of range");
+        std::unique_ptr<tt_context> ctx(new tt_context());
+        ctx->device = device;
+        use_device(ctx.get());
+        check_cuda(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream");
+        for (auto& ev : ctx->ev_integrate) check_cuda(cudaEventCreate(&ev), "event");
+        for (auto& ev : ctx->ev_post) check_cuda(cudaEventCreate(&ev), "event");
+        for (auto& ev : ctx->user_events) check_cuda(cudaEventCreate(&ev), "event");
+        ctx->err_word.alloc(16);
+        ctx->counters.alloc(8 * 8);
+        check_cuda(cudaMallocHost(&ctx->err_host, 16), "cudaMallocHost");
+        *ctx->err_host = 0;
+        *out = ctx.release();
+    });
+}
+
+int32_t tt_context_destroy(tt_context* ctx) {
+    return guarded([&] {
+        if (!ctx) return;
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        for (auto& p : ctx->pools) {
+            p.images.clear();
+            p.scenes.clear();
+        }
+        ctx->err_word = DeviceBuffer();
+        ctx->counters = DeviceBuffer();
+        ctx->l2_flush = DeviceBuffer();
+        for (auto& ev : ctx->ev_integrate) cudaEventDestroy(ev);
+        for (auto& ev : ctx->ev_post) cudaEventDestroy(ev);
+        for (auto& ev : ctx->user_events) cudaEventDestroy(ev);
+        if (ctx->err_host) cudaFreeHost(ctx->err_host);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+    });
+}
+
+int32_t tt_frame_index(tt_context* ctx, uint64_t* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        *out = ctx->frame_index;
+    });
+}
+
+int32_t tt_advance_frame(tt_context* ctx) {
+    return guarded([&] {
+        require(ctx, "null context");
+        ctx->frame_index++;
+    });
+}
+
+int32_t tt_clear_lifetime(tt_context* ctx, uint32_t lifetime) {
+    return guarded([&] {
+        require(ctx, "null context");
+        require(lifetime < (uint32_t)LIFETIMES, "unknown lifetime");
+        use_device(ctx);
+        sync(ctx);
+        Pool& p = ctx->pools[lifetime];
+        p.images.clear();
+        p.scenes.clear();
+        p.epoch++;
+    });
+}
+
+int32_t tt_synchronize(tt_context* ctx) {
+    return guarded([&] {
+        require(ctx, "null context");
+        use_device(ctx);
+        sync(ctx);
+    });
+}
+
+int32_t tt_image_create(tt_context* ctx, uint32_t lifetime, uint32_t width, uint32_t height, tt_handle* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        require(lifetime < (uint32_t)LIFETIMES, "unknown lifetime");
+        require(width > 0 && height > 0 && width <= 65536 && height <= 65536, "bad image extent");
+        use_device(ctx);
+        auto img = std::make_unique<ImageRes>();
+        img->width = width;
+        img->height = height;
+        img->buf.alloc((uint64_t)width * height * 16ull);
+        check_cuda(cudaMemsetAsync(img->buf.ptr, 0, img->buf.bytes, ctx->stream), "memset");
+        Pool& p = ctx->pools[lifetime];
+        p.images.push_back(std::move(img));
+        *out = make_handle(lifetime, KIND_IMAGE, p.epoch, (uint32_t)(p.images.size() - 1));
+    });
+}
+
+int32_t tt_image_write(tt_context* ctx, tt_handle image, const float* host, uint64_t bytes) {
+    return guarded([&] {
+        require(ctx && host, "null argument");
+        use_device(ctx);
+        ImageRes* img = lookup<ImageRes>(ctx, image, KIND_IMAGE);
+        require(bytes == img->buf.bytes, "byte count must equal width * height * 16");
+        check_cuda(cudaMemcpyAsync(img->buf.ptr, host, bytes, cudaMemcpyHostToDevice, ctx->stream), "write");
+        sync(ctx);
+    });
+}
+
+int32_t tt_image_download(tt_context* ctx, tt_handle image, float* host, uint64_t bytes) {
+    return guarded([&] {
+        require(ctx && host, "null argument");
+        use_device(ctx);
+        ImageRes* img = lookup<ImageRes>(ctx, image, KIND_IMAGE);
+        require(bytes == img->buf.bytes, "byte count must equal width * height * 16");
+        check_cuda(cudaMemcpyAsync(host, img->buf.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
+        sync(ctx);
+    });
+}
+
+int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        validate_scene(d);
+        use_device(ctx);
+        cudaStream_t st = ctx->stream;
+        auto s = std::make_unique<SceneRes>();
+        cudaEvent_t e0, e1;
+        check_cuda(cudaEventCreate(&e0), "event");
+        check_cuda(cudaEventCreate(&e1), "event");
+        check_cuda(cudaEventRecord(e0, st), "event");
+        upload(s->positions, d->positions, d->position_count * 3ull, st);
+        upload(s->indices, d->indices, d->index_count, st);
+        upload(s->vertices, d->vertices, d->vertex_count, st);
+        upload(s->materials, d->materials, d->material_count, st);
+        upload(s->instances, d->instances, d->instance_count, st);
+        upload(s->emissive, d->emissive_triangles, d->emissive_triangle_count, st);
+        std::vector<float4> xf(4ull * d->instance_count);
+        for (uint32_t i = 0; i < d->instance_count; ++i) {
+            const float* m = d->instances[i].inverse_transform;
+            for (int r = 0; r < 3; ++r) xf[4ull * i + r] = make_float4(m[r], m[4 + r], m[8 + r], m[12 + r]);
+            uint32_t w[4] = {d->instances[i].mesh_index, d->instances[i].material_index,
+                             d->instances[i].index_offset, d->instances[i].vertex_offset};
+            float4 v;
+            std::memcpy(&v, w, 16);
+            xf[4ull * i + 3] = v;
+        }
+        upload(s->inst_xform, xf.data(), xf.size(), st);
+        BuildInput bi{s->positions.as<int16_t>(), s->indices.as<uint32_t>(), d->meshes, d->mesh_count,
+                      d->instances, d->instance_count};
+        build_scene_bvh(bi, st, BLAS_LEAF_MAX, s->bvh);
+        check_cuda(cudaEventRecord(e1, st), "event");
+        check_cuda(cudaEventSynchronize(e1), "event");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ctx->scene_build_ms = ms;
+        uint64_t need_stack = 3ull * (s->bvh.blas_levels + s->bvh.tlas_levels) + 1ull;
+        if (need_stack > (uint64_t)TRAVERSAL_STACK)
+            fail(TT_ERR_OVERFLOW, "scene BVH is too deep for the traversal stack (" +
+                                      std::to_string(need_stack) + " entries needed)");
+        DevScene& ds = s->dev;
+        ds.positions = s->positions.as<int16_t>();
+        ds.indices = s->indices.as<uint32_t>();
+        ds.vertices = s->vertices.as<tt_vertex>();
+        ds.materials = s->materials.as<tt_material>();
+        ds.instances = s->instances.as<tt_instance>();
+        ds.emissive = s->emissive.as<tt_emissive_triangle>();
+        ds.blas = s->bvh.blas.as<uint4>();
+        ds.tris = s->bvh.tris.as<float4>();
+        ds.tlas = s->bvh.tlas.as<uint4>();
+        ds.inst_xform = s->inst_xform.as<float4>();
+        ds.emissive_count = d->emissive_triangle_count;
+        ds.instance_count = d->instance_count;
+        ds.has_tlas = s->bvh.tlas_nodes > 0 ? 1u : 0u;
+        tt_scene_stats& stt = s->stats;
+        stt.triangle_count = s->bvh.tri_count;
+        stt.instance_count = d->instance_count;
+        stt.emissive_count = d->emissive_triangle_count;
+        stt.blas_nodes = s->bvh.blas_nodes;
+        stt.tlas_nodes = s->bvh.tlas_nodes;
+        stt.blas_levels = s->bvh.blas_levels;
+        stt.tlas_levels = s->bvh.tlas_levels;
+        stt.device_bytes = s->positions.bytes + s->indices.bytes + s->vertices.bytes + s->materials.bytes +
+                           s->instances.bytes + s->emissive.bytes + s->inst_xform.bytes + s->bvh.blas.bytes +
+                           s->bvh.tris.bytes + s->bvh.tlas.bytes;
+        stt.max_stack = need_stack;
+        Pool& p = ctx->pools[TT_LIFETIME_SCENE];
+        p.scenes.push_back(std::move(s));
+        *out = make_handle(TT_LIFETIME_SCENE, KIND_SCENE, p.epoch, (uint32_t)(p.scenes.size() - 1));
+    });
+}
+
+int32_t tt_scene_stats_get(tt_context* ctx, tt_handle scene, tt_scene_stats* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        *out = lookup<SceneRes>(ctx, scene, KIND_SCENE)->stats;
+    });
+}
+
+int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint64_t blas_bytes, void* tris,
+                              uint64_t tri_bytes, void* tlas, uint64_t tlas_bytes) {
+    return guarded([&] {
+        require(ctx, "null context");
+        use_device(ctx);
+        SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
+        require(blas_bytes == s->bvh.blas_nodes * 64ull && tri_bytes == s->bvh.tri_count * 48ull &&
+                    tlas_bytes == s->bvh.tlas_nodes * 64ull,
+                "byte counts must match tt_scene_stats");
+        if (blas && blas_bytes)
+            check_cuda(cudaMemcpyAsync(blas, s->bvh.blas.ptr, blas_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        if (tris && tri_bytes)
+            check_cuda(cudaMemcpyAsync(tris, s->bvh.tris.ptr, tri_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        if (tlas && tlas_bytes)
+            check_cuda(cudaMemcpyAsync(tlas, s->bvh.tlas.ptr, tlas_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        sync(ctx);
+    });
+}
+
+int32_t tt_render(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target) {
+    return guarded([&] { render_impl(ctx, scene, constants, target, false, nullptr); });
+}
+
+int32_t tt_render_counted(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target,
+                          tt_traversal_counters* out) {
+    return guarded([&] {
+        require(out != nullptr, "null counters");
+        render_impl(ctx, scene, constants, target, true, out);
+    });
+}
+
+int32_t tt_tonemap(tt_context* ctx, tt_handle image, const tt_constants* constants, uint32_t format,
+                   void* host_out, uint64_t bytes) {
+    return guarded([&] {
+        require(ctx && constants && host_out, "null argument");
+        require(format == TT_FORMAT_RGBA32F || format == TT_FORMAT_RGBA8_UNORM, "unknown format");
+        use_device(ctx);
+        ImageRes* img = lookup<ImageRes>(ctx, image, KIND_IMAGE);
+        uint64_t n = (uint64_t)img->width * img->height;
+        uint64_t need = n * (format == TT_FORMAT_RGBA32F ? 16ull : 4ull);
+        require(bytes == need, "byte count does not match the image and format");
+        void* d = nullptr;
+        check_cuda(cudaMallocAsync(&d, need, ctx->stream), "cudaMallocAsync");
+        check_cuda(cudaEventRecord(ctx->ev_post[0], ctx->stream), "event");
+        launch_tonemap(img->buf.as<float4>(), n, constants->tonemap, format, d, ctx->stream);
+        check_cuda(cudaGetLastError(), "tonemap launch");
+        check_cuda(cudaEventRecord(ctx->ev_post[1], ctx->stream), "event");
+        ctx->post_timed = true;
+        check_cuda(cudaMemcpyAsync(host_out, d, need, cudaMemcpyDeviceToHost, ctx->stream), "download");
+        check_cuda(cudaFreeAsync(d, ctx->stream), "cudaFreeAsync");
+        sync(ctx);
+    });
+}
+
+int32_t tt_timings_get(tt_context* ctx, tt_timings* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        use_device(ctx);
+        sync(ctx);
+        float a = 0.0f, b = 0.0f;
+        if (ctx->integrate_timed) check_cuda(cudaEventElapsedTime(&a, ctx->ev_integrate[0], ctx->ev_integrate[1]), "elapsed");
+        if (ctx->post_timed) check_cuda(cudaEventElapsedTime(&b, ctx->ev_post[0], ctx->ev_post[1]), "elapsed");
+        out->integrate_ns = (uint64_t)((double)a * 1.0e6);
+        out->post_process_ns = (uint64_t)((double)b * 1.0e6);
+        out->scene_build_ns = (uint64_t)((double)ctx->scene_build_ms * 1.0e6);
+    });
+}
+
+int32_t tt_bsdf_eval_batch(tt_context* ctx, const tt_material_constants* material, const float* samples,
+                           uint32_t n, float* results) {
+    return guarded([&] {
+        require(ctx && material && (n == 0 || (samples && results)), "null argument");
+        batch(ctx, samples, 32ull * n, material, sizeof(tt_material_constants), results, 32ull * n,
+              [&](void* din, void* dex, void* dout) {
+                  launch_bsdf_eval(static_cast<const tt_material_constants*>(dex), static_cast<const float4*>(din), n,
+                                   static_cast<float4*>(dout), ctx->stream);
+              });
+    });
+}
+
+int32_t tt_bsdf_sample_batch(tt_context* ctx, const tt_material_constants* material, const float* samples,
+                             uint32_t n, float* results) {
+    return guarded([&] {
+        require(ctx && material && (n == 0 || (samples && results)), "null argument");
+        batch(ctx, samples, 16ull * n, material, sizeof(tt_material_constants), results, 48ull * n,
+              [&](void* din, void* dex, void* dout) {
+                  launch_bsdf_sample(static_cast<const tt_material_constants*>(dex), static_cast<const float4*>(din),
+                                     n, static_cast<float4*>(dout), ctx->stream);
+              });
+    });
+}
+
+int32_t tt_trace_batch(tt_context* ctx, tt_handle scene, const float* rays, uint32_t n, uint32_t flags,
+                       uint32_t* hits) {
+    return guarded([&] {
+        require(ctx && (n == 0 || (rays && hits)), "null argument");
+        SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
+        arm_error_word(ctx);
+        batch(ctx, rays, 32ull * n, nullptr, 0, hits, 32ull * n, [&](void* din, void*, void* dout) {
+            launch_trace(s->dev, static_cast<const float4*>(din), n, flags, static_cast<uint4*>(dout),
+                         ctx->err_word.as<uint32_t>(), ctx->stream);
+            fetch_error_word(ctx);
+        });
+    });
+}
+
+int32_t tt_math_batch(tt_context* ctx, int32_t which, const float* x, uint64_t n, float* y) {
+    return guarded([&] {
+        require(ctx && (n == 0 || (x && y)), "null argument");
+        require(which >= 0 && which <= 4, "unknown function");
+        batch(ctx, x, 4ull * n, nullptr, 0, y, 4ull * n, [&](void* din, void*, void* dout) {
+            launch_math(which, static_cast<const float*>(din), n, static_cast<float*>(dout), ctx->stream);
+        });
+    });
+}
+
+int32_t tt_flush_l2(tt_context* ctx) {
+    return guarded([&] {
+        require(ctx, "null context");
+        use_device(ctx);
+        if (!ctx->l2_flush.ptr) ctx->l2_flush.alloc(L2_FLUSH_BYTES);
+        check_cuda(cudaMemsetAsync(ctx->l2_flush.ptr, (int)(ctx->frame_index & 0xff), L2_FLUSH_BYTES, ctx->stream),
+                   "flush");
+    });
+}
+
+int32_t tt_event_record(tt_context* ctx, uint32_t slot) {
+    return guarded([&] {
+        require(ctx && slot < (uint32_t)EVENT_SLOTS, "bad argument");
+        use_device(ctx);
+        check_cuda(cudaEventRecord(ctx->user_events[slot], ctx->stream), "event");
+    });
+}
+
+int32_t tt_event_elapsed_ms(tt_context* ctx, uint32_t a, uint32_t b, float* ms) {
+    return guarded([&] {
+        require(ctx && ms && a < (uint32_t)EVENT_SLOTS && b < (uint32_t)EVENT_SLOTS, "bad argument");
+        use_device(ctx);
+        check_cuda(cudaEventSynchronize(ctx->user_events[b]), "event sync");
+        check_cuda(cudaEventElapsedTime(ms, ctx->user_events[a], ctx->user_events[b]), "elapsed");
+    });
+}
+
+int32_t tt_host_alloc(uint64_t bytes, void** out) {
+    return guarded([&] {
+        require(out != nullptr, "null argument");
+        check_cuda(cudaMallocHost(out, bytes ? bytes : 16), "cudaMallocHost");
+    });
+}
+
+int32_t tt_host_free(void* p) {
+    return guarded([&] {
+        if (p) check_cuda(cudaFreeHost(p), "cudaFreeHost");
+    });
+}
+
+}  // extern "C"

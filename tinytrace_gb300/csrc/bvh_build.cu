@@ -1,0 +1,692 @@
+// GPU LBVH build: the replacement for the driver-side BLAS/TLAS builds of the reference
+// (src/scene.rs:130-171 -> crates/tinytrace_backend/src/resource.rs:728-880, 891-1085).
+//
+// Pipeline (one pass builds every mesh's BLAS at once; a second pass builds the TLAS):
+//   1. primitive boxes (triangles: dequantised snorm16 vertices; instances: the 8 transformed
+//      corners of their mesh box) and per-segment centroid bounds (float atomics);
+//   2. 30-bit Morton codes of the centroids, normalised per segment, prefixed by the segment
+//      (mesh) index: key = segment << 30 | morton;
+//   3. stable LSD radix sort of (key, primitive) in 8-bit digits;
+//   4. Karras (2012) binary radix tree over the sorted keys (index tie-break for duplicates);
+//      each segment's primitives form exactly one subtree;
+//   5. bottom-up box refit with one atomic visit counter per node;
+//   6. collapse to 4-wide nodes level by level from the segment roots (greedy expansion of
+//      the largest-area child, subtrees of <= leaf_max primitives become leaves) and 8-bit
+//      quantisation of the child boxes relative to the node box.
+// Every step is deterministic; the CPU oracle restates the same build and the tests compare
+// the node arrays byte for byte.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "tt_common.cuh"
+#include "tt_internal.h"
+
+namespace tt {
+namespace {
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+
+inline unsigned grid_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// ---------------------------------------------------------------- stream-ordered scratch
+struct Scratch {
+    cudaStream_t stream;
+    std::vector<void*> ptrs;
+    explicit Scratch(cudaStream_t s) : stream(s) {}
+    ~Scratch() {
+        for (void* p : ptrs) cudaFreeAsync(p, stream);
+    }
+    template <class T>
+    T* get(uint64_t count) {
+        void* p = nullptr;
+        size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
+        check_cuda(cudaMallocAsync(&p, bytes, stream), "cudaMallocAsync (bvh scratch)");
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+};
+
+// ---------------------------------------------------------------- exclusive scan (u32)
+__global__ void scan_block_kernel(uint32_t* data, uint32_t* block_sums, uint64_t n) {
+    __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_THREADS * 4;
+    uint32_t v[4];
+    uint32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint64_t i = base + (uint64_t)threadIdx.x * 4 + k;
+        v[k] = i < n ? data[i] : 0u;
+        local += v[k];
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_tot[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        warp_tot[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[warp] + incl - local;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint64_t i = base + (uint64_t)threadIdx.x * 4 + k;
+        if (i < n) data[i] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == SCAN_THREADS - 1 && block_sums) block_sums[blockIdx.x] = run;
+}
+__global__ void scan_add_kernel(uint32_t* data, const uint32_t* block_sums, uint64_t n) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) data[i] += block_sums[i / (SCAN_THREADS * 4)];
+}
+// In-place exclusive scan of n u32 values.
+void exclusive_scan(uint32_t* data, uint64_t n, Scratch& sc) {
+    if (n == 0) return;
+    const uint64_t per_block = SCAN_THREADS * 4;
+    uint64_t blocks = (n + per_block - 1) / per_block;
+    if (blocks == 1) {
+        scan_block_kernel<<<1, SCAN_THREADS, 0, sc.stream>>>(data, nullptr, n);
+        return;
+    }
+    uint32_t* sums = sc.get<uint32_t>(blocks);
+    scan_block_kernel<<<(unsigned)blocks, SCAN_THREADS, 0, sc.stream>>>(data, sums, n);
+    exclusive_scan(sums, blocks, sc);
+    scan_add_kernel<<<grid_for(n, 256), 256, 0, sc.stream>>>(data, sums, n);
+}
+
+// ---------------------------------------------------------------- radix sort (u64 key, u32 value)
+__global__ void radix_hist_kernel(const uint64_t* keys, uint32_t n, int shift, uint32_t* hist,
+                                  uint32_t nblocks) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t i = blockIdx.x * SORT_THREADS + threadIdx.x;
+    if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 0xffu], 1u);
+    __syncthreads();
+    hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+__global__ void radix_scatter_kernel(const uint64_t* kin, const uint32_t* vin, uint64_t* kout,
+                                     uint32_t* vout, const uint32_t* offsets, uint32_t n,
+                                     int shift, uint32_t nblocks) {
+    __shared__ uint32_t wh[SORT_WARPS][256];
+    for (int w = 0; w < SORT_WARPS; ++w) wh[w][threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t i = blockIdx.x * SORT_THREADS + threadIdx.x;
+    bool valid = i < n;
+    uint64_t key = valid ? kin[i] : 0ull;
+    uint32_t digit = valid ? ((uint32_t)(key >> shift) & 0xffu) : 256u;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    int leader = __ffs(peers) - 1;
+    if (valid && lane == leader) wh[warp][digit] = __popc(peers);
+    __syncthreads();
+    {
+        uint32_t run = 0;
+        for (int w = 0; w < SORT_WARPS; ++w) {
+            uint32_t c = wh[w][threadIdx.x];
+            wh[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    if (valid) {
+        uint32_t pos = offsets[(uint64_t)digit * nblocks + blockIdx.x] + wh[warp][digit] + rank;
+        kout[pos] = key;
+        vout[pos] = vin[i];
+    }
+}
+// Stable sort of (keys, vals) by the low `bits` bits of the keys. Result in keys/vals.
+void radix_sort(uint64_t*& keys, uint32_t*& vals, uint32_t n, int bits, Scratch& sc) {
+    if (n <= 1) return;
+    uint32_t nblocks = grid_for(n, SORT_THREADS);
+    uint64_t* k2 = sc.get<uint64_t>(n);
+    uint32_t* v2 = sc.get<uint32_t>(n);
+    uint32_t* hist = sc.get<uint32_t>((uint64_t)256 * nblocks);
+    for (int shift = 0; shift < bits; shift += 8) {
+        radix_hist_kernel<<<nblocks, SORT_THREADS, 0, sc.stream>>>(keys, n, shift, hist, nblocks);
+        exclusive_scan(hist, (uint64_t)256 * nblocks, sc);
+        radix_scatter_kernel<<<nblocks, SORT_THREADS, 0, sc.stream>>>(keys, vals, k2, v2, hist, n,
+                                                                     shift, nblocks);
+        std::swap(keys, k2);
+        std::swap(vals, v2);
+    }
+}
+
+// ---------------------------------------------------------------- float atomics
+__device__ __forceinline__ void atomic_min_f(float* a, float v) {
+    if (v >= 0.0f) atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+    else atomicMax(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float* a, float v) {
+    if (v >= 0.0f) atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+    else atomicMin(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ float canon(float v) { return v + 0.0f; }  // -0 -> +0
+
+// ---------------------------------------------------------------- primitives
+// Triangle boxes + records for all meshes.  mesh_tri_base: prefix of triangle counts.
+__global__ void triangle_prims_kernel(const int16_t* positions, const uint32_t* indices,
+                                      const tt_mesh* meshes, const uint32_t* mesh_tri_base,
+                                      uint32_t mesh_count, uint32_t n, float4* lo, float4* hi,
+                                      uint32_t* seg, float4* recs) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    // last mesh with base <= g
+    uint32_t a = 0, b = mesh_count;
+    while (b - a > 1) {
+        uint32_t m = (a + b) / 2;
+        if (mesh_tri_base[m] <= g) a = m;
+        else b = m;
+    }
+    // skip meshes without triangles that share the same base
+    while (a + 1 < mesh_count && mesh_tri_base[a + 1] <= g) ++a;
+    const tt_mesh me = meshes[a];
+    uint32_t p = g - mesh_tri_base[a];
+    uint32_t base = me.index_offset + 3u * p;
+    f3 q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int16_t* s = positions + 3ull * (me.vertex_offset + indices[base + k]);
+        q[k] = f3{dequant_snorm16(s[0]), dequant_snorm16(s[1]), dequant_snorm16(s[2])};
+    }
+    f3 l = f3{fmn(fmn(q[0].x, q[1].x), q[2].x), fmn(fmn(q[0].y, q[1].y), q[2].y),
+              fmn(fmn(q[0].z, q[1].z), q[2].z)};
+    f3 h = f3{fmx(fmx(q[0].x, q[1].x), q[2].x), fmx(fmx(q[0].y, q[1].y), q[2].y),
+              fmx(fmx(q[0].z, q[1].z), q[2].z)};
+    lo[g] = make_float4(canon(l.x), canon(l.y), canon(l.z), 0.0f);
+    hi[g] = make_float4(canon(h.x), canon(h.y), canon(h.z), 0.0f);
+    seg[g] = a;
+    recs[3ull * g + 0] = make_float4(q[0].x, q[0].y, q[0].z, __uint_as_float(p));
+    recs[3ull * g + 1] = make_float4(q[1].x, q[1].y, q[1].z, __uint_as_float(a));
+    recs[3ull * g + 2] = make_float4(q[2].x, q[2].y, q[2].z, 0.0f);
+}
+
+// Instance world boxes from the mesh boxes (8 transformed corners).
+__global__ void instance_prims_kernel(const tt_instance* inst, const uint32_t* ids, uint32_t n,
+                                      const float4* mesh_lo, const float4* mesh_hi, float4* lo,
+                                      float4* hi, uint32_t* seg) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const tt_instance& in = inst[ids[i]];
+    float4 ml = mesh_lo[in.mesh_index], mh = mesh_hi[in.mesh_index];
+    f3 l = splat(__int_as_float(0x7f800000)), h = splat(__int_as_float(0xff800000));
+    for (int k = 0; k < 8; ++k) {
+        f3 c = f3{(k & 1) ? mh.x : ml.x, (k & 2) ? mh.y : ml.y, (k & 4) ? mh.z : ml.z};
+        f3 w = mat43_point(in.transform, c);
+        l = f3{fmn(l.x, w.x), fmn(l.y, w.y), fmn(l.z, w.z)};
+        h = f3{fmx(h.x, w.x), fmx(h.y, w.y), fmx(h.z, w.z)};
+    }
+    lo[i] = make_float4(canon(l.x), canon(l.y), canon(l.z), 0.0f);
+    hi[i] = make_float4(canon(h.x), canon(h.y), canon(h.z), 0.0f);
+    seg[i] = 0u;
+}
+
+__global__ void init_bounds_kernel(float* b, uint32_t* cnt, uint32_t segs) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= segs) return;
+    for (int a = 0; a < 3; ++a) {
+        b[6 * s + a] = __int_as_float(0x7f800000);
+        b[6 * s + 3 + a] = __int_as_float(0xff800000);
+    }
+    cnt[s] = 0u;
+}
+__global__ void centroid_bounds_kernel(const float4* lo, const float4* hi, const uint32_t* seg,
+                                       uint32_t n, float* b, uint32_t* cnt) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 l = lo[i], h = hi[i];
+    float c[3] = {canon((l.x + h.x) * 0.5f), canon((l.y + h.y) * 0.5f), canon((l.z + h.z) * 0.5f)};
+    uint32_t s = seg[i];
+    for (int a = 0; a < 3; ++a) {
+        atomic_min_f(&b[6 * s + a], c[a]);
+        atomic_max_f(&b[6 * s + 3 + a], c[a]);
+    }
+    atomicAdd(&cnt[s], 1u);
+}
+
+__device__ __forceinline__ uint32_t expand_bits10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__device__ __forceinline__ uint32_t quantize_axis(float c, float lo, float hi) {
+    float ext = hi - lo;
+    if (!(ext > 0.0f)) return 0u;
+    float f = (c - lo) / ext;
+    float s = fmn(fmx(f * 1024.0f, 0.0f), 1023.0f);
+    return (uint32_t)s;
+}
+__global__ void morton_kernel(const float4* lo, const float4* hi, const uint32_t* seg, uint32_t n,
+                              const float* b, uint64_t* keys, uint32_t* vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 l = lo[i], h = hi[i];
+    float c[3] = {canon((l.x + h.x) * 0.5f), canon((l.y + h.y) * 0.5f), canon((l.z + h.z) * 0.5f)};
+    uint32_t s = seg[i];
+    const float* bb = b + 6 * s;
+    uint32_t x = quantize_axis(c[0], bb[0], bb[3]);
+    uint32_t y = quantize_axis(c[1], bb[1], bb[4]);
+    uint32_t z = quantize_axis(c[2], bb[2], bb[5]);
+    uint32_t code = (expand_bits10(x) << 2) | (expand_bits10(y) << 1) | expand_bits10(z);
+    keys[i] = ((uint64_t)s << 30) | code;
+    vals[i] = i;
+}
+
+// ---------------------------------------------------------------- Karras hierarchy
+__device__ __forceinline__ int kdelta(const uint64_t* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = k[i], b = k[j];
+    if (a != b) return __clzll((long long)(a ^ b));
+    return 64 + __clz((int)((uint32_t)i ^ (uint32_t)j));
+}
+__global__ void karras_kernel(const uint64_t* k, int n, int* left, int* right, int* first,
+                              int* last, int* parent) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int ni = n - 1;
+    if (i >= ni) return;
+    int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = kdelta(k, n, i, i - d);
+    int lmax = 2;
+    while (kdelta(k, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (kdelta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = kdelta(k, n, i, j);
+    int s = 0;
+    for (int div = 2;; div *= 2) {
+        int t = (l + div - 1) / div;
+        if (kdelta(k, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t == 1) break;
+    }
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    int lc = (lo == gamma) ? (ni + gamma) : gamma;
+    int rc = (hi == gamma + 1) ? (ni + gamma + 1) : (gamma + 1);
+    left[i] = lc;
+    right[i] = rc;
+    first[i] = lo;
+    last[i] = hi;
+    parent[lc] = i;
+    parent[rc] = i;
+}
+
+// ---------------------------------------------------------------- refit
+// Node boxes: index r < ni internal, r >= ni leaf (r - ni = sorted position).
+__global__ void refit_kernel(int n, const uint32_t* order, const float4* plo, const float4* phi,
+                             const int* left, const int* right, const int* parent, float4* blo,
+                             float4* bhi, uint32_t* visits) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int ni = n - 1;
+    int r = ni + j;
+    blo[r] = plo[order[j]];
+    bhi[r] = phi[order[j]];
+    if (ni == 0) return;
+    int p = parent[r];
+    while (p >= 0) {
+        __threadfence();
+        if (atomicAdd(&visits[p], 1u) == 0u) return;
+        int a = left[p], b = right[p];
+        float4 al = __ldcg(&blo[a]), ah = __ldcg(&bhi[a]);
+        float4 bl = __ldcg(&blo[b]), bh = __ldcg(&bhi[b]);
+        blo[p] = make_float4(fmn(al.x, bl.x), fmn(al.y, bl.y), fmn(al.z, bl.z), 0.0f);
+        bhi[p] = make_float4(fmx(ah.x, bh.x), fmx(ah.y, bh.y), fmx(ah.z, bh.z), 0.0f);
+        p = parent[p];
+    }
+}
+
+__global__ void segment_roots_kernel(const uint32_t* seg_first, const uint32_t* seg_count,
+                                     uint32_t segs, int n, const int* first, const int* last,
+                                     int* level) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= segs) return;
+    int ni = n - 1;
+    int a = (int)seg_first[s], c = (int)seg_count[s];
+    int b = a + c - 1;
+    int r;
+    if (c == 0) r = -1;
+    else if (c == 1) r = ni + a;
+    else if (first[a] == a && last[a] == b) r = a;
+    else r = b;
+    level[s] = r;
+}
+
+// ---------------------------------------------------------------- collapse to BVH4
+struct TreeView {
+    int n, ni;
+    const int *left, *right, *first, *last;
+    const float4 *blo, *bhi;
+    __device__ bool is_leaf(int r) const { return r >= ni; }
+    __device__ int nfirst(int r) const { return is_leaf(r) ? r - ni : first[r]; }
+    __device__ int ncount(int r) const { return is_leaf(r) ? 1 : last[r] - first[r] + 1; }
+    __device__ float half_area(int r) const {
+        float4 l = blo[r], h = bhi[r];
+        float ex = h.x - l.x, ey = h.y - l.y, ez = h.z - l.z;
+        return ex * ey + ey * ez + ez * ex;
+    }
+};
+
+__global__ void collapse_choose_kernel(TreeView t, const int* level, uint32_t L, int leaf_max,
+                                       int* chosen, uint32_t* internal_count) {
+    uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= L) return;
+    int r = level[li];
+    int ch[4] = {-1, -1, -1, -1};
+    int cnt = 0;
+    if (r < 0) {
+        cnt = 0;
+    } else if (t.is_leaf(r) || t.ncount(r) <= leaf_max) {
+        ch[0] = r;
+        cnt = 1;
+    } else {
+        ch[0] = t.left[r];
+        ch[1] = t.right[r];
+        cnt = 2;
+        while (cnt < 4) {
+            int best = -1;
+            float best_area = -1.0f;
+            for (int c = 0; c < cnt; ++c) {
+                if (t.is_leaf(ch[c]) || t.ncount(ch[c]) <= leaf_max) continue;
+                float a = t.half_area(ch[c]);
+                if (best < 0 || a > best_area) {
+                    best = c;
+                    best_area = a;
+                }
+            }
+            if (best < 0) break;
+            int v = ch[best];
+            for (int c = cnt; c > best + 1; --c) ch[c] = ch[c - 1];
+            ch[best] = t.left[v];
+            ch[best + 1] = t.right[v];
+            cnt++;
+        }
+    }
+    uint32_t internal = 0;
+    for (int c = 0; c < 4; ++c) {
+        chosen[4 * li + c] = ch[c];
+        if (c < cnt && !(t.is_leaf(ch[c]) || t.ncount(ch[c]) <= leaf_max)) internal++;
+    }
+    internal_count[li] = internal;
+}
+
+__global__ void collapse_emit_kernel(TreeView t, const int* level, uint32_t L, int leaf_max,
+                                     const int* chosen, const uint32_t* next_offset,
+                                     uint64_t node_base, uint64_t next_base, uint4* nodes,
+                                     int* next_level, const uint32_t* order,
+                                     const uint32_t* leaf_ids, int leaf_by_prim) {
+    uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= L) return;
+    int r = level[li];
+    int cnt = 0;
+    uint32_t child[4] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu};
+    uint32_t k = next_offset[li];
+    float clo[4][3], chi[4][3];
+    for (int c = 0; c < 4; ++c) {
+        int v = chosen[4 * li + c];
+        if (v < 0) break;
+        cnt++;
+        float4 l = t.blo[v], h = t.bhi[v];
+        clo[c][0] = l.x; clo[c][1] = l.y; clo[c][2] = l.z;
+        chi[c][0] = h.x; chi[c][1] = h.y; chi[c][2] = h.z;
+        if (t.is_leaf(v) || t.ncount(v) <= leaf_max) {
+            uint32_t f = (uint32_t)t.nfirst(v);
+            uint32_t kk = (uint32_t)t.ncount(v);
+            if (leaf_by_prim) {
+                uint32_t id = leaf_ids ? leaf_ids[order[f]] : order[f];
+                child[c] = 0x80000000u | id;
+            } else {
+                child[c] = 0x80000000u | ((kk - 1u) << 27) | f;
+            }
+        } else {
+            child[c] = (uint32_t)(next_base + k);
+            next_level[k] = v;
+            k++;
+        }
+    }
+    float pmin[3] = {0.0f, 0.0f, 0.0f}, pmax[3] = {0.0f, 0.0f, 0.0f};
+    if (cnt > 0) {
+        float4 l = t.blo[r], h = t.bhi[r];
+        pmin[0] = l.x; pmin[1] = l.y; pmin[2] = l.z;
+        pmax[0] = h.x; pmax[1] = h.y; pmax[2] = h.z;
+    }
+    uint32_t exps = 0, qlo[3] = {0, 0, 0}, qhi[3] = {0, 0, 0};
+    for (int a = 0; a < 3; ++a) {
+        double ext = (double)pmax[a] - (double)pmin[a];
+        int e = -126;
+        if (ext > 0.0) {
+            int ex;
+            frexp(ext / 255.0, &ex);
+            e = ex < -126 ? -126 : (ex > 127 ? 127 : ex);
+        }
+        double scale = ldexp(1.0, e);
+        exps |= (uint32_t)(e + 127) << (8 * a);
+        for (int c = 0; c < 4; ++c) {
+            uint32_t ql = 255u, qh = 0u;
+            if (c < cnt) {
+                double lo = floor(((double)clo[c][a] - (double)pmin[a]) / scale);
+                double hi = ceil(((double)chi[c][a] - (double)pmin[a]) / scale);
+                lo = lo < 0.0 ? 0.0 : (lo > 255.0 ? 255.0 : lo);
+                hi = hi < 0.0 ? 0.0 : (hi > 255.0 ? 255.0 : hi);
+                ql = (uint32_t)lo;
+                qh = (uint32_t)hi;
+            }
+            qlo[a] |= ql << (8 * c);
+            qhi[a] |= qh << (8 * c);
+        }
+    }
+    exps |= (uint32_t)cnt << 24;
+    uint4* nd = nodes + 4ull * (node_base + li);
+    nd[0] = make_uint4(__float_as_uint(pmin[0]), __float_as_uint(pmin[1]), __float_as_uint(pmin[2]), exps);
+    nd[1] = make_uint4(child[0], child[1], child[2], child[3]);
+    nd[2] = make_uint4(qlo[0], qlo[1], qlo[2], qhi[0]);
+    nd[3] = make_uint4(qhi[1], qhi[2], 0u, 0u);
+}
+
+__global__ void gather_records_kernel(const float4* in, const uint32_t* order, uint32_t n,
+                                      float4* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t s = order[i];
+    out[3ull * i + 0] = in[3ull * s + 0];
+    out[3ull * i + 1] = in[3ull * s + 1];
+    out[3ull * i + 2] = in[3ull * s + 2];
+}
+
+__global__ void segment_boxes_kernel(const int* roots, uint32_t segs, const float4* blo,
+                                     const float4* bhi, float4* slo, float4* shi) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= segs) return;
+    int r = roots[s];
+    if (r < 0) {
+        slo[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        shi[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    slo[s] = blo[r];
+    shi[s] = bhi[r];
+}
+
+struct Build4 {
+    uint64_t nodes = 0;
+    uint32_t levels = 0;
+    uint32_t* order = nullptr;  // scratch, sorted position -> primitive
+    float4* blo = nullptr;      // scratch, binary node boxes
+    float4* bhi = nullptr;
+    int* roots = nullptr;       // scratch, segment root binary refs
+};
+
+// Generic BVH4 build over primitive boxes grouped in non-decreasing segments.
+Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uint32_t n,
+                  uint32_t segs, int leaf_max, bool leaf_by_prim, const uint32_t* leaf_ids,
+                  DeviceBuffer& node_buf, Scratch& sc) {
+    cudaStream_t st = sc.stream;
+    Build4 out;
+    float* bounds = sc.get<float>(6ull * segs);
+    uint32_t* seg_count = sc.get<uint32_t>(segs);
+    init_bounds_kernel<<<grid_for(segs, 256), 256, 0, st>>>(bounds, seg_count, segs);
+    if (n > 0)
+        centroid_bounds_kernel<<<grid_for(n, 256), 256, 0, st>>>(plo, phi, seg, n, bounds, seg_count);
+    uint64_t* keys = sc.get<uint64_t>(n);
+    uint32_t* vals = sc.get<uint32_t>(n);
+    if (n > 0) morton_kernel<<<grid_for(n, 256), 256, 0, st>>>(plo, phi, seg, n, bounds, keys, vals);
+    int seg_bits = 0;
+    while ((1u << seg_bits) < segs) ++seg_bits;
+    radix_sort(keys, vals, n, 30 + seg_bits, sc);
+    out.order = vals;
+    // segment first positions
+    uint32_t* seg_first = sc.get<uint32_t>(segs);
+    check_cuda(cudaMemcpyAsync(seg_first, seg_count, 4ull * segs, cudaMemcpyDeviceToDevice, st), "copy");
+    exclusive_scan(seg_first, segs, sc);
+    // hierarchy
+    int ni = n > 0 ? (int)n - 1 : 0;
+    int* left = sc.get<int>(ni);
+    int* right = sc.get<int>(ni);
+    int* first = sc.get<int>(ni);
+    int* last = sc.get<int>(ni);
+    int* parent = sc.get<int>(ni + n);
+    uint32_t* visits = sc.get<uint32_t>(ni);
+    float4* blo = sc.get<float4>(ni + n);
+    float4* bhi = sc.get<float4>(ni + n);
+    check_cuda(cudaMemsetAsync(parent, 0xff, sizeof(int) * (size_t)std::max<uint64_t>(ni + n, 1), st), "memset");
+    check_cuda(cudaMemsetAsync(visits, 0, sizeof(uint32_t) * (size_t)std::max(ni, 1), st), "memset");
+    if (ni > 0) karras_kernel<<<grid_for(ni, 256), 256, 0, st>>>(keys, (int)n, left, right, first, last, parent);
+    if (n > 0)
+        refit_kernel<<<grid_for(n, 256), 256, 0, st>>>((int)n, vals, plo, phi, left, right, parent,
+                                                       blo, bhi, visits);
+    out.blo = blo;
+    out.bhi = bhi;
+    // collapse
+    uint64_t cap = (uint64_t)n + segs + 1;
+    node_buf.alloc(cap * 64ull);
+    int* lvl_a = sc.get<int>(cap);
+    int* lvl_b = sc.get<int>(cap);
+    int* chosen = sc.get<int>(4 * cap);
+    uint32_t* icount = sc.get<uint32_t>(cap + 1);
+    segment_roots_kernel<<<grid_for(segs, 256), 256, 0, st>>>(seg_first, seg_count, segs, (int)n,
+                                                               first, last, lvl_a);
+    int* roots = sc.get<int>(segs);
+    check_cuda(cudaMemcpyAsync(roots, lvl_a, sizeof(int) * segs, cudaMemcpyDeviceToDevice, st), "copy");
+    out.roots = roots;
+    TreeView tv{(int)n, ni, left, right, first, last, blo, bhi};
+    uint64_t base = 0;
+    uint32_t L = segs;
+    while (L > 0) {
+        out.levels++;
+        collapse_choose_kernel<<<grid_for(L, 128), 128, 0, st>>>(tv, lvl_a, L, leaf_max, chosen, icount);
+        check_cuda(cudaMemsetAsync(icount + L, 0, 4, st), "memset");
+        exclusive_scan(icount, (uint64_t)L + 1, sc);
+        uint32_t next = 0;
+        check_cuda(cudaMemcpyAsync(&next, icount + L, 4, cudaMemcpyDeviceToHost, st), "copy");
+        check_cuda(cudaStreamSynchronize(st), "sync");
+        if (base + L + next > cap) fail(TT_ERR_OVERFLOW, "bvh node capacity exceeded");
+        collapse_emit_kernel<<<grid_for(L, 128), 128, 0, st>>>(
+            tv, lvl_a, L, leaf_max, chosen, icount, base, base + L, node_buf.as<uint4>(), lvl_b,
+            vals, leaf_ids, leaf_by_prim ? 1 : 0);
+        base += L;
+        L = next;
+        std::swap(lvl_a, lvl_b);
+    }
+    out.nodes = base;
+    return out;
+}
+
+}  // namespace
+
+void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, BvhResult& out) {
+    Scratch sc(stream);
+    // triangle primitives (mesh order)
+    std::vector<uint32_t> tri_base(in.mesh_count + 1, 0);
+    for (uint32_t m = 0; m < in.mesh_count; ++m)
+        tri_base[m + 1] = tri_base[m] + in.meshes_host[m].index_count / 3u;
+    uint32_t n = tri_base[in.mesh_count];
+    uint32_t segs = std::max<uint32_t>(in.mesh_count, 1);
+    tt_mesh* d_meshes = sc.get<tt_mesh>(segs);
+    uint32_t* d_base = sc.get<uint32_t>(in.mesh_count + 1);
+    if (in.mesh_count) {
+        check_cuda(cudaMemcpyAsync(d_meshes, in.meshes_host, sizeof(tt_mesh) * in.mesh_count,
+                                   cudaMemcpyHostToDevice, stream), "upload meshes");
+        check_cuda(cudaMemcpyAsync(d_base, tri_base.data(), 4ull * (in.mesh_count + 1),
+                                   cudaMemcpyHostToDevice, stream), "upload bases");
+    }
+    if (in.mesh_count == 0) {  // empty scene: no BLAS, no TLAS, every ray misses
+        out.blas.alloc(0);
+        out.tris.alloc(0);
+        out.tlas.alloc(0);
+        out.blas_nodes = out.tlas_nodes = out.tri_count = 0;
+        out.blas_levels = out.tlas_levels = 0;
+        return;
+    }
+    float4* plo = sc.get<float4>(n);
+    float4* phi = sc.get<float4>(n);
+    uint32_t* seg = sc.get<uint32_t>(n);
+    float4* recs = sc.get<float4>(3ull * n);
+    if (n > 0)
+        triangle_prims_kernel<<<grid_for(n, 256), 256, 0, stream>>>(
+            in.positions, in.indices, d_meshes, d_base, in.mesh_count, n, plo, phi, seg, recs);
+    Build4 b = build_bvh4(plo, phi, seg, n, in.mesh_count, leaf_max, false, nullptr, out.blas, sc);
+    out.blas_nodes = b.nodes;
+    out.blas_levels = b.levels;
+    out.tri_count = n;
+    out.tris.alloc(std::max<uint64_t>(n, 1) * 48ull);
+    if (n > 0)
+        gather_records_kernel<<<grid_for(n, 256), 256, 0, stream>>>(recs, b.order, n, out.tris.as<float4>());
+    // mesh boxes -> instance primitives
+    float4* mlo = sc.get<float4>(segs);
+    float4* mhi = sc.get<float4>(segs);
+    if (in.mesh_count)
+        segment_boxes_kernel<<<grid_for(in.mesh_count, 256), 256, 0, stream>>>(b.roots, in.mesh_count,
+                                                                              b.blo, b.bhi, mlo, mhi);
+    std::vector<uint32_t> ids;
+    for (uint32_t i = 0; i < in.instance_count; ++i) {
+        uint32_t m = in.instances_host[i].mesh_index;
+        if (in.meshes_host[m].index_count / 3u > 0) ids.push_back(i);
+    }
+    uint32_t ni = (uint32_t)ids.size();
+    uint32_t* d_ids = sc.get<uint32_t>(ni);
+    tt_instance* d_inst = sc.get<tt_instance>(std::max<uint32_t>(in.instance_count, 1));
+    if (ni) {
+        check_cuda(cudaMemcpyAsync(d_ids, ids.data(), 4ull * ni, cudaMemcpyHostToDevice, stream), "ids");
+        check_cuda(cudaMemcpyAsync(d_inst, in.instances_host, sizeof(tt_instance) * in.instance_count,
+                                   cudaMemcpyHostToDevice, stream), "instances");
+    }
+    float4* ilo = sc.get<float4>(ni);
+    float4* ihi = sc.get<float4>(ni);
+    uint32_t* iseg = sc.get<uint32_t>(ni);
+    if (ni)
+        instance_prims_kernel<<<grid_for(ni, 128), 128, 0, stream>>>(d_inst, d_ids, ni, mlo, mhi,
+                                                                     ilo, ihi, iseg);
+    if (ni > 0) {
+        Build4 tb = build_bvh4(ilo, ihi, iseg, ni, 1, 1, true, d_ids, out.tlas, sc);
+        out.tlas_nodes = tb.nodes;
+        out.tlas_levels = tb.levels;
+    } else {
+        out.tlas_nodes = 0;
+        out.tlas_levels = 0;
+    }
+    check_cuda(cudaStreamSynchronize(stream), "bvh build");
+    check_cuda(cudaGetLastError(), "bvh build kernels");
+}
+
+}  // namespace tt

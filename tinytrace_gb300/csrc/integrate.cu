@@ -1,0 +1,318 @@
+// Path tracer megakernel, tonemap and parity kernels for sm_103a.
+//
+// integrate_kernel restates src/integrate/integrate.glsl:10-347 (the reference's only hot
+// kernel) over the project's BVH4 ray queries.  One thread owns one pixel and runs its
+// sample and bounce loops exactly as the reference does, so every pixel's RNG stream and
+// float operation sequence match the CPU oracle bit for bit.  Threads of a block cover a
+// 16 x 8 pixel tile (coherent primary rays); the traversal stack of each thread is a column
+// of a shared-memory array.
+#include <cuda_runtime.h>
+
+#include "tt_bsdf.cuh"
+#include "tt_bvh.cuh"
+#include "tt_kernels.h"
+
+namespace tt {
+
+constexpr float EXTENSION_TMIN = 1.0e-3f, EXTENSION_TMAX = 1000.0f;  // integrate.glsl:114-117
+constexpr float SHADOW_TMIN = 1.0e-3f, SHADOW_TMAX = 10000.0f;       // integrate.glsl:168-172
+constexpr int TILE_W = 16, TILE_H = 8, BLOCK = TILE_W * TILE_H;
+
+struct ShadeHit {
+    f3 world_position;
+    Basis tangent_space;
+    uint32_t material_index;
+};
+
+// integrate.glsl:22-110 without ray differentials (they only select texture mip levels, and
+// scenes with textures are rejected at scene creation).
+__device__ __forceinline__ ShadeHit get_ray_hit(const DevScene& sc, const Hit& h) {
+    ShadeHit hit;
+    const tt_instance* in = sc.instances + h.instance;
+    hit.material_index = __ldg(&in->material_index);
+    uint32_t index_offset = __ldg(&in->index_offset), vertex_offset = __ldg(&in->vertex_offset);
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = __ldg(&in->transform[k]);
+    uint32_t base = 3u * h.prim + index_offset;
+    f3 pos[3];
+    TangentFrame tf[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        uint32_t vi = __ldg(sc.indices + base + k) + vertex_offset;
+        const int16_t* s = sc.positions + 3ull * vi;
+        f3 p = f3{dequant_snorm16(__ldg(s + 0)), dequant_snorm16(__ldg(s + 1)), dequant_snorm16(__ldg(s + 2))};
+        pos[k] = mat43_point(m, p);
+        tf[k] = decode_tangent_frame(__ldg(&sc.vertices[vi].tangent_frame));
+    }
+    f3 bary = f3{0.0f, h.u, h.v};
+    bary.x = 1.0f - bary.y - bary.z;
+    float nt[16];
+#pragma unroll
+    for (int k = 0; k < 11; ++k) nt[k] = __ldg(&in->normal_transform[k]);
+    hit.tangent_space.normal = normalize(mat3_vec(nt, interp3(bary, tf[0].normal, tf[1].normal, tf[2].normal)));
+    hit.tangent_space.tangent = normalize(mat3_vec(nt, interp3(bary, tf[0].tangent, tf[1].tangent, tf[2].tangent)));
+    float bs = signf(tf[0].bitangent_sign * bary.x + tf[1].bitangent_sign * bary.y + tf[2].bitangent_sign * bary.z);
+    hit.tangent_space.bitangent = normalize(bs * cross(hit.tangent_space.normal, hit.tangent_space.tangent));
+    hit.world_position = bary.x * pos[0] + bary.y * pos[1] + bary.z * pos[2];
+    return hit;
+}
+
+__device__ __forceinline__ f3 material_emissive(const tt_material* mat) {
+    const MatC& m = mat->constants;
+    return col3(m.emission_color) * m.emission_luminance;
+}
+
+// integrate.glsl:195-201
+__device__ __forceinline__ Basis create_surface_basis(const Basis& ts, f3 n) {
+    Basis b;
+    b.normal = transform_to_basis(ts, n);
+    b.tangent = gram_schmidt(b.normal, ts.tangent);
+    b.bitangent = normalize(cross(b.normal, b.tangent));
+    return b;
+}
+
+// integrate.glsl:156-193 with scene.glsl:114-136
+template <bool COUNT>
+__device__ __forceinline__ f3 direct_light_contribution(const DevScene& sc, f3 position, f3 wi,
+                                                        const Basis& basis, const MatC& mat,
+                                                        const Lobes& lobes, uint32_t& g,
+                                                        uint32_t* stack, uint32_t* err,
+                                                        Counters& cnt) {
+    const tt_emissive_triangle* tri = sc.emissive + (xor_shift(g) % sc.emissive_count);
+    f2 rnd = random_vec2(g);
+    f3 bary = sample_triangle(rnd);
+    uint32_t li = __ldg(&tri->instance_index);
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = __ldg(&sc.instances[li].transform[k]);
+    f3 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        p[k] = mat43_point(m, f3{dequant_snorm16(__ldg(&tri->positions[k][0])),
+                                 dequant_snorm16(__ldg(&tri->positions[k][1])),
+                                 dequant_snorm16(__ldg(&tri->positions[k][2]))});
+    float area = fmx(0.00001f, 0.5f * length(cross(p[1] - p[0], p[2] - p[0])));
+    f3 lnormal = normalize(cross(p[1] - p[0], p[2] - p[0]));
+    f3 lpos = interp3(bary, p[0], p[1], p[2]);
+    uint32_t hash = (uint32_t)__ldg(&tri->hash);
+    float light_probability = 1.0f / (float)sc.emissive_count;
+
+    f3 to_light = lpos - position;
+    f3 wo = transform_from_basis(basis, to_light);
+    float d2 = dot(to_light, to_light);
+    f3 dir = to_light / sqrtf(d2);
+    float density = (1.0f / area) * d2 / saturate(dot(-dir, lnormal)) * light_probability;
+    Hit h = trace_closest<COUNT>(sc, position, dir, SHADOW_TMIN, SHADOW_TMAX, false, stack, BLOCK, err, cnt);
+    if (!h.hit) return splat(0.0f);
+    if (h.instance != li) return splat(0.0f);
+    uint32_t tri_index = h.prim + __ldg(&sc.instances[h.instance].index_offset) / 3u;
+    if (tri_index % 0xffffu != hash) return splat(0.0f);
+    f3 emissive = material_emissive(sc.materials + __ldg(&sc.instances[li].material_index));
+    float bd = 0.0f;
+    f3 bsdf = bsdf_evaluate(mat, lobes, wi, wo, bd);
+    return bsdf * emissive * fabsf(cos_theta(wo)) / fmx(density, PDF_EPSILON);
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant__ RenderParams p) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * BLOCK];
+    const tt_constants& c = p.c;
+    const DevScene& sc = p.sc;
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    uint32_t px = blockIdx.x * TILE_W + (threadIdx.x % TILE_W);
+    uint32_t py = blockIdx.y * TILE_H + (threadIdx.x / TILE_W);
+    Counters cnt{0u, 0u, 0u, 0u};
+    uint32_t rays = 0, hits = 0;
+    if (px < W && py < H) {
+        uint32_t* stack = s_stack + threadIdx.x;
+        uint32_t pixel_gen = jenkins_hash((px + py * W) ^ jenkins_hash(c.frame_index));
+        f3 acc = splat(0.0f);
+        f3 cam = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
+        for (uint32_t si = 0; si < c.sample_count; ++si) {
+            float ox = random_float(pixel_gen);
+            float oy = random_float(pixel_gen);
+            f2 off = f2{ox - 0.5f, oy - 0.5f};
+            f2 ndc = f2{(((float)px + off.x) / (float)W) * 2.0f - 1.0f,
+                        (((float)py + off.y) / (float)H) * 2.0f - 1.0f};
+            float4 vsp = mat4_mul(c.inverse_proj, make_float4(-ndc.x, -ndc.y, 1.0f, 1.0f));
+            float4 wd = mat4_mul(c.inverse_view, make_float4(vsp.x, vsp.y, vsp.z, 0.0f));
+            f3 ray_dir = normalize(f3{wd.x, wd.y, wd.z});
+            f3 ray_org = cam;
+            uint32_t g = pixel_gen;
+            f3 path_acc = splat(0.0f), thr = splat(1.0f);
+            for (uint32_t bounce = 0; bounce < c.bounce_count; ++bounce) {
+                if (COUNT) rays++;
+                Hit h = trace_closest<COUNT>(sc, ray_org, ray_dir, EXTENSION_TMIN, EXTENSION_TMAX, true,
+                                             stack, BLOCK, p.err, cnt);
+                if (!h.hit) {
+                    path_acc += splat(1.0f) * thr;
+                    break;
+                }
+                if (COUNT) hits++;
+                ShadeHit hit = get_ray_hit(sc, h);
+                const tt_material* material = sc.materials + hit.material_index;
+                const MatC& mc = material->constants;
+                Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
+                f3 wi = transform_from_basis(basis, -ray_dir);
+                Lobes lobes = bsdf_prepare(mc, wi, g);
+                bool nee = c.light_sampling == LIGHT_SAMPLING_NEE && sc.emissive_count > 0 &&
+                           mc.specular_roughness > 0.15f;
+                if (nee) {
+                    if (COUNT) rays++;
+                    f3 direct = direct_light_contribution<COUNT>(sc, hit.world_position, wi, basis, mc,
+                                                                 lobes, g, stack, p.err, cnt);
+                    path_acc += thr * direct;
+                }
+                if (bounce == 0 || !nee) path_acc += material_emissive(material) * thr;
+                float density = 1.0f;
+                f3 wo = splat(0.0f);
+                int lobe = 0;
+                f3 bsdf = bsdf_sample(mc, lobes, wi, g, wo, density, lobe);
+                ray_dir = transform_to_basis(basis, wo);
+                ray_org = hit.world_position;
+                thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
+            }
+            acc += path_acc;
+        }
+        acc = acc / (float)c.sample_count;
+        float4* t = p.target + (uint64_t)py * W + px;
+        if (c.accumulated_frame_count != 0) {
+            float4 prev = *t;
+            f3 pv = f3{prev.x, prev.y, prev.z};
+            acc = (pv * (float)(c.accumulated_frame_count - 1u) + acc) / (float)c.accumulated_frame_count;
+        }
+        *t = make_float4(acc.x, acc.y, acc.z, 1.0f);
+    }
+    if (COUNT) {
+        unsigned long long v[6] = {rays, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles, cnt.instances, hits};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            unsigned long long x = v[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) == 0) atomicAdd(p.counters + k, x);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- tonemap (tonemap.glsl:1-26)
+__device__ __forceinline__ f3 neutral_tonemap(f3 col) {
+    f3 y = f3{0.2126f * col.x + 0.7152f * col.y + 0.0722f * col.z,
+              -0.1146f * col.x + -0.3854f * col.y + 0.5f * col.z,
+              0.5f * col.x + -0.4542f * col.y + -0.0458f * col.z};
+    float bt = 1.0f - texp(-(sqrtf(y.y * y.y + y.z * y.z) * 2.4f));
+    float desat = fmx((bt - 0.7f) * 0.8f, 0.0f);
+    desat *= desat;
+    f3 desat_color = mix3(col, splat(y.x), desat);
+    float tm_lum = 1.0f - texp(-y.x);
+    float lum = 0.2126f * col.x + 0.7152f * col.y + 0.0722f * col.z;
+    f3 tm0 = col * fmx(0.0f, tm_lum / fmx(1e-5f, lum));
+    f3 tm1 = f3{1.0f - texp(-desat_color.x), 1.0f - texp(-desat_color.y), 1.0f - texp(-desat_color.z)};
+    return mix3(tm0, tm1, bt * bt) * 0.97f;
+}
+
+// display.glsl:6-12, headless: writes RGBA32F or RGBA8 (unorm, round to nearest).
+__global__ void tonemap_kernel(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format,
+                               void* out) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = in[i];
+    f3 col = f3{v.x, v.y, v.z};
+    if (tonemap != 0u) col = neutral_tonemap(col);
+    if (format == TT_FORMAT_RGBA32F) {
+        static_cast<float4*>(out)[i] = make_float4(col.x, col.y, col.z, 1.0f);
+    } else {
+        uint32_t r = (uint32_t)(saturate(col.x) * 255.0f + 0.5f);
+        uint32_t g = (uint32_t)(saturate(col.y) * 255.0f + 0.5f);
+        uint32_t b = (uint32_t)(saturate(col.z) * 255.0f + 0.5f);
+        static_cast<uint32_t*>(out)[i] = r | (g << 8) | (b << 16) | (255u << 24);
+    }
+}
+
+// ---------------------------------------------------------------- parity kernels
+// src/material/test.rs:67-80: bsdf_prepare with Generator(seed) then bsdf_evaluate(wi, wo).
+__global__ void bsdf_eval_kernel(const MatC* m, const float4* samples, uint32_t n, float4* results) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = samples[2 * i], b = samples[2 * i + 1];
+    uint32_t g = __float_as_uint(a.w);
+    f3 wi = f3{a.x, a.y, a.z}, wo = f3{b.x, b.y, b.z};
+    Lobes l = bsdf_prepare(*m, wi, g);
+    float pdf = 0.0f;
+    f3 r = bsdf_evaluate(*m, l, wi, wo, pdf);
+    results[2 * i] = make_float4(r.x, r.y, r.z, pdf);
+    results[2 * i + 1] = make_float4(__uint_as_float(g), l.probs[DIFFUSE], l.probs[METAL], l.probs[SPEC_BRDF]);
+}
+__global__ void bsdf_sample_kernel(const MatC* m, const float4* samples, uint32_t n, float4* results) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = samples[i];
+    uint32_t g = __float_as_uint(a.w);
+    f3 wi = f3{a.x, a.y, a.z};
+    Lobes l = bsdf_prepare(*m, wi, g);
+    f3 wo = splat(0.0f);
+    float pdf = 0.0f;
+    int lobe = 0;
+    f3 r = bsdf_sample(*m, l, wi, g, wo, pdf, lobe);
+    results[3 * i] = make_float4(r.x, r.y, r.z, pdf);
+    results[3 * i + 1] = make_float4(wo.x, wo.y, wo.z, (float)lobe);
+    results[3 * i + 2] = make_float4(__uint_as_float(g), 0.0f, 0.0f, 0.0f);
+}
+__global__ void __launch_bounds__(BLOCK) trace_kernel(DevScene sc, const float4* rays, uint32_t n,
+                                                      uint32_t flags, uint4* hits, uint32_t* err) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * BLOCK];
+    uint32_t i = blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= n) return;
+    float4 a = rays[2 * i], b = rays[2 * i + 1];
+    Counters cnt{0u, 0u, 0u, 0u};
+    Hit h = trace_closest<false>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, a.w, b.w,
+                                 (flags & TT_TRACE_CULL_BACK_FACES) != 0u, s_stack + threadIdx.x,
+                                 BLOCK, err, cnt);
+    if (h.hit) {
+        hits[2 * i] = make_uint4(1u, __float_as_uint(h.t), __float_as_uint(h.u), __float_as_uint(h.v));
+        hits[2 * i + 1] = make_uint4(h.instance, h.prim, 0u, 0u);
+    } else {
+        hits[2 * i] = make_uint4(0u, 0u, 0u, 0u);
+        hits[2 * i + 1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+__global__ void math_kernel(int which, const float* x, uint64_t n, float* y) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float v = x[i], r = 0.0f, s, c;
+    switch (which) {
+        case 0: tsincos(v, &s, &c); r = s; break;
+        case 1: tsincos(v, &s, &c); r = c; break;
+        case 2: r = texp(v); break;
+        case 3: r = tlog(v); break;
+        case 4: r = tacos(v); break;
+        default: r = 0.0f;
+    }
+    y[i] = r;
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st) {
+    dim3 grid((p.c.screen_size[0] + TILE_W - 1) / TILE_W, (p.c.screen_size[1] + TILE_H - 1) / TILE_H);
+    if (counted) integrate_kernel<true><<<grid, BLOCK, 0, st>>>(p);
+    else integrate_kernel<false><<<grid, BLOCK, 0, st>>>(p);
+}
+void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out, cudaStream_t st) {
+    if (n == 0) return;
+    tonemap_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, n, tonemap, format, out);
+}
+void launch_bsdf_eval(const MatC* m, const float4* s, uint32_t n, float4* r, cudaStream_t st) {
+    if (n) bsdf_eval_kernel<<<(n + 127) / 128, 128, 0, st>>>(m, s, n, r);
+}
+void launch_bsdf_sample(const MatC* m, const float4* s, uint32_t n, float4* r, cudaStream_t st) {
+    if (n) bsdf_sample_kernel<<<(n + 127) / 128, 128, 0, st>>>(m, s, n, r);
+}
+void launch_trace(const DevScene& sc, const float4* rays, uint32_t n, uint32_t flags, uint4* hits,
+                  uint32_t* err, cudaStream_t st) {
+    if (n) trace_kernel<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(sc, rays, n, flags, hits, err);
+}
+void launch_math(int which, const float* x, uint64_t n, float* y, cudaStream_t st) {
+    if (n) math_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(which, x, n, y);
+}
+
+}  // namespace tt

@@ -1,0 +1,59 @@
+// Host-side internals shared by the translation units of libtinytrace_cuda.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tinytrace_cuda.h"
+
+namespace tt {
+
+// Status carrying a message; thrown inside the library and converted to a return code at
+// the C ABI boundary.
+struct Error {
+    int32_t code;
+    std::string message;
+};
+[[noreturn]] void fail(int32_t code, const std::string& message);
+void check_cuda(cudaError_t e, const char* what);
+
+// A device allocation owned by a resource.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr(o.ptr), bytes(o.bytes) { o.ptr = nullptr; o.bytes = 0; }
+    DeviceBuffer& operator=(DeviceBuffer&& o) noexcept;
+    ~DeviceBuffer();
+    void alloc(size_t n);
+    template <class T>
+    T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Result of the LBVH build for one scene.
+struct BvhResult {
+    DeviceBuffer blas;   // Node4 records
+    DeviceBuffer tris;   // TriRecord records (BLAS leaf order)
+    DeviceBuffer tlas;   // Node4 records
+    uint64_t blas_nodes = 0, tlas_nodes = 0, tri_count = 0;
+    uint32_t blas_levels = 0, tlas_levels = 0;
+};
+
+struct BuildInput {
+    const int16_t* positions;     // device
+    const uint32_t* indices;      // device
+    const tt_mesh* meshes_host;   // host
+    uint32_t mesh_count;
+    const tt_instance* instances_host;  // host
+    uint32_t instance_count;
+};
+
+// Builds BLAS (one root per mesh, node index == mesh index) and TLAS (root 0) on `stream`.
+void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, BvhResult& out);
+
+}  // namespace tt

@@ -1,0 +1,207 @@
+"""Seeded synthetic scenes for tests and benchmarks, built through the asset pipeline
+(`asset.Scene.insert_mesh` / `insert_material`, i.e. snorm16 positions and packed tangent
+frames as the reference stores them).
+
+* `cornell_box()` — the procedural Cornell box: five axis-aligned wall quads and two boxes
+  (34 triangles) plus one ceiling light quad (2 triangles) of radiance 15; Lambertian
+  OpenPBR base colours red/green/white 0.7 (specular weight 0).
+* `icosphere_field()` — 64 instances of a geodesic sphere (frequency 28: 15,680 triangles)
+  with seeded fractal (sum-of-sinusoids) radial displacement of amplitude 0.1, uniform random
+  rotations, translations in a 100^3 box and scales in [4, 12]; OpenPBR metalness U{0,1} and
+  specular roughness U[0.05, 1]; 1000 emissive triangles whose power P ~ LogNormal(0, 1)
+  gives luminance 100 P / (pi A).  Light meshes come first in the index buffer so that the
+  reference's 16-bit light hash identifies them exactly.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .asset import Material, Model, Node
+from .asset import Scene as AssetScene
+from .camera import Camera
+from .renderer import Config, LightSampling
+
+
+@dataclass
+class Workload:
+    name: str
+    scene: AssetScene
+    camera: Camera
+    extent: tuple
+    config: Config
+
+
+def _quad(a, b, c, d):
+    """Two triangles (a,b,c), (a,c,d); counter-clockwise seen from the front side."""
+    pos = np.array([a, b, c, d], np.float32)
+    n = np.cross(pos[1] - pos[0], pos[2] - pos[0])
+    n = n / np.linalg.norm(n)
+    normals = np.repeat(n[None], 4, 0).astype(np.float32)
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    return pos, np.array([0, 1, 2, 0, 2, 3], np.uint32), normals, uv
+
+
+def _box(lo, hi, angle):
+    """Axis-aligned box rotated about +y by `angle`, outward faces, 12 triangles."""
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    c = (lo + hi) / 2
+    corners = np.array([[x, y, z] for z in (lo[2], hi[2]) for y in (lo[1], hi[1]) for x in (lo[0], hi[0])])
+    ca, sa = np.cos(angle), np.sin(angle)
+    rot = np.array([[ca, 0, sa], [0, 1, 0], [-sa, 0, ca]])
+    corners = (corners - c) @ rot.T + c
+    faces = [(0, 2, 3, 1), (4, 5, 7, 6), (0, 1, 5, 4), (2, 6, 7, 3), (0, 4, 6, 2), (1, 3, 7, 5)]
+    pos, idx, nrm, uv = [], [], [], []
+    for f in faces:
+        p, i, n, u = _quad(*corners[list(f)])
+        # make the quad face outward
+        if np.dot(n[0], p.mean(0) - c) < 0:
+            p, i, n, u = _quad(*corners[list(f)][::-1])
+        idx.append(i + 4 * len(pos))
+        pos.append(p)
+        nrm.append(n)
+        uv.append(u)
+    return np.concatenate(pos), np.concatenate(idx), np.concatenate(nrm), np.concatenate(uv)
+
+
+def lambertian(color) -> Material:
+    return Material(base_color=tuple(float(c) for c in color), specular_weight=0.0)
+
+
+def cornell_box(light_radiance: float = 15.0) -> AssetScene:
+    s = AssetScene()
+    white = s.insert_material(lambertian((0.7, 0.7, 0.7)))
+    red = s.insert_material(lambertian((0.7, 0.05, 0.05)))
+    green = s.insert_material(lambertian((0.05, 0.7, 0.05)))
+    light = s.insert_material(Material(base_color=(0.7, 0.7, 0.7), specular_weight=0.0,
+                                       emission_luminance=light_radiance, emission_color=(1.0, 1.0, 1.0)))
+    items = []
+    # light first: its triangles get the smallest global indices
+    items.append((_quad((-0.25, 1.98, -0.25), (-0.25, 1.98, 0.25), (0.25, 1.98, 0.25), (0.25, 1.98, -0.25)), light))
+    items.append((_quad((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)), white))       # floor, +y
+    items.append((_quad((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)), white))       # ceiling, -y
+    items.append((_quad((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)), white))     # back, +z
+    items.append((_quad((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)), red))       # left, +x
+    items.append((_quad((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)), green))         # right, -x
+    items.append((_box((-0.65, 0.0, -0.6), (-0.05, 1.2, 0.0), 0.3), white))            # tall box
+    items.append((_box((0.1, 0.0, 0.0), (0.7, 0.6, 0.6), -0.3), white))                # short box
+    for (pos, idx, nrm, uv), mat in items:
+        m = s.insert_mesh(pos, uv, idx, nrm)
+        s.root.children.append(Node(models=[Model(m, mat)]))
+    return s
+
+
+def cornell_workload(extent=(256, 256), spp: int = 16, depth: int = 4) -> Workload:
+    cam = Camera.looking_at((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), fov=0.75)
+    cfg = Config(bounce_count=depth, sample_count=spp, tonemap=True,
+                 light_sampling=LightSampling.NEXT_EVENT_ESTIMATION)
+    return Workload("cornell_box_256x256_16spp_d4", cornell_box(), cam, tuple(extent), cfg)
+
+
+# ---------------------------------------------------------------- icosphere field
+def geodesic_sphere(freq: int) -> tuple[np.ndarray, np.ndarray]:
+    """Unit geodesic sphere: each icosahedron face split into freq^2 triangles."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t],
+                  [0, 1, -t], [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    pts, tris = [], []
+    for a, b, c in faces:
+        A, B, C = v[a], v[b], v[c]
+        base = len(pts)
+        ids = {}
+        for i in range(freq + 1):
+            for j in range(freq + 1 - i):
+                p = A + (B - A) * (i / freq) + (C - A) * (j / freq)
+                ids[(i, j)] = len(pts)
+                pts.append(p)
+        for i in range(freq):
+            for j in range(freq - i):
+                tris.append((ids[(i, j)], ids[(i + 1, j)], ids[(i, j + 1)]))
+                if j < freq - i - 1:
+                    tris.append((ids[(i + 1, j)], ids[(i + 1, j + 1)], ids[(i, j + 1)]))
+        del base
+    pts = np.array(pts)
+    pts /= np.linalg.norm(pts, axis=1, keepdims=True)
+    # weld shared edge vertices
+    key = np.round(pts * 1e6).astype(np.int64)
+    _, first, inverse = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    tris = inverse.reshape(-1)[np.array(tris)]
+    pts = pts[first]
+    # outward winding
+    p0, p1, p2 = pts[tris[:, 0]], pts[tris[:, 1]], pts[tris[:, 2]]
+    flip = np.einsum("ij,ij->i", np.cross(p1 - p0, p2 - p0), p0) < 0
+    tris[flip] = tris[flip][:, ::-1]
+    return pts, tris.astype(np.uint32)
+
+
+def _fbm(p: np.ndarray, rng: np.random.Generator, octaves: int = 5) -> np.ndarray:
+    out = np.zeros(len(p))
+    amp, freq, norm = 1.0, 2.0, 0.0
+    for _ in range(octaves):
+        for _ in range(3):
+            k = rng.normal(size=3)
+            k /= np.linalg.norm(k)
+            out += amp * np.sin(freq * (p @ k) + rng.uniform(0, 2 * np.pi))
+            norm += amp
+        amp *= 0.5
+        freq *= 2.0
+    return out / norm
+
+
+def _random_rotation(rng: np.random.Generator) -> np.ndarray:
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def icosphere_field(instances: int = 64, freq: int = 28, lights: int = 1000, seed: int = 7,
+                    box: float = 100.0, displacement: float = 0.1) -> AssetScene:
+    rng = np.random.default_rng(seed)
+    s = AssetScene()
+    half = box / 2.0
+    # emissive triangles first (global triangle index < 65535)
+    for _ in range(lights):
+        power = float(rng.lognormal(0.0, 1.0))
+        size = rng.uniform(1.0, 3.0)
+        tri = rng.normal(size=(3, 3))
+        tri = tri / np.linalg.norm(tri, axis=1, keepdims=True) * size
+        area = 0.5 * np.linalg.norm(np.cross(tri[1] - tri[0], tri[2] - tri[0]))
+        lum = 100.0 * power / (np.pi * max(area, 1e-3))
+        mat = s.insert_material(Material(base_color=(0.8, 0.8, 0.8), emission_luminance=lum,
+                                         emission_color=tuple(rng.uniform(0.6, 1.0, 3))))
+        m = s.insert_mesh(tri.astype(np.float32), np.zeros((3, 2), np.float32), np.array([0, 1, 2], np.uint32))
+        t = np.eye(4)
+        t[:3, 3] = rng.uniform(-half, half, 3)
+        s.root.children.append(Node(transform=t, models=[Model(m, mat)]))
+    base_pts, tris = geodesic_sphere(freq)
+    for _ in range(instances):
+        disp = 1.0 + displacement * _fbm(base_pts, rng)
+        pts = (base_pts * disp[:, None]).astype(np.float32)
+        uv = np.stack([np.arctan2(base_pts[:, 2], base_pts[:, 0]) / (2 * np.pi) + 0.5,
+                       np.arccos(np.clip(base_pts[:, 1], -1, 1)) / np.pi], axis=1).astype(np.float32)
+        m = s.insert_mesh(pts, uv, tris)
+        mat = s.insert_material(Material(base_color=tuple(rng.uniform(0.2, 0.9, 3)),
+                                         base_metalness=float(rng.integers(0, 2)),
+                                         specular_roughness=float(rng.uniform(0.05, 1.0))))
+        t = np.eye(4)
+        t[:3, :3] = _random_rotation(rng) * rng.uniform(4.0, 12.0)
+        t[:3, 3] = rng.uniform(-half, half, 3)
+        s.root.children.append(Node(transform=t, models=[Model(m, mat)]))
+    return s
+
+
+def icosphere_workload(extent=(1920, 1080), spp: int = 64, depth: int = 8, **kw) -> Workload:
+    cam = Camera.looking_at((0.0, 10.0, 95.0), (0.0, 0.0, 0.0), fov=np.pi / 2.0)
+    cfg = Config(bounce_count=depth, sample_count=spp, tonemap=True,
+                 light_sampling=LightSampling.NEXT_EVENT_ESTIMATION)
+    name = f"icosphere_field_{kw.get('instances', 64)}x{20 * kw.get('freq', 28) ** 2}tri_{extent[0]}x{extent[1]}_{spp}spp_d{depth}"
+    return Workload(name, icosphere_field(**kw), cam, tuple(extent), cfg)
