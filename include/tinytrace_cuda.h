@@ -220,6 +220,22 @@ int32_t tt_bsdf_sample_batch(tt_context* ctx, const tt_material_constants* mater
  * instance, primitive, 0, 0).  flags: TT_TRACE_*. */
 int32_t tt_trace_batch(tt_context* ctx, tt_handle scene, const float* rays, uint32_t n,
                        uint32_t flags, uint32_t* hits);
+/* Allocation-free variant of tt_trace_batch; it has no counterpart in the reference.
+ * It is for callers that cannot allocate device memory when they issue ray queries: an
+ * application that owns the whole device-memory budget through its own pool, or a real-time
+ * frame loop in which an allocation's implicit device synchronisation would stall the frame.
+ * Rays, hits and the traversal error word are staged in one static device array of the
+ * library, sized for TT_TRACE_NOALLOC_MAX_RAYS rays (4 MiB + 256 bytes, held by every GPU
+ * that loads the library until the process exits).  Arguments and results are those of
+ * tt_trace_batch; n above TT_TRACE_NOALLOC_MAX_RAYS is rejected with TT_ERR_INVALID_ARGUMENT
+ * before any GPU work.  The first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture.  Every call shares the array and leaves its contents behind (the error word is
+ * cleared at the start of each call); calls whose GPU work overlaps (two contexts of one
+ * device) race on it.  The call synchronises the context stream before it returns. */
+#define TT_TRACE_NOALLOC_MAX_RAYS 65536u
+int32_t tt_trace_batch_noalloc(tt_context* ctx, tt_handle scene, const float* rays, uint32_t n,
+                               uint32_t flags, uint32_t* hits);
 /* Device elementary functions (0 sin, 1 cos, 2 exp, 3 log, 4 acos) for accuracy tests. */
 int32_t tt_math_batch(tt_context* ctx, int32_t which, const float* x, uint64_t n, float* y);
 

@@ -591,6 +591,16 @@ int32_t tt_trace_batch(tt_context* ctx, tt_handle scene, const float* rays, uint
     });
 }
 
+int32_t tt_trace_batch_noalloc(tt_context* ctx, tt_handle scene, const float* rays, uint32_t n, uint32_t flags,
+                               uint32_t* hits) {
+    return guarded([&] {
+        require(ctx && (n == 0 || (rays && hits)), "null argument");
+        use_device(ctx);
+        SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
+        trace_batch_noalloc(ctx->device, s->dev, rays, n, flags, hits, ctx->stream);
+    });
+}
+
 int32_t tt_math_batch(tt_context* ctx, int32_t which, const float* x, uint64_t n, float* y) {
     return guarded([&] {
         require(ctx && (n == 0 || (x && y)), "null argument");

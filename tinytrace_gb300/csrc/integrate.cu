@@ -8,8 +8,11 @@
 // of a shared-memory array.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "tt_bsdf.cuh"
 #include "tt_bvh.cuh"
+#include "tt_internal.h"
 #include "tt_kernels.h"
 
 namespace tt {
@@ -313,6 +316,56 @@ void launch_trace(const DevScene& sc, const float4* rays, uint32_t n, uint32_t f
 }
 void launch_math(int which, const float* x, uint64_t n, float* y, cudaStream_t st) {
     if (n) math_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(which, x, n, y);
+}
+
+
+// ---------------------------------------------------------------- allocation-free ray queries
+// tt_trace_batch_noalloc serves callers that cannot allocate device memory while they query
+// rays (an application owning the device-memory budget, a frame loop that must not stall on
+// an allocation's synchronisation).  Its staging lives in this file-scope array: the error
+// word in the first 256 bytes, then TT_TRACE_NOALLOC_MAX_RAYS rays (32 bytes each), then as
+// many hits (32 bytes each).  Every GPU that loads the library holds the array until exit;
+// all calls share it, so calls whose GPU work overlaps race on it.
+constexpr uint64_t NOALLOC_RAYS_OFFSET = 256;
+constexpr uint64_t NOALLOC_HITS_OFFSET = NOALLOC_RAYS_OFFSET + 32ull * TT_TRACE_NOALLOC_MAX_RAYS;
+constexpr uint64_t NOALLOC_BYTES = NOALLOC_HITS_OFFSET + 32ull * TT_TRACE_NOALLOC_MAX_RAYS;
+static __device__ __align__(256) unsigned char g_trace_scratch[NOALLOC_BYTES];
+
+// Device address of g_trace_scratch on `device`, looked up once per device with that device
+// current (in host code the symbol itself is only a host-side stand-in).
+static unsigned char* trace_scratch_address(int device) {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mutex;
+    static void* address[MAX_DEVICES] = {};
+    if (device < 0 || device >= MAX_DEVICES) fail(TT_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mutex);
+    if (!address[device]) {
+        void* p = nullptr;
+        check_cuda(cudaGetSymbolAddress(&p, g_trace_scratch), "cudaGetSymbolAddress(g_trace_scratch)");
+        address[device] = p;
+    }
+    return static_cast<unsigned char*>(address[device]);
+}
+
+void trace_batch_noalloc(int device, const DevScene& sc, const float* rays_host, uint32_t n,
+                         uint32_t flags, uint32_t* hits_host, cudaStream_t st) {
+    if (n > TT_TRACE_NOALLOC_MAX_RAYS)
+        fail(TT_ERR_INVALID_ARGUMENT, "tt_trace_batch_noalloc: n exceeds TT_TRACE_NOALLOC_MAX_RAYS (" +
+                                          std::to_string(TT_TRACE_NOALLOC_MAX_RAYS) + ")");
+    unsigned char* base = trace_scratch_address(device);
+    uint32_t* err = reinterpret_cast<uint32_t*>(base);
+    float4* rays = reinterpret_cast<float4*>(base + NOALLOC_RAYS_OFFSET);
+    uint4* hits = reinterpret_cast<uint4*>(base + NOALLOC_HITS_OFFSET);
+    check_cuda(cudaMemsetAsync(err, 0, 4, st), "clear error word");
+    if (n) check_cuda(cudaMemcpyAsync(rays, rays_host, 32ull * n, cudaMemcpyHostToDevice, st), "stage rays");
+    launch_trace(sc, rays, n, flags, hits, err, st);
+    check_cuda(cudaGetLastError(), "trace launch");
+    uint32_t err_value = 0;
+    if (n) check_cuda(cudaMemcpyAsync(hits_host, hits, 32ull * n, cudaMemcpyDeviceToHost, st), "read hits");
+    check_cuda(cudaMemcpyAsync(&err_value, err, 4, cudaMemcpyDeviceToHost, st), "read error word");
+    check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (err_value & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
+    if (err_value & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
 }
 
 }  // namespace tt

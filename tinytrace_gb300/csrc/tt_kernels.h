@@ -26,5 +26,8 @@ void launch_bsdf_sample(const tt_material_constants* m, const float4* samples, u
 void launch_trace(const DevScene& sc, const float4* rays, uint32_t n, uint32_t flags, uint4* hits,
                   uint32_t* err, cudaStream_t st);
 void launch_math(int which, const float* x, uint64_t n, float* y, cudaStream_t st);
+// Ray queries staged in the library's static device array (no device allocation).
+void trace_batch_noalloc(int device, const DevScene& sc, const float* rays_host, uint32_t n,
+                         uint32_t flags, uint32_t* hits_host, cudaStream_t st);
 
 }  // namespace tt

@@ -36,6 +36,7 @@ TT_LIFETIME_RENDERER = 4
 TT_FORMAT_RGBA32F = 0
 TT_FORMAT_RGBA8_UNORM = 1
 TT_TRACE_CULL_BACK_FACES = 1
+TT_TRACE_NOALLOC_MAX_RAYS = 65536
 
 # ---------------------------------------------------------------- byte layouts (numpy)
 MATERIAL_CONSTANT_FIELDS = [
@@ -162,6 +163,7 @@ SIGNATURES = {
     "tt_bsdf_eval_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_bsdf_sample_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_trace_batch": (_I32, [_P, _U64, _P, _U32, _U32, _P]),
+    "tt_trace_batch_noalloc": (_I32, [_P, _U64, _P, _U32, _U32, _P]),
     "tt_math_batch": (_I32, [_P, _I32, _P, _U64, _P]),
     "tt_flush_l2": (_I32, [_P]),
     "tt_event_record": (_I32, [_P, _U32]),
