@@ -51,6 +51,8 @@ def parse_args():
     p.add_argument("--lights", type=int, default=1000)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--integrator", default="wavefront", choices=["wavefront", "megakernel"])
+    p.add_argument("--slots", type=int, default=0, help="wavefront paths in flight (0 = library default)")
     return p.parse_args()
 
 
@@ -233,6 +235,9 @@ def run_ours(a, dist: Dist):
     device = dist.local_rank
     w = make_workload(a)
     r = Renderer(w.extent, device=device)
+    integ = native.TT_INTEGRATOR_WAVEFRONT if a.integrator == "wavefront" else native.TT_INTEGRATOR_MEGAKERNEL
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_INTEGRATOR, integ))
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_WAVEFRONT_SLOTS, a.slots))
     r.set_scene(w.scene)
     r.camera = w.camera
     r.set_config(w.config)
@@ -316,7 +321,7 @@ def run_ours(a, dist: Dist):
                        "resolution": [W, H], "spp": spp, "depth": w.config.bounce_count,
                        "light_sampling": "next_event_estimation",
                        "l2": "flushed before every step (512 MiB memset, inside the timed region)",
-                       "parallelism": f"replicas x{dist.world}"},
+                       "parallelism": f"replicas x{dist.world}", "integrator": a.integrator},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 368, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

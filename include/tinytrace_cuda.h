@@ -55,6 +55,13 @@ extern "C" {
 #define TT_FORMAT_RGBA32F 0
 #define TT_FORMAT_RGBA8_UNORM 1
 
+/* integrators (tt_set_option TT_OPTION_INTEGRATOR) */
+#define TT_INTEGRATOR_WAVEFRONT 0
+#define TT_INTEGRATOR_MEGAKERNEL 1
+/* context options */
+#define TT_OPTION_INTEGRATOR 1      /* TT_INTEGRATOR_*; default wavefront */
+#define TT_OPTION_WAVEFRONT_SLOTS 2 /* paths in flight of the wavefront integrator; 0 = default */
+
 /* trace flags */
 #define TT_TRACE_CULL_BACK_FACES 1u
 
@@ -202,6 +209,9 @@ int32_t tt_render_counted(tt_context* ctx, tt_handle scene, const tt_constants* 
  * buffer instead of a swapchain image; format TT_FORMAT_*. */
 int32_t tt_tonemap(tt_context* ctx, tt_handle image, const tt_constants* constants,
                    uint32_t format, void* host_out, uint64_t bytes);
+/* Integrator choice and tuning (no counterpart in the reference: it has one megakernel).
+ * Both integrators produce bit-identical images. */
+int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value);
 /* replaces: src/lib.rs:167-178 Renderer::timings */
 int32_t tt_timings_get(tt_context* ctx, tt_timings* out);
 

@@ -126,10 +126,15 @@ def test_closest_hit_matches_brute_force(gpu_context, name):
         assert hits[:, 0].sum() > len(rays) // 20
 
 
-def _render_pair(ctx, w, frames=1):
+INTEGRATORS = {"wavefront": native.TT_INTEGRATOR_WAVEFRONT, "megakernel": native.TT_INTEGRATOR_MEGAKERNEL}
+
+
+def _render_pair(ctx, w, frames=1, integrator="wavefront", slots=0):
     from tinytrace_gb300.renderer import Renderer
 
     r = Renderer(w.extent)
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_INTEGRATOR, INTEGRATORS[integrator]))
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_WAVEFRONT_SLOTS, slots))
     r.set_scene(w.scene)
     r.camera = w.camera
     r.set_config(w.config)
@@ -145,20 +150,40 @@ def _render_pair(ctx, w, frames=1):
     return gpu
 
 
-def test_render_cornell_c1(gpu_context):
-    img = _render_pair(gpu_context, scenes.cornell_workload())
+@pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
+def test_render_cornell_c1(gpu_context, integrator):
+    img = _render_pair(gpu_context, scenes.cornell_workload(), integrator=integrator)
     assert img[..., :3].mean() > 0.05
 
 
-def test_render_accumulation(gpu_context):
+@pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
+def test_render_accumulation(gpu_context, integrator):
     # frames 0 and 1 both overwrite (n = 0 and n = 1), later frames average
-    _render_pair(gpu_context, scenes.cornell_workload(extent=(48, 40), spp=1, depth=3), frames=4)
+    _render_pair(gpu_context, scenes.cornell_workload(extent=(48, 40), spp=1, depth=3), frames=4,
+                 integrator=integrator)
 
 
-def test_render_field_small(gpu_context):
+@pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
+def test_render_field_small(gpu_context, integrator):
     w = scenes.Workload("field_small", _small_field(), scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)),
                         (96, 54), scenes.Config(bounce_count=8, sample_count=3))
-    _render_pair(gpu_context, w)
+    _render_pair(gpu_context, w, integrator=integrator)
+
+
+def test_render_wavefront_small_pool_and_chunks(gpu_context):
+    # a pool much smaller than the frame (many refills) and 70 samples (two sample chunks)
+    w = scenes.Workload("cornell_pool", scenes.cornell_box(), scenes.cornell_workload().camera, (40, 24),
+                        scenes.Config(bounce_count=5, sample_count=70))
+    _render_pair(gpu_context, w, integrator="wavefront", slots=256)
+
+
+@pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
+def test_render_edge_configs(gpu_context, integrator):
+    base = scenes.cornell_workload(extent=(21, 13))
+    for cfg in (scenes.Config(bounce_count=0, sample_count=2), scenes.Config(bounce_count=1, sample_count=1),
+                scenes.Config(bounce_count=3, sample_count=2, light_sampling=scenes.LightSampling.ON_HIT)):
+        w = scenes.Workload("edge", base.scene, base.camera, base.extent, cfg)
+        _render_pair(gpu_context, w, integrator=integrator)
 
 
 def test_tonemap_bits(gpu_context):

@@ -4,6 +4,7 @@
 // thread-local message; nothing throws or aborts across the ABI.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -72,6 +73,14 @@ struct SceneRes {
     tt_scene_stats stats{};
 };
 
+// Slot pool and queues of the wavefront integrator, grown on demand and kept across frames.
+struct WavefrontBuffers {
+    DeviceBuffer org, dir, thr, acc, pa1, pa0, pe, hit, active, shadow, counters, samples, running;
+    uint32_t slots = 0;
+    uint64_t sample_items = 0;
+    uint32_t pixels = 0;
+};
+
 struct Pool {
     uint32_t epoch = 1;
     std::vector<std::unique_ptr<ImageRes>> images;
@@ -94,6 +103,9 @@ struct tt_context {
     tt::DeviceBuffer err_word, counters, l2_flush;
     uint32_t* err_host = nullptr;  // pinned
     bool err_pending = false;
+    uint32_t integrator = TT_INTEGRATOR_WAVEFRONT;
+    uint32_t wavefront_slots = 0;  // 0 = default
+    tt::WavefrontBuffers wf;
 };
 
 namespace tt {
@@ -226,6 +238,59 @@ int32_t guarded(F&& f) {
 
 using namespace tt;
 
+constexpr uint32_t WAVEFRONT_DEFAULT_SLOTS = 1u << 21;
+constexpr uint32_t WAVEFRONT_MAX_CHUNK_SPP = 64;
+
+// Sizes (growing only) the wavefront pool for this frame and returns its device pointers.
+static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
+    WavefrontBuffers& b = ctx->wf;
+    uint64_t WH = (uint64_t)c.screen_size[0] * c.screen_size[1];
+    uint32_t chunk_spp = std::min<uint32_t>(c.sample_count, WAVEFRONT_MAX_CHUNK_SPP);
+    uint64_t items = WH * chunk_spp;
+    uint32_t want = ctx->wavefront_slots ? ctx->wavefront_slots : WAVEFRONT_DEFAULT_SLOTS;
+    uint32_t slots = (uint32_t)std::min<uint64_t>(want, std::max<uint64_t>(items, 1));
+    slots = (slots + 127u) / 128u * 128u;
+    if (slots > b.slots) {
+        b.org.alloc(16ull * slots);
+        b.dir.alloc(16ull * slots);
+        b.thr.alloc(16ull * slots);
+        b.acc.alloc(16ull * slots);
+        b.pa1.alloc(16ull * slots);
+        b.pa0.alloc(16ull * slots);
+        b.pe.alloc(16ull * slots);
+        b.hit.alloc(16ull * slots);
+        b.active.alloc(4ull * slots);
+        b.shadow.alloc(32ull * slots);
+        b.slots = slots;
+    }
+    if (!b.counters.ptr) b.counters.alloc(64);
+    if (items > b.sample_items) {
+        b.samples.alloc(16ull * items);
+        b.sample_items = items;
+    }
+    if (WH > b.pixels) {
+        b.running.alloc(16ull * WH);
+        b.pixels = (uint32_t)WH;
+    }
+    WfParams w{};
+    w.org = b.org.as<float4>();
+    w.dir = b.dir.as<float4>();
+    w.thr = b.thr.as<float4>();
+    w.acc = b.acc.as<float4>();
+    w.pa1 = b.pa1.as<float4>();
+    w.pa0 = b.pa0.as<float4>();
+    w.pe = b.pe.as<float4>();
+    w.hit = b.hit.as<uint4>();
+    w.active = b.active.as<uint32_t>();
+    w.shadow = b.shadow.as<float4>();
+    w.counters = b.counters.as<uint32_t>();
+    w.samples = b.samples.as<float4>();
+    w.running = b.running.as<float4>();
+    w.P = slots;
+    w.chunk_spp = chunk_spp;
+    return w;
+}
+
 static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c, tt_handle target, bool counted,
                         tt_traversal_counters* out) {
     require(ctx && c, "null argument");
@@ -242,8 +307,12 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     p.counters = ctx->counters.as<unsigned long long>();
     arm_error_word(ctx);
     if (counted) check_cuda(cudaMemsetAsync(ctx->counters.ptr, 0, 64, ctx->stream), "memset");
+    bool wavefront = ctx->integrator == TT_INTEGRATOR_WAVEFRONT && c->sample_count > 0 && c->bounce_count > 0;
+    WfParams w{};
+    if (wavefront) w = wavefront_buffers(ctx, *c);
     check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
-    launch_integrate(p, counted, ctx->stream);
+    if (wavefront) render_wavefront(p, w, ctx->err_host + 1, counted, ctx->stream);
+    else launch_integrate(p, counted, ctx->stream);
     check_cuda(cudaGetLastError(), "integrate launch");
     check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
     ctx->integrate_timed = true;
@@ -536,6 +605,21 @@ int32_t tt_tonemap(tt_context* ctx, tt_handle image, const tt_constants* constan
         check_cuda(cudaMemcpyAsync(host_out, d, need, cudaMemcpyDeviceToHost, ctx->stream), "download");
         check_cuda(cudaFreeAsync(d, ctx->stream), "cudaFreeAsync");
         sync(ctx);
+    });
+}
+
+int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
+    return guarded([&] {
+        require(ctx, "null context");
+        if (option == TT_OPTION_INTEGRATOR) {
+            require(value == TT_INTEGRATOR_WAVEFRONT || value == TT_INTEGRATOR_MEGAKERNEL, "unknown integrator");
+            ctx->integrator = (uint32_t)value;
+        } else if (option == TT_OPTION_WAVEFRONT_SLOTS) {
+            require(value <= (1ull << 26), "wavefront slot count above 2^26");
+            ctx->wavefront_slots = (uint32_t)value;
+        } else {
+            fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
+        }
     });
 }
 

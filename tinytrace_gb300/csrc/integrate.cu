@@ -10,112 +10,13 @@
 
 #include <mutex>
 
-#include "tt_bsdf.cuh"
-#include "tt_bvh.cuh"
+#include "tt_shade.cuh"
 #include "tt_internal.h"
 #include "tt_kernels.h"
 
 namespace tt {
 
-constexpr float EXTENSION_TMIN = 1.0e-3f, EXTENSION_TMAX = 1000.0f;  // integrate.glsl:114-117
-constexpr float SHADOW_TMIN = 1.0e-3f, SHADOW_TMAX = 10000.0f;       // integrate.glsl:168-172
 constexpr int TILE_W = 16, TILE_H = 8, BLOCK = TILE_W * TILE_H;
-
-struct ShadeHit {
-    f3 world_position;
-    Basis tangent_space;
-    uint32_t material_index;
-};
-
-// integrate.glsl:22-110 without ray differentials (they only select texture mip levels, and
-// scenes with textures are rejected at scene creation).
-__device__ __forceinline__ ShadeHit get_ray_hit(const DevScene& sc, const Hit& h) {
-    ShadeHit hit;
-    const tt_instance* in = sc.instances + h.instance;
-    hit.material_index = __ldg(&in->material_index);
-    uint32_t index_offset = __ldg(&in->index_offset), vertex_offset = __ldg(&in->vertex_offset);
-    float m[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) m[k] = __ldg(&in->transform[k]);
-    uint32_t base = 3u * h.prim + index_offset;
-    f3 pos[3];
-    TangentFrame tf[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        uint32_t vi = __ldg(sc.indices + base + k) + vertex_offset;
-        const int16_t* s = sc.positions + 3ull * vi;
-        f3 p = f3{dequant_snorm16(__ldg(s + 0)), dequant_snorm16(__ldg(s + 1)), dequant_snorm16(__ldg(s + 2))};
-        pos[k] = mat43_point(m, p);
-        tf[k] = decode_tangent_frame(__ldg(&sc.vertices[vi].tangent_frame));
-    }
-    f3 bary = f3{0.0f, h.u, h.v};
-    bary.x = 1.0f - bary.y - bary.z;
-    float nt[16];
-#pragma unroll
-    for (int k = 0; k < 11; ++k) nt[k] = __ldg(&in->normal_transform[k]);
-    hit.tangent_space.normal = normalize(mat3_vec(nt, interp3(bary, tf[0].normal, tf[1].normal, tf[2].normal)));
-    hit.tangent_space.tangent = normalize(mat3_vec(nt, interp3(bary, tf[0].tangent, tf[1].tangent, tf[2].tangent)));
-    float bs = signf(tf[0].bitangent_sign * bary.x + tf[1].bitangent_sign * bary.y + tf[2].bitangent_sign * bary.z);
-    hit.tangent_space.bitangent = normalize(bs * cross(hit.tangent_space.normal, hit.tangent_space.tangent));
-    hit.world_position = bary.x * pos[0] + bary.y * pos[1] + bary.z * pos[2];
-    return hit;
-}
-
-__device__ __forceinline__ f3 material_emissive(const tt_material* mat) {
-    const MatC& m = mat->constants;
-    return col3(m.emission_color) * m.emission_luminance;
-}
-
-// integrate.glsl:195-201
-__device__ __forceinline__ Basis create_surface_basis(const Basis& ts, f3 n) {
-    Basis b;
-    b.normal = transform_to_basis(ts, n);
-    b.tangent = gram_schmidt(b.normal, ts.tangent);
-    b.bitangent = normalize(cross(b.normal, b.tangent));
-    return b;
-}
-
-// integrate.glsl:156-193 with scene.glsl:114-136
-template <bool COUNT>
-__device__ __forceinline__ f3 direct_light_contribution(const DevScene& sc, f3 position, f3 wi,
-                                                        const Basis& basis, const MatC& mat,
-                                                        const Lobes& lobes, uint32_t& g,
-                                                        uint32_t* stack, uint32_t* err,
-                                                        Counters& cnt) {
-    const tt_emissive_triangle* tri = sc.emissive + (xor_shift(g) % sc.emissive_count);
-    f2 rnd = random_vec2(g);
-    f3 bary = sample_triangle(rnd);
-    uint32_t li = __ldg(&tri->instance_index);
-    float m[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) m[k] = __ldg(&sc.instances[li].transform[k]);
-    f3 p[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        p[k] = mat43_point(m, f3{dequant_snorm16(__ldg(&tri->positions[k][0])),
-                                 dequant_snorm16(__ldg(&tri->positions[k][1])),
-                                 dequant_snorm16(__ldg(&tri->positions[k][2]))});
-    float area = fmx(0.00001f, 0.5f * length(cross(p[1] - p[0], p[2] - p[0])));
-    f3 lnormal = normalize(cross(p[1] - p[0], p[2] - p[0]));
-    f3 lpos = interp3(bary, p[0], p[1], p[2]);
-    uint32_t hash = (uint32_t)__ldg(&tri->hash);
-    float light_probability = 1.0f / (float)sc.emissive_count;
-
-    f3 to_light = lpos - position;
-    f3 wo = transform_from_basis(basis, to_light);
-    float d2 = dot(to_light, to_light);
-    f3 dir = to_light / sqrtf(d2);
-    float density = (1.0f / area) * d2 / saturate(dot(-dir, lnormal)) * light_probability;
-    Hit h = trace_closest<COUNT>(sc, position, dir, SHADOW_TMIN, SHADOW_TMAX, false, stack, BLOCK, err, cnt);
-    if (!h.hit) return splat(0.0f);
-    if (h.instance != li) return splat(0.0f);
-    uint32_t tri_index = h.prim + __ldg(&sc.instances[h.instance].index_offset) / 3u;
-    if (tri_index % 0xffffu != hash) return splat(0.0f);
-    f3 emissive = material_emissive(sc.materials + __ldg(&sc.instances[li].material_index));
-    float bd = 0.0f;
-    f3 bsdf = bsdf_evaluate(mat, lobes, wi, wo, bd);
-    return bsdf * emissive * fabsf(cos_theta(wo)) / fmx(density, PDF_EPSILON);
-}
 
 template <bool COUNT>
 __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant__ RenderParams p) {
@@ -133,14 +34,8 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
         f3 acc = splat(0.0f);
         f3 cam = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
         for (uint32_t si = 0; si < c.sample_count; ++si) {
-            float ox = random_float(pixel_gen);
-            float oy = random_float(pixel_gen);
-            f2 off = f2{ox - 0.5f, oy - 0.5f};
-            f2 ndc = f2{(((float)px + off.x) / (float)W) * 2.0f - 1.0f,
-                        (((float)py + off.y) / (float)H) * 2.0f - 1.0f};
-            float4 vsp = mat4_mul(c.inverse_proj, make_float4(-ndc.x, -ndc.y, 1.0f, 1.0f));
-            float4 wd = mat4_mul(c.inverse_view, make_float4(vsp.x, vsp.y, vsp.z, 0.0f));
-            f3 ray_dir = normalize(f3{wd.x, wd.y, wd.z});
+            f2 ndc = pixel_ndc(px, py, W, H, pixel_gen);
+            f3 ray_dir = camera_ray_direction(c, ndc);
             f3 ray_org = cam;
             uint32_t g = pixel_gen;
             f3 path_acc = splat(0.0f), thr = splat(1.0f);
@@ -153,7 +48,7 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
                     break;
                 }
                 if (COUNT) hits++;
-                ShadeHit hit = get_ray_hit(sc, h);
+                ShadeHit hit = get_ray_hit(sc, h.instance, h.prim, h.u, h.v);
                 const tt_material* material = sc.materials + hit.material_index;
                 const MatC& mc = material->constants;
                 Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
@@ -163,8 +58,11 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
                            mc.specular_roughness > 0.15f;
                 if (nee) {
                     if (COUNT) rays++;
-                    f3 direct = direct_light_contribution<COUNT>(sc, hit.world_position, wi, basis, mc,
-                                                                 lobes, g, stack, p.err, cnt);
+                    LightSample ls = sample_light(sc, hit.world_position, basis, g);
+                    Hit hs = trace_closest<COUNT>(sc, hit.world_position, ls.dir, SHADOW_TMIN, SHADOW_TMAX, false,
+                                                  stack, BLOCK, p.err, cnt);
+                    f3 direct = light_visible(sc, hs, ls.instance, ls.hash) ? light_contribution(sc, ls, mc, lobes, wi)
+                                                                           : splat(0.0f);
                     path_acc += thr * direct;
                 }
                 if (bounce == 0 || !nee) path_acc += material_emissive(material) * thr;

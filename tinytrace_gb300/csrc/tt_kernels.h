@@ -16,6 +16,21 @@ struct RenderParams {
     unsigned long long* counters;  // 6 counters, instrumented kernel only
 };
 
+// Wavefront integrator (wavefront.cu): device pointers of the slot pool and queues.
+struct WfParams {
+    float4 *org, *dir, *thr, *acc, *pa1, *pa0, *pe;
+    uint4* hit;
+    uint32_t* active;
+    float4* shadow;
+    uint32_t* counters;  // [0] next work item, [1] active paths, [2] shadow rays
+    float4* samples;     // chunk_spp x WH per-sample radiance (band order)
+    float4* running;     // WH running per-pixel sums across chunks
+    uint32_t P, WH;
+    uint32_t chunk_sample0, chunk_spp, chunk_items;
+};
+// Renders with the wavefront integrator; w.chunk_spp is the largest chunk of samples the
+// buffers hold.  Synchronises `st` once per iteration to read the active-path count.
+void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st);
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st);
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out,
                     cudaStream_t st);

@@ -1,0 +1,141 @@
+// Shading pieces of src/integrate/integrate.glsl shared by the megakernel and the wavefront
+// integrator: camera rays, hit reconstruction, emission, the shading basis and emissive-
+// triangle sampling for next-event estimation.  Both integrators call these functions, so a
+// path performs the same operations in the same order whichever integrator runs it.
+#pragma once
+
+#include "tt_bsdf.cuh"
+#include "tt_bvh.cuh"
+
+namespace tt {
+
+constexpr float EXTENSION_TMIN = 1.0e-3f, EXTENSION_TMAX = 1000.0f;  // integrate.glsl:114-117
+constexpr float SHADOW_TMIN = 1.0e-3f, SHADOW_TMAX = 10000.0f;       // integrate.glsl:168-172
+
+// integrate.glsl:129-132 (the two draws come from the pixel generator)
+TT_HD f2 pixel_ndc(uint32_t px, uint32_t py, uint32_t W, uint32_t H, uint32_t& pixel_gen) {
+    float ox = random_float(pixel_gen);
+    float oy = random_float(pixel_gen);
+    f2 off = f2{ox - 0.5f, oy - 0.5f};
+    return f2{(((float)px + off.x) / (float)W) * 2.0f - 1.0f, (((float)py + off.y) / (float)H) * 2.0f - 1.0f};
+}
+
+// integrate.glsl:17-20
+TT_HD f3 camera_ray_direction(const tt_constants& c, f2 ndc) {
+    float4 vsp = mat4_mul(c.inverse_proj, make_float4(-ndc.x, -ndc.y, 1.0f, 1.0f));
+    float4 wd = mat4_mul(c.inverse_view, make_float4(vsp.x, vsp.y, vsp.z, 0.0f));
+    return normalize(f3{wd.x, wd.y, wd.z});
+}
+
+struct ShadeHit {
+    f3 world_position;
+    Basis tangent_space;
+    uint32_t material_index;
+};
+
+// integrate.glsl:22-110 without ray differentials (they only select texture mip levels, and
+// scenes with textures are rejected at scene creation).
+__device__ __forceinline__ ShadeHit get_ray_hit(const DevScene& sc, uint32_t instance, uint32_t prim, float u,
+                                                float v) {
+    ShadeHit hit;
+    const tt_instance* in = sc.instances + instance;
+    hit.material_index = __ldg(&in->material_index);
+    uint32_t index_offset = __ldg(&in->index_offset), vertex_offset = __ldg(&in->vertex_offset);
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = __ldg(&in->transform[k]);
+    uint32_t base = 3u * prim + index_offset;
+    f3 pos[3];
+    TangentFrame tf[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        uint32_t vi = __ldg(sc.indices + base + k) + vertex_offset;
+        const int16_t* s = sc.positions + 3ull * vi;
+        f3 p = f3{dequant_snorm16(__ldg(s + 0)), dequant_snorm16(__ldg(s + 1)), dequant_snorm16(__ldg(s + 2))};
+        pos[k] = mat43_point(m, p);
+        tf[k] = decode_tangent_frame(__ldg(&sc.vertices[vi].tangent_frame));
+    }
+    f3 bary = f3{0.0f, u, v};
+    bary.x = 1.0f - bary.y - bary.z;
+    float nt[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) nt[k] = k < 11 ? __ldg(&in->normal_transform[k]) : 0.0f;
+    hit.tangent_space.normal = normalize(mat3_vec(nt, interp3(bary, tf[0].normal, tf[1].normal, tf[2].normal)));
+    hit.tangent_space.tangent = normalize(mat3_vec(nt, interp3(bary, tf[0].tangent, tf[1].tangent, tf[2].tangent)));
+    float bs = signf(tf[0].bitangent_sign * bary.x + tf[1].bitangent_sign * bary.y + tf[2].bitangent_sign * bary.z);
+    hit.tangent_space.bitangent = normalize(bs * cross(hit.tangent_space.normal, hit.tangent_space.tangent));
+    hit.world_position = bary.x * pos[0] + bary.y * pos[1] + bary.z * pos[2];
+    return hit;
+}
+
+// integrate.glsl:148-154 (constant materials)
+__device__ __forceinline__ f3 material_emissive(const tt_material* mat) {
+    const MatC& m = mat->constants;
+    return col3(m.emission_color) * m.emission_luminance;
+}
+
+// integrate.glsl:195-201
+__device__ __forceinline__ Basis create_surface_basis(const Basis& ts, f3 n) {
+    Basis b;
+    b.normal = transform_to_basis(ts, n);
+    b.tangent = gram_schmidt(b.normal, ts.tangent);
+    b.bitangent = normalize(cross(b.normal, b.tangent));
+    return b;
+}
+
+// scene.glsl:114-136 followed by the geometry part of integrate.glsl:160-167: the light
+// sample, the shadow ray towards it and the solid-angle density.
+struct LightSample {
+    f3 wo;          // direction to the light in the shading basis
+    f3 dir;         // world-space shadow ray direction
+    float density;  // solid-angle density times the light selection probability
+    uint32_t instance, hash;
+};
+__device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 position, const Basis& basis,
+                                                    uint32_t& g) {
+    const tt_emissive_triangle* tri = sc.emissive + (xor_shift(g) % sc.emissive_count);
+    f2 rnd = random_vec2(g);
+    f3 bary = sample_triangle(rnd);
+    LightSample ls;
+    ls.instance = __ldg(&tri->instance_index);
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = __ldg(&sc.instances[ls.instance].transform[k]);
+    f3 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        p[k] = mat43_point(m, f3{dequant_snorm16(__ldg(&tri->positions[k][0])),
+                                 dequant_snorm16(__ldg(&tri->positions[k][1])),
+                                 dequant_snorm16(__ldg(&tri->positions[k][2]))});
+    float area = fmx(0.00001f, 0.5f * length(cross(p[1] - p[0], p[2] - p[0])));
+    f3 lnormal = normalize(cross(p[1] - p[0], p[2] - p[0]));
+    f3 lpos = interp3(bary, p[0], p[1], p[2]);
+    ls.hash = (uint32_t)__ldg(&tri->hash);
+    float light_probability = 1.0f / (float)sc.emissive_count;
+    f3 to_light = lpos - position;
+    ls.wo = transform_from_basis(basis, to_light);
+    float d2 = dot(to_light, to_light);
+    ls.dir = to_light / sqrtf(d2);
+    ls.density = (1.0f / area) * d2 / saturate(dot(-ls.dir, lnormal)) * light_probability;
+    return ls;
+}
+
+// The contribution of integrate.glsl:186-192 when the light is visible.
+__device__ __forceinline__ f3 light_contribution(const DevScene& sc, const LightSample& ls, const MatC& mat,
+                                                 const Lobes& lobes, f3 wi) {
+    f3 emissive = material_emissive(sc.materials + __ldg(&sc.instances[ls.instance].material_index));
+    float bd = 0.0f;
+    f3 bsdf = bsdf_evaluate(mat, lobes, wi, ls.wo, bd);
+    return bsdf * emissive * fabsf(cos_theta(ls.wo)) / fmx(ls.density, PDF_EPSILON);
+}
+
+// integrate.glsl:175-185: the closest shadow hit must be the sampled light triangle.
+__device__ __forceinline__ bool light_visible(const DevScene& sc, const Hit& h, uint32_t light_instance,
+                                              uint32_t hash) {
+    if (!h.hit) return false;
+    if (h.instance != light_instance) return false;
+    uint32_t tri_index = h.prim + __ldg(&sc.instances[h.instance].index_offset) / 3u;
+    return tri_index % 0xffffu == hash;
+}
+
+}  // namespace tt

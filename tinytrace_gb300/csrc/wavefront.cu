@@ -1,0 +1,281 @@
+// Wavefront path tracer for sm_103a: the same per-path computation as integrate_kernel
+// (src/integrate/integrate.glsl), reorganised into stages over compacted queues so that the
+// SIMT lanes of a warp always work on live paths.
+//
+// Work items are (pixel, sample) pairs.  A pool of P path slots holds paths in flight; each
+// iteration runs
+//   regen  (all slots): write finished paths' radiance to the per-sample buffer, give free
+//                       slots the next work items (camera ray: the pixel generator advanced by
+//                       2 draws per earlier sample, then the two jitter draws), and append the
+//                       live slots to the active queue;
+//   extend (active):    closest hit, back faces culled;
+//   shade  (active):    hit reconstruction, bsdf_prepare, next-event estimation (light sample
+//                       and its unoccluded contribution; the shadow ray goes to a queue),
+//                       emission, bsdf_sample and the throughput update;
+//   shadow (queue):     closest hit, light visibility, then the pending additions in the
+//                       reference's order (direct light, then bounce-0 emission).
+// A reduction sums each pixel's samples in sample order and applies the frame accumulation,
+// so the image is bit-identical to the megakernel's and to the CPU oracle's.
+//
+// Slot state in HBM (structure of arrays, 16-byte records): origin + bounce, direction +
+// generator, throughput + work item, path radiance + flags; pending NEE additions (3 x 16 B);
+// hit record (16 B, by queue position); shadow queue entries (32 B).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "tt_internal.h"
+#include "tt_kernels.h"
+#include "tt_shade.cuh"
+
+namespace tt {
+
+constexpr uint32_t F_LIVE = 1u, F_TERM = 2u;
+constexpr uint32_t NO_HIT = 0xffffffffu;
+constexpr int WF_BLOCK = 128;
+
+__device__ __forceinline__ uint32_t lane_mask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+// Warp-aggregated append: every lane of the warp must call it; lanes with `pred` get
+// consecutive positions from one atomicAdd on `counter`.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0u) return 0u;
+    int leader = __ffs(mask) - 1;
+    uint32_t base = 0u;
+    if ((int)(threadIdx.x & 31u) == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + (uint32_t)__popc(mask & lane_mask_lt());
+}
+
+// Pixel of band-ordered index t: bands of 8 rows, column-major inside a band, so a warp's 32
+// consecutive items cover a 4 x 8 pixel block (coherent camera rays).
+__device__ __forceinline__ void band_pixel(uint32_t t, uint32_t W, uint32_t H, uint32_t& x, uint32_t& y) {
+    uint32_t band = t / (8u * W);
+    uint32_t j = t - band * 8u * W;
+    uint32_t rows = min(8u, H - 8u * band);
+    x = j / rows;
+    y = 8u * band + j % rows;
+}
+
+__device__ __forceinline__ f3 xyz(float4 v) { return f3{v.x, v.y, v.z}; }
+__device__ __forceinline__ float4 pack(f3 v, uint32_t w) { return make_float4(v.x, v.y, v.z, __uint_as_float(w)); }
+
+__global__ void __launch_bounds__(WF_BLOCK) wf_regen_kernel(const __grid_constant__ RenderParams p,
+                                                            const __grid_constant__ WfParams w) {
+    uint32_t s = blockIdx.x * WF_BLOCK + threadIdx.x;
+    bool valid = s < w.P;
+    float4 a = valid ? w.acc[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t flags = __float_as_uint(a.w);
+    if (valid && (flags & F_TERM)) {
+        uint32_t item = __float_as_uint(w.thr[s].w);
+        w.samples[item] = make_float4(a.x, a.y, a.z, 0.0f);
+        flags = 0u;
+        w.acc[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    bool live = valid && (flags & F_LIVE);
+    bool need = valid && !live && *(volatile uint32_t*)&w.counters[0] < w.chunk_items;
+    uint32_t item = warp_append(&w.counters[0], need);
+    if (need && item < w.chunk_items) {
+        const tt_constants& c = p.c;
+        uint32_t W = c.screen_size[0], H = c.screen_size[1];
+        uint32_t s_local = item / w.WH, t = item - s_local * w.WH;
+        uint32_t x, y;
+        band_pixel(t, W, H, x, y);
+        uint32_t sample = w.chunk_sample0 + s_local;
+        uint32_t pg = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
+        for (uint32_t k = 0; k < 2u * sample; ++k) xor_shift(pg);
+        f2 ndc = pixel_ndc(x, y, W, H, pg);
+        f3 d = camera_ray_direction(c, ndc);
+        w.org[s] = make_float4(c.camera_position[0], c.camera_position[1], c.camera_position[2], __uint_as_float(0u));
+        w.dir[s] = pack(d, pg);
+        w.thr[s] = pack(splat(1.0f), item);
+        w.acc[s] = pack(splat(0.0f), F_LIVE);
+        live = true;
+    }
+    uint32_t q = warp_append(&w.counters[1], live);
+    if (live) w.active[q] = s;
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(WF_BLOCK) wf_extend_kernel(const __grid_constant__ RenderParams p,
+                                                             const __grid_constant__ WfParams w) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * WF_BLOCK];
+    uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
+    uint32_t n = w.counters[1];
+    Counters cnt{0u, 0u, 0u, 0u};
+    uint32_t hit = 0;
+    if (q < n) {
+        uint32_t s = w.active[q];
+        float4 o = w.org[s], d = w.dir[s];
+        Hit h = trace_closest<COUNT>(p.sc, xyz(o), xyz(d), EXTENSION_TMIN, EXTENSION_TMAX, true,
+                                     s_stack + threadIdx.x, WF_BLOCK, p.err, cnt);
+        w.hit[q] = h.hit ? make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim)
+                         : make_uint4(0u, 0u, NO_HIT, 0u);
+        hit = h.hit ? 1u : 0u;
+    }
+    if (COUNT) {
+        unsigned long long v[6] = {q < n ? 1ull : 0ull, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles,
+                                   cnt.instances, hit};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            unsigned long long x = v[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) == 0 && x) atomicAdd(p.counters + k, x);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(WF_BLOCK) wf_shade_kernel(const __grid_constant__ RenderParams p,
+                                                            const __grid_constant__ WfParams w) {
+    uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
+    uint32_t n = w.counters[1];
+    bool want_shadow = false;
+    uint32_t s = 0, light = 0;
+    f3 sh_org = splat(0.0f), sh_dir = splat(0.0f);
+    if (q < n) {
+        const tt_constants& c = p.c;
+        const DevScene& sc = p.sc;
+        s = w.active[q];
+        uint4 hv = w.hit[q];
+        float4 o4 = w.org[s], d4 = w.dir[s], t4 = w.thr[s], a4 = w.acc[s];
+        f3 thr = xyz(t4), acc = xyz(a4), ray_dir = xyz(d4);
+        uint32_t g = __float_as_uint(d4.w), bounce = __float_as_uint(o4.w);
+        if (hv.z == NO_HIT) {
+            acc += splat(1.0f) * thr;
+            w.acc[s] = pack(acc, F_TERM);
+        } else {
+            ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
+            const tt_material* material = sc.materials + hit.material_index;
+            const MatC& mc = material->constants;
+            Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
+            f3 wi = transform_from_basis(basis, -ray_dir);
+            Lobes lobes = bsdf_prepare(mc, wi, g);
+            bool nee = c.light_sampling == LIGHT_SAMPLING_NEE && sc.emissive_count > 0 && mc.specular_roughness > 0.15f;
+            f3 em = material_emissive(material);
+            if (nee) {
+                LightSample ls = sample_light(sc, hit.world_position, basis, g);
+                f3 contrib = light_contribution(sc, ls, mc, lobes, wi);
+                uint32_t pflags = (bounce == 0u ? 1u : 0u) | (ls.hash << 16);
+                w.pa1[s] = pack(thr * contrib, pflags);
+                w.pa0[s] = pack(thr * splat(0.0f), 0u);
+                w.pe[s] = pack(em * thr, 0u);
+                want_shadow = true;
+                light = ls.instance;
+                sh_org = hit.world_position;
+                sh_dir = ls.dir;
+            } else {
+                acc += em * thr;
+            }
+            float density = 1.0f;
+            f3 wo = splat(0.0f);
+            int lobe = 0;
+            f3 bsdf = bsdf_sample(mc, lobes, wi, g, wo, density, lobe);
+            f3 new_dir = transform_to_basis(basis, wo);
+            thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
+            uint32_t next = bounce + 1u;
+            uint32_t flags = next == c.bounce_count ? F_TERM : F_LIVE;
+            w.org[s] = pack(hit.world_position, next);
+            w.dir[s] = pack(new_dir, g);
+            w.thr[s] = pack(thr, __float_as_uint(t4.w));
+            w.acc[s] = pack(acc, flags);
+        }
+    }
+    uint32_t e = warp_append(&w.counters[2], want_shadow);
+    if (want_shadow) {
+        w.shadow[2ull * e] = pack(sh_org, s);
+        w.shadow[2ull * e + 1] = pack(sh_dir, light);
+    }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(WF_BLOCK) wf_shadow_kernel(const __grid_constant__ RenderParams p,
+                                                             const __grid_constant__ WfParams w) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * WF_BLOCK];
+    uint32_t e = blockIdx.x * WF_BLOCK + threadIdx.x;
+    uint32_t n = w.counters[2];
+    Counters cnt{0u, 0u, 0u, 0u};
+    if (e < n) {
+        float4 o = w.shadow[2ull * e], d = w.shadow[2ull * e + 1];
+        uint32_t s = __float_as_uint(o.w), light = __float_as_uint(d.w);
+        Hit h = trace_closest<COUNT>(p.sc, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX, false,
+                                     s_stack + threadIdx.x, WF_BLOCK, p.err, cnt);
+        float4 a1 = w.pa1[s];
+        uint32_t pflags = __float_as_uint(a1.w);
+        bool vis = light_visible(p.sc, h, light, pflags >> 16);
+        float4 a4 = w.acc[s];
+        f3 acc = xyz(a4);
+        acc += vis ? xyz(a1) : xyz(w.pa0[s]);
+        if (pflags & 1u) acc += xyz(w.pe[s]);
+        w.acc[s] = make_float4(acc.x, acc.y, acc.z, a4.w);
+    }
+    if (COUNT) {
+        unsigned long long v[5] = {e < n ? 1ull : 0ull, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles, cnt.instances};
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            unsigned long long x = v[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) == 0 && x) atomicAdd(p.counters + k, x);
+        }
+    }
+}
+
+// Per pixel: samples of this chunk added in sample order to the running sum; after the last
+// chunk, divide by the sample count and apply the frame accumulation (integrate.glsl:338-346).
+__global__ void wf_reduce_kernel(const __grid_constant__ RenderParams p, const __grid_constant__ WfParams w,
+                                 int last) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= w.WH) return;
+    const tt_constants& c = p.c;
+    f3 acc = w.chunk_sample0 == 0u ? splat(0.0f) : xyz(w.running[t]);
+    for (uint32_t sl = 0; sl < w.chunk_spp; ++sl) acc += xyz(w.samples[(uint64_t)sl * w.WH + t]);
+    if (!last) {
+        w.running[t] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+        return;
+    }
+    uint32_t x, y;
+    band_pixel(t, c.screen_size[0], c.screen_size[1], x, y);
+    acc = acc / (float)c.sample_count;
+    float4* tp = p.target + (uint64_t)y * c.screen_size[0] + x;
+    if (c.accumulated_frame_count != 0) {
+        float4 prev = *tp;
+        acc = (xyz(prev) * (float)(c.accumulated_frame_count - 1u) + acc) / (float)c.accumulated_frame_count;
+    }
+    *tp = make_float4(acc.x, acc.y, acc.z, 1.0f);
+}
+
+void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st) {
+    const tt_constants& c = p.c;
+    uint32_t WH = c.screen_size[0] * c.screen_size[1];
+    uint32_t spp = c.sample_count;
+    uint32_t max_chunk = w.chunk_spp;
+    w.WH = WH;
+    unsigned regen_grid = (w.P + WF_BLOCK - 1) / WF_BLOCK;
+    check_cuda(cudaMemsetAsync(w.acc, 0, 16ull * w.P, st), "memset");  // every slot starts free
+    for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
+        w.chunk_sample0 = s0;
+        w.chunk_spp = std::min(max_chunk, spp - s0);
+        w.chunk_items = WH * w.chunk_spp;
+        check_cuda(cudaMemsetAsync(w.counters, 0, 16, st), "memset");
+        while (true) {
+            check_cuda(cudaMemsetAsync(w.counters + 1, 0, 8, st), "memset");
+            wf_regen_kernel<<<regen_grid, WF_BLOCK, 0, st>>>(p, w);
+            check_cuda(cudaMemcpyAsync(host_count, w.counters + 1, 4, cudaMemcpyDeviceToHost, st), "count");
+            check_cuda(cudaStreamSynchronize(st), "sync");
+            uint32_t n = *host_count;
+            if (n == 0) break;
+            unsigned grid = (n + WF_BLOCK - 1) / WF_BLOCK;
+            if (counted) wf_extend_kernel<true><<<grid, WF_BLOCK, 0, st>>>(p, w);
+            else wf_extend_kernel<false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+            wf_shade_kernel<<<grid, WF_BLOCK, 0, st>>>(p, w);
+            if (counted) wf_shadow_kernel<true><<<grid, WF_BLOCK, 0, st>>>(p, w);
+            else wf_shadow_kernel<false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+        }
+        wf_reduce_kernel<<<(WH + 255) / 256, 256, 0, st>>>(p, w, s0 + w.chunk_spp >= spp ? 1 : 0);
+    }
+}
+
+}  // namespace tt

@@ -37,6 +37,10 @@ TT_FORMAT_RGBA32F = 0
 TT_FORMAT_RGBA8_UNORM = 1
 TT_TRACE_CULL_BACK_FACES = 1
 TT_TRACE_NOALLOC_MAX_RAYS = 65536
+TT_INTEGRATOR_WAVEFRONT = 0
+TT_INTEGRATOR_MEGAKERNEL = 1
+TT_OPTION_INTEGRATOR = 1
+TT_OPTION_WAVEFRONT_SLOTS = 2
 
 # ---------------------------------------------------------------- byte layouts (numpy)
 MATERIAL_CONSTANT_FIELDS = [
@@ -159,6 +163,7 @@ SIGNATURES = {
     "tt_render": (_I32, [_P, _U64, _P, _U64]),
     "tt_render_counted": (_I32, [_P, _U64, _P, _U64, ctypes.POINTER(TraversalCounters)]),
     "tt_tonemap": (_I32, [_P, _U64, _P, _U32, _P, _U64]),
+    "tt_set_option": (_I32, [_P, _U32, _U64]),
     "tt_timings_get": (_I32, [_P, ctypes.POINTER(Timings)]),
     "tt_bsdf_eval_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_bsdf_sample_batch": (_I32, [_P, _P, _P, _U32, _P]),
