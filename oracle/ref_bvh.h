@@ -50,17 +50,16 @@ inline float aabb_half_area(const Aabb& a) {
     return e.x * e.y + e.y * e.z + e.z * e.x;
 }
 
-// ---------------------------------------------------------------- BVH4 node (64 bytes)
+// ---------------------------------------------------------------- BVH4 node (128 bytes)
+// Child boxes as float planes: box[2a][c] = low bound of child c on axis a, box[2a+1][c] the
+// high bound (empty slots: +inf / -inf); then the four child references and the child count.
 struct Node4 {
-    float origin[3];
-    uint8_t exp[3];  // biased exponent of the per-axis scale 2^(exp-127)
-    uint8_t count;   // number of children (0..4)
+    float box[6][4];
     uint32_t child[4];
-    uint8_t qlo[3][4];
-    uint8_t qhi[3][4];
-    uint32_t pad[2];
+    uint32_t count;
+    uint32_t pad[3];
 };
-static_assert(sizeof(Node4) == 64, "Node4 is 64 bytes");
+static_assert(sizeof(Node4) == 128, "Node4 is 128 bytes");
 constexpr uint32_t CHILD_LEAF = 0x80000000u;
 inline uint32_t leaf_ref(uint32_t first, uint32_t count) {
     return CHILD_LEAF | ((count - 1u) << 27) | first;
@@ -126,37 +125,17 @@ inline int karras_delta(const std::vector<uint64_t>& k, int n, int i, int j) {
     return 64 + clz32((uint32_t)i ^ (uint32_t)j);
 }
 
-// Quantise the children of a node (the node box is the union of the child boxes).
-inline void quantize_node(Node4& nd, const Aabb& pbox, const Aabb* cbox, int count) {
-    const float* pmin = &pbox.lo.x;
-    const float* pmax = &pbox.hi.x;
-    for (int a = 0; a < 3; ++a) {
-        double ext = (double)pmax[a] - (double)pmin[a];
-        int e = -126;
-        if (ext > 0.0) {
-            int ex;
-            std::frexp(ext / 255.0, &ex);
-            e = ex < -126 ? -126 : (ex > 127 ? 127 : ex);
-        }
-        double scale = std::ldexp(1.0, e);
-        nd.origin[a] = pmin[a];
-        nd.exp[a] = (uint8_t)(e + 127);
-        for (int c = 0; c < 4; ++c) {
-            if (c < count) {
-                const float* cmin = &cbox[c].lo.x;
-                const float* cmax = &cbox[c].hi.x;
-                double lo = std::floor(((double)cmin[a] - (double)pmin[a]) / scale);
-                double hi = std::ceil(((double)cmax[a] - (double)pmin[a]) / scale);
-                lo = lo < 0.0 ? 0.0 : (lo > 255.0 ? 255.0 : lo);
-                hi = hi < 0.0 ? 0.0 : (hi > 255.0 ? 255.0 : hi);
-                nd.qlo[a][c] = (uint8_t)lo;
-                nd.qhi[a][c] = (uint8_t)hi;
-            } else {
-                nd.qlo[a][c] = 255;
-                nd.qhi[a][c] = 0;
-            }
+// Child boxes of a node (empty slots get +inf / -inf so that no ray enters them).
+inline void fill_node(Node4& nd, const Aabb* cbox, int count) {
+    for (int c = 0; c < 4; ++c) {
+        const float* lo = &cbox[c].lo.x;
+        const float* hi = &cbox[c].hi.x;
+        for (int a = 0; a < 3; ++a) {
+            nd.box[2 * a][c] = c < count ? lo[a] : INFINITY;
+            nd.box[2 * a + 1][c] = c < count ? hi[a] : -INFINITY;
         }
     }
+    nd.count = (uint32_t)count;
 }
 
 // Build BVH4s over primitives grouped in segments (one BVH root per segment, node index =
@@ -298,7 +277,6 @@ inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<
                     cnt++;
                 }
             }
-            nd.count = (uint8_t)cnt;
             Aabb cbx[4];
             for (int c = 0; c < cnt; ++c) {
                 int v = ch[c];
@@ -313,8 +291,7 @@ inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<
                 }
             }
             for (int c = cnt; c < 4; ++c) nd.child[c] = 0xffffffffu;
-            Aabb pb = cnt > 0 ? nbox(r) : Aabb{splat3(0.0f), splat3(0.0f)};
-            quantize_node(nd, pb, cbx, cnt);
+            fill_node(nd, cbx, cnt);
         }
         level.swap(next);
     }
@@ -442,39 +419,46 @@ inline Hit trace_brute(const Geometry& g, v3 o, v3 d, float tmin, float tmax, bo
     return best;
 }
 
-// Conservative slab test of one quantised node against a ray; writes entry distances and
-// returns a child mask.  Bounds are widened by 2^-20 of the terms' magnitudes so that float
-// rounding never culls a box the ray enters.
+// Conservative slab test of one node against a ray.  Per axis, the near plane is the low
+// bound when the inverse direction is non-negative and the high bound otherwise; entry and exit
+// distances are widened by E = 2^-20 (B + |o|) |1/d|, where B bounds the box coordinates, which
+// exceeds the rounding error of fma(plane, 1/d, -o/d), so float rounding never culls a box the
+// ray enters.
 struct NodeRay {
     v3 o, inv;
+    float nob_near[3], nob_far[3];
+    int near[3];
 };
 inline float safe_inv(float d) {
     float a = std::fabs(d) < 1e-20f ? (d < 0.0f ? -1e-20f : 1e-20f) : d;
     return 1.0f / a;
 }
-inline int node_hits(const Node4& nd, const NodeRay& r, float tmin, float tbest, float* tnear) {
-    float A[3], Blo[3], Bhi[3];
-    const float o[3] = {r.o.x, r.o.y, r.o.z};
-    const float inv[3] = {r.inv.x, r.inv.y, r.inv.z};
+inline NodeRay node_ray(v3 o, v3 d, float bound) {
+    NodeRay r;
+    r.o = o;
+    r.inv = v3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+    const float oa[3] = {o.x, o.y, o.z}, ia[3] = {r.inv.x, r.inv.y, r.inv.z};
     for (int a = 0; a < 3; ++a) {
-        float scale = bitsf((uint32_t)nd.exp[a] << 23);
-        A[a] = scale * inv[a];
-        float B = (nd.origin[a] - o[a]) * inv[a];
-        float M = std::fmaf(256.0f, std::fabs(A[a]), std::fabs(B)) * 9.5367431640625e-07f;
-        float s = inv[a] >= 0.0f ? M : -M;
-        Blo[a] = B - s;
-        Bhi[a] = B + s;
+        float nob = -(oa[a] * ia[a]);
+        float E = (bound + std::fabs(oa[a])) * std::fabs(ia[a]) * 9.5367431640625e-07f;
+        r.nob_near[a] = nob - E;
+        r.nob_far[a] = nob + E;
+        r.near[a] = ia[a] >= 0.0f ? 0 : 1;
     }
+    return r;
+}
+inline int node_hits(const Node4& nd, const NodeRay& r, float tmin, float tbest, float* tnear) {
+    const float ia[3] = {r.inv.x, r.inv.y, r.inv.z};
     int mask = 0;
-    for (int c = 0; c < nd.count; ++c) {
+    for (int c = 0; c < 4; ++c) {
         float tn = tmin, tf = tbest;
         for (int a = 0; a < 3; ++a) {
-            float t0 = std::fmaf((float)nd.qlo[a][c], A[a], Blo[a]);
-            float t1 = std::fmaf((float)nd.qhi[a][c], A[a], Bhi[a]);
-            tn = fmx(tn, fmn(t0, t1));
-            tf = fmn(tf, fmx(t0, t1));
+            float t0 = std::fmaf(nd.box[2 * a + r.near[a]][c], ia[a], r.nob_near[a]);
+            float t1 = std::fmaf(nd.box[2 * a + 1 - r.near[a]][c], ia[a], r.nob_far[a]);
+            tn = fmx(tn, t0);
+            tf = fmn(tf, t1);
         }
-        if (tn <= tf) {
+        if (c < (int)nd.count && tn <= tf) {
             mask |= 1 << c;
             tnear[c] = tn;
         }
@@ -487,6 +471,7 @@ struct SceneBvh {
     std::vector<TriRecord> tris;
     std::vector<Node4> tlas;   // root = 0
     int blas_levels = 0, tlas_levels = 0;
+    float tlas_bound = 0.0f;   // max |coordinate| of the instance world boxes
 };
 
 // BLAS over all meshes (segment = mesh) and TLAS over instances (leaf = instance index).
@@ -542,6 +527,11 @@ inline SceneBvh build_scene_bvh(const Geometry& g, int leaf_max) {
         iseg.push_back(0);
         ids.push_back(i);
     }
+    for (const Aabb& b : ibox) {
+        const float* lo = &b.lo.x;
+        const float* hi = &b.hi.x;
+        for (int a = 0; a < 3; ++a) s.tlas_bound = fmx(s.tlas_bound, fmx(std::fabs(lo[a]), std::fabs(hi[a])));
+    }
     BvhBuild tb = build_bvh4(ibox, iseg, 1, 1, true);
     // leaf references hold positions in `ibox`; map them to instance indices
     for (Node4& nd : tb.nodes)
@@ -592,7 +582,7 @@ inline Hit trace_bvh(const Geometry& g, const SceneBvh& s, v3 o, v3 d, float tmi
     Hit best{0, 0.0f, 0.0f, 0.0f, 0u, 0u};
     if (!finite3(d) || s.tlas.empty()) return best;
     float tbest = tmax;
-    NodeRay wr{o, v3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)}};
+    NodeRay wr = node_ray(o, d, s.tlas_bound);
     uint32_t stack[256];
     int sp = 0;
     stack[sp++] = 0;
@@ -610,7 +600,7 @@ inline Hit trace_bvh(const Geometry& g, const SceneBvh& s, v3 o, v3 d, float tmi
                 object_ray(in, o, d, oo, od);
                 if (!finite3(od)) continue;
                 RayPre rp = ray_precompute(oo, od);
-                NodeRay nr{oo, v3{safe_inv(od.x), safe_inv(od.y), safe_inv(od.z)}};
+                NodeRay nr = node_ray(oo, od, 1.0f);
                 trace_blas(s, in.mesh_index, inst, rp, nr, cull_back, tmin, best, tbest);
             } else {
                 stack[sp++] = ch;

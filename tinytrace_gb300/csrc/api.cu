@@ -529,6 +529,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.emissive_count = d->emissive_triangle_count;
         ds.instance_count = d->instance_count;
         ds.has_tlas = s->bvh.tlas_nodes > 0 ? 1u : 0u;
+        ds.tlas_bound = s->bvh.tlas_bound;
         tt_scene_stats& stt = s->stats;
         stt.triangle_count = s->bvh.tri_count;
         stt.instance_count = d->instance_count;
@@ -560,8 +561,8 @@ int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint
         require(ctx, "null context");
         use_device(ctx);
         SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
-        require(blas_bytes == s->bvh.blas_nodes * 64ull && tri_bytes == s->bvh.tri_count * 48ull &&
-                    tlas_bytes == s->bvh.tlas_nodes * 64ull,
+        require(blas_bytes == s->bvh.blas_nodes * 128ull && tri_bytes == s->bvh.tri_count * 48ull &&
+                    tlas_bytes == s->bvh.tlas_nodes * 128ull,
                 "byte counts must match tt_scene_stats");
         if (blas && blas_bytes)
             check_cuda(cudaMemcpyAsync(blas, s->bvh.blas.ptr, blas_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");

@@ -465,43 +465,18 @@ __global__ void collapse_emit_kernel(TreeView t, const int* level, uint32_t L, i
             k++;
         }
     }
-    float pmin[3] = {0.0f, 0.0f, 0.0f}, pmax[3] = {0.0f, 0.0f, 0.0f};
-    if (cnt > 0) {
-        float4 l = t.blo[r], h = t.bhi[r];
-        pmin[0] = l.x; pmin[1] = l.y; pmin[2] = l.z;
-        pmax[0] = h.x; pmax[1] = h.y; pmax[2] = h.z;
-    }
-    uint32_t exps = 0, qlo[3] = {0, 0, 0}, qhi[3] = {0, 0, 0};
-    for (int a = 0; a < 3; ++a) {
-        double ext = (double)pmax[a] - (double)pmin[a];
-        int e = -126;
-        if (ext > 0.0) {
-            int ex;
-            frexp(ext / 255.0, &ex);
-            e = ex < -126 ? -126 : (ex > 127 ? 127 : ex);
+    float bx[6][4];
+    for (int c = 0; c < 4; ++c)
+        for (int a = 0; a < 3; ++a) {
+            bx[2 * a][c] = c < cnt ? clo[c][a] : __int_as_float(0x7f800000);
+            bx[2 * a + 1][c] = c < cnt ? chi[c][a] : __int_as_float(0xff800000);
         }
-        double scale = ldexp(1.0, e);
-        exps |= (uint32_t)(e + 127) << (8 * a);
-        for (int c = 0; c < 4; ++c) {
-            uint32_t ql = 255u, qh = 0u;
-            if (c < cnt) {
-                double lo = floor(((double)clo[c][a] - (double)pmin[a]) / scale);
-                double hi = ceil(((double)chi[c][a] - (double)pmin[a]) / scale);
-                lo = lo < 0.0 ? 0.0 : (lo > 255.0 ? 255.0 : lo);
-                hi = hi < 0.0 ? 0.0 : (hi > 255.0 ? 255.0 : hi);
-                ql = (uint32_t)lo;
-                qh = (uint32_t)hi;
-            }
-            qlo[a] |= ql << (8 * c);
-            qhi[a] |= qh << (8 * c);
-        }
-    }
-    exps |= (uint32_t)cnt << 24;
-    uint4* nd = nodes + 4ull * (node_base + li);
-    nd[0] = make_uint4(__float_as_uint(pmin[0]), __float_as_uint(pmin[1]), __float_as_uint(pmin[2]), exps);
-    nd[1] = make_uint4(child[0], child[1], child[2], child[3]);
-    nd[2] = make_uint4(qlo[0], qlo[1], qlo[2], qhi[0]);
-    nd[3] = make_uint4(qhi[1], qhi[2], 0u, 0u);
+    float4* nd = reinterpret_cast<float4*>(nodes) + 8ull * (node_base + li);
+    for (int k = 0; k < 6; ++k) nd[k] = make_float4(bx[k][0], bx[k][1], bx[k][2], bx[k][3]);
+    uint4* nu = reinterpret_cast<uint4*>(nd);
+    nu[6] = make_uint4(child[0], child[1], child[2], child[3]);
+    nu[7] = make_uint4((uint32_t)cnt, 0u, 0u, 0u);
+    (void)r;
 }
 
 __global__ void gather_records_kernel(const float4* in, const uint32_t* order, uint32_t n,
@@ -579,7 +554,7 @@ Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uin
     out.bhi = bhi;
     // collapse
     uint64_t cap = (uint64_t)n + segs + 1;
-    node_buf.alloc(cap * 64ull);
+    node_buf.alloc(cap * 128ull);
     int* lvl_a = sc.get<int>(cap);
     int* lvl_b = sc.get<int>(cap);
     int* chosen = sc.get<int>(4 * cap);
@@ -681,6 +656,17 @@ void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, Bv
         Build4 tb = build_bvh4(ilo, ihi, iseg, ni, 1, 1, true, d_ids, out.tlas, sc);
         out.tlas_nodes = tb.nodes;
         out.tlas_levels = tb.levels;
+        // scene bound for the conservative slab margins: the root box of the instance tree
+        int root = 0;
+        check_cuda(cudaMemcpyAsync(&root, tb.roots, sizeof(int), cudaMemcpyDeviceToHost, stream), "root");
+        check_cuda(cudaStreamSynchronize(stream), "sync");
+        float4 rb[2];
+        check_cuda(cudaMemcpyAsync(&rb[0], tb.blo + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
+        check_cuda(cudaMemcpyAsync(&rb[1], tb.bhi + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
+        check_cuda(cudaStreamSynchronize(stream), "sync");
+        float bound = 0.0f;
+        for (float v : {rb[0].x, rb[0].y, rb[0].z, rb[1].x, rb[1].y, rb[1].z}) bound = std::max(bound, std::fabs(v));
+        out.tlas_bound = bound;
     } else {
         out.tlas_nodes = 0;
         out.tlas_levels = 0;

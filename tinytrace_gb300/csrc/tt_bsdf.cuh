@@ -14,6 +14,15 @@ namespace tt {
 
 using MatC = tt_material_constants;
 
+// Lobe evaluate/sample functions are compiled out of line: inlined at every call site (albedo
+// estimates, next-event estimation, lobe sampling) they made the shading kernel larger than the
+// instruction cache.  Define TT_INLINE_LOBES to inline them.
+#ifdef TT_INLINE_LOBES
+#define TT_LOBE TT_HD
+#else
+#define TT_LOBE static __device__ __noinline__
+#endif
+
 constexpr float DENOM_TOLERANCE = 1.0e-10f;  // material.glsl:4-8
 constexpr float RADIANCE_EPSILON = 1.0e-12f;
 constexpr float PDF_EPSILON = 1.0e-6f;
@@ -143,12 +152,12 @@ TT_HD f3 energy_compensated_oren_nayar(f3 rho, float sigma, f3 wi, f3 wo) {
                fmx(1e-7f, 1.0f - avg);
 }
 TT_HD f3 diffuse_rho(const MatC& m) { return m.base_weight * col3(m.base_color); }
-TT_HD f3 diffuse_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
+TT_LOBE f3 diffuse_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     if (cos_theta(wi) < DENOM_TOLERANCE || cos_theta(wo) < DENOM_TOLERANCE) return splat(0.0f);
     density = cosine_hemisphere_density(cos_theta(wo));
     return energy_compensated_oren_nayar(diffuse_rho(m), PI / 2.0f * m.base_diffuse_roughness, wi, wo);
 }
-TT_HD f3 diffuse_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
+TT_LOBE f3 diffuse_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
     if (cos_theta(wi) < DENOM_TOLERANCE) return splat(0.0f);
     wo = cosine_hemisphere_sample(random_vec2(g));
     density = cosine_hemisphere_density(cos_theta(wo));
@@ -171,7 +180,7 @@ TT_HD f3 coat_brdf(f3 wi, f3 wo, f3 wir, f3 wor, float ior, f2 alpha, float& den
     return splat(fres) * dist * microfacet_visibility(alpha, wir, wor) /
            fmx(4.0f * fabsf(cos_theta(wo)) * fabsf(cos_theta(wi)), DENOM_TOLERANCE);
 }
-TT_HD f3 coat_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
+TT_LOBE f3 coat_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     if (!is_same_hemisphere(wo, wi)) return splat(0.0f);
     float ior = cos_theta(wi) > 0.0f ? m.coat_ior : 1.0f / m.coat_ior;
     if (fabsf(ior - 1.0f) < IOR_EPSILON) return splat(0.0f);
@@ -179,7 +188,7 @@ TT_HD f3 coat_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     LocalRotation rot = local_frame_rotation(2.0f * PI * m.coat_rotation);
     return coat_brdf(wi, wo, rotate_local(wi, rot), rotate_local(wo, rot), ior, alpha, density);
 }
-TT_HD f3 coat_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
+TT_LOBE f3 coat_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
     float ior = cos_theta(wi) > 0.0f ? m.coat_ior / 1.0f : 1.0f / m.coat_ior;
     if (fabsf(ior - 1.0f) < IOR_EPSILON) return splat(0.0f);
     f2 alpha = microfacet_roughness_to_alpha(m.coat_roughness, m.coat_roughness_anisotropy);
@@ -229,7 +238,7 @@ TT_HD f3 fuzz_density_and_brdf(const MatC& m, f3 dir, f3 wi, float a_inv, float 
     float alb = fuzz_albedo(cos_theta(wi), roughness);
     return col3(m.fuzz_color) * alb * INVERSE_PI * jac;
 }
-TT_HD f3 fuzz_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
+TT_LOBE f3 fuzz_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     if (cos_theta(wi) < DENOM_TOLERANCE || cos_theta(wo) < DENOM_TOLERANCE) return splat(0.0f);
     float roughness = clampf(m.fuzz_roughness, 0.01f, 1.0f);
     LtcBasis b = orthonormal_basis_ltc(wi);
@@ -238,7 +247,7 @@ TT_HD f3 fuzz_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     f3 dir = f3{ic.x * w.x + ic.y * w.z, ic.x * w.y, w.z};
     return fuzz_density_and_brdf(m, dir, wi, ic.x, roughness, density);
 }
-TT_HD f3 fuzz_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
+TT_LOBE f3 fuzz_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
     if (cos_theta(wi) < DENOM_TOLERANCE) return splat(0.0f);
     float roughness = clampf(m.fuzz_roughness, 0.01f, 1.0f);
     f3 dir = cosine_hemisphere_sample(random_vec2(g));
@@ -277,7 +286,7 @@ TT_HD f3 specular_brdf(const MatC& m, f3 wi, f3 wo, f3 wir, f3 wor, f3 mn, f2 al
               fmx(4.0f * fabsf(cos_theta(wo)) * fabsf(cos_theta(wi)), DENOM_TOLERANCE);
     return brdf * col3(m.specular_color);
 }
-TT_HD f3 specular_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
+TT_LOBE f3 specular_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     if (!is_same_hemisphere(wo, wi)) return splat(0.0f);
     float ratio = specular_ior_ratio(m);
     float ior = cos_theta(wi) > 0.0f ? ratio : 1.0f / ratio;
@@ -289,7 +298,7 @@ TT_HD f3 specular_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     if (dot(mn, wir) * cos_theta(wir) < 0.0f || dot(mn, wor) * cos_theta(wor) < 0.0f) return splat(0.0f);
     return specular_brdf(m, wi, wo, wir, wor, mn, alpha, ior, density);
 }
-TT_HD f3 specular_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
+TT_LOBE f3 specular_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
     float ratio = specular_ior_ratio(m);
     float ior = cos_theta(wi) > 0.0f ? ratio : 1.0f / ratio;
     if (fabsf(ior - 1.0f) < IOR_EPSILON) return splat(0.0f);
@@ -336,7 +345,7 @@ TT_HD f3 metal_brdf(const MatC& m, f2 alpha, f3 mn, f3 wi, f3 wo, f3 wir, f3 wor
     float vis = microfacet_visibility(alpha, wir, wor);
     return fres * dist * vis / fmx(4.0f * fabsf(cos_theta(wo)) * fabsf(cos_theta(wi)), DENOM_TOLERANCE);
 }
-TT_HD f3 metal_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
+TT_LOBE f3 metal_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     if (cos_theta(wi) < DENOM_TOLERANCE || cos_theta(wo) < DENOM_TOLERANCE) {
         density = PDF_EPSILON;
         return splat(0.0f);
@@ -347,7 +356,7 @@ TT_HD f3 metal_brdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     f3 mn = normalize(wor + wir);
     return metal_brdf(m, alpha, mn, wi, wo, wir, wor, density);
 }
-TT_HD f3 metal_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
+TT_LOBE f3 metal_brdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
     if (cos_theta(wi) < DENOM_TOLERANCE) {
         density = PDF_EPSILON;
         return splat(0.0f);
@@ -386,7 +395,7 @@ TT_HD f3 specular_btdf(const MatC& m, f3 mn, f2 alpha, f3 wi, f3 wo, f3 wir, f3 
                  fmx(fabsf(cos_theta(wo)) * fabsf(cos_theta(wi)), DENOM_TOLERANCE);
     return btdf * btdf_tint(m);
 }
-TT_HD f3 specular_btdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
+TT_LOBE f3 specular_btdf_evaluate(const MatC& m, f3 wi, f3 wo, float& density) {
     if (is_same_hemisphere(wo, wi)) {
         density = 1.0f;
         return splat(0.0f);
@@ -415,7 +424,7 @@ TT_HD bool refraction_direction(f3 n, float ior, f3 wi, f3& dir) {
     dir = ior * -wi + (ior * cti - ctt) * n;
     return true;
 }
-TT_HD f3 specular_btdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
+TT_LOBE f3 specular_btdf_sample(const MatC& m, f3 wi, uint32_t& g, f3& wo, float& density) {
     float ior = cos_theta(wi) > 0.0f ? 1.0f / m.specular_ior : m.specular_ior;
     if (fabsf(ior - 1.0f) < IOR_EPSILON) {
         wo = -wi;

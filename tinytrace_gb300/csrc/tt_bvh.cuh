@@ -10,10 +10,12 @@
 //     det > 0 (geometric normal cross(p1-p0, p2-p0) facing the ray origin);
 //   * hits count for tmin <= t <= tmax; the closest hit is the smallest t with ties broken
 //     by the smaller (instance, primitive) pair, so any traversal order gives the same hit;
-//   * node boxes are quantised to 8 bits per axis relative to the node box and tested
-//     conservatively (slab bounds widened by 2^-20 of their magnitudes).
+//   * child boxes are tested conservatively: slab distances are widened by
+//     2^-20 (B + |o|) |1/d| per axis (B bounds the box coordinates: 1 in object space, where
+//     vertices are snorm16, the scene bound in world space), more than their rounding error.
 //
-// Layout in HBM: BVH4 nodes are 64-byte records read as four 16-byte vector loads; the
+// Layout in HBM: BVH4 nodes are 128-byte records (six float4 of child-box planes, the child
+// references, the child count) read as seven 16-byte vector loads; the
 // triangles of each mesh are stored in leaf order as 48-byte records (three float4), so a
 // leaf is one contiguous run; per-instance traversal data is a 64-byte record (the three
 // rows of the world-to-object matrix and the mesh index).  The traversal stack lives in
@@ -48,7 +50,7 @@ struct DevScene {
     uint32_t emissive_count;
     uint32_t instance_count;
     uint32_t has_tlas;
-    uint32_t pad;
+    float tlas_bound;  // max |coordinate| of the instance world boxes
 };
 
 struct Hit {
@@ -63,7 +65,7 @@ struct Counters {
 
 struct RayPre {
     f3 o;
-    int kx, ky, kz;
+    uint32_t k;  // kx | ky << 2 | kz << 4
     float sx, sy, sz;
 };
 TT_HD float comp(f3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
@@ -80,9 +82,7 @@ TT_HD RayPre ray_precompute(f3 o, f3 d) {
         kx = ky;
         ky = t;
     }
-    r.kx = kx;
-    r.ky = ky;
-    r.kz = kz;
+    r.k = (uint32_t)kx | ((uint32_t)ky << 2) | ((uint32_t)kz << 4);
     float dz = comp(d, kz);
     r.sx = comp(d, kx) / dz;
     r.sy = comp(d, ky) / dz;
@@ -93,13 +93,14 @@ TT_HD RayPre ray_precompute(f3 o, f3 d) {
 TT_HD bool intersect_triangle(const RayPre& r, f3 p0, f3 p1, f3 p2, bool cull_back, float tmin,
                               float tmax, float& t_out, float& u_out, float& v_out) {
     f3 A = p0 - r.o, B = p1 - r.o, C = p2 - r.o;
-    float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
-    float Ax = comp(A, r.kx) - r.sx * Akz;
-    float Ay = comp(A, r.ky) - r.sy * Akz;
-    float Bx = comp(B, r.kx) - r.sx * Bkz;
-    float By = comp(B, r.ky) - r.sy * Bkz;
-    float Cx = comp(C, r.kx) - r.sx * Ckz;
-    float Cy = comp(C, r.ky) - r.sy * Ckz;
+    int kx = (int)(r.k & 3u), ky = (int)((r.k >> 2) & 3u), kz = (int)(r.k >> 4);
+    float Akz = comp(A, kz), Bkz = comp(B, kz), Ckz = comp(C, kz);
+    float Ax = comp(A, kx) - r.sx * Akz;
+    float Ay = comp(A, ky) - r.sy * Akz;
+    float Bx = comp(B, kx) - r.sx * Bkz;
+    float By = comp(B, ky) - r.sy * Bkz;
+    float Cx = comp(C, kx) - r.sx * Ckz;
+    float Cy = comp(C, ky) - r.sy * Ckz;
     float U = Cx * By - Cy * Bx;
     float V = Ax * Cy - Ay * Cx;
     float W = Bx * Ay - By * Ax;
@@ -138,202 +139,223 @@ TT_HD float safe_inv(float d) {
     return 1.0f / a;
 }
 
+// Per-ray data of the slab test: per axis the inverse direction, the near-plane selector and
+// -o/d widened by the conservative margin towards the near and the far side.
 struct NodeRay {
-    f3 o, inv;
+    f3 inv, nob_near, nob_far;
+    uint32_t near;  // bit a set: the near plane of axis a is the high bound (1/d < 0)
 };
-
-struct NodeData {
-    uint4 q0, q1, q2, q3;
-};
-TT_HD NodeData load_node(const uint4* nodes, uint32_t i) {
-    const uint4* p = nodes + 4ull * i;
-    NodeData n;
-    n.q0 = __ldg(p + 0);
-    n.q1 = __ldg(p + 1);
-    n.q2 = __ldg(p + 2);
-    n.q3 = __ldg(p + 3);
-    return n;
-}
-TT_HD uint32_t byte_of(uint32_t w, int b) { return (w >> (8 * b)) & 0xffu; }
-
-// Conservative slab test of the (up to) four children; returns the hit mask and entry t.
-TT_HD int node_hits(const NodeData& nd, const NodeRay& r, float tmin, float tbest, float* tn_out,
-                    uint32_t* child) {
-    float org[3] = {__uint_as_float(nd.q0.x), __uint_as_float(nd.q0.y), __uint_as_float(nd.q0.z)};
-    uint32_t meta = nd.q0.w;  // exp bytes 0..2, count byte 3
-    int count = (int)byte_of(meta, 3);
-    const float o[3] = {r.o.x, r.o.y, r.o.z};
-    const float inv[3] = {r.inv.x, r.inv.y, r.inv.z};
-    float A[3], Blo[3], Bhi[3];
+TT_HD NodeRay node_ray(f3 o, f3 d, float bound) {
+    NodeRay r;
+    r.inv = f3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+    const float oa[3] = {o.x, o.y, o.z}, ia[3] = {r.inv.x, r.inv.y, r.inv.z};
+    float nn[3], nf[3];
+    r.near = 0u;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float scale = __uint_as_float(byte_of(meta, a) << 23);
-        A[a] = scale * inv[a];
-        float B = (org[a] - o[a]) * inv[a];
-        float M = __fmaf_rn(256.0f, fabsf(A[a]), fabsf(B)) * 9.5367431640625e-07f;
-        float s = inv[a] >= 0.0f ? M : -M;
-        Blo[a] = B - s;
-        Bhi[a] = B + s;
+        float nob = -(oa[a] * ia[a]);
+        float E = (bound + fabsf(oa[a])) * fabsf(ia[a]) * 9.5367431640625e-07f;
+        nn[a] = nob - E;
+        nf[a] = nob + E;
+        if (!(ia[a] >= 0.0f)) r.near |= 1u << a;
     }
-    child[0] = nd.q1.x;
-    child[1] = nd.q1.y;
-    child[2] = nd.q1.z;
-    child[3] = nd.q1.w;
-    // q2: qlo x[4], qlo y[4], qlo z[4], qhi x[4]; q3: qhi y[4], qhi z[4], pad
-    uint32_t lo[3] = {nd.q2.x, nd.q2.y, nd.q2.z};
-    uint32_t hi[3] = {nd.q2.w, nd.q3.x, nd.q3.y};
+    r.nob_near = f3{nn[0], nn[1], nn[2]};
+    r.nob_far = f3{nf[0], nf[1], nf[2]};
+    return r;
+}
+
+// Slab test of the (up to) four children of node `i`; returns the hit mask, entry distances
+// and child references.  Empty slots hold +inf/-inf planes and never pass.
+TT_HD int node_hits(const uint4* nodes, uint32_t i, const NodeRay& r, float tmin, float tbest, float* tn_out,
+                    uint32_t* child) {
+    const float4* p = reinterpret_cast<const float4*>(nodes) + 8ull * i;
+    float4 nx = __ldg(p + ((r.near & 1u) ? 1 : 0)), fx = __ldg(p + ((r.near & 1u) ? 0 : 1));
+    float4 ny = __ldg(p + ((r.near & 2u) ? 3 : 2)), fy = __ldg(p + ((r.near & 2u) ? 2 : 3));
+    float4 nz = __ldg(p + ((r.near & 4u) ? 5 : 4)), fz = __ldg(p + ((r.near & 4u) ? 4 : 5));
+    uint4 ch = __ldg(reinterpret_cast<const uint4*>(p + 6));
+    child[0] = ch.x;
+    child[1] = ch.y;
+    child[2] = ch.z;
+    child[3] = ch.w;
+    const float n4x[4] = {nx.x, nx.y, nx.z, nx.w}, f4x[4] = {fx.x, fx.y, fx.z, fx.w};
+    const float n4y[4] = {ny.x, ny.y, ny.z, ny.w}, f4y[4] = {fy.x, fy.y, fy.z, fy.w};
+    const float n4z[4] = {nz.x, nz.y, nz.z, nz.w}, f4z[4] = {fz.x, fz.y, fz.z, fz.w};
     int mask = 0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        float tn = tmin, tf = tbest;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            float t0 = __fmaf_rn((float)byte_of(lo[a], c), A[a], Blo[a]);
-            float t1 = __fmaf_rn((float)byte_of(hi[a], c), A[a], Bhi[a]);
-            tn = fmx(tn, fmn(t0, t1));
-            tf = fmn(tf, fmx(t0, t1));
-        }
+        float tn = fmx(fmx(__fmaf_rn(n4x[c], r.inv.x, r.nob_near.x), __fmaf_rn(n4y[c], r.inv.y, r.nob_near.y)),
+                       fmx(__fmaf_rn(n4z[c], r.inv.z, r.nob_near.z), tmin));
+        float tf = fmn(fmn(__fmaf_rn(f4x[c], r.inv.x, r.nob_far.x), __fmaf_rn(f4y[c], r.inv.y, r.nob_far.y)),
+                       fmn(__fmaf_rn(f4z[c], r.inv.z, r.nob_far.z), tbest));
         tn_out[c] = tn;
-        if (c < count && tn <= tf) mask |= 1 << c;
+        if (tn <= tf) mask |= 1 << c;
     }
     return mask;
 }
 
 TT_HD f3 tri_vertex(float4 v) { return f3{v.x, v.y, v.z}; }
 
-// Closest hit through the TLAS/BLAS.  `stack` is this thread's column in shared memory
-// (element k at stack[k * stride]).  `err` receives ERR_* bits on overflow/limit.
-template <bool COUNT>
-__device__ __forceinline__ Hit trace_closest(const DevScene& sc, f3 o, f3 d, float tmin,
-                                             float tmax, bool cull, uint32_t* stack, int stride,
-                                             uint32_t* err, Counters& cnt) {
+// Resumable closest-hit traversal through the TLAS/BLAS.  trace_init() sets a ray up and
+// trace_step() performs one unit of work (pop an entry, enter an instance, or visit one node
+// and test its leaf triangles); it returns true when the traversal is finished and the
+// result is in `best`.  `stack` is the thread's column in shared memory (element k at
+// stack[k * stride]); `err` receives ERR_* bits when the stack or the iteration limit would
+// be exceeded, in which case the traversal ends.
+struct TraceState {
+    f3 o, d;     // world ray
+    NodeRay nr;  // slab-test data of the current level (world at the top, object inside instances)
+    RayPre rp;
     Hit best;
-    best.hit = 0;
-    best.t = 0.0f;
-    best.u = 0.0f;
-    best.v = 0.0f;
-    best.instance = 0u;
-    best.prim = 0u;
-    if (!finite3(d) || !sc.has_tlas) return best;
-    float tbest = tmax;
-    NodeRay world{o, f3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)}};
-    NodeRay obj = world;
-    RayPre rp = ray_precompute(o, d);
-    uint32_t inst = 0;
-    bool in_blas = false;
-    int sp = 0;
-    uint32_t cur = 0;
-    bool have = true;
-    uint32_t iterations = 0;
-    while (true) {
-        if (++iterations > TRAVERSAL_ITERATION_LIMIT) {
-            atomicOr(err, ERR_ITERATION_LIMIT);
-            break;
+    float tmin, tbest;
+    uint32_t inst, cur, iterations;
+    int sp;
+    bool in_blas, have, cull;
+};
+
+TT_HD void trace_init(TraceState& st, const DevScene& sc, f3 o, f3 d, float tmin, float tmax, bool cull) {
+    st.best.hit = 0;
+    st.best.t = 0.0f;
+    st.best.u = 0.0f;
+    st.best.v = 0.0f;
+    st.best.instance = 0u;
+    st.best.prim = 0u;
+    st.o = o;
+    st.d = d;
+    st.tmin = tmin;
+    st.tbest = tmax;
+    st.cull = cull;
+    st.nr = node_ray(o, d, sc.tlas_bound);
+    st.rp = ray_precompute(o, d);
+    st.inst = 0u;
+    st.in_blas = false;
+    st.sp = 0;
+    st.cur = 0u;
+    st.iterations = 0u;
+    st.have = finite3(d) && sc.has_tlas != 0u;  // a NaN/inf direction or an empty scene misses
+}
+
+template <bool COUNT>
+__device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
+                                           uint32_t* err, Counters& cnt) {
+    if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {
+        atomicOr(err, ERR_ITERATION_LIMIT);
+        return true;
+    }
+    if (!st.have) {
+        if (st.sp == 0) return true;
+        uint32_t e = stack[(--st.sp) * stride];
+        if (e == STACK_MARKER) {
+            st.in_blas = false;
+            st.nr = node_ray(st.o, st.d, sc.tlas_bound);
+            return false;
         }
-        if (!have) {
-            if (sp == 0) break;
-            uint32_t e = stack[(--sp) * stride];
-            if (e == STACK_MARKER) {
-                in_blas = false;
-                continue;
-            }
-            cur = e;
-            have = true;
+        st.cur = e;
+        st.have = true;
+    }
+    if (!st.in_blas && (st.cur & CHILD_LEAF)) {
+        st.inst = leaf_first(st.cur);
+        const float4* x = sc.inst_xform + 4ull * st.inst;
+        float4 r0 = __ldg(x + 0), r1 = __ldg(x + 1), r2 = __ldg(x + 2);
+        uint32_t mesh = __float_as_uint(__ldg(x + 3).x);
+        f3 o = st.o, d = st.d;
+        f3 oo = f3{r0.x * o.x + r0.y * o.y + r0.z * o.z + r0.w * 1.0f,
+                   r1.x * o.x + r1.y * o.y + r1.z * o.z + r1.w * 1.0f,
+                   r2.x * o.x + r2.y * o.y + r2.z * o.z + r2.w * 1.0f};
+        f3 od = f3{r0.x * d.x + r0.y * d.y + r0.z * d.z, r1.x * d.x + r1.y * d.y + r1.z * d.z,
+                   r2.x * d.x + r2.y * d.y + r2.z * d.z};
+        if (COUNT) cnt.instances++;
+        if (!finite3(od)) {
+            st.have = false;
+            return false;
         }
-        if (!in_blas && (cur & CHILD_LEAF)) {
-            inst = leaf_first(cur);
-            const float4* x = sc.inst_xform + 4ull * inst;
-            float4 r0 = __ldg(x + 0), r1 = __ldg(x + 1), r2 = __ldg(x + 2);
-            uint32_t mesh = __float_as_uint(__ldg(x + 3).x);
-            f3 oo = f3{r0.x * o.x + r0.y * o.y + r0.z * o.z + r0.w * 1.0f,
-                       r1.x * o.x + r1.y * o.y + r1.z * o.z + r1.w * 1.0f,
-                       r2.x * o.x + r2.y * o.y + r2.z * o.z + r2.w * 1.0f};
-            f3 od = f3{r0.x * d.x + r0.y * d.y + r0.z * d.z, r1.x * d.x + r1.y * d.y + r1.z * d.z,
-                       r2.x * d.x + r2.y * d.y + r2.z * d.z};
-            if (COUNT) cnt.instances++;
-            if (!finite3(od)) {
-                have = false;
-                continue;
-            }
-            if (sp >= TRAVERSAL_STACK) {
-                atomicOr(err, ERR_STACK_OVERFLOW);
-                break;
-            }
-            stack[(sp++) * stride] = STACK_MARKER;
-            rp = ray_precompute(oo, od);
-            obj = NodeRay{oo, f3{safe_inv(od.x), safe_inv(od.y), safe_inv(od.z)}};
-            in_blas = true;
-            cur = mesh;
-            continue;
+        if (st.sp >= TRAVERSAL_STACK) {
+            atomicOr(err, ERR_STACK_OVERFLOW);
+            return true;
         }
-        NodeData nd = load_node(in_blas ? sc.blas : sc.tlas, cur);
-        if (COUNT) {
-            if (in_blas) cnt.blas_nodes++;
-            else cnt.tlas_nodes++;
-        }
-        float tn[4];
-        uint32_t ch[4];
-        int mask = node_hits(nd, in_blas ? obj : world, tmin, tbest, tn, ch);
-        // triangle leaves first (in child order)
-        if (in_blas) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (!((mask >> c) & 1) || !(ch[c] & CHILD_LEAF)) continue;
-                uint32_t f = leaf_first(ch[c]), k = leaf_count(ch[c]);
-                for (uint32_t q = f; q < f + k; ++q) {
-                    const float4* tr = sc.tris + 3ull * q;
-                    float4 a = __ldg(tr + 0), b = __ldg(tr + 1), cc = __ldg(tr + 2);
-                    if (COUNT) cnt.triangles++;
-                    float t, u, v;
-                    uint32_t prim = __float_as_uint(a.w);
-                    if (!intersect_triangle(rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), cull,
-                                            tmin, tbest, t, u, v))
-                        continue;
-                    if (closer(t, inst, prim, best)) {
-                        best.hit = 1;
-                        best.t = t;
-                        best.u = u;
-                        best.v = v;
-                        best.instance = inst;
-                        best.prim = prim;
-                        tbest = t;
-                    }
-                }
-            }
-        }
-        // remaining descendants: internal nodes (and instance leaves at the top level),
-        // sorted by entry distance; the nearest is visited next, the others are pushed.
-        float key[4];
-        uint32_t val[4];
+        stack[(st.sp++) * stride] = STACK_MARKER;
+        st.rp = ray_precompute(oo, od);
+        st.nr = node_ray(oo, od, 1.0f);
+        st.in_blas = true;
+        st.cur = mesh;
+        return false;
+    }
+    if (COUNT) {
+        if (st.in_blas) cnt.blas_nodes++;
+        else cnt.tlas_nodes++;
+    }
+    float tn[4];
+    uint32_t ch[4];
+    int mask = node_hits(st.in_blas ? sc.blas : sc.tlas, st.cur, st.nr, st.tmin, st.tbest, tn, ch);
+    // triangle leaves first (in child order)
+    if (st.in_blas) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            bool take = ((mask >> c) & 1) && (!in_blas || !(ch[c] & CHILD_LEAF)) && tn[c] <= tbest;
-            key[c] = take ? tn[c] : __int_as_float(0x7f800000);
-            val[c] = take ? ch[c] : STACK_MARKER;
-        }
-#define TT_SWAP(i, j)                                            \
-    if (key[j] < key[i]) {                                       \
-        float tk = key[i]; key[i] = key[j]; key[j] = tk;         \
-        uint32_t tv = val[i]; val[i] = val[j]; val[j] = tv;      \
-    }
-        TT_SWAP(0, 1) TT_SWAP(2, 3) TT_SWAP(0, 2) TT_SWAP(1, 3) TT_SWAP(1, 2)
-#undef TT_SWAP
-        have = false;
-        if (val[0] != STACK_MARKER) {
-            cur = val[0];
-            have = true;
-#pragma unroll
-            for (int c = 3; c >= 1; --c) {
-                if (val[c] == STACK_MARKER) continue;
-                if (sp >= TRAVERSAL_STACK) {
-                    atomicOr(err, ERR_STACK_OVERFLOW);
-                    return best;
+            if (!((mask >> c) & 1) || !(ch[c] & CHILD_LEAF)) continue;
+            uint32_t f = leaf_first(ch[c]), k = leaf_count(ch[c]);
+            for (uint32_t q = f; q < f + k; ++q) {
+                const float4* tr = sc.tris + 3ull * q;
+                float4 a = __ldg(tr + 0), b = __ldg(tr + 1), cc = __ldg(tr + 2);
+                if (COUNT) cnt.triangles++;
+                float t, u, v;
+                uint32_t prim = __float_as_uint(a.w);
+                if (!intersect_triangle(st.rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), st.cull, st.tmin,
+                                        st.tbest, t, u, v))
+                    continue;
+                if (closer(t, st.inst, prim, st.best)) {
+                    st.best.hit = 1;
+                    st.best.t = t;
+                    st.best.u = u;
+                    st.best.v = v;
+                    st.best.instance = st.inst;
+                    st.best.prim = prim;
+                    st.tbest = t;
                 }
-                stack[(sp++) * stride] = val[c];
             }
         }
     }
-    return best;
+    // remaining descendants: internal nodes (and instance leaves at the top level), sorted by
+    // entry distance; the nearest is visited next, the others are pushed.
+    float key[4];
+    uint32_t val[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        bool take = ((mask >> c) & 1) && (!st.in_blas || !(ch[c] & CHILD_LEAF)) && tn[c] <= st.tbest;
+        key[c] = take ? tn[c] : __int_as_float(0x7f800000);
+        val[c] = take ? ch[c] : STACK_MARKER;
+    }
+#define TT_SWAP(i, j)                                       \
+    if (key[j] < key[i]) {                                  \
+        float tk = key[i]; key[i] = key[j]; key[j] = tk;    \
+        uint32_t tv = val[i]; val[i] = val[j]; val[j] = tv; \
+    }
+    TT_SWAP(0, 1) TT_SWAP(2, 3) TT_SWAP(0, 2) TT_SWAP(1, 3) TT_SWAP(1, 2)
+#undef TT_SWAP
+    st.have = false;
+    if (val[0] != STACK_MARKER) {
+        st.cur = val[0];
+        st.have = true;
+#pragma unroll
+        for (int c = 3; c >= 1; --c) {
+            if (val[c] == STACK_MARKER) continue;
+            if (st.sp >= TRAVERSAL_STACK) {
+                atomicOr(err, ERR_STACK_OVERFLOW);
+                return true;
+            }
+            stack[(st.sp++) * stride] = val[c];
+        }
+    }
+    return false;
+}
+
+// Closest hit, run to completion.
+template <bool COUNT>
+__device__ __forceinline__ Hit trace_closest(const DevScene& sc, f3 o, f3 d, float tmin, float tmax, bool cull,
+                                             uint32_t* stack, int stride, uint32_t* err, Counters& cnt) {
+    TraceState st;
+    trace_init(st, sc, o, d, tmin, tmax, cull);
+    while (!trace_step<COUNT>(st, sc, stack, stride, err, cnt)) {
+    }
+    return st.best;
 }
 
 }  // namespace tt

@@ -37,11 +37,12 @@ struct DeviceBuffer {
 
 // Result of the LBVH build for one scene.
 struct BvhResult {
-    DeviceBuffer blas;   // Node4 records
-    DeviceBuffer tris;   // TriRecord records (BLAS leaf order)
-    DeviceBuffer tlas;   // Node4 records
+    DeviceBuffer blas;   // 128-byte BVH4 nodes
+    DeviceBuffer tris;   // 48-byte triangle records (BLAS leaf order)
+    DeviceBuffer tlas;   // 128-byte BVH4 nodes
     uint64_t blas_nodes = 0, tlas_nodes = 0, tri_count = 0;
     uint32_t blas_levels = 0, tlas_levels = 0;
+    float tlas_bound = 0.0f;  // max |coordinate| of the instance world boxes
 };
 
 struct BuildInput {

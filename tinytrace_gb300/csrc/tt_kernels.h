@@ -22,7 +22,7 @@ struct WfParams {
     uint4* hit;
     uint32_t* active;
     float4* shadow;
-    uint32_t* counters;  // [0] next work item, [1] active paths, [2] shadow rays
+    uint32_t* counters;  // [0] next work item, [1] active paths, [2] shadow rays, [3]/[4] trace queue heads
     float4* samples;     // chunk_spp x WH per-sample radiance (band order)
     float4* running;     // WH running per-pixel sums across chunks
     uint32_t P, WH;

@@ -100,26 +100,90 @@ __global__ void __launch_bounds__(WF_BLOCK) wf_regen_kernel(const __grid_constan
     if (live) w.active[q] = s;
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(WF_BLOCK) wf_extend_kernel(const __grid_constant__ RenderParams p,
-                                                             const __grid_constant__ WfParams w) {
-    __shared__ uint32_t s_stack[TRAVERSAL_STACK * WF_BLOCK];
-    uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
-    uint32_t n = w.counters[1];
+// Extension and shadow rays: persistent warps with per-lane refill.  Each lane traces one ray
+// at a time; when fewer than REFILL_LANES lanes of a warp still have a ray, the idle lanes
+// fetch new rays from the queue (one atomicAdd per warp), so warps keep their lanes busy
+// instead of waiting for their longest ray (the dynamic fetch of Aila & Laine 2009).
+#ifndef TT_TRACE_MIN_BLOCKS
+#define TT_TRACE_MIN_BLOCKS 6
+#endif
+#ifndef TT_REFILL_LANES
+#define TT_REFILL_LANES 16
+#endif
+constexpr int TR_BLOCK = 128;
+constexpr int REFILL_LANES = TT_REFILL_LANES;
+
+template <bool COUNT, bool SHADOW>
+__global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel(const __grid_constant__ RenderParams p,
+                                                                const __grid_constant__ WfParams w) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * TR_BLOCK];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const DevScene& sc = p.sc;
+    const uint32_t n = SHADOW ? w.counters[2] : w.counters[1];
+    uint32_t* head = &w.counters[SHADOW ? 4 : 3];
+    TraceState st;
+    uint32_t item = 0, slot = 0, light = 0;
+    bool active = false;
+    bool drained = false;  // warp-uniform: the queue has no more rays
     Counters cnt{0u, 0u, 0u, 0u};
-    uint32_t hit = 0;
-    if (q < n) {
-        uint32_t s = w.active[q];
-        float4 o = w.org[s], d = w.dir[s];
-        Hit h = trace_closest<COUNT>(p.sc, xyz(o), xyz(d), EXTENSION_TMIN, EXTENSION_TMAX, true,
-                                     s_stack + threadIdx.x, WF_BLOCK, p.err, cnt);
-        w.hit[q] = h.hit ? make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim)
-                         : make_uint4(0u, 0u, NO_HIT, 0u);
-        hit = h.hit ? 1u : 0u;
+    uint32_t rays = 0, hits = 0;
+    while (true) {
+        if (!drained) {
+            bool idle = !active;
+            uint32_t mask = __ballot_sync(0xffffffffu, idle);
+            if (mask) {
+                int leader = __ffs(mask) - 1;
+                uint32_t base = 0;
+                if ((int)(threadIdx.x & 31u) == leader) base = atomicAdd(head, (uint32_t)__popc(mask));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                uint32_t my = base + (uint32_t)__popc(mask & lane_mask_lt());
+                if (idle && my < n) {
+                    item = my;
+                    float4 o, d;
+                    if (SHADOW) {
+                        o = w.shadow[2ull * item];
+                        d = w.shadow[2ull * item + 1];
+                        slot = __float_as_uint(o.w);
+                        light = __float_as_uint(d.w);
+                    } else {
+                        slot = w.active[item];
+                        o = w.org[slot];
+                        d = w.dir[slot];
+                    }
+                    trace_init(st, sc, xyz(o), xyz(d), SHADOW ? SHADOW_TMIN : EXTENSION_TMIN,
+                               SHADOW ? SHADOW_TMAX : EXTENSION_TMAX, !SHADOW);
+                    active = true;
+                    if (COUNT) rays++;
+                }
+                drained = __any_sync(0xffffffffu, idle && my >= n);
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        while (true) {
+            if (active && trace_step<COUNT>(st, sc, stack, TR_BLOCK, p.err, cnt)) {
+                active = false;
+                const Hit& h = st.best;
+                if (SHADOW) {
+                    float4 a1 = w.pa1[slot];
+                    uint32_t pflags = __float_as_uint(a1.w);
+                    bool vis = light_visible(sc, h, light, pflags >> 16);
+                    float4 a4 = w.acc[slot];
+                    f3 acc = xyz(a4);
+                    acc += vis ? xyz(a1) : xyz(w.pa0[slot]);
+                    if (pflags & 1u) acc += xyz(w.pe[slot]);
+                    w.acc[slot] = make_float4(acc.x, acc.y, acc.z, a4.w);
+                } else {
+                    w.hit[item] = h.hit ? make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim)
+                                        : make_uint4(0u, 0u, NO_HIT, 0u);
+                    if (COUNT && h.hit) hits++;
+                }
+            }
+            uint32_t am = __ballot_sync(0xffffffffu, active);
+            if (am == 0u || (!drained && __popc(am) < REFILL_LANES)) break;
+        }
     }
     if (COUNT) {
-        unsigned long long v[6] = {q < n ? 1ull : 0ull, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles,
-                                   cnt.instances, hit};
+        unsigned long long v[6] = {rays, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles, cnt.instances, hits};
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             unsigned long long x = v[k];
@@ -191,38 +255,6 @@ __global__ void __launch_bounds__(WF_BLOCK) wf_shade_kernel(const __grid_constan
     }
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(WF_BLOCK) wf_shadow_kernel(const __grid_constant__ RenderParams p,
-                                                             const __grid_constant__ WfParams w) {
-    __shared__ uint32_t s_stack[TRAVERSAL_STACK * WF_BLOCK];
-    uint32_t e = blockIdx.x * WF_BLOCK + threadIdx.x;
-    uint32_t n = w.counters[2];
-    Counters cnt{0u, 0u, 0u, 0u};
-    if (e < n) {
-        float4 o = w.shadow[2ull * e], d = w.shadow[2ull * e + 1];
-        uint32_t s = __float_as_uint(o.w), light = __float_as_uint(d.w);
-        Hit h = trace_closest<COUNT>(p.sc, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX, false,
-                                     s_stack + threadIdx.x, WF_BLOCK, p.err, cnt);
-        float4 a1 = w.pa1[s];
-        uint32_t pflags = __float_as_uint(a1.w);
-        bool vis = light_visible(p.sc, h, light, pflags >> 16);
-        float4 a4 = w.acc[s];
-        f3 acc = xyz(a4);
-        acc += vis ? xyz(a1) : xyz(w.pa0[s]);
-        if (pflags & 1u) acc += xyz(w.pe[s]);
-        w.acc[s] = make_float4(acc.x, acc.y, acc.z, a4.w);
-    }
-    if (COUNT) {
-        unsigned long long v[5] = {e < n ? 1ull : 0ull, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles, cnt.instances};
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            unsigned long long x = v[k];
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            if ((threadIdx.x & 31) == 0 && x) atomicAdd(p.counters + k, x);
-        }
-    }
-}
-
 // Per pixel: samples of this chunk added in sample order to the running sum; after the last
 // chunk, divide by the sample count and apply the frame accumulation (integrate.glsl:338-346).
 __global__ void wf_reduce_kernel(const __grid_constant__ RenderParams p, const __grid_constant__ WfParams w,
@@ -254,25 +286,35 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
     uint32_t max_chunk = w.chunk_spp;
     w.WH = WH;
     unsigned regen_grid = (w.P + WF_BLOCK - 1) / WF_BLOCK;
+    static int trace_blocks = 0;  // resident blocks of the persistent trace kernel on the whole GPU
+    if (trace_blocks == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wf_trace_kernel<false, false>, TR_BLOCK, 0),
+                   "occupancy");
+        trace_blocks = std::max(1, sms * per_sm);
+    }
     check_cuda(cudaMemsetAsync(w.acc, 0, 16ull * w.P, st), "memset");  // every slot starts free
     for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
         w.chunk_sample0 = s0;
         w.chunk_spp = std::min(max_chunk, spp - s0);
         w.chunk_items = WH * w.chunk_spp;
-        check_cuda(cudaMemsetAsync(w.counters, 0, 16, st), "memset");
+        check_cuda(cudaMemsetAsync(w.counters, 0, 32, st), "memset");
         while (true) {
-            check_cuda(cudaMemsetAsync(w.counters + 1, 0, 8, st), "memset");
+            check_cuda(cudaMemsetAsync(w.counters + 1, 0, 16, st), "memset");
             wf_regen_kernel<<<regen_grid, WF_BLOCK, 0, st>>>(p, w);
             check_cuda(cudaMemcpyAsync(host_count, w.counters + 1, 4, cudaMemcpyDeviceToHost, st), "count");
             check_cuda(cudaStreamSynchronize(st), "sync");
             uint32_t n = *host_count;
             if (n == 0) break;
             unsigned grid = (n + WF_BLOCK - 1) / WF_BLOCK;
-            if (counted) wf_extend_kernel<true><<<grid, WF_BLOCK, 0, st>>>(p, w);
-            else wf_extend_kernel<false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+            unsigned tgrid = std::min<unsigned>(trace_blocks, (n + TR_BLOCK - 1) / TR_BLOCK);
+            if (counted) wf_trace_kernel<true, false><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
+            else wf_trace_kernel<false, false><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
             wf_shade_kernel<<<grid, WF_BLOCK, 0, st>>>(p, w);
-            if (counted) wf_shadow_kernel<true><<<grid, WF_BLOCK, 0, st>>>(p, w);
-            else wf_shadow_kernel<false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+            if (counted) wf_trace_kernel<true, true><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
+            else wf_trace_kernel<false, true><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
         }
         wf_reduce_kernel<<<(WH + 255) / 256, 256, 0, st>>>(p, w, s0 + w.chunk_spp >= spp ? 1 : 0);
     }

@@ -88,8 +88,7 @@ CONSTANTS_DTYPE = np.dtype([("view", "<f4", (16,)), ("proj", "<f4", (16,)), ("pr
                             ("accumulated_frame_count", "<u4"), ("sample_count", "<u4"),
                             ("bounce_count", "<u4"), ("screen_size", "<u4", (2,)), ("tonemap", "<u4"),
                             ("light_sampling", "<u4")])
-NODE4_DTYPE = np.dtype([("origin", "<f4", (3,)), ("exp", "u1", (3,)), ("count", "u1"), ("child", "<u4", (4,)),
-                        ("qlo", "u1", (3, 4)), ("qhi", "u1", (3, 4)), ("pad", "<u4", (2,))])
+NODE4_DTYPE = np.dtype([("box", "<f4", (6, 4)), ("child", "<u4", (4,)), ("count", "<u4"), ("pad", "<u4", (3,))])
 TRI_RECORD_DTYPE = np.dtype([("v0", "<f4", (3,)), ("prim", "<u4"), ("v1", "<f4", (3,)), ("mesh", "<u4"),
                              ("v2", "<f4", (3,)), ("pad", "<u4")])
 
@@ -100,7 +99,7 @@ assert MESH_DTYPE.itemsize == 32
 assert INSTANCE_DTYPE.itemsize == 208
 assert EMISSIVE_DTYPE.itemsize == 36
 assert CONSTANTS_DTYPE.itemsize == 368
-assert NODE4_DTYPE.itemsize == 64
+assert NODE4_DTYPE.itemsize == 128
 assert TRI_RECORD_DTYPE.itemsize == 48
 
 
