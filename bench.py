@@ -332,7 +332,8 @@ def run_ours(a, dist: Dist):
                          "node_fetch_bytes_per_launch": node_bytes,
                          "node_fetch_frac": node_bytes / kernel_s / 1e9 / peak},
             "counters": {"rays": cnt.rays, "blas_nodes": cnt.blas_nodes, "tlas_nodes": cnt.tlas_nodes,
-                         "triangles": cnt.triangles, "instances": cnt.instances, "hits": cnt.hits},
+                         "triangles": cnt.triangles, "instances": cnt.instances, "hits": cnt.hits,
+                         "traversal_step_lane_occupancy": cnt.lane_steps / max(1, 32 * cnt.warp_steps)},
             "scene": {"blas_nodes": int(stats.blas_nodes), "tlas_nodes": int(stats.tlas_nodes),
                       "blas_levels": int(stats.blas_levels), "tlas_levels": int(stats.tlas_levels),
                       "device_bytes": int(stats.device_bytes), "build_ms": None},

@@ -159,6 +159,7 @@ typedef struct tt_scene_stats {
 /* Traversal counters from the instrumented render (roofline accounting). */
 typedef struct tt_traversal_counters {
     uint64_t rays, blas_nodes, tlas_nodes, triangles, instances, hits;
+    uint64_t warp_steps, lane_steps; /* wavefront traversal: warp steps and the active lanes summed over them */
 } tt_traversal_counters;
 
 /* ---------------------------------------------------------------- context */

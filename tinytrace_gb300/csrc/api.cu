@@ -75,7 +75,7 @@ struct SceneRes {
 
 // Slot pool and queues of the wavefront integrator, grown on demand and kept across frames.
 struct WavefrontBuffers {
-    DeviceBuffer org, dir, thr, acc, pa1, pa0, pe, hit, active, shadow, counters, samples, running;
+    DeviceBuffer org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, counters, samples, running;
     uint32_t slots = 0;
     uint64_t sample_items = 0;
     uint32_t pixels = 0;
@@ -259,6 +259,7 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
         b.pa0.alloc(16ull * slots);
         b.pe.alloc(16ull * slots);
         b.hit.alloc(16ull * slots);
+        b.hslot.alloc(4ull * slots);
         b.active.alloc(4ull * slots);
         b.shadow.alloc(32ull * slots);
         b.slots = slots;
@@ -281,6 +282,7 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
     w.pa0 = b.pa0.as<float4>();
     w.pe = b.pe.as<float4>();
     w.hit = b.hit.as<uint4>();
+    w.hslot = b.hslot.as<uint32_t>();
     w.active = b.active.as<uint32_t>();
     w.shadow = b.shadow.as<float4>();
     w.counters = b.counters.as<uint32_t>();
@@ -318,7 +320,7 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     ctx->integrate_timed = true;
     fetch_error_word(ctx);
     if (counted) {
-        unsigned long long h[6];
+        unsigned long long h[8];
         check_cuda(cudaMemcpyAsync(h, ctx->counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "copy");
         sync(ctx);
         out->rays = h[0];
@@ -327,6 +329,8 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
         out->triangles = h[3];
         out->instances = h[4];
         out->hits = h[5];
+        out->warp_steps = h[6];
+        out->lane_steps = h[7];
     }
 }
 

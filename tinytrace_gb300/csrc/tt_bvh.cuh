@@ -104,26 +104,22 @@ TT_HD bool intersect_triangle(const RayPre& r, f3 p0, f3 p1, f3 p2, bool cull_ba
     float U = Cx * By - Cy * Bx;
     float V = Ax * Cy - Ay * Cx;
     float W = Bx * Ay - By * Ax;
-    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {  // rare: resolve edges in double precision
         U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
         V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
         W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
     }
-    if (cull_back) {
-        if (U < 0.0f || V < 0.0f || W < 0.0f) return false;
-    } else {
-        if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
-    }
+    bool neg = U < 0.0f || V < 0.0f || W < 0.0f;
+    bool pos = U > 0.0f || V > 0.0f || W > 0.0f;
     float det = U + V + W;
-    if (det == 0.0f) return false;
     float T = U * (r.sz * Akz) + V * (r.sz * Bkz) + W * (r.sz * Ckz);
     float rcp = 1.0f / det;
     float t = T * rcp;
-    if (!(t >= tmin && t <= tmax)) return false;
+    bool ok = (cull_back ? !neg : !(neg && pos)) && det != 0.0f && t >= tmin && t <= tmax;
     t_out = t;
     u_out = V * rcp;
     v_out = W * rcp;
-    return true;
+    return ok;
 }
 
 TT_HD bool closer(float t, uint32_t inst, uint32_t prim, const Hit& best) {
@@ -196,9 +192,13 @@ TT_HD int node_hits(const uint4* nodes, uint32_t i, const NodeRay& r, float tmin
 TT_HD f3 tri_vertex(float4 v) { return f3{v.x, v.y, v.z}; }
 
 // Resumable closest-hit traversal through the TLAS/BLAS.  trace_init() sets a ray up and
-// trace_step() performs one unit of work (pop an entry, enter an instance, or visit one node
-// and test its leaf triangles); it returns true when the traversal is finished and the
-// result is in `best`.  `stack` is the thread's column in shared memory (element k at
+// trace_step() performs one step; it returns true when the traversal is finished and the
+// result is in `best`.  A step does at most one triangle test (from the lane's pending leaf
+// range) and at most one stack pop or node visit, so that the lanes of a warp execute the
+// same two pieces of code each step instead of one lane's long run of leaf triangles: a node
+// visit sorts its hit children by entry distance, makes the nearest internal child the next
+// node, makes the nearest leaf the pending triangle range when that range is empty, and
+// pushes the rest.  `stack` is the thread's column in shared memory (element k at
 // stack[k * stride]); `err` receives ERR_* bits when the stack or the iteration limit would
 // be exceeded, in which case the traversal ends.
 struct TraceState {
@@ -208,6 +208,7 @@ struct TraceState {
     Hit best;
     float tmin, tbest;
     uint32_t inst, cur, iterations;
+    uint32_t tri_next, tri_left;  // pending triangles of the current instance
     int sp;
     bool in_blas, have, cull;
 };
@@ -231,7 +232,20 @@ TT_HD void trace_init(TraceState& st, const DevScene& sc, f3 o, f3 d, float tmin
     st.sp = 0;
     st.cur = 0u;
     st.iterations = 0u;
+    st.tri_next = 0u;
+    st.tri_left = 0u;
     st.have = finite3(d) && sc.has_tlas != 0u;  // a NaN/inf direction or an empty scene misses
+}
+
+template <bool COUNT>
+__device__ __forceinline__ bool trace_push(TraceState& st, uint32_t* stack, int stride, uint32_t* err,
+                                           uint32_t v) {
+    if (st.sp >= TRAVERSAL_STACK) {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+        return false;
+    }
+    stack[(st.sp++) * stride] = v;
+    return true;
 }
 
 template <bool COUNT>
@@ -241,12 +255,39 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
         atomicOr(err, ERR_ITERATION_LIMIT);
         return true;
     }
+    // 1. one pending triangle
+    if (st.tri_left > 0u) {
+        const float4* tr = sc.tris + 3ull * st.tri_next;
+        float4 a = __ldg(tr + 0), b = __ldg(tr + 1), cc = __ldg(tr + 2);
+        if (COUNT) cnt.triangles++;
+        float t, u, v;
+        uint32_t prim = __float_as_uint(a.w);
+        bool better = intersect_triangle(st.rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), st.cull, st.tmin,
+                                         st.tbest, t, u, v) &&
+                      closer(t, st.inst, prim, st.best);
+        st.best.hit = better ? 1 : st.best.hit;
+        st.best.t = better ? t : st.best.t;
+        st.best.u = better ? u : st.best.u;
+        st.best.v = better ? v : st.best.v;
+        st.best.instance = better ? st.inst : st.best.instance;
+        st.best.prim = better ? prim : st.best.prim;
+        st.tbest = better ? t : st.tbest;
+        st.tri_next++;
+        st.tri_left--;
+    }
+    // 2. one pop or node visit
     if (!st.have) {
+        if (st.tri_left > 0u) return false;  // leave the instance only after its pending triangles
         if (st.sp == 0) return true;
         uint32_t e = stack[(--st.sp) * stride];
         if (e == STACK_MARKER) {
             st.in_blas = false;
             st.nr = node_ray(st.o, st.d, sc.tlas_bound);
+            return false;
+        }
+        if (st.in_blas && (e & CHILD_LEAF)) {  // a postponed leaf becomes the pending range
+            st.tri_next = leaf_first(e);
+            st.tri_left = leaf_count(e);
             return false;
         }
         st.cur = e;
@@ -268,11 +309,7 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
             st.have = false;
             return false;
         }
-        if (st.sp >= TRAVERSAL_STACK) {
-            atomicOr(err, ERR_STACK_OVERFLOW);
-            return true;
-        }
-        stack[(st.sp++) * stride] = STACK_MARKER;
+        if (!trace_push<COUNT>(st, stack, stride, err, STACK_MARKER)) return true;
         st.rp = ray_precompute(oo, od);
         st.nr = node_ray(oo, od, 1.0f);
         st.in_blas = true;
@@ -286,64 +323,54 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
     float tn[4];
     uint32_t ch[4];
     int mask = node_hits(st.in_blas ? sc.blas : sc.tlas, st.cur, st.nr, st.tmin, st.tbest, tn, ch);
-    // triangle leaves first (in child order)
-    if (st.in_blas) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            if (!((mask >> c) & 1) || !(ch[c] & CHILD_LEAF)) continue;
-            uint32_t f = leaf_first(ch[c]), k = leaf_count(ch[c]);
-            for (uint32_t q = f; q < f + k; ++q) {
-                const float4* tr = sc.tris + 3ull * q;
-                float4 a = __ldg(tr + 0), b = __ldg(tr + 1), cc = __ldg(tr + 2);
-                if (COUNT) cnt.triangles++;
-                float t, u, v;
-                uint32_t prim = __float_as_uint(a.w);
-                if (!intersect_triangle(st.rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), st.cull, st.tmin,
-                                        st.tbest, t, u, v))
-                    continue;
-                if (closer(t, st.inst, prim, st.best)) {
-                    st.best.hit = 1;
-                    st.best.t = t;
-                    st.best.u = u;
-                    st.best.v = v;
-                    st.best.instance = st.inst;
-                    st.best.prim = prim;
-                    st.tbest = t;
-                }
-            }
-        }
-    }
-    // remaining descendants: internal nodes (and instance leaves at the top level), sorted by
-    // entry distance; the nearest is visited next, the others are pushed.
     float key[4];
     uint32_t val[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        bool take = ((mask >> c) & 1) && (!st.in_blas || !(ch[c] & CHILD_LEAF)) && tn[c] <= st.tbest;
+        bool take = ((mask >> c) & 1) && tn[c] <= st.tbest;
         key[c] = take ? tn[c] : __int_as_float(0x7f800000);
         val[c] = take ? ch[c] : STACK_MARKER;
     }
-#define TT_SWAP(i, j)                                       \
-    if (key[j] < key[i]) {                                  \
-        float tk = key[i]; key[i] = key[j]; key[j] = tk;    \
-        uint32_t tv = val[i]; val[i] = val[j]; val[j] = tv; \
+#define TT_SWAP(i, j)                                                  \
+    {                                                                  \
+        bool sw = key[j] < key[i];                                     \
+        float k0 = sw ? key[j] : key[i], k1 = sw ? key[i] : key[j];    \
+        uint32_t v0 = sw ? val[j] : val[i], v1 = sw ? val[i] : val[j]; \
+        key[i] = k0; key[j] = k1; val[i] = v0; val[j] = v1;            \
     }
     TT_SWAP(0, 1) TT_SWAP(2, 3) TT_SWAP(0, 2) TT_SWAP(1, 3) TT_SWAP(1, 2)
 #undef TT_SWAP
-    st.have = false;
-    if (val[0] != STACK_MARKER) {
-        st.cur = val[0];
-        st.have = true;
+    // nearest internal child -> next node; nearest triangle leaf -> pending range if free;
+    // the other hit children are pushed, farthest first
+    int next = -1, leaf = -1, npush = 0;
+    uint32_t next_ref = 0u, leaf_ref = 0u;
+    bool push[4];
 #pragma unroll
-        for (int c = 3; c >= 1; --c) {
-            if (val[c] == STACK_MARKER) continue;
-            if (st.sp >= TRAVERSAL_STACK) {
-                atomicOr(err, ERR_STACK_OVERFLOW);
-                return true;
-            }
-            stack[(st.sp++) * stride] = val[c];
-        }
+    for (int c = 0; c < 4; ++c) {
+        bool valid = val[c] != STACK_MARKER;
+        bool is_leaf = st.in_blas && (val[c] & CHILD_LEAF);
+        bool take_leaf = valid && is_leaf && leaf < 0 && st.tri_left == 0u;
+        bool take_next = valid && !is_leaf && next < 0;
+        leaf = take_leaf ? c : leaf;
+        leaf_ref = take_leaf ? val[c] : leaf_ref;
+        next = take_next ? c : next;
+        next_ref = take_next ? val[c] : next_ref;
+        push[c] = valid && !take_leaf && !take_next;
+        npush += push[c] ? 1 : 0;
     }
+    if (st.sp + npush > TRAVERSAL_STACK) {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+        return true;
+    }
+#pragma unroll
+    for (int c = 3; c >= 0; --c) {
+        if (push[c]) stack[st.sp * stride] = val[c];
+        st.sp += push[c] ? 1 : 0;
+    }
+    st.tri_next = leaf >= 0 ? leaf_first(leaf_ref) : st.tri_next;
+    st.tri_left = leaf >= 0 ? leaf_count(leaf_ref) : st.tri_left;
+    st.have = next >= 0;
+    st.cur = next >= 0 ? next_ref : st.cur;
     return false;
 }
 

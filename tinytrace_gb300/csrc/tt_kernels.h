@@ -19,10 +19,12 @@ struct RenderParams {
 // Wavefront integrator (wavefront.cu): device pointers of the slot pool and queues.
 struct WfParams {
     float4 *org, *dir, *thr, *acc, *pa1, *pa0, *pe;
-    uint4* hit;
+    uint4* hit;          // shading queue: hit records
+    uint32_t* hslot;     // shading queue: slots
     uint32_t* active;
     float4* shadow;
-    uint32_t* counters;  // [0] next work item, [1] active paths, [2] shadow rays, [3]/[4] trace queue heads
+    uint32_t* counters;  // [0] next work item, [1] active paths, [2] shadow rays, [3]/[4] trace queue heads,
+                         // [5] shading queue length
     float4* samples;     // chunk_spp x WH per-sample radiance (band order)
     float4* running;     // WH running per-pixel sums across chunks
     uint32_t P, WH;

@@ -8,8 +8,9 @@
 //                       slots the next work items (camera ray: the pixel generator advanced by
 //                       2 draws per earlier sample, then the two jitter draws), and append the
 //                       live slots to the active queue;
-//   extend (active):    closest hit, back faces culled;
-//   shade  (active):    hit reconstruction, bsdf_prepare, next-event estimation (light sample
+//   extend (active):    closest hit, back faces culled; a miss adds the sky and ends the path,
+//                       a hit is appended to the shading queue;
+//   shade  (hits):      hit reconstruction, bsdf_prepare, next-event estimation (light sample
 //                       and its unoccluded contribution; the shadow ray goes to a queue),
 //                       emission, bsdf_sample and the throughput update;
 //   shadow (queue):     closest hit, light visibility, then the pending additions in the
@@ -19,7 +20,7 @@
 //
 // Slot state in HBM (structure of arrays, 16-byte records): origin + bounce, direction +
 // generator, throughput + work item, path radiance + flags; pending NEE additions (3 x 16 B);
-// hit record (16 B, by queue position); shadow queue entries (32 B).
+// shading queue (slot + 16-byte hit record); shadow queue entries (32 B).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -127,6 +128,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
     bool drained = false;  // warp-uniform: the queue has no more rays
     Counters cnt{0u, 0u, 0u, 0u};
     uint32_t rays = 0, hits = 0;
+    unsigned long long warp_steps = 0, lane_steps = 0;  // step-level lane occupancy (instrumented kernel)
     while (true) {
         if (!drained) {
             bool idle = !active;
@@ -160,10 +162,14 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
         }
         if (!__any_sync(0xffffffffu, active)) break;
         while (true) {
+            bool fin = false;
             if (active && trace_step<COUNT>(st, sc, stack, TR_BLOCK, p.err, cnt)) {
+                fin = true;
                 active = false;
-                const Hit& h = st.best;
-                if (SHADOW) {
+            }
+            const Hit& h = st.best;
+            if (SHADOW) {
+                if (fin) {
                     float4 a1 = w.pa1[slot];
                     uint32_t pflags = __float_as_uint(a1.w);
                     bool vis = light_visible(sc, h, light, pflags >> 16);
@@ -172,20 +178,35 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                     acc += vis ? xyz(a1) : xyz(w.pa0[slot]);
                     if (pflags & 1u) acc += xyz(w.pe[slot]);
                     w.acc[slot] = make_float4(acc.x, acc.y, acc.z, a4.w);
-                } else {
-                    w.hit[item] = h.hit ? make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim)
-                                        : make_uint4(0u, 0u, NO_HIT, 0u);
-                    if (COUNT && h.hit) hits++;
+                }
+            } else {
+                // hits go to the compacted shading queue; a miss adds the sky (integrate.glsl:272-276)
+                bool is_hit = fin && h.hit;
+                uint32_t pos = warp_append(&w.counters[5], is_hit);
+                if (is_hit) {
+                    w.hslot[pos] = slot;
+                    w.hit[pos] = make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim);
+                    if (COUNT) hits++;
+                } else if (fin) {
+                    f3 thr = xyz(w.thr[slot]);
+                    f3 acc = xyz(w.acc[slot]);
+                    acc += splat(1.0f) * thr;
+                    w.acc[slot] = pack(acc, F_TERM);
                 }
             }
             uint32_t am = __ballot_sync(0xffffffffu, active);
+            if (COUNT && (threadIdx.x & 31u) == 0u) {
+                warp_steps++;
+                lane_steps += (uint32_t)__popc(am);
+            }
             if (am == 0u || (!drained && __popc(am) < REFILL_LANES)) break;
         }
     }
     if (COUNT) {
-        unsigned long long v[6] = {rays, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles, cnt.instances, hits};
+        unsigned long long v[8] = {rays, cnt.blas_nodes, cnt.tlas_nodes, cnt.triangles, cnt.instances, hits,
+                                   warp_steps, lane_steps};
 #pragma unroll
-        for (int k = 0; k < 6; ++k) {
+        for (int k = 0; k < 8; ++k) {
             unsigned long long x = v[k];
             for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
             if ((threadIdx.x & 31) == 0 && x) atomicAdd(p.counters + k, x);
@@ -196,22 +217,19 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
 __global__ void __launch_bounds__(WF_BLOCK) wf_shade_kernel(const __grid_constant__ RenderParams p,
                                                             const __grid_constant__ WfParams w) {
     uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
-    uint32_t n = w.counters[1];
+    uint32_t n = w.counters[5];
     bool want_shadow = false;
     uint32_t s = 0, light = 0;
     f3 sh_org = splat(0.0f), sh_dir = splat(0.0f);
     if (q < n) {
         const tt_constants& c = p.c;
         const DevScene& sc = p.sc;
-        s = w.active[q];
+        s = w.hslot[q];
         uint4 hv = w.hit[q];
         float4 o4 = w.org[s], d4 = w.dir[s], t4 = w.thr[s], a4 = w.acc[s];
         f3 thr = xyz(t4), acc = xyz(a4), ray_dir = xyz(d4);
         uint32_t g = __float_as_uint(d4.w), bounce = __float_as_uint(o4.w);
-        if (hv.z == NO_HIT) {
-            acc += splat(1.0f) * thr;
-            w.acc[s] = pack(acc, F_TERM);
-        } else {
+        {
             ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
             const tt_material* material = sc.materials + hit.material_index;
             const MatC& mc = material->constants;
@@ -302,7 +320,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
         w.chunk_items = WH * w.chunk_spp;
         check_cuda(cudaMemsetAsync(w.counters, 0, 32, st), "memset");
         while (true) {
-            check_cuda(cudaMemsetAsync(w.counters + 1, 0, 16, st), "memset");
+            check_cuda(cudaMemsetAsync(w.counters + 1, 0, 20, st), "memset");
             wf_regen_kernel<<<regen_grid, WF_BLOCK, 0, st>>>(p, w);
             check_cuda(cudaMemcpyAsync(host_count, w.counters + 1, 4, cudaMemcpyDeviceToHost, st), "count");
             check_cuda(cudaStreamSynchronize(st), "sync");

@@ -136,7 +136,8 @@ class SceneStats(ctypes.Structure):
 
 
 class TraversalCounters(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_uint64) for n in ("rays", "blas_nodes", "tlas_nodes", "triangles", "instances", "hits")]
+    _fields_ = [(n, ctypes.c_uint64) for n in ("rays", "blas_nodes", "tlas_nodes", "triangles", "instances", "hits",
+                                               "warp_steps", "lane_steps")]
 
 
 # Every symbol declared in include/tinytrace_cuda.h: (name, restype, argtypes)
