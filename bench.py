@@ -53,6 +53,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--integrator", default="wavefront", choices=["wavefront", "megakernel"])
     p.add_argument("--slots", type=int, default=0, help="wavefront paths in flight (0 = library default)")
+    p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level"],
+                   help="acceleration structure (auto = flat up to 2^26 instanced triangles)")
     return p.parse_args()
 
 
@@ -238,6 +240,8 @@ def run_ours(a, dist: Dist):
     integ = native.TT_INTEGRATOR_WAVEFRONT if a.integrator == "wavefront" else native.TT_INTEGRATOR_MEGAKERNEL
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_INTEGRATOR, integ))
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_WAVEFRONT_SLOTS, a.slots))
+    accel = {"auto": native.TT_ACCEL_AUTO, "flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL}
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_ACCEL, accel[a.accel]))
     r.set_scene(w.scene)
     r.camera = w.camera
     r.set_config(w.config)
@@ -296,7 +300,7 @@ def run_ours(a, dist: Dist):
     cnt = native.TraversalCounters()
     c = r.constants()
     check(lib.tt_render_counted(ctx, r.scene, native.ptr(c), r.render_target, ctypes.byref(cnt)))
-    node_bytes = (cnt.blas_nodes + cnt.tlas_nodes) * 64
+    node_bytes = (cnt.blas_nodes + cnt.tlas_nodes) * 128
     tri_bytes = cnt.triangles * 48
     inst_bytes = cnt.instances * 64
     hit_bytes = cnt.hits * (208 + 12 + 18 + 24 + 304)
@@ -321,7 +325,8 @@ def run_ours(a, dist: Dist):
                        "resolution": [W, H], "spp": spp, "depth": w.config.bounce_count,
                        "light_sampling": "next_event_estimation",
                        "l2": "flushed before every step (512 MiB memset, inside the timed region)",
-                       "parallelism": f"replicas x{dist.world}", "integrator": a.integrator},
+                       "parallelism": f"replicas x{dist.world}", "integrator": a.integrator,
+                       "accel": "flat" if stats.accel == native.TT_ACCEL_FLAT else "two_level"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 368, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -61,6 +61,11 @@ extern "C" {
 /* context options */
 #define TT_OPTION_INTEGRATOR 1      /* TT_INTEGRATOR_*; default wavefront */
 #define TT_OPTION_WAVEFRONT_SLOTS 2 /* paths in flight of the wavefront integrator; 0 = default */
+#define TT_OPTION_ACCEL 3           /* TT_ACCEL_*: structure built by later tt_scene_create calls */
+/* acceleration structures (tt_set_option TT_OPTION_ACCEL; tt_scene_stats.accel) */
+#define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
+#define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */
+#define TT_ACCEL_TWO_LEVEL 2 /* per-mesh BLAS under a TLAS over instances */
 
 /* trace flags */
 #define TT_TRACE_CULL_BACK_FACES 1u
@@ -149,11 +154,15 @@ typedef struct tt_timings {
     uint64_t scene_build_ns;
 } tt_timings;
 
+/* Scene statistics.  triangle_count counts the triangle records of the structure: the mesh
+ * triangles (two-level) or the instanced triangles (flat).  For a flat scene the tlas fields
+ * describe the flat BVH and the blas fields are zero. */
 typedef struct tt_scene_stats {
     uint64_t triangle_count, instance_count, emissive_count;
     uint64_t blas_nodes, tlas_nodes, blas_levels, tlas_levels;
     uint64_t device_bytes;
     uint64_t max_stack;
+    uint64_t accel; /* TT_ACCEL_FLAT or TT_ACCEL_TWO_LEVEL */
 } tt_scene_stats;
 
 /* Traversal counters from the instrumented render (roofline accounting). */
@@ -193,8 +202,9 @@ int32_t tt_image_download(tt_context* ctx, tt_handle image, float* host, uint64_
  * (crates/tinytrace_backend/src/resource.rs:728-880, 891-1085), which become a GPU LBVH. */
 int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* desc, tt_handle* out);
 int32_t tt_scene_stats_get(tt_context* ctx, tt_handle scene, tt_scene_stats* out);
-/* BVH arrays for node-for-node comparison: blas nodes (64 B each), triangle records
- * (48 B each), tlas nodes (64 B each).  Sizes in bytes must match tt_scene_stats. */
+/* BVH arrays for node-for-node comparison: blas nodes (128 B each), triangle records
+ * (48 B each), tlas nodes (128 B each; the flat BVH of a flat scene).  Sizes in bytes must
+ * match tt_scene_stats. */
 int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint64_t blas_bytes,
                               void* tris, uint64_t tri_bytes, void* tlas, uint64_t tlas_bytes);
 

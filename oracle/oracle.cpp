@@ -267,13 +267,22 @@ void* oracle_scene_create(const OracleSceneDesc* d, int use_bvh, int leaf_max) {
 void oracle_scene_destroy(void* p) { delete static_cast<OracleScene*>(p); }
 
 // BVH arrays for node-for-node comparison with the GPU build.
-void oracle_scene_bvh_info(void* p, uint64_t* out /* blas_nodes, tris, tlas_nodes, blas_levels, tlas_levels */) {
+void oracle_scene_bvh_info(void* p, uint64_t* out /* blas_nodes, tris, tlas_nodes, blas_levels, tlas_levels,
+                                                    flat_nodes, flat_tris, flat_levels */) {
     OracleScene* s = static_cast<OracleScene*>(p);
     out[0] = s->bvh.blas.size();
     out[1] = s->bvh.tris.size();
     out[2] = s->bvh.tlas.size();
     out[3] = (uint64_t)s->bvh.blas_levels;
     out[4] = (uint64_t)s->bvh.tlas_levels;
+    out[5] = s->bvh.flat.size();
+    out[6] = s->bvh.flat_tris.size();
+    out[7] = (uint64_t)s->bvh.flat_levels;
+}
+void oracle_scene_flat_copy(void* p, void* nodes, void* tris) {
+    OracleScene* s = static_cast<OracleScene*>(p);
+    if (nodes) std::memcpy(nodes, s->bvh.flat.data(), s->bvh.flat.size() * sizeof(Node4));
+    if (tris) std::memcpy(tris, s->bvh.flat_tris.data(), s->bvh.flat_tris.size() * sizeof(TriRecord));
 }
 void oracle_scene_bvh_copy(void* p, void* blas, void* tris, void* tlas) {
     OracleScene* s = static_cast<OracleScene*>(p);
@@ -283,7 +292,8 @@ void oracle_scene_bvh_copy(void* p, void* blas, void* tris, void* tlas) {
 }
 
 // rays: n x 8 floats (origin xyz, tmin, direction xyz, tmax); hits: n x 8 words
-// (hit, t, u, v, instance, prim, 0, 0).  flags bit0 = cull back faces, bit1 = brute force.
+// (hit, t, u, v, instance, prim, 0, 0).  flags bit0 = cull back faces, bit1 = brute force,
+// bit2 = the flat BVH.
 void oracle_trace_batch(void* p, const float* rays, uint32_t n, uint32_t flags, uint32_t* hits,
                         int threads) {
     OracleScene* s = static_cast<OracleScene*>(p);
@@ -297,7 +307,8 @@ void oracle_trace_batch(void* p, const float* rays, uint32_t n, uint32_t flags, 
         bool cull = flags & 1u;
         Geometry g = s->geom();
         Hit h = (flags & 2u) || !s->use_bvh ? trace_brute(g, o, d, r[3], r[7], cull)
-                                            : trace_bvh(g, s->bvh, o, d, r[3], r[7], cull);
+                : (flags & 4u)                  ? trace_flat(g, s->bvh, o, d, r[3], r[7], cull)
+                                                : trace_bvh(g, s->bvh, o, d, r[3], r[7], cull);
         uint32_t* out = hits + 8 * i;
         out[0] = (uint32_t)h.hit;
         out[1] = h.hit ? fbits(h.t) : 0u;

@@ -34,6 +34,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_scene_destroy.argtypes = [_P]
         lib.oracle_scene_bvh_info.argtypes = [_P, _P]
         lib.oracle_scene_bvh_copy.argtypes = [_P, _P, _P, _P]
+        lib.oracle_scene_flat_copy.argtypes = [_P, _P, _P]
         lib.oracle_trace_batch.argtypes = [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_int]
         lib.oracle_render.argtypes = [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                       ctypes.c_uint32, ctypes.c_int]
@@ -70,7 +71,7 @@ class OracleScene:
     def bvh(self):
         from tinytrace_gb300.native import NODE4_DTYPE, TRI_RECORD_DTYPE
 
-        info = np.zeros(5, np.uint64)
+        info = np.zeros(8, np.uint64)
         self.lib.oracle_scene_bvh_info(self.handle, _p(info))
         blas = np.zeros(int(info[0]), NODE4_DTYPE)
         tris = np.zeros(int(info[1]), TRI_RECORD_DTYPE)
@@ -78,10 +79,20 @@ class OracleScene:
         self.lib.oracle_scene_bvh_copy(self.handle, _p(blas), _p(tris), _p(tlas))
         return blas, tris, tlas, int(info[3]), int(info[4])
 
-    def trace(self, rays: np.ndarray, cull: bool, brute: bool = False, threads: int = 0) -> np.ndarray:
+    def flat_bvh(self):
+        from tinytrace_gb300.native import NODE4_DTYPE, TRI_RECORD_DTYPE
+
+        info = np.zeros(8, np.uint64)
+        self.lib.oracle_scene_bvh_info(self.handle, _p(info))
+        nodes = np.zeros(int(info[5]), NODE4_DTYPE)
+        tris = np.zeros(int(info[6]), TRI_RECORD_DTYPE)
+        self.lib.oracle_scene_flat_copy(self.handle, _p(nodes), _p(tris))
+        return nodes, tris, int(info[7])
+
+    def trace(self, rays: np.ndarray, cull: bool, brute: bool = False, threads: int = 0, flat: bool = False) -> np.ndarray:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
         hits = np.zeros((len(rays), 8), np.uint32)
-        flags = (1 if cull else 0) | (2 if brute else 0)
+        flags = (1 if cull else 0) | (2 if brute else 0) | (4 if flat else 0)
         self.lib.oracle_trace_batch(self.handle, _p(rays), len(rays), flags, _p(hits), threads)
         return hits
 

@@ -472,7 +472,51 @@ struct SceneBvh {
     std::vector<Node4> tlas;   // root = 0
     int blas_levels = 0, tlas_levels = 0;
     float tlas_bound = 0.0f;   // max |coordinate| of the instance world boxes
+    // single-level ("flat") BVH over the world boxes of every (instance, triangle) pair;
+    // its triangle records keep object-space vertices and hold the instance in `mesh`
+    std::vector<Node4> flat;
+    std::vector<TriRecord> flat_tris;
+    int flat_levels = 0;
+    float flat_bound = 0.0f;   // max |coordinate| of the triangle world boxes
 };
+
+// The flat BVH: primitives are the (instance, triangle) pairs in instance order; a primitive's
+// box is the box of its three vertices transformed to world space.
+inline void build_flat_bvh(const Geometry& g, int leaf_max, SceneBvh& s) {
+    std::vector<Aabb> boxes;
+    std::vector<uint32_t> seg;
+    std::vector<TriRecord> recs;
+    for (uint32_t i = 0; i < g.instance_count; ++i) {
+        const Instance& in = g.instances[i];
+        const Mesh& me = g.meshes[in.mesh_index];
+        uint32_t tris = me.index_count / 3u;
+        for (uint32_t p = 0; p < tris; ++p) {
+            v3 q[3];
+            triangle_object(g, in, p, q[0], q[1], q[2]);
+            v3 w0 = mat43_point(in.transform, q[0]), w1 = mat43_point(in.transform, q[1]),
+               w2 = mat43_point(in.transform, q[2]);
+            Aabb b = canon_box(aabb_point(aabb_point(Aabb{w0, w0}, w1), w2));
+            boxes.push_back(b);
+            seg.push_back(0);
+            const float* lo = &b.lo.x;
+            const float* hi = &b.hi.x;
+            for (int a = 0; a < 3; ++a) s.flat_bound = fmx(s.flat_bound, fmx(std::fabs(lo[a]), std::fabs(hi[a])));
+            TriRecord tr;
+            tr.v0[0] = q[0].x; tr.v0[1] = q[0].y; tr.v0[2] = q[0].z;
+            tr.v1[0] = q[1].x; tr.v1[1] = q[1].y; tr.v1[2] = q[1].z;
+            tr.v2[0] = q[2].x; tr.v2[1] = q[2].y; tr.v2[2] = q[2].z;
+            tr.prim = p;
+            tr.mesh = i;
+            tr.pad = 0;
+            recs.push_back(tr);
+        }
+    }
+    BvhBuild b = build_bvh4(boxes, seg, 1, leaf_max, false);
+    s.flat = b.nodes;
+    s.flat_levels = b.levels;
+    s.flat_tris.resize(recs.size());
+    for (size_t k = 0; k < recs.size(); ++k) s.flat_tris[k] = recs[b.order[k]];
+}
 
 // BLAS over all meshes (segment = mesh) and TLAS over instances (leaf = instance index).
 inline SceneBvh build_scene_bvh(const Geometry& g, int leaf_max) {
@@ -539,6 +583,7 @@ inline SceneBvh build_scene_bvh(const Geometry& g, int leaf_max) {
             if (nd.child[c] & CHILD_LEAF) nd.child[c] = leaf_ref(ids[leaf_first(nd.child[c])], 1u);
     s.tlas = tb.nodes;
     s.tlas_levels = tb.levels;
+    build_flat_bvh(g, leaf_max, s);
     return s;
 }
 
@@ -604,6 +649,53 @@ inline Hit trace_bvh(const Geometry& g, const SceneBvh& s, v3 o, v3 d, float tmi
                 trace_blas(s, in.mesh_index, inst, rp, nr, cull_back, tmin, best, tbest);
             } else {
                 stack[sp++] = ch;
+            }
+        }
+    }
+    return best;
+}
+
+// Closest hit through the flat BVH: each triangle is tested in its instance's object space.
+inline Hit trace_flat(const Geometry& g, const SceneBvh& s, v3 o, v3 d, float tmin, float tmax, bool cull_back) {
+    Hit best{0, 0.0f, 0.0f, 0.0f, 0u, 0u};
+    if (!finite3(d) || s.flat.empty()) return best;
+    float tbest = tmax;
+    NodeRay wr = node_ray(o, d, s.flat_bound);
+    uint32_t cur = 0xffffffffu;
+    bool skip = false;  // the object ray of instance `cur` is not finite: its triangles miss
+    RayPre rp{};
+    uint32_t stack[256];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const Node4& nd = s.flat[stack[--sp]];
+        float tn[4];
+        int mask = node_hits(nd, wr, tmin, tbest, tn);
+        for (int c = 0; c < (int)nd.count; ++c) {
+            if (!(mask & (1 << c))) continue;
+            uint32_t ch = nd.child[c];
+            if (!(ch & CHILD_LEAF)) {
+                stack[sp++] = ch;
+                continue;
+            }
+            for (uint32_t q = leaf_first(ch); q < leaf_first(ch) + leaf_count(ch); ++q) {
+                const TriRecord& tr = s.flat_tris[q];
+                if (tr.mesh != cur) {
+                    cur = tr.mesh;
+                    v3 oo, od;
+                    object_ray(g.instances[cur], o, d, oo, od);
+                    skip = !finite3(od);
+                    rp = ray_precompute(oo, od);
+                }
+                float t, u, v;
+                if (skip) continue;
+                if (!intersect_triangle(rp, v3{tr.v0[0], tr.v0[1], tr.v0[2]}, v3{tr.v1[0], tr.v1[1], tr.v1[2]},
+                                        v3{tr.v2[0], tr.v2[1], tr.v2[2]}, cull_back, tmin, tbest, t, u, v))
+                    continue;
+                if (closer(t, cur, tr.prim, best)) {
+                    best = Hit{1, t, u, v, cur, tr.prim};
+                    tbest = t;
+                }
             }
         }
     }

@@ -76,17 +76,43 @@ def _small_field():
     return scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11)
 
 
+ACCELS = {"flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL}
+
+
+def _create_scene(ctx, arrays, accel):
+    check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_ACCEL, ACCELS[accel]))
+    try:
+        return ctx.create_scene(arrays)
+    finally:
+        check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_ACCEL, native.TT_ACCEL_AUTO))
+
+
+@pytest.mark.parametrize("accel", ["two_level", "flat"])
 @pytest.mark.parametrize("name", ["cornell", "field"])
-def test_bvh_topology_bits(gpu_context, name):
+def test_bvh_topology_bits(gpu_context, name, accel):
     scene = scenes.cornell_box() if name == "cornell" else _small_field()
     arrays = SceneArrays(scene)
-    h = gpu_context.create_scene(arrays)
+    h = _create_scene(gpu_context, arrays, accel)
     blas, tris, tlas, st = _gpu_bvh(gpu_context, h)
-    ob, ot, otl, bl, tl = oracle.OracleScene(arrays).bvh()
-    assert (st.blas_levels, st.tlas_levels) == (bl, tl)
-    assert blas.tobytes() == ob.tobytes(), "BLAS nodes differ"
-    assert tris.tobytes() == ot.tobytes(), "triangle records differ"
-    assert tlas.tobytes() == otl.tobytes(), "TLAS nodes differ"
+    orc = oracle.OracleScene(arrays)
+    if accel == "two_level":
+        assert st.accel == native.TT_ACCEL_TWO_LEVEL
+        ob, ot, otl, bl, tl = orc.bvh()
+        assert (st.blas_levels, st.tlas_levels) == (bl, tl)
+        assert blas.tobytes() == ob.tobytes(), "BLAS nodes differ"
+        assert tris.tobytes() == ot.tobytes(), "triangle records differ"
+        assert tlas.tobytes() == otl.tobytes(), "TLAS nodes differ"
+    else:
+        assert st.accel == native.TT_ACCEL_FLAT
+        on, ot, ol = orc.flat_bvh()
+        assert st.blas_nodes == 0 and st.tlas_levels == ol
+        assert tris.tobytes() == ot.tobytes(), "flat triangle records differ"
+        assert tlas.tobytes() == on.tobytes(), "flat BVH nodes differ"
+
+
+def test_accel_auto_is_flat(gpu_context):
+    h = gpu_context.create_scene(SceneArrays(scenes.cornell_box()))
+    assert gpu_context.scene_stats(h).accel == native.TT_ACCEL_FLAT
 
 
 def _random_rays(rng, n, center, spread):
@@ -100,11 +126,12 @@ def _random_rays(rng, n, center, spread):
     return rays
 
 
+@pytest.mark.parametrize("accel", ["two_level", "flat"])
 @pytest.mark.parametrize("name", ["cornell", "field"])
-def test_closest_hit_matches_brute_force(gpu_context, name):
+def test_closest_hit_matches_brute_force(gpu_context, name, accel):
     scene = scenes.cornell_box() if name == "cornell" else _small_field()
     arrays = SceneArrays(scene)
-    h = gpu_context.create_scene(arrays)
+    h = _create_scene(gpu_context, arrays, accel)
     rng = np.random.default_rng(5)
     center, spread = ((0, 1, 0), 1.2) if name == "cornell" else ((0, 0, 0), 60.0)
     rays = _random_rays(rng, 20000, np.array(center), spread)
@@ -120,7 +147,7 @@ def test_closest_hit_matches_brute_force(gpu_context, name):
         check(gpu_context.lib.tt_trace_batch(gpu_context.handle, h, native.ptr(rays), len(rays),
                                              1 if cull else 0, native.ptr(hits)))
         brute = orc.trace(rays, cull=cull, brute=True)
-        bvh = orc.trace(rays, cull=cull, brute=False)
+        bvh = orc.trace(rays, cull=cull, brute=False, flat=accel == "flat")
         assert np.array_equal(bvh, brute), "oracle BVH traversal differs from brute force"
         assert np.array_equal(hits, brute), f"GPU closest hits differ (cull={cull}): {np.sum(np.any(hits != brute, 1))}"
         assert hits[:, 0].sum() > len(rays) // 20
@@ -129,12 +156,13 @@ def test_closest_hit_matches_brute_force(gpu_context, name):
 INTEGRATORS = {"wavefront": native.TT_INTEGRATOR_WAVEFRONT, "megakernel": native.TT_INTEGRATOR_MEGAKERNEL}
 
 
-def _render_pair(ctx, w, frames=1, integrator="wavefront", slots=0):
+def _render_pair(ctx, w, frames=1, integrator="wavefront", slots=0, accel="flat"):
     from tinytrace_gb300.renderer import Renderer
 
     r = Renderer(w.extent)
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_INTEGRATOR, INTEGRATORS[integrator]))
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_WAVEFRONT_SLOTS, slots))
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_ACCEL, ACCELS[accel]))
     r.set_scene(w.scene)
     r.camera = w.camera
     r.set_config(w.config)
@@ -150,9 +178,10 @@ def _render_pair(ctx, w, frames=1, integrator="wavefront", slots=0):
     return gpu
 
 
+@pytest.mark.parametrize("accel", ["flat", "two_level"])
 @pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
-def test_render_cornell_c1(gpu_context, integrator):
-    img = _render_pair(gpu_context, scenes.cornell_workload(), integrator=integrator)
+def test_render_cornell_c1(gpu_context, integrator, accel):
+    img = _render_pair(gpu_context, scenes.cornell_workload(), integrator=integrator, accel=accel)
     assert img[..., :3].mean() > 0.05
 
 
@@ -163,11 +192,12 @@ def test_render_accumulation(gpu_context, integrator):
                  integrator=integrator)
 
 
+@pytest.mark.parametrize("accel", ["flat", "two_level"])
 @pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
-def test_render_field_small(gpu_context, integrator):
+def test_render_field_small(gpu_context, integrator, accel):
     w = scenes.Workload("field_small", _small_field(), scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)),
                         (96, 54), scenes.Config(bounce_count=8, sample_count=3))
-    _render_pair(gpu_context, w, integrator=integrator)
+    _render_pair(gpu_context, w, integrator=integrator, accel=accel)
 
 
 def test_render_wavefront_small_pool_and_chunks(gpu_context):

@@ -1,0 +1,184 @@
+"""Analytic properties of the oracle's OpenPBR BSDF (CPU only).
+
+The reference's tests pin no BSDF value (its material harness asserts nothing), so the
+restatement of src/material/*.glsl is checked against properties the model must have:
+
+* bsdf_sample and bsdf_evaluate describe the same distribution: evaluating at a sampled
+  direction, with the same generator seed (so the same stochastic lobe albedos), returns
+  the sampled value and mixture pdf, and the sampled estimator of the directional albedo
+  agrees with a uniform-sphere estimator built from bsdf_evaluate alone;
+* energy: the directional albedo of a material with white colours stays at or below one;
+* the Lambertian limit (Oren-Nayar roughness 0, no specular) has albedo equal to
+  base_weight * base_color, is reciprocal and has the cosine pdf.
+"""
+import numpy as np
+import pytest
+
+from materials import material_suite, random_directions
+from oracle import oracle
+from tinytrace_gb300.asset import Material
+
+
+def _eval(m, wi, wo, seeds):
+    n = len(wi)
+    s = np.zeros((n, 8), np.float32)
+    s[:, 0:3] = wi
+    s[:, 3] = seeds.astype(np.uint32).view(np.float32)
+    s[:, 4:7] = wo
+    return oracle.bsdf_eval(np.ascontiguousarray(m), s)
+
+
+def _sample(m, wi, seeds):
+    n = len(wi)
+    s = np.zeros((n, 4), np.float32)
+    s[:, 0:3] = wi
+    s[:, 3] = seeds.astype(np.uint32).view(np.float32)
+    return oracle.bsdf_sample(np.ascontiguousarray(m), s)
+
+
+def _wi(theta_deg: float, n: int) -> np.ndarray:
+    t = np.radians(theta_deg)
+    return np.tile(np.array([np.sin(t), 0.0, np.cos(t)], np.float32), (n, 1))
+
+
+def _seeds(rng, n):
+    return rng.integers(1, 2**32, n, dtype=np.uint64).astype(np.uint32)
+
+
+ROUGH = [
+    Material(),
+    Material(specular_weight=0.0, base_diffuse_roughness=0.5),
+    Material(base_metalness=1.0, specular_roughness=0.5),
+    Material(coat_weight=1.0, coat_roughness=0.4, specular_roughness=0.5),
+    Material(fuzz_weight=1.0, fuzz_roughness=0.5),
+    Material(transmission_weight=1.0, specular_roughness=0.5),
+    Material(specular_roughness=0.6, specular_roughness_anisotropy=0.6, specular_rotation=0.2),
+]
+
+
+@pytest.mark.parametrize("k", range(len(ROUGH)))
+def test_sample_matches_evaluate(k):
+    """f and pdf returned by bsdf_sample equal bsdf_evaluate at the sampled direction."""
+    m = ROUGH[k].constants()
+    rng = np.random.default_rng(100 + k)
+    n = 20000
+    wi = random_directions(rng, n)
+    wi[:, 2] = np.abs(wi[:, 2]) + 0.05
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    seeds = _seeds(rng, n)
+    smp = _sample(m, wi, seeds)
+    # lobe -1: no lobe selected (every stochastic albedo estimate was zero); f = 0, pdf = 1
+    ok = (smp[:, 7] >= 0) & (smp[:, 3] > 1e-3) & np.all(np.isfinite(smp[:, :7]), axis=1)
+    assert ok.mean() > 0.5
+    ev = _eval(m, wi[ok], smp[ok, 4:7], seeds[ok])
+    f_s, f_e = smp[ok, 0:3].astype(np.float64), ev[:, 0:3].astype(np.float64)
+    p_s, p_e = smp[ok, 3].astype(np.float64), ev[:, 3].astype(np.float64)
+    rel_f = np.abs(f_s - f_e).max(axis=1) / np.maximum(np.abs(f_e).max(axis=1), 1e-3)
+    rel_p = np.abs(p_s - p_e) / np.maximum(p_e, 1e-3)
+    # the sampled lobe's value comes from its sampling routine; allow float rounding only
+    assert np.mean(rel_f < 1e-3) > 0.995, np.percentile(rel_f, 99.9)
+    assert np.mean(rel_p < 1e-3) > 0.995, np.percentile(rel_p, 99.9)
+
+
+def _albedo_sampled(m, wi, seeds):
+    smp = _sample(m, wi, seeds)
+    w = smp[:, 0:3].astype(np.float64) * np.abs(smp[:, 6:7]) / np.maximum(smp[:, 3:4], 1e-6)
+    w[~np.isfinite(w).all(axis=1)] = 0.0
+    return w.mean(axis=0), w.std(axis=0) / np.sqrt(len(w))
+
+
+def _albedo_uniform(m, wi, seeds, rng):
+    wo = random_directions(rng, len(wi))
+    ev = _eval(m, wi, wo, seeds)
+    w = ev[:, 0:3].astype(np.float64) * np.abs(wo[:, 2:3]) * (4.0 * np.pi)
+    return w.mean(axis=0), w.std(axis=0) / np.sqrt(len(w))
+
+
+@pytest.mark.parametrize("k", range(len(ROUGH)))
+@pytest.mark.parametrize("theta", [10.0, 60.0])
+def test_sampled_albedo_matches_uniform_estimate(k, theta):
+    """E[f |cos| / pdf] under bsdf_sample equals the integral of f |cos| from bsdf_evaluate."""
+    m = ROUGH[k].constants()
+    rng = np.random.default_rng(200 + k)
+    n = 200000
+    wi = _wi(theta, n)
+    a_s, e_s = _albedo_sampled(m, wi, _seeds(rng, n))
+    a_u, e_u = _albedo_uniform(m, wi, _seeds(rng, n), rng)
+    tol = 5.0 * np.sqrt(e_s**2 + e_u**2) + 0.01
+    assert np.all(np.abs(a_s - a_u) < tol), (a_s, a_u, tol)
+
+
+@pytest.mark.parametrize("k", range(len(ROUGH)))
+def test_white_furnace_energy(k):
+    """With white colours no material reflects or transmits more energy than arrives."""
+    mat = ROUGH[k]
+    mat.base_color = (1.0, 1.0, 1.0)
+    m = mat.constants()
+    rng = np.random.default_rng(300 + k)
+    n = 200000
+    for theta in (0.0, 45.0, 80.0):
+        a, err = _albedo_sampled(m, _wi(theta, n), _seeds(rng, n))
+        assert np.all(a < 1.0 + 5 * err + 0.01), (theta, a)
+
+
+def test_lambertian_limit():
+    base = np.array([0.9, 0.5, 0.25])
+    m = Material(specular_weight=0.0, base_diffuse_roughness=0.0, base_weight=0.8,
+                 base_color=tuple(base)).constants()
+    rng = np.random.default_rng(5)
+    n = 50000
+    wi = random_directions(rng, n)
+    wi[:, 2] = np.abs(wi[:, 2])
+    wo = random_directions(rng, n)
+    wo[:, 2] = np.abs(wo[:, 2])
+    seeds = _seeds(rng, n)
+    ev = _eval(m, wi, wo, seeds)
+    expect = 0.8 * base / np.pi
+    assert np.allclose(ev[:, 0:3], expect, rtol=1e-5)
+    assert np.allclose(ev[:, 3], wo[:, 2] / np.pi, rtol=1e-5, atol=1e-7)
+    rev = _eval(m, wo, wi, seeds)
+    assert np.allclose(ev[:, 0:3], rev[:, 0:3], rtol=1e-6)
+    a, _ = _albedo_sampled(m, _wi(30.0, n), seeds)
+    assert np.allclose(a, 0.8 * base, rtol=1e-4)
+
+
+def test_oren_nayar_reciprocity():
+    m = Material(specular_weight=0.0, base_diffuse_roughness=0.8).constants()
+    rng = np.random.default_rng(6)
+    n = 50000
+    wi = random_directions(rng, n)
+    wi[:, 2] = np.abs(wi[:, 2]) + 1e-3
+    wo = random_directions(rng, n)
+    wo[:, 2] = np.abs(wo[:, 2]) + 1e-3
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    seeds = _seeds(rng, n)
+    a = _eval(m, wi, wo, seeds)[:, 0:3]
+    b = _eval(m, wo, wi, seeds)[:, 0:3]
+    assert np.allclose(a, b, rtol=2e-4, atol=1e-7)
+
+
+def test_below_surface_is_black_for_opaque_materials():
+    """Reflection-only materials return zero for directions on opposite sides."""
+    for mat in (Material(specular_weight=0.0), Material(base_metalness=1.0, specular_roughness=0.3)):
+        m = mat.constants()
+        rng = np.random.default_rng(8)
+        n = 5000
+        wi = random_directions(rng, n)
+        wi[:, 2] = np.abs(wi[:, 2]) + 0.01
+        wo = random_directions(rng, n)
+        wo[:, 2] = -np.abs(wo[:, 2]) - 0.01
+        ev = _eval(m, wi, wo, _seeds(rng, n))
+        assert np.all(ev[:, 0:3] == 0.0)
+
+
+def test_suite_outputs_are_finite():
+    rng = np.random.default_rng(9)
+    for m in material_suite():
+        n = 2000
+        wi = random_directions(rng, n)
+        wi[:, 2] = np.abs(wi[:, 2]) + 0.01
+        wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+        smp = _sample(m, wi, _seeds(rng, n))
+        assert np.isfinite(smp[:, 0:8]).all()
+        assert (smp[:, 3] >= 0).all()

@@ -60,6 +60,7 @@ constexpr int LIFETIMES = 5;
 constexpr int EVENT_SLOTS = 16;
 constexpr size_t L2_FLUSH_BYTES = 512ull << 20;
 constexpr int BLAS_LEAF_MAX = 3;
+constexpr uint64_t FLAT_AUTO_MAX_TRIANGLES = 1ull << 26;
 
 struct ImageRes {
     DeviceBuffer buf;
@@ -105,6 +106,7 @@ struct tt_context {
     bool err_pending = false;
     uint32_t integrator = TT_INTEGRATOR_WAVEFRONT;
     uint32_t wavefront_slots = 0;  // 0 = default
+    uint32_t accel = TT_ACCEL_AUTO;
     tt::WavefrontBuffers wf;
 };
 
@@ -192,6 +194,7 @@ void validate_scene(const tt_scene_desc* d) {
         tris += me.index_count / 3u;
     }
     require(tris < (1ull << 27), "more than 2^27 triangles in one scene");
+    require(d->instance_count < (1ull << 27), "more than 2^27 instances in one scene");
     for (uint32_t i = 0; i < d->instance_count; ++i) {
         const tt_instance& in = d->instances[i];
         require(in.mesh_index < d->mesh_count, "instance mesh_index out of range");
@@ -507,7 +510,12 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         upload(s->inst_xform, xf.data(), xf.size(), st);
         BuildInput bi{s->positions.as<int16_t>(), s->indices.as<uint32_t>(), d->meshes, d->mesh_count,
                       d->instances, d->instance_count};
-        build_scene_bvh(bi, st, BLAS_LEAF_MAX, s->bvh);
+        uint64_t instanced = 0;
+        for (uint32_t i = 0; i < d->instance_count; ++i) instanced += d->meshes[d->instances[i].mesh_index].index_count / 3u;
+        bool flat = ctx->accel == TT_ACCEL_FLAT || (ctx->accel == TT_ACCEL_AUTO && instanced <= FLAT_AUTO_MAX_TRIANGLES);
+        if (flat && instanced >= (1ull << 27))
+            fail(TT_ERR_OVERFLOW, "more than 2^27 instanced triangles for the flat BVH");
+        build_scene_bvh(bi, st, BLAS_LEAF_MAX, flat, s->bvh);
         check_cuda(cudaEventRecord(e1, st), "event");
         check_cuda(cudaEventSynchronize(e1), "event");
         float ms = 0.0f;
@@ -515,7 +523,8 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         ctx->scene_build_ms = ms;
-        uint64_t need_stack = 3ull * (s->bvh.blas_levels + s->bvh.tlas_levels) + 1ull;
+        uint64_t need_stack = flat ? 3ull * s->bvh.flat_levels + 1ull
+                                   : 3ull * (s->bvh.blas_levels + s->bvh.tlas_levels) + 1ull;
         if (need_stack > (uint64_t)TRAVERSAL_STACK)
             fail(TT_ERR_OVERFLOW, "scene BVH is too deep for the traversal stack (" +
                                       std::to_string(need_stack) + " entries needed)");
@@ -526,25 +535,41 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.materials = s->materials.as<tt_material>();
         ds.instances = s->instances.as<tt_instance>();
         ds.emissive = s->emissive.as<tt_emissive_triangle>();
-        ds.blas = s->bvh.blas.as<uint4>();
-        ds.tris = s->bvh.tris.as<float4>();
-        ds.tlas = s->bvh.tlas.as<uint4>();
         ds.inst_xform = s->inst_xform.as<float4>();
         ds.emissive_count = d->emissive_triangle_count;
         ds.instance_count = d->instance_count;
-        ds.has_tlas = s->bvh.tlas_nodes > 0 ? 1u : 0u;
-        ds.tlas_bound = s->bvh.tlas_bound;
         tt_scene_stats& stt = s->stats;
-        stt.triangle_count = s->bvh.tri_count;
         stt.instance_count = d->instance_count;
         stt.emissive_count = d->emissive_triangle_count;
-        stt.blas_nodes = s->bvh.blas_nodes;
-        stt.tlas_nodes = s->bvh.tlas_nodes;
-        stt.blas_levels = s->bvh.blas_levels;
-        stt.tlas_levels = s->bvh.tlas_levels;
+        if (flat) {
+            ds.blas = nullptr;
+            ds.tris = s->bvh.flat_tris.as<float4>();
+            ds.tlas = s->bvh.flat_nodes_buf.as<uint4>();
+            ds.has_tlas = s->bvh.flat_nodes > 0 ? 1u : 0u;
+            ds.tlas_bound = s->bvh.flat_bound;
+            ds.flat = 1u;
+            stt.triangle_count = s->bvh.flat_tri_count;
+            stt.tlas_nodes = s->bvh.flat_nodes;
+            stt.tlas_levels = s->bvh.flat_levels;
+            stt.accel = TT_ACCEL_FLAT;
+        } else {
+            ds.blas = s->bvh.blas.as<uint4>();
+            ds.tris = s->bvh.tris.as<float4>();
+            ds.tlas = s->bvh.tlas.as<uint4>();
+            ds.has_tlas = s->bvh.tlas_nodes > 0 ? 1u : 0u;
+            ds.tlas_bound = s->bvh.tlas_bound;
+            ds.flat = 0u;
+            stt.triangle_count = s->bvh.tri_count;
+            stt.blas_nodes = s->bvh.blas_nodes;
+            stt.tlas_nodes = s->bvh.tlas_nodes;
+            stt.blas_levels = s->bvh.blas_levels;
+            stt.tlas_levels = s->bvh.tlas_levels;
+            stt.accel = TT_ACCEL_TWO_LEVEL;
+        }
         stt.device_bytes = s->positions.bytes + s->indices.bytes + s->vertices.bytes + s->materials.bytes +
                            s->instances.bytes + s->emissive.bytes + s->inst_xform.bytes + s->bvh.blas.bytes +
-                           s->bvh.tris.bytes + s->bvh.tlas.bytes;
+                           s->bvh.tris.bytes + s->bvh.tlas.bytes + s->bvh.flat_nodes_buf.bytes +
+                           s->bvh.flat_tris.bytes;
         stt.max_stack = need_stack;
         Pool& p = ctx->pools[TT_LIFETIME_SCENE];
         p.scenes.push_back(std::move(s));
@@ -565,15 +590,19 @@ int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint
         require(ctx, "null context");
         use_device(ctx);
         SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
-        require(blas_bytes == s->bvh.blas_nodes * 128ull && tri_bytes == s->bvh.tri_count * 48ull &&
-                    tlas_bytes == s->bvh.tlas_nodes * 128ull,
+        const tt_scene_stats& stt = s->stats;
+        require(blas_bytes == stt.blas_nodes * 128ull && tri_bytes == stt.triangle_count * 48ull &&
+                    tlas_bytes == stt.tlas_nodes * 128ull,
                 "byte counts must match tt_scene_stats");
+        bool flat = s->bvh.flat;
+        const void* src_tris = flat ? s->bvh.flat_tris.ptr : s->bvh.tris.ptr;
+        const void* src_tlas = flat ? s->bvh.flat_nodes_buf.ptr : s->bvh.tlas.ptr;
         if (blas && blas_bytes)
             check_cuda(cudaMemcpyAsync(blas, s->bvh.blas.ptr, blas_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
         if (tris && tri_bytes)
-            check_cuda(cudaMemcpyAsync(tris, s->bvh.tris.ptr, tri_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+            check_cuda(cudaMemcpyAsync(tris, src_tris, tri_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
         if (tlas && tlas_bytes)
-            check_cuda(cudaMemcpyAsync(tlas, s->bvh.tlas.ptr, tlas_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+            check_cuda(cudaMemcpyAsync(tlas, src_tlas, tlas_bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy");
         sync(ctx);
     });
 }
@@ -622,6 +651,10 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else if (option == TT_OPTION_WAVEFRONT_SLOTS) {
             require(value <= (1ull << 26), "wavefront slot count above 2^26");
             ctx->wavefront_slots = (uint32_t)value;
+        } else if (option == TT_OPTION_ACCEL) {
+            require(value == TT_ACCEL_AUTO || value == TT_ACCEL_FLAT || value == TT_ACCEL_TWO_LEVEL,
+                    "unknown acceleration structure");
+            ctx->accel = (uint32_t)value;
         } else {
             fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
         }

@@ -239,6 +239,40 @@ __global__ void instance_prims_kernel(const tt_instance* inst, const uint32_t* i
     seg[i] = 0u;
 }
 
+// World boxes and records of all (instance, triangle) pairs, instance-major.  inst_tri_base:
+// prefix of the instances' triangle counts.
+__global__ void flat_prims_kernel(const int16_t* positions, const uint32_t* indices, const tt_instance* inst,
+                                  const uint32_t* inst_tri_base, uint32_t instance_count, uint32_t n, float4* lo,
+                                  float4* hi, uint32_t* seg, float4* recs) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    uint32_t a = 0, b = instance_count;
+    while (b - a > 1) {
+        uint32_t m = (a + b) / 2;
+        if (inst_tri_base[m] <= g) a = m;
+        else b = m;
+    }
+    while (a + 1 < instance_count && inst_tri_base[a + 1] <= g) ++a;
+    const tt_instance& in = inst[a];
+    uint32_t p = g - inst_tri_base[a];
+    uint32_t base = in.index_offset + 3u * p;
+    f3 q[3], w[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int16_t* s = positions + 3ull * (in.vertex_offset + indices[base + k]);
+        q[k] = f3{dequant_snorm16(s[0]), dequant_snorm16(s[1]), dequant_snorm16(s[2])};
+        w[k] = mat43_point(in.transform, q[k]);
+    }
+    f3 l = f3{fmn(fmn(w[0].x, w[1].x), w[2].x), fmn(fmn(w[0].y, w[1].y), w[2].y), fmn(fmn(w[0].z, w[1].z), w[2].z)};
+    f3 h = f3{fmx(fmx(w[0].x, w[1].x), w[2].x), fmx(fmx(w[0].y, w[1].y), w[2].y), fmx(fmx(w[0].z, w[1].z), w[2].z)};
+    lo[g] = make_float4(canon(l.x), canon(l.y), canon(l.z), 0.0f);
+    hi[g] = make_float4(canon(h.x), canon(h.y), canon(h.z), 0.0f);
+    seg[g] = 0u;
+    recs[3ull * g + 0] = make_float4(q[0].x, q[0].y, q[0].z, __uint_as_float(p));
+    recs[3ull * g + 1] = make_float4(q[1].x, q[1].y, q[1].z, __uint_as_float(a));
+    recs[3ull * g + 2] = make_float4(q[2].x, q[2].y, q[2].z, 0.0f);
+}
+
 __global__ void init_bounds_kernel(float* b, uint32_t* cnt, uint32_t segs) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= segs) return;
@@ -589,7 +623,62 @@ Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uin
 
 }  // namespace
 
-void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, BvhResult& out) {
+// Max |coordinate| of the root box of a built tree (the bound of the slab-test margins).
+static float root_bound(const Build4& b, cudaStream_t stream) {
+    int root = 0;
+    check_cuda(cudaMemcpyAsync(&root, b.roots, sizeof(int), cudaMemcpyDeviceToHost, stream), "root");
+    check_cuda(cudaStreamSynchronize(stream), "sync");
+    float4 rb[2];
+    check_cuda(cudaMemcpyAsync(&rb[0], b.blo + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
+    check_cuda(cudaMemcpyAsync(&rb[1], b.bhi + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
+    check_cuda(cudaStreamSynchronize(stream), "sync");
+    float bound = 0.0f;
+    for (float v : {rb[0].x, rb[0].y, rb[0].z, rb[1].x, rb[1].y, rb[1].z}) bound = std::max(bound, std::fabs(v));
+    return bound;
+}
+
+static void build_flat(const BuildInput& in, cudaStream_t stream, int leaf_max, BvhResult& out) {
+    Scratch sc(stream);
+    out.flat = true;
+    std::vector<uint32_t> base(in.instance_count + 1, 0);
+    for (uint32_t i = 0; i < in.instance_count; ++i)
+        base[i + 1] = base[i] + in.meshes_host[in.instances_host[i].mesh_index].index_count / 3u;
+    uint32_t n = base[in.instance_count];
+    out.flat_tri_count = n;
+    out.flat_tris.alloc(std::max<uint64_t>(n, 1) * 48ull);
+    if (n == 0) {
+        out.flat_nodes_buf.alloc(0);
+        out.flat_nodes = 0;
+        out.flat_levels = 0;
+        check_cuda(cudaStreamSynchronize(stream), "bvh build");
+        return;
+    }
+    tt_instance* d_inst = sc.get<tt_instance>(in.instance_count);
+    uint32_t* d_base = sc.get<uint32_t>(in.instance_count + 1);
+    check_cuda(cudaMemcpyAsync(d_inst, in.instances_host, sizeof(tt_instance) * in.instance_count,
+                               cudaMemcpyHostToDevice, stream), "instances");
+    check_cuda(cudaMemcpyAsync(d_base, base.data(), 4ull * (in.instance_count + 1), cudaMemcpyHostToDevice, stream),
+               "bases");
+    float4* plo = sc.get<float4>(n);
+    float4* phi = sc.get<float4>(n);
+    uint32_t* seg = sc.get<uint32_t>(n);
+    float4* recs = sc.get<float4>(3ull * n);
+    flat_prims_kernel<<<grid_for(n, 256), 256, 0, stream>>>(in.positions, in.indices, d_inst, d_base,
+                                                             in.instance_count, n, plo, phi, seg, recs);
+    Build4 b = build_bvh4(plo, phi, seg, n, 1, leaf_max, false, nullptr, out.flat_nodes_buf, sc);
+    out.flat_nodes = b.nodes;
+    out.flat_levels = b.levels;
+    gather_records_kernel<<<grid_for(n, 256), 256, 0, stream>>>(recs, b.order, n, out.flat_tris.as<float4>());
+    out.flat_bound = root_bound(b, stream);
+    check_cuda(cudaStreamSynchronize(stream), "bvh build");
+    check_cuda(cudaGetLastError(), "bvh build kernels");
+}
+
+void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, BvhResult& out) {
+    if (flat) {
+        build_flat(in, stream, leaf_max, out);
+        return;
+    }
     Scratch sc(stream);
     // triangle primitives (mesh order)
     std::vector<uint32_t> tri_base(in.mesh_count + 1, 0);
@@ -656,17 +745,7 @@ void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, Bv
         Build4 tb = build_bvh4(ilo, ihi, iseg, ni, 1, 1, true, d_ids, out.tlas, sc);
         out.tlas_nodes = tb.nodes;
         out.tlas_levels = tb.levels;
-        // scene bound for the conservative slab margins: the root box of the instance tree
-        int root = 0;
-        check_cuda(cudaMemcpyAsync(&root, tb.roots, sizeof(int), cudaMemcpyDeviceToHost, stream), "root");
-        check_cuda(cudaStreamSynchronize(stream), "sync");
-        float4 rb[2];
-        check_cuda(cudaMemcpyAsync(&rb[0], tb.blo + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
-        check_cuda(cudaMemcpyAsync(&rb[1], tb.bhi + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
-        check_cuda(cudaStreamSynchronize(stream), "sync");
-        float bound = 0.0f;
-        for (float v : {rb[0].x, rb[0].y, rb[0].z, rb[1].x, rb[1].y, rb[1].z}) bound = std::max(bound, std::fabs(v));
-        out.tlas_bound = bound;
+        out.tlas_bound = root_bound(tb, stream);  // bound of the world-space slab margins
     } else {
         out.tlas_nodes = 0;
         out.tlas_levels = 0;

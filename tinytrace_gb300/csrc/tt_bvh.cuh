@@ -1,5 +1,9 @@
-// Two-level BVH4 traversal on sm_103a: the replacement for the RT-core ray queries of the
-// reference (GL_EXT_ray_query in src/integrate/integrate.glsl:112-127 and 168-185).
+// BVH4 traversal on sm_103a: the replacement for the RT-core ray queries of the reference
+// (GL_EXT_ray_query in src/integrate/integrate.glsl:112-127 and 168-185).  A scene carries one
+// of two acceleration structures: the two-level one (a TLAS over instances whose leaves enter
+// per-mesh BLAS in object space) or the flat one (a single BVH over the world boxes of every
+// (instance, triangle) pair, whose records keep object-space vertices and the instance index).
+// Both find the same closest hit, bit for bit.
 //
 // Semantics (identical to the CPU oracle's ray queries):
 //   * instances are intersected in object space, o' = inverse_transform * (o, 1),
@@ -43,14 +47,15 @@ struct DevScene {
     const tt_material* materials;
     const tt_instance* instances;
     const tt_emissive_triangle* emissive;
-    const uint4* blas;        // 4 x uint4 per node
+    const uint4* blas;        // 8 x uint4 per node (two-level only)
     const float4* tris;       // 3 x float4 per triangle record
-    const uint4* tlas;        // 4 x uint4 per node
+    const uint4* tlas;        // 8 x uint4 per node: the TLAS, or the flat BVH
     const float4* inst_xform; // 4 x float4 per instance: inverse rows 0..2, (mesh, material, index_offset, vertex_offset)
     uint32_t emissive_count;
     uint32_t instance_count;
     uint32_t has_tlas;
-    float tlas_bound;  // max |coordinate| of the instance world boxes
+    float tlas_bound;  // max |coordinate| of the world boxes in `tlas`
+    uint32_t flat;     // 1: `tlas`/`tris` hold the flat BVH
 };
 
 struct Hit {
@@ -204,13 +209,14 @@ TT_HD f3 tri_vertex(float4 v) { return f3{v.x, v.y, v.z}; }
 struct TraceState {
     f3 o, d;     // world ray
     NodeRay nr;  // slab-test data of the current level (world at the top, object inside instances)
-    RayPre rp;
+    RayPre rp;   // triangle-test data of the instance `inst` (object space)
     Hit best;
     float tmin, tbest;
     uint32_t inst, cur, iterations;
-    uint32_t tri_next, tri_left;  // pending triangles of the current instance
+    uint32_t tri_next, tri_left;  // pending triangles
     int sp;
-    bool in_blas, have, cull;
+    bool in_blas;  // two-level: inside an instance; flat: the object ray of `inst` is not finite
+    bool have, cull;
 };
 
 TT_HD void trace_init(TraceState& st, const DevScene& sc, f3 o, f3 d, float tmin, float tmax, bool cull) {
@@ -227,7 +233,7 @@ TT_HD void trace_init(TraceState& st, const DevScene& sc, f3 o, f3 d, float tmin
     st.cull = cull;
     st.nr = node_ray(o, d, sc.tlas_bound);
     st.rp = ray_precompute(o, d);
-    st.inst = 0u;
+    st.inst = sc.flat ? 0xffffffffu : 0u;  // flat: no object ray set up yet
     st.in_blas = false;
     st.sp = 0;
     st.cur = 0u;
@@ -248,9 +254,142 @@ __device__ __forceinline__ bool trace_push(TraceState& st, uint32_t* stack, int 
     return true;
 }
 
+// The object-space ray of instance `inst`: o' = inverse * (o, 1), d' = mat3(inverse) * d.
+__device__ __forceinline__ void instance_ray(const DevScene& sc, uint32_t inst, f3 o, f3 d, f3& oo, f3& od,
+                                             uint32_t& mesh) {
+    const float4* x = sc.inst_xform + 4ull * inst;
+    float4 r0 = __ldg(x + 0), r1 = __ldg(x + 1), r2 = __ldg(x + 2);
+    mesh = __float_as_uint(__ldg(x + 3).x);
+    oo = f3{r0.x * o.x + r0.y * o.y + r0.z * o.z + r0.w * 1.0f, r1.x * o.x + r1.y * o.y + r1.z * o.z + r1.w * 1.0f,
+            r2.x * o.x + r2.y * o.y + r2.z * o.z + r2.w * 1.0f};
+    od = f3{r0.x * d.x + r0.y * d.y + r0.z * d.z, r1.x * d.x + r1.y * d.y + r1.z * d.z,
+            r2.x * d.x + r2.y * d.y + r2.z * d.z};
+}
+
+// Sorts the hit children of a node by entry distance and splits them into the nearest
+// internal child (the next node), the nearest leaf (the pending triangle range, when that is
+// free and `leaves` is set) and the rest, pushed farthest first.  Returns false on overflow.
+__device__ __forceinline__ bool visit_children(TraceState& st, int mask, const float* tn, const uint32_t* ch,
+                                               bool leaves, uint32_t* stack, int stride, uint32_t* err) {
+    float key[4];
+    uint32_t val[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        bool take = ((mask >> c) & 1) && tn[c] <= st.tbest;
+        key[c] = take ? tn[c] : __int_as_float(0x7f800000);
+        val[c] = take ? ch[c] : STACK_MARKER;
+    }
+#define TT_SWAP(i, j)                                                  \
+    {                                                                  \
+        bool sw = key[j] < key[i];                                     \
+        float k0 = sw ? key[j] : key[i], k1 = sw ? key[i] : key[j];    \
+        uint32_t v0 = sw ? val[j] : val[i], v1 = sw ? val[i] : val[j]; \
+        key[i] = k0; key[j] = k1; val[i] = v0; val[j] = v1;            \
+    }
+    TT_SWAP(0, 1) TT_SWAP(2, 3) TT_SWAP(0, 2) TT_SWAP(1, 3) TT_SWAP(1, 2)
+#undef TT_SWAP
+    int next = -1, leaf = -1, npush = 0;
+    uint32_t next_ref = 0u, leaf_ref = 0u;
+    bool push[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        bool valid = val[c] != STACK_MARKER;
+        bool is_leaf = leaves && (val[c] & CHILD_LEAF);
+        bool take_leaf = valid && is_leaf && leaf < 0 && st.tri_left == 0u;
+        bool take_next = valid && !is_leaf && next < 0;
+        leaf = take_leaf ? c : leaf;
+        leaf_ref = take_leaf ? val[c] : leaf_ref;
+        next = take_next ? c : next;
+        next_ref = take_next ? val[c] : next_ref;
+        push[c] = valid && !take_leaf && !take_next;
+        npush += push[c] ? 1 : 0;
+    }
+    if (st.sp + npush > TRAVERSAL_STACK) {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+        return false;
+    }
+#pragma unroll
+    for (int c = 3; c >= 0; --c) {
+        if (push[c]) stack[st.sp * stride] = val[c];
+        st.sp += push[c] ? 1 : 0;
+    }
+    st.tri_next = leaf >= 0 ? leaf_first(leaf_ref) : st.tri_next;
+    st.tri_left = leaf >= 0 ? leaf_count(leaf_ref) : st.tri_left;
+    st.have = next >= 0;
+    st.cur = next >= 0 ? next_ref : st.cur;
+    return true;
+}
+
+// One step through the flat BVH: the pending triangle (setting up the object ray of its
+// instance when it differs from the last one), then one pop or node visit.  Internal nodes
+// are popped while triangles are pending; a leaf waits until the pending range is done.
+// Node visits are counted as TLAS nodes, object-ray set-ups as instances.
 template <bool COUNT>
+__device__ __forceinline__ bool trace_step_flat(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
+                                                uint32_t* err, Counters& cnt) {
+    if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {
+        atomicOr(err, ERR_ITERATION_LIMIT);
+        return true;
+    }
+    if (st.tri_left > 0u) {
+        const float4* tr = sc.tris + 3ull * st.tri_next;
+        float4 a = __ldg(tr + 0), b = __ldg(tr + 1), cc = __ldg(tr + 2);
+        uint32_t prim = __float_as_uint(a.w), inst = __float_as_uint(b.w);
+        if (inst != st.inst) {
+            f3 oo, od;
+            uint32_t mesh;
+            instance_ray(sc, inst, st.o, st.d, oo, od, mesh);
+            st.inst = inst;
+            st.in_blas = !finite3(od);
+            st.rp = ray_precompute(oo, od);
+            if (COUNT) cnt.instances++;
+        }
+        if (COUNT) cnt.triangles++;
+        float t, u, v;
+        bool better = !st.in_blas &&
+                      intersect_triangle(st.rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), st.cull, st.tmin,
+                                         st.tbest, t, u, v) &&
+                      closer(t, st.inst, prim, st.best);
+        st.best.hit = better ? 1 : st.best.hit;
+        st.best.t = better ? t : st.best.t;
+        st.best.u = better ? u : st.best.u;
+        st.best.v = better ? v : st.best.v;
+        st.best.instance = better ? st.inst : st.best.instance;
+        st.best.prim = better ? prim : st.best.prim;
+        st.tbest = better ? t : st.tbest;
+        st.tri_next++;
+        st.tri_left--;
+    }
+    if (!st.have) {
+        if (st.sp == 0) return st.tri_left == 0u;
+        uint32_t e = stack[(st.sp - 1) * stride];
+        if (e & CHILD_LEAF) {
+            if (st.tri_left > 0u) return false;
+            --st.sp;
+            st.tri_next = leaf_first(e);
+            st.tri_left = leaf_count(e);
+            return false;
+        }
+        --st.sp;
+        st.cur = e;
+        st.have = true;
+    }
+    if (COUNT) cnt.tlas_nodes++;
+    float tn[4];
+    uint32_t ch[4];
+    int mask = node_hits(sc.tlas, st.cur, st.nr, st.tmin, st.tbest, tn, ch);
+    return !visit_children(st, mask, tn, ch, true, stack, stride, err);
+}
+
+// ACCEL: ACCEL_ANY dispatches on the scene at run time; ACCEL_FLAT_ONLY and ACCEL_TWO_LEVEL_ONLY
+// compile one structure's step (the caller has checked sc.flat).
+constexpr int ACCEL_ANY = 0, ACCEL_FLAT_ONLY = 1, ACCEL_TWO_LEVEL_ONLY = 2;
+
+template <bool COUNT, int ACCEL = ACCEL_ANY>
 __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
                                            uint32_t* err, Counters& cnt) {
+    if (ACCEL == ACCEL_FLAT_ONLY || (ACCEL == ACCEL_ANY && sc.flat))
+        return trace_step_flat<COUNT>(st, sc, stack, stride, err, cnt);
     if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {
         atomicOr(err, ERR_ITERATION_LIMIT);
         return true;
@@ -295,15 +434,9 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
     }
     if (!st.in_blas && (st.cur & CHILD_LEAF)) {
         st.inst = leaf_first(st.cur);
-        const float4* x = sc.inst_xform + 4ull * st.inst;
-        float4 r0 = __ldg(x + 0), r1 = __ldg(x + 1), r2 = __ldg(x + 2);
-        uint32_t mesh = __float_as_uint(__ldg(x + 3).x);
-        f3 o = st.o, d = st.d;
-        f3 oo = f3{r0.x * o.x + r0.y * o.y + r0.z * o.z + r0.w * 1.0f,
-                   r1.x * o.x + r1.y * o.y + r1.z * o.z + r1.w * 1.0f,
-                   r2.x * o.x + r2.y * o.y + r2.z * o.z + r2.w * 1.0f};
-        f3 od = f3{r0.x * d.x + r0.y * d.y + r0.z * d.z, r1.x * d.x + r1.y * d.y + r1.z * d.z,
-                   r2.x * d.x + r2.y * d.y + r2.z * d.z};
+        f3 oo, od;
+        uint32_t mesh;
+        instance_ray(sc, st.inst, st.o, st.d, oo, od, mesh);
         if (COUNT) cnt.instances++;
         if (!finite3(od)) {
             st.have = false;
@@ -323,55 +456,7 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
     float tn[4];
     uint32_t ch[4];
     int mask = node_hits(st.in_blas ? sc.blas : sc.tlas, st.cur, st.nr, st.tmin, st.tbest, tn, ch);
-    float key[4];
-    uint32_t val[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        bool take = ((mask >> c) & 1) && tn[c] <= st.tbest;
-        key[c] = take ? tn[c] : __int_as_float(0x7f800000);
-        val[c] = take ? ch[c] : STACK_MARKER;
-    }
-#define TT_SWAP(i, j)                                                  \
-    {                                                                  \
-        bool sw = key[j] < key[i];                                     \
-        float k0 = sw ? key[j] : key[i], k1 = sw ? key[i] : key[j];    \
-        uint32_t v0 = sw ? val[j] : val[i], v1 = sw ? val[i] : val[j]; \
-        key[i] = k0; key[j] = k1; val[i] = v0; val[j] = v1;            \
-    }
-    TT_SWAP(0, 1) TT_SWAP(2, 3) TT_SWAP(0, 2) TT_SWAP(1, 3) TT_SWAP(1, 2)
-#undef TT_SWAP
-    // nearest internal child -> next node; nearest triangle leaf -> pending range if free;
-    // the other hit children are pushed, farthest first
-    int next = -1, leaf = -1, npush = 0;
-    uint32_t next_ref = 0u, leaf_ref = 0u;
-    bool push[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        bool valid = val[c] != STACK_MARKER;
-        bool is_leaf = st.in_blas && (val[c] & CHILD_LEAF);
-        bool take_leaf = valid && is_leaf && leaf < 0 && st.tri_left == 0u;
-        bool take_next = valid && !is_leaf && next < 0;
-        leaf = take_leaf ? c : leaf;
-        leaf_ref = take_leaf ? val[c] : leaf_ref;
-        next = take_next ? c : next;
-        next_ref = take_next ? val[c] : next_ref;
-        push[c] = valid && !take_leaf && !take_next;
-        npush += push[c] ? 1 : 0;
-    }
-    if (st.sp + npush > TRAVERSAL_STACK) {
-        atomicOr(err, ERR_STACK_OVERFLOW);
-        return true;
-    }
-#pragma unroll
-    for (int c = 3; c >= 0; --c) {
-        if (push[c]) stack[st.sp * stride] = val[c];
-        st.sp += push[c] ? 1 : 0;
-    }
-    st.tri_next = leaf >= 0 ? leaf_first(leaf_ref) : st.tri_next;
-    st.tri_left = leaf >= 0 ? leaf_count(leaf_ref) : st.tri_left;
-    st.have = next >= 0;
-    st.cur = next >= 0 ? next_ref : st.cur;
-    return false;
+    return !visit_children(st, mask, tn, ch, st.in_blas, stack, stride, err);
 }
 
 // Closest hit, run to completion.

@@ -43,6 +43,13 @@ struct BvhResult {
     uint64_t blas_nodes = 0, tlas_nodes = 0, tri_count = 0;
     uint32_t blas_levels = 0, tlas_levels = 0;
     float tlas_bound = 0.0f;  // max |coordinate| of the instance world boxes
+    // single-level BVH over the world boxes of every (instance, triangle) pair
+    bool flat = false;
+    DeviceBuffer flat_nodes_buf;  // 128-byte BVH4 nodes
+    DeviceBuffer flat_tris;       // 48-byte records: object-space vertices, primitive, instance
+    uint64_t flat_nodes = 0, flat_tri_count = 0;
+    uint32_t flat_levels = 0;
+    float flat_bound = 0.0f;      // max |coordinate| of the triangle world boxes
 };
 
 struct BuildInput {
@@ -54,7 +61,9 @@ struct BuildInput {
     uint32_t instance_count;
 };
 
-// Builds BLAS (one root per mesh, node index == mesh index) and TLAS (root 0) on `stream`.
-void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, BvhResult& out);
+// Builds, on `stream`, either the two-level structure (BLAS with one root per mesh, node index
+// == mesh index, and TLAS with root 0) or, when `flat`, one BVH over the world boxes of all
+// (instance, triangle) pairs (root 0).
+void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, BvhResult& out);
 
 }  // namespace tt

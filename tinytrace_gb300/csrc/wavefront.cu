@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(WF_BLOCK) wf_regen_kernel(const __grid_constan
 constexpr int TR_BLOCK = 128;
 constexpr int REFILL_LANES = TT_REFILL_LANES;
 
-template <bool COUNT, bool SHADOW>
+template <bool COUNT, bool SHADOW, int ACCEL>
 __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel(const __grid_constant__ RenderParams p,
                                                                 const __grid_constant__ WfParams w) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * TR_BLOCK];
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
         if (!__any_sync(0xffffffffu, active)) break;
         while (true) {
             bool fin = false;
-            if (active && trace_step<COUNT>(st, sc, stack, TR_BLOCK, p.err, cnt)) {
+            if (active && trace_step<COUNT, ACCEL>(st, sc, stack, TR_BLOCK, p.err, cnt)) {
                 fin = true;
                 active = false;
             }
@@ -297,6 +297,17 @@ __global__ void wf_reduce_kernel(const __grid_constant__ RenderParams p, const _
     *tp = make_float4(acc.x, acc.y, acc.z, 1.0f);
 }
 
+template <bool SHADOW>
+static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid, bool counted, cudaStream_t st) {
+    if (p.sc.flat) {
+        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+        else wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+    } else {
+        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_TWO_LEVEL_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+        else wf_trace_kernel<false, SHADOW, ACCEL_TWO_LEVEL_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+    }
+}
+
 void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st) {
     const tt_constants& c = p.c;
     uint32_t WH = c.screen_size[0] * c.screen_size[1];
@@ -309,7 +320,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
         int dev = 0, sms = 0, per_sm = 0;
         check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
         check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
-        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wf_trace_kernel<false, false>, TR_BLOCK, 0),
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wf_trace_kernel<false, false, ACCEL_FLAT_ONLY>, TR_BLOCK, 0),
                    "occupancy");
         trace_blocks = std::max(1, sms * per_sm);
     }
@@ -328,11 +339,9 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
             if (n == 0) break;
             unsigned grid = (n + WF_BLOCK - 1) / WF_BLOCK;
             unsigned tgrid = std::min<unsigned>(trace_blocks, (n + TR_BLOCK - 1) / TR_BLOCK);
-            if (counted) wf_trace_kernel<true, false><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
-            else wf_trace_kernel<false, false><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
+            launch_trace<false>(p, w, tgrid, counted, st);
             wf_shade_kernel<<<grid, WF_BLOCK, 0, st>>>(p, w);
-            if (counted) wf_trace_kernel<true, true><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
-            else wf_trace_kernel<false, true><<<tgrid, TR_BLOCK, 0, st>>>(p, w);
+            launch_trace<true>(p, w, tgrid, counted, st);
         }
         wf_reduce_kernel<<<(WH + 255) / 256, 256, 0, st>>>(p, w, s0 + w.chunk_spp >= spp ? 1 : 0);
     }

@@ -41,6 +41,10 @@ TT_INTEGRATOR_WAVEFRONT = 0
 TT_INTEGRATOR_MEGAKERNEL = 1
 TT_OPTION_INTEGRATOR = 1
 TT_OPTION_WAVEFRONT_SLOTS = 2
+TT_OPTION_ACCEL = 3
+TT_ACCEL_AUTO = 0
+TT_ACCEL_FLAT = 1
+TT_ACCEL_TWO_LEVEL = 2
 
 # ---------------------------------------------------------------- byte layouts (numpy)
 MATERIAL_CONSTANT_FIELDS = [
@@ -132,7 +136,7 @@ class Timings(ctypes.Structure):
 class SceneStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("triangle_count", "instance_count", "emissive_count", "blas_nodes",
                                                "tlas_nodes", "blas_levels", "tlas_levels", "device_bytes",
-                                               "max_stack")]
+                                               "max_stack", "accel")]
 
 
 class TraversalCounters(ctypes.Structure):
