@@ -169,34 +169,42 @@ def make_workload(a):
                                      instances=a.instances, freq=a.freq, lights=a.lights)
 
 
-def cpu_baseline(w, arrays, target_seconds: float) -> dict:
-    """The oracle (a scalar C++ restatement, OpenMP over pixels on every host core) on a
-    band of rows of the same frame at 1 sample per pixel."""
-    from oracle import oracle
-    from tinytrace_gb300.renderer import Config, make_constants
+_CPU_SCENES: dict = {}
 
-    cfg = Config(bounce_count=w.config.bounce_count, sample_count=1, tonemap=w.config.tonemap,
-                 light_sampling=w.config.light_sampling)
+
+def cpu_baseline(w, arrays, target_seconds: float) -> dict:
+    """The oracle (a scalar C++ restatement, OpenMP over pixels on every host core, tracing
+    through the flat BVH) on a centred band of rows of the same frame, same spp and depth.
+    The band is sized from a calibration run so that the timed part takes ~target_seconds."""
+    from oracle import oracle
+    from tinytrace_gb300.renderer import make_constants
+
+    key = id(arrays)
     t0 = time.perf_counter()
-    orc = oracle.OracleScene(arrays)
+    if key not in _CPU_SCENES:
+        _CPU_SCENES[key] = oracle.OracleScene(arrays, flat=True)
+    orc = _CPU_SCENES[key]
     build_s = time.perf_counter() - t0
-    c = make_constants(w.camera, w.extent, cfg, 0, 0)
+    c = make_constants(w.camera, w.extent, w.config, 0, 0)
     W, H = w.extent
+    spp = w.config.sample_count
     target = np.zeros((H, W, 4), np.float32)
-    # calibrate on a thin band, then size the band for ~target_seconds
-    y0 = H // 2 - 4
+    threads = os.cpu_count() or 1
+    # calibrate on a thin band, then size the band (whole rows) for ~target_seconds
+    y0 = H // 2 - 1
     t0 = time.perf_counter()
-    orc.render(c, target, rows=(y0, y0 + 8))
+    orc.render(c, target, rows=(y0, y0 + 2), threads=threads)
     dt = max(time.perf_counter() - t0, 1e-3)
-    rows = int(max(8, min(H, 8 * target_seconds / dt)))
+    rows = int(max(2, min(H, 2 * target_seconds / dt)))
     y0 = max(0, H // 2 - rows // 2)
     t0 = time.perf_counter()
-    orc.render(c, target, rows=(y0, y0 + rows))
+    orc.render(c, target, rows=(y0, y0 + rows), threads=threads)
     dt = time.perf_counter() - t0
-    samples = rows * W
-    return {"value": samples / dt / 1e6, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{rows} rows x {W} px of the {W}x{H} frame at 1 spp, depth {cfg.bounce_count} "
-                      f"({samples} samples, {dt:.1f} s; BVH build {build_s:.1f} s excluded)"}
+    samples = rows * W * spp
+    return {"value": samples / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{rows} centred rows x {W} px of the {W}x{H} frame at {spp} spp, depth "
+                      f"{w.config.bounce_count} ({samples} samples, {dt:.1f} s; BVH build {build_s:.1f} s "
+                      f"excluded)"}
 
 
 def run_reference(a, dist: Dist):

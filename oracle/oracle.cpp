@@ -40,6 +40,7 @@ struct OracleScene {
     std::vector<EmissiveTriangle> emissive;
     SceneBvh bvh;
     bool use_bvh = true;
+    bool flat = false;  // the integrator traces through the flat BVH instead of the two-level one
     Geometry geom() const {
         return Geometry{positions.data(), indices.data(), instances.data(),
                         (uint32_t)instances.size(), meshes.data(), (uint32_t)meshes.size()};
@@ -52,8 +53,8 @@ struct OracleScene {
 
 Hit trace(const OracleScene& s, v3 o, v3 d, float tmin, float tmax, bool cull) {
     Geometry g = s.geom();
-    return s.use_bvh ? trace_bvh(g, s.bvh, o, d, tmin, tmax, cull)
-                     : trace_brute(g, o, d, tmin, tmax, cull);
+    if (!s.use_bvh) return trace_brute(g, o, d, tmin, tmax, cull);
+    return s.flat ? trace_flat(g, s.bvh, o, d, tmin, tmax, cull) : trace_bvh(g, s.bvh, o, d, tmin, tmax, cull);
 }
 
 struct Ray {
@@ -250,7 +251,9 @@ struct OracleSceneDesc {
     const EmissiveTriangle* emissive;
 };
 
-void* oracle_scene_create(const OracleSceneDesc* d, int use_bvh, int leaf_max) {
+// accel: 0 brute force, 1 two-level BVH, 2 flat BVH (the structure render() traces through;
+// both BVHs are built whenever accel != 0).
+void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
     OracleScene* s = new OracleScene();
     copy_in(s->positions, d->positions, d->position_count * 3u);
     copy_in(s->indices, d->indices, d->index_count);
@@ -259,7 +262,8 @@ void* oracle_scene_create(const OracleSceneDesc* d, int use_bvh, int leaf_max) {
     copy_in(s->meshes, d->meshes, d->mesh_count);
     copy_in(s->instances, d->instances, d->instance_count);
     copy_in(s->emissive, d->emissive, d->emissive_count);
-    s->use_bvh = use_bvh != 0;
+    s->use_bvh = accel != 0;
+    s->flat = accel == 2;
     if (s->use_bvh) s->bvh = build_scene_bvh(s->geom(), leaf_max);
     return s;
 }

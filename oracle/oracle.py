@@ -53,14 +53,16 @@ def _p(a):
 class OracleScene:
     """CPU restatement of the scene (brute-force or LBVH ray queries)."""
 
-    def __init__(self, arrays, use_bvh: bool = True, leaf_max: int = 3):
+    def __init__(self, arrays, use_bvh: bool = True, leaf_max: int = 3, flat: bool = False):
+        """use_bvh=False traces by brute force; otherwise render() traces through the
+        two-level BVH, or the flat one when `flat` (the hits are the same)."""
         self.arrays = arrays  # keeps the borrowed arrays alive
         d = OracleSceneDesc(_p(arrays.positions), len(arrays.positions), _p(arrays.indices), len(arrays.indices),
                             _p(arrays.vertices), len(arrays.vertices), _p(arrays.materials), len(arrays.materials),
                             len(arrays.meshes), _p(arrays.meshes), _p(arrays.instances), len(arrays.instances),
                             len(arrays.emissive), _p(arrays.emissive))
         self.lib = load()
-        self.handle = self.lib.oracle_scene_create(ctypes.byref(d), 1 if use_bvh else 0, leaf_max)
+        self.handle = self.lib.oracle_scene_create(ctypes.byref(d), (2 if flat else 1) if use_bvh else 0, leaf_max)
 
     def __del__(self):
         try:

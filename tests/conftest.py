@@ -38,3 +38,25 @@ def gpu_context():
     ctx = Context(0)
     yield ctx
     ctx.close()
+
+
+GOLDEN = ROOT / "tests" / "golden" / "oracle_golden.npz"
+
+
+@pytest.fixture(scope="session")
+def golden():
+    """Frozen oracle inputs and outputs (tests/golden/make_golden.py)."""
+    with np.load(GOLDEN, allow_pickle=False) as z:
+        return {k: z[k] for k in z.files}
+
+
+def golden_scene(golden, name):
+    from tinytrace_gb300.renderer import SceneArrays
+
+    return SceneArrays.from_arrays(golden, prefix=f"scene_{name}_")
+
+
+def golden_constants(golden, name):
+    from tinytrace_gb300 import native
+
+    return np.frombuffer(golden[f"render_{name}_constants"].tobytes(), native.CONSTANTS_DTYPE)[0].copy()

@@ -1,0 +1,79 @@
+"""Multi-process host logic of bench.py on CPU (gloo, world size 2).
+
+The path does not shard: N GPUs run N independent replicas and bench.py only needs a
+barrier and a max-over-ranks of the timed region.  These tests run that logic as two gloo
+ranks on 127.0.0.1, and the reference arm under torchrun, where rank 0 alone works and
+prints one JSON line.
+"""
+import json
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank: int, world: int, port: int, out_dir: str) -> None:
+    os.environ.update(WORLD_SIZE=str(world), RANK=str(rank), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    d = bench.Dist()
+    try:
+        d.barrier()
+        m = d.max(float(rank * 10 + 1))
+        d.barrier()
+        Path(out_dir, f"rank{rank}.json").write_text(json.dumps({"world": d.world, "max": m}))
+    finally:
+        d.close()
+
+
+def test_gloo_max_over_ranks(tmp_path):
+    import torch.multiprocessing as mp
+
+    port = free_port()
+    mp.start_processes(_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True, start_method="spawn")
+    for r in range(2):
+        res = json.loads((tmp_path / f"rank{r}.json").read_text())
+        assert res == {"world": 2, "max": 11.0}
+
+
+def test_reference_arm_under_torchrun():
+    """rank 0 times the CPU path and prints one line; rank 1 exits 0 without work."""
+    port = free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+           "--gpus", "2", "--steps", "1", "--warmup", "1", "--width", "48", "--height", "24", "--spp", "2",
+           "--depth", "3", "--instances", "2", "--freq", "4", "--lights", "3"]
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    res = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300, env=env)
+    assert res.returncode == 0, res.stderr[-2000:]
+    lines = [ln for ln in res.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, res.stdout
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    assert line["higher_is_better"] is True and line["unit"] == "Msamples/s"
+
+
+@pytest.mark.parametrize("world", [1])
+def test_single_process_dist_is_a_no_op(world, monkeypatch):
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    d = bench.Dist()
+    assert d.world == world and d.max(3.5) == 3.5
+    d.barrier()
+    d.close()

@@ -99,6 +99,23 @@ class SceneArrays:
         self.meshes = np.ascontiguousarray(scene.mesh_array)
         self.instances, self.emissive = flatten_scene(scene)
 
+    FIELDS = ("positions", "indices", "vertices", "materials", "meshes", "instances", "emissive")
+
+    def save(self, path, prefix: str = "") -> dict:
+        """The arrays as a dict (and, when `path` is given, an .npz file) for reloading with
+        `from_arrays` without re-running the scene generator."""
+        d = {prefix + k: getattr(self, k) for k in self.FIELDS}
+        if path is not None:
+            np.savez_compressed(path, **d)
+        return d
+
+    @classmethod
+    def from_arrays(cls, data, prefix: str = "") -> "SceneArrays":
+        self = cls.__new__(cls)
+        for k in cls.FIELDS:
+            setattr(self, k, np.ascontiguousarray(data[prefix + k]))
+        return self
+
     @property
     def triangle_count(self) -> int:
         return int(sum(int(m["index_count"]) // 3 for m in self.meshes))

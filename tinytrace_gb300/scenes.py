@@ -199,6 +199,32 @@ def icosphere_field(instances: int = 64, freq: int = 28, lights: int = 1000, see
     return s
 
 
+def instanced_spheres(copies: int = 40, freq: int = 6, seed: int = 3, box: float = 20.0) -> AssetScene:
+    """One displaced sphere mesh placed `copies` times with overlapping world boxes (rotated,
+    scaled and mirrored transforms) and one emissive triangle: the instancing case."""
+    rng = np.random.default_rng(seed)
+    s = AssetScene()
+    light = s.insert_material(Material(emission_luminance=50.0))
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], np.float32)
+    lm = s.insert_mesh(tri, np.zeros((3, 2), np.float32), np.array([0, 2, 1], np.uint32))
+    t = np.eye(4)
+    t[:3, :3] *= 3.0
+    t[:3, 3] = (0.0, box, 0.0)
+    s.root.children.append(Node(transform=t, models=[Model(lm, light)]))
+    base_pts, tris = geodesic_sphere(freq)
+    pts = (base_pts * (1.0 + 0.1 * _fbm(base_pts, rng))[:, None]).astype(np.float32)
+    m = s.insert_mesh(pts, None, tris)
+    mat = s.insert_material(Material(base_color=(0.7, 0.6, 0.5), specular_roughness=0.4))
+    for k in range(copies):
+        t = np.eye(4)
+        t[:3, :3] = _random_rotation(rng) * rng.uniform(1.0, 4.0)
+        if k % 7 == 3:
+            t[:3, 0] *= -1.0  # mirrored instance: flips the triangle winding
+        t[:3, 3] = rng.uniform(-box / 2, box / 2, 3)
+        s.root.children.append(Node(transform=t, models=[Model(m, mat)]))
+    return s
+
+
 def icosphere_workload(extent=(1920, 1080), spp: int = 64, depth: int = 8, **kw) -> Workload:
     cam = Camera.looking_at((0.0, 10.0, 95.0), (0.0, 0.0, 0.0), fov=np.pi / 2.0)
     cfg = Config(bounce_count=depth, sample_count=spp, tonemap=True,
