@@ -151,13 +151,24 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch() -> float | None:
-    """dram__bytes_read.sum + dram__bytes_write.sum of one integrate launch of this workload,
-    from the committed ncu summary (profiles/integrate_icosphere_field_1080p.md)."""
-    f = ROOT / "profiles" / "integrate_icosphere_field_1080p.md"
-    if not f.exists():
+# Algorithmic bytes per unit of traversal work (wf_trace_kernel): a BVH4 node is one 128-byte
+# record (six float4 planes + child references); a triangle test reads one 48-byte record; an
+# object-ray set-up reads the instance's three inverse rows and its mesh word (64 bytes); a
+# traced ray reads its origin and direction (32 bytes) and writes its result (hit record or
+# radiance update, counted as 32 bytes).
+NODE_BYTES = 128
+TRI_RECORD_BYTES = 48
+INSTANCE_RAY_BYTES = 64
+RAY_STATE_BYTES = 64
+PROFILE = ROOT / "profiles" / "wf_trace_kernel_icosphere_field_1080p.md"
+
+
+def ncu_dram_bytes_per_ray() -> float | None:
+    """DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced ray of
+    wf_trace_kernel, from the committed ncu summary of the 1-spp capture of this scene."""
+    if not PROFILE.exists():
         return None
-    m = re.search(r"traffic_per_launch_bytes:\s*([0-9.eE+]+)", f.read_text())
+    m = re.search(r"dram_bytes_per_ray:\s*([0-9.eE+]+)", PROFILE.read_text())
     return float(m.group(1)) if m else None
 
 
@@ -264,6 +275,8 @@ def run_ours(a, dist: Dist):
         r.render_to_target()
         r.present()
 
+    # per-launch CUDA events on the integrator's stream, read after each step
+    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 1))
     for _ in range(a.warmup):
         step()
     check(lib.tt_synchronize(ctx))
@@ -273,9 +286,17 @@ def run_ours(a, dist: Dist):
     check(lib.tt_synchronize(ctx))
     check(lib.tt_event_record(ctx, 0))
     kernel_ns = []
+    stage_ns = np.zeros(native.TT_STAGE_COUNT)
+    stage_launches = np.zeros(native.TT_STAGE_COUNT, np.int64)
+    stage_overflow = False
     for _ in range(a.steps):
         step()
         kernel_ns.append(r.timings().integrate * 1e9)  # synchronises; integrate-kernel events
+        stt = native.StageTimings()
+        check(lib.tt_stage_timings_get(ctx, ctypes.byref(stt)))
+        stage_ns += np.array(stt.ns[:], np.float64)
+        stage_launches += np.array(stt.launches[:], np.int64)
+        stage_overflow |= bool(stt.overflow)
     check(lib.tt_event_record(ctx, 1))
     ms = ctypes.c_float()
     check(lib.tt_event_elapsed_ms(ctx, 0, 1, ctypes.byref(ms)))
@@ -304,26 +325,42 @@ def run_ours(a, dist: Dist):
     check(lib.tt_host_free(host))
     e2e = samples_per_step * e2e_steps * dist.world / e2e_s / 1e6
 
-    # roofline accounting: counters of the instrumented kernel on the same frame
+    # roofline accounting of the dominant kernel (wf_trace_kernel: the extend and shadow
+    # stages) from the traversal counters of an instrumented render of the same frame
     cnt = native.TraversalCounters()
     c = r.constants()
     check(lib.tt_render_counted(ctx, r.scene, native.ptr(c), r.render_target, ctypes.byref(cnt)))
-    node_bytes = (cnt.blas_nodes + cnt.tlas_nodes) * 128
-    tri_bytes = cnt.triangles * 48
-    inst_bytes = cnt.instances * 64
-    hit_bytes = cnt.hits * (208 + 12 + 18 + 24 + 304)
-    target_bytes = W * H * 16 * 2
-    alg_bytes = node_bytes + tri_bytes + inst_bytes + hit_bytes + target_bytes
+    node_bytes = (cnt.blas_nodes + cnt.tlas_nodes) * NODE_BYTES
+    trace_bytes = (node_bytes + cnt.triangles * TRI_RECORD_BYTES + cnt.instances * INSTANCE_RAY_BYTES
+                   + cnt.rays * RAY_STATE_BYTES)
+    trace_stages = [native.TT_STAGE_EXTEND, native.TT_STAGE_SHADOW]
+    trace_launches = int(stage_launches[trace_stages].sum()) / a.steps  # per frame
+    trace_s = float(stage_ns[trace_stages].sum()) / a.steps / 1e9  # per frame
     kernel_s = statistics.mean(kernel_ns) / 1e9
     peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / kernel_s / 1e9
+    if trace_launches > 0:
+        bytes_per_launch = trace_bytes / trace_launches
+        launch_s = trace_s / trace_launches
+        achieved = bytes_per_launch / launch_s / 1e9
+        node_achieved = node_bytes / trace_s / 1e9
+        rays_per_launch = cnt.rays / trace_launches
+        per_ray = ncu_dram_bytes_per_ray()
+        traffic = per_ray * rays_per_launch if per_ray is not None else None
+    else:  # the megakernel does everything in one launch
+        bytes_per_launch, launch_s = trace_bytes, kernel_s
+        achieved = trace_bytes / kernel_s / 1e9
+        node_achieved = node_bytes / kernel_s / 1e9
+        rays_per_launch, traffic = cnt.rays, None
+    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 0))
 
     out_line = None
     if dist.rank == 0:
         cpu = None
         if not a.no_cpu_baseline:
             cpu = cpu_baseline(w, r.scene_arrays, a.cpu_seconds)
-        traffic = ncu_traffic_per_launch()
+        stages = {name: {"ms_per_step": stage_ns[i] / a.steps / 1e6,
+                         "launches_per_step": int(stage_launches[i]) / a.steps}
+                  for i, name in enumerate(native.STAGE_NAMES) if stage_launches[i] > 0}
         out_line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": total_s * 1e3 / a.steps, "higher_is_better": True,
@@ -338,12 +375,16 @@ def run_ours(a, dist: Dist):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 368, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": traffic, "kernel": "integrate_kernel",
-                         "kernel_ms": kernel_s * 1e3,
-                         "algorithmic_bytes_per_launch": alg_bytes,
-                         "node_fetch_bytes_per_launch": node_bytes,
-                         "node_fetch_frac": node_bytes / kernel_s / 1e9 / peak},
+                         "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "traffic": traffic,
+                         "kernel": "wf_trace_kernel" if trace_launches > 0 else "integrate_kernel",
+                         "launches_per_step": trace_launches, "launch_ms": launch_s * 1e3,
+                         "algorithmic_bytes_per_launch": bytes_per_launch, "rays_per_launch": rays_per_launch,
+                         "bytes_per_unit": {"node": NODE_BYTES, "triangle_record": TRI_RECORD_BYTES,
+                                            "instance_ray_setup": INSTANCE_RAY_BYTES, "ray_state": RAY_STATE_BYTES},
+                         "node_fetch_gbs": node_achieved, "node_fetch_frac": node_achieved / peak,
+                         "traffic_source": "ncu dram bytes per ray of the 1-spp capture x rays per launch"},
+            "stages": stages,
             "counters": {"rays": cnt.rays, "blas_nodes": cnt.blas_nodes, "tlas_nodes": cnt.tlas_nodes,
                          "triangles": cnt.triangles, "instances": cnt.instances, "hits": cnt.hits,
                          "traversal_step_lane_occupancy": cnt.lane_steps / max(1, 32 * cnt.warp_steps)},
@@ -351,7 +392,8 @@ def run_ours(a, dist: Dist):
                       "blas_levels": int(stats.blas_levels), "tlas_levels": int(stats.tlas_levels),
                       "device_bytes": int(stats.device_bytes), "build_ms": None},
             "clocks": clk,
-            "gpu_launches": a.steps,
+            "gpu_launches": int(stage_launches.sum()),
+            "gpu_launches_overflow": stage_overflow,
             "cpu_baseline": cpu,
         }
         t = native.Timings()

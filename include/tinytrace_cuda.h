@@ -62,6 +62,7 @@ extern "C" {
 #define TT_OPTION_INTEGRATOR 1      /* TT_INTEGRATOR_*; default wavefront */
 #define TT_OPTION_WAVEFRONT_SLOTS 2 /* paths in flight of the wavefront integrator; 0 = default */
 #define TT_OPTION_ACCEL 3           /* TT_ACCEL_*: structure built by later tt_scene_create calls */
+#define TT_OPTION_STAGE_TIMING 4    /* 1: CUDA events around every integrator launch (tt_stage_timings_get) */
 /* acceleration structures (tt_set_option TT_OPTION_ACCEL; tt_scene_stats.accel) */
 #define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
 #define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */
@@ -165,6 +166,22 @@ typedef struct tt_scene_stats {
     uint64_t accel; /* TT_ACCEL_FLAT or TT_ACCEL_TWO_LEVEL */
 } tt_scene_stats;
 
+/* Device time per integrator stage of the last render, summed over its launches (with
+ * TT_OPTION_STAGE_TIMING on).  Extends the integrate/post-process timestamps of
+ * src/lib.rs:149-193 (backend timing.rs:62-68) to the wavefront stages. */
+#define TT_STAGE_REGEN 0
+#define TT_STAGE_EXTEND 1  /* closest-hit trace of extension rays */
+#define TT_STAGE_SHADE 2
+#define TT_STAGE_SHADOW 3  /* closest-hit trace of shadow rays */
+#define TT_STAGE_REDUCE 4
+#define TT_STAGE_MEGAKERNEL 5
+#define TT_STAGE_COUNT 8
+typedef struct tt_stage_timings {
+    uint64_t ns[TT_STAGE_COUNT];
+    uint64_t launches[TT_STAGE_COUNT];
+    uint64_t overflow; /* 1: more launches than the 4096 recorded per render */
+} tt_stage_timings;
+
 /* Traversal counters from the instrumented render (roofline accounting). */
 typedef struct tt_traversal_counters {
     uint64_t rays, blas_nodes, tlas_nodes, triangles, instances, hits;
@@ -225,6 +242,8 @@ int32_t tt_tonemap(tt_context* ctx, tt_handle image, const tt_constants* constan
 int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value);
 /* replaces: src/lib.rs:167-178 Renderer::timings */
 int32_t tt_timings_get(tt_context* ctx, tt_timings* out);
+/* Per-stage device time of the last render (synchronises the context's stream). */
+int32_t tt_stage_timings_get(tt_context* ctx, tt_stage_timings* out);
 
 /* ---------------------------------------------------------------- parity entry points */
 /* replaces: src/material/test.rs:112-151 BdsfSampler::sample.  samples: n x 8 floats

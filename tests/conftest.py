@@ -59,4 +59,4 @@ def golden_scene(golden, name):
 def golden_constants(golden, name):
     from tinytrace_gb300 import native
 
-    return np.frombuffer(golden[f"render_{name}_constants"].tobytes(), native.CONSTANTS_DTYPE)[0].copy()
+    return np.frombuffer(golden[f"render_{name}_constants"].tobytes(), native.CONSTANTS_DTYPE).reshape(()).copy()

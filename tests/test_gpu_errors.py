@@ -113,3 +113,30 @@ def test_empty_scene_renders_sky(ctx):
     native.check(ctx.lib.tt_render(ctx.handle, scene, native.ptr(c), img))
     out = ctx.download(img, 16, 8)
     assert np.all(out[..., :3] == 1.0)
+
+
+def test_stage_timings(ctx):
+    """TT_OPTION_STAGE_TIMING records every wavefront launch; without it the call reports an error."""
+    from tinytrace_gb300.renderer import make_constants
+
+    rc, scene = _create(ctx, _cornell())
+    assert rc == native.TT_OK
+    w = scenes.cornell_workload(extent=(32, 16), spp=3, depth=4)
+    c = make_constants(w.camera, w.extent, w.config, 0, 0)
+    img = ctx.create_image(native.TT_LIFETIME_FRAME, 32, 16)
+    native.check(ctx.lib.tt_render(ctx.handle, scene, native.ptr(c), img))
+    st = native.StageTimings()
+    assert ctx.lib.tt_stage_timings_get(ctx.handle, ctypes.byref(st)) == native.TT_ERR_INVALID_ARGUMENT
+    native.check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_STAGE_TIMING, 1))
+    native.check(ctx.lib.tt_render(ctx.handle, scene, native.ptr(c), img))
+    native.check(ctx.lib.tt_stage_timings_get(ctx.handle, ctypes.byref(st)))
+    launches = list(st.launches)
+    for s in (native.TT_STAGE_REGEN, native.TT_STAGE_EXTEND, native.TT_STAGE_SHADE, native.TT_STAGE_SHADOW):
+        assert launches[s] >= 4 and st.ns[s] > 0, (s, launches)
+    assert launches[native.TT_STAGE_EXTEND] == launches[native.TT_STAGE_SHADOW]
+    assert launches[native.TT_STAGE_REDUCE] == 1 and launches[native.TT_STAGE_MEGAKERNEL] == 0
+    assert st.overflow == 0
+    native.check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_INTEGRATOR, native.TT_INTEGRATOR_MEGAKERNEL))
+    native.check(ctx.lib.tt_render(ctx.handle, scene, native.ptr(c), img))
+    native.check(ctx.lib.tt_stage_timings_get(ctx.handle, ctypes.byref(st)))
+    assert list(st.launches)[native.TT_STAGE_MEGAKERNEL] == 1 and sum(st.launches) == 1

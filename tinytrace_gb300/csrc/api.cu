@@ -108,6 +108,9 @@ struct tt_context {
     uint32_t wavefront_slots = 0;  // 0 = default
     uint32_t accel = TT_ACCEL_AUTO;
     tt::WavefrontBuffers wf;
+    bool stage_timing = false;
+    std::vector<cudaEvent_t> stage_events;  // 2 * StageTimer::MAX_LAUNCHES, created on first use
+    tt::StageTimer stage_timer;
 };
 
 namespace tt {
@@ -315,9 +318,27 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     bool wavefront = ctx->integrator == TT_INTEGRATOR_WAVEFRONT && c->sample_count > 0 && c->bounce_count > 0;
     WfParams w{};
     if (wavefront) w = wavefront_buffers(ctx, *c);
+    StageTimer* timer = nullptr;
+    if (ctx->stage_timing) {
+        if (ctx->stage_events.empty()) {
+            ctx->stage_events.resize(2 * StageTimer::MAX_LAUNCHES);
+            for (auto& ev : ctx->stage_events) check_cuda(cudaEventCreate(&ev), "event");
+        }
+        timer = &ctx->stage_timer;
+        timer->events = ctx->stage_events.data();
+        timer->count = 0;
+        timer->overflow = false;
+        timer->open = false;
+    }
+    ctx->stage_timer.count = timer ? 0 : -1;  // -1: the last render was not timed per stage
     check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
-    if (wavefront) render_wavefront(p, w, ctx->err_host + 1, counted, ctx->stream);
-    else launch_integrate(p, counted, ctx->stream);
+    if (wavefront) {
+        render_wavefront(p, w, ctx->err_host + 1, counted, ctx->stream, timer);
+    } else {
+        stage_begin(timer, TT_STAGE_MEGAKERNEL, ctx->stream);
+        launch_integrate(p, counted, ctx->stream);
+        stage_end(timer, ctx->stream);
+    }
     check_cuda(cudaGetLastError(), "integrate launch");
     check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
     ctx->integrate_timed = true;
@@ -400,6 +421,7 @@ int32_t tt_context_destroy(tt_context* ctx) {
         for (auto& ev : ctx->ev_integrate) cudaEventDestroy(ev);
         for (auto& ev : ctx->ev_post) cudaEventDestroy(ev);
         for (auto& ev : ctx->user_events) cudaEventDestroy(ev);
+        for (auto& ev : ctx->stage_events) cudaEventDestroy(ev);
         if (ctx->err_host) cudaFreeHost(ctx->err_host);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -651,6 +673,9 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else if (option == TT_OPTION_WAVEFRONT_SLOTS) {
             require(value <= (1ull << 26), "wavefront slot count above 2^26");
             ctx->wavefront_slots = (uint32_t)value;
+        } else if (option == TT_OPTION_STAGE_TIMING) {
+            require(value <= 1, "stage timing is 0 or 1");
+            ctx->stage_timing = value != 0;
         } else if (option == TT_OPTION_ACCEL) {
             require(value == TT_ACCEL_AUTO || value == TT_ACCEL_FLAT || value == TT_ACCEL_TWO_LEVEL,
                     "unknown acceleration structure");
@@ -658,6 +683,24 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else {
             fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
         }
+    });
+}
+
+int32_t tt_stage_timings_get(tt_context* ctx, tt_stage_timings* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        use_device(ctx);
+        sync(ctx);
+        *out = tt_stage_timings{};
+        const StageTimer& t = ctx->stage_timer;
+        require(t.count >= 0, "the last render ran without TT_OPTION_STAGE_TIMING");
+        for (int i = 0; i < t.count; ++i) {
+            float ms = 0.0f;
+            check_cuda(cudaEventElapsedTime(&ms, ctx->stage_events[2 * i], ctx->stage_events[2 * i + 1]), "elapsed");
+            out->ns[t.stage[i]] += (uint64_t)((double)ms * 1.0e6);
+            out->launches[t.stage[i]] += 1;
+        }
+        out->overflow = t.overflow ? 1u : 0u;
     });
 }
 

@@ -30,9 +30,37 @@ struct WfParams {
     uint32_t P, WH;
     uint32_t chunk_sample0, chunk_spp, chunk_items;
 };
+// Optional per-launch timing: a pair of CUDA events recorded on the launching stream around
+// each integrator launch, tagged with its TT_STAGE_*.  `events` holds 2 * MAX_LAUNCHES events
+// owned by the context; launches past MAX_LAUNCHES are not recorded (overflow).
+struct StageTimer {
+    static constexpr int MAX_LAUNCHES = 4096;
+    cudaEvent_t* events = nullptr;
+    uint8_t stage[MAX_LAUNCHES];
+    int count = 0;
+    bool overflow = false, open = false;
+};
+inline void stage_begin(StageTimer* t, int stage, cudaStream_t st) {
+    if (!t) return;
+    t->open = t->count < StageTimer::MAX_LAUNCHES;
+    if (!t->open) {
+        t->overflow = true;
+        return;
+    }
+    t->stage[t->count] = (uint8_t)stage;
+    cudaEventRecord(t->events[2 * t->count], st);
+}
+inline void stage_end(StageTimer* t, cudaStream_t st) {
+    if (!t || !t->open) return;
+    cudaEventRecord(t->events[2 * t->count + 1], st);
+    t->count++;
+    t->open = false;
+}
+
 // Renders with the wavefront integrator; w.chunk_spp is the largest chunk of samples the
 // buffers hold.  Synchronises `st` once per iteration to read the active-path count.
-void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st);
+void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
+                      StageTimer* timer);
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st);
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out,
                     cudaStream_t st);

@@ -308,7 +308,8 @@ static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid
     }
 }
 
-void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st) {
+void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
+                      StageTimer* timer) {
     const tt_constants& c = p.c;
     uint32_t WH = c.screen_size[0] * c.screen_size[1];
     uint32_t spp = c.sample_count;
@@ -332,18 +333,28 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
         check_cuda(cudaMemsetAsync(w.counters, 0, 32, st), "memset");
         while (true) {
             check_cuda(cudaMemsetAsync(w.counters + 1, 0, 20, st), "memset");
+            stage_begin(timer, TT_STAGE_REGEN, st);
             wf_regen_kernel<<<regen_grid, WF_BLOCK, 0, st>>>(p, w);
+            stage_end(timer, st);
             check_cuda(cudaMemcpyAsync(host_count, w.counters + 1, 4, cudaMemcpyDeviceToHost, st), "count");
             check_cuda(cudaStreamSynchronize(st), "sync");
             uint32_t n = *host_count;
             if (n == 0) break;
             unsigned grid = (n + WF_BLOCK - 1) / WF_BLOCK;
             unsigned tgrid = std::min<unsigned>(trace_blocks, (n + TR_BLOCK - 1) / TR_BLOCK);
+            stage_begin(timer, TT_STAGE_EXTEND, st);
             launch_trace<false>(p, w, tgrid, counted, st);
+            stage_end(timer, st);
+            stage_begin(timer, TT_STAGE_SHADE, st);
             wf_shade_kernel<<<grid, WF_BLOCK, 0, st>>>(p, w);
+            stage_end(timer, st);
+            stage_begin(timer, TT_STAGE_SHADOW, st);
             launch_trace<true>(p, w, tgrid, counted, st);
+            stage_end(timer, st);
         }
+        stage_begin(timer, TT_STAGE_REDUCE, st);
         wf_reduce_kernel<<<(WH + 255) / 256, 256, 0, st>>>(p, w, s0 + w.chunk_spp >= spp ? 1 : 0);
+        stage_end(timer, st);
     }
 }
 

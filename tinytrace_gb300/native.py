@@ -45,6 +45,15 @@ TT_OPTION_ACCEL = 3
 TT_ACCEL_AUTO = 0
 TT_ACCEL_FLAT = 1
 TT_ACCEL_TWO_LEVEL = 2
+TT_OPTION_STAGE_TIMING = 4
+TT_STAGE_REGEN = 0
+TT_STAGE_EXTEND = 1
+TT_STAGE_SHADE = 2
+TT_STAGE_SHADOW = 3
+TT_STAGE_REDUCE = 4
+TT_STAGE_MEGAKERNEL = 5
+TT_STAGE_COUNT = 8
+STAGE_NAMES = ("regen", "extend", "shade", "shadow", "reduce", "megakernel")
 
 # ---------------------------------------------------------------- byte layouts (numpy)
 MATERIAL_CONSTANT_FIELDS = [
@@ -139,6 +148,10 @@ class SceneStats(ctypes.Structure):
                                                "max_stack", "accel")]
 
 
+class StageTimings(ctypes.Structure):
+    _fields_ = [("ns", ctypes.c_uint64 * 8), ("launches", ctypes.c_uint64 * 8), ("overflow", ctypes.c_uint64)]
+
+
 class TraversalCounters(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("rays", "blas_nodes", "tlas_nodes", "triangles", "instances", "hits",
                                                "warp_steps", "lane_steps")]
@@ -169,6 +182,7 @@ SIGNATURES = {
     "tt_tonemap": (_I32, [_P, _U64, _P, _U32, _P, _U64]),
     "tt_set_option": (_I32, [_P, _U32, _U64]),
     "tt_timings_get": (_I32, [_P, ctypes.POINTER(Timings)]),
+    "tt_stage_timings_get": (_I32, [_P, ctypes.POINTER(StageTimings)]),
     "tt_bsdf_eval_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_bsdf_sample_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_trace_batch": (_I32, [_P, _U64, _P, _U32, _U32, _P]),
