@@ -68,7 +68,7 @@ struct ImageRes {
 };
 
 struct SceneRes {
-    DeviceBuffer positions, indices, vertices, materials, instances, emissive, inst_xform;
+    DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform;
     BvhResult bvh;
     DevScene dev{};
     tt_scene_stats stats{};
@@ -517,6 +517,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         upload(s->indices, d->indices, d->index_count, st);
         upload(s->vertices, d->vertices, d->vertex_count, st);
         upload(s->materials, d->materials, d->material_count, st);
+        upload(s->meshes, d->meshes, d->mesh_count, st);
         upload(s->instances, d->instances, d->instance_count, st);
         upload(s->emissive, d->emissive_triangles, d->emissive_triangle_count, st);
         std::vector<float4> xf(4ull * d->instance_count);
@@ -556,6 +557,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.vertices = s->vertices.as<tt_vertex>();
         ds.materials = s->materials.as<tt_material>();
         ds.instances = s->instances.as<tt_instance>();
+        ds.meshes = s->meshes.as<tt_mesh>();
         ds.emissive = s->emissive.as<tt_emissive_triangle>();
         ds.inst_xform = s->inst_xform.as<float4>();
         ds.emissive_count = d->emissive_triangle_count;
@@ -588,7 +590,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             stt.tlas_levels = s->bvh.tlas_levels;
             stt.accel = TT_ACCEL_TWO_LEVEL;
         }
-        stt.device_bytes = s->positions.bytes + s->indices.bytes + s->vertices.bytes + s->materials.bytes +
+        stt.device_bytes = s->positions.bytes + s->indices.bytes + s->vertices.bytes + s->materials.bytes + s->meshes.bytes +
                            s->instances.bytes + s->emissive.bytes + s->inst_xform.bytes + s->bvh.blas.bytes +
                            s->bvh.tris.bytes + s->bvh.tlas.bytes + s->bvh.flat_nodes_buf.bytes +
                            s->bvh.flat_tris.bytes;

@@ -32,7 +32,10 @@ namespace tt {
 
 constexpr uint32_t CHILD_LEAF = 0x80000000u;
 constexpr uint32_t STACK_MARKER = 0xffffffffu;
-constexpr int TRAVERSAL_STACK = 64;
+#ifndef TT_TRAVERSAL_STACK
+#define TT_TRAVERSAL_STACK 64
+#endif
+constexpr int TRAVERSAL_STACK = TT_TRAVERSAL_STACK;  // entries per thread, in shared memory
 constexpr uint32_t TRAVERSAL_ITERATION_LIMIT = 1u << 24;
 constexpr uint32_t ERR_STACK_OVERFLOW = 1u;
 constexpr uint32_t ERR_ITERATION_LIMIT = 2u;
@@ -46,6 +49,7 @@ struct DevScene {
     const tt_vertex* vertices;
     const tt_material* materials;
     const tt_instance* instances;
+    const tt_mesh* meshes;
     const tt_emissive_triangle* emissive;
     const uint4* blas;        // 8 x uint4 per node (two-level only)
     const float4* tris;       // 3 x float4 per triangle record

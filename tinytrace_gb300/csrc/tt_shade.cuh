@@ -129,6 +129,48 @@ __device__ __forceinline__ f3 light_contribution(const DevScene& sc, const Light
     return bsdf * emissive * fabsf(cos_theta(ls.wo)) / fmx(ls.density, PDF_EPSILON);
 }
 
+// The triangle the visibility test of integrate.glsl:175-185 accepts, found before the shadow
+// ray is traced.  In a light instance of at most 65,535 triangles exactly one primitive p can
+// satisfy (p + index_offset / 3) % 0xffff == hash (none when hash == 0xffff or p would lie past
+// the mesh): the ray is visible iff its closest hit is that triangle.  Returns
+//   0  no primitive qualifies, or the ray misses it: not visible, nothing to trace;
+//   1  `best`/`tbest` hold the ray's hit on it: trace for a closer hit (any closer hit occludes);
+//   2  the instance has more than 65,535 triangles: trace plainly and test the closest hit.
+// The hit is computed exactly as the traversal computes it (object ray of the instance, the
+// same watertight test on the same dequantised vertices), so a traversal seeded with it finds
+// the same closest hit as an unseeded one.
+__device__ __forceinline__ int shadow_target(const DevScene& sc, uint32_t light_instance, uint32_t hash, f3 o,
+                                             f3 d, float tmin, float tmax, Hit& best, float& tbest) {
+    const tt_instance* in = sc.instances + light_instance;
+    uint32_t index_offset = __ldg(&in->index_offset), vertex_offset = __ldg(&in->vertex_offset);
+    uint32_t tri_count = __ldg(&sc.meshes[__ldg(&in->mesh_index)].index_count) / 3u;
+    if (tri_count > 0xffffu) return 2;
+    if (hash >= 0xffffu) return 0;
+    uint32_t r = (index_offset / 3u) % 0xffffu;
+    uint32_t prim = hash >= r ? hash - r : hash + 0xffffu - r;
+    if (prim >= tri_count) return 0;
+    f3 oo, od;
+    uint32_t mesh;
+    instance_ray(sc, light_instance, o, d, oo, od, mesh);
+    if (!finite3(d) || !finite3(od)) return 0;
+    f3 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int16_t* s = sc.positions + 3ull * (__ldg(sc.indices + index_offset + 3u * prim + k) + vertex_offset);
+        p[k] = f3{dequant_snorm16(__ldg(s + 0)), dequant_snorm16(__ldg(s + 1)), dequant_snorm16(__ldg(s + 2))};
+    }
+    float t, u, v;
+    if (!intersect_triangle(ray_precompute(oo, od), p[0], p[1], p[2], false, tmin, tmax, t, u, v)) return 0;
+    best.hit = 1;
+    best.t = t;
+    best.u = u;
+    best.v = v;
+    best.instance = light_instance;
+    best.prim = prim;
+    tbest = t;
+    return 1;
+}
+
 // integrate.glsl:175-185: the closest shadow hit must be the sampled light triangle.
 __device__ __forceinline__ bool light_visible(const DevScene& sc, const Hit& h, uint32_t light_instance,
                                               uint32_t hash) {

@@ -52,6 +52,31 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
     return base + (uint32_t)__popc(mask & lane_mask_lt());
 }
 
+// Block-aggregated append: every thread of the block must call it; threads with `pred` get
+// consecutive positions from one atomicAdd per block on `counter` (the position order
+// inside the block is irrelevant to the results).  `s_warp` holds BLOCK / 32 + 1 words.
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_append(uint32_t* counter, bool pred, uint32_t* s_warp) {
+    constexpr int WARPS = BLOCK / 32;
+    uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
+    if (lane == 0) s_warp[warp] = (uint32_t)__popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t sum = 0u;
+        for (int k = 0; k < WARPS; ++k) {
+            uint32_t c = s_warp[k];
+            s_warp[k] = sum;
+            sum += c;
+        }
+        s_warp[WARPS] = sum ? atomicAdd(counter, sum) : 0u;
+    }
+    __syncthreads();
+    uint32_t pos = s_warp[WARPS] + s_warp[warp] + (uint32_t)__popc(mask & lane_mask_lt());
+    __syncthreads();
+    return pos;
+}
+
 // Pixel of band-ordered index t: bands of 8 rows, column-major inside a band, so a warp's 32
 // consecutive items cover a 4 x 8 pixel block (coherent camera rays).
 __device__ __forceinline__ void band_pixel(uint32_t t, uint32_t W, uint32_t H, uint32_t& x, uint32_t& y) {
@@ -65,9 +90,12 @@ __device__ __forceinline__ void band_pixel(uint32_t t, uint32_t W, uint32_t H, u
 __device__ __forceinline__ f3 xyz(float4 v) { return f3{v.x, v.y, v.z}; }
 __device__ __forceinline__ float4 pack(f3 v, uint32_t w) { return make_float4(v.x, v.y, v.z, __uint_as_float(w)); }
 
-__global__ void __launch_bounds__(WF_BLOCK) wf_regen_kernel(const __grid_constant__ RenderParams p,
-                                                            const __grid_constant__ WfParams w) {
-    uint32_t s = blockIdx.x * WF_BLOCK + threadIdx.x;
+constexpr int REGEN_BLOCK = 512;
+
+__global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_constant__ RenderParams p,
+                                                               const __grid_constant__ WfParams w) {
+    __shared__ uint32_t s_warp[REGEN_BLOCK / 32 + 1];
+    uint32_t s = blockIdx.x * REGEN_BLOCK + threadIdx.x;
     bool valid = s < w.P;
     float4 a = valid ? w.acc[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint32_t flags = __float_as_uint(a.w);
@@ -79,7 +107,7 @@ __global__ void __launch_bounds__(WF_BLOCK) wf_regen_kernel(const __grid_constan
     }
     bool live = valid && (flags & F_LIVE);
     bool need = valid && !live && *(volatile uint32_t*)&w.counters[0] < w.chunk_items;
-    uint32_t item = warp_append(&w.counters[0], need);
+    uint32_t item = block_append<REGEN_BLOCK>(&w.counters[0], need, s_warp);
     if (need && item < w.chunk_items) {
         const tt_constants& c = p.c;
         uint32_t W = c.screen_size[0], H = c.screen_size[1];
@@ -97,7 +125,7 @@ __global__ void __launch_bounds__(WF_BLOCK) wf_regen_kernel(const __grid_constan
         w.acc[s] = pack(splat(0.0f), F_LIVE);
         live = true;
     }
-    uint32_t q = warp_append(&w.counters[1], live);
+    uint32_t q = block_append<REGEN_BLOCK>(&w.counters[1], live, s_warp);
     if (live) w.active[q] = s;
 }
 
@@ -123,8 +151,9 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
     const uint32_t n = SHADOW ? w.counters[2] : w.counters[1];
     uint32_t* head = &w.counters[SHADOW ? 4 : 3];
     TraceState st;
-    uint32_t item = 0, slot = 0, light = 0;
+    uint32_t item = 0, slot = 0, light = 0, target_prim = 0;
     bool active = false;
+    bool seeded = false;  // shadow ray seeded with its light triangle: any change of the closest hit occludes
     bool drained = false;  // warp-uniform: the queue has no more rays
     Counters cnt{0u, 0u, 0u, 0u};
     uint32_t rays = 0, hits = 0;
@@ -154,6 +183,14 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                     }
                     trace_init(st, sc, xyz(o), xyz(d), SHADOW ? SHADOW_TMIN : EXTENSION_TMIN,
                                SHADOW ? SHADOW_TMAX : EXTENSION_TMAX, !SHADOW);
+                    if (SHADOW) {
+                        uint32_t hash = __float_as_uint(w.pa1[slot].w) >> 16;
+                        int mode = shadow_target(sc, light, hash, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX,
+                                                 st.best, st.tbest);
+                        if (mode == 0) st.have = false;  // not visible: the first step finishes
+                        seeded = mode == 1;
+                        target_prim = st.best.prim;
+                    }
                     active = true;
                     if (COUNT) rays++;
                 }
@@ -163,7 +200,8 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
         if (!__any_sync(0xffffffffu, active)) break;
         while (true) {
             bool fin = false;
-            if (active && trace_step<COUNT, ACCEL>(st, sc, stack, TR_BLOCK, p.err, cnt)) {
+            if (active && (trace_step<COUNT, ACCEL>(st, sc, stack, TR_BLOCK, p.err, cnt) ||
+                           (SHADOW && seeded && (st.best.prim != target_prim || st.best.instance != light)))) {
                 fin = true;
                 active = false;
             }
@@ -241,14 +279,26 @@ __global__ void __launch_bounds__(WF_BLOCK) wf_shade_kernel(const __grid_constan
             if (nee) {
                 LightSample ls = sample_light(sc, hit.world_position, basis, g);
                 f3 contrib = light_contribution(sc, ls, mc, lobes, wi);
-                uint32_t pflags = (bounce == 0u ? 1u : 0u) | (ls.hash << 16);
-                w.pa1[s] = pack(thr * contrib, pflags);
-                w.pa0[s] = pack(thr * splat(0.0f), 0u);
-                w.pe[s] = pack(em * thr, 0u);
-                want_shadow = true;
-                light = ls.instance;
-                sh_org = hit.world_position;
-                sh_dir = ls.dir;
+                f3 a1 = thr * contrib, a0 = thr * splat(0.0f);
+                // When the visible and the occluded update have the same bits (the light faces
+                // away, or the BSDF is zero towards it) the shadow ray cannot change the result:
+                // apply the update here, in the order the shadow stage would, and trace nothing.
+                bool same = __float_as_uint(a1.x) == __float_as_uint(a0.x) &&
+                            __float_as_uint(a1.y) == __float_as_uint(a0.y) &&
+                            __float_as_uint(a1.z) == __float_as_uint(a0.z);
+                if (same) {
+                    acc += a1;
+                    if (bounce == 0u) acc += em * thr;
+                } else {
+                    uint32_t pflags = (bounce == 0u ? 1u : 0u) | (ls.hash << 16);
+                    w.pa1[s] = pack(a1, pflags);
+                    w.pa0[s] = pack(a0, 0u);
+                    w.pe[s] = pack(em * thr, 0u);
+                    want_shadow = true;
+                    light = ls.instance;
+                    sh_org = hit.world_position;
+                    sh_dir = ls.dir;
+                }
             } else {
                 acc += em * thr;
             }
@@ -266,7 +316,8 @@ __global__ void __launch_bounds__(WF_BLOCK) wf_shade_kernel(const __grid_constan
             w.acc[s] = pack(acc, flags);
         }
     }
-    uint32_t e = warp_append(&w.counters[2], want_shadow);
+    __shared__ uint32_t s_warp[WF_BLOCK / 32 + 1];
+    uint32_t e = block_append<WF_BLOCK>(&w.counters[2], want_shadow, s_warp);
     if (want_shadow) {
         w.shadow[2ull * e] = pack(sh_org, s);
         w.shadow[2ull * e + 1] = pack(sh_dir, light);
@@ -315,7 +366,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
     uint32_t spp = c.sample_count;
     uint32_t max_chunk = w.chunk_spp;
     w.WH = WH;
-    unsigned regen_grid = (w.P + WF_BLOCK - 1) / WF_BLOCK;
+    unsigned regen_grid = (w.P + REGEN_BLOCK - 1) / REGEN_BLOCK;
     static int trace_blocks = 0;  // resident blocks of the persistent trace kernel on the whole GPU
     if (trace_blocks == 0) {
         int dev = 0, sms = 0, per_sm = 0;
@@ -334,7 +385,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
         while (true) {
             check_cuda(cudaMemsetAsync(w.counters + 1, 0, 20, st), "memset");
             stage_begin(timer, TT_STAGE_REGEN, st);
-            wf_regen_kernel<<<regen_grid, WF_BLOCK, 0, st>>>(p, w);
+            wf_regen_kernel<<<regen_grid, REGEN_BLOCK, 0, st>>>(p, w);
             stage_end(timer, st);
             check_cuda(cudaMemcpyAsync(host_count, w.counters + 1, 4, cudaMemcpyDeviceToHost, st), "count");
             check_cuda(cudaStreamSynchronize(st), "sync");
