@@ -59,7 +59,10 @@ constexpr uint32_t KIND_IMAGE = 1, KIND_SCENE = 2;
 constexpr int LIFETIMES = 5;
 constexpr int EVENT_SLOTS = 16;
 constexpr size_t L2_FLUSH_BYTES = 512ull << 20;
-constexpr int BLAS_LEAF_MAX = 3;
+#ifndef TT_LEAF_MAX
+#define TT_LEAF_MAX 3
+#endif
+constexpr int BLAS_LEAF_MAX = TT_LEAF_MAX;  // triangles per leaf
 constexpr uint64_t FLAT_AUTO_MAX_TRIANGLES = 1ull << 26;
 
 struct ImageRes {

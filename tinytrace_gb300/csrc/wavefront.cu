@@ -252,7 +252,10 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
     }
 }
 
-__global__ void __launch_bounds__(WF_BLOCK) wf_shade_kernel(const __grid_constant__ RenderParams p,
+#ifndef TT_SHADE_MIN_BLOCKS
+#define TT_SHADE_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel(const __grid_constant__ RenderParams p,
                                                             const __grid_constant__ WfParams w) {
     uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
     uint32_t n = w.counters[5];
