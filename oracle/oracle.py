@@ -53,7 +53,7 @@ def _p(a):
 class OracleScene:
     """CPU restatement of the scene (brute-force or LBVH ray queries)."""
 
-    def __init__(self, arrays, use_bvh: bool = True, leaf_max: int = 3, flat: bool = False):
+    def __init__(self, arrays, use_bvh: bool = True, leaf_max: int = 2, flat: bool = False):
         """use_bvh=False traces by brute force; otherwise render() traces through the
         two-level BVH, or the flat one when `flat` (the hits are the same)."""
         self.arrays = arrays  # keeps the borrowed arrays alive

@@ -74,7 +74,7 @@ def test_flat_bvh_structure(name):
 
     def leaf(ref, box):
         first, count = leaf_range(ref)
-        assert count <= 3
+        assert count <= 2
         seen[first:first + count] += 1
         for r in tris[first:first + count]:
             inst = arrays.instances[int(r["mesh"])]
@@ -107,7 +107,7 @@ def test_two_level_bvh_structure(name):
 
         def leaf(ref, box, m=m, prims=prims):
             first, count = leaf_range(ref)
-            assert count <= 3
+            assert count <= 2
             for r in tris[first:first + count]:
                 assert int(r["mesh"]) == m
                 prims.append(int(r["prim"]))

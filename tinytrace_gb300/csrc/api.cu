@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <new>
 #include <string>
@@ -60,7 +61,7 @@ constexpr int LIFETIMES = 5;
 constexpr int EVENT_SLOTS = 16;
 constexpr size_t L2_FLUSH_BYTES = 512ull << 20;
 #ifndef TT_LEAF_MAX
-#define TT_LEAF_MAX 3
+#define TT_LEAF_MAX 2
 #endif
 constexpr int BLAS_LEAF_MAX = TT_LEAF_MAX;  // triangles per leaf
 constexpr uint64_t FLAT_AUTO_MAX_TRIANGLES = 1ull << 26;
@@ -71,7 +72,7 @@ struct ImageRes {
 };
 
 struct SceneRes {
-    DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform;
+    DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform, inst_bucket;
     BvhResult bvh;
     DevScene dev{};
     tt_scene_stats stats{};
@@ -175,6 +176,42 @@ void upload(DeviceBuffer& b, const T* host, uint64_t count, cudaStream_t st) {
     if (count) check_cuda(cudaMemcpyAsync(b.ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
 }
 
+// Which shading code a material runs: the OpenPBR lobes that can carry weight, NEE eligibility
+// (integrate.glsl:293-295) and emission.  Hits on materials with equal signatures share one
+// shading queue of the wavefront integrator.
+uint32_t shading_signature(const tt_material_constants& m) {
+    uint32_t sig = 0u;
+    if (m.fuzz_weight > 0.0f) sig |= 1u;
+    if (m.coat_weight > 0.0f) sig |= 2u;
+    if (m.base_metalness > 0.0f) sig |= 4u;
+    if (m.base_metalness < 1.0f && m.specular_weight > 0.0f) sig |= 8u;
+    if (m.base_metalness < 1.0f && m.transmission_weight > 0.0f) sig |= 16u;
+    if (m.base_metalness < 1.0f && m.transmission_weight < 1.0f) sig |= 32u;
+    if (m.specular_roughness > 0.15f) sig |= 64u;
+    if (m.emission_luminance > 0.0f) sig |= 128u;
+    return sig;
+}
+
+// Shading-queue bucket per instance: the HIT_BUCKETS - 1 signatures covering the most
+// instanced triangles get their own bucket, all others share the last one.
+std::vector<uint8_t> instance_buckets(const tt_scene_desc* d) {
+    std::map<uint32_t, uint64_t> weight;
+    std::vector<uint32_t> sig(d->instance_count);
+    for (uint32_t i = 0; i < d->instance_count; ++i) {
+        const tt_instance& in = d->instances[i];
+        sig[i] = shading_signature(d->materials[in.material_index].constants);
+        weight[sig[i]] += d->meshes[in.mesh_index].index_count / 3u + 1u;
+    }
+    std::vector<std::pair<uint64_t, uint32_t>> order;
+    for (auto& kv : weight) order.push_back({kv.second, kv.first});
+    std::sort(order.begin(), order.end(), [](auto& a, auto& b) { return a.first != b.first ? a.first > b.first : a.second < b.second; });
+    std::map<uint32_t, uint8_t> bucket;
+    for (size_t k = 0; k < order.size(); ++k) bucket[order[k].second] = (uint8_t)std::min<size_t>(k, HIT_BUCKETS - 1);
+    std::vector<uint8_t> out(std::max<uint32_t>(d->instance_count, 1), 0);
+    for (uint32_t i = 0; i < d->instance_count; ++i) out[i] = bucket[sig[i]];
+    return out;
+}
+
 // Host-side validation: every index the kernels will follow must be in range.
 void validate_scene(const tt_scene_desc* d) {
     require(d != nullptr, "scene desc is null");
@@ -267,8 +304,8 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
         b.pa1.alloc(16ull * slots);
         b.pa0.alloc(16ull * slots);
         b.pe.alloc(16ull * slots);
-        b.hit.alloc(16ull * slots);
-        b.hslot.alloc(4ull * slots);
+        b.hit.alloc(16ull * HIT_BUCKETS * slots);
+        b.hslot.alloc(4ull * HIT_BUCKETS * slots);
         b.active.alloc(4ull * slots);
         b.shadow.alloc(32ull * slots);
         b.slots = slots;
@@ -534,6 +571,8 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             xf[4ull * i + 3] = v;
         }
         upload(s->inst_xform, xf.data(), xf.size(), st);
+        std::vector<uint8_t> buckets = instance_buckets(d);
+        upload(s->inst_bucket, buckets.data(), buckets.size(), st);
         BuildInput bi{s->positions.as<int16_t>(), s->indices.as<uint32_t>(), d->meshes, d->mesh_count,
                       d->instances, d->instance_count};
         uint64_t instanced = 0;
@@ -563,6 +602,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.meshes = s->meshes.as<tt_mesh>();
         ds.emissive = s->emissive.as<tt_emissive_triangle>();
         ds.inst_xform = s->inst_xform.as<float4>();
+        ds.inst_bucket = s->inst_bucket.as<uint8_t>();
         ds.emissive_count = d->emissive_triangle_count;
         ds.instance_count = d->instance_count;
         tt_scene_stats& stt = s->stats;
@@ -594,7 +634,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             stt.accel = TT_ACCEL_TWO_LEVEL;
         }
         stt.device_bytes = s->positions.bytes + s->indices.bytes + s->vertices.bytes + s->materials.bytes + s->meshes.bytes +
-                           s->instances.bytes + s->emissive.bytes + s->inst_xform.bytes + s->bvh.blas.bytes +
+                           s->instances.bytes + s->emissive.bytes + s->inst_xform.bytes + s->inst_bucket.bytes + s->bvh.blas.bytes +
                            s->bvh.tris.bytes + s->bvh.tlas.bytes + s->bvh.flat_nodes_buf.bytes +
                            s->bvh.flat_tris.bytes;
         stt.max_stack = need_stack;

@@ -1,9 +1,12 @@
 // GPU LBVH build: the replacement for the driver-side BLAS/TLAS builds of the reference
 // (src/scene.rs:130-171 -> crates/tinytrace_backend/src/resource.rs:728-880, 891-1085).
 //
-// Pipeline (one pass builds every mesh's BLAS at once; a second pass builds the TLAS):
-//   1. primitive boxes (triangles: dequantised snorm16 vertices; instances: the 8 transformed
-//      corners of their mesh box) and per-segment centroid bounds (float atomics);
+// Two structures share the pipeline below.  Two-level: one pass builds every mesh's BLAS at
+// once (segment = mesh), a second pass the TLAS over instances.  Flat: one pass over the world
+// boxes of all (instance, triangle) pairs (one segment).
+//   1. primitive boxes (triangles: dequantised snorm16 vertices, transformed to world space for
+//      the flat structure; instances: the 8 transformed corners of their mesh box) and
+//      per-segment centroid bounds (float atomics);
 //   2. 30-bit Morton codes of the centroids, normalised per segment, prefixed by the segment
 //      (mesh) index: key = segment << 30 | morton;
 //   3. stable LSD radix sort of (key, primitive) in 8-bit digits;
@@ -11,8 +14,8 @@
 //      each segment's primitives form exactly one subtree;
 //   5. bottom-up box refit with one atomic visit counter per node;
 //   6. collapse to 4-wide nodes level by level from the segment roots (greedy expansion of
-//      the largest-area child, subtrees of <= leaf_max primitives become leaves) and 8-bit
-//      quantisation of the child boxes relative to the node box.
+//      the largest-area child, subtrees of <= leaf_max primitives become leaves), child boxes
+//      stored as float planes (128-byte nodes).
 // Every step is deterministic; the CPU oracle restates the same build and the tests compare
 // the node arrays byte for byte.
 #include <cuda_runtime.h>

@@ -17,14 +17,16 @@ struct RenderParams {
 };
 
 // Wavefront integrator (wavefront.cu): device pointers of the slot pool and queues.
+constexpr uint32_t HIT_BUCKETS = 4;                // shading queues, one per material bucket
+constexpr uint32_t WF_COUNTERS = 5 + HIT_BUCKETS;  // words of WfParams::counters
 struct WfParams {
     float4 *org, *dir, *thr, *acc, *pa1, *pa0, *pe;
-    uint4* hit;          // shading queue: hit records
-    uint32_t* hslot;     // shading queue: slots
+    uint4* hit;          // shading queues: hit records, HIT_BUCKETS x P
+    uint32_t* hslot;     // shading queues: slots, HIT_BUCKETS x P
     uint32_t* active;
     float4* shadow;
     uint32_t* counters;  // [0] next work item, [1] active paths, [2] shadow rays, [3]/[4] trace queue heads,
-                         // [5] shading queue length
+                         // [5 + b] length of shading queue b
     float4* samples;     // chunk_spp x WH per-sample radiance (band order)
     float4* running;     // WH running per-pixel sums across chunks
     uint32_t P, WH;

@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
 #define TT_TRACE_MIN_BLOCKS 6
 #endif
 #ifndef TT_REFILL_LANES
-#define TT_REFILL_LANES 16
+#define TT_REFILL_LANES 20
 #endif
 constexpr int TR_BLOCK = 128;
 constexpr int REFILL_LANES = TT_REFILL_LANES;
@@ -219,11 +219,19 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                 }
             } else {
                 // hits go to the compacted shading queue; a miss adds the sky (integrate.glsl:272-276)
+                // one queue per material bucket, so that the shade stage's warps share lobe sets
                 bool is_hit = fin && h.hit;
-                uint32_t pos = warp_append(&w.counters[5], is_hit);
+                uint32_t bucket = is_hit ? (uint32_t)__ldg(sc.inst_bucket + h.instance) : 0u;
+                uint32_t pos = 0u;
+#pragma unroll
+                for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
+                    uint32_t pb = warp_append(&w.counters[5 + b], is_hit && bucket == b);
+                    pos = bucket == b ? pb : pos;
+                }
                 if (is_hit) {
-                    w.hslot[pos] = slot;
-                    w.hit[pos] = make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim);
+                    uint64_t at = (uint64_t)bucket * w.P + pos;
+                    w.hslot[at] = slot;
+                    w.hit[at] = make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim);
                     if (COUNT) hits++;
                 } else if (fin) {
                     f3 thr = xyz(w.thr[slot]);
@@ -253,20 +261,31 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
 }
 
 #ifndef TT_SHADE_MIN_BLOCKS
-#define TT_SHADE_MIN_BLOCKS 1
+#define TT_SHADE_MIN_BLOCKS 6
 #endif
 __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel(const __grid_constant__ RenderParams p,
                                                             const __grid_constant__ WfParams w) {
+    // thread q shades entry q of the bucket queues laid end to end
     uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
-    uint32_t n = w.counters[5];
+    uint64_t at = 0;
+    uint32_t start = 0;
+    bool have = false;
+#pragma unroll
+    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
+        uint32_t cnt = w.counters[5 + b];
+        bool in = !have && q >= start && q < start + cnt;
+        at = in ? (uint64_t)b * w.P + (q - start) : at;
+        have = have || in;
+        start += cnt;
+    }
     bool want_shadow = false;
     uint32_t s = 0, light = 0;
     f3 sh_org = splat(0.0f), sh_dir = splat(0.0f);
-    if (q < n) {
+    if (have) {
         const tt_constants& c = p.c;
         const DevScene& sc = p.sc;
-        s = w.hslot[q];
-        uint4 hv = w.hit[q];
+        s = w.hslot[at];
+        uint4 hv = w.hit[at];
         float4 o4 = w.org[s], d4 = w.dir[s], t4 = w.thr[s], a4 = w.acc[s];
         f3 thr = xyz(t4), acc = xyz(a4), ray_dir = xyz(d4);
         uint32_t g = __float_as_uint(d4.w), bounce = __float_as_uint(o4.w);
@@ -384,9 +403,9 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
         w.chunk_sample0 = s0;
         w.chunk_spp = std::min(max_chunk, spp - s0);
         w.chunk_items = WH * w.chunk_spp;
-        check_cuda(cudaMemsetAsync(w.counters, 0, 32, st), "memset");
+        check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * WF_COUNTERS, st), "memset");
         while (true) {
-            check_cuda(cudaMemsetAsync(w.counters + 1, 0, 20, st), "memset");
+            check_cuda(cudaMemsetAsync(w.counters + 1, 0, 4ull * (WF_COUNTERS - 1), st), "memset");
             stage_begin(timer, TT_STAGE_REGEN, st);
             wf_regen_kernel<<<regen_grid, REGEN_BLOCK, 0, st>>>(p, w);
             stage_end(timer, st);
