@@ -5,11 +5,12 @@ GPUs, every rank renders its own full frame; scaling is weak).
 
 Prints one JSON line (rank 0).  `value` is the device-resident throughput (scene, BVH and
 target already in HBM), `e2e` the same metric through Renderer.render_to_texture with the
-target downloaded to pinned host memory every step.  `roofline` relates the integrate
-kernel's algorithmic bytes (BVH nodes, triangle records, instance records, hit shading
-data; counted by the instrumented kernel on the same frame) to its CUDA-event duration and
-the measured HBM copy bandwidth.  `cpu_baseline` times the CPU oracle on a bounded sample
-of the same frame.
+target downloaded to pinned host memory every step.  `roofline` relates the dominant
+kernel's (wf_trace_kernel: extension and shadow rays) algorithmic bytes per launch (BVH
+nodes, triangle records, object-ray set-ups, ray state; counted by the instrumented kernels
+on the same frame) to its mean CUDA-event launch duration and the measured HBM copy
+bandwidth; `traffic` is its DRAM bytes per launch from the committed ncu summary.
+`cpu_baseline` times the CPU oracle on a bounded sample of the same frame.
 
 --impl reference times the reference path tracer's CPU restatement (the oracle: the
 reference itself is Rust + Vulkan/GLSL and cannot run on this machine) on the host cores.
@@ -53,6 +54,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--integrator", default="wavefront", choices=["wavefront", "megakernel"])
     p.add_argument("--slots", type=int, default=0, help="wavefront paths in flight (0 = library default)")
+    p.add_argument("--host-loop", action="store_true", help="drive the wavefront loop from the host (no CUDA graph)")
+    p.add_argument("--no-autotune", action="store_true", help="skip tt_autotune before the warm-up")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level"],
                    help="acceleration structure (auto = flat up to 2^26 instanced triangles)")
     return p.parse_args()
@@ -163,12 +166,12 @@ RAY_STATE_BYTES = 64
 PROFILE = ROOT / "profiles" / "wf_trace_kernel_icosphere_field_1080p.md"
 
 
-def ncu_dram_bytes_per_ray() -> float | None:
-    """DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced ray of
-    wf_trace_kernel, from the committed ncu summary of the 1-spp capture of this scene."""
+def ncu_traffic_per_launch() -> float | None:
+    """dram__bytes_read.sum + dram__bytes_write.sum per wf_trace_kernel launch of this
+    workload (mean over one frame's launches), from the committed ncu summary."""
     if not PROFILE.exists():
         return None
-    m = re.search(r"dram_bytes_per_ray:\s*([0-9.eE+]+)", PROFILE.read_text())
+    m = re.search(r"traffic_per_launch_bytes:\s*([0-9.eE+]+)", PROFILE.read_text())
     return float(m.group(1)) if m else None
 
 
@@ -275,8 +278,12 @@ def run_ours(a, dist: Dist):
         r.render_to_target()
         r.present()
 
-    # per-launch CUDA events on the integrator's stream, read after each step
-    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 1))
+    check(lib.tt_set_option(ctx, native.TT_OPTION_GRAPHS, 0 if a.host_loop else 1))
+    tuning = None
+    if not a.no_autotune and a.integrator == "wavefront" and not a.slots:
+        t = r.autotune(sample_count=8)  # short 8-spp renders of the same frame, before the warm-up
+        tuning = {"slots": t.slots, "refill_lanes": t.refill_lanes, "trace_blocks_per_sm": t.trace_blocks_per_sm,
+                  "renders": t.renders, "default_ms_8spp": t.default_ms, "tuned_ms_8spp": t.best_ms}
     for _ in range(a.warmup):
         step()
     check(lib.tt_synchronize(ctx))
@@ -286,17 +293,9 @@ def run_ours(a, dist: Dist):
     check(lib.tt_synchronize(ctx))
     check(lib.tt_event_record(ctx, 0))
     kernel_ns = []
-    stage_ns = np.zeros(native.TT_STAGE_COUNT)
-    stage_launches = np.zeros(native.TT_STAGE_COUNT, np.int64)
-    stage_overflow = False
     for _ in range(a.steps):
         step()
         kernel_ns.append(r.timings().integrate * 1e9)  # synchronises; integrate-kernel events
-        stt = native.StageTimings()
-        check(lib.tt_stage_timings_get(ctx, ctypes.byref(stt)))
-        stage_ns += np.array(stt.ns[:], np.float64)
-        stage_launches += np.array(stt.launches[:], np.int64)
-        stage_overflow |= bool(stt.overflow)
     check(lib.tt_event_record(ctx, 1))
     ms = ctypes.c_float()
     check(lib.tt_event_elapsed_ms(ctx, 0, 1, ctypes.byref(ms)))
@@ -305,6 +304,30 @@ def run_ours(a, dist: Dist):
     dist.barrier()
     total_s = dist.max(ms.value / 1e3)
     value = samples_per_step * a.steps * dist.world / total_s / 1e6
+
+    # per-launch timing: a second loop of the same K steps with CUDA events around every
+    # integrator launch on its stream (this drives the loop from the host)
+    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 1))
+    step()
+    stage_ns = np.zeros(native.TT_STAGE_COUNT)
+    stage_launches = np.zeros(native.TT_STAGE_COUNT, np.int64)
+    stage_overflow = False
+    timed_ns = []
+    for _ in range(a.steps):
+        step()
+        timed_ns.append(r.timings().integrate * 1e9)
+        stt = native.StageTimings()
+        check(lib.tt_stage_timings_get(ctx, ctypes.byref(stt)))
+        stage_ns += np.array(stt.ns[:], np.float64)
+        stage_launches += np.array(stt.launches[:], np.int64)
+        stage_overflow |= bool(stt.overflow)
+    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 0))
+    regen_per_step = int(stage_launches[native.TT_STAGE_REGEN]) // a.steps
+    reduce_per_step = int(stage_launches[native.TT_STAGE_REDUCE]) // a.steps
+    if a.host_loop or a.integrator != "wavefront":
+        launches_per_step = int(stage_launches.sum()) // a.steps
+    else:  # graph loop: regen, control, extend, shade and shadow every iteration, then the reduction
+        launches_per_step = 5 * regen_per_step + reduce_per_step
 
     # end to end through the public API: render_to_texture into pinned host memory
     host = ctypes.c_void_p()
@@ -344,14 +367,13 @@ def run_ours(a, dist: Dist):
         achieved = bytes_per_launch / launch_s / 1e9
         node_achieved = node_bytes / trace_s / 1e9
         rays_per_launch = cnt.rays / trace_launches
-        per_ray = ncu_dram_bytes_per_ray()
-        traffic = per_ray * rays_per_launch if per_ray is not None else None
+        default_workload = (W, H, spp, w.config.bounce_count) == (1920, 1080, 64, 8)
+        traffic = ncu_traffic_per_launch() if default_workload and a.accel != "two_level" else None
     else:  # the megakernel does everything in one launch
         bytes_per_launch, launch_s = trace_bytes, kernel_s
         achieved = trace_bytes / kernel_s / 1e9
         node_achieved = node_bytes / kernel_s / 1e9
         rays_per_launch, traffic = cnt.rays, None
-    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 0))
 
     out_line = None
     if dist.rank == 0:
@@ -371,7 +393,8 @@ def run_ours(a, dist: Dist):
                        "light_sampling": "next_event_estimation",
                        "l2": "flushed before every step (512 MiB memset, inside the timed region)",
                        "parallelism": f"replicas x{dist.world}", "integrator": a.integrator,
-                       "accel": "flat" if stats.accel == native.TT_ACCEL_FLAT else "two_level"},
+                       "accel": "flat" if stats.accel == native.TT_ACCEL_FLAT else "two_level",
+                       "autotune": tuning},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 368, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -383,7 +406,8 @@ def run_ours(a, dist: Dist):
                          "bytes_per_unit": {"node": NODE_BYTES, "triangle_record": TRI_RECORD_BYTES,
                                             "instance_ray_setup": INSTANCE_RAY_BYTES, "ray_state": RAY_STATE_BYTES},
                          "node_fetch_gbs": node_achieved, "node_fetch_frac": node_achieved / peak,
-                         "traffic_source": "ncu dram bytes per ray of the 1-spp capture x rays per launch"},
+                         "traffic_source": "ncu dram bytes per launch, full workload "
+                                           "(profiles/wf_trace_kernel_icosphere_field_1080p.md)"},
             "stages": stages,
             "counters": {"rays": cnt.rays, "blas_nodes": cnt.blas_nodes, "tlas_nodes": cnt.tlas_nodes,
                          "triangles": cnt.triangles, "instances": cnt.instances, "hits": cnt.hits,
@@ -392,8 +416,9 @@ def run_ours(a, dist: Dist):
                       "blas_levels": int(stats.blas_levels), "tlas_levels": int(stats.tlas_levels),
                       "device_bytes": int(stats.device_bytes), "build_ms": None},
             "clocks": clk,
-            "gpu_launches": int(stage_launches.sum()),
+            "gpu_launches": launches_per_step * a.steps,
             "gpu_launches_overflow": stage_overflow,
+            "loop": "host-driven" if a.host_loop else "device-side while loop in one CUDA graph per render",
             "cpu_baseline": cpu,
         }
         t = native.Timings()

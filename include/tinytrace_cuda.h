@@ -63,6 +63,10 @@ extern "C" {
 #define TT_OPTION_WAVEFRONT_SLOTS 2 /* paths in flight of the wavefront integrator; 0 = default */
 #define TT_OPTION_ACCEL 3           /* TT_ACCEL_*: structure built by later tt_scene_create calls */
 #define TT_OPTION_STAGE_TIMING 4    /* 1: CUDA events around every integrator launch (tt_stage_timings_get) */
+#define TT_OPTION_GRAPHS 5          /* 1 (default): the wavefront loop runs on the device inside one CUDA graph per
+                                       render; 0: the host drives it (also used while stage timing is on) */
+#define TT_OPTION_REFILL_LANES 6    /* trace warps refill idle lanes below this many busy lanes (1..32; 20) */
+#define TT_OPTION_TRACE_BLOCKS_PER_SM 7 /* resident blocks per SM of the trace kernel (0 = all that fit) */
 /* acceleration structures (tt_set_option TT_OPTION_ACCEL; tt_scene_stats.accel) */
 #define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
 #define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */
@@ -242,6 +246,17 @@ int32_t tt_tonemap(tt_context* ctx, tt_handle image, const tt_constants* constan
 int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value);
 /* replaces: src/lib.rs:167-178 Renderer::timings */
 int32_t tt_timings_get(tt_context* ctx, tt_timings* out);
+/* Autotuner (no reference counterpart: the reference's ray-query pipeline has no tunables).
+ * Times renders of `constants` (give it a few samples per pixel) into `target` while it
+ * varies, one after the other, the wavefront pool size, the trace kernel's refill threshold
+ * and its resident blocks per SM, keeps the fastest of each, and leaves those options set on
+ * the context.  The last render's image stays in `target`. */
+typedef struct tt_tune_result {
+    uint32_t slots, refill_lanes, trace_blocks_per_sm, renders;
+    float default_ms, best_ms;
+} tt_tune_result;
+int32_t tt_autotune(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target,
+                    tt_tune_result* out);
 /* Per-stage device time of the last render (synchronises the context's stream). */
 int32_t tt_stage_timings_get(tt_context* ctx, tt_stage_timings* out);
 

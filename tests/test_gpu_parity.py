@@ -236,3 +236,45 @@ def test_tonemap_bits(gpu_context):
     exp8 = (np.clip(np.nan_to_num(ref, nan=0.0), 0, 1) * np.float32(255) + np.float32(0.5)).astype(np.uint8)
     exp8[..., 3] = 255
     assert np.array_equal(out8, exp8)
+
+
+@pytest.mark.parametrize("graphs", [0, 1])
+def test_render_host_and_graph_loops(gpu_context, graphs):
+    """The wavefront loop driven from the host and as a device-side while loop inside one CUDA
+    graph give the oracle's image; the small pool makes the loop run many iterations and two
+    sample chunks exercise two loops in one graph."""
+    from tinytrace_gb300.renderer import Renderer
+
+    w = scenes.Workload("cornell_loop", scenes.cornell_box(), scenes.cornell_workload().camera, (40, 24),
+                        scenes.Config(bounce_count=5, sample_count=70))
+    r = Renderer(w.extent)
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_GRAPHS, graphs))
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_WAVEFRONT_SLOTS, 300))
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    r.set_config(w.config)
+    c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
+    gpu = r.render_to_texture()
+    cpu = oracle.OracleScene(r.scene_arrays).render(c)
+    assert_same_bits(gpu, cpu, f"loop graphs={graphs}")
+    r.close()
+
+
+def test_autotune_keeps_the_image(gpu_context):
+    """tt_autotune leaves valid options on the context and renders stay bit-exact with them."""
+    from tinytrace_gb300.renderer import Renderer
+
+    w = scenes.Workload("field_tune", _small_field(), scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)),
+                        (96, 54), scenes.Config(bounce_count=6, sample_count=4))
+    r = Renderer(w.extent)
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    r.set_config(w.config)
+    res = r.autotune(sample_count=2)
+    assert res.renders >= 10 and res.best_ms <= res.default_ms and res.best_ms > 0
+    assert res.slots >= 128 and 1 <= res.refill_lanes <= 32 and res.trace_blocks_per_sm >= 1
+    c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
+    gpu = r.render_to_texture()
+    cpu = oracle.OracleScene(r.scene_arrays).render(c)
+    assert_same_bits(gpu, cpu, "after autotune")
+    r.close()

@@ -113,6 +113,11 @@ struct tt_context {
     uint32_t accel = TT_ACCEL_AUTO;
     tt::WavefrontBuffers wf;
     bool stage_timing = false;
+    bool graphs = true;
+    uint32_t refill_lanes = 20;       // TT_OPTION_REFILL_LANES
+    uint32_t trace_blocks_per_sm = 0; // TT_OPTION_TRACE_BLOCKS_PER_SM (0 = as many as fit)
+    int occupancy_sms = 0, occupancy_blocks = 0;
+    cudaStream_t capture[2] = {nullptr, nullptr};  // capture streams of the graph-driven loop
     std::vector<cudaEvent_t> stage_events;  // 2 * StageTimer::MAX_LAUNCHES, created on first use
     tt::StageTimer stage_timer;
 };
@@ -336,6 +341,11 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
     w.running = b.running.as<float4>();
     w.P = slots;
     w.chunk_spp = chunk_spp;
+    w.refill = ctx->refill_lanes;
+    if (ctx->occupancy_sms == 0) trace_occupancy(&ctx->occupancy_sms, &ctx->occupancy_blocks);
+    int per_sm = ctx->trace_blocks_per_sm ? std::min<int>(ctx->trace_blocks_per_sm, ctx->occupancy_blocks)
+                                          : ctx->occupancy_blocks;
+    w.trace_blocks = (uint32_t)std::max(1, ctx->occupancy_sms * per_sm);
     return w;
 }
 
@@ -372,7 +382,11 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     }
     ctx->stage_timer.count = timer ? 0 : -1;  // -1: the last render was not timed per stage
     check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
-    if (wavefront) {
+    if (wavefront && ctx->graphs && !timer) {
+        for (auto& cs : ctx->capture)
+            if (!cs) check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+        render_wavefront_graph(p, w, counted, ctx->stream, ctx->capture[0], ctx->capture[1]);
+    } else if (wavefront) {
         render_wavefront(p, w, ctx->err_host + 1, counted, ctx->stream, timer);
     } else {
         stage_begin(timer, TT_STAGE_MEGAKERNEL, ctx->stream);
@@ -462,6 +476,8 @@ int32_t tt_context_destroy(tt_context* ctx) {
         for (auto& ev : ctx->ev_post) cudaEventDestroy(ev);
         for (auto& ev : ctx->user_events) cudaEventDestroy(ev);
         for (auto& ev : ctx->stage_events) cudaEventDestroy(ev);
+        for (auto& cs : ctx->capture)
+            if (cs) cudaStreamDestroy(cs);
         if (ctx->err_host) cudaFreeHost(ctx->err_host);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -718,6 +734,15 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else if (option == TT_OPTION_WAVEFRONT_SLOTS) {
             require(value <= (1ull << 26), "wavefront slot count above 2^26");
             ctx->wavefront_slots = (uint32_t)value;
+        } else if (option == TT_OPTION_REFILL_LANES) {
+            require(value >= 1 && value <= 32, "refill lanes must be in 1..32");
+            ctx->refill_lanes = (uint32_t)value;
+        } else if (option == TT_OPTION_TRACE_BLOCKS_PER_SM) {
+            require(value <= 64, "trace blocks per SM above 64");
+            ctx->trace_blocks_per_sm = (uint32_t)value;
+        } else if (option == TT_OPTION_GRAPHS) {
+            require(value <= 1, "graphs is 0 or 1");
+            ctx->graphs = value != 0;
         } else if (option == TT_OPTION_STAGE_TIMING) {
             require(value <= 1, "stage timing is 0 or 1");
             ctx->stage_timing = value != 0;
@@ -728,6 +753,66 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else {
             fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
         }
+    });
+}
+
+int32_t tt_autotune(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target,
+                    tt_tune_result* out) {
+    return guarded([&] {
+        require(ctx && constants && out, "null argument");
+        use_device(ctx);
+        require(ctx->integrator == TT_INTEGRATOR_WAVEFRONT, "the autotuner tunes the wavefront integrator");
+        bool timing = ctx->stage_timing;
+        ctx->stage_timing = false;
+        *out = tt_tune_result{};
+        // integrate time of one render (the fastest of two, after a warm-up render)
+        auto measure = [&]() -> float {
+            float best = INFINITY;
+            for (int k = 0; k < 3; ++k) {
+                render_impl(ctx, scene, constants, target, false, nullptr);
+                sync(ctx);
+                float ms = 0.0f;
+                check_cuda(cudaEventElapsedTime(&ms, ctx->ev_integrate[0], ctx->ev_integrate[1]), "elapsed");
+                if (k > 0) best = std::min(best, ms);
+                out->renders++;
+            }
+            return best;
+        };
+        if (ctx->occupancy_sms == 0) trace_occupancy(&ctx->occupancy_sms, &ctx->occupancy_blocks);
+        out->default_ms = measure();
+        float best = out->default_ms;
+        auto tune = [&](uint32_t& option, std::vector<uint32_t> candidates) {
+            uint32_t keep = option;
+            for (uint32_t v : candidates) {
+                if (v == keep) continue;
+                option = v;
+                float ms = measure();
+                if (ms < best) {
+                    best = ms;
+                    keep = v;
+                }
+            }
+            option = keep;
+        };
+        uint64_t items = (uint64_t)constants->screen_size[0] * constants->screen_size[1] *
+                         std::min<uint32_t>(constants->sample_count, WAVEFRONT_MAX_CHUNK_SPP);
+        std::vector<uint32_t> slots;
+        for (uint32_t s = 1u << 18; s <= (1u << 22); s <<= 1)
+            if (s <= std::max<uint64_t>(items, 1u << 18)) slots.push_back(s);
+        if (ctx->wavefront_slots == 0) ctx->wavefront_slots = WAVEFRONT_DEFAULT_SLOTS;
+        tune(ctx->wavefront_slots, slots);
+        tune(ctx->refill_lanes, {8u, 12u, 16u, 20u, 24u, 28u});
+        std::vector<uint32_t> blocks;
+        for (int b = ctx->occupancy_blocks; b >= 1 && b >= ctx->occupancy_blocks - 2; --b) blocks.push_back((uint32_t)b);
+        if (ctx->trace_blocks_per_sm == 0) ctx->trace_blocks_per_sm = (uint32_t)ctx->occupancy_blocks;
+        tune(ctx->trace_blocks_per_sm, blocks);
+        render_impl(ctx, scene, constants, target, false, nullptr);  // leave the tuned image in the target
+        out->renders++;
+        ctx->stage_timing = timing;
+        out->slots = ctx->wavefront_slots;
+        out->refill_lanes = ctx->refill_lanes;
+        out->trace_blocks_per_sm = ctx->trace_blocks_per_sm;
+        out->best_ms = best;
     });
 }
 

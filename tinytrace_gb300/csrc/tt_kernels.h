@@ -18,7 +18,9 @@ struct RenderParams {
 
 // Wavefront integrator (wavefront.cu): device pointers of the slot pool and queues.
 constexpr uint32_t HIT_BUCKETS = 4;                // shading queues, one per material bucket
-constexpr uint32_t WF_COUNTERS = 5 + HIT_BUCKETS;  // words of WfParams::counters
+constexpr uint32_t WF_COUNTERS = 5 + HIT_BUCKETS;  // queue words of WfParams::counters
+constexpr uint32_t CTRL_ITERATION = 15;            // iteration count of the device-side loop
+constexpr uint32_t CTRL_WORDS = 16;                // words of WfParams::counters
 struct WfParams {
     float4 *org, *dir, *thr, *acc, *pa1, *pa0, *pe;
     uint4* hit;          // shading queues: hit records, HIT_BUCKETS x P
@@ -31,7 +33,11 @@ struct WfParams {
     float4* running;     // WH running per-pixel sums across chunks
     uint32_t P, WH;
     uint32_t chunk_sample0, chunk_spp, chunk_items;
+    uint32_t refill;        // a trace warp refills its idle lanes when fewer than this many hold a ray
+    uint32_t trace_blocks;  // grid of the persistent trace kernel (host side)
 };
+// SM count and resident blocks per SM of the persistent trace kernel.
+void trace_occupancy(int* sms, int* blocks_per_sm);
 // Optional per-launch timing: a pair of CUDA events recorded on the launching stream around
 // each integrator launch, tagged with its TT_STAGE_*.  `events` holds 2 * MAX_LAUNCHES events
 // owned by the context; launches past MAX_LAUNCHES are not recorded (overflow).
@@ -63,6 +69,11 @@ inline void stage_end(StageTimer* t, cudaStream_t st) {
 // buffers hold.  Synchronises `st` once per iteration to read the active-path count.
 void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
                       StageTimer* timer);
+// The same loop with no host synchronisation: each sample chunk's iterations run as a
+// device-side while loop (a conditional node) of one CUDA graph, captured on `cs` and
+// `body_stream` and launched on `st`.
+void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cudaStream_t st, cudaStream_t cs,
+                            cudaStream_t body_stream);
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st);
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out,
                     cudaStream_t st);

@@ -130,17 +130,13 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
 }
 
 // Extension and shadow rays: persistent warps with per-lane refill.  Each lane traces one ray
-// at a time; when fewer than REFILL_LANES lanes of a warp still have a ray, the idle lanes
+// at a time; when fewer than w.refill lanes of a warp still have a ray, the idle lanes
 // fetch new rays from the queue (one atomicAdd per warp), so warps keep their lanes busy
 // instead of waiting for their longest ray (the dynamic fetch of Aila & Laine 2009).
 #ifndef TT_TRACE_MIN_BLOCKS
 #define TT_TRACE_MIN_BLOCKS 6
 #endif
-#ifndef TT_REFILL_LANES
-#define TT_REFILL_LANES 20
-#endif
 constexpr int TR_BLOCK = 128;
-constexpr int REFILL_LANES = TT_REFILL_LANES;
 
 template <bool COUNT, bool SHADOW, int ACCEL>
 __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel(const __grid_constant__ RenderParams p,
@@ -245,7 +241,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                 warp_steps++;
                 lane_steps += (uint32_t)__popc(am);
             }
-            if (am == 0u || (!drained && __popc(am) < REFILL_LANES)) break;
+            if (am == 0u || (!drained && (uint32_t)__popc(am) < w.refill)) break;
         }
     }
     if (COUNT) {
@@ -381,6 +377,86 @@ static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid
     }
 }
 
+// Device-side loop control: counts the chunk's iterations and keeps the graph's while loop
+// running while paths are live, for at most `limit` iterations (then ERR_ITERATION_LIMIT).
+__global__ void wf_control_kernel(uint32_t* counters, cudaGraphConditionalHandle handle, uint32_t limit,
+                                  uint32_t* err) {
+    uint32_t n = counters[1];
+    uint32_t it = ++counters[CTRL_ITERATION];
+    bool more = n > 0u && it < limit;
+    if (n > 0u && it >= limit) atomicOr(err, ERR_ITERATION_LIMIT);
+    cudaGraphSetConditional(handle, more ? 1u : 0u);
+}
+
+void trace_occupancy(int* sms, int* blocks_per_sm) {
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    check_cuda(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, wf_trace_kernel<false, false, ACCEL_FLAT_ONLY>,
+                                                             TR_BLOCK, 0),
+               "occupancy");
+}
+
+void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cudaStream_t st, cudaStream_t cs,
+                            cudaStream_t body_stream) {
+    const tt_constants& c = p.c;
+    uint32_t WH = c.screen_size[0] * c.screen_size[1];
+    uint32_t spp = c.sample_count;
+    uint32_t max_chunk = w.chunk_spp;
+    w.WH = WH;
+    unsigned regen_grid = (w.P + REGEN_BLOCK - 1) / REGEN_BLOCK;
+    unsigned shade_grid = (w.P + WF_BLOCK - 1) / WF_BLOCK;
+    unsigned tgrid = w.trace_blocks;
+    cudaGraph_t g = nullptr;
+    check_cuda(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+    check_cuda(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "capture");
+    check_cuda(cudaMemsetAsync(w.acc, 0, 16ull * w.P, cs), "memset");  // every slot starts free
+    for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
+        w.chunk_sample0 = s0;
+        w.chunk_spp = std::min(max_chunk, spp - s0);
+        w.chunk_items = WH * w.chunk_spp;
+        check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CTRL_WORDS, cs), "memset");
+        // while (paths are live) { regen; extend; shade; shadow }
+        cudaStreamCaptureStatus status;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        check_cuda(cudaStreamGetCaptureInfo(cs, &status, nullptr, &cg, &deps, nullptr, &ndeps), "capture info");
+        cudaGraphConditionalHandle handle;
+        check_cuda(cudaGraphConditionalHandleCreate(&handle, cg, 1u, cudaGraphCondAssignDefault), "conditional handle");
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop;
+        check_cuda(cudaGraphAddNode(&loop, cg, deps, nullptr, ndeps, &cp), "conditional node");
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        check_cuda(cudaStreamBeginCaptureToGraph(body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                   "body capture");
+        uint64_t rounds = (uint64_t)w.chunk_items / w.P + 1u;
+        uint32_t limit = (uint32_t)std::min<uint64_t>(2ull * rounds * (c.bounce_count + 2u) + 16u, 0x7fffffffu);
+        check_cuda(cudaMemsetAsync(w.counters + 1, 0, 4ull * (WF_COUNTERS - 1), body_stream), "memset");
+        wf_regen_kernel<<<regen_grid, REGEN_BLOCK, 0, body_stream>>>(p, w);
+        wf_control_kernel<<<1, 1, 0, body_stream>>>(w.counters, handle, limit, p.err);
+        launch_trace<false>(p, w, tgrid, counted, body_stream);
+        wf_shade_kernel<<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w);
+        launch_trace<true>(p, w, tgrid, counted, body_stream);
+        check_cuda(cudaStreamEndCapture(body_stream, &body), "body capture end");
+        check_cuda(cudaStreamUpdateCaptureDependencies(cs, &loop, nullptr, 1, cudaStreamSetCaptureDependencies),
+                   "capture dependencies");
+        wf_reduce_kernel<<<(WH + 255) / 256, 256, 0, cs>>>(p, w, s0 + w.chunk_spp >= spp ? 1 : 0);
+    }
+    check_cuda(cudaStreamEndCapture(cs, &g), "capture end");
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    check_cuda(e, "cudaGraphInstantiate");
+    e = cudaGraphLaunch(exec, st);
+    cudaGraphExecDestroy(exec);  // freed when the launch completes
+    check_cuda(e, "cudaGraphLaunch");
+}
+
 void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
                       StageTimer* timer) {
     const tt_constants& c = p.c;
@@ -389,15 +465,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
     uint32_t max_chunk = w.chunk_spp;
     w.WH = WH;
     unsigned regen_grid = (w.P + REGEN_BLOCK - 1) / REGEN_BLOCK;
-    static int trace_blocks = 0;  // resident blocks of the persistent trace kernel on the whole GPU
-    if (trace_blocks == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
-        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
-        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wf_trace_kernel<false, false, ACCEL_FLAT_ONLY>, TR_BLOCK, 0),
-                   "occupancy");
-        trace_blocks = std::max(1, sms * per_sm);
-    }
+    unsigned trace_blocks = w.trace_blocks;
     check_cuda(cudaMemsetAsync(w.acc, 0, 16ull * w.P, st), "memset");  // every slot starts free
     for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
         w.chunk_sample0 = s0;

@@ -46,6 +46,9 @@ TT_ACCEL_AUTO = 0
 TT_ACCEL_FLAT = 1
 TT_ACCEL_TWO_LEVEL = 2
 TT_OPTION_STAGE_TIMING = 4
+TT_OPTION_GRAPHS = 5
+TT_OPTION_REFILL_LANES = 6
+TT_OPTION_TRACE_BLOCKS_PER_SM = 7
 TT_STAGE_REGEN = 0
 TT_STAGE_EXTEND = 1
 TT_STAGE_SHADE = 2
@@ -152,6 +155,11 @@ class StageTimings(ctypes.Structure):
     _fields_ = [("ns", ctypes.c_uint64 * 8), ("launches", ctypes.c_uint64 * 8), ("overflow", ctypes.c_uint64)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_uint32), ("refill_lanes", ctypes.c_uint32), ("trace_blocks_per_sm", ctypes.c_uint32),
+                ("renders", ctypes.c_uint32), ("default_ms", ctypes.c_float), ("best_ms", ctypes.c_float)]
+
+
 class TraversalCounters(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("rays", "blas_nodes", "tlas_nodes", "triangles", "instances", "hits",
                                                "warp_steps", "lane_steps")]
@@ -183,6 +191,7 @@ SIGNATURES = {
     "tt_set_option": (_I32, [_P, _U32, _U64]),
     "tt_timings_get": (_I32, [_P, ctypes.POINTER(Timings)]),
     "tt_stage_timings_get": (_I32, [_P, ctypes.POINTER(StageTimings)]),
+    "tt_autotune": (_I32, [_P, _U64, _P, _U64, ctypes.POINTER(TuneResult)]),
     "tt_bsdf_eval_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_bsdf_sample_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_trace_batch": (_I32, [_P, _U64, _P, _U32, _U32, _P]),

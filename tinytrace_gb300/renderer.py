@@ -264,6 +264,19 @@ class Renderer:
         check(self.context.lib.tt_render(self.context.handle, self.scene, native.ptr(c), self.render_target))
         self.accumulated_frame_count += 1
 
+    def autotune(self, sample_count: int = 8) -> native.TuneResult:
+        """Tunes the wavefront integrator's pool size, refill threshold and trace-kernel
+        residency for the current scene and camera (tt_autotune) with short renders of
+        `sample_count` samples per pixel.  The accumulation restarts afterwards."""
+        cfg = Config(bounce_count=self._config.bounce_count, sample_count=sample_count, tonemap=self._config.tonemap,
+                     light_sampling=self._config.light_sampling)
+        c = make_constants(self.camera, self.extent, cfg, self.context.frame_index(), 0)
+        res = native.TuneResult()
+        check(self.context.lib.tt_autotune(self.context.handle, self.scene, native.ptr(c), self.render_target,
+                                           ctypes.byref(res)))
+        self.accumulated_frame_count = 0
+        return res
+
     def reset_accumulation(self) -> None:
         self.accumulated_frame_count = 0
 
