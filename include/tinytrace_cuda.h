@@ -257,6 +257,43 @@ typedef struct tt_tune_result {
 } tt_tune_result;
 int32_t tt_autotune(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target,
                     tt_tune_result* out);
+/* ---------------------------------------------------------------- serving
+ * Continuous-batching render server (no reference counterpart: the reference renders one frame
+ * at a time on the caller's thread).  Scenes are created on the server's context beforehand and
+ * stay resident; while a server lives, the caller neither clears the scene lifetime nor uses the
+ * context from another thread.  Submitted requests (scene + constants) queue in arrival order; a
+ * scheduler thread admits the head of the queue whenever an execution slot is free and its
+ * device memory fits in the HBM budget next to the requests already in flight, runs it as one
+ * CUDA graph (the wavefront integrator's device-side loop) on the slot's own stream, so that
+ * admitted requests overlap on the device, copies the image into the caller's buffer and marks
+ * the request done.  A request's image is the same, bit for bit, alone or among others. */
+typedef struct tt_server tt_server;
+typedef struct tt_server_config {
+    uint64_t hbm_budget_bytes;  /* device memory in-flight requests may hold (0 = 150 GB) */
+    uint32_t max_inflight;      /* execution slots (0 = 8) */
+    uint32_t paths_per_request; /* wavefront paths in flight per request (0 = 2^20) */
+} tt_server_config;
+typedef struct tt_server_stats {
+    uint64_t submitted, completed, failed, queued, inflight;
+    uint64_t bytes_in_flight, peak_bytes_in_flight, peak_inflight;
+} tt_server_stats;
+#define TT_REQUEST_QUEUED 0
+#define TT_REQUEST_RUNNING 1
+#define TT_REQUEST_DONE 2
+#define TT_REQUEST_FAILED 3
+int32_t tt_server_create(tt_context* ctx, const tt_server_config* config, tt_server** out);
+/* Finishes the queued and in-flight requests, then stops the scheduler. */
+int32_t tt_server_destroy(tt_server* server);
+/* host_rgba32f: width * height * 16 bytes, written when the request completes; it must stay
+ * valid until then.  constants.sample_count and bounce_count must be at least 1. */
+int32_t tt_server_submit(tt_server* server, tt_handle scene, const tt_constants* constants, float* host_rgba32f,
+                         uint64_t bytes, uint64_t* request_id);
+/* Status (TT_REQUEST_*) and, once done, submit-to-completion latency in milliseconds. */
+int32_t tt_server_status(tt_server* server, uint64_t request_id, int32_t* status, double* latency_ms);
+/* Blocks until the request is done or failed, or timeout_ms passes (then TT_ERR_TIMEOUT). */
+int32_t tt_server_wait(tt_server* server, uint64_t request_id, uint32_t timeout_ms, int32_t* status);
+int32_t tt_server_stats_get(tt_server* server, tt_server_stats* out);
+
 /* Per-stage device time of the last render (synchronises the context's stream). */
 int32_t tt_stage_timings_get(tt_context* ctx, tt_stage_timings* out);
 

@@ -349,6 +349,15 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
     return w;
 }
 
+namespace tt {
+void set_last_error(const std::string& message) { g_last_error = message; }
+DevScene scene_view(tt_context* ctx, tt_handle scene) {
+    require(ctx, "null context");
+    return lookup<SceneRes>(ctx, scene, KIND_SCENE)->dev;
+}
+int context_device(tt_context* ctx) { return ctx->device; }
+}  // namespace tt
+
 static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c, tt_handle target, bool counted,
                         tt_traversal_counters* out) {
     require(ctx && c, "null argument");

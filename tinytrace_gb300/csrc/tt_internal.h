@@ -61,6 +61,9 @@ struct BuildInput {
     uint32_t instance_count;
 };
 
+// Thread-local message behind tt_last_error.
+void set_last_error(const std::string& message);
+
 // Builds, on `stream`, either the two-level structure (BLAS with one root per mesh, node index
 // == mesh index, and TLAS with root 0) or, when `flat`, one BVH over the world boxes of all
 // (instance, triangle) pairs (root 0).

@@ -47,6 +47,10 @@ TT_ACCEL_FLAT = 1
 TT_ACCEL_TWO_LEVEL = 2
 TT_OPTION_STAGE_TIMING = 4
 TT_OPTION_GRAPHS = 5
+TT_REQUEST_QUEUED = 0
+TT_REQUEST_RUNNING = 1
+TT_REQUEST_DONE = 2
+TT_REQUEST_FAILED = 3
 TT_OPTION_REFILL_LANES = 6
 TT_OPTION_TRACE_BLOCKS_PER_SM = 7
 TT_STAGE_REGEN = 0
@@ -160,6 +164,16 @@ class TuneResult(ctypes.Structure):
                 ("renders", ctypes.c_uint32), ("default_ms", ctypes.c_float), ("best_ms", ctypes.c_float)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
+                ("paths_per_request", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "queued", "inflight",
+                                               "bytes_in_flight", "peak_bytes_in_flight", "peak_inflight")]
+
+
 class TraversalCounters(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("rays", "blas_nodes", "tlas_nodes", "triangles", "instances", "hits",
                                                "warp_steps", "lane_steps")]
@@ -192,6 +206,12 @@ SIGNATURES = {
     "tt_timings_get": (_I32, [_P, ctypes.POINTER(Timings)]),
     "tt_stage_timings_get": (_I32, [_P, ctypes.POINTER(StageTimings)]),
     "tt_autotune": (_I32, [_P, _U64, _P, _U64, ctypes.POINTER(TuneResult)]),
+    "tt_server_create": (_I32, [_P, ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "tt_server_destroy": (_I32, [_P]),
+    "tt_server_submit": (_I32, [_P, _U64, _P, _P, _U64, ctypes.POINTER(ctypes.c_uint64)]),
+    "tt_server_status": (_I32, [_P, _U64, ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_double)]),
+    "tt_server_wait": (_I32, [_P, _U64, _U32, ctypes.POINTER(_I32)]),
+    "tt_server_stats_get": (_I32, [_P, ctypes.POINTER(ServerStats)]),
     "tt_bsdf_eval_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_bsdf_sample_batch": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_trace_batch": (_I32, [_P, _U64, _P, _U32, _U32, _P]),
