@@ -56,6 +56,9 @@ def parse_args():
     p.add_argument("--slots", type=int, default=0, help="wavefront paths in flight (0 = library default)")
     p.add_argument("--host-loop", action="store_true", help="drive the wavefront loop from the host (no CUDA graph)")
     p.add_argument("--no-autotune", action="store_true", help="skip tt_autotune before the warm-up")
+    p.add_argument("--no-serve", action="store_true", help="skip the serving sample")
+    p.add_argument("--serve-rates", default="2,8,32", help="Poisson arrival rates (requests/s) of the serving sample")
+    p.add_argument("--serve-requests", type=int, default=12, help="requests per arrival rate")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level"],
                    help="acceleration structure (auto = flat up to 2^26 instanced triangles)")
     return p.parse_args()
@@ -249,6 +252,59 @@ def run_reference(a, dist: Dist):
     print(json.dumps(out))
 
 
+# ---------------------------------------------------------------- serving sample
+SERVE_SCENES = [(1, 7), (4, 11), (16, 18), (64, 28), (128, 44)]  # (instances, frequency): 1e3 .. 5e6 triangles
+
+
+def run_serving(a, ctx) -> dict:
+    """Continuous batching under Poisson arrivals: requests with resolution side ~U{256..2048},
+    spp ~U{1..256}, depth 8, on scenes whose triangle count is drawn log-uniformly in
+    [1e3, 5e6] (nearest of five generated sizes); all scenes resident, HBM budget 150 GB."""
+    from tinytrace_gb300 import scenes
+    from tinytrace_gb300.renderer import Config, SceneArrays, make_constants
+    from tinytrace_gb300.server import RenderServer
+
+    rng = np.random.default_rng(2024)
+    pool = []
+    for inst, freq in SERVE_SCENES:
+        arr = SceneArrays(scenes.icosphere_field(instances=inst, freq=freq, lights=max(4, min(1000, 16 * inst)),
+                                                 seed=100 + inst))
+        pool.append((arr.triangle_count, ctx.create_scene(arr)))
+    cam = scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0))
+    logs = np.log10([t for t, _ in pool])
+    out = {"requests_per_rate": a.serve_requests, "scenes_triangles": [int(t) for t, _ in pool],
+           "hbm_budget_gb": 150, "max_inflight": 8, "rates": []}
+    for rate in [float(x) for x in a.serve_rates.split(",")]:
+        reqs = []
+        for k in range(a.serve_requests):
+            side = int(rng.integers(16, 129)) * 16
+            spp = int(rng.integers(1, 257))
+            scene = pool[int(np.argmin(np.abs(logs - rng.uniform(3.0, np.log10(5e6)))))][1]
+            c = make_constants(cam, (side, side), Config(bounce_count=8, sample_count=spp), k, 0)
+            reqs.append((scene, c, side * side * spp))
+        gaps = rng.exponential(1.0 / rate, len(reqs))
+        with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=8) as srv:
+            t0 = time.perf_counter()
+            ids = []
+            due = t0
+            for (scene, c, _), gap in zip(reqs, gaps):
+                due += gap
+                time.sleep(max(0.0, due - time.perf_counter()))
+                ids.append(srv.submit(scene, c))
+            for i in ids:
+                srv.wait(i)
+            makespan = time.perf_counter() - t0
+            lat = np.array([srv.status(i)[1] for i in ids])
+            st = srv.stats()
+        samples = sum(n for _, _, n in reqs)
+        out["rates"].append({"arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50)),
+                             "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                             "throughput_msamples_s": samples / makespan / 1e6,
+                             "completed_per_s": len(ids) / makespan, "peak_inflight": int(st.peak_inflight),
+                             "failed": int(st.failed)})
+    return out
+
+
 def run_ours(a, dist: Dist):
     import ctypes
 
@@ -424,6 +480,11 @@ def run_ours(a, dist: Dist):
         t = native.Timings()
         check(lib.tt_timings_get(ctx, ctypes.byref(t)))
         out_line["scene"]["build_ms"] = t.scene_build_ns / 1e6
+        if not a.no_serve and dist.world == 1:
+            try:
+                out_line["serving"] = run_serving(a, r.context)
+            except Exception as e:  # the serving sample never invalidates the headline line
+                out_line["serving"] = {"error": f"{type(e).__name__}: {e}"}
     r.close()
     if out_line is not None:
         print(json.dumps(out_line))
