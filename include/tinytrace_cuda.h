@@ -257,6 +257,26 @@ typedef struct tt_tune_result {
 } tt_tune_result;
 int32_t tt_autotune(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target,
                     tt_tune_result* out);
+/* ---------------------------------------------------------------- ReSTIR DI
+ * Direct lighting at the primary hit by spatiotemporal reservoir resampling over the emissive
+ * triangles (Bitterli et al. 2020): an addition with no reference counterpart (the reference
+ * samples one light per vertex, src/includes/scene.glsl:114-136).  One sample per pixel per
+ * frame; the context keeps the previous frame's G-buffer, reservoirs and camera for temporal
+ * reuse; the frame accumulation rule of tt_render applies to the target. */
+typedef struct tt_restir_config {
+    uint32_t candidates;         /* initial light candidates per pixel (32) */
+    float temporal_m_cap;        /* previous-frame M capped at this many times `candidates` (20) */
+    uint32_t spatial_neighbours; /* neighbours merged per pixel (5) */
+    float spatial_radius;        /* neighbour disk radius in pixels (30) */
+} tt_restir_config;
+int32_t tt_restir_configure(tt_context* ctx, const tt_restir_config* config);
+/* Forgets the previous frame (the next frame does no temporal reuse). */
+int32_t tt_restir_reset(tt_context* ctx);
+int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target);
+/* Final reservoirs of the last ReSTIR frame, width * height * 32 bytes (row-major pixels:
+ * light index u32, r1, r2, w_sum, M, W, 0, 0). */
+int32_t tt_restir_download(tt_context* ctx, void* reservoirs, uint64_t bytes);
+
 /* ---------------------------------------------------------------- serving
  * Continuous-batching render server (no reference counterpart: the reference renders one frame
  * at a time on the caller's thread).  Scenes are created on the server's context beforehand and

@@ -206,6 +206,330 @@ v3 render_pixel(const OracleScene& s, const Constants& c, uint32_t px, uint32_t 
     return acc / (float)c.sample_count;
 }
 
+// ---------------------------------------------------------------- ReSTIR DI
+// The project's spatiotemporal reservoir resampling for direct light (Bitterli et al. 2020),
+// restated pass by pass on the CPU as the checker of tinytrace_gb300/csrc/restir.cu; the
+// reference has no such pass.  Same operations and random-number order as the device code.
+struct RSurface {
+    bool hit = false;
+    v3 pos{}, normal{}, tangent{}, wi{};
+    float dist = 0.0f;
+    uint32_t material = 0, instance = 0, seed = 0;
+};
+struct RRes {
+    uint32_t light;
+    float r1, r2, w_sum, M, W, pad0, pad1;
+};
+static_assert(sizeof(RRes) == 32, "reservoir record");
+constexpr uint32_t R_NO_LIGHT = 0xffffffffu;
+
+RRes r_empty() { return RRes{R_NO_LIGHT, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}; }
+
+struct RState {  // shading state rebuilt from a G-buffer record
+    v3 pos, wi;
+    Basis basis;
+    const MaterialConstants* mc;
+    Lobes lobes;
+    uint32_t seed;
+    float dist;
+};
+bool r_load(const OracleScene& s, const RSurface& q, RState& st) {
+    if (!q.hit) return false;
+    st.pos = q.pos;
+    st.dist = q.dist;
+    st.basis.normal = q.normal;
+    st.basis.tangent = q.tangent;
+    st.basis.bitangent = normalize(cross(q.normal, q.tangent));
+    st.wi = q.wi;
+    st.seed = q.seed;
+    st.mc = &s.materials[q.material].constants;
+    Generator g{q.seed};
+    st.lobes = bsdf_prepare(*st.mc, st.wi, g);
+    return true;
+}
+
+struct RLight {
+    v3 pos, normal, emission;
+    float area;
+    uint32_t instance;
+};
+RLight r_light(const OracleScene& s, uint32_t light, float r1, float r2) {
+    const EmissiveTriangle& t = s.emissive[light];
+    const Instance& in = s.instances[t.instance_index];
+    v3 p[3];
+    for (int k = 0; k < 3; ++k) p[k] = mat43_point(in.transform, dequantize_snorm3(t.positions[k]));
+    v3 e = cross(p[1] - p[0], p[2] - p[0]);
+    RLight L;
+    L.area = fmx(0.00001f, 0.5f * length(e));
+    L.normal = normalize(e);
+    L.pos = interp3(sample_triangle(v2{r1, r2}), p[0], p[1], p[2]);
+    L.emission = material_emissive(s.materials[in.material_index]);
+    L.instance = t.instance_index;
+    return L;
+}
+
+float r_luminance(v3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+// f * Le * |cos| * cosL / d^2 (unshadowed, area measure)
+v3 r_contribution(const RState& st, const RLight& L) {
+    v3 d = L.pos - st.pos;
+    float d2 = dot(d, d);
+    v3 dir = d / std::sqrt(d2);
+    float cos_light = dot(-dir, L.normal);
+    if (!(cos_light > 0.0f) || !(d2 > 0.0f)) return splat3(0.0f);
+    v3 wo = transform_from_basis(st.basis, d);
+    float density = 0.0f;
+    v3 f = bsdf_evaluate(*st.mc, st.lobes, st.wi, wo, density);
+    return f * L.emission * (std::fabs(cos_theta(wo)) * cos_light / d2);
+}
+
+bool r_update(RRes& r, uint32_t light, float r1, float r2, float w, float m, Generator& g) {
+    r.w_sum += w;
+    r.M += m;
+    float u = random_float(g);
+    bool take = w > 0.0f && u * r.w_sum < w;
+    if (take) {
+        r.light = light;
+        r.r1 = r1;
+        r.r2 = r2;
+    }
+    return take;
+}
+
+struct RestirOracle {
+    const OracleScene* s = nullptr;
+    uint32_t W = 0, H = 0, cur = 0;
+    std::vector<RSurface> gb[2];
+    std::vector<RRes> fin[2], init, temp;
+    std::vector<uint32_t> light_prim;
+    bool hist_valid = false;
+    float hist_cam[3] = {0, 0, 0}, hist_view[16] = {}, hist_ip[16] = {};
+    uint32_t candidates = 32, neighbours = 5;
+    float m_cap_factor = 20.0f, radius = 30.0f;
+};
+
+bool r_visible(const RestirOracle& R, v3 pos, const RLight& L, uint32_t light) {
+    v3 d = L.pos - pos;
+    v3 dir = d / std::sqrt(dot(d, d));
+    Hit h = trace(*R.s, pos, dir, SHADOW_TMIN, SHADOW_TMAX, false);
+    return h.hit && h.instance == L.instance && h.prim == R.light_prim[light];
+}
+
+// The emissive triangle's primitive in its instance's mesh: the triangle with the same snorm16
+// positions, the running index first.
+std::vector<uint32_t> r_light_prims(const OracleScene& s) {
+    std::vector<uint32_t> out(s.emissive.size(), 0xffffffffu);
+    std::vector<uint32_t> next(s.instances.size(), 0);
+    for (size_t e = 0; e < s.emissive.size(); ++e) {
+        const EmissiveTriangle& t = s.emissive[e];
+        const Instance& in = s.instances[t.instance_index];
+        const Mesh& me = s.meshes[in.mesh_index];
+        uint32_t tris = me.index_count / 3u;
+        auto same = [&](uint32_t p) {
+            for (int k = 0; k < 3; ++k) {
+                const int16_t* v = &s.positions[3u * (me.vertex_offset + s.indices[me.index_offset + 3u * p + k])];
+                for (int a = 0; a < 3; ++a)
+                    if (v[a] != t.positions[k][a]) return false;
+            }
+            return true;
+        };
+        uint32_t guess = next[t.instance_index];
+        if (guess < tris && same(guess)) out[e] = guess;
+        else
+            for (uint32_t p = 0; p < tris; ++p)
+                if (same(p)) {
+                    out[e] = p;
+                    break;
+                }
+        if (out[e] != 0xffffffffu) next[t.instance_index] = out[e] + 1u;
+    }
+    return out;
+}
+
+RSurface r_gbuffer(const RestirOracle& R, const Constants& c, uint32_t x, uint32_t y) {
+    const OracleScene& s = *R.s;
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    Generator g = init_generator_from_pixel(x, y, W, c.frame_index);
+    float ox = random_float(g);
+    float oy = random_float(g);
+    v2 ndc = v2{(((float)x + (ox - 0.5f)) / (float)W) * 2.0f - 1.0f, (((float)y + (oy - 0.5f)) / (float)H) * 2.0f - 1.0f};
+    v3 dir = camera_ray_direction(c, ndc);
+    v3 org = xyz(c.camera_position);
+    Hit h = trace(s, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true);
+    RSurface q;
+    q.seed = g.state;
+    if (!h.hit) return q;
+    RayHit hit = get_ray_hit(s, h);
+    const MaterialConstants& mc = s.materials[hit.material_index].constants;
+    Basis basis = create_surface_basis(hit.tangent_space, xyz(mc.geometry_normal));
+    q.hit = true;
+    q.pos = hit.world_position;
+    q.dist = length(hit.world_position - org);
+    q.normal = basis.normal;
+    q.tangent = basis.tangent;
+    q.wi = transform_from_basis(basis, -dir);
+    q.material = hit.material_index;
+    q.instance = h.instance;
+    return q;
+}
+
+RRes r_initial(const RestirOracle& R, const RSurface& q) {
+    const OracleScene& s = *R.s;
+    RState st;
+    RRes r = r_empty();
+    if (!r_load(s, q, st) || s.emissive.empty()) return r;
+    Generator g{jenkins_hash(st.seed + 1u)};
+    float lights = (float)s.emissive.size();
+    float chosen = 0.0f;
+    for (uint32_t k = 0; k < R.candidates; ++k) {
+        uint32_t light = random_uint(g, (uint32_t)s.emissive.size());
+        float r1 = random_float(g);
+        float r2 = random_float(g);
+        RLight L = r_light(s, light, r1, r2);
+        float ph = r_luminance(r_contribution(st, L));
+        float w = ph * (lights * L.area);
+        if (r_update(r, light, r1, r2, w, 1.0f, g)) chosen = ph;
+    }
+    r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
+    if (r.W > 0.0f && !r_visible(R, st.pos, r_light(s, r.light, r.r1, r.r2), r.light)) r.W = 0.0f;
+    return r;
+}
+
+float r_target(const RestirOracle& R, const RState& st, uint32_t light, float r1, float r2) {
+    if (light == R_NO_LIGHT) return 0.0f;
+    return r_luminance(r_contribution(st, r_light(*R.s, light, r1, r2)));
+}
+
+void r_merge(const RestirOracle& R, const RState& st, RRes& r, const RRes& q, float cap, float& chosen, Generator& g) {
+    float m = fmn(q.M, cap);
+    float ph = r_target(R, st, q.light, q.r1, q.r2);
+    float w = ph * q.W * m;
+    if (r_update(r, q.light, q.r1, q.r2, w, m, g)) chosen = ph;
+}
+
+bool r_similar(const RSurface& q, v3 normal, float dist) {
+    if (!q.hit) return false;
+    return dot(q.normal, normal) > 0.90630779f && std::fabs(q.dist - dist) <= 0.1f * dist;
+}
+
+bool r_reproject(const RestirOracle& R, v3 pos, uint32_t& px, uint32_t& py) {
+    v3 d = pos - v3{R.hist_cam[0], R.hist_cam[1], R.hist_cam[2]};
+    const float* v = R.hist_view;
+    v3 u = v3{v[0] * d.x + v[4] * d.y + v[8] * d.z, v[1] * d.x + v[5] * d.y + v[9] * d.z,
+              v[2] * d.x + v[6] * d.y + v[10] * d.z};
+    const float* ip = R.hist_ip;
+    v3 a = v3{ip[0], ip[1], ip[2]}, b = v3{ip[4], ip[5], ip[6]};
+    v3 cc = v3{ip[8] + ip[12], ip[9] + ip[13], ip[10] + ip[14]};
+    v3 c0 = -a, c1 = -b, c2 = -u, rhs = -cc;
+    float det = dot(c0, cross(c1, c2));
+    if (!(std::fabs(det) > 0.0f)) return false;
+    float nx = dot(rhs, cross(c1, c2)) / det;
+    float ny = dot(c0, cross(rhs, c2)) / det;
+    float sc = dot(c0, cross(c1, rhs)) / det;
+    if (!(sc > 0.0f)) return false;
+    float fx = (nx + 1.0f) * 0.5f * (float)R.W, fy = (ny + 1.0f) * 0.5f * (float)R.H;
+    if (!(fx >= 0.0f && fx < (float)R.W && fy >= 0.0f && fy < (float)R.H)) return false;
+    px = (uint32_t)fx;
+    py = (uint32_t)fy;
+    return true;
+}
+
+// One ReSTIR frame into `target` (W*H RGBA32F, read for accumulation).
+void restir_frame(RestirOracle& R, const Constants& c, float* target) {
+    const OracleScene& s = *R.s;
+    uint32_t W = R.W, H = R.H;
+    uint64_t n = (uint64_t)W * H;
+    std::vector<RSurface>& gb = R.gb[R.cur];
+    const std::vector<RSurface>& pgb = R.gb[R.cur ^ 1u];
+    std::vector<RRes>& out = R.fin[R.cur];
+    const std::vector<RRes>& prev = R.fin[R.cur ^ 1u];
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)n; ++i) gb[i] = r_gbuffer(R, c, (uint32_t)(i % W), (uint32_t)(i / W));
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)n; ++i) R.init[i] = r_initial(R, gb[i]);
+    float cap = R.m_cap_factor * (float)R.candidates;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {  // temporal
+        RRes cur = R.init[i];
+        RState st;
+        uint32_t px, py;
+        if (!R.hist_valid || !r_load(s, gb[i], st) || !r_reproject(R, st.pos, px, py)) {
+            R.temp[i] = cur;
+            continue;
+        }
+        uint64_t j = (uint64_t)py * W + px;
+        v3 from_prev = st.pos - v3{R.hist_cam[0], R.hist_cam[1], R.hist_cam[2]};
+        if (!r_similar(pgb[j], st.basis.normal, length(from_prev))) {
+            R.temp[i] = cur;
+            continue;
+        }
+        Generator g{jenkins_hash(st.seed + 2u)};
+        RRes r = r_empty();
+        float chosen = 0.0f;
+        r_merge(R, st, r, cur, cur.M, chosen, g);
+        r_merge(R, st, r, prev[j], cap, chosen, g);
+        r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
+        R.temp[i] = r;
+    }
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {  // spatial
+        uint32_t x = (uint32_t)(i % W), y = (uint32_t)(i / W);
+        RState st;
+        RRes cur = R.temp[i];
+        if (!r_load(s, gb[i], st)) {
+            out[i] = cur;
+            continue;
+        }
+        Generator g{jenkins_hash(st.seed + 3u)};
+        RRes r = r_empty();
+        float chosen = 0.0f;
+        r_merge(R, st, r, cur, cur.M, chosen, g);
+        for (uint32_t k = 0; k < R.neighbours; ++k) {
+            float rr = R.radius * std::sqrt(random_float(g));
+            float angle = TAU * random_float(g);
+            float sn, cs;
+            tsincos(angle, &sn, &cs);
+            float qx = (float)x + rr * cs, qy = (float)y + rr * sn;
+            if (!(qx >= 0.0f && qx < (float)W && qy >= 0.0f && qy < (float)H)) continue;
+            uint64_t j = (uint64_t)(uint32_t)qy * W + (uint32_t)qx;
+            if (j == (uint64_t)i || !r_similar(gb[j], st.basis.normal, st.dist)) continue;
+            r_merge(R, st, r, R.temp[j], R.temp[j].M, chosen, g);
+        }
+        r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
+        out[i] = r;
+    }
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {  // shade
+        RState st;
+        v3 radiance;
+        if (!r_load(s, gb[i], st)) {
+            radiance = splat3(1.0f);
+        } else {
+            radiance = material_emissive(s.materials[gb[i].material]);
+            const RRes& r = out[i];
+            if (r.light != R_NO_LIGHT && r.W > 0.0f) {
+                RLight L = r_light(s, r.light, r.r1, r.r2);
+                v3 contrib = r_contribution(st, L);
+                if (r_visible(R, st.pos, L, r.light)) radiance += contrib * r.W;
+            }
+        }
+        float* t = target + 4ull * i;
+        if (c.accumulated_frame_count != 0) {
+            v3 prevc = v3{t[0], t[1], t[2]};
+            radiance = (prevc * (float)(c.accumulated_frame_count - 1u) + radiance) / (float)c.accumulated_frame_count;
+        }
+        t[0] = radiance.x;
+        t[1] = radiance.y;
+        t[2] = radiance.z;
+        t[3] = 1.0f;
+    }
+    std::memcpy(R.hist_cam, &c.camera_position, sizeof(R.hist_cam));
+    std::memcpy(R.hist_view, c.view, sizeof(R.hist_view));
+    std::memcpy(R.hist_ip, c.inverse_proj, sizeof(R.hist_ip));
+    R.hist_valid = true;
+    R.cur ^= 1u;
+}
+
 // tonemap.glsl:1-26
 v3 neutral_tonemap(v3 col) {
     v3 y = v3{0.2126f * col.x + 0.7152f * col.y + 0.0722f * col.z,
@@ -400,6 +724,41 @@ void oracle_bsdf_sample_batch(const MaterialConstants* m, const float* samples, 
         r[4] = wo.x; r[5] = wo.y; r[6] = wo.z; r[7] = (float)lobe;
         r[8] = bitsf(g.state); r[9] = 0.0f; r[10] = 0.0f; r[11] = 0.0f;
     }
+}
+
+// ReSTIR DI state of the oracle: config = {candidates, m_cap_factor, neighbours, radius}.
+void* oracle_restir_create(void* scene, uint32_t width, uint32_t height, uint32_t candidates, float m_cap_factor,
+                           uint32_t neighbours, float radius) {
+    RestirOracle* R = new RestirOracle();
+    R->s = static_cast<OracleScene*>(scene);
+    R->W = width;
+    R->H = height;
+    uint64_t n = (uint64_t)width * height;
+    for (int k = 0; k < 2; ++k) {
+        R->gb[k].assign(n, RSurface{});
+        R->fin[k].assign(n, r_empty());
+    }
+    R->init.assign(n, r_empty());
+    R->temp.assign(n, r_empty());
+    R->light_prim = r_light_prims(*R->s);
+    R->candidates = candidates;
+    R->m_cap_factor = m_cap_factor;
+    R->neighbours = neighbours;
+    R->radius = radius;
+    return R;
+}
+void oracle_restir_destroy(void* p) { delete static_cast<RestirOracle*>(p); }
+void oracle_restir_frame(void* p, const Constants* c, float* target, int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#endif
+    restir_frame(*static_cast<RestirOracle*>(p), *c, target);
+}
+// Final reservoirs of the last frame (W*H records of 32 bytes).
+void oracle_restir_reservoirs(void* p, void* out) {
+    RestirOracle* R = static_cast<RestirOracle*>(p);
+    const std::vector<RRes>& f = R->fin[R->cur ^ 1u];
+    std::memcpy(out, f.data(), f.size() * sizeof(RRes));
 }
 
 // Elementary functions, for accuracy tests against libm.

@@ -42,6 +42,12 @@ def load() -> ctypes.CDLL:
         lib.oracle_bsdf_eval_batch.argtypes = [_P, _P, ctypes.c_uint32, _P]
         lib.oracle_bsdf_sample_batch.argtypes = [_P, _P, ctypes.c_uint32, _P]
         lib.oracle_math.argtypes = [ctypes.c_int, _P, ctypes.c_uint64, _P]
+        lib.oracle_restir_create.restype = _P
+        lib.oracle_restir_create.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                             ctypes.c_uint32, ctypes.c_float]
+        lib.oracle_restir_destroy.argtypes = [_P]
+        lib.oracle_restir_frame.argtypes = [_P, _P, _P, ctypes.c_int]
+        lib.oracle_restir_reservoirs.argtypes = [_P, _P]
         _lib = lib
     return _lib
 
@@ -108,6 +114,35 @@ class OracleScene:
         c = np.ascontiguousarray(constants)
         self.lib.oracle_render(self.handle, _p(c), _p(target), y0, y1, x0, x1, threads)
         return target
+
+
+class OracleRestir:
+    """ReSTIR DI frames on the CPU (the checker of tt_render_restir), keeping the previous
+    frame's G-buffer, reservoirs and camera like the device context does."""
+
+    def __init__(self, scene: "OracleScene", width: int, height: int, candidates: int = 32,
+                 m_cap_factor: float = 20.0, neighbours: int = 5, radius: float = 30.0):
+        self.scene = scene  # keeps the scene alive
+        self.lib = scene.lib
+        self.width, self.height = width, height
+        self.handle = self.lib.oracle_restir_create(scene.handle, width, height, candidates, m_cap_factor,
+                                                    neighbours, radius)
+
+    def __del__(self):
+        try:
+            self.lib.oracle_restir_destroy(self.handle)
+        except Exception:
+            pass
+
+    def frame(self, constants: np.ndarray, target: np.ndarray, threads: int = 0) -> np.ndarray:
+        c = np.ascontiguousarray(constants)
+        self.lib.oracle_restir_frame(self.handle, _p(c), _p(target), threads)
+        return target
+
+    def reservoirs(self) -> np.ndarray:
+        out = np.zeros((self.height, self.width, 8), np.float32)
+        self.lib.oracle_restir_reservoirs(self.handle, _p(out))
+        return out
 
 
 def tonemap(image: np.ndarray, enabled: bool = True) -> np.ndarray:

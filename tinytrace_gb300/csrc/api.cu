@@ -72,7 +72,7 @@ struct ImageRes {
 };
 
 struct SceneRes {
-    DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform, inst_bucket;
+    DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform, inst_bucket, light_prim;
     BvhResult bvh;
     DevScene dev{};
     tt_scene_stats stats{};
@@ -84,6 +84,16 @@ struct WavefrontBuffers {
     uint32_t slots = 0;
     uint64_t sample_items = 0;
     uint32_t pixels = 0;
+};
+
+// ReSTIR DI state kept between frames: two G-buffers and two final reservoir arrays
+// (current and previous frame), the initial and temporal reservoirs, the previous camera.
+struct RestirState {
+    DeviceBuffer gbuf[2], final_res[2], initial, temporal;
+    uint64_t pixels = 0;
+    uint32_t cur = 0;
+    RestirHistory history{};
+    tt_restir_config config{32u, 20.0f, 5u, 30.0f};
 };
 
 struct Pool {
@@ -120,6 +130,7 @@ struct tt_context {
     cudaStream_t capture[2] = {nullptr, nullptr};  // capture streams of the graph-driven loop
     std::vector<cudaEvent_t> stage_events;  // 2 * StageTimer::MAX_LAUNCHES, created on first use
     tt::StageTimer stage_timer;
+    tt::RestirState restir;
 };
 
 namespace tt {
@@ -214,6 +225,39 @@ std::vector<uint8_t> instance_buckets(const tt_scene_desc* d) {
     for (size_t k = 0; k < order.size(); ++k) bucket[order[k].second] = (uint8_t)std::min<size_t>(k, HIT_BUCKETS - 1);
     std::vector<uint8_t> out(std::max<uint32_t>(d->instance_count, 1), 0);
     for (uint32_t i = 0; i < d->instance_count; ++i) out[i] = bucket[sig[i]];
+    return out;
+}
+
+// Primitive index of each emissive triangle inside its instance's mesh (the triangle whose
+// snorm16 positions it copies; Scene::new lists a model's triangles in order,
+// src/asset/mod.rs:163-193, so the running index is tried first).  0xffffffff: no match.
+std::vector<uint32_t> light_primitives(const tt_scene_desc* d) {
+    std::vector<uint32_t> out(std::max<uint64_t>(d->emissive_triangle_count, 1), 0xffffffffu);
+    std::vector<uint32_t> next(d->instance_count, 0);
+    for (uint32_t e = 0; e < d->emissive_triangle_count; ++e) {
+        const tt_emissive_triangle& t = d->emissive_triangles[e];
+        const tt_instance& in = d->instances[t.instance_index];
+        const tt_mesh& me = d->meshes[in.mesh_index];
+        uint32_t tris = me.index_count / 3u;
+        auto same = [&](uint32_t p) {
+            for (int k = 0; k < 3; ++k) {
+                const int16_t* v = d->positions + 3ull * (me.vertex_offset + d->indices[me.index_offset + 3u * p + k]);
+                if (v[0] != t.positions[k][0] || v[1] != t.positions[k][1] || v[2] != t.positions[k][2]) return false;
+            }
+            return true;
+        };
+        uint32_t guess = next[t.instance_index];
+        if (guess < tris && same(guess)) {
+            out[e] = guess;
+        } else {
+            for (uint32_t p = 0; p < tris; ++p)
+                if (same(p)) {
+                    out[e] = p;
+                    break;
+                }
+        }
+        if (out[e] != 0xffffffffu) next[t.instance_index] = out[e] + 1u;
+    }
     return out;
 }
 
@@ -585,6 +629,8 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         upload(s->meshes, d->meshes, d->mesh_count, st);
         upload(s->instances, d->instances, d->instance_count, st);
         upload(s->emissive, d->emissive_triangles, d->emissive_triangle_count, st);
+        std::vector<uint32_t> lprim = light_primitives(d);
+        upload(s->light_prim, lprim.data(), lprim.size(), st);
         std::vector<float4> xf(4ull * d->instance_count);
         for (uint32_t i = 0; i < d->instance_count; ++i) {
             const float* m = d->instances[i].inverse_transform;
@@ -625,6 +671,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.materials = s->materials.as<tt_material>();
         ds.instances = s->instances.as<tt_instance>();
         ds.meshes = s->meshes.as<tt_mesh>();
+        ds.light_prim = s->light_prim.as<uint32_t>();
         ds.emissive = s->emissive.as<tt_emissive_triangle>();
         ds.inst_xform = s->inst_xform.as<float4>();
         ds.inst_bucket = s->inst_bucket.as<uint8_t>();
@@ -822,6 +869,87 @@ int32_t tt_autotune(tt_context* ctx, tt_handle scene, const tt_constants* consta
         out->refill_lanes = ctx->refill_lanes;
         out->trace_blocks_per_sm = ctx->trace_blocks_per_sm;
         out->best_ms = best;
+    });
+}
+
+int32_t tt_restir_configure(tt_context* ctx, const tt_restir_config* config) {
+    return guarded([&] {
+        require(ctx && config, "null argument");
+        require(config->candidates >= 1 && config->candidates <= 1024, "candidates must be in 1..1024");
+        require(config->temporal_m_cap >= 0.0f && std::isfinite(config->temporal_m_cap), "bad temporal M cap");
+        require(config->spatial_neighbours <= 64, "at most 64 spatial neighbours");
+        require(config->spatial_radius >= 0.0f && config->spatial_radius <= 4096.0f, "bad spatial radius");
+        ctx->restir.config = *config;
+    });
+}
+
+int32_t tt_restir_reset(tt_context* ctx) {
+    return guarded([&] {
+        require(ctx, "null context");
+        ctx->restir.history.valid = 0u;
+    });
+}
+
+int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target) {
+    return guarded([&] {
+        require(ctx && constants, "null argument");
+        use_device(ctx);
+        SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
+        ImageRes* img = lookup<ImageRes>(ctx, target, KIND_IMAGE);
+        require(constants->screen_size[0] == img->width && constants->screen_size[1] == img->height,
+                "constants.screen_size must equal the target extent");
+        RestirState& R = ctx->restir;
+        uint64_t WH = (uint64_t)img->width * img->height;
+        if (WH != R.pixels) {
+            for (auto& b : R.gbuf) b.alloc(64ull * WH);
+            for (auto& b : R.final_res) b.alloc(32ull * WH);
+            R.initial.alloc(32ull * WH);
+            R.temporal.alloc(32ull * WH);
+            R.pixels = WH;
+            R.history.valid = 0u;
+        }
+        RenderParams p;
+        p.sc = s->dev;
+        p.c = *constants;
+        p.target = img->buf.as<float4>();
+        p.err = ctx->err_word.as<uint32_t>();
+        p.counters = ctx->counters.as<unsigned long long>();
+        RestirParams rp;
+        rp.gbuf = R.gbuf[R.cur].as<Surface>();
+        rp.prev_gbuf = R.gbuf[R.cur ^ 1u].as<Surface>();
+        rp.initial = R.initial.as<Reservoir>();
+        rp.temporal = R.temporal.as<Reservoir>();
+        rp.final_out = R.final_res[R.cur].as<Reservoir>();
+        rp.prev = R.final_res[R.cur ^ 1u].as<Reservoir>();
+        rp.history = R.history;
+        rp.candidates = R.config.candidates;
+        rp.neighbours = R.config.spatial_neighbours;
+        rp.m_cap = R.config.temporal_m_cap * (float)R.config.candidates;
+        rp.radius = R.config.spatial_radius;
+        arm_error_word(ctx);
+        check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
+        render_restir(p, rp, ctx->stream);
+        check_cuda(cudaGetLastError(), "restir launch");
+        check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
+        ctx->integrate_timed = true;
+        fetch_error_word(ctx);
+        std::memcpy(R.history.camera_position, constants->camera_position, sizeof(R.history.camera_position));
+        std::memcpy(R.history.view, constants->view, sizeof(R.history.view));
+        std::memcpy(R.history.inverse_proj, constants->inverse_proj, sizeof(R.history.inverse_proj));
+        R.history.valid = 1u;
+        R.cur ^= 1u;
+    });
+}
+
+int32_t tt_restir_download(tt_context* ctx, void* reservoirs, uint64_t bytes) {
+    return guarded([&] {
+        require(ctx && reservoirs, "null argument");
+        use_device(ctx);
+        RestirState& R = ctx->restir;
+        require(R.pixels > 0 && bytes == 32ull * R.pixels, "byte count must equal width * height * 32");
+        check_cuda(cudaMemcpyAsync(reservoirs, R.final_res[R.cur ^ 1u].ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream),
+                   "download");
+        sync(ctx);
     });
 }
 

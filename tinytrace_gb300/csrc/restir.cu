@@ -1,0 +1,279 @@
+// ReSTIR DI kernels (the passes described in tt_restir.cuh), one thread per pixel in 16 x 8
+// tiles; each pass reads and writes whole-frame arrays in HBM:
+//   G-buffer 64 B / pixel (current and previous frame), reservoirs 32 B / pixel
+//   (initial, temporal, final; the final array of frame n is the history of frame n + 1).
+#include <cuda_runtime.h>
+
+#include "tt_internal.h"
+#include "tt_kernels.h"
+#include "tt_restir.cuh"
+
+namespace tt {
+
+constexpr int RT_TILE_X = 16, RT_TILE_Y = 8, RT_BLOCK = RT_TILE_X * RT_TILE_Y;
+constexpr uint32_t PASS_INITIAL = 1u, PASS_TEMPORAL = 2u, PASS_SPATIAL = 3u;
+
+__device__ __forceinline__ bool pixel_of_thread(const tt_constants& c, uint32_t& x, uint32_t& y) {
+    x = blockIdx.x * RT_TILE_X + threadIdx.x % RT_TILE_X;
+    y = blockIdx.y * RT_TILE_Y + threadIdx.x / RT_TILE_X;
+    return x < c.screen_size[0] && y < c.screen_size[1];
+}
+
+// Rebuilds the pixel's shading state from its G-buffer record.
+struct ShadingState {
+    f3 pos, wi;
+    Basis basis;
+    const tt_material* material;
+    Lobes lobes;
+    uint32_t seed;
+    float dist;
+};
+__device__ __forceinline__ bool load_surface(const DevScene& sc, const Surface& s, ShadingState& st) {
+    uint32_t mat = __float_as_uint(s.normal_mat.w);
+    if (mat == NO_SURFACE) return false;
+    st.pos = f3{s.pos_dist.x, s.pos_dist.y, s.pos_dist.z};
+    st.dist = s.pos_dist.w;
+    st.basis.normal = f3{s.normal_mat.x, s.normal_mat.y, s.normal_mat.z};
+    st.basis.tangent = f3{s.tangent_inst.x, s.tangent_inst.y, s.tangent_inst.z};
+    st.basis.bitangent = normalize(cross(st.basis.normal, st.basis.tangent));
+    st.wi = f3{s.wi_seed.x, s.wi_seed.y, s.wi_seed.z};
+    st.seed = __float_as_uint(s.wi_seed.w);
+    st.material = sc.materials + mat;
+    uint32_t g = st.seed;
+    st.lobes = bsdf_prepare(st.material->constants, st.wi, g);
+    return true;
+}
+
+__device__ __forceinline__ float target_of(const DevScene& sc, const ShadingState& st, uint32_t light, float r1,
+                                           float r2) {
+    if (light == NO_LIGHT) return 0.0f;
+    LightPoint lp = light_point(sc, light, r1, r2);
+    return luminance(restir_contribution(st.material->constants, st.lobes, st.basis, st.wi, st.pos, lp));
+}
+
+__global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
+                                                                  Surface* gbuf) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
+    const tt_constants& c = p.c;
+    if (!pixel_of_thread(c, x, y)) return;
+    const DevScene& sc = p.sc;
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    uint32_t g = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
+    f2 ndc = pixel_ndc(x, y, W, H, g);
+    f3 dir = camera_ray_direction(c, ndc);
+    f3 org = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
+    Counters cnt{0u, 0u, 0u, 0u};
+    Hit h = trace_closest<false>(sc, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true, s_stack + threadIdx.x, RT_BLOCK,
+                                 p.err, cnt);
+    Surface s;
+    if (!h.hit) {
+        s.pos_dist = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        s.normal_mat = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(NO_SURFACE));
+        s.tangent_inst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        s.wi_seed = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(g));
+    } else {
+        ShadeHit hit = get_ray_hit(sc, h.instance, h.prim, h.u, h.v);
+        const MatC& mc = sc.materials[hit.material_index].constants;
+        Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
+        f3 wi = transform_from_basis(basis, -dir);
+        f3 to = hit.world_position - org;
+        s.pos_dist = make_float4(hit.world_position.x, hit.world_position.y, hit.world_position.z, length(to));
+        s.normal_mat = make_float4(basis.normal.x, basis.normal.y, basis.normal.z, __uint_as_float(hit.material_index));
+        s.tangent_inst = make_float4(basis.tangent.x, basis.tangent.y, basis.tangent.z, __uint_as_float(h.instance));
+        s.wi_seed = make_float4(wi.x, wi.y, wi.z, __uint_as_float(g));
+    }
+    gbuf[(uint64_t)y * W + x] = s;
+}
+
+__global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_constant__ RenderParams p,
+                                                                  const Surface* gbuf, Reservoir* out,
+                                                                  uint32_t candidates) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
+    const tt_constants& c = p.c;
+    if (!pixel_of_thread(c, x, y)) return;
+    const DevScene& sc = p.sc;
+    uint64_t i = (uint64_t)y * c.screen_size[0] + x;
+    ShadingState st;
+    Reservoir r = empty_reservoir();
+    if (load_surface(sc, gbuf[i], st) && sc.emissive_count > 0) {
+        uint32_t g = jenkins_hash(st.seed + PASS_INITIAL);
+        float inv_p_pick = (float)sc.emissive_count;
+        float chosen = 0.0f;
+        for (uint32_t k = 0; k < candidates; ++k) {
+            uint32_t light = xor_shift(g) % sc.emissive_count;
+            float r1 = random_float(g);
+            float r2 = random_float(g);
+            LightPoint lp = light_point(sc, light, r1, r2);
+            float ph = luminance(restir_contribution(st.material->constants, st.lobes, st.basis, st.wi, st.pos, lp));
+            float w = ph * (inv_p_pick * lp.area);  // p^ / p, p = 1 / (lights * area)
+            if (reservoir_update(r, light, r1, r2, w, 1.0f, g)) chosen = ph;
+        }
+        r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
+        if (r.W > 0.0f) {
+            LightPoint lp = light_point(sc, r.light, r.r1, r.r2);
+            if (!restir_visible<false>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err)) r.W = 0.0f;
+        }
+    }
+    out[i] = r;
+}
+
+// Merges reservoir q (from another pixel or frame) into r, re-targeted at this pixel.
+__device__ __forceinline__ void merge(const DevScene& sc, const ShadingState& st, Reservoir& r, const Reservoir& q,
+                                      float m_cap, float& chosen, uint32_t& g) {
+    float m = fmn(q.M, m_cap);
+    float ph = target_of(sc, st, q.light, q.r1, q.r2);
+    float w = ph * q.W * m;
+    if (reservoir_update(r, q.light, q.r1, q.r2, w, m, g)) chosen = ph;
+}
+
+// Pixel of the previous frame that saw world position pos, or false (behind the camera or
+// outside the image).  Solves  s * u = -nx * a - ny * b + c  for (nx, ny, s), where u is the
+// position in the previous camera's view space and a, b, c are the inverse projection's
+// columns that map NDC to view-space ray directions (the camera ray of integrate.glsl:17-20).
+__device__ __forceinline__ bool reproject(const RestirHistory& hist, f3 pos, uint32_t W, uint32_t H, uint32_t& px,
+                                          uint32_t& py) {
+    f3 d = pos - f3{hist.camera_position[0], hist.camera_position[1], hist.camera_position[2]};
+    const float* v = hist.view;  // column-major
+    f3 u = f3{v[0] * d.x + v[4] * d.y + v[8] * d.z, v[1] * d.x + v[5] * d.y + v[9] * d.z,
+              v[2] * d.x + v[6] * d.y + v[10] * d.z};
+    const float* ip = hist.inverse_proj;
+    f3 a = f3{ip[0], ip[1], ip[2]}, b = f3{ip[4], ip[5], ip[6]};
+    f3 cc = f3{ip[8] + ip[12], ip[9] + ip[13], ip[10] + ip[14]};
+    // columns of the system matrix: -a, -b, -u; right-hand side: -c
+    f3 c0 = -a, c1 = -b, c2 = -u, rhs = -cc;
+    float det = dot(c0, cross(c1, c2));
+    if (!(fabsf(det) > 0.0f)) return false;
+    float nx = dot(rhs, cross(c1, c2)) / det;
+    float ny = dot(c0, cross(rhs, c2)) / det;
+    float s = dot(c0, cross(c1, rhs)) / det;
+    if (!(s > 0.0f)) return false;
+    float fx = (nx + 1.0f) * 0.5f * (float)W, fy = (ny + 1.0f) * 0.5f * (float)H;
+    if (!(fx >= 0.0f && fx < (float)W && fy >= 0.0f && fy < (float)H)) return false;
+    px = (uint32_t)fx;
+    py = (uint32_t)fy;
+    return true;
+}
+
+// Surfaces similar enough to share samples: normals within 25 degrees, camera distances
+// within 10 %.
+__device__ __forceinline__ bool similar(const Surface& q, f3 normal, float dist) {
+    if (__float_as_uint(q.normal_mat.w) == NO_SURFACE) return false;
+    f3 n = f3{q.normal_mat.x, q.normal_mat.y, q.normal_mat.z};
+    return dot(n, normal) > 0.90630779f && fabsf(q.pos_dist.w - dist) <= 0.1f * dist;
+}
+
+__global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_constant__ RenderParams p,
+                                                                   const __grid_constant__ RestirHistory hist,
+                                                                   const Surface* gbuf, const Surface* prev_gbuf,
+                                                                   const Reservoir* initial, const Reservoir* prev,
+                                                                   Reservoir* out, float m_cap) {
+    uint32_t x, y;
+    const tt_constants& c = p.c;
+    if (!pixel_of_thread(c, x, y)) return;
+    const DevScene& sc = p.sc;
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    uint64_t i = (uint64_t)y * W + x;
+    Reservoir cur = initial[i];
+    ShadingState st;
+    uint32_t px, py;
+    if (!hist.valid || !load_surface(sc, gbuf[i], st) || !reproject(hist, st.pos, W, H, px, py)) {
+        out[i] = cur;
+        return;
+    }
+    uint64_t j = (uint64_t)py * W + px;
+    f3 from_prev = st.pos - f3{hist.camera_position[0], hist.camera_position[1], hist.camera_position[2]};
+    if (!similar(prev_gbuf[j], st.basis.normal, length(from_prev))) {
+        out[i] = cur;
+        return;
+    }
+    uint32_t g = jenkins_hash(st.seed + PASS_TEMPORAL);
+    Reservoir r = empty_reservoir();
+    float chosen = 0.0f;
+    merge(sc, st, r, cur, cur.M, chosen, g);
+    merge(sc, st, r, prev[j], m_cap, chosen, g);
+    r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
+    out[i] = r;
+}
+
+__global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_constant__ RenderParams p,
+                                                                  const Surface* gbuf, const Reservoir* in,
+                                                                  Reservoir* out, uint32_t neighbours, float radius) {
+    uint32_t x, y;
+    const tt_constants& c = p.c;
+    if (!pixel_of_thread(c, x, y)) return;
+    const DevScene& sc = p.sc;
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    uint64_t i = (uint64_t)y * W + x;
+    ShadingState st;
+    Reservoir cur = in[i];
+    if (!load_surface(sc, gbuf[i], st)) {
+        out[i] = cur;
+        return;
+    }
+    uint32_t g = jenkins_hash(st.seed + PASS_SPATIAL);
+    Reservoir r = empty_reservoir();
+    float chosen = 0.0f;
+    merge(sc, st, r, cur, cur.M, chosen, g);
+    for (uint32_t k = 0; k < neighbours; ++k) {
+        float rr = radius * sqrtf(random_float(g));
+        float angle = TAU * random_float(g);
+        float sn, cs;
+        tsincos(angle, &sn, &cs);
+        float qx = (float)x + rr * cs, qy = (float)y + rr * sn;
+        if (!(qx >= 0.0f && qx < (float)W && qy >= 0.0f && qy < (float)H)) continue;
+        uint64_t j = (uint64_t)(uint32_t)qy * W + (uint32_t)qx;
+        if (j == i || !similar(gbuf[j], st.basis.normal, st.dist)) continue;
+        const Reservoir q = in[j];
+        merge(sc, st, r, q, q.M, chosen, g);
+    }
+    r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
+    out[i] = r;
+}
+
+__global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_constant__ RenderParams p,
+                                                                const Surface* gbuf, const Reservoir* res) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
+    const tt_constants& c = p.c;
+    if (!pixel_of_thread(c, x, y)) return;
+    const DevScene& sc = p.sc;
+    uint32_t W = c.screen_size[0];
+    uint64_t i = (uint64_t)y * W + x;
+    ShadingState st;
+    f3 radiance;
+    if (!load_surface(sc, gbuf[i], st)) {
+        radiance = splat(1.0f);  // the white sky of integrate.glsl:272-276
+    } else {
+        radiance = material_emissive(st.material);
+        Reservoir r = res[i];
+        if (r.light != NO_LIGHT && r.W > 0.0f) {
+            LightPoint lp = light_point(sc, r.light, r.r1, r.r2);
+            f3 contrib = restir_contribution(st.material->constants, st.lobes, st.basis, st.wi, st.pos, lp);
+            if (restir_visible<false>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err))
+                radiance += contrib * r.W;
+        }
+    }
+    float4* tp = p.target + i;
+    if (c.accumulated_frame_count != 0) {
+        float4 prev = *tp;
+        radiance = (f3{prev.x, prev.y, prev.z} * (float)(c.accumulated_frame_count - 1u) + radiance) /
+                   (float)c.accumulated_frame_count;
+    }
+    *tp = make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
+}
+
+void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {
+    const tt_constants& c = p.c;
+    dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
+    restir_gbuffer_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf);
+    restir_initial_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.initial, rp.candidates);
+    restir_temporal_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.prev_gbuf, rp.initial, rp.prev,
+                                                      rp.temporal, rp.m_cap);
+    restir_spatial_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.temporal, rp.final_out, rp.neighbours,
+                                                     rp.radius);
+    restir_shade_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.final_out);
+}
+
+}  // namespace tt

@@ -51,6 +51,7 @@ struct DevScene {
     const tt_instance* instances;
     const tt_mesh* meshes;
     const tt_emissive_triangle* emissive;
+    const uint32_t* light_prim;  // primitive index of each emissive triangle in its instance's mesh
     const uint4* blas;        // 8 x uint4 per node (two-level only)
     const float4* tris;       // 3 x float4 per triangle record
     const uint4* tlas;        // 8 x uint4 per node: the TLAS, or the flat BVH

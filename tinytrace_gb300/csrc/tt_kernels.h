@@ -75,6 +75,24 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
 void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cudaStream_t st, cudaStream_t cs,
                             cudaStream_t body_stream);
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st);
+
+// ReSTIR DI (restir.cu): the previous frame's camera and the frame's buffers.
+struct RestirHistory {
+    float camera_position[3];
+    float view[16];          // column-major, as in tt_constants
+    float inverse_proj[16];  // column-major
+    uint32_t valid;          // 0: no previous frame (no temporal reuse)
+};
+struct Surface;
+struct Reservoir;
+struct RestirParams {
+    Surface *gbuf, *prev_gbuf;
+    Reservoir *initial, *temporal, *final_out, *prev;
+    RestirHistory history;
+    uint32_t candidates, neighbours;
+    float m_cap, radius;
+};
+void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st);
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out,
                     cudaStream_t st);
 void launch_bsdf_eval(const tt_material_constants* m, const float4* samples, uint32_t n,

@@ -1,0 +1,133 @@
+// ReSTIR DI (spatiotemporal reservoir resampling for direct lighting; Bitterli, Wyman, Pharr,
+// Shirley, Lefohn & Jarosz, SIGGRAPH 2020) on the emissive triangles of the scene.  This is an
+// addition: the reference samples one light per vertex (src/includes/scene.glsl:114-136).
+//
+// Per pixel and frame (1 sample per pixel, direct light at the primary hit):
+//   G-buffer   camera ray (the path tracer's jitter), closest hit with back faces culled,
+//              shading basis, outgoing direction, material, the generator state before
+//              bsdf_prepare (each pass rebuilds the same stochastic lobe albedos from it);
+//   initial    C candidates x_i = (light, r1, r2) from the source density p = 1 / (lights *
+//              area) in area measure, streaming RIS with weight p^(x) / p(x), where the target
+//              p^(x) is the luminance of the unshadowed contribution f * Le * |cos| * cosL / d^2;
+//              then the chosen sample's visibility (shadow ray; occluded => W = 0);
+//   temporal   reprojection of the primary hit into the previous frame's camera; when the
+//              previous pixel's surface is similar (normal within 25 degrees, camera distance
+//              within 10 %) its reservoir is merged, its M capped at 20 x C;
+//   spatial    up to 5 neighbours in a 30-pixel disk with similar surfaces are merged;
+//   shade      the final sample's contribution times W and its visibility (a second shadow
+//              ray), plus the primary hit's emission; misses see the white sky.
+// Reservoir merging is the biased combination of the paper (no 1/Z correction).  Visibility
+// means the closest hit is the light sample's own triangle (instance and primitive), with the
+// shadow rays' semantics of the path tracer (no culling, t in [1e-3, 1e4]).
+//
+// Random streams: the G-buffer pass uses the pixel generator of the path tracer (two jitter
+// draws); every later pass starts its own stream from jenkins_hash(seed + pass), where seed is
+// the stored generator state.  The CPU oracle restates every pass with the same operations,
+// and the tests compare the images and reservoirs bit for bit.
+#pragma once
+
+#include "tt_shade.cuh"
+
+namespace tt {
+
+struct Reservoir {
+    uint32_t light;    // emissive triangle index (0xffffffff: empty)
+    float r1, r2;      // the sample_triangle random numbers of the chosen point
+    float w_sum;       // running sum of resampling weights
+    float M;           // candidates represented
+    float W;           // unbiased contribution weight of the chosen sample
+    float pad0, pad1;  // 32-byte records
+};
+
+constexpr uint32_t NO_LIGHT = 0xffffffffu;
+constexpr uint32_t NO_SURFACE = 0xffffffffu;
+
+// G-buffer record of one pixel (64 bytes).
+struct Surface {
+    float4 pos_dist;      // world position, distance from the camera
+    float4 normal_mat;    // shading normal, material index bits (NO_SURFACE: the camera ray missed)
+    float4 tangent_inst;  // shading tangent, instance bits
+    float4 wi_seed;       // outgoing direction in the shading basis, generator state bits
+};
+
+TT_HD float luminance(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+// World position, normal (one-sided, cross(p1-p0, p2-p0)), area and emission of a light point.
+struct LightPoint {
+    f3 pos, normal, emission;
+    float area;
+    uint32_t instance;
+};
+__device__ __forceinline__ LightPoint light_point(const DevScene& sc, uint32_t light, float r1, float r2) {
+    const tt_emissive_triangle* tri = sc.emissive + light;
+    LightPoint lp;
+    lp.instance = __ldg(&tri->instance_index);
+    const tt_instance* in = sc.instances + lp.instance;
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = __ldg(&in->transform[k]);
+    f3 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        p[k] = mat43_point(m, f3{dequant_snorm16(__ldg(&tri->positions[k][0])),
+                                 dequant_snorm16(__ldg(&tri->positions[k][1])),
+                                 dequant_snorm16(__ldg(&tri->positions[k][2]))});
+    f3 e = cross(p[1] - p[0], p[2] - p[0]);
+    lp.area = fmx(0.00001f, 0.5f * length(e));
+    lp.normal = normalize(e);
+    lp.pos = interp3(sample_triangle(f2{r1, r2}), p[0], p[1], p[2]);
+    lp.emission = material_emissive(sc.materials + __ldg(&in->material_index));
+    return lp;
+}
+
+// Unshadowed contribution f * Le * |cos| * cosL / d^2 of light point lp at the surface.
+__device__ __forceinline__ f3 restir_contribution(const MatC& mc, const Lobes& lobes, const Basis& basis, f3 wi,
+                                                  f3 pos, const LightPoint& lp) {
+    f3 d = lp.pos - pos;
+    float d2 = dot(d, d);
+    f3 dir = d / sqrtf(d2);
+    float cos_light = dot(-dir, lp.normal);
+    if (!(cos_light > 0.0f) || !(d2 > 0.0f)) return splat(0.0f);
+    f3 wo = transform_from_basis(basis, d);
+    float density = 0.0f;
+    f3 f = bsdf_evaluate(mc, lobes, wi, wo, density);
+    return f * lp.emission * (fabsf(cos_theta(wo)) * cos_light / d2);
+}
+
+// Weighted reservoir update: the candidate replaces the sample with probability w / w_sum.
+TT_HD bool reservoir_update(Reservoir& r, uint32_t light, float r1, float r2, float w, float m, uint32_t& g) {
+    r.w_sum += w;
+    r.M += m;
+    float u = random_float(g);
+    bool take = w > 0.0f && u * r.w_sum < w;
+    if (take) {
+        r.light = light;
+        r.r1 = r1;
+        r.r2 = r2;
+    }
+    return take;
+}
+
+TT_HD Reservoir empty_reservoir() {
+    Reservoir r;
+    r.light = NO_LIGHT;
+    r.r1 = r.r2 = 0.0f;
+    r.w_sum = 0.0f;
+    r.M = 0.0f;
+    r.W = 0.0f;
+    r.pad0 = r.pad1 = 0.0f;
+    return r;
+}
+
+// Visibility of a light point: the closest hit along the shadow ray is its own triangle.
+template <bool COUNT>
+__device__ __forceinline__ bool restir_visible(const DevScene& sc, f3 pos, const LightPoint& lp, uint32_t light,
+                                               uint32_t* stack, int stride, uint32_t* err) {
+    f3 d = lp.pos - pos;
+    f3 dir = d / sqrtf(dot(d, d));
+    Counters cnt{0u, 0u, 0u, 0u};
+    Hit h = trace_closest<COUNT>(sc, pos, dir, SHADOW_TMIN, SHADOW_TMAX, false, stack, stride, err, cnt);
+    return h.hit && h.instance == lp.instance && h.prim == __ldg(sc.light_prim + light);
+}
+
+}  // namespace tt

@@ -159,6 +159,11 @@ class StageTimings(ctypes.Structure):
     _fields_ = [("ns", ctypes.c_uint64 * 8), ("launches", ctypes.c_uint64 * 8), ("overflow", ctypes.c_uint64)]
 
 
+class RestirConfig(ctypes.Structure):
+    _fields_ = [("candidates", ctypes.c_uint32), ("temporal_m_cap", ctypes.c_float),
+                ("spatial_neighbours", ctypes.c_uint32), ("spatial_radius", ctypes.c_float)]
+
+
 class TuneResult(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("refill_lanes", ctypes.c_uint32), ("trace_blocks_per_sm", ctypes.c_uint32),
                 ("renders", ctypes.c_uint32), ("default_ms", ctypes.c_float), ("best_ms", ctypes.c_float)]
@@ -206,6 +211,10 @@ SIGNATURES = {
     "tt_timings_get": (_I32, [_P, ctypes.POINTER(Timings)]),
     "tt_stage_timings_get": (_I32, [_P, ctypes.POINTER(StageTimings)]),
     "tt_autotune": (_I32, [_P, _U64, _P, _U64, ctypes.POINTER(TuneResult)]),
+    "tt_restir_configure": (_I32, [_P, ctypes.POINTER(RestirConfig)]),
+    "tt_restir_reset": (_I32, [_P]),
+    "tt_render_restir": (_I32, [_P, _U64, _P, _U64]),
+    "tt_restir_download": (_I32, [_P, _P, _U64]),
     "tt_server_create": (_I32, [_P, ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "tt_server_destroy": (_I32, [_P]),
     "tt_server_submit": (_I32, [_P, _U64, _P, _P, _U64, ctypes.POINTER(ctypes.c_uint64)]),

@@ -264,6 +264,27 @@ class Renderer:
         check(self.context.lib.tt_render(self.context.handle, self.scene, native.ptr(c), self.render_target))
         self.accumulated_frame_count += 1
 
+    def render_restir_to_target(self) -> None:
+        """One ReSTIR DI frame (direct light at the primary hit, 1 sample per pixel) into the
+        render target, with the same accumulation rule as render_to_target."""
+        c = self.constants()
+        check(self.context.lib.tt_render_restir(self.context.handle, self.scene, native.ptr(c), self.render_target))
+        self.accumulated_frame_count += 1
+
+    def restir_configure(self, candidates: int = 32, temporal_m_cap: float = 20.0, spatial_neighbours: int = 5,
+                         spatial_radius: float = 30.0) -> None:
+        cfg = native.RestirConfig(candidates, temporal_m_cap, spatial_neighbours, spatial_radius)
+        check(self.context.lib.tt_restir_configure(self.context.handle, ctypes.byref(cfg)))
+
+    def restir_reset(self) -> None:
+        check(self.context.lib.tt_restir_reset(self.context.handle))
+
+    def restir_reservoirs(self) -> np.ndarray:
+        w, h = self.extent
+        out = np.zeros((h, w, 8), np.float32)
+        check(self.context.lib.tt_restir_download(self.context.handle, native.ptr(out), out.nbytes))
+        return out
+
     def autotune(self, sample_count: int = 8) -> native.TuneResult:
         """Tunes the wavefront integrator's pool size, refill threshold and trace-kernel
         residency for the current scene and camera (tt_autotune) with short renders of

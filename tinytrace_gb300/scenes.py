@@ -79,7 +79,7 @@ def cornell_box(light_radiance: float = 15.0) -> AssetScene:
                                        emission_luminance=light_radiance, emission_color=(1.0, 1.0, 1.0)))
     items = []
     # light first: its triangles get the smallest global indices
-    items.append((_quad((-0.25, 1.98, -0.25), (-0.25, 1.98, 0.25), (0.25, 1.98, 0.25), (0.25, 1.98, -0.25)), light))
+    items.append((_quad((-0.25, 1.98, -0.25), (0.25, 1.98, -0.25), (0.25, 1.98, 0.25), (-0.25, 1.98, 0.25)), light))  # -y
     items.append((_quad((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)), white))       # floor, +y
     items.append((_quad((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)), white))       # ceiling, -y
     items.append((_quad((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)), white))     # back, +z
