@@ -57,6 +57,7 @@ def parse_args():
     p.add_argument("--host-loop", action="store_true", help="drive the wavefront loop from the host (no CUDA graph)")
     p.add_argument("--no-autotune", action="store_true", help="skip tt_autotune before the warm-up")
     p.add_argument("--no-serve", action="store_true", help="skip the serving sample")
+    p.add_argument("--no-restir", action="store_true", help="skip the ReSTIR DI sample")
     p.add_argument("--serve-rates", default="2,8,32", help="Poisson arrival rates (requests/s) of the serving sample")
     p.add_argument("--serve-requests", type=int, default=12, help="requests per arrival rate")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level"],
@@ -250,6 +251,53 @@ def run_reference(a, dist: Dist):
            "note": "reference arm = the reference path tracer restated on the CPU (oracle/); the reference "
                    "itself (Rust + Vulkan ray queries) cannot run on this machine"}
     print(json.dumps(out))
+
+
+# ---------------------------------------------------------------- ReSTIR DI sample
+def run_restir(a, device: int) -> dict:
+    """ReSTIR DI on the 2.1 M-triangle, 100 k-light scene: 1920x1080, 1 sample per pixel per frame,
+    32 candidates, temporal reuse (M cap 20 x), 5 spatial neighbours in 30 px, a 60-frame orbit;
+    device time of the 60 frames by CUDA events on the context stream."""
+    import ctypes
+
+    from tinytrace_gb300 import native, scenes
+    from tinytrace_gb300.native import check
+    from tinytrace_gb300.renderer import Config, Renderer
+
+    W, H, frames = a.width, a.height, 60
+    r = Renderer((W, H), device=device)
+    scene = scenes.restir_field()
+    r.set_scene(scene)
+    r.set_config(Config(bounce_count=1, sample_count=1))
+    lib, ctx = r.context.lib, r.context.handle
+
+    def orbit(f):
+        ang = 2.0 * np.pi * f / frames
+        return scenes.Camera.looking_at((95.0 * np.sin(ang), 10.0, 95.0 * np.cos(ang)), (0.0, 0.0, 0.0))
+
+    for f in range(3):
+        r.camera = orbit(f)
+        r.render_restir_to_target()
+        r.present()
+    r.restir_reset()
+    check(lib.tt_synchronize(ctx))
+    check(lib.tt_event_record(ctx, 2))
+    for f in range(frames):
+        r.camera = orbit(f)
+        check(lib.tt_flush_l2(ctx))
+        r.render_restir_to_target()
+        r.present()
+    check(lib.tt_event_record(ctx, 3))
+    ms = ctypes.c_float()
+    check(lib.tt_event_elapsed_ms(ctx, 2, 3, ctypes.byref(ms)))
+    img = r.context.download(r.render_target, W, H)
+    stats = r.context.scene_stats(r.scene)
+    r.close()
+    return {"workload": f"restir_field_{stats.triangle_count}tri_{int(stats.emissive_count)}lights_{W}x{H}_60frames",
+            "ms_per_frame": ms.value / frames, "msamples_per_s": W * H * frames / (ms.value / 1e3) / 1e6,
+            "candidates": 32, "temporal_m_cap": 20, "spatial_neighbours": 5, "spatial_radius_px": 30,
+            "l2": "flushed before every frame", "image_mean": float(img[..., :3].mean()),
+            "image_finite": bool(np.isfinite(img).all())}
 
 
 # ---------------------------------------------------------------- serving sample
@@ -480,6 +528,11 @@ def run_ours(a, dist: Dist):
         t = native.Timings()
         check(lib.tt_timings_get(ctx, ctypes.byref(t)))
         out_line["scene"]["build_ms"] = t.scene_build_ns / 1e6
+        if not a.no_restir and dist.world == 1:
+            try:
+                out_line["restir"] = run_restir(a, device)
+            except Exception as e:
+                out_line["restir"] = {"error": f"{type(e).__name__}: {e}"}
         if not a.no_serve and dist.world == 1:
             try:
                 out_line["serving"] = run_serving(a, r.context)

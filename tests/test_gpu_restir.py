@@ -38,7 +38,7 @@ def test_restir_frames_match_oracle(gpu_context, name):
     cpu = np.zeros((extent[1], extent[0], 4), np.float32)
     for f in range(6):
         r.camera = _orbit(center, radius, height, f)
-        c = make_constants(r.camera, extent, r.config, r.context.frame_index(), r.accumulated_frame_count)
+        c = make_constants(r.camera, extent, r.config(), r.context.frame_index(), r.accumulated_frame_count)
         r.render_restir_to_target()
         gpu = r.context.download(r.render_target, *extent)
         R.frame(c, cpu)
@@ -63,7 +63,7 @@ def test_restir_config_and_reset(gpu_context):
             r.restir_reset()
             R = oracle.OracleRestir(orc, *extent, candidates=8, m_cap_factor=4.0, neighbours=2, radius=10.0)
         r.camera = _orbit(center, radius, height, f)
-        c = make_constants(r.camera, extent, r.config, r.context.frame_index(), r.accumulated_frame_count)
+        c = make_constants(r.camera, extent, r.config(), r.context.frame_index(), r.accumulated_frame_count)
         r.render_restir_to_target()
         R.frame(c, cpu)
         assert_same_bits(r.context.download(r.render_target, *extent), cpu, f"frame {f}")

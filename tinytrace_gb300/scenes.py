@@ -206,7 +206,7 @@ def instanced_spheres(copies: int = 40, freq: int = 6, seed: int = 3, box: float
     s = AssetScene()
     light = s.insert_material(Material(emission_luminance=50.0))
     tri = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], np.float32)
-    lm = s.insert_mesh(tri, np.zeros((3, 2), np.float32), np.array([0, 2, 1], np.uint32))
+    lm = s.insert_mesh(tri, np.zeros((3, 2), np.float32), np.array([0, 1, 2], np.uint32))  # faces -y
     t = np.eye(4)
     t[:3, :3] *= 3.0
     t[:3, 3] = (0.0, box, 0.0)
@@ -221,6 +221,42 @@ def instanced_spheres(copies: int = 40, freq: int = 6, seed: int = 3, box: float
         if k % 7 == 3:
             t[:3, 0] *= -1.0  # mirrored instance: flips the triangle winding
         t[:3, 3] = rng.uniform(-box / 2, box / 2, 3)
+        s.root.children.append(Node(transform=t, models=[Model(m, mat)]))
+    return s
+
+
+def restir_field(instances: int = 128, freq: int = 28, light_meshes: int = 100, triangles_per_light: int = 1000,
+                 seed: int = 9, box: float = 100.0, displacement: float = 0.1) -> AssetScene:
+    """The many-light scene of the ReSTIR workload: `instances` displaced icospheres (128 x
+    15,680 = 2.0 M triangles at the defaults) and light_meshes x triangles_per_light emissive
+    triangles scattered through the box (100 k at the defaults), one emissive material per light
+    mesh with power ~ LogNormal(0, 1)."""
+    rng = np.random.default_rng(seed)
+    s = AssetScene()
+    half = box / 2.0
+    for _ in range(light_meshes):
+        n = triangles_per_light
+        centers = rng.uniform(-half, half, (n, 1, 3))
+        tri = rng.normal(size=(n, 3, 3))
+        tri = tri / np.linalg.norm(tri, axis=2, keepdims=True) * rng.uniform(0.3, 1.0, (n, 1, 1))
+        pts = (centers + tri).reshape(-1, 3).astype(np.float32)
+        area = 0.5 * np.linalg.norm(np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]), axis=1).mean()
+        lum = 100.0 * float(rng.lognormal(0.0, 1.0)) / (np.pi * max(area, 1e-3) * n) * 50.0
+        mat = s.insert_material(Material(base_color=(0.8, 0.8, 0.8), emission_luminance=lum,
+                                         emission_color=tuple(rng.uniform(0.6, 1.0, 3))))
+        m = s.insert_mesh(pts, np.zeros((len(pts), 2), np.float32), np.arange(len(pts), dtype=np.uint32))
+        s.root.children.append(Node(models=[Model(m, mat)]))
+    base_pts, tris = geodesic_sphere(freq)
+    for _ in range(instances):
+        disp = 1.0 + displacement * _fbm(base_pts, rng)
+        pts = (base_pts * disp[:, None]).astype(np.float32)
+        m = s.insert_mesh(pts, None, tris)
+        mat = s.insert_material(Material(base_color=tuple(rng.uniform(0.2, 0.9, 3)),
+                                         base_metalness=float(rng.integers(0, 2)),
+                                         specular_roughness=float(rng.uniform(0.05, 1.0))))
+        t = np.eye(4)
+        t[:3, :3] = _random_rotation(rng) * rng.uniform(4.0, 12.0)
+        t[:3, 3] = rng.uniform(-half, half, 3)
         s.root.children.append(Node(transform=t, models=[Model(m, mat)]))
     return s
 
