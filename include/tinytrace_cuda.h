@@ -223,6 +223,12 @@ int32_t tt_image_download(tt_context* ctx, tt_handle image, float* host, uint64_
  * (crates/tinytrace_backend/src/resource.rs:728-880, 891-1085), which become a GPU LBVH. */
 int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* desc, tt_handle* out);
 int32_t tt_scene_stats_get(tt_context* ctx, tt_handle scene, tt_scene_stats* out);
+/* Moves instances (the TLAS update of the reference: TlasBuildMode::Update,
+ * crates/tinytrace_backend/src/resource.rs:993-1003): new transforms, inverse and normal
+ * transforms for all `count` instances of the scene (mesh, material and offsets unchanged).
+ * The world-space structure (flat BVH or TLAS) keeps its topology and refits its boxes, so
+ * closest hits stay exact; traversal slows as instances move far from where it was built. */
+int32_t tt_scene_update_instances(tt_context* ctx, tt_handle scene, const tt_instance* instances, uint32_t count);
 /* BVH arrays for node-for-node comparison: blas nodes (128 B each), triangle records
  * (48 B each), tlas nodes (128 B each; the flat BVH of a flat scene).  Sizes in bytes must
  * match tt_scene_stats. */

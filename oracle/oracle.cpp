@@ -726,6 +726,14 @@ void oracle_bsdf_sample_batch(const MaterialConstants* m, const float* samples, 
     }
 }
 
+// New instance transforms (same count, meshes, materials): refits both world structures.
+void oracle_scene_update_instances(void* p, const Instance* instances, uint32_t count) {
+    OracleScene* s = static_cast<OracleScene*>(p);
+    if (count != s->instances.size()) return;
+    std::memcpy(s->instances.data(), instances, sizeof(Instance) * count);
+    if (s->use_bvh) refit_world_structures(s->geom(), s->bvh);
+}
+
 // ReSTIR DI state of the oracle: config = {candidates, m_cap_factor, neighbours, radius}.
 void* oracle_restir_create(void* scene, uint32_t width, uint32_t height, uint32_t candidates, float m_cap_factor,
                            uint32_t neighbours, float radius) {

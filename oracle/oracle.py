@@ -42,6 +42,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_bsdf_eval_batch.argtypes = [_P, _P, ctypes.c_uint32, _P]
         lib.oracle_bsdf_sample_batch.argtypes = [_P, _P, ctypes.c_uint32, _P]
         lib.oracle_math.argtypes = [ctypes.c_int, _P, ctypes.c_uint64, _P]
+        lib.oracle_scene_update_instances.argtypes = [_P, _P, ctypes.c_uint32]
         lib.oracle_restir_create.restype = _P
         lib.oracle_restir_create.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                              ctypes.c_uint32, ctypes.c_float]
@@ -96,6 +97,12 @@ class OracleScene:
         tris = np.zeros(int(info[6]), TRI_RECORD_DTYPE)
         self.lib.oracle_scene_flat_copy(self.handle, _p(nodes), _p(tris))
         return nodes, tris, int(info[7])
+
+    def update_instances(self, instances: np.ndarray) -> None:
+        """New instance transforms (the TLAS update); refits both world structures."""
+        inst = np.ascontiguousarray(instances)
+        self.arrays.instances = inst
+        self.lib.oracle_scene_update_instances(self.handle, _p(inst), len(inst))
 
     def trace(self, rays: np.ndarray, cull: bool, brute: bool = False, threads: int = 0, flat: bool = False) -> np.ndarray:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)

@@ -587,6 +587,76 @@ inline SceneBvh build_scene_bvh(const Geometry& g, int leaf_max) {
     return s;
 }
 
+// ---------------------------------------------------------------- refit (instance update)
+// Union of a node's child boxes.
+inline Aabb node_union(const Node4& nd) {
+    Aabb b = aabb_empty();
+    for (uint32_t c = 0; c < nd.count; ++c)
+        b = aabb_union(b, Aabb{v3{nd.box[0][c], nd.box[2][c], nd.box[4][c]}, v3{nd.box[1][c], nd.box[3][c], nd.box[5][c]}});
+    return b;
+}
+inline void set_child_box(Node4& nd, int c, const Aabb& b) {
+    nd.box[0][c] = b.lo.x;
+    nd.box[1][c] = b.hi.x;
+    nd.box[2][c] = b.lo.y;
+    nd.box[3][c] = b.hi.y;
+    nd.box[4][c] = b.lo.z;
+    nd.box[5][c] = b.hi.z;
+}
+inline float root_bound(const std::vector<Node4>& nodes) {
+    float bound = 0.0f;
+    if (nodes.empty()) return bound;
+    const Node4& r = nodes[0];
+    for (int k = 0; k < 6; ++k)
+        for (uint32_t c = 0; c < r.count; ++c) bound = fmx(bound, std::fabs(r.box[k][c]));
+    return bound;
+}
+// Refits the flat BVH and the TLAS to the instances' current transforms (topology kept):
+// children have larger node indices than their parents, so one reverse pass suffices.
+inline void refit_world_structures(const Geometry& g, SceneBvh& s) {
+    for (size_t i = s.flat.size(); i-- > 0;) {
+        Node4& nd = s.flat[i];
+        for (uint32_t c = 0; c < nd.count; ++c) {
+            uint32_t r = nd.child[c];
+            Aabb b = aabb_empty();
+            if (r & CHILD_LEAF) {
+                for (uint32_t q = leaf_first(r); q < leaf_first(r) + leaf_count(r); ++q) {
+                    const TriRecord& tr = s.flat_tris[q];
+                    const Instance& in = g.instances[tr.mesh];
+                    v3 w0 = mat43_point(in.transform, v3{tr.v0[0], tr.v0[1], tr.v0[2]});
+                    v3 w1 = mat43_point(in.transform, v3{tr.v1[0], tr.v1[1], tr.v1[2]});
+                    v3 w2 = mat43_point(in.transform, v3{tr.v2[0], tr.v2[1], tr.v2[2]});
+                    b = aabb_union(b, canon_box(aabb_point(aabb_point(Aabb{w0, w0}, w1), w2)));
+                }
+            } else {
+                b = node_union(s.flat[r]);
+            }
+            set_child_box(nd, (int)c, b);
+        }
+    }
+    s.flat_bound = root_bound(s.flat);
+    for (size_t i = s.tlas.size(); i-- > 0;) {
+        Node4& nd = s.tlas[i];
+        for (uint32_t c = 0; c < nd.count; ++c) {
+            uint32_t r = nd.child[c];
+            Aabb b = aabb_empty();
+            if (r & CHILD_LEAF) {
+                const Instance& in = g.instances[leaf_first(r)];
+                Aabb mb = node_union(s.blas[in.mesh_index]);
+                for (int k = 0; k < 8; ++k) {
+                    v3 cc = v3{(k & 1) ? mb.hi.x : mb.lo.x, (k & 2) ? mb.hi.y : mb.lo.y, (k & 4) ? mb.hi.z : mb.lo.z};
+                    b = aabb_point(b, mat43_point(in.transform, cc));
+                }
+                b = canon_box(b);
+            } else {
+                b = node_union(s.tlas[r]);
+            }
+            set_child_box(nd, (int)c, b);
+        }
+    }
+    s.tlas_bound = root_bound(s.tlas);
+}
+
 inline void trace_blas(const SceneBvh& s, uint32_t root, uint32_t inst, const RayPre& rp,
                        const NodeRay& nr, bool cull_back, float tmin, Hit& best, float& tbest) {
     uint32_t stack[256];

@@ -76,6 +76,8 @@ struct SceneRes {
     BvhResult bvh;
     DevScene dev{};
     tt_scene_stats stats{};
+    std::vector<tt_instance> host_instances;  // for tt_scene_update_instances' checks
+    uint32_t material_count = 0;
 };
 
 // Slot pool and queues of the wavefront integrator, grown on demand and kept across frames.
@@ -628,6 +630,8 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         upload(s->materials, d->materials, d->material_count, st);
         upload(s->meshes, d->meshes, d->mesh_count, st);
         upload(s->instances, d->instances, d->instance_count, st);
+        s->host_instances.assign(d->instances, d->instances + d->instance_count);
+        s->material_count = d->material_count;
         upload(s->emissive, d->emissive_triangles, d->emissive_triangle_count, st);
         std::vector<uint32_t> lprim = light_primitives(d);
         upload(s->light_prim, lprim.data(), lprim.size(), st);
@@ -713,6 +717,43 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         Pool& p = ctx->pools[TT_LIFETIME_SCENE];
         p.scenes.push_back(std::move(s));
         *out = make_handle(TT_LIFETIME_SCENE, KIND_SCENE, p.epoch, (uint32_t)(p.scenes.size() - 1));
+    });
+}
+
+int32_t tt_scene_update_instances(tt_context* ctx, tt_handle scene, const tt_instance* instances, uint32_t count) {
+    return guarded([&] {
+        require(ctx && (count == 0 || instances), "null argument");
+        use_device(ctx);
+        SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
+        require(count == s->host_instances.size(), "instance count must equal the scene's");
+        for (uint32_t i = 0; i < count; ++i) {
+            const tt_instance &a = instances[i], &b = s->host_instances[i];
+            require(a.mesh_index == b.mesh_index && a.index_offset == b.index_offset &&
+                        a.vertex_offset == b.vertex_offset && a.material_index == b.material_index,
+                    "an update may change transforms only (mesh, material and offsets stay)");
+            for (int k = 0; k < 16; ++k)
+                require(std::isfinite(a.transform[k]) && std::isfinite(a.inverse_transform[k]) &&
+                            std::isfinite(a.normal_transform[k]),
+                        "instance matrices must be finite");
+        }
+        cudaStream_t st = ctx->stream;
+        if (count) {
+            check_cuda(cudaMemcpyAsync(s->instances.ptr, instances, sizeof(tt_instance) * count, cudaMemcpyHostToDevice, st),
+                       "instances");
+            std::vector<float4> xf(4ull * count);
+            for (uint32_t i = 0; i < count; ++i) {
+                const float* m = instances[i].inverse_transform;
+                for (int r = 0; r < 3; ++r) xf[4ull * i + r] = make_float4(m[r], m[4 + r], m[8 + r], m[12 + r]);
+                uint32_t w[4] = {instances[i].mesh_index, instances[i].material_index, instances[i].index_offset,
+                                 instances[i].vertex_offset};
+                std::memcpy(&xf[4ull * i + 3], w, 16);
+            }
+            check_cuda(cudaMemcpyAsync(s->inst_xform.ptr, xf.data(), 16ull * xf.size(), cudaMemcpyHostToDevice, st),
+                       "instance rows");
+            refit_scene_bvh(s->instances.as<tt_instance>(), st, s->bvh);  // synchronises the stream
+            s->dev.tlas_bound = s->bvh.flat ? s->bvh.flat_bound : s->bvh.tlas_bound;
+            s->host_instances.assign(instances, instances + count);
+        }
     });
 }
 

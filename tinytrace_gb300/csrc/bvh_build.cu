@@ -543,6 +543,7 @@ __global__ void segment_boxes_kernel(const int* roots, uint32_t segs, const floa
 struct Build4 {
     uint64_t nodes = 0;
     uint32_t levels = 0;
+    std::vector<uint64_t> level_start;  // first node of each level (levels + 1 entries)
     uint32_t* order = nullptr;  // scratch, sorted position -> primitive
     float4* blo = nullptr;      // scratch, binary node boxes
     float4* bhi = nullptr;
@@ -606,6 +607,7 @@ Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uin
     uint32_t L = segs;
     while (L > 0) {
         out.levels++;
+        out.level_start.push_back(base);
         collapse_choose_kernel<<<grid_for(L, 128), 128, 0, st>>>(tv, lvl_a, L, leaf_max, chosen, icount);
         check_cuda(cudaMemsetAsync(icount + L, 0, 4, st), "memset");
         exclusive_scan(icount, (uint64_t)L + 1, sc);
@@ -621,6 +623,7 @@ Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uin
         std::swap(lvl_a, lvl_b);
     }
     out.nodes = base;
+    out.level_start.push_back(base);
     return out;
 }
 
@@ -671,10 +674,131 @@ static void build_flat(const BuildInput& in, cudaStream_t stream, int leaf_max, 
     Build4 b = build_bvh4(plo, phi, seg, n, 1, leaf_max, false, nullptr, out.flat_nodes_buf, sc);
     out.flat_nodes = b.nodes;
     out.flat_levels = b.levels;
+    out.flat_level_start = b.level_start;
     gather_records_kernel<<<grid_for(n, 256), 256, 0, stream>>>(recs, b.order, n, out.flat_tris.as<float4>());
     out.flat_bound = root_bound(b, stream);
     check_cuda(cudaStreamSynchronize(stream), "bvh build");
     check_cuda(cudaGetLastError(), "bvh build kernels");
+}
+
+// ---------------------------------------------------------------- refit (instance update)
+// Child boxes of node j: the union of its planes over its children.
+static __device__ __forceinline__ void node_box(const uint4* nodes, uint32_t j, f3& lo, f3& hi) {
+    const float4* p = reinterpret_cast<const float4*>(nodes) + 8ull * j;
+    uint32_t cnt = reinterpret_cast<const uint4*>(p)[7].x;
+    float4 lx = p[0], hx = p[1], ly = p[2], hy = p[3], lz = p[4], hz = p[5];
+    const float al[3][4] = {{lx.x, lx.y, lx.z, lx.w}, {ly.x, ly.y, ly.z, ly.w}, {lz.x, lz.y, lz.z, lz.w}};
+    const float ah[3][4] = {{hx.x, hx.y, hx.z, hx.w}, {hy.x, hy.y, hy.z, hy.w}, {hz.x, hz.y, hz.z, hz.w}};
+    float l[3], h[3];
+    for (int a = 0; a < 3; ++a) {
+        l[a] = __int_as_float(0x7f800000);
+        h[a] = __int_as_float(0xff800000);
+        for (uint32_t c = 0; c < cnt; ++c) {
+            l[a] = fmn(l[a], al[a][c]);
+            h[a] = fmx(h[a], ah[a][c]);
+        }
+    }
+    lo = f3{l[0], l[1], l[2]};
+    hi = f3{h[0], h[1], h[2]};
+}
+
+// World box of one flat record (object-space vertices, instance in b.w) under the instance's
+// current transform: the flat build's box (flat_prims_kernel).
+static __device__ __forceinline__ void record_box(const float4* recs, uint32_t q, const tt_instance* inst, f3& lo, f3& hi) {
+    float4 a = recs[3ull * q], b = recs[3ull * q + 1], c = recs[3ull * q + 2];
+    const tt_instance& in = inst[__float_as_uint(b.w)];
+    f3 w0 = mat43_point(in.transform, f3{a.x, a.y, a.z});
+    f3 w1 = mat43_point(in.transform, f3{b.x, b.y, b.z});
+    f3 w2 = mat43_point(in.transform, f3{c.x, c.y, c.z});
+    lo = f3{canon(fmn(fmn(w0.x, w1.x), w2.x)), canon(fmn(fmn(w0.y, w1.y), w2.y)), canon(fmn(fmn(w0.z, w1.z), w2.z))};
+    hi = f3{canon(fmx(fmx(w0.x, w1.x), w2.x)), canon(fmx(fmx(w0.y, w1.y), w2.y)), canon(fmx(fmx(w0.z, w1.z), w2.z))};
+}
+
+// World box of an instance from its mesh's BLAS root box (instance_prims_kernel).
+static __device__ __forceinline__ void instance_box(const tt_instance& in, const uint4* blas, f3& lo, f3& hi) {
+    f3 ml, mh;
+    node_box(blas, in.mesh_index, ml, mh);
+    f3 l = splat(__int_as_float(0x7f800000)), h = splat(__int_as_float(0xff800000));
+    for (int k = 0; k < 8; ++k) {
+        f3 c = f3{(k & 1) ? mh.x : ml.x, (k & 2) ? mh.y : ml.y, (k & 4) ? mh.z : ml.z};
+        f3 w = mat43_point(in.transform, c);
+        l = f3{fmn(l.x, w.x), fmn(l.y, w.y), fmn(l.z, w.z)};
+        h = f3{fmx(h.x, w.x), fmx(h.y, w.y), fmx(h.z, w.z)};
+    }
+    lo = f3{canon(l.x), canon(l.y), canon(l.z)};
+    hi = f3{canon(h.x), canon(h.y), canon(h.z)};
+}
+
+// Refits the nodes [start, end) of one level from their children (deeper levels are done).
+static __global__ void refit_level_kernel(uint4* nodes, uint64_t start, uint64_t end, const float4* recs,
+                                   const tt_instance* inst, const uint4* blas, int tlas) {
+    uint64_t i = start + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    float4* p = reinterpret_cast<float4*>(nodes) + 8ull * i;
+    uint4 ch = reinterpret_cast<uint4*>(p)[6];
+    uint32_t cnt = reinterpret_cast<uint4*>(p)[7].x;
+    const uint32_t child[4] = {ch.x, ch.y, ch.z, ch.w};
+    float bx[6][4];
+    for (int c = 0; c < 4; ++c) {
+        f3 lo = splat(__int_as_float(0x7f800000)), hi = splat(__int_as_float(0xff800000));
+        if ((uint32_t)c < cnt) {
+            uint32_t r = child[c];
+            if (r & 0x80000000u) {
+                if (tlas) {
+                    instance_box(inst[r & 0x07ffffffu], blas, lo, hi);
+                } else {
+                    uint32_t f = r & 0x07ffffffu, k = ((r >> 27) & 0xfu) + 1u;
+                    for (uint32_t q = f; q < f + k; ++q) {
+                        f3 l, h;
+                        record_box(recs, q, inst, l, h);
+                        lo = f3{fmn(lo.x, l.x), fmn(lo.y, l.y), fmn(lo.z, l.z)};
+                        hi = f3{fmx(hi.x, h.x), fmx(hi.y, h.y), fmx(hi.z, h.z)};
+                    }
+                }
+            } else {
+                node_box(nodes, r, lo, hi);
+            }
+        }
+        bx[0][c] = lo.x;
+        bx[1][c] = hi.x;
+        bx[2][c] = lo.y;
+        bx[3][c] = hi.y;
+        bx[4][c] = lo.z;
+        bx[5][c] = hi.z;
+    }
+    for (int k = 0; k < 6; ++k) p[k] = make_float4(bx[k][0], bx[k][1], bx[k][2], bx[k][3]);
+}
+
+// Root-node bound: max |coordinate| over the root's child boxes.
+static float root_node_bound(const DeviceBuffer& nodes, cudaStream_t stream) {
+    float4 pl[8];
+    check_cuda(cudaMemcpyAsync(pl, nodes.ptr, 128, cudaMemcpyDeviceToHost, stream), "root node");
+    check_cuda(cudaStreamSynchronize(stream), "sync");
+    uint32_t cnt = reinterpret_cast<const uint4*>(pl)[7].x;
+    float bound = 0.0f;
+    for (int k = 0; k < 6; ++k) {
+        const float v[4] = {pl[k].x, pl[k].y, pl[k].z, pl[k].w};
+        for (uint32_t c = 0; c < cnt; ++c) bound = std::max(bound, std::fabs(v[c]));
+    }
+    return bound;
+}
+
+void refit_scene_bvh(const tt_instance* d_instances, cudaStream_t stream, BvhResult& b) {
+    bool flat = b.flat;
+    DeviceBuffer& nodes = flat ? b.flat_nodes_buf : b.tlas;
+    const std::vector<uint64_t>& ls = flat ? b.flat_level_start : b.tlas_level_start;
+    if ((flat ? b.flat_nodes : b.tlas_nodes) == 0) return;
+    for (size_t l = ls.size() - 1; l-- > 0;) {
+        uint64_t start = ls[l], end = ls[l + 1];
+        if (end <= start) continue;
+        refit_level_kernel<<<grid_for(end - start, 128), 128, 0, stream>>>(
+            nodes.as<uint4>(), start, end, flat ? b.flat_tris.as<float4>() : nullptr, d_instances,
+            flat ? nullptr : b.blas.as<uint4>(), flat ? 0 : 1);
+    }
+    check_cuda(cudaGetLastError(), "refit");
+    float bound = root_node_bound(nodes, stream);
+    if (flat) b.flat_bound = bound;
+    else b.tlas_bound = bound;
 }
 
 void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, BvhResult& out) {
@@ -748,6 +872,7 @@ void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bo
         Build4 tb = build_bvh4(ilo, ihi, iseg, ni, 1, 1, true, d_ids, out.tlas, sc);
         out.tlas_nodes = tb.nodes;
         out.tlas_levels = tb.levels;
+        out.tlas_level_start = tb.level_start;
         out.tlas_bound = root_bound(tb, stream);  // bound of the world-space slab margins
     } else {
         out.tlas_nodes = 0;

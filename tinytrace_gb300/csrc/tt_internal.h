@@ -43,6 +43,7 @@ struct BvhResult {
     uint64_t blas_nodes = 0, tlas_nodes = 0, tri_count = 0;
     uint32_t blas_levels = 0, tlas_levels = 0;
     float tlas_bound = 0.0f;  // max |coordinate| of the instance world boxes
+    std::vector<uint64_t> tlas_level_start, flat_level_start;  // first node of each level (+ end)
     // single-level BVH over the world boxes of every (instance, triangle) pair
     bool flat = false;
     DeviceBuffer flat_nodes_buf;  // 128-byte BVH4 nodes
@@ -68,5 +69,9 @@ void set_last_error(const std::string& message);
 // == mesh index, and TLAS with root 0) or, when `flat`, one BVH over the world boxes of all
 // (instance, triangle) pairs (root 0).
 void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, BvhResult& out);
+
+// Refits the world-space structure (the flat BVH, or the TLAS) to new instance transforms
+// (device array `d_instances`), keeping its topology; updates the slab-margin bound.
+void refit_scene_bvh(const tt_instance* d_instances, cudaStream_t stream, BvhResult& b);
 
 }  // namespace tt

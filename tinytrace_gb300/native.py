@@ -211,6 +211,7 @@ SIGNATURES = {
     "tt_timings_get": (_I32, [_P, ctypes.POINTER(Timings)]),
     "tt_stage_timings_get": (_I32, [_P, ctypes.POINTER(StageTimings)]),
     "tt_autotune": (_I32, [_P, _U64, _P, _U64, ctypes.POINTER(TuneResult)]),
+    "tt_scene_update_instances": (_I32, [_P, _U64, _P, _U32]),
     "tt_restir_configure": (_I32, [_P, ctypes.POINTER(RestirConfig)]),
     "tt_restir_reset": (_I32, [_P]),
     "tt_render_restir": (_I32, [_P, _U64, _P, _U64]),
