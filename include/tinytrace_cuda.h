@@ -283,6 +283,30 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
  * light index u32, r1, r2, w_sum, M, W, 0, 0). */
 int32_t tt_restir_download(tt_context* ctx, void* reservoirs, uint64_t bytes);
 
+/* ---------------------------------------------------------------- learned radiance cache
+ * An addition without reference counterpart: a hash-grid-encoded MLP predicting outgoing
+ * radiance from (position in the scene's unit cube, outgoing direction, shading normal,
+ * roughness), trained online on radiance the path tracer produces (Mueller et al. 2021/2022).
+ * Grid: 16 levels x 2^19 entries x 2 features; MLP: 64 inputs, 4 hidden layers of 64 ReLU
+ * units, 3 outputs; queries are 12 floats: pos xyz, dir xyz, normal xyz, roughness, 0, 0. */
+#define TT_CACHE_WEIGHTS 16896u          /* 4 x 64 x 64 hidden weights + 8 x 64 output rows (3 used) */
+#define TT_CACHE_GRID_FLOATS 16777216u   /* 16 levels x 2^19 entries x 2 features */
+typedef struct tt_cache_config {
+    float learning_rate;            /* Adam step size (1e-2) */
+    uint32_t train_paths_per_frame; /* paths traced to full depth to produce training radiance (65536) */
+    uint32_t terminate_depth;       /* other paths end in the cache at this vertex (2) */
+    uint32_t seed;                  /* parameter initialisation */
+} tt_cache_config;
+/* (Re)initialises the cache with `config`; tt_set_option(TT_OPTION_RADIANCE_CACHE, 1) makes
+ * tt_render use it. */
+int32_t tt_cache_configure(tt_context* ctx, const tt_cache_config* config);
+int32_t tt_cache_query(tt_context* ctx, const float* queries, uint32_t n, float* radiance);
+/* One Adam step on the mean relative L2 loss of n (query, target radiance) pairs; returns the
+ * summed loss before the step. */
+int32_t tt_cache_train(tt_context* ctx, const float* queries, const float* targets, uint32_t n, float* loss);
+/* FP32 parameters: grid (TT_CACHE_GRID_FLOATS, may be null) and weights (TT_CACHE_WEIGHTS). */
+int32_t tt_cache_parameters(tt_context* ctx, float* grid, float* weights);
+
 /* ---------------------------------------------------------------- serving
  * Continuous-batching render server (no reference counterpart: the reference renders one frame
  * at a time on the caller's thread).  Scenes are created on the server's context beforehand and

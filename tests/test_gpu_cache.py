@@ -1,0 +1,115 @@
+"""The learned radiance cache's CUDA kernels against the NumPy reference (GPU required).
+
+Tolerances: queries run in FP16 on the tensor cores, so they are compared with the reference's
+FP16 emulation within 2e-3 of the output scale; training is FP32, so the first Adam step (which
+moves every parameter with a nonzero gradient by exactly the learning rate, against the sign of
+its gradient) must agree in sign with the reference's float64 gradients, and the reported loss
+within 1e-4 relative."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cache_reference as cr
+from tinytrace_gb300 import native
+from tinytrace_gb300.native import check
+
+pytestmark = pytest.mark.gpu
+
+
+def _configure(ctx, seed=3, lr=1e-2):
+    cfg = native.CacheConfig(lr, 65536, 2, seed)
+    check(ctx.lib.tt_cache_configure(ctx.handle, ctypes.byref(cfg)))
+
+
+def _params(ctx):
+    grid = np.zeros(native.TT_CACHE_GRID_FLOATS, np.float32)
+    w = np.zeros(native.TT_CACHE_WEIGHTS, np.float32)
+    check(ctx.lib.tt_cache_parameters(ctx.handle, native.ptr(grid), native.ptr(w)))
+    return grid.reshape(cr.LEVELS, cr.TABLE, 2), w
+
+
+def _queries(rng, n):
+    q = np.zeros((n, 12), np.float32)
+    q[:, 0:3] = rng.uniform(0, 1, (n, 3))
+    d = rng.normal(size=(n, 3))
+    q[:, 3:6] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    m = rng.normal(size=(n, 3))
+    q[:, 6:9] = m / np.linalg.norm(m, axis=1, keepdims=True)
+    q[:, 9] = rng.uniform(0, 1, n)
+    return q
+
+
+def _field(q):
+    """A smooth synthetic radiance field to learn."""
+    p, d = q[:, 0:3], q[:, 3:6]
+    r = 1.0 + 0.8 * np.sin(6.0 * p[:, 0]) * np.cos(5.0 * p[:, 1]) + 0.5 * d[:, 2]
+    g = 1.0 + 0.6 * np.cos(4.0 * p[:, 2] + 2.0 * d[:, 0])
+    b = 0.5 + 0.4 * p[:, 1] * (1.0 + d[:, 1])
+    return np.stack([r, g, b], axis=1).astype(np.float32)
+
+
+def _train(ctx, q, t):
+    loss = ctypes.c_float()
+    check(ctx.lib.tt_cache_train(ctx.handle, native.ptr(q), native.ptr(t), len(q), ctypes.byref(loss)))
+    return loss.value
+
+
+def _query(ctx, q):
+    out = np.zeros((len(q), 3), np.float32)
+    check(ctx.lib.tt_cache_query(ctx.handle, native.ptr(q), len(q), native.ptr(out)))
+    return out
+
+
+def test_first_step_follows_the_reference_gradients(gpu_context):
+    ctx = gpu_context
+    _configure(ctx, seed=5)
+    rng = np.random.default_rng(1)
+    q = _queries(rng, 2048)
+    t = _field(q)
+    grid0, w0 = _params(ctx)
+    loss = _train(ctx, q, t)
+    grid1, w1 = _params(ctx)
+    ref_loss, g_w, g_grid = cr.loss_and_grads(q.astype(np.float64), t.astype(np.float64), grid0.astype(np.float64),
+                                              w0.astype(np.float64))
+    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    for before, after, g, name in ((w0, w1, g_w, "weights"), (grid0.ravel(), grid1.ravel(), g_grid.ravel(), "grid")):
+        big = np.abs(g) > 1e-4 * np.abs(g).max()
+        step = after.astype(np.float64) - before
+        agree = np.sign(step[big]) == -np.sign(g[big])
+        assert agree.mean() > 0.99, (name, agree.mean(), big.sum())
+        assert np.allclose(np.abs(step[big]), 1e-2, rtol=1e-2, atol=1e-5), name
+
+
+def test_queries_match_the_reference(gpu_context):
+    ctx = gpu_context
+    _configure(ctx, seed=7)
+    rng = np.random.default_rng(2)
+    for _ in range(20):  # move the parameters away from their initial values
+        qt = _queries(rng, 4096)
+        _train(ctx, qt, _field(qt))
+    grid, w = _params(ctx)
+    q = _queries(rng, 3000)
+    got = _query(ctx, q)
+    x = cr.encode(q.astype(np.float64), grid.astype(np.float64))
+    want16, _ = cr.forward(x, w, fp16=True)
+    want32, _ = cr.forward(x, w, fp16=False)
+    scale = np.abs(want32).max()
+    assert scale > 0.1
+    assert np.abs(got - want16).max() <= 2e-3 * scale + 1e-4, np.abs(got - want16).max() / scale
+    assert np.abs(got - want32).max() <= 2e-2 * scale
+
+
+def test_learns_a_smooth_field(gpu_context):
+    ctx = gpu_context
+    _configure(ctx, seed=11)
+    rng = np.random.default_rng(3)
+    first = None
+    for step in range(300):
+        q = _queries(rng, 8192)
+        loss = _train(ctx, q, _field(q)) / (3 * len(q))
+        first = loss if first is None else first
+    assert loss < first / 10, (first, loss)
+    q = _queries(rng, 4096)
+    err = np.abs(_query(ctx, q) - _field(q)).mean() / np.abs(_field(q)).mean()
+    assert err < 0.1, err

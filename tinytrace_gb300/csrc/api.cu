@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "tt_internal.h"
+#include "tt_cache.cuh"
 #include "tt_kernels.h"
 
 namespace tt {
@@ -98,6 +99,19 @@ struct RestirState {
     tt_restir_config config{32u, 20.0f, 5u, 30.0f};
 };
 
+// Learned radiance cache: device parameters and the configuration.
+struct CacheState {
+    DeviceBuffer grid, grid_m, grid_v, grid_grad, w, w_m, w_v, w_grad, w16, loss;
+    tt_cache_config config{1e-2f, 65536u, 2u, 1u};
+    uint32_t step = 0;
+    bool ready = false;
+    CacheDevice dev() const {
+        return CacheDevice{grid.as<float>(), grid_m.as<float>(), grid_v.as<float>(), grid_grad.as<float>(),
+                           w.as<float>(), w_m.as<float>(), w_v.as<float>(), w_grad.as<float>(), w16.as<__half>(),
+                           loss.as<float>()};
+    }
+};
+
 struct Pool {
     uint32_t epoch = 1;
     std::vector<std::unique_ptr<ImageRes>> images;
@@ -133,6 +147,7 @@ struct tt_context {
     std::vector<cudaEvent_t> stage_events;  // 2 * StageTimer::MAX_LAUNCHES, created on first use
     tt::StageTimer stage_timer;
     tt::RestirState restir;
+    tt::CacheState cache;
 };
 
 namespace tt {
@@ -990,6 +1005,80 @@ int32_t tt_restir_download(tt_context* ctx, void* reservoirs, uint64_t bytes) {
         require(R.pixels > 0 && bytes == 32ull * R.pixels, "byte count must equal width * height * 32");
         check_cuda(cudaMemcpyAsync(reservoirs, R.final_res[R.cur ^ 1u].ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream),
                    "download");
+        sync(ctx);
+    });
+}
+
+static void cache_ready(tt_context* ctx) {
+    CacheState& C = ctx->cache;
+    if (C.ready) return;
+    C.grid.alloc(4 * CACHE_GRID_PARAMS);
+    C.grid_m.alloc(4 * CACHE_GRID_PARAMS);
+    C.grid_v.alloc(4 * CACHE_GRID_PARAMS);
+    C.grid_grad.alloc(4 * CACHE_GRID_PARAMS);
+    C.w.alloc(4 * CACHE_PARAMS);
+    C.w_m.alloc(4 * CACHE_PARAMS);
+    C.w_v.alloc(4 * CACHE_PARAMS);
+    C.w_grad.alloc(4 * CACHE_PARAMS);
+    C.w16.alloc(2 * CACHE_PARAMS);
+    C.loss.alloc(16);
+    cache_set_level_scales();
+    cache_init(C.dev(), C.config.seed, ctx->stream);
+    C.step = 0;
+    C.ready = true;
+}
+
+int32_t tt_cache_configure(tt_context* ctx, const tt_cache_config* config) {
+    return guarded([&] {
+        require(ctx && config, "null argument");
+        require(config->learning_rate > 0.0f && std::isfinite(config->learning_rate), "bad learning rate");
+        require(config->terminate_depth >= 1, "terminate_depth must be at least 1");
+        use_device(ctx);
+        ctx->cache.config = *config;
+        ctx->cache.ready = false;
+        cache_ready(ctx);
+        sync(ctx);
+    });
+}
+
+int32_t tt_cache_query(tt_context* ctx, const float* queries, uint32_t n, float* radiance) {
+    return guarded([&] {
+        require(ctx && (n == 0 || (queries && radiance)), "null argument");
+        use_device(ctx);
+        cache_ready(ctx);
+        CacheDevice d = ctx->cache.dev();
+        batch(ctx, queries, 48ull * n, nullptr, 0, radiance, 12ull * n, [&](void* din, void*, void* dout) {
+            cache_infer(d, static_cast<const CacheQuery*>(din), n, static_cast<float*>(dout), ctx->stream);
+        });
+    });
+}
+
+int32_t tt_cache_train(tt_context* ctx, const float* queries, const float* targets, uint32_t n, float* loss) {
+    return guarded([&] {
+        require(ctx && (n == 0 || (queries && targets)), "null argument");
+        use_device(ctx);
+        cache_ready(ctx);
+        CacheState& C = ctx->cache;
+        CacheDevice d = C.dev();
+        uint32_t step = ++C.step;
+        batch(ctx, queries, 48ull * n, targets, 12ull * n, nullptr, 0, [&](void* din, void* dex, void*) {
+            cache_train_step(d, static_cast<const CacheQuery*>(din), static_cast<const float*>(dex), n,
+                             C.config.learning_rate, step, ctx->stream);
+        });
+        if (loss) check_cuda(cudaMemcpy(loss, C.loss.ptr, 4, cudaMemcpyDeviceToHost), "loss");
+    });
+}
+
+int32_t tt_cache_parameters(tt_context* ctx, float* grid, float* weights) {
+    return guarded([&] {
+        require(ctx && weights, "null argument");
+        use_device(ctx);
+        cache_ready(ctx);
+        CacheState& C = ctx->cache;
+        if (grid)
+            check_cuda(cudaMemcpyAsync(grid, C.grid.ptr, 4 * CACHE_GRID_PARAMS, cudaMemcpyDeviceToHost, ctx->stream),
+                       "grid");
+        check_cuda(cudaMemcpyAsync(weights, C.w.ptr, 4 * CACHE_PARAMS, cudaMemcpyDeviceToHost, ctx->stream), "weights");
         sync(ctx);
     });
 }

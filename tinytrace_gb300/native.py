@@ -51,6 +51,8 @@ TT_REQUEST_QUEUED = 0
 TT_REQUEST_RUNNING = 1
 TT_REQUEST_DONE = 2
 TT_REQUEST_FAILED = 3
+TT_CACHE_WEIGHTS = 16896
+TT_CACHE_GRID_FLOATS = 16777216
 TT_OPTION_REFILL_LANES = 6
 TT_OPTION_TRACE_BLOCKS_PER_SM = 7
 TT_STAGE_REGEN = 0
@@ -164,6 +166,11 @@ class RestirConfig(ctypes.Structure):
                 ("spatial_neighbours", ctypes.c_uint32), ("spatial_radius", ctypes.c_float)]
 
 
+class CacheConfig(ctypes.Structure):
+    _fields_ = [("learning_rate", ctypes.c_float), ("train_paths_per_frame", ctypes.c_uint32),
+                ("terminate_depth", ctypes.c_uint32), ("seed", ctypes.c_uint32)]
+
+
 class TuneResult(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("refill_lanes", ctypes.c_uint32), ("trace_blocks_per_sm", ctypes.c_uint32),
                 ("renders", ctypes.c_uint32), ("default_ms", ctypes.c_float), ("best_ms", ctypes.c_float)]
@@ -212,6 +219,10 @@ SIGNATURES = {
     "tt_stage_timings_get": (_I32, [_P, ctypes.POINTER(StageTimings)]),
     "tt_autotune": (_I32, [_P, _U64, _P, _U64, ctypes.POINTER(TuneResult)]),
     "tt_scene_update_instances": (_I32, [_P, _U64, _P, _U32]),
+    "tt_cache_configure": (_I32, [_P, ctypes.POINTER(CacheConfig)]),
+    "tt_cache_query": (_I32, [_P, _P, _U32, _P]),
+    "tt_cache_train": (_I32, [_P, _P, _P, _U32, _P]),
+    "tt_cache_parameters": (_I32, [_P, _P, _P]),
     "tt_restir_configure": (_I32, [_P, ctypes.POINTER(RestirConfig)]),
     "tt_restir_reset": (_I32, [_P]),
     "tt_render_restir": (_I32, [_P, _U64, _P, _U64]),
