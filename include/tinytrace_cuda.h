@@ -67,6 +67,8 @@ extern "C" {
                                        render; 0: the host drives it (also used while stage timing is on) */
 #define TT_OPTION_REFILL_LANES 6    /* trace warps refill idle lanes below this many busy lanes (1..32; 20) */
 #define TT_OPTION_TRACE_BLOCKS_PER_SM 7 /* resident blocks per SM of the trace kernel (0 = all that fit) */
+#define TT_OPTION_RADIANCE_CACHE 8  /* 1: wavefront renders end paths in the learned radiance cache and
+                                       train it after every frame (tt_cache_configure) */
 /* acceleration structures (tt_set_option TT_OPTION_ACCEL; tt_scene_stats.accel) */
 #define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
 #define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */
@@ -179,6 +181,7 @@ typedef struct tt_scene_stats {
 #define TT_STAGE_SHADOW 3  /* closest-hit trace of shadow rays */
 #define TT_STAGE_REDUCE 4
 #define TT_STAGE_MEGAKERNEL 5
+#define TT_STAGE_CACHE 6   /* radiance-cache queries of paths ending in the cache */
 #define TT_STAGE_COUNT 8
 typedef struct tt_stage_timings {
     uint64_t ns[TT_STAGE_COUNT];
@@ -306,6 +309,13 @@ int32_t tt_cache_query(tt_context* ctx, const float* queries, uint32_t n, float*
 int32_t tt_cache_train(tt_context* ctx, const float* queries, const float* targets, uint32_t n, float* loss);
 /* FP32 parameters: grid (TT_CACHE_GRID_FLOATS, may be null) and weights (TT_CACHE_WEIGHTS). */
 int32_t tt_cache_parameters(tt_context* ctx, float* grid, float* weights);
+typedef struct tt_cache_status {
+    uint64_t steps;      /* Adam steps taken */
+    uint64_t pairs;      /* training pairs built from the last cached frame */
+    float last_loss;     /* mean relative L2 loss of the last step */
+    float pad;
+} tt_cache_status;
+int32_t tt_cache_status_get(tt_context* ctx, tt_cache_status* out);
 
 /* ---------------------------------------------------------------- serving
  * Continuous-batching render server (no reference counterpart: the reference renders one frame

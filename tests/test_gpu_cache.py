@@ -113,3 +113,58 @@ def test_learns_a_smooth_field(gpu_context):
     q = _queries(rng, 4096)
     err = np.abs(_query(ctx, q) - _field(q)).mean() / np.abs(_field(q)).mean()
     assert err < 0.1, err
+
+
+def _cache_renderer(extent=(96, 54), spp=8, depth=6, terminate=2):
+    from tinytrace_gb300 import scenes
+    from tinytrace_gb300.renderer import Config, Renderer
+
+    w = scenes.Workload("field_small", scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11),
+                        scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)), extent,
+                        Config(bounce_count=depth, sample_count=spp))
+    r = Renderer(w.extent)
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    r.set_config(w.config)
+    cfg = native.CacheConfig(1e-2, 4096, terminate, 1)
+    check(r.context.lib.tt_cache_configure(r.context.handle, ctypes.byref(cfg)))
+    return r, w
+
+
+def test_cache_plumbing_leaves_the_estimator_alone(gpu_context):
+    """With the cache vertex beyond the last bounce no path ends in the cache, so the image is
+    the plain path tracer's bit for bit (training paths only record their vertices)."""
+    from conftest import assert_same_bits
+    from oracle import oracle
+    from tinytrace_gb300.renderer import make_constants
+
+    r, w = _cache_renderer(terminate=6)
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_RADIANCE_CACHE, 1))
+    c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
+    img = r.render_to_texture()
+    assert_same_bits(img, oracle.OracleScene(r.scene_arrays).render(c), "cache beyond the last bounce")
+    st = native.CacheStatus()
+    check(r.context.lib.tt_cache_status_get(r.context.handle, ctypes.byref(st)))
+    assert st.pairs > 0 and st.steps >= 1
+    r.close()
+
+
+def test_cached_render_trains_and_stays_close(gpu_context):
+    """Paths ending in the cache at the third vertex: after online training the frame mean is
+    within 15 % of the plain path tracer's and the training loss has dropped."""
+    r, w = _cache_renderer(spp=16)
+    plain = r.render_to_texture()
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_RADIANCE_CACHE, 1))
+    losses = []
+    for f in range(24):
+        r.reset_accumulation()
+        img = r.render_to_texture()
+        st = native.CacheStatus()
+        check(r.context.lib.tt_cache_status_get(r.context.handle, ctypes.byref(st)))
+        losses.append(st.last_loss)
+        r.present()
+    assert np.isfinite(img).all() and st.pairs > 1000
+    assert np.mean(losses[-4:]) < np.mean(losses[:4])
+    a, b = img[..., :3].mean(), plain[..., :3].mean()
+    assert abs(a - b) <= 0.15 * b, (a, b)
+    r.close()

@@ -99,9 +99,15 @@ struct RestirState {
     tt_restir_config config{32u, 20.0f, 5u, 30.0f};
 };
 
-// Learned radiance cache: device parameters and the configuration.
+// Learned radiance cache: device parameters, the configuration and the integrator's buffers
+// (queued queries, training records and pairs).
 struct CacheState {
     DeviceBuffer grid, grid_m, grid_v, grid_grad, w, w_m, w_v, w_grad, w16, loss;
+    DeviceBuffer cq, cq_slot, cq_out, rec, train_final, tq, tt, tcount;
+    uint64_t cq_cap = 0, rec_cap = 0, final_cap = 0;
+    bool enabled = false;
+    float last_loss = 0.0f;
+    uint32_t last_pairs = 0;
     tt_cache_config config{1e-2f, 65536u, 2u, 1u};
     uint32_t step = 0;
     bool ready = false;
@@ -419,6 +425,86 @@ DevScene scene_view(tt_context* ctx, tt_handle scene) {
 int context_device(tt_context* ctx) { return ctx->device; }
 }  // namespace tt
 
+static void cache_ready(tt_context* ctx) {
+    CacheState& C = ctx->cache;
+    if (C.ready) return;
+    C.grid.alloc(4 * CACHE_GRID_PARAMS);
+    C.grid_m.alloc(4 * CACHE_GRID_PARAMS);
+    C.grid_v.alloc(4 * CACHE_GRID_PARAMS);
+    C.grid_grad.alloc(4 * CACHE_GRID_PARAMS);
+    C.w.alloc(4 * CACHE_PARAMS);
+    C.w_m.alloc(4 * CACHE_PARAMS);
+    C.w_v.alloc(4 * CACHE_PARAMS);
+    C.w_grad.alloc(4 * CACHE_PARAMS);
+    C.w16.alloc(2 * CACHE_PARAMS);
+    C.loss.alloc(16);
+    cache_set_level_scales();
+    cache_init(C.dev(), C.config.seed, ctx->stream);
+    C.step = 0;
+    C.ready = true;
+}
+
+// Radiance-cache buffers of one frame: queued queries (one per path slot), training records
+// (train_paths_per_frame paths x (bounce_count + 1) vertices) and the pairs built from them.
+static void cache_frame_buffers(tt_context* ctx, const tt_constants& c, const DevScene& sc, WfParams& w) {
+    cache_ready(ctx);
+    CacheState& C = ctx->cache;
+    if (w.P > C.cq_cap) {
+        C.cq.alloc(48ull * w.P);
+        C.cq_slot.alloc(4ull * w.P);
+        C.cq_out.alloc(12ull * w.P);
+        C.cq_cap = w.P;
+    }
+    uint64_t items = (uint64_t)c.screen_size[0] * c.screen_size[1] * c.sample_count;
+    uint32_t paths = std::max<uint32_t>(C.config.train_paths_per_frame, 1u);
+    uint64_t stride = std::max<uint64_t>(items / paths, 1);
+    require(stride <= 0xffffffffull, "too many samples per training path");
+    uint64_t final_n = items / stride + 1;
+    uint64_t rec_n = final_n * (c.bounce_count + 1ull);
+    if (final_n > C.final_cap) {
+        C.train_final.alloc(16ull * final_n);
+        C.final_cap = final_n;
+    }
+    if (rec_n > C.rec_cap) {
+        C.rec.alloc(sizeof(TrainRecord) * rec_n);
+        C.tq.alloc(48ull * rec_n);
+        C.tt.alloc(12ull * rec_n);
+        C.rec_cap = rec_n;
+    }
+    if (!C.tcount.ptr) C.tcount.alloc(16);
+    w.cache_on = 1u;
+    w.cache_depth = C.config.terminate_depth;
+    w.train_stride = (uint32_t)stride;
+    w.rec_cap = (uint32_t)std::min<uint64_t>(C.rec_cap, 0xffffffffull);
+    w.cache_bound = sc.tlas_bound > 0.0f ? sc.tlas_bound : 1.0f;
+    w.cq = C.cq.as<CacheQuery>();
+    w.cq_slot = C.cq_slot.as<uint32_t>();
+    w.cq_out = C.cq_out.as<float>();
+    w.rec = C.rec.as<TrainRecord>();
+    w.train_final = C.train_final.as<float4>();
+    w.cache_grid = C.grid.as<float>();
+    w.cache_w16 = C.w16.as<__half>();
+}
+
+// After a cached frame: training pairs from the frame's training paths, then up to four Adam
+// steps of at most 16,384 pairs each.
+static void cache_train_after_frame(tt_context* ctx, const WfParams& w) {
+    CacheState& C = ctx->cache;
+    cudaStream_t st = ctx->stream;
+    cache_targets(w.rec, w.counters + CTRL_RECORDS, w.rec_cap, w.train_final, C.tq.as<CacheQuery>(), C.tt.as<float>(),
+                  C.tcount.as<uint32_t>(), st);
+    uint32_t pairs = 0;
+    check_cuda(cudaMemcpyAsync(&pairs, C.tcount.ptr, 4, cudaMemcpyDeviceToHost, st), "pairs");
+    check_cuda(cudaStreamSynchronize(st), "sync");
+    C.last_pairs = pairs;
+    constexpr uint32_t BATCH = 16384;
+    for (uint32_t k = 0; k < 4 && k * BATCH < pairs; ++k) {
+        uint32_t n = std::min(BATCH, pairs - k * BATCH);
+        cache_train_step(C.dev(), C.tq.as<CacheQuery>() + (uint64_t)k * BATCH, C.tt.as<float>() + 3ull * k * BATCH, n,
+                         C.config.learning_rate, ++C.step, st);
+    }
+}
+
 static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c, tt_handle target, bool counted,
                         tt_traversal_counters* out) {
     require(ctx && c, "null argument");
@@ -438,6 +524,8 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     bool wavefront = ctx->integrator == TT_INTEGRATOR_WAVEFRONT && c->sample_count > 0 && c->bounce_count > 0;
     WfParams w{};
     if (wavefront) w = wavefront_buffers(ctx, *c);
+    bool cached = wavefront && ctx->cache.enabled && !counted;
+    if (cached) cache_frame_buffers(ctx, *c, s->dev, w);
     StageTimer* timer = nullptr;
     if (ctx->stage_timing) {
         if (ctx->stage_events.empty()) {
@@ -467,6 +555,7 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
     ctx->integrate_timed = true;
     fetch_error_word(ctx);
+    if (cached) cache_train_after_frame(ctx, w);
     if (counted) {
         unsigned long long h[8];
         check_cuda(cudaMemcpyAsync(h, ctx->counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "copy");
@@ -852,6 +941,9 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else if (option == TT_OPTION_TRACE_BLOCKS_PER_SM) {
             require(value <= 64, "trace blocks per SM above 64");
             ctx->trace_blocks_per_sm = (uint32_t)value;
+        } else if (option == TT_OPTION_RADIANCE_CACHE) {
+            require(value <= 1, "radiance cache is 0 or 1");
+            ctx->cache.enabled = value != 0;
         } else if (option == TT_OPTION_GRAPHS) {
             require(value <= 1, "graphs is 0 or 1");
             ctx->graphs = value != 0;
@@ -1009,24 +1101,6 @@ int32_t tt_restir_download(tt_context* ctx, void* reservoirs, uint64_t bytes) {
     });
 }
 
-static void cache_ready(tt_context* ctx) {
-    CacheState& C = ctx->cache;
-    if (C.ready) return;
-    C.grid.alloc(4 * CACHE_GRID_PARAMS);
-    C.grid_m.alloc(4 * CACHE_GRID_PARAMS);
-    C.grid_v.alloc(4 * CACHE_GRID_PARAMS);
-    C.grid_grad.alloc(4 * CACHE_GRID_PARAMS);
-    C.w.alloc(4 * CACHE_PARAMS);
-    C.w_m.alloc(4 * CACHE_PARAMS);
-    C.w_v.alloc(4 * CACHE_PARAMS);
-    C.w_grad.alloc(4 * CACHE_PARAMS);
-    C.w16.alloc(2 * CACHE_PARAMS);
-    C.loss.alloc(16);
-    cache_set_level_scales();
-    cache_init(C.dev(), C.config.seed, ctx->stream);
-    C.step = 0;
-    C.ready = true;
-}
 
 int32_t tt_cache_configure(tt_context* ctx, const tt_cache_config* config) {
     return guarded([&] {
@@ -1066,6 +1140,24 @@ int32_t tt_cache_train(tt_context* ctx, const float* queries, const float* targe
                              C.config.learning_rate, step, ctx->stream);
         });
         if (loss) check_cuda(cudaMemcpy(loss, C.loss.ptr, 4, cudaMemcpyDeviceToHost), "loss");
+    });
+}
+
+int32_t tt_cache_status_get(tt_context* ctx, tt_cache_status* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        use_device(ctx);
+        sync(ctx);
+        CacheState& C = ctx->cache;
+        *out = tt_cache_status{};
+        out->steps = C.step;
+        out->pairs = C.last_pairs;
+        if (C.ready && C.step > 0) {
+            float sum = 0.0f;
+            check_cuda(cudaMemcpy(&sum, C.loss.ptr, 4, cudaMemcpyDeviceToHost), "loss");
+            uint32_t n = std::min<uint32_t>(16384u, std::max<uint32_t>(C.last_pairs, 1u));
+            out->last_loss = sum / (3.0f * (float)n);
+        }
     });
 }
 

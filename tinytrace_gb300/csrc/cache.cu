@@ -27,6 +27,7 @@
 
 #include "tt_cache.cuh"
 #include "tt_internal.h"
+#include "tt_kernels.h"
 
 namespace tt {
 
@@ -104,8 +105,9 @@ constexpr int INF_WARPS = 4;
 // out[i] = MLP(encode(q[i])) for n queries; the FP16 weights (CACHE_PARAMS halves) are copied
 // to shared memory once per block.
 __global__ void __launch_bounds__(INF_WARPS * 32) cache_infer_kernel(const CacheQuery* q, uint32_t n,
-                                                                     const float* grid, const __half* w16,
-                                                                     float* out) {
+                                                                     const uint32_t* count, const float* grid,
+                                                                     const __half* w16, float* out) {
+    if (count) n = min(n, *count);  // queue length written by an earlier kernel
     __shared__ __align__(16) __half s_w[CACHE_PARAMS];
     __shared__ __align__(16) __half s_x[INF_WARPS][16][CACHE_WIDTH + 8];  // +8: spread smem banks
     for (uint32_t k = threadIdx.x; k < CACHE_PARAMS / 8; k += blockDim.x)
@@ -346,7 +348,45 @@ void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* o
     if (n == 0) return;
     uint32_t tiles = (n + 15u) / 16u;
     uint32_t blocks = std::min<uint32_t>((tiles + INF_WARPS - 1) / INF_WARPS, 152u * 8u);
-    cache_infer_kernel<<<blocks, INF_WARPS * 32, 0, st>>>(q, n, d.grid, d.w16, out);
+    cache_infer_kernel<<<blocks, INF_WARPS * 32, 0, st>>>(q, n, nullptr, d.grid, d.w16, out);
+}
+
+void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,
+                       uint32_t max_n, float* out, cudaStream_t st) {
+    if (max_n == 0) return;
+    uint32_t tiles = (max_n + 15u) / 16u;
+    uint32_t blocks = std::min<uint32_t>((tiles + INF_WARPS - 1) / INF_WARPS, 152u * 8u);
+    cache_infer_kernel<<<blocks, INF_WARPS * 32, 0, st>>>(q, max_n, count, grid, w16, out);
+}
+
+// Training pairs of the frame's records: target = (final - before) / throughput, kept when the
+// throughput is above 1e-6 in every channel and the target is finite; order not preserved.
+__global__ void cache_targets_kernel(const TrainRecord* rec, const uint32_t* rec_count, uint32_t cap,
+                                     const float4* final_radiance, CacheQuery* q, float* t, uint32_t* count) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = min(*rec_count, cap);
+    if (i >= n) return;
+    const TrainRecord& r = rec[i];
+    float4 f = final_radiance[r.path];
+    float fin[3] = {f.x, f.y, f.z};
+    float tg[3];
+    bool ok = true;
+    for (int c = 0; c < 3; ++c) {
+        ok = ok && r.thr[c] > 1e-6f;
+        tg[c] = (fin[c] - r.before[c]) / r.thr[c];
+        ok = ok && isfinite(tg[c]);
+    }
+    if (!ok) return;
+    uint32_t k = atomicAdd(count, 1u);
+    for (int c = 0; c < 12; ++c) reinterpret_cast<float*>(q + k)[c] = r.q[c];
+    for (int c = 0; c < 3; ++c) t[3ull * k + c] = fmaxf(tg[c], 0.0f);
+}
+
+void cache_targets(const TrainRecord* rec, const uint32_t* rec_count, uint32_t cap, const float4* final_radiance,
+                   CacheQuery* q, float* t, uint32_t* count, cudaStream_t st) {
+    check_cuda(cudaMemsetAsync(count, 0, 4, st), "memset");
+    if (cap == 0) return;
+    cache_targets_kernel<<<(cap + 255) / 256, 256, 0, st>>>(rec, rec_count, cap, final_radiance, q, t, count);
 }
 
 void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,

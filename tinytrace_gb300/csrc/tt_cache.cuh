@@ -39,6 +39,12 @@ void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* o
 void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
                       uint32_t step, cudaStream_t st);
 void cache_init(const CacheDevice& d, uint32_t seed, cudaStream_t st);
+// Queries whose count is in device memory (at most max_n of them).
+void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,
+                       uint32_t max_n, float* out, cudaStream_t st);
+struct TrainRecord;
+void cache_targets(const TrainRecord* rec, const uint32_t* rec_count, uint32_t cap, const float4* final_radiance,
+                   CacheQuery* q, float* t, uint32_t* count, cudaStream_t st);
 void cache_set_level_scales();
 
 }  // namespace tt

@@ -1,6 +1,7 @@
 // Kernel launch interface between the C ABI (api.cu) and the device code (integrate.cu).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/tinytrace_cuda.h"
@@ -18,9 +19,23 @@ struct RenderParams {
 
 // Wavefront integrator (wavefront.cu): device pointers of the slot pool and queues.
 constexpr uint32_t HIT_BUCKETS = 4;                // shading queues, one per material bucket
-constexpr uint32_t WF_COUNTERS = 5 + HIT_BUCKETS;  // queue words of WfParams::counters
+constexpr uint32_t CACHE_QUEUE = 5 + HIT_BUCKETS;  // counters word: queued radiance-cache queries
+constexpr uint32_t WF_COUNTERS = 6 + HIT_BUCKETS;  // words cleared every iteration: [1, WF_COUNTERS)
+constexpr uint32_t CTRL_RECORDS = 14;              // training records of the frame (cleared per frame)
 constexpr uint32_t CTRL_ITERATION = 15;            // iteration count of the device-side loop
 constexpr uint32_t CTRL_WORDS = 16;                // words of WfParams::counters
+constexpr uint32_t CHUNK_WORDS = 14;               // words cleared per sample chunk: [0, CHUNK_WORDS)
+
+struct CacheQuery;
+// A vertex of a training path: its query, the throughput arriving at it and the path radiance
+// before its contributions (the training target is (final - before) / throughput).
+struct TrainRecord {
+    float q[12];
+    float thr[3];
+    float before[3];
+    uint32_t path;  // training path id (global work item / stride)
+    uint32_t pad;
+};
 struct WfParams {
     float4 *org, *dir, *thr, *acc, *pa1, *pa0, *pe;
     uint4* hit;          // shading queues: hit records, HIT_BUCKETS x P
@@ -35,6 +50,16 @@ struct WfParams {
     uint32_t chunk_sample0, chunk_spp, chunk_items;
     uint32_t refill;        // a trace warp refills its idle lanes when fewer than this many hold a ray
     uint32_t trace_blocks;  // grid of the persistent trace kernel (host side)
+    // learned radiance cache (cache_on = 0: off)
+    uint32_t cache_on, cache_depth, train_stride, rec_cap;
+    float cache_bound;      // positions map to the unit cube as p / bound * 0.5 + 0.5
+    CacheQuery* cq;         // queued queries (P)
+    uint32_t* cq_slot;      // their slots
+    float* cq_out;          // their radiance (3 P)
+    TrainRecord* rec;       // training records of the frame (rec_cap)
+    float4* train_final;    // final radiance of each training path
+    const float* cache_grid;
+    const __half* cache_w16;
 };
 // SM count and resident blocks per SM of the persistent trace kernel.
 void trace_occupancy(int* sms, int* blocks_per_sm);

@@ -25,13 +25,16 @@
 
 #include <algorithm>
 
+#include "tt_cache.cuh"
 #include "tt_internal.h"
 #include "tt_kernels.h"
 #include "tt_shade.cuh"
 
 namespace tt {
 
-constexpr uint32_t F_LIVE = 1u, F_TERM = 2u;
+// Path flags (acc.w): live, terminated (radiance ready), training path of the radiance cache,
+// waiting for its radiance-cache query.
+constexpr uint32_t F_LIVE = 1u, F_TERM = 2u, F_TRAIN = 4u, F_CACHE = 8u;
 constexpr uint32_t NO_HIT = 0xffffffffu;
 constexpr int WF_BLOCK = 128;
 
@@ -102,6 +105,8 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
     if (valid && (flags & F_TERM)) {
         uint32_t item = __float_as_uint(w.thr[s].w);
         w.samples[item] = make_float4(a.x, a.y, a.z, 0.0f);
+        if (flags & F_TRAIN)
+            w.train_final[((uint64_t)w.chunk_sample0 * w.WH + item) / w.train_stride] = make_float4(a.x, a.y, a.z, 0.0f);
         flags = 0u;
         w.acc[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
@@ -122,7 +127,8 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
         w.org[s] = make_float4(c.camera_position[0], c.camera_position[1], c.camera_position[2], __uint_as_float(0u));
         w.dir[s] = pack(d, pg);
         w.thr[s] = pack(splat(1.0f), item);
-        w.acc[s] = pack(splat(0.0f), F_LIVE);
+        bool train = w.cache_on && ((uint64_t)w.chunk_sample0 * w.WH + item) % w.train_stride == 0u;
+        w.acc[s] = pack(splat(0.0f), F_LIVE | (train ? F_TRAIN : 0u));
         live = true;
     }
     uint32_t q = block_append<REGEN_BLOCK>(&w.counters[1], live, s_warp);
@@ -231,9 +237,10 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                     if (COUNT) hits++;
                 } else if (fin) {
                     f3 thr = xyz(w.thr[slot]);
-                    f3 acc = xyz(w.acc[slot]);
+                    float4 a4 = w.acc[slot];
+                    f3 acc = xyz(a4);
                     acc += splat(1.0f) * thr;
-                    w.acc[slot] = pack(acc, F_TERM);
+                    w.acc[slot] = pack(acc, F_TERM | (__float_as_uint(a4.w) & F_TRAIN));
                 }
             }
             uint32_t am = __ballot_sync(0xffffffffu, active);
@@ -259,6 +266,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
 #ifndef TT_SHADE_MIN_BLOCKS
 #define TT_SHADE_MIN_BLOCKS 6
 #endif
+template <bool CACHE>
 __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel(const __grid_constant__ RenderParams p,
                                                             const __grid_constant__ WfParams w) {
     // thread q shades entry q of the bucket queues laid end to end
@@ -274,9 +282,12 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
         have = have || in;
         start += cnt;
     }
-    bool want_shadow = false;
+    bool want_shadow = false, want_cache = false, want_record = false;
     uint32_t s = 0, light = 0;
     f3 sh_org = splat(0.0f), sh_dir = splat(0.0f);
+    float qv[12];          // radiance-cache query of this vertex (cache or training record)
+    f3 rec_thr = splat(0.0f), rec_before = splat(0.0f);
+    uint32_t rec_path = 0;
     if (have) {
         const tt_constants& c = p.c;
         const DevScene& sc = p.sc;
@@ -285,11 +296,35 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
         float4 o4 = w.org[s], d4 = w.dir[s], t4 = w.thr[s], a4 = w.acc[s];
         f3 thr = xyz(t4), acc = xyz(a4), ray_dir = xyz(d4);
         uint32_t g = __float_as_uint(d4.w), bounce = __float_as_uint(o4.w);
+        uint32_t train = __float_as_uint(a4.w) & F_TRAIN;
+        ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
+        const tt_material* material = sc.materials + hit.material_index;
+        const MatC& mc = material->constants;
+        Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
         {
-            ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
-            const tt_material* material = sc.materials + hit.material_index;
-            const MatC& mc = material->constants;
-            Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
+            if (CACHE) {
+                float ib = 0.5f / w.cache_bound;
+                qv[0] = hit.world_position.x * ib + 0.5f;
+                qv[1] = hit.world_position.y * ib + 0.5f;
+                qv[2] = hit.world_position.z * ib + 0.5f;
+                qv[3] = -ray_dir.x;
+                qv[4] = -ray_dir.y;
+                qv[5] = -ray_dir.z;
+                qv[6] = basis.normal.x;
+                qv[7] = basis.normal.y;
+                qv[8] = basis.normal.z;
+                qv[9] = mc.specular_roughness;
+                qv[10] = qv[11] = 0.0f;
+                want_cache = !train && bounce == w.cache_depth;
+                want_record = train != 0u;
+                rec_thr = thr;
+                rec_before = acc;
+                rec_path = (uint32_t)(((uint64_t)w.chunk_sample0 * w.WH + __float_as_uint(t4.w)) / w.train_stride);
+            }
+        }
+        if (want_cache) {  // the path ends in the cache: its radiance comes from the query
+            w.acc[s] = pack(acc, F_CACHE);
+        } else {
             f3 wi = transform_from_basis(basis, -ray_dir);
             Lobes lobes = bsdf_prepare(mc, wi, g);
             bool nee = c.light_sampling == LIGHT_SAMPLING_NEE && sc.emissive_count > 0 && mc.specular_roughness > 0.15f;
@@ -327,7 +362,7 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
             f3 new_dir = transform_to_basis(basis, wo);
             thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
             uint32_t next = bounce + 1u;
-            uint32_t flags = next == c.bounce_count ? F_TERM : F_LIVE;
+            uint32_t flags = (next == c.bounce_count ? F_TERM : F_LIVE) | train;
             w.org[s] = pack(hit.world_position, next);
             w.dir[s] = pack(new_dir, g);
             w.thr[s] = pack(thr, __float_as_uint(t4.w));
@@ -340,6 +375,35 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
         w.shadow[2ull * e] = pack(sh_org, s);
         w.shadow[2ull * e + 1] = pack(sh_dir, light);
     }
+    if (CACHE) {
+        uint32_t cq = block_append<WF_BLOCK>(&w.counters[CACHE_QUEUE], want_cache, s_warp);
+        if (want_cache) {
+            float4* dst = reinterpret_cast<float4*>(w.cq) + 3ull * cq;
+            dst[0] = make_float4(qv[0], qv[1], qv[2], qv[3]);
+            dst[1] = make_float4(qv[4], qv[5], qv[6], qv[7]);
+            dst[2] = make_float4(qv[8], qv[9], qv[10], qv[11]);
+            w.cq_slot[cq] = s;
+        }
+        uint32_t r = block_append<WF_BLOCK>(&w.counters[CTRL_RECORDS], want_record, s_warp);
+        if (want_record && r < w.rec_cap) {
+            float4* dst = reinterpret_cast<float4*>(w.rec + r);
+            dst[0] = make_float4(qv[0], qv[1], qv[2], qv[3]);
+            dst[1] = make_float4(qv[4], qv[5], qv[6], qv[7]);
+            dst[2] = make_float4(qv[8], qv[9], qv[10], qv[11]);
+            dst[3] = make_float4(rec_thr.x, rec_thr.y, rec_thr.z, rec_before.x);
+            dst[4] = make_float4(rec_before.y, rec_before.z, __uint_as_float(rec_path), 0.0f);
+        }
+    }
+}
+
+// Radiance-cache results of this iteration's queued paths: acc += throughput * max(L, 0).
+__global__ void wf_cache_apply_kernel(const __grid_constant__ WfParams w) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.counters[CACHE_QUEUE]) return;
+    uint32_t s = w.cq_slot[i];
+    f3 L = f3{fmaxf(w.cq_out[3ull * i], 0.0f), fmaxf(w.cq_out[3ull * i + 1], 0.0f), fmaxf(w.cq_out[3ull * i + 2], 0.0f)};
+    f3 acc = xyz(w.acc[s]) + xyz(w.thr[s]) * L;
+    w.acc[s] = pack(acc, F_TERM);
 }
 
 // Per pixel: samples of this chunk added in sample order to the running sum; after the last
@@ -411,11 +475,13 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
     check_cuda(cudaGraphCreate(&g, 0), "cudaGraphCreate");
     check_cuda(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "capture");
     check_cuda(cudaMemsetAsync(w.acc, 0, 16ull * w.P, cs), "memset");  // every slot starts free
+    check_cuda(cudaMemsetAsync(w.counters + CTRL_RECORDS, 0, 4, cs), "memset");
     for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
         w.chunk_sample0 = s0;
         w.chunk_spp = std::min(max_chunk, spp - s0);
         w.chunk_items = WH * w.chunk_spp;
-        check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CTRL_WORDS, cs), "memset");
+        check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CHUNK_WORDS, cs), "memset");
+        check_cuda(cudaMemsetAsync(w.counters + CTRL_ITERATION, 0, 4, cs), "memset");
         // while (paths are live) { regen; extend; shade; shadow }
         cudaStreamCaptureStatus status;
         cudaGraph_t cg = nullptr;
@@ -440,8 +506,13 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
         wf_regen_kernel<<<regen_grid, REGEN_BLOCK, 0, body_stream>>>(p, w);
         wf_control_kernel<<<1, 1, 0, body_stream>>>(w.counters, handle, limit, p.err);
         launch_trace<false>(p, w, tgrid, counted, body_stream);
-        wf_shade_kernel<<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w);
+        if (w.cache_on) wf_shade_kernel<true><<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w);
+        else wf_shade_kernel<false><<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w);
         launch_trace<true>(p, w, tgrid, counted, body_stream);
+        if (w.cache_on) {
+            cache_infer_queue(w.cache_grid, w.cache_w16, w.cq, w.counters + CACHE_QUEUE, w.P, w.cq_out, body_stream);
+            wf_cache_apply_kernel<<<(w.P + 255) / 256, 256, 0, body_stream>>>(w);
+        }
         check_cuda(cudaStreamEndCapture(body_stream, &body), "body capture end");
         check_cuda(cudaStreamUpdateCaptureDependencies(cs, &loop, nullptr, 1, cudaStreamSetCaptureDependencies),
                    "capture dependencies");
@@ -467,11 +538,12 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
     unsigned regen_grid = (w.P + REGEN_BLOCK - 1) / REGEN_BLOCK;
     unsigned trace_blocks = w.trace_blocks;
     check_cuda(cudaMemsetAsync(w.acc, 0, 16ull * w.P, st), "memset");  // every slot starts free
+    check_cuda(cudaMemsetAsync(w.counters + CTRL_RECORDS, 0, 4, st), "memset");
     for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
         w.chunk_sample0 = s0;
         w.chunk_spp = std::min(max_chunk, spp - s0);
         w.chunk_items = WH * w.chunk_spp;
-        check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * WF_COUNTERS, st), "memset");
+        check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CHUNK_WORDS, st), "memset");
         while (true) {
             check_cuda(cudaMemsetAsync(w.counters + 1, 0, 4ull * (WF_COUNTERS - 1), st), "memset");
             stage_begin(timer, TT_STAGE_REGEN, st);
@@ -487,11 +559,18 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
             launch_trace<false>(p, w, tgrid, counted, st);
             stage_end(timer, st);
             stage_begin(timer, TT_STAGE_SHADE, st);
-            wf_shade_kernel<<<grid, WF_BLOCK, 0, st>>>(p, w);
+            if (w.cache_on) wf_shade_kernel<true><<<grid, WF_BLOCK, 0, st>>>(p, w);
+            else wf_shade_kernel<false><<<grid, WF_BLOCK, 0, st>>>(p, w);
             stage_end(timer, st);
             stage_begin(timer, TT_STAGE_SHADOW, st);
             launch_trace<true>(p, w, tgrid, counted, st);
             stage_end(timer, st);
+            if (w.cache_on) {
+                stage_begin(timer, TT_STAGE_CACHE, st);
+                cache_infer_queue(w.cache_grid, w.cache_w16, w.cq, w.counters + CACHE_QUEUE, n, w.cq_out, st);
+                wf_cache_apply_kernel<<<grid, WF_BLOCK, 0, st>>>(w);
+                stage_end(timer, st);
+            }
         }
         stage_begin(timer, TT_STAGE_REDUCE, st);
         wf_reduce_kernel<<<(WH + 255) / 256, 256, 0, st>>>(p, w, s0 + w.chunk_spp >= spp ? 1 : 0);

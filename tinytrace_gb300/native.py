@@ -51,6 +51,8 @@ TT_REQUEST_QUEUED = 0
 TT_REQUEST_RUNNING = 1
 TT_REQUEST_DONE = 2
 TT_REQUEST_FAILED = 3
+TT_OPTION_RADIANCE_CACHE = 8
+TT_STAGE_CACHE = 6
 TT_CACHE_WEIGHTS = 16896
 TT_CACHE_GRID_FLOATS = 16777216
 TT_OPTION_REFILL_LANES = 6
@@ -62,7 +64,7 @@ TT_STAGE_SHADOW = 3
 TT_STAGE_REDUCE = 4
 TT_STAGE_MEGAKERNEL = 5
 TT_STAGE_COUNT = 8
-STAGE_NAMES = ("regen", "extend", "shade", "shadow", "reduce", "megakernel")
+STAGE_NAMES = ("regen", "extend", "shade", "shadow", "reduce", "megakernel", "cache")
 
 # ---------------------------------------------------------------- byte layouts (numpy)
 MATERIAL_CONSTANT_FIELDS = [
@@ -171,6 +173,11 @@ class CacheConfig(ctypes.Structure):
                 ("terminate_depth", ctypes.c_uint32), ("seed", ctypes.c_uint32)]
 
 
+class CacheStatus(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint64), ("pairs", ctypes.c_uint64), ("last_loss", ctypes.c_float),
+                ("pad", ctypes.c_float)]
+
+
 class TuneResult(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_uint32), ("refill_lanes", ctypes.c_uint32), ("trace_blocks_per_sm", ctypes.c_uint32),
                 ("renders", ctypes.c_uint32), ("default_ms", ctypes.c_float), ("best_ms", ctypes.c_float)]
@@ -223,6 +230,7 @@ SIGNATURES = {
     "tt_cache_query": (_I32, [_P, _P, _U32, _P]),
     "tt_cache_train": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_cache_parameters": (_I32, [_P, _P, _P]),
+    "tt_cache_status_get": (_I32, [_P, ctypes.POINTER(CacheStatus)]),
     "tt_restir_configure": (_I32, [_P, ctypes.POINTER(RestirConfig)]),
     "tt_restir_reset": (_I32, [_P]),
     "tt_render_restir": (_I32, [_P, _U64, _P, _U64]),
