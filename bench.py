@@ -58,6 +58,7 @@ def parse_args():
     p.add_argument("--no-autotune", action="store_true", help="skip tt_autotune before the warm-up")
     p.add_argument("--no-serve", action="store_true", help="skip the serving sample")
     p.add_argument("--no-restir", action="store_true", help="skip the ReSTIR DI sample")
+    p.add_argument("--no-cache", action="store_true", help="skip the radiance-cache sample")
     p.add_argument("--serve-rates", default="2,8,32", help="Poisson arrival rates (requests/s) of the serving sample")
     p.add_argument("--serve-requests", type=int, default=12, help="requests per arrival rate")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level"],
@@ -300,6 +301,66 @@ def run_restir(a, device: int) -> dict:
             "image_finite": bool(np.isfinite(img).all())}
 
 
+# ---------------------------------------------------------------- radiance-cache sample
+def run_cache(a, device: int) -> dict:
+    """Equal-RMSE comparison of the learned radiance cache with the plain path tracer on the
+    benchmark frame (1M triangles, 1920x1080, depth 8): the reference is a 1024-spp plain
+    render; plain and cached frames at S spp are timed by CUDA events around the whole render
+    call (for the cache: queries, training-pair building and the Adam steps after the frame)
+    and compared by RMSE; efficiency = 1 / (time x MSE), and the ratio cached / plain is the
+    speed-up at equal RMSE.  The cache trains online for 32 frames before it is measured."""
+    import ctypes
+
+    from tinytrace_gb300 import native
+    from tinytrace_gb300.native import check
+    from tinytrace_gb300.renderer import Config, Renderer
+
+    w = make_workload(a)
+    W, H = w.extent
+    r = Renderer((W, H), device=device)
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    lib, ctx = r.context.lib, r.context.handle
+
+    def frame(spp, timed=True):
+        r.set_config(Config(bounce_count=w.config.bounce_count, sample_count=spp))
+        r.reset_accumulation()
+        check(lib.tt_synchronize(ctx))
+        check(lib.tt_event_record(ctx, 4))
+        r.render_to_target()
+        check(lib.tt_event_record(ctx, 5))
+        ms = ctypes.c_float()
+        check(lib.tt_event_elapsed_ms(ctx, 4, 5, ctypes.byref(ms)))
+        img = r.context.download(r.render_target, W, H)[..., :3].astype(np.float64)
+        r.present()
+        return img, ms.value
+
+    ref, ref_ms = frame(1024)
+    out = {"reference_spp": 1024, "reference_ms": ref_ms, "terminate_depth": 2, "train_paths_per_frame": 65536,
+           "warmup_frames": 32, "results": []}
+    plain = {}
+    for spp in (4, 16):
+        img, ms = frame(spp)
+        plain[spp] = (ms, float(np.mean((img - ref) ** 2)))
+    cfg = native.CacheConfig(1e-2, 65536, 2, 1)
+    check(lib.tt_cache_configure(ctx, ctypes.byref(cfg)))
+    check(lib.tt_set_option(ctx, native.TT_OPTION_RADIANCE_CACHE, 1))
+    for _ in range(32):
+        frame(16)
+    for spp in (4, 16):
+        img, ms = frame(spp)
+        mse = float(np.mean((img - ref) ** 2))
+        pms, pmse = plain[spp]
+        out["results"].append({"spp": spp, "plain_ms": pms, "plain_rmse": pmse ** 0.5, "cached_ms": ms,
+                               "cached_rmse": mse ** 0.5,
+                               "equal_rmse_speedup": (pms * pmse) / (ms * mse)})
+    st = native.CacheStatus()
+    check(lib.tt_cache_status_get(ctx, ctypes.byref(st)))
+    out["training"] = {"steps": int(st.steps), "pairs_last_frame": int(st.pairs), "last_loss": st.last_loss}
+    r.close()
+    return out
+
+
 # ---------------------------------------------------------------- serving sample
 SERVE_SCENES = [(1, 7), (4, 11), (16, 18), (64, 28), (128, 44)]  # (instances, frequency): 1e3 .. 5e6 triangles
 
@@ -528,6 +589,11 @@ def run_ours(a, dist: Dist):
         t = native.Timings()
         check(lib.tt_timings_get(ctx, ctypes.byref(t)))
         out_line["scene"]["build_ms"] = t.scene_build_ns / 1e6
+        if not a.no_cache and dist.world == 1:
+            try:
+                out_line["radiance_cache"] = run_cache(a, device)
+            except Exception as e:
+                out_line["radiance_cache"] = {"error": f"{type(e).__name__}: {e}"}
         if not a.no_restir and dist.world == 1:
             try:
                 out_line["restir"] = run_restir(a, device)
