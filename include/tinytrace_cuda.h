@@ -232,6 +232,54 @@ int32_t tt_scene_stats_get(tt_context* ctx, tt_handle scene, tt_scene_stats* out
  * The world-space structure (flat BVH or TLAS) keeps its topology and refits its boxes, so
  * closest hits stay exact; traversal slows as instances move far from where it was built. */
 int32_t tt_scene_update_instances(tt_context* ctx, tt_handle scene, const tt_instance* instances, uint32_t count);
+/* ---------------------------------------------------------------- mesh ingest */
+/* One mesh as Scene::insert_mesh receives it (src/asset/mod.rs:20-27 Mesh), FP32 host arrays.
+ * texture_coordinates (vertex_count x 2), indices (index_count), normals (vertex_count x 3)
+ * and tangents (vertex_count x 4) may be NULL: zeros, 0..vertex_count-1, normals generated
+ * from the triangles (src/asset/mod.rs:226-242), tangents generated. */
+typedef struct tt_mesh_data {
+    const float* positions;
+    const float* texture_coordinates;
+    const uint32_t* indices;
+    const float* normals;
+    const float* tangents;
+    uint32_t vertex_count, index_count;
+} tt_mesh_data;
+
+/* replaces: src/asset/mod.rs:89-161 Scene::insert_mesh (host loop) with the per-vertex work on
+ * the device: writes vertex_count snorm16 positions (x, y, z) relative to the bounding sphere
+ * (src/asset/mod.rs:308-321) to `positions`, vertex_count packed vertices (f16 texture
+ * coordinates, TangentFrame of src/asset/normal.rs:17-36) to `vertices`, and the mesh record
+ * with the given offsets to `mesh`.  Generated tangents are cross(up, n) / |.| with w = +1
+ * (up = +y unless |n.y| >= 0.999, then +x) in place of the reference's mikktspace tangents.
+ * TT_ERR_INVALID_ARGUMENT for an index >= vertex_count or a degenerate or non-finite bounding
+ * sphere (the reference panics on both). */
+int32_t tt_mesh_ingest(tt_context* ctx, const tt_mesh_data* mesh, uint32_t vertex_offset, uint32_t index_offset,
+                       int16_t* positions, tt_vertex* vertices, tt_mesh* mesh_out);
+
+/* The scene arrays and the (mesh, instance) pairs of the emissive models, in scene order. */
+typedef struct tt_emissive_source {
+    const int16_t* positions; /* vertex_count x 3 (all meshes) */
+    const tt_vertex* vertices;
+    uint64_t vertex_count;
+    const uint32_t* indices;
+    uint64_t index_count;
+    const tt_mesh* meshes;
+    uint32_t mesh_count;
+    uint32_t model_count;
+    const uint32_t* model_mesh;     /* model_count mesh indices */
+    const uint32_t* model_instance; /* model_count instance indices */
+} tt_emissive_source;
+
+/* replaces: src/asset/mod.rs:163-193 Scene::emissive_triangles_in_model over every emissive
+ * model (src/scene.rs:29-64 collects them): the triangles of the models in order, each with
+ * its quantised positions, texture coordinates, hash (index_offset / 3 + offset % 65535) as
+ * u16 and instance index.  `capacity` triangles fit in `out`; `*count` receives the number
+ * written.  TT_ERR_INVALID_ARGUMENT for a mesh, index or vertex out of range,
+ * TT_ERR_OVERFLOW when `capacity` is too small. */
+int32_t tt_emissive_extract(tt_context* ctx, const tt_emissive_source* source, tt_emissive_triangle* out,
+                            uint64_t capacity, uint64_t* count);
+
 /* BVH arrays for node-for-node comparison: blas nodes (128 B each), triangle records
  * (48 B each), tlas nodes (128 B each; the flat BVH of a flat scene).  Sizes in bytes must
  * match tt_scene_stats. */

@@ -22,6 +22,7 @@
 
 #include "ref_bsdf.h"
 #include "ref_bvh.h"
+#include "ref_ingest.h"
 
 using namespace ref;
 
@@ -781,6 +782,19 @@ void oracle_math(int which, const float* x, uint64_t n, float* y) {
             default: y[i] = 0.0f;
         }
     }
+}
+
+// atan2 of the tangent-frame encoding, for accuracy tests against libm.
+void oracle_atan2(const float* y, const float* x, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) out[i] = tatan2(y[i], x[i]);
+}
+
+// Scene::insert_mesh restated (ref_ingest.h); vertices are 8-byte ProcessedVertex records.
+int oracle_mesh_ingest(const float* positions, const float* uv, const uint32_t* indices, const float* normals,
+                       const float* tangents, uint32_t n, uint32_t m, int16_t* out_positions, void* out_vertices,
+                       float* sphere) {
+    return ref::mesh_ingest(positions, uv, indices, normals, tangents, n, m, out_positions,
+                            static_cast<ref::IngestVertex*>(out_vertices), sphere);
 }
 
 int oracle_abi_version(void) { return 1; }

@@ -49,6 +49,9 @@ def load() -> ctypes.CDLL:
         lib.oracle_restir_destroy.argtypes = [_P]
         lib.oracle_restir_frame.argtypes = [_P, _P, _P, ctypes.c_int]
         lib.oracle_restir_reservoirs.argtypes = [_P, _P]
+        lib.oracle_atan2.argtypes = [_P, _P, ctypes.c_uint64, _P]
+        lib.oracle_mesh_ingest.restype = ctypes.c_int
+        lib.oracle_mesh_ingest.argtypes = [_P, _P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P]
         _lib = lib
     return _lib
 
@@ -180,3 +183,60 @@ def math(which: int, x: np.ndarray) -> np.ndarray:
     y = np.zeros_like(x)
     load().oracle_math(which, _p(x), x.size, _p(y))
     return y
+
+
+def atan2(y: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """tatan2, the atan2 of the tangent-frame encoding."""
+    y = np.ascontiguousarray(y, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(y)
+    load().oracle_atan2(_p(y), _p(x), y.size, _p(out))
+    return out
+
+
+VERTEX_DTYPE = np.dtype([("texture_coordinates", "<f2", (2,)), ("tangent_frame", "<u4")])
+EMISSIVE_DTYPE = np.dtype([("positions", "<i2", (3, 3)), ("hash", "<u2"),
+                           ("texture_coordinates", "<f2", (3, 2)), ("instance_index", "<u4")])
+
+
+def mesh_ingest(positions, texture_coordinates=None, indices=None, normals=None, tangents=None):
+    """Scene::insert_mesh (src/asset/mod.rs:89-161) restated: (snorm16 positions (n, 3),
+    vertices (n,) of VERTEX_DTYPE, (centre x, y, z, radius)); ValueError where the reference
+    panics (index out of range, index count not a multiple of 3, degenerate sphere)."""
+    def arr(a, dtype, width):
+        return None if a is None else np.ascontiguousarray(np.asarray(a, dtype).reshape(-1, width) if width
+                                                            else np.asarray(a, dtype).reshape(-1))
+    p = arr(positions, np.float32, 3)
+    uv, nrm, tan = arr(texture_coordinates, np.float32, 2), arr(normals, np.float32, 3), arr(tangents, np.float32, 4)
+    idx = arr(indices, np.uint32, 0)
+    n = len(p)
+    out_p = np.zeros((n, 3), np.int16)
+    out_v = np.zeros(n, VERTEX_DTYPE)
+    sphere = np.zeros(4, np.float32)
+    rc = load().oracle_mesh_ingest(_p(p), _p(uv), _p(idx), _p(nrm), _p(tan), n, 0 if idx is None else len(idx),
+                                   _p(out_p), _p(out_v), _p(sphere))
+    if rc != 0:
+        raise ValueError("mesh rejected (the reference panics on it)")
+    return out_p, out_v, sphere
+
+
+def emissive_triangles(positions, vertices, indices, meshes, models):
+    """Scene::emissive_triangles_in_model (src/asset/mod.rs:163-193) for the (mesh index,
+    instance index) pairs `models` in order; `meshes` is a structured array with the
+    vertex_offset / index_offset / index_count fields of ProcessedMesh."""
+    positions = np.asarray(positions).reshape(-1, 3)
+    uv = np.asarray(vertices)["texture_coordinates"]
+    indices = np.asarray(indices).reshape(-1)
+    out = []
+    for mesh_index, instance_index in models:
+        me = meshes[mesh_index]
+        vo, io, ic = int(me["vertex_offset"]), int(me["index_offset"]), int(me["index_count"])
+        tri = indices[io:io + ic // 3 * 3].reshape(-1, 3).astype(np.int64) + vo
+        e = np.zeros(len(tri), EMISSIVE_DTYPE)
+        e["positions"] = positions[tri]
+        e["texture_coordinates"] = uv[tri]
+        offset = np.arange(len(tri), dtype=np.int64)
+        e["hash"] = ((io // 3 + offset % 65535) & 0xFFFF).astype(np.uint16)
+        e["instance_index"] = instance_index
+        out.append(e)
+    return np.concatenate(out) if out else np.zeros(0, EMISSIVE_DTYPE)

@@ -234,4 +234,55 @@ inline float tacos(float x) {
     return (PI_1 - 2.0f * asin_small(y)) + PI_2;
 }
 
+// atan(t) for 0 <= t <= 1: two half-angle steps atan(t) = 2 atan(t / (1 + sqrt(1 + t^2)))
+// bring the argument below tan(pi/16), then the Maclaurin series of atan through r^15.
+inline float atan_unit(float t) {
+    float r = t / (1.0f + std::sqrt(std::fmaf(t, t, 1.0f)));
+    r = r / (1.0f + std::sqrt(std::fmaf(r, r, 1.0f)));
+    float z = r * r;
+    float p = std::fmaf(z, -0.0666666666666667f, 0.0769230769230769f);
+    p = std::fmaf(z, p, -0.0909090909090909f);
+    p = std::fmaf(z, p, 0.1111111111111111f);
+    p = std::fmaf(z, p, -0.1428571428571429f);
+    p = std::fmaf(z, p, 0.2f);
+    p = std::fmaf(z, p, -0.3333333333333333f);
+    return 4.0f * std::fmaf(r * z, p, r);
+}
+
+// atan2(y, x) by octant: atan_unit of min/max, reflected about pi/4 and pi/2, signed by y.
+inline float tatan2(float y, float x) {
+    if (x != x || y != y) return x + y;
+    float ax = std::fabs(x), ay = std::fabs(y);
+    float a;
+    if (ax == 0.0f && ay == 0.0f) {
+        a = 0.0f;
+    } else if (ax == ay) {
+        a = 0.785398185253143310546875f;  // pi/4, also for two infinities
+    } else if (ay > ax) {
+        a = (PIO2_1 - atan_unit(ax / ay)) + PIO2_2;
+    } else {
+        a = atan_unit(ay / ax);
+    }
+    if (std::signbit(x)) a = (PI_1 - a) + PI_2;
+    return std::signbit(y) ? -a : a;
+}
+
+// IEEE binary32 -> binary16, round to nearest even (f16::from_f32 of the half crate).
+inline uint16_t float_to_half(float f) {
+    uint32_t u = fbits(f);
+    uint16_t sign = (uint16_t)((u >> 16) & 0x8000u);
+    uint32_t a = u & 0x7fffffffu;
+    if (a > 0x7f800000u) return sign | 0x7e00u;   // NaN
+    if (a >= 0x47800000u) return sign | 0x7c00u;  // >= 65536 (and infinity)
+    if (a < 0x38800000u) {                        // below 2^-14: subnormal half or zero
+        float v = bitsf(a) * 16777216.0f;          // in units of 2^-24, exact
+        float r = (v + 12582912.0f) - 12582912.0f;  // round to an integer, ties to even
+        return sign | (uint16_t)r;
+    }
+    uint32_t h = (a >> 13) - (112u << 10);
+    uint32_t rem = a & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h += 1u;
+    return sign | (uint16_t)h;
+}
+
 }  // namespace ref

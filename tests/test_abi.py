@@ -74,6 +74,8 @@ def test_struct_sizes():
     assert ctypes.sizeof(native.SceneStats) == 10 * 8
     assert ctypes.sizeof(native.TraversalCounters) == 8 * 8
     assert ctypes.sizeof(native.Timings) == 3 * 8
+    assert ctypes.sizeof(native.MeshData) == 5 * 8 + 2 * 4
+    assert ctypes.sizeof(native.EmissiveSource) == 9 * 8
 
 
 def test_abi_version(lib):

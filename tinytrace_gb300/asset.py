@@ -279,6 +279,34 @@ class Scene:
         self._index_total += len(indices)
         return mesh_index
 
+    def append_processed_mesh(self, positions: np.ndarray, indices: np.ndarray, vertices: np.ndarray,
+                              center, radius: float) -> int:
+        """Appends a mesh whose positions (snorm16), vertices (packed) and bounding sphere were
+        produced elsewhere (tt_mesh_ingest); returns its index."""
+        self._cache = None
+        positions = np.ascontiguousarray(positions, np.int16).reshape(-1, 3)
+        indices = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        vertices = np.ascontiguousarray(vertices, VERTEX_DTYPE).reshape(-1)
+        if len(vertices) != len(positions):
+            raise ValueError("positions and vertices differ in length")
+        mesh_index = len(self.meshes)
+        self._positions.append(positions)
+        self._indices.append(indices)
+        self._vertices.append(vertices)
+        self.meshes.append(np.array((np.asarray(center, np.float32), np.float32(radius), self._vertex_total,
+                                     len(positions), self._index_total, len(indices)), MESH_DTYPE))
+        self._vertex_total += len(positions)
+        self._index_total += len(indices)
+        return mesh_index
+
+    @property
+    def vertex_total(self) -> int:
+        return self._vertex_total
+
+    @property
+    def index_total(self) -> int:
+        return self._index_total
+
     def insert_material(self, material: Material) -> int:
         """Scene::insert_material (src/asset/material.rs:305-357) for constant materials."""
         index = len(self.materials)

@@ -868,6 +868,35 @@ int32_t tt_scene_stats_get(tt_context* ctx, tt_handle scene, tt_scene_stats* out
     });
 }
 
+int32_t tt_mesh_ingest(tt_context* ctx, const tt_mesh_data* mesh, uint32_t vertex_offset, uint32_t index_offset,
+                       int16_t* positions, tt_vertex* vertices, tt_mesh* mesh_out) {
+    return guarded([&] {
+        require(ctx && mesh && mesh_out, "null argument");
+        require(mesh->vertex_count == 0 || (mesh->positions && positions && vertices), "null array");
+        require(mesh->index_count == 0 || mesh->indices, "null indices");
+        use_device(ctx);
+        mesh_ingest(*mesh, vertex_offset, index_offset, positions, vertices, mesh_out, ctx->stream);
+    });
+}
+
+int32_t tt_emissive_extract(tt_context* ctx, const tt_emissive_source* source, tt_emissive_triangle* out,
+                            uint64_t capacity, uint64_t* count) {
+    return guarded([&] {
+        require(ctx && source && count, "null argument");
+        const tt_emissive_source& s = *source;
+        require(s.model_count == 0 || (s.model_mesh && s.model_instance && s.meshes), "null model arrays");
+        require((s.vertex_count == 0 || (s.positions && s.vertices)) && (s.index_count == 0 || s.indices),
+                "null scene arrays");
+        std::vector<uint64_t> first;
+        uint64_t total = emissive_count(s, first);
+        *count = total;
+        if (total > capacity) fail(TT_ERR_OVERFLOW, "emissive output capacity too small");
+        require(total == 0 || out, "null output");
+        use_device(ctx);
+        emissive_extract(s, out, ctx->stream);
+    });
+}
+
 int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint64_t blas_bytes, void* tris,
                               uint64_t tri_bytes, void* tlas, uint64_t tlas_bytes) {
     return guarded([&] {

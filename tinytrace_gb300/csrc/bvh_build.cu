@@ -882,4 +882,9 @@ void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bo
     check_cuda(cudaGetLastError(), "bvh build kernels");
 }
 
+void exclusive_scan_u32(uint32_t* data, uint64_t n, cudaStream_t stream) {
+    Scratch sc(stream);
+    exclusive_scan(data, n, sc);
+}
+
 }  // namespace tt

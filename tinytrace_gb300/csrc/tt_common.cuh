@@ -185,6 +185,39 @@ TT_HD float tacos(float x) {
     return (PI_1 - 2.0f * asin_small(y)) + PI_2;
 }
 
+// atan(t) for 0 <= t <= 1: two half-angle steps atan(t) = 2 atan(t / (1 + sqrt(1 + t^2)))
+// bring the argument below tan(pi/16), then the Maclaurin series of atan through r^15.
+TT_HD float atan_unit(float t) {
+    float r = t / (1.0f + sqrtf(__fmaf_rn(t, t, 1.0f)));
+    r = r / (1.0f + sqrtf(__fmaf_rn(r, r, 1.0f)));
+    float z = r * r;
+    float p = __fmaf_rn(z, -0.0666666666666667f, 0.0769230769230769f);
+    p = __fmaf_rn(z, p, -0.0909090909090909f);
+    p = __fmaf_rn(z, p, 0.1111111111111111f);
+    p = __fmaf_rn(z, p, -0.1428571428571429f);
+    p = __fmaf_rn(z, p, 0.2f);
+    p = __fmaf_rn(z, p, -0.3333333333333333f);
+    return 4.0f * __fmaf_rn(r * z, p, r);
+}
+
+// atan2(y, x) by octant: atan_unit of min/max, reflected about pi/4 and pi/2, signed by y.
+TT_HD float tatan2(float y, float x) {
+    if (x != x || y != y) return x + y;
+    float ax = fabsf(x), ay = fabsf(y);
+    float a;
+    if (ax == 0.0f && ay == 0.0f) {
+        a = 0.0f;
+    } else if (ax == ay) {
+        a = 0.785398185253143310546875f;  // pi/4, also for two infinities
+    } else if (ay > ax) {
+        a = (PIO2_1 - atan_unit(ax / ay)) + PIO2_2;
+    } else {
+        a = atan_unit(ay / ax);
+    }
+    if (signbit(x)) a = (PI_1 - a) + PI_2;
+    return signbit(y) ? -a : a;
+}
+
 // ---------------------------------------------------------------- constants
 constexpr float PI = 3.1415926535897932f;
 constexpr float TAU = 6.283185307179586f;

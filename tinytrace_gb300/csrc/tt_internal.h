@@ -74,4 +74,18 @@ void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bo
 // (device array `d_instances`), keeping its topology; updates the slab-margin bound.
 void refit_scene_bvh(const tt_instance* d_instances, cudaStream_t stream, BvhResult& b);
 
+// In-place exclusive prefix sum of n device u32 values on `stream`.
+void exclusive_scan_u32(uint32_t* data, uint64_t n, cudaStream_t stream);
+
+// Scene::insert_mesh (src/asset/mod.rs:89-161) with the per-vertex work on the device: host
+// arrays in, snorm16 positions, packed vertices and the mesh record out.
+void mesh_ingest(const tt_mesh_data& mesh, uint32_t vertex_offset, uint32_t index_offset, int16_t* out_positions,
+                 tt_vertex* out_vertices, tt_mesh* out_mesh, cudaStream_t st);
+
+// Scene::emissive_triangles_in_model (src/asset/mod.rs:163-193) for a list of models.
+// emissive_count checks the models' meshes and index ranges and returns the triangle total
+// (`first`: the exclusive prefix of the models' triangle counts).
+uint64_t emissive_count(const tt_emissive_source& src, std::vector<uint64_t>& first);
+void emissive_extract(const tt_emissive_source& src, tt_emissive_triangle* out, cudaStream_t st);
+
 }  // namespace tt

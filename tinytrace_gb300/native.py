@@ -127,6 +127,23 @@ assert NODE4_DTYPE.itemsize == 128
 assert TRI_RECORD_DTYPE.itemsize == 48
 
 
+class MeshData(ctypes.Structure):
+    """tt_mesh_data"""
+
+    _fields_ = [("positions", ctypes.c_void_p), ("texture_coordinates", ctypes.c_void_p),
+                ("indices", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("tangents", ctypes.c_void_p),
+                ("vertex_count", ctypes.c_uint32), ("index_count", ctypes.c_uint32)]
+
+
+class EmissiveSource(ctypes.Structure):
+    """tt_emissive_source"""
+
+    _fields_ = [("positions", ctypes.c_void_p), ("vertices", ctypes.c_void_p), ("vertex_count", ctypes.c_uint64),
+                ("indices", ctypes.c_void_p), ("index_count", ctypes.c_uint64), ("meshes", ctypes.c_void_p),
+                ("mesh_count", ctypes.c_uint32), ("model_count", ctypes.c_uint32),
+                ("model_mesh", ctypes.c_void_p), ("model_instance", ctypes.c_void_p)]
+
+
 class SceneDesc(ctypes.Structure):
     """tt_scene_desc"""
 
@@ -226,6 +243,8 @@ SIGNATURES = {
     "tt_stage_timings_get": (_I32, [_P, ctypes.POINTER(StageTimings)]),
     "tt_autotune": (_I32, [_P, _U64, _P, _U64, ctypes.POINTER(TuneResult)]),
     "tt_scene_update_instances": (_I32, [_P, _U64, _P, _U32]),
+    "tt_mesh_ingest": (_I32, [_P, ctypes.POINTER(MeshData), _U32, _U32, _P, _P, _P]),
+    "tt_emissive_extract": (_I32, [_P, ctypes.POINTER(EmissiveSource), _P, _U64, ctypes.POINTER(_U64)]),
     "tt_cache_configure": (_I32, [_P, ctypes.POINTER(CacheConfig)]),
     "tt_cache_query": (_I32, [_P, _P, _U32, _P]),
     "tt_cache_train": (_I32, [_P, _P, _P, _U32, _P]),

@@ -55,12 +55,15 @@ def _scale_translation(center: np.ndarray, radius: float) -> np.ndarray:
     return m
 
 
-def flatten_scene(scene: AssetScene) -> tuple[np.ndarray, np.ndarray]:
+def flatten_scene(scene: AssetScene, emissive_fn=None) -> tuple[np.ndarray, np.ndarray]:
     """Scene::new's node-tree walk (src/scene.rs:29-64): one Instance per model with
     position transform = node transform * S(radius) T(centre), inverse, normal transform
-    = transform^-T, plus the emissive triangles of emissive models."""
+    = transform^-T, plus the emissive triangles of emissive models.  `emissive_fn`, when
+    given, extracts the triangles of all emissive (mesh index, instance index) models in one
+    call (DeviceIngest.emissive_triangles) instead of model by model on the host."""
     instances: list = []
     emissive: list = []
+    emissive_models: list = []
 
     def visit(_index, node, parent):
         transform = parent @ np.asarray(node.transform, np.float64)
@@ -77,6 +80,10 @@ def flatten_scene(scene: AssetScene) -> tuple[np.ndarray, np.ndarray]:
             inst["mesh_index"] = model.mesh_index
             idx = len(instances)
             instances.append(inst)
+            if emissive_fn is not None:
+                if model.material_index in scene.emissive_materials:
+                    emissive_models.append((model.mesh_index, idx))
+                continue
             tris = scene.emissive_triangles_in_model(model, idx)
             if tris is not None:
                 emissive.append(tris)
@@ -84,6 +91,8 @@ def flatten_scene(scene: AssetScene) -> tuple[np.ndarray, np.ndarray]:
 
     depth_first_node_tree(scene.root, np.eye(4), visit)
     inst_arr = np.array(instances, INSTANCE_DTYPE).reshape(-1) if instances else np.zeros(0, INSTANCE_DTYPE)
+    if emissive_fn is not None:
+        emissive = [emissive_fn(emissive_models)] if emissive_models else []
     em_arr = np.concatenate(emissive) if emissive else np.zeros(0, EMISSIVE_DTYPE)
     return np.ascontiguousarray(inst_arr), np.ascontiguousarray(em_arr)
 
@@ -91,13 +100,13 @@ def flatten_scene(scene: AssetScene) -> tuple[np.ndarray, np.ndarray]:
 class SceneArrays:
     """The byte arrays of one scene exactly as tt_scene_desc borrows them."""
 
-    def __init__(self, scene: AssetScene):
+    def __init__(self, scene: AssetScene, emissive_fn=None):
         self.positions = np.ascontiguousarray(scene.positions, np.int16).reshape(-1, 3)
         self.indices = np.ascontiguousarray(scene.indices, np.uint32)
         self.vertices = np.ascontiguousarray(scene.vertices)
         self.materials = np.ascontiguousarray(scene.material_array)
         self.meshes = np.ascontiguousarray(scene.mesh_array)
-        self.instances, self.emissive = flatten_scene(scene)
+        self.instances, self.emissive = flatten_scene(scene, emissive_fn)
 
     FIELDS = ("positions", "indices", "vertices", "materials", "meshes", "instances", "emissive")
 
