@@ -135,8 +135,26 @@ typedef struct tt_emissive_triangle {
     uint32_t instance_index;
 } tt_emissive_triangle;
 
+/* texture formats of ProcessedTexture (src/asset/texture.rs:62-118) */
+#define TT_TEXTURE_BC1_SRGB 1  /* ImageFormat::RgbaBc1Srgb: 8-byte BC1 blocks, sRGB colour */
+#define TT_TEXTURE_BC5_UNORM 2 /* ImageFormat::RgBc5Unorm: 16-byte blocks, two BC4 channels */
+#define TT_TEXTURE_R8_UNORM 3  /* ImageFormat::R8Unorm */
+#define TT_TEXTURE_R16_FLOAT 4 /* ImageFormat::R16Float */
+#define TT_TEXTURE_MAX_LEVELS 16
+
+/* src/asset/texture.rs:41-46 ProcessedTexture: `data` holds the mip levels back to back, level 0
+ * first; level k has (width >> k) x (height >> k) texels, row-major (BC formats: 4 x 4 blocks,
+ * row-major, partial blocks at the edges).  Sampled as the scene sampler of src/scene.rs:121-128
+ * samples it (trilinear, repeat). */
+typedef struct tt_texture {
+    uint32_t format, width, height, level_count;
+    const uint8_t* data;
+    uint64_t bytes;
+} tt_texture;
+
 /* The arrays of asset::Scene (src/asset/mod.rs:77-86) plus the flattened instances and
- * emissive triangles that Scene::new derives from the node tree (src/scene.rs:29-64). */
+ * emissive triangles that Scene::new derives from the node tree (src/scene.rs:29-64).
+ * Materials name textures by their index in `textures` (u32::MAX: none). */
 typedef struct tt_scene_desc {
     const int16_t* positions; /* position_count x [i16; 3], snorm16 */
     uint64_t position_count;
@@ -152,6 +170,9 @@ typedef struct tt_scene_desc {
     uint32_t instance_count;
     uint32_t emissive_triangle_count;
     const tt_emissive_triangle* emissive_triangles;
+    const tt_texture* textures;
+    uint32_t texture_count;
+    uint32_t reserved;
 } tt_scene_desc;
 
 /* src/lib.rs:228-232 Timings, in nanoseconds of device time */
@@ -329,6 +350,7 @@ typedef struct tt_restir_config {
 int32_t tt_restir_configure(tt_context* ctx, const tt_restir_config* config);
 /* Forgets the previous frame (the next frame does no temporal reuse). */
 int32_t tt_restir_reset(tt_context* ctx);
+/* TT_ERR_UNSUPPORTED for a scene whose materials sample textures. */
 int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target);
 /* Final reservoirs of the last ReSTIR frame, width * height * 32 bytes (row-major pixels:
  * light index u32, r1, r2, w_sum, M, W, 0, 0). */
@@ -440,6 +462,10 @@ int32_t tt_trace_batch_noalloc(tt_context* ctx, tt_handle scene, const float* ra
 int32_t tt_math_batch(tt_context* ctx, int32_t which, const float* x, uint64_t n, float* y);
 
 /* ---------------------------------------------------------------- measurement helpers */
+/* textureLod of texture `texture` of a scene at n (u, v, lod) float triples -> n RGBA floats
+ * (the sampling the shading kernels perform; for parity tests of the decoders and filter). */
+int32_t tt_texture_sample_batch(tt_context* ctx, tt_handle scene, uint32_t texture, const float* uvl, uint32_t n,
+                                float* rgba);
 /* Write a buffer larger than L2 on the context stream. */
 int32_t tt_flush_l2(tt_context* ctx);
 /* Record event `slot` (0..15) on the context stream / elapsed ms between two slots. */

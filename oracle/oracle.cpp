@@ -23,6 +23,7 @@
 #include "ref_bsdf.h"
 #include "ref_bvh.h"
 #include "ref_ingest.h"
+#include "ref_texture.h"
 
 using namespace ref;
 
@@ -39,6 +40,7 @@ struct OracleScene {
     std::vector<Mesh> meshes;
     std::vector<Instance> instances;
     std::vector<EmissiveTriangle> emissive;
+    std::vector<Texture> textures;
     SceneBvh bvh;
     bool use_bvh = true;
     bool flat = false;  // the integrator traces through the flat BVH instead of the two-level one
@@ -72,13 +74,13 @@ v3 camera_ray_direction(const Constants& c, v2 ndc) {
 struct RayHit {
     v3 world_position;
     Basis tangent_space;
-    v2 uv;
+    v2 uv, uv_ddx, uv_ddy;
     uint32_t instance_index, material_index;
 };
 
-// integrate.glsl:22-110 (ray differentials are skipped: they only select texture mips and
-// scenes handed to this oracle carry no textures).
-RayHit get_ray_hit(const OracleScene& s, const Hit& h) {
+// integrate.glsl:22-110; `bounce`, `ndc` and `origin` feed the ray differentials of the
+// primary hit (integrate.glsl:89-106).
+RayHit get_ray_hit(const OracleScene& s, const Constants& c, const Hit& h, uint32_t bounce, v2 ndc, v3 origin) {
     RayHit hit;
     const Instance& in = s.instances[h.instance];
     hit.instance_index = h.instance;
@@ -105,10 +107,18 @@ RayHit get_ray_hit(const OracleScene& s, const Hit& h) {
         normalize(bs * cross(hit.tangent_space.normal, hit.tangent_space.tangent));
     hit.uv = interp2(bary, uv_of(tv[0]->uv), uv_of(tv[1]->uv), uv_of(tv[2]->uv));
     hit.world_position = bary.x * pos[0] + bary.y * pos[1] + bary.z * pos[2];
+    hit.uv_ddx = hit.uv_ddy = v2{0.0f, 0.0f};
+    if (bounce == 0) {
+        v2 texel = v2{2.0f / (float)c.screen_size[0], 2.0f / (float)c.screen_size[1]};
+        v3 hx = triangle_intersection(pos, origin, camera_ray_direction(c, v2{ndc.x + texel.x, ndc.y}));
+        v3 hy = triangle_intersection(pos, origin, camera_ray_direction(c, v2{ndc.x, ndc.y + texel.y}));
+        hit.uv_ddx = interp2(bary - hx, uv_of(tv[0]->uv), uv_of(tv[1]->uv), uv_of(tv[2]->uv));
+        hit.uv_ddy = interp2(bary - hy, uv_of(tv[0]->uv), uv_of(tv[1]->uv), uv_of(tv[2]->uv));
+    }
     return hit;
 }
 
-// integrate.glsl:148-154 (constant materials)
+// integrate.glsl:148-154 for a material without emission textures
 v3 material_emissive(const Material& m) {
     return xyz(m.constants.emission_color) * m.constants.emission_luminance;
 }
@@ -130,7 +140,7 @@ v3 direct_light_contribution(const OracleScene& s, v3 position, v3 wi, const Bas
     uint32_t tri = h.prim + s.instances[h.instance].index_offset / 3u;
     if (tri % 0xffffu != ls.hash) return splat3(0.0f);
     const Material& lm = s.materials[s.instances[ls.instance].material_index];
-    v3 emissive = material_emissive(lm);
+    v3 emissive = material_emissive(lm, s.textures, ls.uv, 4.0f);  // integrate.glsl:188-189
     float bd = 0.0f;
     v3 bsdf = bsdf_evaluate(mat, lobes, wi, wo, bd);
     return bsdf * emissive * std::fabs(cos_theta(wo)) / fmx(density, PDF_EPSILON);
@@ -160,9 +170,10 @@ bool next_path_segment(const OracleScene& s, const Constants& c, PathState& ps, 
         ps.accumulated += splat3(1.0f) * ps.throughput;
         return false;
     }
-    RayHit hit = get_ray_hit(s, h);
+    RayHit hit = get_ray_hit(s, c, h, bounce, ps.ndc, ps.ray.origin);
+    if (bounce == 0) ps.mip_level = calculate_mip_level(hit.uv_ddx, hit.uv_ddy, c.screen_size);
     const Material& material = s.materials[hit.material_index];
-    const MaterialConstants& mc = material.constants;
+    const MaterialConstants mc = load_textures(material, s.textures, hit.uv, ps.mip_level);
     Basis basis = create_surface_basis(hit.tangent_space, xyz(mc.geometry_normal));
     v3 wi = transform_from_basis(basis, -ps.ray.direction);
     Lobes lobes = bsdf_prepare(mc, wi, ps.generator);
@@ -174,7 +185,7 @@ bool next_path_segment(const OracleScene& s, const Constants& c, PathState& ps, 
         ps.accumulated += ps.throughput * direct;
     }
     if (bounce == 0 || !nee) {
-        v3 emissive = material_emissive(material);
+        v3 emissive = material_emissive(material, s.textures, hit.uv, ps.mip_level);
         ps.accumulated += emissive * ps.throughput;
     }
     float density = 1.0f;
@@ -360,7 +371,7 @@ RSurface r_gbuffer(const RestirOracle& R, const Constants& c, uint32_t x, uint32
     RSurface q;
     q.seed = g.state;
     if (!h.hit) return q;
-    RayHit hit = get_ray_hit(s, h);
+    RayHit hit = get_ray_hit(s, c, h, 1u, ndc, org);  // constant materials: no differentials needed
     const MaterialConstants& mc = s.materials[hit.material_index].constants;
     Basis basis = create_surface_basis(hit.tangent_space, xyz(mc.geometry_normal));
     q.hit = true;
@@ -574,6 +585,9 @@ struct OracleSceneDesc {
     uint32_t instance_count;
     uint32_t emissive_count;
     const EmissiveTriangle* emissive;
+    const TextureDesc* textures;
+    uint32_t texture_count;
+    uint32_t reserved;
 };
 
 // accel: 0 brute force, 1 two-level BVH, 2 flat BVH (the structure render() traces through;
@@ -587,6 +601,20 @@ void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
     copy_in(s->meshes, d->meshes, d->mesh_count);
     copy_in(s->instances, d->instances, d->instance_count);
     copy_in(s->emissive, d->emissive, d->emissive_count);
+    s->textures.resize(d->texture_count);
+    for (uint32_t t = 0; t < d->texture_count; ++t) {
+        const TextureDesc& td = d->textures[t];
+        Texture& tx = s->textures[t];
+        tx.format = td.format;
+        tx.width = td.width;
+        tx.height = td.height;
+        uint64_t at = 0;
+        for (uint32_t l = 0; l < td.level_count; ++l) {
+            uint64_t n = texture_level_bytes(td.format, td.width >> l, td.height >> l);
+            tx.levels.emplace_back(td.data + at, td.data + at + n);
+            at += n;
+        }
+    }
     s->use_bvh = accel != 0;
     s->flat = accel == 2;
     if (s->use_bvh) s->bvh = build_scene_bvh(s->geom(), leaf_max);
@@ -781,6 +809,18 @@ void oracle_math(int which, const float* x, uint64_t n, float* y) {
             case 4: y[i] = tacos(x[i]); break;
             default: y[i] = 0.0f;
         }
+    }
+}
+
+// textureLod of texture `index` of a scene at n (u, v, lod) triples -> n RGBA.
+void oracle_texture_sample(void* p, uint32_t index, const float* uvl, uint32_t n, float* rgba) {
+    const OracleScene* s = static_cast<const OracleScene*>(p);
+    for (uint32_t i = 0; i < n; ++i) {
+        v4 r = sample_texture(s->textures[index], v2{uvl[3 * i], uvl[3 * i + 1]}, uvl[3 * i + 2]);
+        rgba[4 * i] = r.x;
+        rgba[4 * i + 1] = r.y;
+        rgba[4 * i + 2] = r.z;
+        rgba[4 * i + 3] = r.w;
     }
 }
 

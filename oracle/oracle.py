@@ -21,7 +21,24 @@ class OracleSceneDesc(ctypes.Structure):
                 ("index_count", ctypes.c_uint64), ("vertices", _P), ("vertex_count", ctypes.c_uint64),
                 ("materials", _P), ("material_count", ctypes.c_uint32), ("mesh_count", ctypes.c_uint32),
                 ("meshes", _P), ("instances", _P), ("instance_count", ctypes.c_uint32),
-                ("emissive_count", ctypes.c_uint32), ("emissive", _P)]
+                ("emissive_count", ctypes.c_uint32), ("emissive", _P), ("textures", _P),
+                ("texture_count", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class OracleTexture(ctypes.Structure):  # tt_texture
+    _fields_ = [("format", ctypes.c_uint32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("level_count", ctypes.c_uint32), ("data", _P), ("bytes", ctypes.c_uint64)]
+
+
+def _textures(arrays):
+    info = np.asarray(getattr(arrays, "texture_info", np.zeros((0, 5), np.uint64)), np.uint64).reshape(-1, 5)
+    data = getattr(arrays, "texture_data", np.zeros(0, np.uint8))
+    out = (OracleTexture * max(len(info), 1))()
+    at = 0
+    for i, (fmt, w, h, levels, nbytes) in enumerate(info.tolist()):
+        out[i] = OracleTexture(fmt, w, h, levels, (data.ctypes.data + at) if nbytes else None, nbytes)
+        at += nbytes
+    return out, len(info)
 
 
 def load() -> ctypes.CDLL:
@@ -50,6 +67,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_restir_frame.argtypes = [_P, _P, _P, ctypes.c_int]
         lib.oracle_restir_reservoirs.argtypes = [_P, _P]
         lib.oracle_atan2.argtypes = [_P, _P, ctypes.c_uint64, _P]
+        lib.oracle_texture_sample.argtypes = [_P, ctypes.c_uint32, _P, ctypes.c_uint32, _P]
         lib.oracle_mesh_ingest.restype = ctypes.c_int
         lib.oracle_mesh_ingest.argtypes = [_P, _P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P]
         _lib = lib
@@ -67,10 +85,11 @@ class OracleScene:
         """use_bvh=False traces by brute force; otherwise render() traces through the
         two-level BVH, or the flat one when `flat` (the hits are the same)."""
         self.arrays = arrays  # keeps the borrowed arrays alive
+        self._tex, ntex = _textures(arrays)
         d = OracleSceneDesc(_p(arrays.positions), len(arrays.positions), _p(arrays.indices), len(arrays.indices),
                             _p(arrays.vertices), len(arrays.vertices), _p(arrays.materials), len(arrays.materials),
                             len(arrays.meshes), _p(arrays.meshes), _p(arrays.instances), len(arrays.instances),
-                            len(arrays.emissive), _p(arrays.emissive))
+                            len(arrays.emissive), _p(arrays.emissive), ctypes.addressof(self._tex), ntex, 0)
         self.lib = load()
         self.handle = self.lib.oracle_scene_create(ctypes.byref(d), (2 if flat else 1) if use_bvh else 0, leaf_max)
 
@@ -79,6 +98,13 @@ class OracleScene:
             self.lib.oracle_scene_destroy(self.handle)
         except Exception:
             pass
+
+    def texture_sample(self, index: int, uvl: np.ndarray) -> np.ndarray:
+        """textureLod of texture `index` at (n, 3) (u, v, lod) -> (n, 4) RGBA."""
+        uvl = np.ascontiguousarray(uvl, np.float32).reshape(-1, 3)
+        out = np.zeros((len(uvl), 4), np.float32)
+        self.lib.oracle_texture_sample(self.handle, index, _p(uvl), len(uvl), _p(out))
+        return out
 
     def bvh(self):
         from tinytrace_gb300.native import NODE4_DTYPE, TRI_RECORD_DTYPE

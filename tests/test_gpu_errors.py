@@ -49,12 +49,12 @@ def test_non_finite_instance_matrix(ctx):
     assert rc == native.TT_ERR_INVALID_ARGUMENT and b"finite" in ctx.lib.tt_last_error()
 
 
-def test_textured_material_is_unsupported(ctx):
+def test_texture_index_without_textures(ctx):
     a = _cornell()
     a.materials = a.materials.copy()
-    a.materials["textures"][0, 3] = 0
+    a.materials["textures"][0, 3] = 0  # the scene holds no textures
     rc, _ = _create(ctx, a)
-    assert rc == native.TT_ERR_UNSUPPORTED
+    assert rc == native.TT_ERR_INVALID_ARGUMENT
 
 
 def test_bad_mesh_and_material_indices(ctx):

@@ -81,7 +81,7 @@ def _arena_bytes(w, h, spp, paths):
     chunk = min(spp, 64)
     items = wh * chunk
     p = (min(paths, max(items, 1)) + 127) // 128 * 128
-    sizes = [16 * p] * 7 + [16 * 4 * p, 4 * 4 * p, 4 * p, 32 * p, 64, 16 * items, 16 * wh, 16 * wh]
+    sizes = [16 * p] * 7 + [16 * 4 * p, 4 * 4 * p, 4 * p, 32 * p, 8 * p, 64, 16 * items, 16 * wh, 16 * wh]
     return sum((s + 255) // 256 * 256 for s in sizes) + 256
 
 

@@ -24,7 +24,9 @@ INVALID_INDEX = 0xFFFFFFFF
 def quantize_unorm(v: np.ndarray, n: int) -> np.ndarray:
     """src/math/mod.rs:24-29"""
     scale = np.float32((1 << n) - 1)
-    v = np.clip(np.asarray(v, np.float32), np.float32(0.0), np.float32(1.0))
+    v = np.asarray(v, np.float32)
+    v = np.where(v >= 0, v, np.float32(0.0))  # NaN -> 0, as the comparisons of the reference
+    v = np.where(v <= 1, v, np.float32(1.0)).astype(np.float32)
     return (v * scale + np.float32(0.5)).astype(np.int32)
 
 
@@ -158,17 +160,25 @@ class Material:
     emission_color: tuple = (1.0, 1.0, 1.0)
     geometry_opacity: float = 1.0
     geometry_normal: tuple = (0.0, 0.0, 1.0)
+    # Param::Texture: parameter name -> texture, (h, w, 3) floats for colours and normals,
+    # (h, w) floats for scalars; the parameter's constant is then the type's default (zero)
+    textures: dict = field(default_factory=dict)
 
     def is_emissive(self) -> bool:
         """src/asset/material.rs:177-183"""
+        if "emission_luminance" in self.textures:
+            return bool(np.any(np.asarray(self.textures["emission_luminance"]) > 0.0))
         return self.emission_luminance > 0.0
 
     def constants(self) -> np.ndarray:
-        """Material::constants (src/asset/material.rs:233-265); vec3s extended with 0."""
+        """Material::constants (src/asset/material.rs:233-265); vec3s extended with 0, textured
+        parameters zero (Param::constant_or_default, material.rs:20-25)."""
         from .native import MATERIAL_CONSTANTS_DTYPE
 
         c = np.zeros((), MATERIAL_CONSTANTS_DTYPE)
         for name in MATERIAL_CONSTANTS_DTYPE.names:
+            if name in self.textures:
+                continue
             v = getattr(self, name)
             if isinstance(v, tuple):
                 c[name] = (*v, 0.0)
@@ -209,6 +219,7 @@ class Scene:
         self.meshes: list[np.ndarray] = []
         self.materials: list[np.ndarray] = []
         self.emissive_materials: set[int] = set()
+        self.textures: list = []  # texture.ProcessedTexture
         self.root = Node()
         self._vertex_total = 0
         self._index_total = 0
@@ -308,13 +319,21 @@ class Scene:
         return self._index_total
 
     def insert_material(self, material: Material) -> int:
-        """Scene::insert_material (src/asset/material.rs:305-357) for constant materials."""
+        """Scene::insert_material (src/asset/material.rs:305-357): textured parameters are
+        processed (texture.process) and referenced by their index in `textures`."""
+        from . import texture
+
         index = len(self.materials)
         if material.is_emissive():
             self.emissive_materials.add(index)
         m = np.zeros((), MATERIAL_DTYPE)
         m["constants"] = material.constants()
         m["textures"] = INVALID_INDEX
+        for name, tex in material.textures.items():
+            if name not in texture.SLOTS:
+                raise ValueError(f"{name} is not a material parameter")
+            m["textures"][texture.SLOTS.index(name)] = len(self.textures)
+            self.textures.append(texture.process(name, np.asarray(tex, np.float32)))
         self.materials.append(m)
         return index
 

@@ -17,6 +17,7 @@
 #include "tt_internal.h"
 #include "tt_cache.cuh"
 #include "tt_kernels.h"
+#include "tt_texture.cuh"
 
 namespace tt {
 
@@ -74,6 +75,7 @@ struct ImageRes {
 
 struct SceneRes {
     DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform, inst_bucket, light_prim;
+    DeviceBuffer tex_table, tex_data, srgb;
     BvhResult bvh;
     DevScene dev{};
     tt_scene_stats stats{};
@@ -83,7 +85,7 @@ struct SceneRes {
 
 // Slot pool and queues of the wavefront integrator, grown on demand and kept across frames.
 struct WavefrontBuffers {
-    DeviceBuffer org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, counters, samples, running;
+    DeviceBuffer org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, counters, samples, running, ndc_mip;
     uint32_t slots = 0;
     uint64_t sample_items = 0;
     uint32_t pixels = 0;
@@ -325,10 +327,77 @@ void validate_scene(const tt_scene_desc* d) {
     for (uint32_t e = 0; e < d->emissive_triangle_count; ++e)
         require(d->emissive_triangles[e].instance_index < d->instance_count,
                 "emissive triangle instance_index out of range");
+    require(d->texture_count == 0 || d->textures, "textures pointer is null");
+    for (uint32_t t = 0; t < d->texture_count; ++t) {
+        const tt_texture& tx = d->textures[t];
+        require(tx.format >= TT_TEXTURE_BC1_SRGB && tx.format <= TT_TEXTURE_R16_FLOAT, "unknown texture format");
+        require(tx.width >= 1 && tx.height >= 1 && tx.width <= 65536 && tx.height <= 65536, "bad texture extent");
+        require(tx.level_count >= 1 && tx.level_count <= TT_TEXTURE_MAX_LEVELS, "bad texture level count");
+        require((tx.width >> (tx.level_count - 1)) >= 1 && (tx.height >> (tx.level_count - 1)) >= 1,
+                "texture level count exceeds its mip chain");
+        uint64_t bytes = 0;
+        for (uint32_t l = 0; l < tx.level_count; ++l) bytes += texture_level_bytes(tx.format, tx.width >> l, tx.height >> l);
+        require(tx.bytes == bytes, "texture byte count does not match its levels");
+        require(bytes == 0 || tx.data, "texture data pointer is null");
+    }
     for (uint32_t m = 0; m < d->material_count; ++m)
+        for (int t = 0; t < 27; ++t) {
+            uint32_t index = d->materials[m].textures[t];
+            require(index == 0xffffffffu || index < d->texture_count, "material texture index out of range");
+        }
+}
+
+// The texture table and level data on the device (levels 16-byte aligned), the sRGB table,
+// and the materials with their set texture slots recorded in the padding word.
+void upload_textures(const tt_scene_desc* d, SceneRes* s, cudaStream_t st) {
+    std::vector<DevTexture> table(d->texture_count);
+    uint64_t total = 0;
+    for (uint32_t t = 0; t < d->texture_count; ++t) {
+        const tt_texture& tx = d->textures[t];
+        DevTexture& dt = table[t];
+        dt = DevTexture{};
+        dt.format = tx.format;
+        dt.levels = tx.level_count;
+        dt.width = tx.width;
+        dt.height = tx.height;
+        for (uint32_t l = 0; l < tx.level_count; ++l) {
+            dt.offset[l] = total;
+            total += (texture_level_bytes(tx.format, tx.width >> l, tx.height >> l) + 15u) / 16u * 16u;
+        }
+    }
+    std::vector<uint8_t> data(total);
+    for (uint32_t t = 0; t < d->texture_count; ++t) {
+        const tt_texture& tx = d->textures[t];
+        uint64_t at = 0;
+        for (uint32_t l = 0; l < tx.level_count; ++l) {
+            uint64_t n = texture_level_bytes(tx.format, tx.width >> l, tx.height >> l);
+            std::memcpy(data.data() + table[t].offset[l], tx.data + at, n);
+            at += n;
+        }
+    }
+    upload(s->tex_table, table.data(), table.size(), st);
+    upload(s->tex_data, data.data(), data.size(), st);
+    std::vector<float> srgb(256);
+    for (int i = 0; i < 256; ++i) {  // sRGB EOTF
+        double c = i / 255.0;
+        srgb[i] = (float)(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
+    }
+    upload(s->srgb, srgb.data(), srgb.size(), st);
+    std::vector<tt_material> mats(d->materials, d->materials + d->material_count);
+    bool textured = false;
+    for (tt_material& m : mats) {
+        uint32_t mask = 0;
         for (int t = 0; t < 27; ++t)
-            if (d->materials[m].textures[t] != 0xffffffffu)
-                fail(TT_ERR_UNSUPPORTED, "textured materials are not supported (texture index set)");
+            if (m.textures[t] != 0xffffffffu) mask |= 1u << t;
+        m.padding = mask;
+        textured = textured || (mask & (LOAD_SLOTS | EMISSION_SLOTS)) != 0u;
+    }
+    upload(s->materials, mats.data(), mats.size(), st);
+    check_cuda(cudaStreamSynchronize(st), "texture upload");  // the host staging vectors go out of scope
+    s->dev.textures = s->tex_table.as<DevTexture>();
+    s->dev.tex_data = s->tex_data.as<uint8_t>();
+    s->dev.srgb = s->srgb.as<float>();
+    s->dev.textured = textured ? 1u : 0u;
 }
 
 template <class F>
@@ -380,6 +449,7 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
         b.hslot.alloc(4ull * HIT_BUCKETS * slots);
         b.active.alloc(4ull * slots);
         b.shadow.alloc(32ull * slots);
+        b.ndc_mip.alloc(8ull * slots);
         b.slots = slots;
     }
     if (!b.counters.ptr) b.counters.alloc(64);
@@ -406,6 +476,7 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
     w.counters = b.counters.as<uint32_t>();
     w.samples = b.samples.as<float4>();
     w.running = b.running.as<float4>();
+    w.ndc_mip = b.ndc_mip.as<float2>();
     w.P = slots;
     w.chunk_spp = chunk_spp;
     w.refill = ctx->refill_lanes;
@@ -524,6 +595,7 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     bool wavefront = ctx->integrator == TT_INTEGRATOR_WAVEFRONT && c->sample_count > 0 && c->bounce_count > 0;
     WfParams w{};
     if (wavefront) w = wavefront_buffers(ctx, *c);
+    if (!s->dev.textured) w.ndc_mip = nullptr;
     bool cached = wavefront && ctx->cache.enabled && !counted;
     if (cached) cache_frame_buffers(ctx, *c, s->dev, w);
     StageTimer* timer = nullptr;
@@ -731,7 +803,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         upload(s->positions, d->positions, d->position_count * 3ull, st);
         upload(s->indices, d->indices, d->index_count, st);
         upload(s->vertices, d->vertices, d->vertex_count, st);
-        upload(s->materials, d->materials, d->material_count, st);
+        upload_textures(d, s.get(), st);
         upload(s->meshes, d->meshes, d->mesh_count, st);
         upload(s->instances, d->instances, d->instance_count, st);
         s->host_instances.assign(d->instances, d->instances + d->instance_count);
@@ -1075,6 +1147,7 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         ImageRes* img = lookup<ImageRes>(ctx, target, KIND_IMAGE);
         require(constants->screen_size[0] == img->width && constants->screen_size[1] == img->height,
                 "constants.screen_size must equal the target extent");
+        if (s->dev.textured) fail(TT_ERR_UNSUPPORTED, "ReSTIR DI shades constant materials only");
         RestirState& R = ctx->restir;
         uint64_t WH = (uint64_t)img->width * img->height;
         if (WH != R.pixels) {
@@ -1290,6 +1363,21 @@ int32_t tt_math_batch(tt_context* ctx, int32_t which, const float* x, uint64_t n
         require(which >= 0 && which <= 4, "unknown function");
         batch(ctx, x, 4ull * n, nullptr, 0, y, 4ull * n, [&](void* din, void*, void* dout) {
             launch_math(which, static_cast<const float*>(din), n, static_cast<float*>(dout), ctx->stream);
+        });
+    });
+}
+
+int32_t tt_texture_sample_batch(tt_context* ctx, tt_handle scene, uint32_t texture, const float* uvl, uint32_t n,
+                                float* rgba) {
+    return guarded([&] {
+        require(ctx && (n == 0 || (uvl && rgba)), "null argument");
+        use_device(ctx);
+        SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
+        require(texture < s->tex_table.bytes / sizeof(DevTexture), "texture index out of range");
+        DevScene sc = s->dev;
+        batch(ctx, uvl, 12ull * n, nullptr, 0, rgba, 16ull * n, [&](void* din, void*, void* dout) {
+            launch_texture_sample(sc, texture, static_cast<const float*>(din), n, static_cast<float4*>(dout),
+                                  ctx->stream);
         });
     });
 }

@@ -18,7 +18,7 @@ namespace tt {
 
 constexpr int TILE_W = 16, TILE_H = 8, BLOCK = TILE_W * TILE_H;
 
-template <bool COUNT>
+template <bool COUNT, bool TEX>
 __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant__ RenderParams p) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * BLOCK];
     const tt_constants& c = p.c;
@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
             f3 ray_org = cam;
             uint32_t g = pixel_gen;
             f3 path_acc = splat(0.0f), thr = splat(1.0f);
+            float mip_level = 1.0f;  // integrate.glsl:215-216
             for (uint32_t bounce = 0; bounce < c.bounce_count; ++bounce) {
                 if (COUNT) rays++;
                 Hit h = trace_closest<COUNT>(sc, ray_org, ray_dir, EXTENSION_TMIN, EXTENSION_TMAX, true,
@@ -49,8 +50,10 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
                 }
                 if (COUNT) hits++;
                 ShadeHit hit = get_ray_hit(sc, h.instance, h.prim, h.u, h.v);
+                if (TEX && bounce == 0) mip_level = primary_mip_level(c, hit, ray_org, ndc);
                 const tt_material* material = sc.materials + hit.material_index;
-                const MatC& mc = material->constants;
+                MatC local;
+                const MatC& mc = hit_material<TEX>(sc, material, hit.uv, mip_level, local);
                 Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
                 f3 wi = transform_from_basis(basis, -ray_dir);
                 Lobes lobes = bsdf_prepare(mc, wi, g);
@@ -61,11 +64,11 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
                     LightSample ls = sample_light(sc, hit.world_position, basis, g);
                     Hit hs = trace_closest<COUNT>(sc, hit.world_position, ls.dir, SHADOW_TMIN, SHADOW_TMAX, false,
                                                   stack, BLOCK, p.err, cnt);
-                    f3 direct = light_visible(sc, hs, ls.instance, ls.hash) ? light_contribution(sc, ls, mc, lobes, wi)
+                    f3 direct = light_visible(sc, hs, ls.instance, ls.hash) ? light_contribution<TEX>(sc, ls, mc, lobes, wi)
                                                                            : splat(0.0f);
                     path_acc += thr * direct;
                 }
-                if (bounce == 0 || !nee) path_acc += material_emissive(material) * thr;
+                if (bounce == 0 || !nee) path_acc += hit_emissive<TEX>(sc, material, hit.uv, mip_level) * thr;
                 float density = 1.0f;
                 f3 wo = splat(0.0f);
                 int lobe = 0;
@@ -195,8 +198,13 @@ __global__ void math_kernel(int which, const float* x, uint64_t n, float* y) {
 // ---------------------------------------------------------------- launchers
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st) {
     dim3 grid((p.c.screen_size[0] + TILE_W - 1) / TILE_W, (p.c.screen_size[1] + TILE_H - 1) / TILE_H);
-    if (counted) integrate_kernel<true><<<grid, BLOCK, 0, st>>>(p);
-    else integrate_kernel<false><<<grid, BLOCK, 0, st>>>(p);
+    if (p.sc.textured) {
+        if (counted) integrate_kernel<true, true><<<grid, BLOCK, 0, st>>>(p);
+        else integrate_kernel<false, true><<<grid, BLOCK, 0, st>>>(p);
+    } else {
+        if (counted) integrate_kernel<true, false><<<grid, BLOCK, 0, st>>>(p);
+        else integrate_kernel<false, false><<<grid, BLOCK, 0, st>>>(p);
+    }
 }
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out, cudaStream_t st) {
     if (n == 0) return;
@@ -212,6 +220,17 @@ void launch_trace(const DevScene& sc, const float4* rays, uint32_t n, uint32_t f
                   uint32_t* err, cudaStream_t st) {
     if (n) trace_kernel<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(sc, rays, n, flags, hits, err);
 }
+// textureLod of one texture at (u, v, lod) triples, for parity tests of the decoders and filter.
+__global__ void texture_sample_kernel(DevScene sc, uint32_t index, const float* uvl, uint32_t n, float4* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = sample_texture(sc, index, f2{uvl[3ull * i], uvl[3ull * i + 1]}, uvl[3ull * i + 2]);
+}
+void launch_texture_sample(const DevScene& sc, uint32_t index, const float* uvl, uint32_t n, float4* out,
+                           cudaStream_t st) {
+    if (n) texture_sample_kernel<<<(n + 127) / 128, 128, 0, st>>>(sc, index, uvl, n, out);
+}
+
 void launch_math(int which, const float* x, uint64_t n, float* y, cudaStream_t st) {
     if (n) math_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(which, x, n, y);
 }

@@ -55,7 +55,8 @@ struct Request {
 struct Layout {
     uint32_t P = 0, chunk_spp = 0;
     uint64_t WH = 0, items = 0;
-    uint64_t org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, counters, samples, running, target, total;
+    uint64_t org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, ndc_mip, counters, samples, running, target,
+        total;
 };
 
 Layout layout_for(const tt_constants& c, uint32_t paths) {
@@ -82,6 +83,7 @@ Layout layout_for(const tt_constants& c, uint32_t paths) {
     L.hslot = take(4ull * HIT_BUCKETS * L.P);
     L.active = take(4ull * L.P);
     L.shadow = take(32ull * L.P);
+    L.ndc_mip = take(8ull * L.P);
     L.counters = take(4ull * CTRL_WORDS);
     L.samples = take(16ull * L.items);
     L.running = take(16ull * L.WH);
@@ -153,6 +155,7 @@ void tt_server::launch(Slot& s, Request& r) {
     w.counters = reinterpret_cast<uint32_t*>(arena + L.counters);
     w.samples = reinterpret_cast<float4*>(arena + L.samples);
     w.running = reinterpret_cast<float4*>(arena + L.running);
+    w.ndc_mip = r.sc.textured ? reinterpret_cast<float2*>(arena + L.ndc_mip) : nullptr;
     w.P = L.P;
     w.chunk_spp = L.chunk_spp;
     w.refill = 20;

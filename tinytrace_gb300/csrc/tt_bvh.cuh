@@ -43,6 +43,13 @@ constexpr uint32_t ERR_ITERATION_LIMIT = 2u;
 TT_HD uint32_t leaf_first(uint32_t r) { return r & 0x07ffffffu; }
 TT_HD uint32_t leaf_count(uint32_t r) { return ((r >> 27) & 0xfu) + 1u; }
 
+// One texture: format (TEX_*), mip levels, level-0 extent and the byte offset of every level
+// in the scene's texture data (levels of max(1, w >> k) x max(1, h >> k) texels, 16-byte aligned).
+struct DevTexture {
+    uint32_t format, levels, width, height;
+    uint64_t offset[16];
+};
+
 struct DevScene {
     const int16_t* positions;
     const uint32_t* indices;
@@ -62,6 +69,10 @@ struct DevScene {
     uint32_t has_tlas;
     float tlas_bound;  // max |coordinate| of the world boxes in `tlas`
     uint32_t flat;     // 1: `tlas`/`tris` hold the flat BVH
+    const DevTexture* textures;  // texture table (null when the scene has no textures)
+    const uint8_t* tex_data;     // all texture levels
+    const float* srgb;           // 256-entry sRGB-to-linear table
+    uint32_t textured;           // 1 when some material samples a texture
 };
 
 struct Hit {

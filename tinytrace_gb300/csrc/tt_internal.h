@@ -74,6 +74,17 @@ void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bo
 // (device array `d_instances`), keeping its topology; updates the slab-margin bound.
 void refit_scene_bvh(const tt_instance* d_instances, cudaStream_t stream, BvhResult& b);
 
+// Bytes of one texture level of w x h texels (BC formats in 4 x 4 blocks).
+inline uint64_t texture_level_bytes(uint32_t format, uint32_t w, uint32_t h) {
+    uint64_t blocks = (uint64_t)((w + 3u) / 4u) * ((h + 3u) / 4u);
+    switch (format) {
+        case TT_TEXTURE_BC1_SRGB: return 8ull * blocks;
+        case TT_TEXTURE_BC5_UNORM: return 16ull * blocks;
+        case TT_TEXTURE_R8_UNORM: return (uint64_t)w * h;
+        default: return 2ull * w * h;  // TT_TEXTURE_R16_FLOAT
+    }
+}
+
 // In-place exclusive prefix sum of n device u32 values on `stream`.
 void exclusive_scan_u32(uint32_t* data, uint64_t n, cudaStream_t stream);
 

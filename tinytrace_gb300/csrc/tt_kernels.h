@@ -60,6 +60,9 @@ struct WfParams {
     float4* train_final;    // final radiance of each training path
     const float* cache_grid;
     const __half* cache_w16;
+    // textured scenes: per slot, the primary ray's ndc (written by regen) and then the mip
+    // level of the path (x, written at bounce 0); null without textures
+    float2* ndc_mip;
 };
 // SM count and resident blocks per SM of the persistent trace kernel.
 void trace_occupancy(int* sms, int* blocks_per_sm);
@@ -127,6 +130,8 @@ void launch_bsdf_sample(const tt_material_constants* m, const float4* samples, u
 void launch_trace(const DevScene& sc, const float4* rays, uint32_t n, uint32_t flags, uint4* hits,
                   uint32_t* err, cudaStream_t st);
 void launch_math(int which, const float* x, uint64_t n, float* y, cudaStream_t st);
+void launch_texture_sample(const DevScene& sc, uint32_t index, const float* uvl, uint32_t n, float4* out,
+                           cudaStream_t st);
 // Ray queries staged in the library's static device array (no device allocation).
 void trace_batch_noalloc(int device, const DevScene& sc, const float* rays_host, uint32_t n,
                          uint32_t flags, uint32_t* hits_host, cudaStream_t st);

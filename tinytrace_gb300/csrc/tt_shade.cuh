@@ -6,6 +6,7 @@
 
 #include "tt_bsdf.cuh"
 #include "tt_bvh.cuh"
+#include "tt_texture.cuh"
 
 namespace tt {
 
@@ -31,10 +32,14 @@ struct ShadeHit {
     f3 world_position;
     Basis tangent_space;
     uint32_t material_index;
+    // texturing inputs (dead code unless a textured instantiation reads them)
+    f2 uv;                // interpolated texture coordinates
+    f3 bary;              // barycentrics of the hit
+    f3 world[3];          // world-space triangle vertices
+    uint32_t tc[3];       // the vertices' f16 texture coordinates
 };
 
-// integrate.glsl:22-110 without ray differentials (they only select texture mip levels, and
-// scenes with textures are rejected at scene creation).
+// integrate.glsl:22-110; the ray differentials of the primary hit are primary_mip_level.
 __device__ __forceinline__ ShadeHit get_ray_hit(const DevScene& sc, uint32_t instance, uint32_t prim, float u,
                                                 float v) {
     ShadeHit hit;
@@ -54,6 +59,8 @@ __device__ __forceinline__ ShadeHit get_ray_hit(const DevScene& sc, uint32_t ins
         f3 p = f3{dequant_snorm16(__ldg(s + 0)), dequant_snorm16(__ldg(s + 1)), dequant_snorm16(__ldg(s + 2))};
         pos[k] = mat43_point(m, p);
         tf[k] = decode_tangent_frame(__ldg(&sc.vertices[vi].tangent_frame));
+        hit.tc[k] = __ldg(reinterpret_cast<const uint32_t*>(&sc.vertices[vi].texture_coordinates));
+        hit.world[k] = pos[k];
     }
     f3 bary = f3{0.0f, u, v};
     bary.x = 1.0f - bary.y - bary.z;
@@ -65,7 +72,50 @@ __device__ __forceinline__ ShadeHit get_ray_hit(const DevScene& sc, uint32_t ins
     float bs = signf(tf[0].bitangent_sign * bary.x + tf[1].bitangent_sign * bary.y + tf[2].bitangent_sign * bary.z);
     hit.tangent_space.bitangent = normalize(bs * cross(hit.tangent_space.normal, hit.tangent_space.tangent));
     hit.world_position = bary.x * pos[0] + bary.y * pos[1] + bary.z * pos[2];
+    hit.bary = bary;
+    hit.uv = interp_uv(bary, hit.tc[0], hit.tc[1], hit.tc[2]);
     return hit;
+}
+
+// calculate_mip_level (integrate.glsl:134-139) of the texture-coordinate differentials of the
+// primary hit (integrate.glsl:91-106): the camera rays one texel right and one texel up,
+// crossed with the hit triangle's plane.
+__device__ __forceinline__ float primary_mip_level(const tt_constants& c, const ShadeHit& hit, f3 origin, f2 ndc) {
+    f2 texel = f2{2.0f / (float)c.screen_size[0], 2.0f / (float)c.screen_size[1]};
+    f3 hx = triangle_barycentrics(hit.world, origin, camera_ray_direction(c, f2{ndc.x + texel.x, ndc.y}));
+    f3 hy = triangle_barycentrics(hit.world, origin, camera_ray_direction(c, f2{ndc.x, ndc.y + texel.y}));
+    f2 ddx = interp_uv(hit.bary - hx, hit.tc[0], hit.tc[1], hit.tc[2]);
+    f2 ddy = interp_uv(hit.bary - hy, hit.tc[0], hit.tc[1], hit.tc[2]);
+    float sw = (float)c.screen_size[0], sh = (float)c.screen_size[1];
+    f2 sx = f2{ddx.x * sw, ddx.y * sh}, sy = f2{ddy.x * sw, ddy.y * sh};
+    float gx = sx.x * sx.x + sx.y * sx.y, gy = sy.x * sy.x + sy.y * sy.y;
+    return 0.5f * (tlog(fmx(gx, gy)) * LOG2E);
+}
+
+// The material constants a hit shades with: the material's own, or (textured) a copy with
+// the sampled slots replaced; `local` holds the copy.
+template <bool TEX>
+__device__ __forceinline__ const MatC& hit_material(const DevScene& sc, const tt_material* mat, f2 uv, float lod,
+                                                    MatC& local) {
+    if (TEX) {
+        uint32_t mask = __ldg(&mat->padding);
+        if (mask & LOAD_SLOTS) {
+            local = mat->constants;
+            load_textures(sc, mat, mask, uv, lod, local);
+            return local;
+        }
+    }
+    return mat->constants;
+}
+
+template <bool TEX>
+__device__ __forceinline__ f3 hit_emissive(const DevScene& sc, const tt_material* mat, f2 uv, float lod) {
+    if (TEX) {
+        uint32_t mask = __ldg(&mat->padding);
+        if (mask & EMISSION_SLOTS) return material_emissive_textured(sc, mat, mask, uv, lod);
+    }
+    const MatC& m = mat->constants;
+    return col3(m.emission_color) * m.emission_luminance;
 }
 
 // integrate.glsl:148-154 (constant materials)
@@ -90,6 +140,7 @@ struct LightSample {
     f3 dir;         // world-space shadow ray direction
     float density;  // solid-angle density times the light selection probability
     uint32_t instance, hash;
+    f2 uv;          // texture coordinates of the light point (read by textured shading only)
 };
 __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 position, const Basis& basis,
                                                     uint32_t& g) {
@@ -110,6 +161,10 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 posit
     float area = fmx(0.00001f, 0.5f * length(cross(p[1] - p[0], p[2] - p[0])));
     f3 lnormal = normalize(cross(p[1] - p[0], p[2] - p[0]));
     f3 lpos = interp3(bary, p[0], p[1], p[2]);
+    uint32_t tc[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) tc[k] = __ldg(reinterpret_cast<const uint32_t*>(&tri->texture_coordinates[k]));
+    ls.uv = interp_uv(bary, tc[0], tc[1], tc[2]);
     ls.hash = (uint32_t)__ldg(&tri->hash);
     float light_probability = 1.0f / (float)sc.emissive_count;
     f3 to_light = lpos - position;
@@ -120,10 +175,12 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 posit
     return ls;
 }
 
-// The contribution of integrate.glsl:186-192 when the light is visible.
+// The contribution of integrate.glsl:186-192 when the light is visible (the light's emission
+// textures are sampled at mip level 4, integrate.glsl:188-189).
+template <bool TEX = false>
 __device__ __forceinline__ f3 light_contribution(const DevScene& sc, const LightSample& ls, const MatC& mat,
                                                  const Lobes& lobes, f3 wi) {
-    f3 emissive = material_emissive(sc.materials + __ldg(&sc.instances[ls.instance].material_index));
+    f3 emissive = hit_emissive<TEX>(sc, sc.materials + __ldg(&sc.instances[ls.instance].material_index), ls.uv, 4.0f);
     float bd = 0.0f;
     f3 bsdf = bsdf_evaluate(mat, lobes, wi, ls.wo, bd);
     return bsdf * emissive * fabsf(cos_theta(ls.wo)) / fmx(ls.density, PDF_EPSILON);

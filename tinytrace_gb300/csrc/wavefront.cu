@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
         for (uint32_t k = 0; k < 2u * sample; ++k) xor_shift(pg);
         f2 ndc = pixel_ndc(x, y, W, H, pg);
         f3 d = camera_ray_direction(c, ndc);
+        if (w.ndc_mip) w.ndc_mip[s] = make_float2(ndc.x, ndc.y);
         w.org[s] = make_float4(c.camera_position[0], c.camera_position[1], c.camera_position[2], __uint_as_float(0u));
         w.dir[s] = pack(d, pg);
         w.thr[s] = pack(splat(1.0f), item);
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
 #ifndef TT_SHADE_MIN_BLOCKS
 #define TT_SHADE_MIN_BLOCKS 6
 #endif
-template <bool CACHE>
+template <bool CACHE, bool TEX>
 __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel(const __grid_constant__ RenderParams p,
                                                             const __grid_constant__ WfParams w) {
     // thread q shades entry q of the bucket queues laid end to end
@@ -298,8 +299,19 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
         uint32_t g = __float_as_uint(d4.w), bounce = __float_as_uint(o4.w);
         uint32_t train = __float_as_uint(a4.w) & F_TRAIN;
         ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
+        float mip_level = 1.0f;
+        if (TEX) {
+            float2 nm = w.ndc_mip[s];
+            if (bounce == 0u) {
+                mip_level = primary_mip_level(c, hit, xyz(o4), f2{nm.x, nm.y});
+                w.ndc_mip[s] = make_float2(mip_level, nm.y);
+            } else {
+                mip_level = nm.x;
+            }
+        }
         const tt_material* material = sc.materials + hit.material_index;
-        const MatC& mc = material->constants;
+        MatC local;
+        const MatC& mc = hit_material<TEX>(sc, material, hit.uv, mip_level, local);
         Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
         {
             if (CACHE) {
@@ -328,10 +340,10 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
             f3 wi = transform_from_basis(basis, -ray_dir);
             Lobes lobes = bsdf_prepare(mc, wi, g);
             bool nee = c.light_sampling == LIGHT_SAMPLING_NEE && sc.emissive_count > 0 && mc.specular_roughness > 0.15f;
-            f3 em = material_emissive(material);
+            f3 em = hit_emissive<TEX>(sc, material, hit.uv, mip_level);
             if (nee) {
                 LightSample ls = sample_light(sc, hit.world_position, basis, g);
-                f3 contrib = light_contribution(sc, ls, mc, lobes, wi);
+                f3 contrib = light_contribution<TEX>(sc, ls, mc, lobes, wi);
                 f3 a1 = thr * contrib, a0 = thr * splat(0.0f);
                 // When the visible and the occluded update have the same bits (the light faces
                 // away, or the BSDF is zero towards it) the shadow ray cannot change the result:
@@ -441,6 +453,17 @@ static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid
     }
 }
 
+static void launch_shade(const RenderParams& p, const WfParams& w, unsigned grid, cudaStream_t st) {
+    bool tex = p.sc.textured != 0u;
+    if (w.cache_on) {
+        if (tex) wf_shade_kernel<true, true><<<grid, WF_BLOCK, 0, st>>>(p, w);
+        else wf_shade_kernel<true, false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+    } else {
+        if (tex) wf_shade_kernel<false, true><<<grid, WF_BLOCK, 0, st>>>(p, w);
+        else wf_shade_kernel<false, false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+    }
+}
+
 // Device-side loop control: counts the chunk's iterations and keeps the graph's while loop
 // running while paths are live, for at most `limit` iterations (then ERR_ITERATION_LIMIT).
 __global__ void wf_control_kernel(uint32_t* counters, cudaGraphConditionalHandle handle, uint32_t limit,
@@ -506,8 +529,7 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
         wf_regen_kernel<<<regen_grid, REGEN_BLOCK, 0, body_stream>>>(p, w);
         wf_control_kernel<<<1, 1, 0, body_stream>>>(w.counters, handle, limit, p.err);
         launch_trace<false>(p, w, tgrid, counted, body_stream);
-        if (w.cache_on) wf_shade_kernel<true><<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w);
-        else wf_shade_kernel<false><<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w);
+        launch_shade(p, w, shade_grid, body_stream);
         launch_trace<true>(p, w, tgrid, counted, body_stream);
         if (w.cache_on) {
             cache_infer_queue(w.cache_grid, w.cache_w16, w.cq, w.counters + CACHE_QUEUE, w.P, w.cq_out, body_stream);
@@ -559,8 +581,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
             launch_trace<false>(p, w, tgrid, counted, st);
             stage_end(timer, st);
             stage_begin(timer, TT_STAGE_SHADE, st);
-            if (w.cache_on) wf_shade_kernel<true><<<grid, WF_BLOCK, 0, st>>>(p, w);
-            else wf_shade_kernel<false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+            launch_shade(p, w, grid, st);
             stage_end(timer, st);
             stage_begin(timer, TT_STAGE_SHADOW, st);
             launch_trace<true>(p, w, tgrid, counted, st);

@@ -35,6 +35,11 @@ TT_LIFETIME_RENDERER = 4
 
 TT_FORMAT_RGBA32F = 0
 TT_FORMAT_RGBA8_UNORM = 1
+TT_TEXTURE_BC1_SRGB = 1
+TT_TEXTURE_BC5_UNORM = 2
+TT_TEXTURE_R8_UNORM = 3
+TT_TEXTURE_R16_FLOAT = 4
+TT_TEXTURE_MAX_LEVELS = 16
 TT_TRACE_CULL_BACK_FACES = 1
 TT_TRACE_NOALLOC_MAX_RAYS = 65536
 TT_INTEGRATOR_WAVEFRONT = 0
@@ -144,6 +149,13 @@ class EmissiveSource(ctypes.Structure):
                 ("model_mesh", ctypes.c_void_p), ("model_instance", ctypes.c_void_p)]
 
 
+class TextureDesc(ctypes.Structure):
+    """tt_texture"""
+
+    _fields_ = [("format", ctypes.c_uint32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("level_count", ctypes.c_uint32), ("data", ctypes.c_void_p), ("bytes", ctypes.c_uint64)]
+
+
 class SceneDesc(ctypes.Structure):
     """tt_scene_desc"""
 
@@ -162,6 +174,9 @@ class SceneDesc(ctypes.Structure):
         ("instance_count", ctypes.c_uint32),
         ("emissive_triangle_count", ctypes.c_uint32),
         ("emissive_triangles", ctypes.c_void_p),
+        ("textures", ctypes.c_void_p),
+        ("texture_count", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
 
@@ -265,6 +280,7 @@ SIGNATURES = {
     "tt_trace_batch": (_I32, [_P, _U64, _P, _U32, _U32, _P]),
     "tt_trace_batch_noalloc": (_I32, [_P, _U64, _P, _U32, _U32, _P]),
     "tt_math_batch": (_I32, [_P, _I32, _P, _U64, _P]),
+    "tt_texture_sample_batch": (_I32, [_P, _U64, _U32, _P, _U32, _P]),
     "tt_flush_l2": (_I32, [_P]),
     "tt_event_record": (_I32, [_P, _U32]),
     "tt_event_elapsed_ms": (_I32, [_P, _U32, _U32, ctypes.POINTER(ctypes.c_float)]),

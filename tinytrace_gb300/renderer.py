@@ -107,8 +107,14 @@ class SceneArrays:
         self.materials = np.ascontiguousarray(scene.material_array)
         self.meshes = np.ascontiguousarray(scene.mesh_array)
         self.instances, self.emissive = flatten_scene(scene, emissive_fn)
+        # textures: (format, width, height, level count, byte count) rows and all level data
+        textures = getattr(scene, "textures", [])
+        self.texture_info = np.array([(t.format, t.width, t.height, len(t.levels), len(t.data)) for t in textures],
+                                     np.uint64).reshape(-1, 5)
+        self.texture_data = np.frombuffer(b"".join(t.data for t in textures), np.uint8).copy()
 
-    FIELDS = ("positions", "indices", "vertices", "materials", "meshes", "instances", "emissive")
+    FIELDS = ("positions", "indices", "vertices", "materials", "meshes", "instances", "emissive", "texture_info",
+              "texture_data")
 
     def save(self, path, prefix: str = "") -> dict:
         """The arrays as a dict (and, when `path` is given, an .npz file) for reloading with
@@ -121,9 +127,24 @@ class SceneArrays:
     @classmethod
     def from_arrays(cls, data, prefix: str = "") -> "SceneArrays":
         self = cls.__new__(cls)
+        empty = {"texture_info": np.zeros((0, 5), np.uint64), "texture_data": np.zeros(0, np.uint8)}
         for k in cls.FIELDS:
-            setattr(self, k, np.ascontiguousarray(data[prefix + k]))
+            v = data[prefix + k] if (prefix + k) in data else empty[k]
+            setattr(self, k, np.ascontiguousarray(v))
         return self
+
+    def texture_descs(self):
+        """ctypes array of tt_texture pointing into texture_data (kept alive by the caller)."""
+        info = np.asarray(self.texture_info, np.uint64).reshape(-1, 5)
+        arr = (native.TextureDesc * max(len(info), 1))()
+        base = self.texture_data.ctypes.data if self.texture_data.size else None
+        at = 0
+        for i, (fmt, w, h, levels, nbytes) in enumerate(info.tolist()):
+            arr[i].format, arr[i].width, arr[i].height, arr[i].level_count = fmt, w, h, levels
+            arr[i].data = (base + at) if base is not None and nbytes else None
+            arr[i].bytes = nbytes
+            at += nbytes
+        return arr
 
     @property
     def triangle_count(self) -> int:
@@ -145,6 +166,9 @@ class SceneArrays:
         d.instance_count = len(self.instances)
         d.emissive_triangle_count = len(self.emissive)
         d.emissive_triangles = native.ptr(self.emissive)
+        self._texture_descs = self.texture_descs()
+        d.textures = ctypes.addressof(self._texture_descs)
+        d.texture_count = len(self.texture_info)
         return d
 
 

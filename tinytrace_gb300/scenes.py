@@ -5,6 +5,7 @@ frames as the reference stores them).
 * `cornell_box()` — the procedural Cornell box: five axis-aligned wall quads and two boxes
   (34 triangles) plus one ceiling light quad (2 triangles) of radiance 15; Lambertian
   OpenPBR base colours red/green/white 0.7 (specular weight 0).
+* `textured_cornell()` — the Cornell box with every texture format in use (see below).
 * `icosphere_field()` — 64 instances of a geodesic sphere (frequency 28: 15,680 triangles)
   with seeded fractal (sum-of-sinusoids) radial displacement of amplitude 0.1, uniform random
   rotations, translations in a 100^3 box and scales in [4, 12]; OpenPBR metalness U{0,1} and
@@ -89,6 +90,61 @@ def cornell_box(light_radiance: float = 15.0) -> AssetScene:
     items.append((_box((0.1, 0.0, 0.0), (0.7, 0.6, 0.6), -0.3), white))                # short box
     for (pos, idx, nrm, uv), mat in items:
         m = s.insert_mesh(pos, uv, idx, nrm)
+        s.root.children.append(Node(models=[Model(m, mat)]))
+    return s
+
+
+def _checker(h: int, w: int, cells: int, a, b) -> np.ndarray:
+    y, x = np.mgrid[0:h, 0:w]
+    m = ((x * cells // w + y * cells // h) % 2).astype(bool)
+    return np.where(m[..., None], np.asarray(a, np.float32), np.asarray(b, np.float32)).astype(np.float32)
+
+
+def textured_cornell(seed: int = 5) -> AssetScene:
+    """The Cornell box with textured materials covering every texture format and the slots
+    the renderer samples: a BC1 checker base colour and an R8 roughness ramp on the floor
+    (texture coordinates repeating 4 x), a BC5 normal map (seeded bumps) on the back wall, an
+    R8 metalness stripe texture of odd extent (22 x 38, partial blocks) on the tall box, and an
+    emissive light with BC1 colour and R16F luminance textures."""
+    rng = np.random.default_rng(seed)
+    s = AssetScene()
+    white = s.insert_material(lambertian((0.7, 0.7, 0.7)))
+    red = s.insert_material(lambertian((0.7, 0.05, 0.05)))
+    green = s.insert_material(lambertian((0.05, 0.7, 0.05)))
+    floor = s.insert_material(Material(specular_weight=1.0, textures={
+        "base_color": _checker(256, 256, 8, (0.8, 0.75, 0.7), (0.15, 0.2, 0.3)),
+        "specular_roughness": np.tile(np.linspace(0.1, 0.9, 64, dtype=np.float32), (64, 1)),
+    }))
+    yy, xx = np.mgrid[0:64, 0:64] / 64.0
+    bumps = np.stack([0.3 * np.sin(2 * np.pi * 4 * xx + rng.uniform(0, 6)),
+                      0.3 * np.cos(2 * np.pi * 3 * yy + rng.uniform(0, 6)), np.ones_like(xx)], -1)
+    bumps /= np.linalg.norm(bumps, axis=-1, keepdims=True)
+    back = s.insert_material(Material(base_color=(0.6, 0.6, 0.6), specular_weight=0.5,
+                                       textures={"geometry_normal": bumps.astype(np.float32)}))
+    stripes = ((np.arange(22)[None, :] // 3 + np.arange(38)[:, None] // 5) % 2).astype(np.float32)
+    metal = s.insert_material(Material(base_color=(0.9, 0.6, 0.3), specular_roughness=0.35,
+                                       textures={"base_metalness": stripes}))
+    lum = (10.0 + 20.0 * rng.random((16, 16))).astype(np.float32)
+    light = s.insert_material(Material(base_color=(0.7, 0.7, 0.7), specular_weight=0.0, textures={
+        "emission_color": _checker(32, 32, 4, (1.0, 0.9, 0.7), (0.7, 0.8, 1.0)),
+        "emission_luminance": lum,
+    }))
+    items = []
+    items.append((_quad((-0.25, 1.98, -0.25), (0.25, 1.98, -0.25), (0.25, 1.98, 0.25), (-0.25, 1.98, 0.25)), light))
+    items.append((_quad((-1, 0, 1), (1, 0, 1), (1, 0, -1), (-1, 0, -1)), floor, 4.0))
+    items.append((_quad((-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)), white))
+    items.append((_quad((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)), back))
+    items.append((_quad((-1, 0, 1), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1)), red))
+    items.append((_quad((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)), green))
+    items.append((_box((-0.65, 0.0, -0.6), (-0.05, 1.2, 0.0), 0.3), metal))
+    items.append((_box((0.1, 0.0, 0.0), (0.7, 0.6, 0.6), -0.3), white))
+    for item in items:
+        (pos, idx, nrm, uv), mat = item[0], item[1]
+        scale = item[2] if len(item) > 2 else 1.0
+        tangents = None
+        if mat == back:  # tangent along +x for the normal map
+            tangents = np.tile(np.array([1.0, 0.0, 0.0, 1.0], np.float32), (len(pos), 1))
+        m = s.insert_mesh(pos, uv * np.float32(scale), idx, nrm, tangents)
         s.root.children.append(Node(models=[Model(m, mat)]))
     return s
 
