@@ -11,9 +11,24 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from tinytrace_gb300 import gltf
+from tinytrace_gb300 import asset, gltf
 from tinytrace_gb300.camera import Camera
 from tinytrace_gb300.renderer import Config, SceneArrays, flatten_scene, make_constants
+
+def _png_rgba(img: np.ndarray) -> bytes:
+    """A minimal RGBA8 PNG (filter 0) of an (h, w, 4) uint8 image."""
+    import zlib
+
+    def chunk(kind, body):
+        return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+
+    h, w = img.shape[:2]
+    raw = b"".join(b"\0" + img[y].tobytes() for y in range(h))
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0))
+            + chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+
+
+IMAGE = np.random.default_rng(3).integers(0, 256, (8, 8, 4)).astype(np.uint8)
 
 QUAD_POS = np.array([[-1, 0, -1], [1, 0, -1], [1, 0, 1], [-1, 0, 1]], np.float32)
 QUAD_IDX = np.array([0, 2, 1, 0, 3, 2], np.uint16)
@@ -49,9 +64,13 @@ def _doc(uri):
             {"emissiveFactor": [1.0, 0.9, 0.8], "pbrMetallicRoughness": {"metallicFactor": 0.0},
              "extensions": {"KHR_materials_emissive_strength": {"emissiveStrength": 30.0}}},
             {"pbrMetallicRoughness": {"baseColorFactor": [0.2, 0.4, 0.6, 1.0],
-                                      "baseColorTexture": {"index": 0}},
+                                      "baseColorTexture": {"index": 0},
+                                      "metallicRoughnessTexture": {"index": 0}, "roughnessFactor": 0.5},
+             "normalTexture": {"index": 0},
              "extensions": {"KHR_materials_transmission": {"transmissionFactor": 0.5}}},
         ],
+        "images": [{"uri": "data:image/png;base64," + base64.b64encode(_png_rgba(IMAGE)).decode()}],
+        "textures": [{"source": 0}],
         "meshes": [
             {"primitives": [{"attributes": {"POSITION": 0, "NORMAL": 3}, "indices": 1, "material": 0}]},
             {"primitives": [{"attributes": {"POSITION": 2}, "material": 1},
@@ -94,14 +113,24 @@ def _write(tmp_path: Path, kind: str) -> Path:
 def test_import(tmp_path, kind):
     imp = gltf.load(_write(tmp_path, kind))
     s = imp.scene
-    assert imp.meshes == 3 and imp.materials == 3 and imp.ignored_textures == 1  # (mesh, primitive) pairs
+    assert imp.meshes == 3 and imp.materials == 3 and imp.ignored_textures == 0  # (mesh, primitive) pairs
     mats = s.material_array["constants"]
     assert np.allclose(mats[0]["base_color"][:3], [0.6, 0.5, 0.4]) and np.isclose(mats[0]["specular_roughness"], 0.7)
     assert np.isclose(mats[0]["specular_ior"], 1.33) and np.isclose(mats[0]["specular_weight"], 0.5)
     assert np.isclose(mats[1]["emission_luminance"], 30.0) and np.allclose(mats[1]["emission_color"][:3], [1, 0.9, 0.8])
     assert np.isclose(mats[1]["specular_roughness"], 1.0)  # glTF default roughness
     assert np.isclose(mats[2]["transmission_weight"], 0.5)
-    assert np.allclose(mats[2]["transmission_color"][:3], [0.8, 0.6, 0.4])
+    # textured parameters: constants zero, textures processed (gltf.rs:259-305)
+    assert np.array_equal(mats[2]["base_color"], [0, 0, 0, 0]) and mats[2]["base_metalness"] == 0.0
+    slots = s.material_array["textures"][2]
+    from tinytrace_gb300 import texture
+    used = {texture.SLOTS[k] for k in range(27) if slots[k] != 0xFFFFFFFF}
+    assert used == {"base_color", "base_metalness", "specular_roughness", "geometry_normal", "transmission_color"}
+    assert len(s.textures) == 5
+    t = s.textures[slots[texture.SLOTS.index("specular_roughness")]]
+    assert t.format == texture.TT_TEXTURE_R8_UNORM and (t.width, t.height) == (8, 8)
+    g = IMAGE[..., 1].astype(np.float32) / np.float32(255) * np.float32(0.5)
+    assert t.levels[0] == asset.quantize_unorm(g, 8).astype(np.uint8).tobytes()
     instances, emissive = flatten_scene(s)
     assert len(instances) == 3 and len(emissive) == 1
     # the light triangle: parent translation (0, 1.5, 0) * rotation of 180 degrees about x * scale 2

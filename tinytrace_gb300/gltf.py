@@ -12,11 +12,19 @@ into an `asset.Scene`, following the reference importer (src/asset/gltf.rs):
 * the node tree of the default scene (or the first scene), node matrices or TRS composed as
   T * R * S.
 
-Differences from the reference: textures are not loaded (the renderer takes constant
-materials; a textured parameter keeps its factor and the texture is counted in
-`Import.ignored_textures`), tangents missing from the file come from
-`asset.default_tangents` instead of mikktspace, and `.glb` containers are read (the
-reference rejects them).
+* textures (gltf.rs:86-137, 259-366): PNG images (from files, data URIs or buffer views)
+  decoded to 8-bit RGBA, scaled to [0, 1] and multiplied by their factors: base colour
+  (x baseColorFactor), metallic (blue) and roughness (green) x their factors, normals
+  (rgb * 2 - 1), emission (x emissiveFactor), specular weight (alpha x specularFactor),
+  specular colour (x specularColorFactor); a transmission texture sets the specular weight
+  (transmission x red), as the reference does; the transmission colour follows a textured
+  base colour as 1 - colour.
+
+Differences from the reference: tangents missing from the file come from
+`asset.default_tangents` instead of mikktspace; `.glb` containers are read (the reference
+rejects them); images that are not PNG are skipped and counted in
+`Import.ignored_textures` (the reference panics); grey PNGs become RGB (the reference
+reinterprets their bytes as RGBA).
 """
 from __future__ import annotations
 
@@ -28,6 +36,7 @@ from pathlib import Path
 
 import numpy as np
 
+from . import png
 from .asset import Material, Model, Node, Scene
 
 COMPONENT = {5120: np.int8, 5121: np.uint8, 5122: np.int16, 5123: np.uint16, 5125: np.uint32, 5126: np.float32}
@@ -125,6 +134,29 @@ def _node_matrix(node: dict) -> np.ndarray:
     return t @ r @ s
 
 
+def _image_rgba(doc: dict, reader: _Reader, base: Path, texture_index: int, cache: dict) -> np.ndarray | None:
+    """(h, w, 4) float32 RGBA in [0, 1] of a glTF texture (dequantize_unorm of its 8-bit
+    samples), or None for an image that is not PNG."""
+    source = doc["textures"][texture_index]["source"]
+    if source in cache:
+        return cache[source]
+    img = doc["images"][source]
+    if "bufferView" in img:
+        view = doc["bufferViews"][img["bufferView"]]
+        start = view.get("byteOffset", 0)
+        data = bytes(reader.buffers[view["buffer"]][start:start + view["byteLength"]])
+    elif img.get("uri", "").startswith("data:"):
+        data = base64.b64decode(img["uri"].split(",", 1)[1])
+    else:
+        data = (base / img["uri"]).read_bytes()
+    try:
+        rgba = png.decode(data).astype(np.float32) / np.float32(255.0)
+    except png.PngError:
+        rgba = None
+    cache[source] = rgba
+    return rgba
+
+
 def load(path: str | Path, scene: Scene | None = None) -> Import:
     """Imports the file's default scene into `scene` (a new one by default)."""
     path = Path(path)
@@ -133,7 +165,17 @@ def load(path: str | Path, scene: Scene | None = None) -> Import:
     scene = scene if scene is not None else Scene()
     mesh_cache: dict[tuple[int, int], int] = {}
     material_cache: dict[int, int] = {}
+    image_cache: dict[int, np.ndarray | None] = {}
     ignored = 0
+
+    def image(info: dict | None) -> np.ndarray | None:
+        nonlocal ignored
+        if info is None:
+            return None
+        rgba = _image_rgba(doc, reader, path.parent, info["index"], image_cache)
+        if rgba is None:
+            ignored += 1
+        return rgba
 
     def material(index: int | None) -> int:
         nonlocal ignored
@@ -144,27 +186,54 @@ def load(path: str | Path, scene: Scene | None = None) -> Import:
         pbr = src.get("pbrMetallicRoughness", {})
         ext = src.get("extensions", {})
         m = Material()
-        base = pbr.get("baseColorFactor", [1.0, 1.0, 1.0, 1.0])
+        f32 = np.float32
+        base = np.asarray(pbr.get("baseColorFactor", [1.0, 1.0, 1.0, 1.0]), f32)
         m.base_color = tuple(float(v) for v in base[:3])
-        m.base_metalness = float(pbr.get("metallicFactor", 1.0))
-        m.specular_roughness = float(pbr.get("roughnessFactor", 1.0))
-        m.emission_color = tuple(float(v) for v in src.get("emissiveFactor", [0.0, 0.0, 0.0]))
+        tex = image(pbr.get("baseColorTexture"))
+        if tex is not None:
+            m.textures["base_color"] = (base * tex)[..., :3]
+        metalness = f32(pbr.get("metallicFactor", 1.0))
+        roughness = f32(pbr.get("roughnessFactor", 1.0))
+        m.base_metalness, m.specular_roughness = float(metalness), float(roughness)
+        tex = image(pbr.get("metallicRoughnessTexture"))
+        if tex is not None:
+            m.textures["base_metalness"] = tex[..., 2] * metalness
+            m.textures["specular_roughness"] = tex[..., 1] * roughness
+        tex = image(src.get("normalTexture"))
+        if tex is not None:
+            m.textures["geometry_normal"] = tex[..., :3] * f32(2.0) - f32(1.0)
+        emissive = np.asarray(src.get("emissiveFactor", [0.0, 0.0, 0.0]), f32)
+        m.emission_color = tuple(float(v) for v in emissive)
+        tex = image(src.get("emissiveTexture"))
+        if tex is not None:
+            m.textures["emission_color"] = emissive * tex[..., :3]
         if "KHR_materials_emissive_strength" in ext:
             m.emission_luminance = float(ext["KHR_materials_emissive_strength"].get("emissiveStrength", 1.0))
         if "KHR_materials_specular" in ext:
             spec = ext["KHR_materials_specular"]
-            m.specular_weight = float(spec.get("specularFactor", 1.0))
-            m.specular_color = tuple(float(v) for v in spec.get("specularColorFactor", [1.0, 1.0, 1.0]))
-            ignored += sum(k in spec for k in ("specularTexture", "specularColorTexture"))
+            factor = f32(spec.get("specularFactor", 1.0))
+            color = np.asarray(spec.get("specularColorFactor", [1.0, 1.0, 1.0]), f32)
+            m.specular_weight = float(factor)
+            m.specular_color = tuple(float(v) for v in color)
+            tex = image(spec.get("specularTexture"))
+            if tex is not None:
+                m.textures["specular_weight"] = tex[..., 3] * factor
+            tex = image(spec.get("specularColorTexture"))
+            if tex is not None:
+                m.textures["specular_color"] = color * tex[..., :3]
         if "KHR_materials_ior" in ext:
             m.specular_ior = float(ext["KHR_materials_ior"].get("ior", 1.5))
         if "KHR_materials_transmission" in ext:
             tr = ext["KHR_materials_transmission"]
-            m.transmission_weight = float(tr.get("transmissionFactor", 0.0))
+            factor = f32(tr.get("transmissionFactor", 0.0))
+            tex = image(tr.get("transmissionTexture"))
+            if tex is not None:  # gltf.rs:358-365 assigns it to the specular weight
+                m.textures["specular_weight"] = factor * tex[..., 0]
+            else:
+                m.transmission_weight = float(factor)
             m.transmission_color = tuple(1.0 - c for c in m.base_color)
-            ignored += "transmissionTexture" in tr
-        ignored += sum(k in pbr for k in ("baseColorTexture", "metallicRoughnessTexture"))
-        ignored += sum(k in src for k in ("normalTexture", "emissiveTexture"))
+            if "base_color" in m.textures:
+                m.textures["transmission_color"] = f32(1.0) - m.textures["base_color"]
         material_cache[key] = scene.insert_material(m)
         return material_cache[key]
 
