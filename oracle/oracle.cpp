@@ -227,6 +227,8 @@ struct RSurface {
     v3 pos{}, normal{}, tangent{}, wi{};
     float dist = 0.0f;
     uint32_t material = 0, instance = 0, seed = 0;
+    v2 uv{};          // texture coordinates of the hit
+    float mip = 0.0f; // mip level of the primary hit (integrate.glsl:134-139)
 };
 struct RRes {
     uint32_t light;
@@ -240,10 +242,13 @@ RRes r_empty() { return RRes{R_NO_LIGHT, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0
 struct RState {  // shading state rebuilt from a G-buffer record
     v3 pos, wi;
     Basis basis;
+    MaterialConstants mat;  // the material with its textures sampled at the hit
     const MaterialConstants* mc;
     Lobes lobes;
     uint32_t seed;
     float dist;
+    v2 uv;
+    float mip;
 };
 bool r_load(const OracleScene& s, const RSurface& q, RState& st) {
     if (!q.hit) return false;
@@ -254,7 +259,10 @@ bool r_load(const OracleScene& s, const RSurface& q, RState& st) {
     st.basis.bitangent = normalize(cross(q.normal, q.tangent));
     st.wi = q.wi;
     st.seed = q.seed;
-    st.mc = &s.materials[q.material].constants;
+    st.uv = q.uv;
+    st.mip = q.mip;
+    st.mat = load_textures(s.materials[q.material], s.textures, q.uv, q.mip);
+    st.mc = &st.mat;
     Generator g{q.seed};
     st.lobes = bsdf_prepare(*st.mc, st.wi, g);
     return true;
@@ -274,8 +282,10 @@ RLight r_light(const OracleScene& s, uint32_t light, float r1, float r2) {
     RLight L;
     L.area = fmx(0.00001f, 0.5f * length(e));
     L.normal = normalize(e);
-    L.pos = interp3(sample_triangle(v2{r1, r2}), p[0], p[1], p[2]);
-    L.emission = material_emissive(s.materials[in.material_index]);
+    v3 bary = sample_triangle(v2{r1, r2});
+    L.pos = interp3(bary, p[0], p[1], p[2]);
+    v2 uv = interp2(bary, uv_of(t.uv[0]), uv_of(t.uv[1]), uv_of(t.uv[2]));
+    L.emission = material_emissive(s.materials[in.material_index], s.textures, uv, 4.0f);
     L.instance = t.instance_index;
     return L;
 }
@@ -371,8 +381,10 @@ RSurface r_gbuffer(const RestirOracle& R, const Constants& c, uint32_t x, uint32
     RSurface q;
     q.seed = g.state;
     if (!h.hit) return q;
-    RayHit hit = get_ray_hit(s, c, h, 1u, ndc, org);  // constant materials: no differentials needed
-    const MaterialConstants& mc = s.materials[hit.material_index].constants;
+    RayHit hit = get_ray_hit(s, c, h, 0u, ndc, org);
+    q.mip = calculate_mip_level(hit.uv_ddx, hit.uv_ddy, c.screen_size);
+    q.uv = hit.uv;
+    const MaterialConstants mc = load_textures(s.materials[hit.material_index], s.textures, q.uv, q.mip);
     Basis basis = create_surface_basis(hit.tangent_space, xyz(mc.geometry_normal));
     q.hit = true;
     q.pos = hit.world_position;
@@ -517,7 +529,7 @@ void restir_frame(RestirOracle& R, const Constants& c, float* target) {
         if (!r_load(s, gb[i], st)) {
             radiance = splat3(1.0f);
         } else {
-            radiance = material_emissive(s.materials[gb[i].material]);
+            radiance = material_emissive(s.materials[gb[i].material], s.textures, st.uv, st.mip);
             const RRes& r = out[i];
             if (r.light != R_NO_LIGHT && r.W > 0.0f) {
                 RLight L = r_light(s, r.light, r.r1, r.r2);

@@ -1,6 +1,6 @@
 """ReSTIR DI on the GPU (tt_render_restir) against the CPU oracle, bit for bit: images and the
 final reservoirs of every frame, with a moving camera (temporal reprojection), on scenes with
-few and with many lights."""
+few and with many lights and with textured materials and lights."""
 import numpy as np
 import pytest
 
@@ -24,6 +24,7 @@ CASES = {
     "field": (lambda: scenes.icosphere_field(instances=6, freq=8, lights=300, seed=11), (0.0, 0.0, 0.0), 95.0, 10.0,
               (96, 54)),
     "instanced": (lambda: scenes.instanced_spheres(), (0.0, 0.0, 0.0), 40.0, 6.0, (80, 60)),
+    "textured": (lambda: scenes.textured_cornell(), (0.0, 1.0, 0.0), 3.4, 1.0, (64, 48)),
 }
 
 

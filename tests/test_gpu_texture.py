@@ -1,8 +1,8 @@
 """Textured materials on the GPU against the oracle, bit for bit: texel decoding and
 trilinear filtering of every format (tt_texture_sample_batch), and renders of the textured
 Cornell box (BC1 colour, BC5 normal map, R8 roughness / metalness, R16F and BC1 emission) by
-the wavefront integrator (graph and host loops), the megakernel and the server; scenes with
-malformed textures are rejected."""
+the wavefront integrator (graph and host loops), the megakernel and the server (ReSTIR's
+textured frames are in test_gpu_restir); scenes with malformed textures are rejected."""
 import ctypes
 
 import numpy as np
@@ -104,7 +104,4 @@ def test_textured_scene_rejects(gpu_context):
 
     for m in (bad_index, bad_bytes, bad_levels, bad_format):
         assert create(m) == native.TT_ERR_INVALID_ARGUMENT, m.__name__
-    h = ctx.create_scene(good)  # the context still works
-    img = ctx.create_image(native.TT_LIFETIME_FRAME, 16, 16)
-    c = make_constants(CAMERA, (16, 16), Config(bounce_count=2, sample_count=1), 0, 0)
-    assert ctx.lib.tt_render_restir(ctx.handle, h, native.ptr(c), img) == native.TT_ERR_UNSUPPORTED
+    ctx.create_scene(good)  # the context still works

@@ -64,3 +64,21 @@ def test_deterministic_and_thread_independent():
         R.frame(make_constants(w.camera, w.extent, Config(bounce_count=1, sample_count=1), f, f), img, threads=1)
     assert a.tobytes() == img.tobytes()
     assert Ra.reservoirs().tobytes() == R.reservoirs().tobytes()
+
+
+def test_textured_restir_frames_are_deterministic():
+    from tinytrace_gb300 import scenes
+    from tinytrace_gb300.camera import Camera
+    from tinytrace_gb300.renderer import Config, SceneArrays, make_constants
+
+    a = SceneArrays(scenes.textured_cornell())
+    cam = Camera.looking_at((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), fov=0.8)
+    imgs = []
+    for _ in range(2):
+        R = oracle.OracleRestir(oracle.OracleScene(a), 40, 30)
+        img = np.zeros((30, 40, 4), np.float32)
+        for f in range(2):
+            R.frame(make_constants(cam, (40, 30), Config(bounce_count=1, sample_count=1), f, 0), img)
+        imgs.append(img.copy())
+    assert np.isfinite(imgs[0]).all() and imgs[0][..., :3].max() > 0
+    assert np.array_equal(imgs[0], imgs[1])

@@ -94,7 +94,7 @@ struct WavefrontBuffers {
 // ReSTIR DI state kept between frames: two G-buffers and two final reservoir arrays
 // (current and previous frame), the initial and temporal reservoirs, the previous camera.
 struct RestirState {
-    DeviceBuffer gbuf[2], final_res[2], initial, temporal;
+    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex;
     uint64_t pixels = 0;
     uint32_t cur = 0;
     RestirHistory history{};
@@ -1147,7 +1147,6 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         ImageRes* img = lookup<ImageRes>(ctx, target, KIND_IMAGE);
         require(constants->screen_size[0] == img->width && constants->screen_size[1] == img->height,
                 "constants.screen_size must equal the target extent");
-        if (s->dev.textured) fail(TT_ERR_UNSUPPORTED, "ReSTIR DI shades constant materials only");
         RestirState& R = ctx->restir;
         uint64_t WH = (uint64_t)img->width * img->height;
         if (WH != R.pixels) {
@@ -1165,6 +1164,11 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         p.err = ctx->err_word.as<uint32_t>();
         p.counters = ctx->counters.as<unsigned long long>();
         RestirParams rp;
+        rp.gtex = nullptr;
+        if (s->dev.textured) {
+            if (R.gtex.bytes < 16ull * WH) R.gtex.alloc(16ull * WH);
+            rp.gtex = R.gtex.as<float4>();
+        }
         rp.gbuf = R.gbuf[R.cur].as<Surface>();
         rp.prev_gbuf = R.gbuf[R.cur ^ 1u].as<Surface>();
         rp.initial = R.initial.as<Reservoir>();

@@ -24,11 +24,17 @@ struct ShadingState {
     f3 pos, wi;
     Basis basis;
     const tt_material* material;
+    const MatC* mc;  // the material's constants, or `local` with its textures sampled
+    MatC local;
     Lobes lobes;
     uint32_t seed;
     float dist;
+    f2 uv;
+    float mip;
 };
-__device__ __forceinline__ bool load_surface(const DevScene& sc, const Surface& s, ShadingState& st) {
+template <bool TEX>
+__device__ __forceinline__ bool load_surface(const DevScene& sc, const Surface& s, const float4* gtex, uint64_t i,
+                                             ShadingState& st) {
     uint32_t mat = __float_as_uint(s.normal_mat.w);
     if (mat == NO_SURFACE) return false;
     st.pos = f3{s.pos_dist.x, s.pos_dist.y, s.pos_dist.z};
@@ -39,20 +45,30 @@ __device__ __forceinline__ bool load_surface(const DevScene& sc, const Surface& 
     st.wi = f3{s.wi_seed.x, s.wi_seed.y, s.wi_seed.z};
     st.seed = __float_as_uint(s.wi_seed.w);
     st.material = sc.materials + mat;
+    st.uv = f2{0.0f, 0.0f};
+    st.mip = 0.0f;
+    if (TEX) {
+        float4 t = gtex[i];
+        st.uv = f2{t.x, t.y};
+        st.mip = t.z;
+    }
+    st.mc = &hit_material<TEX>(sc, st.material, st.uv, st.mip, st.local);
     uint32_t g = st.seed;
-    st.lobes = bsdf_prepare(st.material->constants, st.wi, g);
+    st.lobes = bsdf_prepare(*st.mc, st.wi, g);
     return true;
 }
 
+template <bool TEX>
 __device__ __forceinline__ float target_of(const DevScene& sc, const ShadingState& st, uint32_t light, float r1,
                                            float r2) {
     if (light == NO_LIGHT) return 0.0f;
-    LightPoint lp = light_point(sc, light, r1, r2);
-    return luminance(restir_contribution(st.material->constants, st.lobes, st.basis, st.wi, st.pos, lp));
+    LightPoint lp = light_point<TEX>(sc, light, r1, r2);
+    return luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
 }
 
+template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
-                                                                  Surface* gbuf) {
+                                                                  Surface* gbuf, float4* gtex) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     uint32_t x, y;
     const tt_constants& c = p.c;
@@ -74,7 +90,13 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
         s.wi_seed = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(g));
     } else {
         ShadeHit hit = get_ray_hit(sc, h.instance, h.prim, h.u, h.v);
-        const MatC& mc = sc.materials[hit.material_index].constants;
+        float mip = 0.0f;
+        if (TEX) {
+            mip = primary_mip_level(c, hit, org, ndc);
+            gtex[(uint64_t)y * W + x] = make_float4(hit.uv.x, hit.uv.y, mip, 0.0f);
+        }
+        MatC local;
+        const MatC& mc = hit_material<TEX>(sc, sc.materials + hit.material_index, hit.uv, mip, local);
         Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
         f3 wi = transform_from_basis(basis, -dir);
         f3 to = hit.world_position - org;
@@ -86,9 +108,10 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     gbuf[(uint64_t)y * W + x] = s;
 }
 
+template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_constant__ RenderParams p,
-                                                                  const Surface* gbuf, Reservoir* out,
-                                                                  uint32_t candidates) {
+                                                                  const Surface* gbuf, const float4* gtex,
+                                                                  Reservoir* out, uint32_t candidates) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     uint32_t x, y;
     const tt_constants& c = p.c;
@@ -97,7 +120,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_c
     uint64_t i = (uint64_t)y * c.screen_size[0] + x;
     ShadingState st;
     Reservoir r = empty_reservoir();
-    if (load_surface(sc, gbuf[i], st) && sc.emissive_count > 0) {
+    if (load_surface<TEX>(sc, gbuf[i], gtex, i, st) && sc.emissive_count > 0) {
         uint32_t g = jenkins_hash(st.seed + PASS_INITIAL);
         float inv_p_pick = (float)sc.emissive_count;
         float chosen = 0.0f;
@@ -105,14 +128,14 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_c
             uint32_t light = xor_shift(g) % sc.emissive_count;
             float r1 = random_float(g);
             float r2 = random_float(g);
-            LightPoint lp = light_point(sc, light, r1, r2);
-            float ph = luminance(restir_contribution(st.material->constants, st.lobes, st.basis, st.wi, st.pos, lp));
+            LightPoint lp = light_point<TEX>(sc, light, r1, r2);
+            float ph = luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
             float w = ph * (inv_p_pick * lp.area);  // p^ / p, p = 1 / (lights * area)
             if (reservoir_update(r, light, r1, r2, w, 1.0f, g)) chosen = ph;
         }
         r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
         if (r.W > 0.0f) {
-            LightPoint lp = light_point(sc, r.light, r.r1, r.r2);
+            LightPoint lp = light_point<TEX>(sc, r.light, r.r1, r.r2);
             if (!restir_visible<false>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err)) r.W = 0.0f;
         }
     }
@@ -120,10 +143,11 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_c
 }
 
 // Merges reservoir q (from another pixel or frame) into r, re-targeted at this pixel.
+template <bool TEX>
 __device__ __forceinline__ void merge(const DevScene& sc, const ShadingState& st, Reservoir& r, const Reservoir& q,
                                       float m_cap, float& chosen, uint32_t& g) {
     float m = fmn(q.M, m_cap);
-    float ph = target_of(sc, st, q.light, q.r1, q.r2);
+    float ph = target_of<TEX>(sc, st, q.light, q.r1, q.r2);
     float w = ph * q.W * m;
     if (reservoir_update(r, q.light, q.r1, q.r2, w, m, g)) chosen = ph;
 }
@@ -164,9 +188,11 @@ __device__ __forceinline__ bool similar(const Surface& q, f3 normal, float dist)
     return dot(n, normal) > 0.90630779f && fabsf(q.pos_dist.w - dist) <= 0.1f * dist;
 }
 
+template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_constant__ RenderParams p,
                                                                    const __grid_constant__ RestirHistory hist,
-                                                                   const Surface* gbuf, const Surface* prev_gbuf,
+                                                                   const Surface* gbuf, const float4* gtex,
+                                                                   const Surface* prev_gbuf,
                                                                    const Reservoir* initial, const Reservoir* prev,
                                                                    Reservoir* out, float m_cap) {
     uint32_t x, y;
@@ -178,7 +204,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_
     Reservoir cur = initial[i];
     ShadingState st;
     uint32_t px, py;
-    if (!hist.valid || !load_surface(sc, gbuf[i], st) || !reproject(hist, st.pos, W, H, px, py)) {
+    if (!hist.valid || !load_surface<TEX>(sc, gbuf[i], gtex, i, st) || !reproject(hist, st.pos, W, H, px, py)) {
         out[i] = cur;
         return;
     }
@@ -191,14 +217,16 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_
     uint32_t g = jenkins_hash(st.seed + PASS_TEMPORAL);
     Reservoir r = empty_reservoir();
     float chosen = 0.0f;
-    merge(sc, st, r, cur, cur.M, chosen, g);
-    merge(sc, st, r, prev[j], m_cap, chosen, g);
+    merge<TEX>(sc, st, r, cur, cur.M, chosen, g);
+    merge<TEX>(sc, st, r, prev[j], m_cap, chosen, g);
     r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
     out[i] = r;
 }
 
+template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_constant__ RenderParams p,
-                                                                  const Surface* gbuf, const Reservoir* in,
+                                                                  const Surface* gbuf, const float4* gtex,
+                                                                  const Reservoir* in,
                                                                   Reservoir* out, uint32_t neighbours, float radius) {
     uint32_t x, y;
     const tt_constants& c = p.c;
@@ -208,14 +236,14 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
     uint64_t i = (uint64_t)y * W + x;
     ShadingState st;
     Reservoir cur = in[i];
-    if (!load_surface(sc, gbuf[i], st)) {
+    if (!load_surface<TEX>(sc, gbuf[i], gtex, i, st)) {
         out[i] = cur;
         return;
     }
     uint32_t g = jenkins_hash(st.seed + PASS_SPATIAL);
     Reservoir r = empty_reservoir();
     float chosen = 0.0f;
-    merge(sc, st, r, cur, cur.M, chosen, g);
+    merge<TEX>(sc, st, r, cur, cur.M, chosen, g);
     for (uint32_t k = 0; k < neighbours; ++k) {
         float rr = radius * sqrtf(random_float(g));
         float angle = TAU * random_float(g);
@@ -226,14 +254,16 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
         uint64_t j = (uint64_t)(uint32_t)qy * W + (uint32_t)qx;
         if (j == i || !similar(gbuf[j], st.basis.normal, st.dist)) continue;
         const Reservoir q = in[j];
-        merge(sc, st, r, q, q.M, chosen, g);
+        merge<TEX>(sc, st, r, q, q.M, chosen, g);
     }
     r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
     out[i] = r;
 }
 
+template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_constant__ RenderParams p,
-                                                                const Surface* gbuf, const Reservoir* res) {
+                                                                const Surface* gbuf, const float4* gtex,
+                                                                const Reservoir* res) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     uint32_t x, y;
     const tt_constants& c = p.c;
@@ -243,14 +273,14 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
     uint64_t i = (uint64_t)y * W + x;
     ShadingState st;
     f3 radiance;
-    if (!load_surface(sc, gbuf[i], st)) {
+    if (!load_surface<TEX>(sc, gbuf[i], gtex, i, st)) {
         radiance = splat(1.0f);  // the white sky of integrate.glsl:272-276
     } else {
-        radiance = material_emissive(st.material);
+        radiance = hit_emissive<TEX>(sc, st.material, st.uv, st.mip);
         Reservoir r = res[i];
         if (r.light != NO_LIGHT && r.W > 0.0f) {
-            LightPoint lp = light_point(sc, r.light, r.r1, r.r2);
-            f3 contrib = restir_contribution(st.material->constants, st.lobes, st.basis, st.wi, st.pos, lp);
+            LightPoint lp = light_point<TEX>(sc, r.light, r.r1, r.r2);
+            f3 contrib = restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp);
             if (restir_visible<false>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err))
                 radiance += contrib * r.W;
         }
@@ -264,16 +294,22 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
     *tp = make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
 }
 
-void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {
+template <bool TEX>
+static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {
     const tt_constants& c = p.c;
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
-    restir_gbuffer_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf);
-    restir_initial_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.initial, rp.candidates);
-    restir_temporal_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.prev_gbuf, rp.initial, rp.prev,
-                                                      rp.temporal, rp.m_cap);
-    restir_spatial_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.temporal, rp.final_out, rp.neighbours,
-                                                     rp.radius);
-    restir_shade_kernel<<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.final_out);
+    restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex);
+    restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.initial, rp.candidates);
+    restir_temporal_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.prev_gbuf, rp.initial,
+                                                           rp.prev, rp.temporal, rp.m_cap);
+    restir_spatial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.temporal, rp.final_out,
+                                                          rp.neighbours, rp.radius);
+    restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.final_out);
+}
+
+void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {
+    if (p.sc.textured && rp.gtex) restir_passes<true>(p, rp, st);
+    else restir_passes<false>(p, rp, st);
 }
 
 }  // namespace tt

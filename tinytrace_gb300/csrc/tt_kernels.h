@@ -115,6 +115,7 @@ struct Surface;
 struct Reservoir;
 struct RestirParams {
     Surface *gbuf, *prev_gbuf;
+    float4* gtex;  // textured scenes: per pixel (u, v, mip level, 0) of the primary hit; else null
     Reservoir *initial, *temporal, *final_out, *prev;
     RestirHistory history;
     uint32_t candidates, neighbours;

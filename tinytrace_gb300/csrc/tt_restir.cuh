@@ -58,6 +58,7 @@ struct LightPoint {
     float area;
     uint32_t instance;
 };
+template <bool TEX>
 __device__ __forceinline__ LightPoint light_point(const DevScene& sc, uint32_t light, float r1, float r2) {
     const tt_emissive_triangle* tri = sc.emissive + light;
     LightPoint lp;
@@ -75,8 +76,16 @@ __device__ __forceinline__ LightPoint light_point(const DevScene& sc, uint32_t l
     f3 e = cross(p[1] - p[0], p[2] - p[0]);
     lp.area = fmx(0.00001f, 0.5f * length(e));
     lp.normal = normalize(e);
-    lp.pos = interp3(sample_triangle(f2{r1, r2}), p[0], p[1], p[2]);
-    lp.emission = material_emissive(sc.materials + __ldg(&in->material_index));
+    f3 bary = sample_triangle(f2{r1, r2});
+    lp.pos = interp3(bary, p[0], p[1], p[2]);
+    f2 uv = f2{0.0f, 0.0f};
+    if (TEX) {
+        uint32_t tc[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) tc[k] = __ldg(reinterpret_cast<const uint32_t*>(&tri->texture_coordinates[k]));
+        uv = interp_uv(bary, tc[0], tc[1], tc[2]);
+    }
+    lp.emission = hit_emissive<TEX>(sc, sc.materials + __ldg(&in->material_index), uv, 4.0f);
     return lp;
 }
 
