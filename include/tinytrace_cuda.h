@@ -365,11 +365,17 @@ int32_t tt_restir_download(tt_context* ctx, void* reservoirs, uint64_t bytes);
  * units, 3 outputs; queries are 12 floats: pos xyz, dir xyz, normal xyz, roughness, 0, 0. */
 #define TT_CACHE_WEIGHTS 16896u          /* 4 x 64 x 64 hidden weights + 8 x 64 output rows (3 used) */
 #define TT_CACHE_GRID_FLOATS 16777216u   /* 16 levels x 2^19 entries x 2 features */
+/* Defaults of a context that was never configured: {1e-2, 262144, 1, 1, 0.01}. */
 typedef struct tt_cache_config {
-    float learning_rate;            /* Adam step size (1e-2) */
-    uint32_t train_paths_per_frame; /* paths traced to full depth to produce training radiance (65536) */
-    uint32_t terminate_depth;       /* other paths end in the cache at this vertex (2) */
+    float learning_rate;            /* Adam step size */
+    uint32_t train_paths_per_frame; /* paths traced to full depth to produce training radiance */
+    uint32_t terminate_depth;       /* other paths end in the cache at this vertex, or, with a spread
+                                       threshold, at the first vertex from this depth on whose path
+                                       spread exceeds it */
     uint32_t seed;                  /* parameter initialisation */
+    float spread_threshold;         /* 0: end at terminate_depth; c > 0: the path-spread rule of neural
+                                       radiance caching (Mueller et al. 2021): end where
+                                       sum_i sqrt(d_i^2 / (p_i |cos_i|)) > c * sqrt(d_1^2 / (4 pi |cos_1|)) */
 } tt_cache_config;
 /* (Re)initialises the cache with `config`; tt_set_option(TT_OPTION_RADIANCE_CACHE, 1) makes
  * tt_render use it. */

@@ -115,18 +115,19 @@ def test_learns_a_smooth_field(gpu_context):
     assert err < 0.1, err
 
 
-def _cache_renderer(extent=(96, 54), spp=8, depth=6, terminate=2, train_paths=4096):
+def _cache_renderer(extent=(96, 54), spp=8, depth=6, terminate=2, train_paths=4096, spread=0.0, scene=None,
+                    camera=None):
     from tinytrace_gb300 import scenes
     from tinytrace_gb300.renderer import Config, Renderer
 
-    w = scenes.Workload("field_small", scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11),
-                        scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)), extent,
+    w = scenes.Workload("field_small", scene or scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11),
+                        camera or scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)), extent,
                         Config(bounce_count=depth, sample_count=spp))
     r = Renderer(w.extent)
     r.set_scene(w.scene)
     r.camera = w.camera
     r.set_config(w.config)
-    cfg = native.CacheConfig(1e-2, train_paths, terminate, 1)
+    cfg = native.CacheConfig(1e-2, train_paths, terminate, 1, spread)
     check(r.context.lib.tt_cache_configure(r.context.handle, ctypes.byref(cfg)))
     return r, w
 
@@ -167,4 +168,47 @@ def test_cached_render_trains_and_stays_close(gpu_context):
     assert np.mean(losses[-4:]) < np.mean(losses[:4])
     a, b = img[..., :3].mean(), plain[..., :3].mean()
     assert abs(a - b) <= 0.15 * b, (a, b)
+    r.close()
+
+
+def test_spread_rule_without_termination_is_the_plain_tracer(gpu_context):
+    """With the path-spread rule and a threshold no path reaches, no path ends in the cache:
+    the image is the plain path tracer's bit for bit."""
+    from conftest import assert_same_bits
+    from oracle import oracle
+    from tinytrace_gb300.renderer import make_constants
+
+    r, w = _cache_renderer(terminate=1, spread=1e30)
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_RADIANCE_CACHE, 1))
+    c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
+    assert_same_bits(r.render_to_texture(), oracle.OracleScene(r.scene_arrays).render(c), "spread rule, no ending")
+    r.close()
+
+
+def test_spread_rule_in_a_closed_room(gpu_context):
+    """The path-spread rule in the textured Cornell box (every path bounces to full depth):
+    after online training the frame mean is within 10 % of the plain tracer's and the cached
+    frames are faster."""
+    import time
+
+    from tinytrace_gb300 import scenes
+
+    cam = scenes.Camera.looking_at((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), fov=0.75)
+    r, w = _cache_renderer(extent=(256, 192), spp=16, depth=8, terminate=1, train_paths=16384, spread=0.01,
+                           scene=scenes.textured_cornell(), camera=cam)
+    plain = np.zeros((192, 256, 3))
+    for f in range(4):
+        r.reset_accumulation()
+        plain += r.render_to_texture()[..., :3] / 4
+        r.present()
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_RADIANCE_CACHE, 1))
+    for f in range(32):
+        r.reset_accumulation()
+        img = r.render_to_texture()
+        r.present()
+    st = native.CacheStatus()
+    check(r.context.lib.tt_cache_status_get(r.context.handle, ctypes.byref(st)))
+    assert np.isfinite(img).all() and st.pairs > 1000 and st.steps >= 32
+    a, b = img[..., :3].mean(), plain.mean()
+    assert abs(a - b) <= 0.10 * b, (a, b)
     r.close()

@@ -105,12 +105,12 @@ struct RestirState {
 // (queued queries, training records and pairs).
 struct CacheState {
     DeviceBuffer grid, grid_m, grid_v, grid_grad, w, w_m, w_v, w_grad, w16, loss;
-    DeviceBuffer cq, cq_slot, cq_out, rec, train_final, tq, tt, tcount;
+    DeviceBuffer cq, cq_slot, cq_out, rec, train_final, tq, tt, tcount, spread;
     uint64_t cq_cap = 0, rec_cap = 0, final_cap = 0;
     bool enabled = false;
     float last_loss = 0.0f;
     uint32_t last_pairs = 0;
-    tt_cache_config config{1e-2f, 65536u, 2u, 1u};
+    tt_cache_config config{1e-2f, 262144u, 1u, 1u, 0.01f};
     uint32_t step = 0;
     bool ready = false;
     CacheDevice dev() const {
@@ -524,6 +524,7 @@ static void cache_frame_buffers(tt_context* ctx, const tt_constants& c, const De
         C.cq.alloc(48ull * w.P);
         C.cq_slot.alloc(4ull * w.P);
         C.cq_out.alloc(12ull * w.P);
+        C.spread.alloc(16ull * w.P);
         C.cq_cap = w.P;
     }
     uint64_t items = (uint64_t)c.screen_size[0] * c.screen_size[1] * c.sample_count;
@@ -545,6 +546,8 @@ static void cache_frame_buffers(tt_context* ctx, const tt_constants& c, const De
     if (!C.tcount.ptr) C.tcount.alloc(16);
     w.cache_on = 1u;
     w.cache_depth = C.config.terminate_depth;
+    w.spread_c = C.config.spread_threshold;
+    w.spread = C.spread.as<float4>();
     w.train_stride = (uint32_t)stride;
     w.rec_cap = (uint32_t)std::min<uint64_t>(C.rec_cap, 0xffffffffull);
     w.cache_bound = sc.tlas_bound > 0.0f ? sc.tlas_bound : 1.0f;
@@ -1213,6 +1216,7 @@ int32_t tt_cache_configure(tt_context* ctx, const tt_cache_config* config) {
         require(ctx && config, "null argument");
         require(config->learning_rate > 0.0f && std::isfinite(config->learning_rate), "bad learning rate");
         require(config->terminate_depth >= 1, "terminate_depth must be at least 1");
+        require(config->spread_threshold >= 0.0f && std::isfinite(config->spread_threshold), "bad spread threshold");
         use_device(ctx);
         ctx->cache.config = *config;
         ctx->cache.ready = false;

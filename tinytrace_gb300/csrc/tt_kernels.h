@@ -53,6 +53,8 @@ struct WfParams {
     // learned radiance cache (cache_on = 0: off)
     uint32_t cache_on, cache_depth, train_stride, rec_cap;
     float cache_bound;      // positions map to the unit cube as p / bound * 0.5 + 0.5
+    float spread_c;         // > 0: end paths by their spread (tt_cache_config.spread_threshold)
+    float4* spread;         // per slot: spread sum, primary footprint a0, pdf of the last direction
     CacheQuery* cq;         // queued queries (P)
     uint32_t* cq_slot;      // their slots
     float* cq_out;          // their radiance (3 P)

@@ -129,6 +129,7 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
         w.dir[s] = pack(d, pg);
         w.thr[s] = pack(splat(1.0f), item);
         bool train = w.cache_on && ((uint64_t)w.chunk_sample0 * w.WH + item) % w.train_stride == 0u;
+        if (w.cache_on) w.spread[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         w.acc[s] = pack(splat(0.0f), F_LIVE | (train ? F_TRAIN : 0u));
         live = true;
     }
@@ -327,7 +328,21 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
                 qv[8] = basis.normal.z;
                 qv[9] = mc.specular_roughness;
                 qv[10] = qv[11] = 0.0f;
-                want_cache = !train && bounce == w.cache_depth;
+                if (w.spread_c > 0.0f) {
+                    // path spread (neural radiance caching, Mueller et al. 2021, section 4):
+                    // a += sqrt(d^2 / (p |cos|)) per vertex after the first, a0 from a uniform
+                    // sphere pdf at the first; the path ends in the cache once a > c a0
+                    float4 sp = w.spread[s];
+                    f3 seg = hit.world_position - xyz(o4);
+                    float d2 = dot(seg, seg);
+                    float cs = fmaxf(fabsf(dot(basis.normal, ray_dir)), 1e-4f);
+                    if (bounce == 0u) sp.y = sqrtf(d2 / (4.0f * PI * cs));
+                    else sp.x += sqrtf(d2 / (fmaxf(sp.z, 1e-20f) * cs));
+                    w.spread[s] = sp;
+                    want_cache = !train && bounce >= w.cache_depth && sp.x > w.spread_c * sp.y;
+                } else {
+                    want_cache = !train && bounce == w.cache_depth;
+                }
                 want_record = train != 0u;
                 rec_thr = thr;
                 rec_before = acc;
@@ -371,6 +386,7 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
             f3 wo = splat(0.0f);
             int lobe = 0;
             f3 bsdf = bsdf_sample(mc, lobes, wi, g, wo, density, lobe);
+            if (CACHE && w.spread_c > 0.0f) w.spread[s].z = density;
             f3 new_dir = transform_to_basis(basis, wo);
             thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
             uint32_t next = bounce + 1u;

@@ -202,7 +202,7 @@ class RestirConfig(ctypes.Structure):
 
 class CacheConfig(ctypes.Structure):
     _fields_ = [("learning_rate", ctypes.c_float), ("train_paths_per_frame", ctypes.c_uint32),
-                ("terminate_depth", ctypes.c_uint32), ("seed", ctypes.c_uint32)]
+                ("terminate_depth", ctypes.c_uint32), ("seed", ctypes.c_uint32), ("spread_threshold", ctypes.c_float)]
 
 
 class CacheStatus(ctypes.Structure):

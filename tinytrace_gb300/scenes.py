@@ -219,9 +219,29 @@ def _random_rotation(rng: np.random.Generator) -> np.ndarray:
                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
 
 
+def _sphere_textures(rng: np.random.Generator, base_color, size: int = 256) -> dict:
+    """Procedural textures of one textured sphere material: a BC1 base colour (stripes of the
+    material's colour and a random second colour), an R8 roughness noise and, for half of the
+    materials, a BC5 bump normal map."""
+    y, x = np.mgrid[0:size, 0:size] / size
+    k = rng.integers(2, 9, 2)
+    stripes = (np.sin(2 * np.pi * (k[0] * x + k[1] * y)) > 0)[..., None]
+    other = rng.uniform(0.1, 0.9, 3)
+    tex = {"base_color": np.where(stripes, np.asarray(base_color), other).astype(np.float32)}
+    rough = 0.5 + 0.45 * np.sin(2 * np.pi * (rng.integers(1, 6) * x)) * np.cos(2 * np.pi * rng.integers(1, 6) * y)
+    tex["specular_roughness"] = rough[::2, ::2].astype(np.float32)
+    if rng.random() < 0.5:
+        n = np.stack([0.3 * np.sin(2 * np.pi * 6 * x), 0.3 * np.sin(2 * np.pi * 6 * y), np.ones_like(x)], -1)
+        tex["geometry_normal"] = (n / np.linalg.norm(n, axis=-1, keepdims=True))[::2, ::2].astype(np.float32)
+    return tex
+
+
 def icosphere_field(instances: int = 64, freq: int = 28, lights: int = 1000, seed: int = 7,
-                    box: float = 100.0, displacement: float = 0.1) -> AssetScene:
+                    box: float = 100.0, displacement: float = 0.1, textured: bool = False) -> AssetScene:
+    """`textured`: every sphere's material also samples textures (_sphere_textures, from a
+    separate generator, so the geometry and constants are those of the untextured field)."""
     rng = np.random.default_rng(seed)
+    tex_rng = np.random.default_rng(seed + 1000)
     s = AssetScene()
     half = box / 2.0
     # emissive triangles first (global triangle index < 65535)
@@ -245,9 +265,11 @@ def icosphere_field(instances: int = 64, freq: int = 28, lights: int = 1000, see
         uv = np.stack([np.arctan2(base_pts[:, 2], base_pts[:, 0]) / (2 * np.pi) + 0.5,
                        np.arccos(np.clip(base_pts[:, 1], -1, 1)) / np.pi], axis=1).astype(np.float32)
         m = s.insert_mesh(pts, uv, tris)
-        mat = s.insert_material(Material(base_color=tuple(rng.uniform(0.2, 0.9, 3)),
-                                         base_metalness=float(rng.integers(0, 2)),
-                                         specular_roughness=float(rng.uniform(0.05, 1.0))))
+        material = Material(base_color=tuple(rng.uniform(0.2, 0.9, 3)), base_metalness=float(rng.integers(0, 2)),
+                            specular_roughness=float(rng.uniform(0.05, 1.0)))
+        if textured:
+            material.textures = _sphere_textures(tex_rng, material.base_color)
+        mat = s.insert_material(material)
         t = np.eye(4)
         t[:3, :3] = _random_rotation(rng) * rng.uniform(4.0, 12.0)
         t[:3, 3] = rng.uniform(-half, half, 3)
