@@ -197,6 +197,7 @@ void check_device_errors(tt_context* ctx) {
     uint32_t e = *ctx->err_host;
     if (e & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
     if (e & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
+    if (e & ERR_TENSOR_WAIT) fail(TT_ERR_TIMEOUT, "radiance-cache tensor-core wait limit reached");
 }
 void sync(tt_context* ctx) {
     check_cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
@@ -1231,9 +1232,13 @@ int32_t tt_cache_query(tt_context* ctx, const float* queries, uint32_t n, float*
         use_device(ctx);
         cache_ready(ctx);
         CacheDevice d = ctx->cache.dev();
+        arm_error_word(ctx);
         batch(ctx, queries, 48ull * n, nullptr, 0, radiance, 12ull * n, [&](void* din, void*, void* dout) {
-            cache_infer(d, static_cast<const CacheQuery*>(din), n, static_cast<float*>(dout), ctx->stream);
+            cache_infer(d, static_cast<const CacheQuery*>(din), n, static_cast<float*>(dout),
+                        ctx->err_word.as<uint32_t>(), ctx->stream);
         });
+        fetch_error_word(ctx);
+        sync(ctx);
     });
 }
 

@@ -12,9 +12,9 @@
 //   MLP       64 inputs (32 grid features, direction * 0.5 + 0.5, normal * 0.5 + 0.5,
 //             roughness, zero padding) -> 4 hidden layers of 64 ReLU units -> 3 outputs (RGB,
 //             linear), no biases.  Weights [out][in] row-major, FP32 master copy, FP16 copy.
-//   inference FP16 inputs and weights on the tensor cores (mma.sync m16n8k16, FP32
-//             accumulation), 16 queries per warp, weights staged in shared memory, the hidden
-//             activations passed from accumulator to operand registers between layers.
+//   inference FP16 inputs and weights on the 5th-generation tensor cores (tcgen05.mma, FP32
+//             accumulation in tensor memory), 128 queries per CTA, weights and activations in
+//             shared memory, ReLU and FP16 conversion between layers on the CUDA cores.
 //   training  FP32 on the CUDA cores: forward, relative L2 loss (y - t)^2 / (y^2 + 0.01)
 //             (y not differentiated in the denominator), backward into weight gradients
 //             (shared-memory accumulation, one atomic per weight per block) and grid gradients
@@ -86,101 +86,208 @@ __device__ __forceinline__ void encode(const CacheQuery& q, const float* grid, f
     for (int k = 39; k < CACHE_WIDTH; ++k) x[k] = 0.0f;
 }
 
-// ---------------------------------------------------------------- inference (tensor cores)
+// ---------------------------------------------------------------- inference (tcgen05 tensor cores)
+// One CTA of 128 threads owns 128 queries at a time (thread t: query row t).  Per layer the
+// activations A (128 x 64 FP16) and the layer's weights B (64 x 64 FP16, [out][in]) sit in
+// shared memory in the canonical K-major layout without swizzling: 8-row x 16-byte core
+// matrices, the 8 core matrices of a row group 128 bytes apart along K (leading byte offset)
+// and row groups 1024 bytes apart (stride byte offset).  One thread issues the layer's four
+// tcgen05.mma (M 128, N 64, K 16, FP32 accumulation in 64 TMEM columns) and commits them to
+// an mbarrier; every warp then reads its 32 TMEM lanes (tcgen05.ld 32x32b), applies ReLU,
+// converts to FP16 and writes the next layer's A.  The output layer uses N 16 (3 rows used).
+// Waits on the mbarrier are bounded: past the limit the kernel raises ERR_TENSOR_WAIT, stops
+// issuing, and still releases its TMEM.
+constexpr int TC_THREADS = 128;
+constexpr int TC_ROWS = 128;
+constexpr uint32_t TC_TMEM_COLS = 64;
+constexpr uint32_t TC_OUT_N = 16;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+// dynamic shared memory: hidden weights, output weights, activations, mbarrier, TMEM address
+constexpr uint32_t TC_W_BYTES = CACHE_WIDTH * CACHE_WIDTH * 2;     // 8 KB per hidden layer
+constexpr uint32_t TC_WOUT_BYTES = TC_OUT_N * CACHE_WIDTH * 2;     // 2 KB
+constexpr uint32_t TC_A_BYTES = TC_ROWS * CACHE_WIDTH * 2;         // 16 KB
+constexpr uint32_t TC_OFF_WOUT = CACHE_HIDDEN_LAYERS * TC_W_BYTES;
+constexpr uint32_t TC_OFF_A = TC_OFF_WOUT + TC_WOUT_BYTES;
+constexpr uint32_t TC_OFF_BAR = TC_OFF_A + TC_A_BYTES;
+constexpr uint32_t TC_SMEM = TC_OFF_BAR + 16 + 1024;  // + alignment slack
+
+// Byte offset of element (row, k) of a 64-wide K-major operand in the core-matrix layout.
+__device__ __forceinline__ uint32_t core_offset(uint32_t row, uint32_t k) {
+    return (row >> 3) * 1024u + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start address, leading byte offset 128, stride byte offset
+// 1024 (all >> 4), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+           (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, FP16 A and B, both K-major, M = 128.
+__host__ __device__ constexpr uint32_t mma_idesc(uint32_t n) { return (1u << 4) | ((n >> 3) << 17) | ((128u >> 4) << 24); }
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+// Bounded wait for the mbarrier phase `parity`; false when the limit ran out.
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < TC_WAIT_LIMIT; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t pack_half2(float a, float b) {
     __half2 h = __floats2half2_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, const uint32_t* b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+// Writes 64 values of row `row` (as FP16, ReLU applied when `relu`) into the A operand.
+__device__ __forceinline__ void store_row(uint8_t* a, uint32_t row, const float* v, bool relu) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        float x[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = relu ? fmaxf(v[8 * j + k], 0.0f) : v[8 * j + k];
+        uint4 u = make_uint4(pack_half2(x[0], x[1]), pack_half2(x[2], x[3]), pack_half2(x[4], x[5]),
+                             pack_half2(x[6], x[7]));
+        *reinterpret_cast<uint4*>(a + core_offset(row, 8u * j)) = u;
+    }
 }
 
-constexpr int INF_WARPS = 4;
+// out[i] = MLP(encode(q[i])) for n queries (n = min(n, *count) when count is given).
+__global__ void __launch_bounds__(TC_THREADS) cache_infer_tc_kernel(const CacheQuery* q, uint32_t n,
+                                                                    const uint32_t* count, const float* grid,
+                                                                    const __half* w16, float* out, uint32_t* err) {
+    extern __shared__ uint8_t tc_smem_raw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023u) & ~uintptr_t(1023));
+    uint8_t* s_a = sm + TC_OFF_A;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(sm + TC_OFF_BAR);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + TC_OFF_BAR + 8);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    if (count) n = min(n, *count);
 
-// out[i] = MLP(encode(q[i])) for n queries; the FP16 weights (CACHE_PARAMS halves) are copied
-// to shared memory once per block.
-__global__ void __launch_bounds__(INF_WARPS * 32) cache_infer_kernel(const CacheQuery* q, uint32_t n,
-                                                                     const uint32_t* count, const float* grid,
-                                                                     const __half* w16, float* out) {
-    if (count) n = min(n, *count);  // queue length written by an earlier kernel
-    __shared__ __align__(16) __half s_w[CACHE_PARAMS];
-    __shared__ __align__(16) __half s_x[INF_WARPS][16][CACHE_WIDTH + 8];  // +8: spread smem banks
-    for (uint32_t k = threadIdx.x; k < CACHE_PARAMS / 8; k += blockDim.x)
-        reinterpret_cast<uint4*>(s_w)[k] = reinterpret_cast<const uint4*>(w16)[k];
+    // weights into the core-matrix layout: hidden layers [n][k], then 16 output rows (3..15 zero)
+    for (uint32_t c = tid; c < CACHE_HIDDEN_LAYERS * CACHE_WIDTH * 8u; c += TC_THREADS) {
+        uint32_t layer = c / (CACHE_WIDTH * 8u), r = (c / 8u) % CACHE_WIDTH, j = c % 8u;
+        uint4 v = reinterpret_cast<const uint4*>(w16 + (uint64_t)layer * CACHE_WIDTH * CACHE_WIDTH +
+                                                 (uint64_t)r * CACHE_WIDTH)[j];
+        *reinterpret_cast<uint4*>(sm + layer * TC_W_BYTES + core_offset(r, 8u * j)) = v;
+    }
+    for (uint32_t c = tid; c < TC_OUT_N * 8u; c += TC_THREADS) {
+        uint32_t r = c / 8u, j = c % 8u;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (r < (uint32_t)CACHE_OUT_ROWS)
+            v = reinterpret_cast<const uint4*>(w16 + (uint64_t)CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH +
+                                               (uint64_t)r * CACHE_WIDTH)[j];
+        *reinterpret_cast<uint4*>(sm + TC_OFF_WOUT + core_offset(r, 8u * j)) = v;
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(s_bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(s_tmem)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t tiles = (n + 15u) / 16u;
-    for (uint32_t tile = blockIdx.x * INF_WARPS + warp; tile < tiles; tile += gridDim.x * INF_WARPS) {
-        // encode: two lanes per query row, the first does levels 0..7 and the extras
-        uint32_t row = lane >> 1, half_ = lane & 1;
-        uint32_t i = tile * 16u + row;
-        float x[CACHE_WIDTH];
-        if (i < n) {
-            encode(q[i], grid, x);
-        } else {
-            for (int k = 0; k < CACHE_WIDTH; ++k) x[k] = 0.0f;
+    tc_fence_after();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t bar = smem_u32(s_bar);
+    const uint32_t a_addr = smem_u32(s_a), w_addr = smem_u32(sm);
+    const uint32_t lane_taddr = tmem + ((32u * warp) << 16);
+    uint32_t phase = 0;
+    bool ok = true;
+    const uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
+    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        uint32_t i = tile * TC_ROWS + tid;
+        {
+            float x[CACHE_WIDTH];
+            if (i < n) {
+                encode(q[i], grid, x);
+            } else {
+#pragma unroll
+                for (int k = 0; k < CACHE_WIDTH; ++k) x[k] = 0.0f;
+            }
+            store_row(s_a, tid, x, false);
         }
-        for (int k = half_ * 32; k < half_ * 32 + 32; ++k) s_x[warp][row][k] = __float2half_rn(x[k]);
-        __syncwarp();
-        // layer 0: A from shared memory
-        uint32_t a[4][4];
+        for (int layer = 0; layer <= CACHE_HIDDEN_LAYERS && ok; ++layer) {
+            const bool last = layer == CACHE_HIDDEN_LAYERS;
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                uint32_t b_addr = last ? w_addr + TC_OFF_WOUT : w_addr + (uint32_t)layer * TC_W_BYTES;
+                uint32_t idesc = mma_idesc(last ? TC_OUT_N : (uint32_t)CACHE_WIDTH);
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            a[kk][0] = *reinterpret_cast<const uint32_t*>(&s_x[warp][g][16 * kk + 2 * t]);
-            a[kk][1] = *reinterpret_cast<const uint32_t*>(&s_x[warp][g + 8][16 * kk + 2 * t]);
-            a[kk][2] = *reinterpret_cast<const uint32_t*>(&s_x[warp][g][16 * kk + 2 * t + 8]);
-            a[kk][3] = *reinterpret_cast<const uint32_t*>(&s_x[warp][g + 8][16 * kk + 2 * t + 8]);
-        }
-        __syncwarp();
-        for (int layer = 0; layer < CACHE_HIDDEN_LAYERS; ++layer) {
-            const __half* W = s_w + layer * CACHE_WIDTH * CACHE_WIDTH;
-            float c[8][4];
+                for (uint32_t kk = 0; kk < CACHE_WIDTH / 16; ++kk)
+                    mma_f16(tmem, smem_desc(a_addr + 256u * kk), smem_desc(b_addr + 256u * kk), idesc, kk);
+                mma_commit(bar);
+            }
+            ok = __syncthreads_and(bar_wait(bar, phase) ? 1 : 0) != 0;  // one verdict for the whole CTA
+            phase ^= 1u;
+            tc_fence_after();
+            if (!ok) break;
+            if (!last) {
+                float v[CACHE_WIDTH];
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    uint32_t b[2];
-                    const __half* wr = W + (8 * nt + g) * CACHE_WIDTH + 16 * kk + 2 * t;
-                    b[0] = *reinterpret_cast<const uint32_t*>(wr);
-                    b[1] = *reinterpret_cast<const uint32_t*>(wr + 8);
-                    mma16816(c[nt], a[kk], b);
+                for (int c = 0; c < CACHE_WIDTH; c += 16) tmem_ld16(lane_taddr + (uint32_t)c, v + c);
+                tmem_ld_wait();
+                store_row(s_a, tid, v, true);
+            } else {
+                float v[16];
+                tmem_ld16(lane_taddr, v);
+                tmem_ld_wait();
+                if (i < n) {
+                    out[3ull * i] = v[0];
+                    out[3ull * i + 1] = v[1];
+                    out[3ull * i + 2] = v[2];
                 }
-            }
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {  // ReLU, then the accumulators become the next A
-                a[kk][0] = pack_half2(fmaxf(c[2 * kk][0], 0.0f), fmaxf(c[2 * kk][1], 0.0f));
-                a[kk][1] = pack_half2(fmaxf(c[2 * kk][2], 0.0f), fmaxf(c[2 * kk][3], 0.0f));
-                a[kk][2] = pack_half2(fmaxf(c[2 * kk + 1][0], 0.0f), fmaxf(c[2 * kk + 1][1], 0.0f));
-                a[kk][3] = pack_half2(fmaxf(c[2 * kk + 1][2], 0.0f), fmaxf(c[2 * kk + 1][3], 0.0f));
-            }
-        }
-        // output layer: 8 rows of W (3 used), one n-tile
-        const __half* W = s_w + CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH;
-        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            uint32_t b[2];
-            const __half* wr = W + g * CACHE_WIDTH + 16 * kk + 2 * t;
-            b[0] = *reinterpret_cast<const uint32_t*>(wr);
-            b[1] = *reinterpret_cast<const uint32_t*>(wr + 8);
-            mma16816(c, a[kk], b);
-        }
-        // c[0], c[1]: row g, columns 2t, 2t+1; c[2], c[3]: row g + 8
-        uint32_t i0 = tile * 16u + g, i1 = i0 + 8u;
-        for (int h = 0; h < 2; ++h) {
-            int col = 2 * t + h;
-            if (col < 3) {
-                if (i0 < n) out[3ull * i0 + col] = c[h];
-                if (i1 < n) out[3ull * i1 + col] = c[2 + h];
             }
         }
     }
+    if (!ok && err) atomicOr(err, ERR_TENSOR_WAIT);
+    // every MMA of this CTA was waited for (or the wait ran out and nothing more was issued)
+    tc_fence_before();
+    __syncthreads();
+    if (!ok) bar_wait(bar, phase ^ 1u);  // one more bounded wait for the last commit in flight
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS)
+                     : "memory");
 }
 
 // ---------------------------------------------------------------- training (FP32)
@@ -344,19 +451,27 @@ __global__ void cache_init_kernel(float* grid, float* w, __half* w16, uint32_t s
     }
 }
 
-void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* out, cudaStream_t st) {
+static void launch_infer(const CacheQuery* q, uint32_t n, const uint32_t* count, const float* grid,
+                         const __half* w16, float* out, uint32_t* err, cudaStream_t st) {
     if (n == 0) return;
-    uint32_t tiles = (n + 15u) / 16u;
-    uint32_t blocks = std::min<uint32_t>((tiles + INF_WARPS - 1) / INF_WARPS, 152u * 8u);
-    cache_infer_kernel<<<blocks, INF_WARPS * 32, 0, st>>>(q, n, nullptr, d.grid, d.w16, out);
+    static bool attr = false;
+    if (!attr) {
+        check_cuda(cudaFuncSetAttribute(cache_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM),
+                   "infer smem");
+        attr = true;
+    }
+    uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
+    uint32_t blocks = std::min<uint32_t>(tiles, 152u * 4u);
+    cache_infer_tc_kernel<<<blocks, TC_THREADS, TC_SMEM, st>>>(q, n, count, grid, w16, out, err);
+}
+
+void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* out, uint32_t* err, cudaStream_t st) {
+    launch_infer(q, n, nullptr, d.grid, d.w16, out, err, st);
 }
 
 void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,
-                       uint32_t max_n, float* out, cudaStream_t st) {
-    if (max_n == 0) return;
-    uint32_t tiles = (max_n + 15u) / 16u;
-    uint32_t blocks = std::min<uint32_t>((tiles + INF_WARPS - 1) / INF_WARPS, 152u * 8u);
-    cache_infer_kernel<<<blocks, INF_WARPS * 32, 0, st>>>(q, max_n, count, grid, w16, out);
+                       uint32_t max_n, float* out, uint32_t* err, cudaStream_t st) {
+    launch_infer(q, max_n, count, grid, w16, out, err, st);
 }
 
 // Training pairs of the frame's records: target = (final - before) / throughput, kept when the

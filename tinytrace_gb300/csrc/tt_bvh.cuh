@@ -39,6 +39,7 @@ constexpr int TRAVERSAL_STACK = TT_TRAVERSAL_STACK;  // entries per thread, in s
 constexpr uint32_t TRAVERSAL_ITERATION_LIMIT = 1u << 24;
 constexpr uint32_t ERR_STACK_OVERFLOW = 1u;
 constexpr uint32_t ERR_ITERATION_LIMIT = 2u;
+constexpr uint32_t ERR_TENSOR_WAIT = 4u;  // a tensor-core completion wait ran out (cache queries)
 
 TT_HD uint32_t leaf_first(uint32_t r) { return r & 0x07ffffffu; }
 TT_HD uint32_t leaf_count(uint32_t r) { return ((r >> 27) & 0xfu) + 1u; }

@@ -34,14 +34,15 @@ struct CacheDevice {
     float* loss;                                // [0]: summed loss of the last step
 };
 
-void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* out, cudaStream_t st);
+// err: device error word (ERR_TENSOR_WAIT), may be null.
+void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* out, uint32_t* err, cudaStream_t st);
 // One Adam step on n samples: gradients of the mean relative L2 loss.
 void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
                       uint32_t step, cudaStream_t st);
 void cache_init(const CacheDevice& d, uint32_t seed, cudaStream_t st);
 // Queries whose count is in device memory (at most max_n of them).
 void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,
-                       uint32_t max_n, float* out, cudaStream_t st);
+                       uint32_t max_n, float* out, uint32_t* err, cudaStream_t st);
 struct TrainRecord;
 void cache_targets(const TrainRecord* rec, const uint32_t* rec_count, uint32_t cap, const float4* final_radiance,
                    CacheQuery* q, float* t, uint32_t* count, cudaStream_t st);

@@ -548,7 +548,8 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
         launch_shade(p, w, shade_grid, body_stream);
         launch_trace<true>(p, w, tgrid, counted, body_stream);
         if (w.cache_on) {
-            cache_infer_queue(w.cache_grid, w.cache_w16, w.cq, w.counters + CACHE_QUEUE, w.P, w.cq_out, body_stream);
+            cache_infer_queue(w.cache_grid, w.cache_w16, w.cq, w.counters + CACHE_QUEUE, w.P, w.cq_out, p.err,
+                              body_stream);
             wf_cache_apply_kernel<<<(w.P + 255) / 256, 256, 0, body_stream>>>(w);
         }
         check_cuda(cudaStreamEndCapture(body_stream, &body), "body capture end");
@@ -604,7 +605,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
             stage_end(timer, st);
             if (w.cache_on) {
                 stage_begin(timer, TT_STAGE_CACHE, st);
-                cache_infer_queue(w.cache_grid, w.cache_w16, w.cq, w.counters + CACHE_QUEUE, n, w.cq_out, st);
+                cache_infer_queue(w.cache_grid, w.cache_w16, w.cq, w.counters + CACHE_QUEUE, n, w.cq_out, p.err, st);
                 wf_cache_apply_kernel<<<grid, WF_BLOCK, 0, st>>>(w);
                 stage_end(timer, st);
             }
