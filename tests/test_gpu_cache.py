@@ -212,3 +212,23 @@ def test_spread_rule_in_a_closed_room(gpu_context):
     a, b = img[..., :3].mean(), plain.mean()
     assert abs(a - b) <= 0.10 * b, (a, b)
     r.close()
+
+
+def test_large_query_batch(gpu_context):
+    """2^20 queries (8,192 tiles of 128 over many CTAs per SM): a sample of rows matches the
+    reference's FP16 emulation as in test_queries_match_the_reference."""
+    ctx = gpu_context
+    _configure(ctx, seed=13)
+    rng = np.random.default_rng(5)
+    for _ in range(5):
+        qt = _queries(rng, 4096)
+        _train(ctx, qt, _field(qt))
+    grid, w = _params(ctx)
+    q = _queries(rng, 1 << 20)
+    got = _query(ctx, q)
+    assert np.isfinite(got).all()
+    pick = rng.choice(len(q), 2000, replace=False)
+    x = cr.encode(q[pick].astype(np.float64), grid.astype(np.float64))
+    want16, _ = cr.forward(x, w, fp16=True)
+    scale = np.abs(want16).max()
+    assert np.abs(got[pick] - want16).max() <= 2e-3 * scale + 1e-4

@@ -170,16 +170,54 @@ __device__ __forceinline__ uint32_t pack_half2(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-// Writes 64 values of row `row` (as FP16, ReLU applied when `relu`) into the A operand.
-__device__ __forceinline__ void store_row(uint8_t* a, uint32_t row, const float* v, bool relu) {
+// The 64 FP16 inputs of one query written straight into row `row` of the A operand, 16 bytes
+// (8 inputs) at a time: the grid features of levels 4c..4c+3 (float2 gathers of the 8 corners),
+// then direction, normal, roughness and zero padding.  Same values as encode().
+__device__ __forceinline__ void encode_row(const CacheQuery& q, const float* grid, uint8_t* a, uint32_t row) {
+    float3 p = make_float3(fminf(fmaxf(q.pos[0], 0.0f), 1.0f), fminf(fmaxf(q.pos[1], 0.0f), 1.0f),
+                           fminf(fmaxf(q.pos[2], 0.0f), 1.0f));
+#pragma unroll 1
+    for (int c = 0; c < CACHE_LEVELS / 4; ++c) {
+        uint32_t h[4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        float x[8];
+        for (int j = 0; j < 4; ++j) {
+            int l = 4 * c + j;
+            uint32_t idx[8];
+            float w[8];
+            grid_corners(p, l, idx, w);
+            const float2* g = reinterpret_cast<const float2*>(grid + 2ull * CACHE_TABLE * l);
+            float f0 = 0.0f, f1 = 0.0f;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) x[k] = relu ? fmaxf(v[8 * j + k], 0.0f) : v[8 * j + k];
-        uint4 u = make_uint4(pack_half2(x[0], x[1]), pack_half2(x[2], x[3]), pack_half2(x[4], x[5]),
-                             pack_half2(x[6], x[7]));
-        *reinterpret_cast<uint4*>(a + core_offset(row, 8u * j)) = u;
+            for (int k = 0; k < 8; ++k) {
+                float2 v = __ldg(g + idx[k]);
+                f0 += w[k] * v.x;
+                f1 += w[k] * v.y;
+            }
+            h[j] = pack_half2(f0, f1);
+        }
+        *reinterpret_cast<uint4*>(a + core_offset(row, 8u * c)) = make_uint4(h[0], h[1], h[2], h[3]);
+    }
+    *reinterpret_cast<uint4*>(a + core_offset(row, 32u)) =
+        make_uint4(pack_half2(q.dir[0] * 0.5f + 0.5f, q.dir[1] * 0.5f + 0.5f),
+                   pack_half2(q.dir[2] * 0.5f + 0.5f, q.normal[0] * 0.5f + 0.5f),
+                   pack_half2(q.normal[1] * 0.5f + 0.5f, q.normal[2] * 0.5f + 0.5f), pack_half2(q.roughness, 0.0f));
+#pragma unroll
+    for (int c = 5; c < 8; ++c) *reinterpret_cast<uint4*>(a + core_offset(row, 8u * c)) = make_uint4(0u, 0u, 0u, 0u);
+}
+__device__ __forceinline__ void zero_row(uint8_t* a, uint32_t row) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(a + core_offset(row, 8u * c)) = make_uint4(0u, 0u, 0u, 0u);
+}
+// 16 accumulator columns (c0..c0+15) of row `row`, ReLU, FP16, into the A operand.
+__device__ __forceinline__ void store_relu16(uint8_t* a, uint32_t row, uint32_t c0, const float* v) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const float* x = v + 8 * j;
+        uint4 u = make_uint4(pack_half2(fmaxf(x[0], 0.0f), fmaxf(x[1], 0.0f)),
+                             pack_half2(fmaxf(x[2], 0.0f), fmaxf(x[3], 0.0f)),
+                             pack_half2(fmaxf(x[4], 0.0f), fmaxf(x[5], 0.0f)),
+                             pack_half2(fmaxf(x[6], 0.0f), fmaxf(x[7], 0.0f)));
+        *reinterpret_cast<uint4*>(a + core_offset(row, c0 + 8u * j)) = u;
     }
 }
 
@@ -233,16 +271,8 @@ __global__ void __launch_bounds__(TC_THREADS) cache_infer_tc_kernel(const CacheQ
     const uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
     for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         uint32_t i = tile * TC_ROWS + tid;
-        {
-            float x[CACHE_WIDTH];
-            if (i < n) {
-                encode(q[i], grid, x);
-            } else {
-#pragma unroll
-                for (int k = 0; k < CACHE_WIDTH; ++k) x[k] = 0.0f;
-            }
-            store_row(s_a, tid, x, false);
-        }
+        if (i < n) encode_row(q[i], grid, s_a, tid);
+        else zero_row(s_a, tid);
         for (int layer = 0; layer <= CACHE_HIDDEN_LAYERS && ok; ++layer) {
             const bool last = layer == CACHE_HIDDEN_LAYERS;
             fence_async_smem();
@@ -262,11 +292,13 @@ __global__ void __launch_bounds__(TC_THREADS) cache_infer_tc_kernel(const CacheQ
             tc_fence_after();
             if (!ok) break;
             if (!last) {
-                float v[CACHE_WIDTH];
 #pragma unroll
-                for (int c = 0; c < CACHE_WIDTH; c += 16) tmem_ld16(lane_taddr + (uint32_t)c, v + c);
-                tmem_ld_wait();
-                store_row(s_a, tid, v, true);
+                for (int c = 0; c < CACHE_WIDTH; c += 16) {
+                    float v[16];
+                    tmem_ld16(lane_taddr + (uint32_t)c, v);
+                    tmem_ld_wait();
+                    store_relu16(s_a, tid, (uint32_t)c, v);
+                }
             } else {
                 float v[16];
                 tmem_ld16(lane_taddr, v);
