@@ -69,6 +69,13 @@ extern "C" {
 #define TT_OPTION_TRACE_BLOCKS_PER_SM 7 /* resident blocks per SM of the trace kernel (0 = all that fit) */
 #define TT_OPTION_RADIANCE_CACHE 8  /* 1: wavefront renders end paths in the learned radiance cache and
                                        train it after every frame (tt_cache_configure) */
+#define TT_OPTION_LIGHT_VISIBILITY 9 /* TT_LIGHT_VISIBILITY_*: the shadow test of next-event estimation */
+/* light visibility (tt_set_option TT_OPTION_LIGHT_VISIBILITY) */
+#define TT_LIGHT_VISIBILITY_HASH 0     /* the reference's test (src/integrate/integrate.glsl:180-185): the
+                                          hit instance is the light's and (prim + index_offset / 3) % 0xffff
+                                          equals the light's 16-bit hash; lights at global triangle index
+                                          >= 65535 never pass (parity, default) */
+#define TT_LIGHT_VISIBILITY_TRIANGLE 1 /* the hit is the sampled emissive triangle itself (full 32-bit id) */
 /* acceleration structures (tt_set_option TT_OPTION_ACCEL; tt_scene_stats.accel) */
 #define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
 #define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */

@@ -42,6 +42,8 @@ struct OracleScene {
     std::vector<EmissiveTriangle> emissive;
     std::vector<Texture> textures;
     SceneBvh bvh;
+    std::vector<uint32_t> light_prim;  // primitive of each emissive triangle in its instance's mesh
+    bool light_exact = false;          // visibility tests the sampled triangle itself (full id)
     bool use_bvh = true;
     bool flat = false;  // the integrator traces through the flat BVH instead of the two-level one
     Geometry geom() const {
@@ -137,8 +139,12 @@ v3 direct_light_contribution(const OracleScene& s, v3 position, v3 wi, const Bas
     Hit h = trace(s, ray.origin, ray.direction, SHADOW_TMIN, SHADOW_TMAX, false);
     if (!h.hit) return splat3(0.0f);
     if (h.instance != ls.instance) return splat3(0.0f);
-    uint32_t tri = h.prim + s.instances[h.instance].index_offset / 3u;
-    if (tri % 0xffffu != ls.hash) return splat3(0.0f);
+    if (s.light_exact) {
+        if (h.prim != s.light_prim[ls.index]) return splat3(0.0f);
+    } else {
+        uint32_t tri = h.prim + s.instances[h.instance].index_offset / 3u;
+        if (tri % 0xffffu != ls.hash) return splat3(0.0f);
+    }
     const Material& lm = s.materials[s.instances[ls.instance].material_index];
     v3 emissive = material_emissive(lm, s.textures, ls.uv, 4.0f);  // integrate.glsl:188-189
     float bd = 0.0f;
@@ -627,6 +633,7 @@ void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
             at += n;
         }
     }
+    s->light_prim = r_light_prims(*s);
     s->use_bvh = accel != 0;
     s->flat = accel == 2;
     if (s->use_bvh) s->bvh = build_scene_bvh(s->geom(), leaf_max);
@@ -634,6 +641,9 @@ void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
 }
 
 void oracle_scene_destroy(void* p) { delete static_cast<OracleScene*>(p); }
+
+// 0: the reference's 16-bit hash visibility test; 1: the sampled triangle itself.
+void oracle_scene_set_light_exact(void* p, int exact) { static_cast<OracleScene*>(p)->light_exact = exact != 0; }
 
 // BVH arrays for node-for-node comparison with the GPU build.
 void oracle_scene_bvh_info(void* p, uint64_t* out /* blas_nodes, tris, tlas_nodes, blas_levels, tlas_levels,

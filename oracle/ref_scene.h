@@ -230,9 +230,11 @@ struct DirectLightSample {
     v2 uv;
     uint32_t instance, hash;
     float area, light_probability;
+    uint32_t index;  // the emissive triangle drawn
 };
 inline DirectLightSample sample_random_light(const SceneView& sc, Generator& g) {
-    const EmissiveTriangle& tri = sc.emissive[random_uint(g, sc.emissive_count)];
+    uint32_t index = random_uint(g, sc.emissive_count);
+    const EmissiveTriangle& tri = sc.emissive[index];
     v3 bary = sample_triangle(random_vec2(g));
     const float* m = sc.instances[tri.instance_index].transform;
     v3 p0 = mat43_point(m, dequantize_snorm3(tri.positions[0]));
@@ -247,6 +249,7 @@ inline DirectLightSample sample_random_light(const SceneView& sc, Generator& g) 
     s.instance = tri.instance_index;
     s.hash = (uint32_t)tri.hash;
     s.light_probability = 1.0f / (float)sc.emissive_count;
+    s.index = index;
     return s;
 }
 

@@ -278,3 +278,29 @@ def test_autotune_keeps_the_image(gpu_context):
     cpu = oracle.OracleScene(r.scene_arrays).render(c)
     assert_same_bits(gpu, cpu, "after autotune")
     r.close()
+
+
+@pytest.mark.parametrize("mode", ["hash", "triangle"])
+@pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
+def test_light_visibility_modes(gpu_context, integrator, mode):
+    """Both visibility tests of next-event estimation on a scene whose lights lie past global
+    triangle index 65535 (the reference's hash never matches there), bit for bit."""
+    from tinytrace_gb300.renderer import Renderer
+
+    extent = (64, 48)
+    cfg = scenes.Config(bounce_count=4, sample_count=3)
+    cam = scenes.Camera.looking_at((0.0, 3.0, 4.0), (0.0, 0.0, 0.0), fov=0.8)
+    r = Renderer(extent)
+    lib, hd = r.context.lib, r.context.handle
+    check(lib.tt_set_option(hd, native.TT_OPTION_INTEGRATOR, INTEGRATORS[integrator]))
+    value = native.TT_LIGHT_VISIBILITY_TRIANGLE if mode == "triangle" else native.TT_LIGHT_VISIBILITY_HASH
+    check(lib.tt_set_option(hd, native.TT_OPTION_LIGHT_VISIBILITY, value))
+    assert lib.tt_set_option(hd, native.TT_OPTION_LIGHT_VISIBILITY, 7) == native.TT_ERR_INVALID_ARGUMENT
+    r.set_scene(scenes.late_lights())
+    r.camera = cam
+    r.set_config(cfg)
+    orc = oracle.OracleScene(r.scene_arrays)
+    orc.set_light_exact(mode == "triangle")
+    c = make_constants(cam, extent, cfg, r.context.frame_index(), r.accumulated_frame_count)
+    assert_same_bits(r.render_to_texture(), orc.render(c), f"light visibility {mode} {integrator}")
+    r.close()

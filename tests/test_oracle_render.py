@@ -111,3 +111,26 @@ def test_tonemap_curve():
     y = oracle.tonemap(img, True)[0, :, 0]
     assert np.all(np.diff(y) >= -2.5e-7) and y.max() <= 0.97 + 1e-6
     assert np.array_equal(oracle.tonemap(img, False), img)
+
+
+def test_light_visibility_modes():
+    """The reference's 16-bit light hash fails for lights at global triangle index >= 65535
+    (next-event estimation sees nothing); the exact mode tests the sampled triangle and sees
+    them.  Where every light lies below index 65535 the two modes give the same image."""
+    from tinytrace_gb300 import scenes
+    from tinytrace_gb300.camera import Camera
+    from tinytrace_gb300.renderer import Config, SceneArrays, make_constants
+
+    cam = Camera.looking_at((0.0, 3.0, 4.0), (0.0, 0.0, 0.0), fov=0.8)
+    c = make_constants(cam, (40, 30), Config(bounce_count=3, sample_count=2), 0, 0)
+    o = oracle.OracleScene(SceneArrays(scenes.late_lights()))
+    hashed = o.render(c)
+    o.set_light_exact(True)
+    exact = o.render(c)
+    assert exact[..., :3].mean() > hashed[..., :3].mean() * 1.01
+    w = scenes.cornell_workload(extent=(32, 32), spp=2, depth=3)
+    cc = make_constants(w.camera, w.extent, w.config, 0, 0)
+    o = oracle.OracleScene(SceneArrays(w.scene))
+    a = o.render(cc)
+    o.set_light_exact(True)
+    assert np.array_equal(a, o.render(cc))

@@ -148,6 +148,7 @@ struct tt_context {
     tt::WavefrontBuffers wf;
     bool stage_timing = false;
     bool graphs = true;
+    uint32_t light_visibility = TT_LIGHT_VISIBILITY_HASH;  // TT_OPTION_LIGHT_VISIBILITY
     uint32_t refill_lanes = 20;       // TT_OPTION_REFILL_LANES
     uint32_t trace_blocks_per_sm = 0; // TT_OPTION_TRACE_BLOCKS_PER_SM (0 = as many as fit)
     int occupancy_sms = 0, occupancy_blocks = 0;
@@ -492,7 +493,9 @@ namespace tt {
 void set_last_error(const std::string& message) { g_last_error = message; }
 DevScene scene_view(tt_context* ctx, tt_handle scene) {
     require(ctx, "null context");
-    return lookup<SceneRes>(ctx, scene, KIND_SCENE)->dev;
+    DevScene d = lookup<SceneRes>(ctx, scene, KIND_SCENE)->dev;
+    d.light_exact = ctx->light_visibility == TT_LIGHT_VISIBILITY_TRIANGLE ? 1u : 0u;
+    return d;
 }
 int context_device(tt_context* ctx) { return ctx->device; }
 }  // namespace tt
@@ -590,6 +593,7 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
             "constants.screen_size must equal the target extent");
     RenderParams p;
     p.sc = s->dev;
+    p.sc.light_exact = ctx->light_visibility == TT_LIGHT_VISIBILITY_TRIANGLE ? 1u : 0u;
     p.c = *c;
     p.target = img->buf.as<float4>();
     p.err = ctx->err_word.as<uint32_t>();
@@ -1046,6 +1050,10 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else if (option == TT_OPTION_TRACE_BLOCKS_PER_SM) {
             require(value <= 64, "trace blocks per SM above 64");
             ctx->trace_blocks_per_sm = (uint32_t)value;
+        } else if (option == TT_OPTION_LIGHT_VISIBILITY) {
+            require(value == TT_LIGHT_VISIBILITY_HASH || value == TT_LIGHT_VISIBILITY_TRIANGLE,
+                    "unknown light visibility");
+            ctx->light_visibility = (uint32_t)value;
         } else if (option == TT_OPTION_RADIANCE_CACHE) {
             require(value <= 1, "radiance cache is 0 or 1");
             ctx->cache.enabled = value != 0;

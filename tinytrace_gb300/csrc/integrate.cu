@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
                     LightSample ls = sample_light(sc, hit.world_position, basis, g);
                     Hit hs = trace_closest<COUNT>(sc, hit.world_position, ls.dir, SHADOW_TMIN, SHADOW_TMAX, false,
                                                   stack, BLOCK, p.err, cnt);
-                    f3 direct = light_visible(sc, hs, ls.instance, ls.hash) ? light_contribution<TEX>(sc, ls, mc, lobes, wi)
+                    f3 direct = light_visible(sc, hs, ls.instance, ls.hash, ls.prim) ? light_contribution<TEX>(sc, ls, mc, lobes, wi)
                                                                            : splat(0.0f);
                     path_acc += thr * direct;
                 }

@@ -74,6 +74,7 @@ struct DevScene {
     const uint8_t* tex_data;     // all texture levels
     const float* srgb;           // 256-entry sRGB-to-linear table
     uint32_t textured;           // 1 when some material samples a texture
+    uint32_t light_exact;        // TT_LIGHT_VISIBILITY_TRIANGLE: shadow rays test the sampled triangle itself
 };
 
 struct Hit {

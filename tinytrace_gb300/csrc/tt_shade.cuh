@@ -140,11 +140,13 @@ struct LightSample {
     f3 dir;         // world-space shadow ray direction
     float density;  // solid-angle density times the light selection probability
     uint32_t instance, hash;
+    uint32_t prim;  // primitive of the light triangle in its instance's mesh (exact visibility)
     f2 uv;          // texture coordinates of the light point (read by textured shading only)
 };
 __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 position, const Basis& basis,
                                                     uint32_t& g) {
-    const tt_emissive_triangle* tri = sc.emissive + (xor_shift(g) % sc.emissive_count);
+    uint32_t light = xor_shift(g) % sc.emissive_count;
+    const tt_emissive_triangle* tri = sc.emissive + light;
     f2 rnd = random_vec2(g);
     f3 bary = sample_triangle(rnd);
     LightSample ls;
@@ -166,6 +168,7 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 posit
     for (int k = 0; k < 3; ++k) tc[k] = __ldg(reinterpret_cast<const uint32_t*>(&tri->texture_coordinates[k]));
     ls.uv = interp_uv(bary, tc[0], tc[1], tc[2]);
     ls.hash = (uint32_t)__ldg(&tri->hash);
+    ls.prim = sc.light_exact ? __ldg(sc.light_prim + light) : 0xffffffffu;
     float light_probability = 1.0f / (float)sc.emissive_count;
     f3 to_light = lpos - position;
     ls.wo = transform_from_basis(basis, to_light);
@@ -196,16 +199,23 @@ __device__ __forceinline__ f3 light_contribution(const DevScene& sc, const Light
 // The hit is computed exactly as the traversal computes it (object ray of the instance, the
 // same watertight test on the same dequantised vertices), so a traversal seeded with it finds
 // the same closest hit as an unseeded one.
-__device__ __forceinline__ int shadow_target(const DevScene& sc, uint32_t light_instance, uint32_t hash, f3 o,
-                                             f3 d, float tmin, float tmax, Hit& best, float& tbest) {
+__device__ __forceinline__ int shadow_target(const DevScene& sc, uint32_t light_instance, uint32_t hash,
+                                             uint32_t exact_prim, f3 o, f3 d, float tmin, float tmax, Hit& best,
+                                             float& tbest) {
     const tt_instance* in = sc.instances + light_instance;
     uint32_t index_offset = __ldg(&in->index_offset), vertex_offset = __ldg(&in->vertex_offset);
     uint32_t tri_count = __ldg(&sc.meshes[__ldg(&in->mesh_index)].index_count) / 3u;
-    if (tri_count > 0xffffu) return 2;
-    if (hash >= 0xffffu) return 0;
-    uint32_t r = (index_offset / 3u) % 0xffffu;
-    uint32_t prim = hash >= r ? hash - r : hash + 0xffffu - r;
-    if (prim >= tri_count) return 0;
+    uint32_t prim;
+    if (sc.light_exact) {  // the sampled triangle itself
+        prim = exact_prim;
+        if (prim >= tri_count) return 0;
+    } else {
+        if (tri_count > 0xffffu) return 2;
+        if (hash >= 0xffffu) return 0;
+        uint32_t r = (index_offset / 3u) % 0xffffu;
+        prim = hash >= r ? hash - r : hash + 0xffffu - r;
+        if (prim >= tri_count) return 0;
+    }
     f3 oo, od;
     uint32_t mesh;
     instance_ray(sc, light_instance, o, d, oo, od, mesh);
@@ -230,9 +240,10 @@ __device__ __forceinline__ int shadow_target(const DevScene& sc, uint32_t light_
 
 // integrate.glsl:175-185: the closest shadow hit must be the sampled light triangle.
 __device__ __forceinline__ bool light_visible(const DevScene& sc, const Hit& h, uint32_t light_instance,
-                                              uint32_t hash) {
+                                              uint32_t hash, uint32_t exact_prim) {
     if (!h.hit) return false;
     if (h.instance != light_instance) return false;
+    if (sc.light_exact) return h.prim == exact_prim;
     uint32_t tri_index = h.prim + __ldg(&sc.instances[h.instance].index_offset) / 3u;
     return tri_index % 0xffffu == hash;
 }

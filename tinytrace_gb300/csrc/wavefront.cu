@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                                SHADOW ? SHADOW_TMAX : EXTENSION_TMAX, !SHADOW);
                     if (SHADOW) {
                         uint32_t hash = __float_as_uint(w.pa1[slot].w) >> 16;
-                        int mode = shadow_target(sc, light, hash, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX,
+                        uint32_t exact = __float_as_uint(w.pa0[slot].w);
+                        int mode = shadow_target(sc, light, hash, exact, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX,
                                                  st.best, st.tbest);
                         if (mode == 0) st.have = false;  // not visible: the first step finishes
                         seeded = mode == 1;
@@ -214,10 +215,11 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                 if (fin) {
                     float4 a1 = w.pa1[slot];
                     uint32_t pflags = __float_as_uint(a1.w);
-                    bool vis = light_visible(sc, h, light, pflags >> 16);
+                    float4 a0 = w.pa0[slot];
+                    bool vis = light_visible(sc, h, light, pflags >> 16, __float_as_uint(a0.w));
                     float4 a4 = w.acc[slot];
                     f3 acc = xyz(a4);
-                    acc += vis ? xyz(a1) : xyz(w.pa0[slot]);
+                    acc += vis ? xyz(a1) : xyz(a0);
                     if (pflags & 1u) acc += xyz(w.pe[slot]);
                     w.acc[slot] = make_float4(acc.x, acc.y, acc.z, a4.w);
                 }
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
                 } else {
                     uint32_t pflags = (bounce == 0u ? 1u : 0u) | (ls.hash << 16);
                     w.pa1[s] = pack(a1, pflags);
-                    w.pa0[s] = pack(a0, 0u);
+                    w.pa0[s] = pack(a0, ls.prim);
                     w.pe[s] = pack(em * thr, 0u);
                     want_shadow = true;
                     light = ls.instance;

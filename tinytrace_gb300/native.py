@@ -35,6 +35,9 @@ TT_LIFETIME_RENDERER = 4
 
 TT_FORMAT_RGBA32F = 0
 TT_FORMAT_RGBA8_UNORM = 1
+TT_OPTION_LIGHT_VISIBILITY = 9
+TT_LIGHT_VISIBILITY_HASH = 0
+TT_LIGHT_VISIBILITY_TRIANGLE = 1
 TT_TEXTURE_BC1_SRGB = 1
 TT_TEXTURE_BC5_UNORM = 2
 TT_TEXTURE_R8_UNORM = 3

@@ -149,6 +149,27 @@ def textured_cornell(seed: int = 5) -> AssetScene:
     return s
 
 
+def late_lights(freq: int = 60, lights: int = 6) -> AssetScene:
+    """A sphere of 20 freq^2 triangles (72,000 at freq 60) inserted before `lights` emissive
+    triangles, so that every light triangle has a global index >= 65535: the reference's 16-bit
+    light hash (src/asset/mod.rs:186 against src/integrate/integrate.glsl:184) then never
+    matches and next-event estimation sees no light, unless visibility tests the sampled
+    triangle itself (TT_LIGHT_VISIBILITY_TRIANGLE)."""
+    s = AssetScene()
+    pts, tris = geodesic_sphere(freq)
+    body = s.insert_material(Material(base_color=(0.7, 0.7, 0.7), specular_roughness=0.6))
+    m = s.insert_mesh(pts.astype(np.float32), None, tris)
+    s.root.children.append(Node(models=[Model(m, body)]))
+    for k in range(lights):
+        a = 2.0 * np.pi * k / lights
+        c = np.array([2.5 * np.cos(a), 2.5, 2.5 * np.sin(a)])
+        tri = np.array([c + [-0.4, 0.0, -0.4], c + [0.4, 0.0, -0.4], c + [0.4, 0.0, 0.4]], np.float32)  # faces -y
+        mat = s.insert_material(Material(emission_luminance=20.0, emission_color=(1.0, 0.9, 0.8)))
+        lm = s.insert_mesh(tri, None, np.array([0, 1, 2], np.uint32), np.tile([0.0, -1.0, 0.0], (3, 1)))
+        s.root.children.append(Node(models=[Model(lm, mat)]))
+    return s
+
+
 def cornell_workload(extent=(256, 256), spp: int = 16, depth: int = 4) -> Workload:
     cam = Camera.looking_at((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), fov=0.75)
     cfg = Config(bounce_count=depth, sample_count=spp, tonemap=True,
