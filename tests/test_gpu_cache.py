@@ -1,10 +1,11 @@
 """The learned radiance cache's CUDA kernels against the NumPy reference (GPU required).
 
-Tolerances: queries run in FP16 on the tensor cores, so they are compared with the reference's
-FP16 emulation within 2e-3 of the output scale; training is FP32, so the first Adam step (which
-moves every parameter with a nonzero gradient by exactly the learning rate, against the sign of
-its gradient) must agree in sign with the reference's float64 gradients, and the reported loss
-within 1e-4 relative."""
+Tolerances: queries and training run FP16-in / FP32-accumulate on the tensor cores, so queries
+are compared with the reference's FP16 emulation within 2e-3 of the output scale, the reported
+loss with the loss of that FP16 forward pass within 1e-3 relative, and the first Adam step
+(which moves every parameter with a nonzero gradient by exactly the learning rate, against the
+sign of its gradient) must agree in sign with the reference's float64 gradients on 98 % of the
+parameters whose gradient is above 1e-4 of the largest."""
 import ctypes
 
 import numpy as np
@@ -72,12 +73,14 @@ def test_first_step_follows_the_reference_gradients(gpu_context):
     grid1, w1 = _params(ctx)
     ref_loss, g_w, g_grid = cr.loss_and_grads(q.astype(np.float64), t.astype(np.float64), grid0.astype(np.float64),
                                               w0.astype(np.float64))
-    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    y16, _ = cr.forward(cr.encode(q.astype(np.float64), grid0.astype(np.float64)), w0, fp16=True)
+    loss16 = float((((y16 - t) ** 2) / (y16 * y16 + 0.01)).sum())
+    assert abs(loss - loss16) <= 1e-3 * loss16, (loss, loss16, ref_loss)
     for before, after, g, name in ((w0, w1, g_w, "weights"), (grid0.ravel(), grid1.ravel(), g_grid.ravel(), "grid")):
         big = np.abs(g) > 1e-4 * np.abs(g).max()
         step = after.astype(np.float64) - before
         agree = np.sign(step[big]) == -np.sign(g[big])
-        assert agree.mean() > 0.99, (name, agree.mean(), big.sum())
+        assert agree.mean() > 0.98, (name, agree.mean(), big.sum())
         assert np.allclose(np.abs(step[big]), 1e-2, rtol=1e-2, atol=1e-5), name
 
 

@@ -579,7 +579,7 @@ static void cache_train_after_frame(tt_context* ctx, const WfParams& w) {
     for (uint32_t k = 0; k < 4 && k * BATCH < pairs; ++k) {
         uint32_t n = std::min(BATCH, pairs - k * BATCH);
         cache_train_step(C.dev(), C.tq.as<CacheQuery>() + (uint64_t)k * BATCH, C.tt.as<float>() + 3ull * k * BATCH, n,
-                         C.config.learning_rate, ++C.step, st);
+                         C.config.learning_rate, ++C.step, ctx->err_word.as<uint32_t>(), st);
     }
 }
 
@@ -634,8 +634,8 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     check_cuda(cudaGetLastError(), "integrate launch");
     check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
     ctx->integrate_timed = true;
-    fetch_error_word(ctx);
     if (cached) cache_train_after_frame(ctx, w);
+    fetch_error_word(ctx);
     if (counted) {
         unsigned long long h[8];
         check_cuda(cudaMemcpyAsync(h, ctx->counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "copy");
@@ -1258,10 +1258,13 @@ int32_t tt_cache_train(tt_context* ctx, const float* queries, const float* targe
         CacheState& C = ctx->cache;
         CacheDevice d = C.dev();
         uint32_t step = ++C.step;
+        arm_error_word(ctx);
         batch(ctx, queries, 48ull * n, targets, 12ull * n, nullptr, 0, [&](void* din, void* dex, void*) {
             cache_train_step(d, static_cast<const CacheQuery*>(din), static_cast<const float*>(dex), n,
-                             C.config.learning_rate, step, ctx->stream);
+                             C.config.learning_rate, step, ctx->err_word.as<uint32_t>(), ctx->stream);
         });
+        fetch_error_word(ctx);
+        sync(ctx);
         if (loss) check_cuda(cudaMemcpy(loss, C.loss.ptr, 4, cudaMemcpyDeviceToHost), "loss");
     });
 }

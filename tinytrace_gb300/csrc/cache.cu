@@ -15,10 +15,11 @@
 //   inference FP16 inputs and weights on the 5th-generation tensor cores (tcgen05.mma, FP32
 //             accumulation in tensor memory), 128 queries per CTA, weights and activations in
 //             shared memory, ReLU and FP16 conversion between layers on the CUDA cores.
-//   training  FP32 on the CUDA cores: forward, relative L2 loss (y - t)^2 / (y^2 + 0.01)
-//             (y not differentiated in the denominator), backward into weight gradients
-//             (shared-memory accumulation, one atomic per weight per block) and grid gradients
-//             (atomics on the 8 corners), then Adam (beta 0.9 / 0.99, eps 1e-15).
+//   training  FP16 in, FP32 accumulate on the tensor cores (tcgen05): forward keeping every
+//             layer's activations, relative L2 loss (y - t)^2 / (y^2 + 0.01) (y not
+//             differentiated in the denominator), backward through the layers and weight
+//             gradients accumulated in TMEM, grid gradients by atomics on the 8 corners; then Adam
+//             on the FP32 master parameters (beta 0.9 / 0.99, eps 1e-15).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -58,32 +59,6 @@ __device__ __forceinline__ void grid_corners(const float3& p, int l, uint32_t* i
         idx[c] = h & (CACHE_TABLE - 1u);
         w[c] = ((c & 1) ? tx : 1.0f - tx) * ((c & 2) ? ty : 1.0f - ty) * ((c & 4) ? tz : 1.0f - tz);
     }
-}
-
-// The 64 network inputs of one query (FP32).
-__device__ __forceinline__ void encode(const CacheQuery& q, const float* grid, float* x) {
-    float3 p = make_float3(fminf(fmaxf(q.pos[0], 0.0f), 1.0f), fminf(fmaxf(q.pos[1], 0.0f), 1.0f),
-                           fminf(fmaxf(q.pos[2], 0.0f), 1.0f));
-    for (int l = 0; l < CACHE_LEVELS; ++l) {
-        uint32_t idx[8];
-        float w[8];
-        grid_corners(p, l, idx, w);
-        float f0 = 0.0f, f1 = 0.0f;
-        const float* g = grid + 2ull * CACHE_TABLE * l;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            f0 += w[c] * g[2ull * idx[c]];
-            f1 += w[c] * g[2ull * idx[c] + 1];
-        }
-        x[2 * l] = f0;
-        x[2 * l + 1] = f1;
-    }
-    for (int k = 0; k < 3; ++k) {
-        x[32 + k] = q.dir[k] * 0.5f + 0.5f;
-        x[35 + k] = q.normal[k] * 0.5f + 0.5f;
-    }
-    x[38] = q.roughness;
-    for (int k = 39; k < CACHE_WIDTH; ++k) x[k] = 0.0f;
 }
 
 // ---------------------------------------------------------------- inference (tcgen05 tensor cores)
@@ -322,125 +297,264 @@ __global__ void __launch_bounds__(TC_THREADS) cache_infer_tc_kernel(const CacheQ
                      : "memory");
 }
 
-// ---------------------------------------------------------------- training (FP32)
-constexpr int TRAIN_THREADS = 64;  // one per neuron
-constexpr int TRAIN_CHUNK = 32;    // samples per pass through the network
-constexpr uint32_t TRAIN_SMEM =
-    sizeof(float) * (CACHE_PARAMS * 2 + 5 * TRAIN_CHUNK * CACHE_WIDTH + 2 * TRAIN_CHUNK * CACHE_WIDTH + 2 * TRAIN_CHUNK * 3);
+// ---------------------------------------------------------------- training (tcgen05 tensor cores)
+// One CTA (128 threads, one per sample row) takes tiles of 128 training pairs.  Forward: the
+// inference layers, keeping every layer's FP16 activations H0..H4 in shared memory.  Loss and
+// output gradient in FP32 per thread: g = 2 (y - t) / (y^2 + 0.01), clamped to +-2^14 (the
+// factor 1 / (3 n) of the mean is applied when the FP32 gradients leave the CTA).  Backward:
+// per layer, from the gradient of its output (in TMEM) the thread forms delta = g * (H > 0) in
+// FP16 and writes it twice, row-major as the A operand of delta . W (the next gradient) and
+// transposed as the A operand of delta^T . H (the weight gradient); H's transpose is the B
+// operand.  Weight gradients accumulate in TMEM across all tiles of the CTA and are added to the
+// global FP32 gradient once at the end; the input gradient's 32 grid-feature columns scatter
+// onto the hash grid with atomics.  Operands (K-major core-matrix layout, no swizzle):
+//   forward weights W_l [out][in], W_out [16][64]; backward weights W_l^T [in][out] and
+//   W_out^T [64][16]; activations H0..H4 and delta [128][64]; output gradient [128][16];
+//   transposed operands [128][128] (rows 64..127 zero) and [64][128], output gradient^T [16][128].
+// TMEM (512 columns): 0..63 scratch accumulator, 64 + 64 l weight gradient of layer l (lanes =
+// output neuron), 320..335 output-layer gradient transposed (lanes = input neuron).
+constexpr uint32_t TT_OFF_WB = 4 * TC_W_BYTES + TC_WOUT_BYTES;      // backward weights
+constexpr uint32_t TT_OFF_H = TT_OFF_WB + 4 * TC_W_BYTES + TC_WOUT_BYTES;
+constexpr uint32_t TT_H_BYTES = TC_ROWS * CACHE_WIDTH * 2;            // 16 KB
+constexpr uint32_t TT_OFF_G = TT_OFF_H + 5 * TT_H_BYTES;              // delta, row-major
+constexpr uint32_t TT_OFF_DY = TT_OFF_G + TT_H_BYTES;                 // output gradient [128][16]
+constexpr uint32_t TT_OFF_AT = TT_OFF_DY + TC_ROWS * 16 * 2;          // [128][128] transposed A
+constexpr uint32_t TT_OFF_BT = TT_OFF_AT + 128 * 128 * 2;             // [64][128] transposed B
+constexpr uint32_t TT_OFF_DYT = TT_OFF_BT + 64 * 128 * 2;             // [16][128]
+constexpr uint32_t TT_OFF_BAR = TT_OFF_DYT + 16 * 128 * 2;
+constexpr uint32_t TT_SMEM = TT_OFF_BAR + 16 + 1024;
+constexpr uint32_t TT_TMEM_COLS = 512;
+constexpr float TT_GRAD_CLAMP = 16384.0f;  // |dL/dy| per output, before the mean's 1 / (3 n)
+constexpr float TT_GRAD_SCALE = 1.0f / 64.0f;  // FP16 headroom of the backward pass; undone at the end
 
-__global__ void __launch_bounds__(TRAIN_THREADS) cache_train_kernel(const CacheQuery* q, const float* target,
-                                                                    uint32_t n, const float* grid, const float* w,
+// Byte offset of (row, k) in a K-major core-matrix operand whose rows are `kdim` elements long.
+__device__ __forceinline__ uint32_t core_offset_k(uint32_t row, uint32_t k, uint32_t kdim) {
+    return (row >> 3) * (kdim * 16u) + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+__device__ __forceinline__ uint64_t smem_desc_k(uint32_t addr, uint32_t kdim) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)((kdim * 16u) >> 4) << 32) |
+           (1ull << 46);
+}
+__device__ __forceinline__ void store_half(uint8_t* base, uint32_t off, float v) {
+    *reinterpret_cast<__half*>(base + off) = __float2half_rn(v);
+}
+__device__ __forceinline__ float load_half(const uint8_t* base, uint32_t off) {
+    return __half2float(*reinterpret_cast<const __half*>(base + off));
+}
+// Issues `ksteps` MMAs of K 16 (A and B K-major with row length kdim) into TMEM column `col`.
+__device__ __forceinline__ void mma_chain(uint32_t tmem_col, uint32_t a, uint32_t b, uint32_t kdim, uint32_t n,
+                                          uint32_t ksteps, bool accumulate) {
+    uint32_t idesc = mma_idesc(n);
+    for (uint32_t kk = 0; kk < ksteps; ++kk)
+        mma_f16(tmem_col, smem_desc_k(a + 256u * kk, kdim), smem_desc_k(b + 256u * kk, kdim), idesc,
+                (accumulate || kk > 0) ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(TC_THREADS) cache_train_tc_kernel(const CacheQuery* q, const float* target, uint32_t n,
+                                                                    const float* grid, const __half* w16,
                                                                     float* w_grad, float* grid_grad, float* loss,
-                                                                    float inv_count) {
-    extern __shared__ float sm[];
-    float* s_w = sm;                                      // CACHE_PARAMS
-    float* s_dw = s_w + CACHE_PARAMS;                     // CACHE_PARAMS
-    float* act = s_dw + CACHE_PARAMS;                     // [5][CHUNK][64]: input, hidden 1..4
-    float* delta = act + 5 * TRAIN_CHUNK * CACHE_WIDTH;   // [2][CHUNK][64]
-    float* y = delta + 2 * TRAIN_CHUNK * CACHE_WIDTH;     // [CHUNK][3]
-    float* dy = y + TRAIN_CHUNK * 3;                      // [CHUNK][3]
-    const int j = threadIdx.x;
-    for (uint32_t k = j; k < CACHE_PARAMS; k += TRAIN_THREADS) {
-        s_w[k] = w[k];
-        s_dw[k] = 0.0f;
+                                                                    float inv_count, uint32_t* err) {
+    inv_count = inv_count / TT_GRAD_SCALE;  // the output gradient was scaled by TT_GRAD_SCALE
+    extern __shared__ uint8_t tt_smem_raw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tt_smem_raw) + 1023u) & ~uintptr_t(1023));
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(sm + TT_OFF_BAR);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + TT_OFF_BAR + 8);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t base = smem_u32(sm);
+
+    // weights: forward [out][in] and backward [in][out], FP16, core-matrix layout
+    for (uint32_t e = tid; e < CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH; e += TC_THREADS) {
+        uint32_t l = e / (CACHE_WIDTH * CACHE_WIDTH), o = (e / CACHE_WIDTH) % CACHE_WIDTH, i = e % CACHE_WIDTH;
+        __half v = w16[e];
+        *reinterpret_cast<__half*>(sm + l * TC_W_BYTES + core_offset_k(o, i, 64)) = v;
+        *reinterpret_cast<__half*>(sm + TT_OFF_WB + l * TC_W_BYTES + core_offset_k(i, o, 64)) = v;
     }
-    float block_loss = 0.0f;
-    uint32_t chunks = (n + TRAIN_CHUNK - 1) / TRAIN_CHUNK;
-    for (uint32_t chunk = blockIdx.x; chunk < chunks; chunk += gridDim.x) {
-        uint32_t base = chunk * TRAIN_CHUNK;
+    for (uint32_t e = tid; e < 16u * CACHE_WIDTH; e += TC_THREADS) {
+        uint32_t o = e / CACHE_WIDTH, i = e % CACHE_WIDTH;
+        __half v = o < (uint32_t)CACHE_OUT_ROWS ? w16[CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH + e]
+                                                : __float2half_rn(0.0f);
+        *reinterpret_cast<__half*>(sm + 4 * TC_W_BYTES + core_offset_k(o, i, 64)) = v;
+        *reinterpret_cast<__half*>(sm + TT_OFF_WB + 4 * TC_W_BYTES + core_offset_k(i, o, 16)) = v;
+    }
+    // rows 64..127 of the transposed A operand stay zero
+    for (uint32_t e = tid; e < 64u * 128u / 8u; e += TC_THREADS) {
+        uint32_t r = 64u + e / 16u, c = (e % 16u) * 8u;
+        *reinterpret_cast<uint4*>(sm + TT_OFF_AT + core_offset_k(r, c, 128)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(s_bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(s_tmem)),
+                     "r"(TT_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t bar = smem_u32(s_bar);
+    const uint32_t lane = tmem + ((32u * warp) << 16);
+    uint32_t phase = 0;
+    bool ok = true;
+    uint32_t done_tiles = 0;
+    float my_loss = 0.0f;
+
+    // one MMA batch: barrier, issue by thread 0, commit, bounded wait (CTA-uniform verdict)
+    auto run = [&](auto issue) {
+        fence_async_smem();
+        tc_fence_before();
         __syncthreads();
-        if (j < TRAIN_CHUNK) {
-            float x[CACHE_WIDTH];
-            if (base + j < n) encode(q[base + j], grid, x);
-            else for (int k = 0; k < CACHE_WIDTH; ++k) x[k] = 0.0f;
-            for (int k = 0; k < CACHE_WIDTH; ++k) act[j * CACHE_WIDTH + k] = x[k];
+        tc_fence_after();
+        if (tid == 0) {
+            issue();
+            mma_commit(bar);
         }
-        __syncthreads();
-        for (int l = 0; l < CACHE_HIDDEN_LAYERS; ++l) {  // forward
-            const float* W = s_w + l * CACHE_WIDTH * CACHE_WIDTH + j * CACHE_WIDTH;
-            const float* in = act + l * TRAIN_CHUNK * CACHE_WIDTH;
-            float* out = act + (l + 1) * TRAIN_CHUNK * CACHE_WIDTH;
-            for (int s = 0; s < TRAIN_CHUNK; ++s) {
-                float z = 0.0f;
-                for (int k = 0; k < CACHE_WIDTH; ++k) z += W[k] * in[s * CACHE_WIDTH + k];
-                out[s * CACHE_WIDTH + j] = fmaxf(z, 0.0f);
+        ok = __syncthreads_and(bar_wait(bar, phase) ? 1 : 0) != 0;
+        phase ^= 1u;
+        tc_fence_after();
+        return ok;
+    };
+
+    const uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
+    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const uint32_t i = tile * TC_ROWS + tid;
+        const bool valid = i < n;
+        const bool acc = done_tiles > 0;
+        uint8_t* h0 = sm + TT_OFF_H;
+        if (valid) encode_row(q[i], grid, h0, tid);
+        else zero_row(h0, tid);
+        // forward
+        for (int l = 0; l < CACHE_HIDDEN_LAYERS && ok; ++l) {
+            uint32_t a = base + TT_OFF_H + (uint32_t)l * TT_H_BYTES, b = base + (uint32_t)l * TC_W_BYTES;
+            if (!run([&] { mma_chain(tmem, a, b, 64, 64, 4, false); })) break;
+            uint8_t* hn = sm + TT_OFF_H + (uint32_t)(l + 1) * TT_H_BYTES;
+#pragma unroll
+            for (int c = 0; c < CACHE_WIDTH; c += 16) {
+                float v[16];
+                tmem_ld16(lane + (uint32_t)c, v);
+                tmem_ld_wait();
+                store_relu16(hn, tid, (uint32_t)c, v);
             }
-            __syncthreads();
         }
-        const float* Wo = s_w + CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH;
-        const float* h4 = act + 4 * TRAIN_CHUNK * CACHE_WIDTH;
-        if (j < 3) {  // output and loss gradient
-            for (int s = 0; s < TRAIN_CHUNK; ++s) {
-                float z = 0.0f;
-                for (int k = 0; k < CACHE_WIDTH; ++k) z += Wo[j * CACHE_WIDTH + k] * h4[s * CACHE_WIDTH + k];
-                y[s * 3 + j] = z;
-                float g = 0.0f;
-                if (base + s < n) {
-                    float d = z - target[3ull * (base + s) + j];
-                    float den = z * z + 0.01f;
-                    block_loss += d * d / den;
-                    g = 2.0f * d / den * inv_count;
+        if (!ok) break;
+        if (!run([&] { mma_chain(tmem, base + TT_OFF_H + 4 * TT_H_BYTES, base + 4 * TC_W_BYTES, 64, 16, 4, false); }))
+            break;
+        // loss and output gradient (rows of padding samples are zero)
+        {
+            float v[16];
+            tmem_ld16(lane, v);
+            tmem_ld_wait();
+            float g[3] = {0.0f, 0.0f, 0.0f};
+            if (valid) {
+                for (int c = 0; c < 3; ++c) {
+                    float d = v[c] - target[3ull * i + c];
+                    float den = v[c] * v[c] + 0.01f;
+                    my_loss += d * d / den;
+                    g[c] = fminf(fmaxf(2.0f * d / den, -TT_GRAD_CLAMP), TT_GRAD_CLAMP) * TT_GRAD_SCALE;
                 }
-                dy[s * 3 + j] = g;
             }
+            for (uint32_t c = 0; c < 16; ++c) {
+                float x = c < 3 ? g[c] : 0.0f;
+                store_half(sm + TT_OFF_DY, core_offset_k(tid, c, 16), x);
+                store_half(sm + TT_OFF_DYT, core_offset_k(c, tid, 128), x);
+            }
+            // H4^T as the A operand of the output layer's gradient, transposed: D[in][out]
+            const uint8_t* h4 = sm + TT_OFF_H + 4 * TT_H_BYTES;
+            for (uint32_t c = 0; c < 64; ++c)
+                store_half(sm + TT_OFF_AT, core_offset_k(c, tid, 128), load_half(h4, core_offset_k(tid, c, 64)));
         }
-        __syncthreads();
-        float* dcur = delta;
-        float* dnext = delta + TRAIN_CHUNK * CACHE_WIDTH;
-        {  // output layer: weight gradients (rows 0..2) and the delta of hidden layer 4
-            for (int r = 0; r < 3; ++r) {
-                float acc = 0.0f;
-                for (int s = 0; s < TRAIN_CHUNK; ++s) acc += dy[s * 3 + r] * h4[s * CACHE_WIDTH + j];
-                s_dw[CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH + r * CACHE_WIDTH + j] += acc;
+        // dW_out^T += H4^T . dy (N 16) and the gradient of H4: dy . W_out (K 16)
+        if (!run([&] {
+                mma_chain(tmem + 320u, base + TT_OFF_AT, base + TT_OFF_DYT, 128, 16, 8, acc);
+                mma_chain(tmem, base + TT_OFF_DY, base + TT_OFF_WB + 4 * TC_W_BYTES, 16, 64, 1, false);
+            }))
+            break;
+        // hidden layers, last to first: delta_l = grad(H_{l+1}) * (H_{l+1} > 0)
+        for (int l = CACHE_HIDDEN_LAYERS - 1; l >= 0 && ok; --l) {
+            const uint8_t* hout = sm + TT_OFF_H + (uint32_t)(l + 1) * TT_H_BYTES;
+            const uint8_t* hin = sm + TT_OFF_H + (uint32_t)l * TT_H_BYTES;
+#pragma unroll
+            for (int c = 0; c < CACHE_WIDTH; c += 16) {
+                float v[16];
+                tmem_ld16(lane + (uint32_t)c, v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    uint32_t col = (uint32_t)(c + k);
+                    float d = load_half(hout, core_offset_k(tid, col, 64)) > 0.0f ? v[k] : 0.0f;
+                    store_half(sm + TT_OFF_G, core_offset_k(tid, col, 64), d);
+                    store_half(sm + TT_OFF_AT, core_offset_k(col, tid, 128), d);
+                    store_half(sm + TT_OFF_BT, core_offset_k(col, tid, 128), load_half(hin, core_offset_k(tid, col, 64)));
+                }
             }
-            for (int s = 0; s < TRAIN_CHUNK; ++s) {
-                float d = 0.0f;
-                for (int r = 0; r < 3; ++r) d += Wo[r * CACHE_WIDTH + j] * dy[s * 3 + r];
-                dcur[s * CACHE_WIDTH + j] = h4[s * CACHE_WIDTH + j] > 0.0f ? d : 0.0f;
-            }
+            const uint32_t dw = tmem + 64u + 64u * (uint32_t)l;
+            const uint32_t wb = base + TT_OFF_WB + (uint32_t)l * TC_W_BYTES;
+            if (!run([&] {
+                    mma_chain(dw, base + TT_OFF_AT, base + TT_OFF_BT, 128, 64, 8, acc);  // dW_l += delta^T . H_l
+                    mma_chain(tmem, base + TT_OFF_G, wb, 64, 64, 4, false);              // grad(H_l) = delta . W_l
+                }))
+                break;
         }
-        __syncthreads();
-        for (int l = CACHE_HIDDEN_LAYERS - 1; l >= 0; --l) {  // hidden layers, last to first
-            const float* in = act + l * TRAIN_CHUNK * CACHE_WIDTH;
-            const float* W = s_w + l * CACHE_WIDTH * CACHE_WIDTH;
-            float* dW = s_dw + l * CACHE_WIDTH * CACHE_WIDTH;
-            for (int k = 0; k < CACHE_WIDTH; ++k) {  // row j of dW_l
-                float acc = 0.0f;
-                for (int s = 0; s < TRAIN_CHUNK; ++s) acc += dcur[s * CACHE_WIDTH + j] * in[s * CACHE_WIDTH + k];
-                dW[j * CACHE_WIDTH + k] += acc;
-            }
-            for (int s = 0; s < TRAIN_CHUNK; ++s) {  // delta of this layer's input, component j
-                float d = 0.0f;
-                for (int r = 0; r < CACHE_WIDTH; ++r) d += W[r * CACHE_WIDTH + j] * dcur[s * CACHE_WIDTH + r];
-                dnext[s * CACHE_WIDTH + j] = (l == 0 || in[s * CACHE_WIDTH + j] > 0.0f) ? d : 0.0f;
-            }
-            __syncthreads();
-            float* tmp = dcur;
-            dcur = dnext;
-            dnext = tmp;
-        }
-        // dcur: gradient of the inputs; grid features are inputs 0..31
-        if (j < TRAIN_CHUNK && base + j < n) {
-            const CacheQuery& qq = q[base + j];
-            float3 p = make_float3(fminf(fmaxf(qq.pos[0], 0.0f), 1.0f), fminf(fmaxf(qq.pos[1], 0.0f), 1.0f),
-                                   fminf(fmaxf(qq.pos[2], 0.0f), 1.0f));
+        if (!ok) break;
+        // grad(H0): the 32 grid-feature columns scatter onto the grid (the TMEM loads are
+        // warp-collective, so every lane loads)
+        float gx[32];
+        tmem_ld16(lane, gx);
+        tmem_ld16(lane + 16u, gx + 16);
+        tmem_ld_wait();
+        if (valid) {
+            float3 p = make_float3(fminf(fmaxf(q[i].pos[0], 0.0f), 1.0f), fminf(fmaxf(q[i].pos[1], 0.0f), 1.0f),
+                                   fminf(fmaxf(q[i].pos[2], 0.0f), 1.0f));
             for (int l = 0; l < CACHE_LEVELS; ++l) {
                 uint32_t idx[8];
-                float wc[8];
-                grid_corners(p, l, idx, wc);
-                float g0 = dcur[j * CACHE_WIDTH + 2 * l], g1 = dcur[j * CACHE_WIDTH + 2 * l + 1];
+                float wgt[8];
+                grid_corners(p, l, idx, wgt);
                 float* gg = grid_grad + 2ull * CACHE_TABLE * l;
+                float g0 = gx[2 * l] * inv_count, g1 = gx[2 * l + 1] * inv_count;
+#pragma unroll
                 for (int c = 0; c < 8; ++c) {
-                    if (g0 != 0.0f) atomicAdd(gg + 2ull * idx[c], wc[c] * g0);
-                    if (g1 != 0.0f) atomicAdd(gg + 2ull * idx[c] + 1, wc[c] * g1);
+                    atomicAdd(gg + 2ull * idx[c], wgt[c] * g0);
+                    atomicAdd(gg + 2ull * idx[c] + 1, wgt[c] * g1);
                 }
             }
         }
+        ++done_tiles;
     }
+    // weight gradients leave TMEM once: lanes 0..63 hold the output neurons of each layer
+    tc_fence_before();
     __syncthreads();
-    for (uint32_t k = j; k < CACHE_PARAMS; k += TRAIN_THREADS)
-        if (s_dw[k] != 0.0f) atomicAdd(w_grad + k, s_dw[k]);
-    if (j < 3 && block_loss != 0.0f) atomicAdd(loss, block_loss);
+    tc_fence_after();
+    if (ok && done_tiles > 0 && warp < 2) {
+        for (int l = 0; l < CACHE_HIDDEN_LAYERS; ++l) {
+            for (int c = 0; c < CACHE_WIDTH; c += 16) {
+                float v[16];
+                tmem_ld16(lane + 64u + 64u * (uint32_t)l + (uint32_t)c, v);
+                tmem_ld_wait();
+                float* dst = w_grad + (uint64_t)l * CACHE_WIDTH * CACHE_WIDTH + (uint64_t)tid * CACHE_WIDTH + c;
+                for (int k = 0; k < 16; ++k) atomicAdd(dst + k, v[k] * inv_count);
+            }
+        }
+        float v[16];
+        tmem_ld16(lane + 320u, v);  // lane = input neuron, columns = outputs
+        tmem_ld_wait();
+        for (int o = 0; o < 3; ++o)
+            atomicAdd(w_grad + CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH + (uint64_t)o * CACHE_WIDTH + tid, v[o] * inv_count);
+    }
+    float block_loss = my_loss;
+    for (int o = 16; o > 0; o >>= 1) block_loss += __shfl_down_sync(0xffffffffu, block_loss, o);
+    if ((tid & 31u) == 0 && block_loss != 0.0f) atomicAdd(loss, block_loss);
+    if (!ok && err) atomicOr(err, ERR_TENSOR_WAIT);
+    tc_fence_before();
+    __syncthreads();
+    if (!ok) bar_wait(bar, phase ^ 1u);
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TT_TMEM_COLS)
+                     : "memory");
 }
 
 // Adam on `count` parameters; the gradient is consumed (zeroed).  FP16 copy when w16 != null.
@@ -537,19 +651,19 @@ void cache_targets(const TrainRecord* rec, const uint32_t* rec_count, uint32_t c
 }
 
 void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
-                      uint32_t step, cudaStream_t st) {
+                      uint32_t step, uint32_t* err, cudaStream_t st) {
     if (n == 0) return;
     static bool attr = false;
     if (!attr) {
-        check_cuda(cudaFuncSetAttribute(cache_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TRAIN_SMEM),
+        check_cuda(cudaFuncSetAttribute(cache_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TT_SMEM),
                    "train smem");
         attr = true;
     }
-    uint32_t chunks = (n + TRAIN_CHUNK - 1) / TRAIN_CHUNK;
-    uint32_t blocks = std::min<uint32_t>(chunks, 152u);
+    uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
+    uint32_t blocks = std::min<uint32_t>(tiles, 152u);
     check_cuda(cudaMemsetAsync(d.loss, 0, 4, st), "memset");
-    cache_train_kernel<<<blocks, TRAIN_THREADS, TRAIN_SMEM, st>>>(q, target, n, d.grid, d.w, d.w_grad, d.grid_grad,
-                                                                  d.loss, 1.0f / (3.0f * (float)n));
+    cache_train_tc_kernel<<<blocks, TC_THREADS, TT_SMEM, st>>>(q, target, n, d.grid, d.w16, d.w_grad, d.grid_grad,
+                                                               d.loss, 1.0f / (3.0f * (float)n), err);
     float c1 = 1.0f - std::pow(0.9f, (float)step), c2 = 1.0f - std::pow(0.99f, (float)step);
     cache_adam_kernel<<<(CACHE_PARAMS + 255) / 256, 256, 0, st>>>(d.w, d.w_m, d.w_v, d.w_grad, d.w16, CACHE_PARAMS,
                                                                   lr, c1, c2);

@@ -38,7 +38,7 @@ struct CacheDevice {
 void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* out, uint32_t* err, cudaStream_t st);
 // One Adam step on n samples: gradients of the mean relative L2 loss.
 void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
-                      uint32_t step, cudaStream_t st);
+                      uint32_t step, uint32_t* err, cudaStream_t st);
 void cache_init(const CacheDevice& d, uint32_t seed, cudaStream_t st);
 // Queries whose count is in device memory (at most max_n of them).
 void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,
