@@ -61,6 +61,7 @@ def parse_args():
     p.add_argument("--no-cache", action="store_true", help="skip the radiance-cache sample")
     p.add_argument("--no-textured", action="store_true", help="skip the textured-materials sample")
     p.add_argument("--no-ingest", action="store_true", help="skip the device mesh-ingest sample")
+    p.add_argument("--no-light-selection", action="store_true", help="skip the light-selection sample")
     p.add_argument("--serve-rates", default="2,8,32", help="Poisson arrival rates (requests/s) of the serving sample")
     p.add_argument("--serve-requests", type=int, default=12, help="requests per arrival rate")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level"],
@@ -430,6 +431,61 @@ def run_textured(a, device: int) -> dict:
     return out
 
 
+# ---------------------------------------------------------------- light-selection sample
+def run_light_selection(a, device: int) -> dict:
+    """Power-proportional light selection (TT_LIGHT_SELECTION_POWER, an alias table over the
+    1000 log-normal lights) against the reference's uniform pick on the benchmark field at
+    960x540, depth 8, 16 spp: device time (CUDA events, 4 frames averaged) and error against a
+    16,384-spp uniform reference, by tonemapped MSE and MSE; equal-error speed-up =
+    (t_uniform e_uniform) / (t_power e_power).  The two estimators converge to the same image."""
+    import ctypes
+
+    from tinytrace_gb300 import native
+    from tinytrace_gb300.native import check
+    from tinytrace_gb300.renderer import Config, Renderer
+
+    W, H = a.width // 2, a.height // 2
+    w = make_workload(a)
+    r = Renderer((W, H), device=device)
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    lib, ctx = r.context.lib, r.context.handle
+
+    def frame(spp):
+        r.set_config(Config(bounce_count=a.depth, sample_count=spp))
+        r.reset_accumulation()
+        check(lib.tt_synchronize(ctx))
+        check(lib.tt_event_record(ctx, 4))
+        r.render_to_target()
+        check(lib.tt_event_record(ctx, 5))
+        ms = ctypes.c_float()
+        check(lib.tt_event_elapsed_ms(ctx, 4, 5, ctypes.byref(ms)))
+        img = r.context.download(r.render_target, W, H)[..., :3].astype(np.float64)
+        r.present()
+        return img, ms.value
+
+    ref = np.zeros((H, W, 3))
+    for _ in range(16):
+        ref += frame(1024)[0] / 16.0
+    tref = ref / (1.0 + ref)
+    out = {"workload": f"icosphere_field_{W}x{H}_16spp_d{a.depth}", "reference_spp": 16384, "modes": {}}
+    for name, value in (("uniform", native.TT_LIGHT_SELECTION_UNIFORM), ("power", native.TT_LIGHT_SELECTION_POWER)):
+        check(lib.tt_set_option(ctx, native.TT_OPTION_LIGHT_SELECTION, value))
+        frame(16)
+        ms = tm = mse = 0.0
+        for _ in range(4):
+            img, t = frame(16)
+            ms += t / 4.0
+            tm += float(np.mean((img / (1.0 + img) - tref) ** 2)) / 4.0
+            mse += float(np.mean((img - ref) ** 2)) / 4.0
+        out["modes"][name] = {"ms": ms, "tonemapped_mse": tm, "mse": mse, "mean": float(img.mean())}
+    u, p = out["modes"]["uniform"], out["modes"]["power"]
+    out["equal_error_speedup_tonemapped"] = (u["ms"] * u["tonemapped_mse"]) / (p["ms"] * p["tonemapped_mse"])
+    out["equal_error_speedup_mse"] = (u["ms"] * u["mse"]) / (p["ms"] * p["mse"])
+    r.close()
+    return out
+
+
 # ---------------------------------------------------------------- device ingest sample
 def _grid_mesh(n: int):
     """A height-field grid of n x n vertices, 2 (n - 1)^2 triangles, with texture coordinates."""
@@ -734,6 +790,11 @@ def run_ours(a, dist: Dist):
                 out_line["textured"] = run_textured(a, device)
             except Exception as e:
                 out_line["textured"] = {"error": f"{type(e).__name__}: {e}"}
+        if not a.no_light_selection and dist.world == 1:
+            try:
+                out_line["light_selection"] = run_light_selection(a, device)
+            except Exception as e:
+                out_line["light_selection"] = {"error": f"{type(e).__name__}: {e}"}
         if not a.no_ingest and dist.world == 1:
             try:
                 out_line["ingest"] = run_ingest(a, device)

@@ -76,6 +76,12 @@ extern "C" {
                                           equals the light's 16-bit hash; lights at global triangle index
                                           >= 65535 never pass (parity, default) */
 #define TT_LIGHT_VISIBILITY_TRIANGLE 1 /* the hit is the sampled emissive triangle itself (full 32-bit id) */
+#define TT_OPTION_LIGHT_SELECTION 10   /* TT_LIGHT_SELECTION_*: how next-event estimation picks a light */
+#define TT_LIGHT_SELECTION_UNIFORM 0   /* the reference's uniform pick, random_uint(count) (default) */
+#define TT_LIGHT_SELECTION_POWER 1     /* proportional to emitted power (luminance x emission x world area)
+                                          through an alias table built at scene creation (Vose's method in
+                                          double precision); draws: random_uint(count), then one float for
+                                          the alias coin; the density uses the light's own probability */
 /* acceleration structures (tt_set_option TT_OPTION_ACCEL; tt_scene_stats.accel) */
 #define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
 #define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */

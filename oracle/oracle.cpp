@@ -43,6 +43,8 @@ struct OracleScene {
     std::vector<Texture> textures;
     SceneBvh bvh;
     std::vector<uint32_t> light_prim;  // primitive of each emissive triangle in its instance's mesh
+    std::vector<LightAlias> light_alias;  // power-proportional selection (built for every scene)
+    bool light_power = false;             // next-event estimation picks lights through light_alias
     bool light_exact = false;          // visibility tests the sampled triangle itself (full id)
     bool use_bvh = true;
     bool flat = false;  // the integrator traces through the flat BVH instead of the two-level one
@@ -52,7 +54,8 @@ struct OracleScene {
     }
     SceneView view() const {
         return SceneView{positions.data(), indices.data(), vertices.data(), materials.data(),
-                         instances.data(), emissive.data(), (uint32_t)emissive.size()};
+                         instances.data(), emissive.data(), (uint32_t)emissive.size(),
+                         light_power && !light_alias.empty() ? light_alias.data() : nullptr};
     }
 };
 
@@ -587,6 +590,61 @@ void copy_in(std::vector<T>& dst, const void* src, uint64_t count) {
 
 extern "C" {
 
+// Alias table by emitted power: emission_luminance x luminance(emission_color) x world-space
+// area in double precision (area alone for textured emission), Vose's method with index-ordered
+// work stacks, as the library builds it (the table is an input the CUDA path receives).
+std::vector<LightAlias> build_light_alias(const OracleScene& s) {
+    uint32_t n = (uint32_t)s.emissive.size();
+    std::vector<LightAlias> out(n);
+    if (n == 0) return out;
+    std::vector<double> power(n);
+    double total = 0.0;
+    for (uint32_t e = 0; e < n; ++e) {
+        const EmissiveTriangle& t = s.emissive[e];
+        const Instance& in = s.instances[t.instance_index];
+        const Material& m = s.materials[in.material_index];
+        double p[3][3];
+        for (int k = 0; k < 3; ++k) {
+            double v[3] = {t.positions[k][0] / 32767.0, t.positions[k][1] / 32767.0, t.positions[k][2] / 32767.0};
+            for (int r = 0; r < 3; ++r)
+                p[k][r] = in.transform[r] * v[0] + in.transform[4 + r] * v[1] + in.transform[8 + r] * v[2] +
+                          in.transform[12 + r];
+        }
+        double e1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+        double e2[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+        double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        double area = 0.5 * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        bool textured = m.textures[T_EMISSION_COLOR] != NO_TEXTURE || m.textures[T_EMISSION_LUMINANCE] != NO_TEXTURE;
+        const MaterialConstants& mc = m.constants;
+        double lum = 0.2126 * mc.emission_color.x + 0.7152 * mc.emission_color.y + 0.0722 * mc.emission_color.z;
+        double pw = textured ? area : (double)mc.emission_luminance * lum * area;
+        power[e] = std::isfinite(pw) && pw > 0.0 ? pw : 0.0;
+        total += power[e];
+    }
+    if (!(total > 0.0)) {
+        for (uint32_t e = 0; e < n; ++e) out[e] = LightAlias{1.0f, e, (float)(1.0 / n)};
+        return out;
+    }
+    std::vector<double> scaled(n), keep(n, 1.0);
+    std::vector<uint32_t> small, large, alias(n);
+    for (uint32_t e = 0; e < n; ++e) {
+        scaled[e] = power[e] / total * (double)n;
+        (scaled[e] < 1.0 ? small : large).push_back(e);
+        alias[e] = e;
+    }
+    while (!small.empty() && !large.empty()) {
+        uint32_t sm = small.back(), lg = large.back();
+        small.pop_back();
+        large.pop_back();
+        keep[sm] = scaled[sm];
+        alias[sm] = lg;
+        scaled[lg] = (scaled[lg] + scaled[sm]) - 1.0;
+        (scaled[lg] < 1.0 ? small : large).push_back(lg);
+    }
+    for (uint32_t e = 0; e < n; ++e) out[e] = LightAlias{(float)keep[e], alias[e], (float)(power[e] / total)};
+    return out;
+}
+
 // Layout of tt_scene_desc (include/tinytrace_cuda.h): pointers + counts.
 struct OracleSceneDesc {
     const int16_t* positions;
@@ -634,6 +692,7 @@ void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
         }
     }
     s->light_prim = r_light_prims(*s);
+    s->light_alias = build_light_alias(*s);
     s->use_bvh = accel != 0;
     s->flat = accel == 2;
     if (s->use_bvh) s->bvh = build_scene_bvh(s->geom(), leaf_max);
@@ -641,6 +700,9 @@ void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
 }
 
 void oracle_scene_destroy(void* p) { delete static_cast<OracleScene*>(p); }
+
+// 0: the reference's uniform light pick; 1: power-proportional through the alias table.
+void oracle_scene_set_light_power(void* p, int power) { static_cast<OracleScene*>(p)->light_power = power != 0; }
 
 // 0: the reference's 16-bit hash visibility test; 1: the sampled triangle itself.
 void oracle_scene_set_light_exact(void* p, int exact) { static_cast<OracleScene*>(p)->light_exact = exact != 0; }
@@ -783,6 +845,7 @@ void oracle_scene_update_instances(void* p, const Instance* instances, uint32_t 
     if (count != s->instances.size()) return;
     std::memcpy(s->instances.data(), instances, sizeof(Instance) * count);
     if (s->use_bvh) refit_world_structures(s->geom(), s->bvh);
+    s->light_alias = build_light_alias(*s);
 }
 
 // ReSTIR DI state of the oracle: config = {candidates, m_cap_factor, neighbours, radius}.

@@ -68,6 +68,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_restir_reservoirs.argtypes = [_P, _P]
         lib.oracle_atan2.argtypes = [_P, _P, ctypes.c_uint64, _P]
         lib.oracle_scene_set_light_exact.argtypes = [_P, ctypes.c_int]
+        lib.oracle_scene_set_light_power.argtypes = [_P, ctypes.c_int]
         lib.oracle_texture_sample.argtypes = [_P, ctypes.c_uint32, _P, ctypes.c_uint32, _P]
         lib.oracle_mesh_ingest.restype = ctypes.c_int
         lib.oracle_mesh_ingest.argtypes = [_P, _P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P]
@@ -104,6 +105,11 @@ class OracleScene:
         """Visibility of next-event estimation: the reference's hash test (False) or the sampled
         triangle itself (True)."""
         self.lib.oracle_scene_set_light_exact(self.handle, 1 if exact else 0)
+
+    def set_light_power(self, power: bool) -> None:
+        """Light selection of next-event estimation: uniform (False, the reference's) or by
+        emitted power through the alias table (True)."""
+        self.lib.oracle_scene_set_light_power(self.handle, 1 if power else 0)
 
     def texture_sample(self, index: int, uvl: np.ndarray) -> np.ndarray:
         """textureLod of texture `index` at (n, 3) (u, v, lod) -> (n, 4) RGBA."""

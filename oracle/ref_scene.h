@@ -214,6 +214,13 @@ inline v2 interp2(v3 b, v2 a0, v2 a1, v2 a2) {
 }
 inline v2 uv_of(const uint16_t* h) { return v2{half_to_float(h[0]), half_to_float(h[1])}; }
 
+// Alias-table entry of one emissive triangle (power-proportional light selection).
+struct LightAlias {
+    float keep;
+    uint32_t alias;
+    float pdf;
+};
+
 struct SceneView {
     const int16_t* positions;  // [i16;3]
     const uint32_t* indices;
@@ -222,6 +229,7 @@ struct SceneView {
     const Instance* instances;
     const EmissiveTriangle* emissive;
     uint32_t emissive_count;
+    const LightAlias* light_alias;  // non-null: pick lights by power
 };
 
 // ---------------------------------------------------------------- scene.glsl:107-136
@@ -234,6 +242,12 @@ struct DirectLightSample {
 };
 inline DirectLightSample sample_random_light(const SceneView& sc, Generator& g) {
     uint32_t index = random_uint(g, sc.emissive_count);
+    float light_probability = 1.0f / (float)sc.emissive_count;
+    if (sc.light_alias) {  // keep `index` with its probability, else its alias
+        float coin = random_float(g);
+        if (!(coin < sc.light_alias[index].keep)) index = sc.light_alias[index].alias;
+        light_probability = sc.light_alias[index].pdf;
+    }
     const EmissiveTriangle& tri = sc.emissive[index];
     v3 bary = sample_triangle(random_vec2(g));
     const float* m = sc.instances[tri.instance_index].transform;
@@ -248,7 +262,7 @@ inline DirectLightSample sample_random_light(const SceneView& sc, Generator& g) 
     s.barycentric = bary;
     s.instance = tri.instance_index;
     s.hash = (uint32_t)tri.hash;
-    s.light_probability = 1.0f / (float)sc.emissive_count;
+    s.light_probability = light_probability;
     s.index = index;
     return s;
 }

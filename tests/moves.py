@@ -10,12 +10,16 @@ def _rotation(rng, angle):
     return np.eye(3) + np.sin(angle) * k + (1 - np.cos(angle)) * (k @ k)
 
 
-def moved_instances(instances: np.ndarray, rng, max_angle=0.6, max_shift=3.0) -> np.ndarray:
+def moved_instances(instances: np.ndarray, rng, max_angle=0.6, max_shift=3.0, scale=0.0) -> np.ndarray:
+    """`scale` > 0 also scales each instance about its centre by a factor in [1 - scale, 1 + scale]
+    (world-space areas change)."""
     out = instances.copy()
     for i in range(len(out)):
         t = np.asarray(out[i]["transform"], np.float64).reshape(4, 4).T
         m = np.eye(4)
         r = _rotation(rng, rng.uniform(-max_angle, max_angle))
+        if scale > 0.0:
+            r = r * rng.uniform(1.0 - scale, 1.0 + scale)
         c = t[:3, 3]
         m[:3, :3] = r
         m[:3, 3] = c - r @ c + rng.uniform(-max_shift, max_shift, 3)

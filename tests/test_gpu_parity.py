@@ -304,3 +304,33 @@ def test_light_visibility_modes(gpu_context, integrator, mode):
     c = make_constants(cam, extent, cfg, r.context.frame_index(), r.accumulated_frame_count)
     assert_same_bits(r.render_to_texture(), orc.render(c), f"light visibility {mode} {integrator}")
     r.close()
+
+
+@pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
+def test_power_light_selection(gpu_context, integrator):
+    """Power-proportional light selection through the alias table, bit for bit with the
+    oracle's restatement, before and after the instances move (the table follows the new
+    world-space areas)."""
+    from moves import moved_instances
+    from tinytrace_gb300.renderer import Renderer
+
+    w = scenes.icosphere_workload(extent=(64, 40), spp=3, depth=4, instances=6, freq=8, lights=300)
+    r = Renderer(w.extent)
+    lib, hd = r.context.lib, r.context.handle
+    check(lib.tt_set_option(hd, native.TT_OPTION_INTEGRATOR, INTEGRATORS[integrator]))
+    check(lib.tt_set_option(hd, native.TT_OPTION_LIGHT_SELECTION, native.TT_LIGHT_SELECTION_POWER))
+    assert lib.tt_set_option(hd, native.TT_OPTION_LIGHT_SELECTION, 5) == native.TT_ERR_INVALID_ARGUMENT
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    r.set_config(w.config)
+    orc = oracle.OracleScene(r.scene_arrays)
+    orc.set_light_power(True)
+    c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
+    assert_same_bits(r.render_to_texture(), orc.render(c), f"power selection {integrator}")
+    inst = moved_instances(r.scene_arrays.instances, np.random.default_rng(4), scale=0.2)
+    check(lib.tt_scene_update_instances(hd, r.scene, native.ptr(inst), len(inst)))
+    orc.update_instances(inst)
+    r.reset_accumulation()
+    c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
+    assert_same_bits(r.render_to_texture(), orc.render(c), f"power selection after update {integrator}")
+    r.close()

@@ -26,7 +26,7 @@ NVCC_FLAGS = ARCH + [
     "-std=c++17",
     "-fmad=false",
     "-Xcompiler",
-    "-fPIC",
+    "-fPIC,-ffp-contract=off",
     "-Xptxas",
     "-warn-spills",
 ]

@@ -75,11 +75,13 @@ struct ImageRes {
 
 struct SceneRes {
     DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform, inst_bucket, light_prim;
-    DeviceBuffer tex_table, tex_data, srgb;
+    DeviceBuffer tex_table, tex_data, srgb, light_alias;
     BvhResult bvh;
     DevScene dev{};
     tt_scene_stats stats{};
     std::vector<tt_instance> host_instances;  // for tt_scene_update_instances' checks
+    std::vector<tt_emissive_triangle> host_emissive;  // to rebuild the light alias table on updates
+    std::vector<tt_material> host_materials;
     uint32_t material_count = 0;
 };
 
@@ -149,6 +151,7 @@ struct tt_context {
     bool stage_timing = false;
     bool graphs = true;
     uint32_t light_visibility = TT_LIGHT_VISIBILITY_HASH;  // TT_OPTION_LIGHT_VISIBILITY
+    uint32_t light_selection = TT_LIGHT_SELECTION_UNIFORM; // TT_OPTION_LIGHT_SELECTION
     uint32_t refill_lanes = 20;       // TT_OPTION_REFILL_LANES
     uint32_t trace_blocks_per_sm = 0; // TT_OPTION_TRACE_BLOCKS_PER_SM (0 = as many as fit)
     int occupancy_sms = 0, occupancy_blocks = 0;
@@ -285,6 +288,70 @@ std::vector<uint32_t> light_primitives(const tt_scene_desc* d) {
         }
         if (out[e] != 0xffffffffu) next[t.instance_index] = out[e] + 1u;
     }
+    return out;
+}
+
+// Alias table of the emissive triangles by emitted power (TT_LIGHT_SELECTION_POWER): power =
+// emission_luminance x luminance(emission_color) x world-space area in double precision (area
+// alone when the emission is textured), Vose's alias method with index-ordered work stacks;
+// entries (keep probability, alias, pdf = power / total, 0).  All powers zero: uniform.
+static float bits_float(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+std::vector<float4> light_alias_table(const tt_scene_desc* d) {
+    uint32_t n = d->emissive_triangle_count;
+    std::vector<float4> out(std::max<uint32_t>(n, 1u), make_float4(1.0f, 0.0f, 0.0f, 0.0f));
+    if (n == 0) return out;
+    std::vector<double> power(n);
+    double total = 0.0;
+    for (uint32_t e = 0; e < n; ++e) {
+        const tt_emissive_triangle& t = d->emissive_triangles[e];
+        const tt_instance& in = d->instances[t.instance_index];
+        const tt_material& m = d->materials[in.material_index];
+        double p[3][3];
+        for (int k = 0; k < 3; ++k) {
+            double v[3] = {t.positions[k][0] / 32767.0, t.positions[k][1] / 32767.0, t.positions[k][2] / 32767.0};
+            for (int r = 0; r < 3; ++r)
+                p[k][r] = in.transform[r] * v[0] + in.transform[4 + r] * v[1] + in.transform[8 + r] * v[2] +
+                          in.transform[12 + r];
+        }
+        double e1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+        double e2[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+        double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        double area = 0.5 * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        bool textured = m.textures[5] != 0xffffffffu || m.textures[25] != 0xffffffffu;
+        const tt_material_constants& mc = m.constants;
+        double lum = 0.2126 * mc.emission_color[0] + 0.7152 * mc.emission_color[1] + 0.0722 * mc.emission_color[2];
+        double pw = textured ? area : (double)mc.emission_luminance * lum * area;
+        power[e] = std::isfinite(pw) && pw > 0.0 ? pw : 0.0;
+        total += power[e];
+    }
+    if (!(total > 0.0)) {
+        for (uint32_t e = 0; e < n; ++e) out[e] = make_float4(1.0f, bits_float(e), (float)(1.0 / n), 0.0f);
+        return out;
+    }
+    std::vector<double> scaled(n);
+    std::vector<uint32_t> small, large;
+    for (uint32_t e = 0; e < n; ++e) {
+        scaled[e] = power[e] / total * (double)n;
+        (scaled[e] < 1.0 ? small : large).push_back(e);
+    }
+    std::vector<uint32_t> alias(n);
+    std::vector<double> keep(n, 1.0);
+    for (uint32_t e = 0; e < n; ++e) alias[e] = e;
+    while (!small.empty() && !large.empty()) {
+        uint32_t s = small.back(), g = large.back();
+        small.pop_back();
+        large.pop_back();
+        keep[s] = scaled[s];
+        alias[s] = g;
+        scaled[g] = (scaled[g] + scaled[s]) - 1.0;
+        (scaled[g] < 1.0 ? small : large).push_back(g);
+    }
+    for (uint32_t e = 0; e < n; ++e)
+        out[e] = make_float4((float)keep[e], bits_float(alias[e]), (float)(power[e] / total), 0.0f);
     return out;
 }
 
@@ -495,6 +562,7 @@ DevScene scene_view(tt_context* ctx, tt_handle scene) {
     require(ctx, "null context");
     DevScene d = lookup<SceneRes>(ctx, scene, KIND_SCENE)->dev;
     d.light_exact = ctx->light_visibility == TT_LIGHT_VISIBILITY_TRIANGLE ? 1u : 0u;
+    d.light_power = ctx->light_selection == TT_LIGHT_SELECTION_POWER ? 1u : 0u;
     return d;
 }
 int context_device(tt_context* ctx) { return ctx->device; }
@@ -594,6 +662,7 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     RenderParams p;
     p.sc = s->dev;
     p.sc.light_exact = ctx->light_visibility == TT_LIGHT_VISIBILITY_TRIANGLE ? 1u : 0u;
+    p.sc.light_power = ctx->light_selection == TT_LIGHT_SELECTION_POWER ? 1u : 0u;
     p.c = *c;
     p.target = img->buf.as<float4>();
     p.err = ctx->err_word.as<uint32_t>();
@@ -815,10 +884,14 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         upload(s->meshes, d->meshes, d->mesh_count, st);
         upload(s->instances, d->instances, d->instance_count, st);
         s->host_instances.assign(d->instances, d->instances + d->instance_count);
+        s->host_emissive.assign(d->emissive_triangles, d->emissive_triangles + d->emissive_triangle_count);
+        s->host_materials.assign(d->materials, d->materials + d->material_count);
         s->material_count = d->material_count;
         upload(s->emissive, d->emissive_triangles, d->emissive_triangle_count, st);
         std::vector<uint32_t> lprim = light_primitives(d);
         upload(s->light_prim, lprim.data(), lprim.size(), st);
+        std::vector<float4> alias = light_alias_table(d);
+        upload(s->light_alias, alias.data(), alias.size(), st);
         std::vector<float4> xf(4ull * d->instance_count);
         for (uint32_t i = 0; i < d->instance_count; ++i) {
             const float* m = d->instances[i].inverse_transform;
@@ -860,6 +933,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.instances = s->instances.as<tt_instance>();
         ds.meshes = s->meshes.as<tt_mesh>();
         ds.light_prim = s->light_prim.as<uint32_t>();
+        ds.light_alias = s->light_alias.as<float4>();
         ds.emissive = s->emissive.as<tt_emissive_triangle>();
         ds.inst_xform = s->inst_xform.as<float4>();
         ds.inst_bucket = s->inst_bucket.as<uint8_t>();
@@ -937,6 +1011,18 @@ int32_t tt_scene_update_instances(tt_context* ctx, tt_handle scene, const tt_ins
             refit_scene_bvh(s->instances.as<tt_instance>(), st, s->bvh);  // synchronises the stream
             s->dev.tlas_bound = s->bvh.flat ? s->bvh.flat_bound : s->bvh.tlas_bound;
             s->host_instances.assign(instances, instances + count);
+            // emitted powers follow the new world-space areas
+            tt_scene_desc ld{};
+            ld.instances = s->host_instances.data();
+            ld.instance_count = count;
+            ld.materials = s->host_materials.data();
+            ld.material_count = (uint32_t)s->host_materials.size();
+            ld.emissive_triangles = s->host_emissive.data();
+            ld.emissive_triangle_count = (uint32_t)s->host_emissive.size();
+            std::vector<float4> alias = light_alias_table(&ld);
+            check_cuda(cudaMemcpyAsync(s->light_alias.ptr, alias.data(), 16ull * alias.size(), cudaMemcpyHostToDevice, st),
+                       "light alias table");
+            check_cuda(cudaStreamSynchronize(st), "light alias table");
         }
     });
 }
@@ -1054,6 +1140,9 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
             require(value == TT_LIGHT_VISIBILITY_HASH || value == TT_LIGHT_VISIBILITY_TRIANGLE,
                     "unknown light visibility");
             ctx->light_visibility = (uint32_t)value;
+        } else if (option == TT_OPTION_LIGHT_SELECTION) {
+            require(value == TT_LIGHT_SELECTION_UNIFORM || value == TT_LIGHT_SELECTION_POWER, "unknown light selection");
+            ctx->light_selection = (uint32_t)value;
         } else if (option == TT_OPTION_RADIANCE_CACHE) {
             require(value <= 1, "radiance cache is 0 or 1");
             ctx->cache.enabled = value != 0;

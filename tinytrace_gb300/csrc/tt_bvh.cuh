@@ -75,6 +75,8 @@ struct DevScene {
     const float* srgb;           // 256-entry sRGB-to-linear table
     uint32_t textured;           // 1 when some material samples a texture
     uint32_t light_exact;        // TT_LIGHT_VISIBILITY_TRIANGLE: shadow rays test the sampled triangle itself
+    uint32_t light_power;        // TT_LIGHT_SELECTION_POWER: lights picked through `light_alias`
+    const float4* light_alias;   // per emissive triangle: (keep probability, alias index bits, pdf, 0)
 };
 
 struct Hit {

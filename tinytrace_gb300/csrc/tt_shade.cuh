@@ -146,6 +146,13 @@ struct LightSample {
 __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 position, const Basis& basis,
                                                     uint32_t& g) {
     uint32_t light = xor_shift(g) % sc.emissive_count;
+    float light_probability = 1.0f / (float)sc.emissive_count;
+    if (sc.light_power) {  // alias table: keep `light` with its probability, else take its alias
+        float4 e = __ldg(sc.light_alias + light);
+        float coin = random_float(g);
+        if (!(coin < e.x)) light = __float_as_uint(e.y);
+        light_probability = __ldg(&sc.light_alias[light].z);
+    }
     const tt_emissive_triangle* tri = sc.emissive + light;
     f2 rnd = random_vec2(g);
     f3 bary = sample_triangle(rnd);
@@ -169,7 +176,6 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 posit
     ls.uv = interp_uv(bary, tc[0], tc[1], tc[2]);
     ls.hash = (uint32_t)__ldg(&tri->hash);
     ls.prim = sc.light_exact ? __ldg(sc.light_prim + light) : 0xffffffffu;
-    float light_probability = 1.0f / (float)sc.emissive_count;
     f3 to_light = lpos - position;
     ls.wo = transform_from_basis(basis, to_light);
     float d2 = dot(to_light, to_light);

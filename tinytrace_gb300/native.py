@@ -38,6 +38,9 @@ TT_FORMAT_RGBA8_UNORM = 1
 TT_OPTION_LIGHT_VISIBILITY = 9
 TT_LIGHT_VISIBILITY_HASH = 0
 TT_LIGHT_VISIBILITY_TRIANGLE = 1
+TT_OPTION_LIGHT_SELECTION = 10
+TT_LIGHT_SELECTION_UNIFORM = 0
+TT_LIGHT_SELECTION_POWER = 1
 TT_TEXTURE_BC1_SRGB = 1
 TT_TEXTURE_BC5_UNORM = 2
 TT_TEXTURE_R8_UNORM = 3
