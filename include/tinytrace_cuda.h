@@ -363,7 +363,8 @@ typedef struct tt_restir_config {
 int32_t tt_restir_configure(tt_context* ctx, const tt_restir_config* config);
 /* Forgets the previous frame (the next frame does no temporal reuse). */
 int32_t tt_restir_reset(tt_context* ctx);
-/* Textured materials are sampled at the primary hit with its ray-differential mip level and
+/* Candidates follow TT_OPTION_LIGHT_SELECTION (uniform, or by emitted power).  Textured
+ * materials are sampled at the primary hit with its ray-differential mip level and
  * at light points with mip level 4, as the path tracer samples them. */
 int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* constants, tt_handle target);
 /* Final reservoirs of the last ReSTIR frame, width * height * 32 bytes (row-major pixels:

@@ -416,11 +416,17 @@ RRes r_initial(const RestirOracle& R, const RSurface& q) {
     float chosen = 0.0f;
     for (uint32_t k = 0; k < R.candidates; ++k) {
         uint32_t light = random_uint(g, (uint32_t)s.emissive.size());
+        float inv_p = lights;
+        if (s.light_power) {  // candidates by emitted power
+            float coin = random_float(g);
+            if (!(coin < s.light_alias[light].keep)) light = s.light_alias[light].alias;
+            inv_p = 1.0f / s.light_alias[light].pdf;
+        }
         float r1 = random_float(g);
         float r2 = random_float(g);
         RLight L = r_light(s, light, r1, r2);
         float ph = r_luminance(r_contribution(st, L));
-        float w = ph * (lights * L.area);
+        float w = ph * (inv_p * L.area);
         if (r_update(r, light, r1, r2, w, 1.0f, g)) chosen = ph;
     }
     r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;

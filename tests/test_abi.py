@@ -57,7 +57,8 @@ def test_constants_match_header():
     for name, value in defines.items():
         if hasattr(native, name):
             assert getattr(native, name) == value, name
-    for name in ("TT_OK", "TT_ERR_NO_DEVICE", "TT_OPTION_ACCEL", "TT_ACCEL_FLAT", "TT_TRACE_NOALLOC_MAX_RAYS"):
+    for name in ("TT_OK", "TT_ERR_NO_DEVICE", "TT_OPTION_ACCEL", "TT_ACCEL_FLAT", "TT_TRACE_NOALLOC_MAX_RAYS",
+                 "TT_OPTION_LIGHT_VISIBILITY", "TT_OPTION_LIGHT_SELECTION", "TT_TEXTURE_BC5_UNORM"):
         assert name in defines
 
 

@@ -71,3 +71,30 @@ def test_restir_config_and_reset(gpu_context):
         r.present()
     assert r.restir_reservoirs()[..., 4].max() <= 3 * 8
     r.close()
+
+
+def test_restir_power_candidates(gpu_context):
+    """ReSTIR with candidates drawn by emitted power (TT_LIGHT_SELECTION_POWER), bit for bit."""
+    from tinytrace_gb300 import native
+    from tinytrace_gb300.native import check
+
+    make, center, radius, height, extent = CASES["field"]
+    r = Renderer(extent)
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_LIGHT_SELECTION,
+                                      native.TT_LIGHT_SELECTION_POWER))
+    r.set_scene(make())
+    r.set_config(Config(bounce_count=1, sample_count=1))
+    orc = oracle.OracleScene(r.scene_arrays)
+    orc.set_light_power(True)
+    R = oracle.OracleRestir(orc, *extent)
+    cpu = np.zeros((extent[1], extent[0], 4), np.float32)
+    for f in range(3):
+        r.camera = _orbit(center, radius, height, f)
+        c = make_constants(r.camera, extent, r.config(), r.context.frame_index(), r.accumulated_frame_count)
+        r.render_restir_to_target()
+        gpu = r.context.download(r.render_target, *extent)
+        R.frame(c, cpu)
+        assert_same_bits(gpu, cpu, f"power candidates frame {f} image")
+        assert_same_bits(r.restir_reservoirs(), R.reservoirs(), f"power candidates frame {f} reservoirs")
+        r.present()
+    r.close()

@@ -1260,6 +1260,7 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         }
         RenderParams p;
         p.sc = s->dev;
+        p.sc.light_power = ctx->light_selection == TT_LIGHT_SELECTION_POWER ? 1u : 0u;
         p.c = *constants;
         p.target = img->buf.as<float4>();
         p.err = ctx->err_word.as<uint32_t>();

@@ -126,11 +126,18 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_c
         float chosen = 0.0f;
         for (uint32_t k = 0; k < candidates; ++k) {
             uint32_t light = xor_shift(g) % sc.emissive_count;
+            float inv_p = inv_p_pick;
+            if (sc.light_power) {  // candidates by emitted power (TT_LIGHT_SELECTION_POWER)
+                float4 e = __ldg(sc.light_alias + light);
+                float coin = random_float(g);
+                if (!(coin < e.x)) light = __float_as_uint(e.y);
+                inv_p = 1.0f / __ldg(&sc.light_alias[light].z);
+            }
             float r1 = random_float(g);
             float r2 = random_float(g);
             LightPoint lp = light_point<TEX>(sc, light, r1, r2);
             float ph = luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
-            float w = ph * (inv_p_pick * lp.area);  // p^ / p, p = 1 / (lights * area)
+            float w = ph * (inv_p * lp.area);  // p^ / p, p = pick probability / area
             if (reservoir_update(r, light, r1, r2, w, 1.0f, g)) chosen = ph;
         }
         r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
