@@ -334,3 +334,14 @@ def test_power_light_selection(gpu_context, integrator):
     c = make_constants(w.camera, w.extent, w.config, r.context.frame_index(), r.accumulated_frame_count)
     assert_same_bits(r.render_to_texture(), orc.render(c), f"power selection after update {integrator}")
     r.close()
+
+
+def test_render_large_frame_and_many_chunks(gpu_context):
+    """A 3840x2160 frame (8.3 M pixels, 32-bit item and pixel arithmetic at scale) and a tiny
+    frame at 200 spp (four sample chunks: 64 + 64 + 64 + 8), both bit for bit."""
+    big = scenes.Workload("cornell_4k", scenes.cornell_box(), scenes.cornell_workload().camera, (3840, 2160),
+                          scenes.Config(bounce_count=2, sample_count=1))
+    _render_pair(gpu_context, big, integrator="wavefront")
+    many = scenes.Workload("cornell_200spp", scenes.cornell_box(), scenes.cornell_workload().camera, (8, 6),
+                           scenes.Config(bounce_count=3, sample_count=200))
+    _render_pair(gpu_context, many, integrator="wavefront")

@@ -600,11 +600,13 @@ __global__ void cache_init_kernel(float* grid, float* w, __half* w16, uint32_t s
 static void launch_infer(const CacheQuery* q, uint32_t n, const uint32_t* count, const float* grid,
                          const __half* w16, float* out, uint32_t* err, cudaStream_t st) {
     if (n == 0) return;
-    static bool attr = false;
-    if (!attr) {
+    static bool attr[64] = {};  // per device: the shared-memory opt-in is a per-device function attribute
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
         check_cuda(cudaFuncSetAttribute(cache_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM),
                    "infer smem");
-        attr = true;
+        if (dev >= 0 && dev < 64) attr[dev] = true;
     }
     uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
     uint32_t blocks = std::min<uint32_t>(tiles, 152u * 4u);
@@ -653,11 +655,13 @@ void cache_targets(const TrainRecord* rec, const uint32_t* rec_count, uint32_t c
 void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
                       uint32_t step, uint32_t* err, cudaStream_t st) {
     if (n == 0) return;
-    static bool attr = false;
-    if (!attr) {
+    static bool attr[64] = {};  // per device: the shared-memory opt-in is a per-device function attribute
+    int dev = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
         check_cuda(cudaFuncSetAttribute(cache_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TT_SMEM),
                    "train smem");
-        attr = true;
+        if (dev >= 0 && dev < 64) attr[dev] = true;
     }
     uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
     uint32_t blocks = std::min<uint32_t>(tiles, 152u);
