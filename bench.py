@@ -183,6 +183,20 @@ def ncu_traffic_per_launch() -> float | None:
     return float(m.group(1)) if m else None
 
 
+def ncu_trace_metrics() -> dict | None:
+    """L2 hit rate and warp execution efficiency of the extension-ray trace kernel from the
+    committed ncu summary (full capture on a 1-spp case of the same frame)."""
+    if not PROFILE.exists():
+        return None
+    text = PROFILE.read_text()
+    l2 = re.search(r"\| L2 hit rate \| ([0-9.]+) %", text)
+    tpi = re.search(r"\| threads per instruction \(of 32\) \| ([0-9.]+)", text)
+    if not (l2 and tpi):
+        return None
+    return {"l2_hit_rate": float(l2.group(1)) / 100.0, "warp_execution_efficiency": float(tpi.group(1)) / 32.0,
+            "source": "ncu --set full, extension-ray launch, 1 spp (profiles/wf_trace_kernel_icosphere_field_1080p.md)"}
+
+
 # ---------------------------------------------------------------- workload
 def make_workload(a):
     from tinytrace_gb300 import scenes
@@ -759,6 +773,7 @@ def run_ours(a, dist: Dist):
                          "bytes_per_unit": {"node": NODE_BYTES, "triangle_record": TRI_RECORD_BYTES,
                                             "instance_ray_setup": INSTANCE_RAY_BYTES, "ray_state": RAY_STATE_BYTES},
                          "node_fetch_gbs": node_achieved, "node_fetch_frac": node_achieved / peak,
+                         "ncu": ncu_trace_metrics(),
                          "traffic_source": "ncu dram bytes per launch, full workload "
                                            "(profiles/wf_trace_kernel_icosphere_field_1080p.md)"},
             "stages": stages,
