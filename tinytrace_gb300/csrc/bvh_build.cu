@@ -285,18 +285,48 @@ __global__ void init_bounds_kernel(float* b, uint32_t* cnt, uint32_t segs) {
     }
     cnt[s] = 0u;
 }
+// Per-segment centroid bounds and primitive counts.  Segments are contiguous runs of
+// primitives, so most warps lie inside one segment: those reduce their lanes with shuffles
+// and lane 0 issues one atomic per bound (min/max are exact, so the grouping does not change
+// the result).  A NaN centroid (non-finite transform) leaves the bounds unchanged, as fminf /
+// fmaxf do in the sequential restatement.
 __global__ void centroid_bounds_kernel(const float4* lo, const float4* hi, const uint32_t* seg,
                                        uint32_t n, float* b, uint32_t* cnt) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 l = lo[i], h = hi[i];
-    float c[3] = {canon((l.x + h.x) * 0.5f), canon((l.y + h.y) * 0.5f), canon((l.z + h.z) * 0.5f)};
-    uint32_t s = seg[i];
-    for (int a = 0; a < 3; ++a) {
-        atomic_min_f(&b[6 * s + a], c[a]);
-        atomic_max_f(&b[6 * s + 3 + a], c[a]);
+    if (i - (threadIdx.x & 31u) >= n) return;  // whole warp past the end
+    bool valid = i < n;
+    float cmin[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+    float cmax[3] = {__int_as_float(0xff800000), __int_as_float(0xff800000), __int_as_float(0xff800000)};
+    uint32_t s = 0xffffffffu;
+    if (valid) {
+        float4 l = lo[i], h = hi[i];
+        cmin[0] = cmax[0] = canon((l.x + h.x) * 0.5f);
+        cmin[1] = cmax[1] = canon((l.y + h.y) * 0.5f);
+        cmin[2] = cmax[2] = canon((l.z + h.z) * 0.5f);
+        s = seg[i];
     }
-    atomicAdd(&cnt[s], 1u);
+    uint32_t s0 = __shfl_sync(0xffffffffu, s, 0);  // lane 0 is valid
+    if (__all_sync(0xffffffffu, !valid || s == s0)) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                cmin[a] = fmn(cmin[a], __shfl_xor_sync(0xffffffffu, cmin[a], off));
+                cmax[a] = fmx(cmax[a], __shfl_xor_sync(0xffffffffu, cmax[a], off));
+            }
+        }
+        uint32_t k = (uint32_t)__popc(__ballot_sync(0xffffffffu, valid));
+        if ((threadIdx.x & 31u) != 0u) return;
+        s = s0;
+        atomicAdd(&cnt[s], k);
+    } else {
+        if (!valid) return;
+        atomicAdd(&cnt[s], 1u);
+    }
+    for (int a = 0; a < 3; ++a) {
+        if (cmin[a] == cmin[a]) atomic_min_f(&b[6 * s + a], cmin[a]);
+        if (cmax[a] == cmax[a]) atomic_max_f(&b[6 * s + 3 + a], cmax[a]);
+    }
 }
 
 __device__ __forceinline__ uint32_t expand_bits10(uint32_t v) {

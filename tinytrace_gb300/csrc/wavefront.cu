@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
         if (!__any_sync(0xffffffffu, active)) break;
         while (true) {
             bool fin = false;
-            if (active && (trace_step<COUNT, ACCEL>(st, sc, stack, TR_BLOCK, p.err, cnt) ||
+            if (active && (trace_step<COUNT, ACCEL, SHADOW>(st, sc, stack, TR_BLOCK, p.err, cnt) ||
                            (SHADOW && seeded && (st.best.prim != target_prim || st.best.instance != light)))) {
                 fin = true;
                 active = false;
