@@ -239,6 +239,42 @@ TT_HD uint32_t xor_shift(uint32_t& s) {
     s ^= s << 5;
     return s;
 }
+// Jump-ahead of xor_shift: each step is linear over GF(2), so k steps map a state x to M^k x
+// for one 32 x 32 bit matrix M.  A matrix is stored as its 32 columns (the images of 1 << j),
+// and applying it XORs the columns of the set bits of x: k steps for any k in 32 selects.
+struct XsJump {
+    uint32_t col[32];
+};
+__host__ __device__ constexpr uint32_t xs_step(uint32_t s) {
+    s ^= s << 13;
+    s ^= s >> 17;
+    s ^= s << 5;
+    return s;
+}
+__host__ __device__ constexpr uint32_t xs_apply(const XsJump& m, uint32_t x) {
+    uint32_t acc = 0u;
+    for (int j = 0; j < 32; ++j) acc ^= m.col[j] & (0u - ((x >> j) & 1u));
+    return acc;
+}
+__host__ __device__ constexpr XsJump xs_compose(const XsJump& a, const XsJump& b) {  // a after b
+    XsJump r{};
+    for (int j = 0; j < 32; ++j) r.col[j] = xs_apply(a, b.col[j]);
+    return r;
+}
+__host__ __device__ constexpr XsJump xs_power(uint64_t k) {  // M^k by squaring
+    XsJump base{}, r{};
+    for (int j = 0; j < 32; ++j) {
+        base.col[j] = xs_step(1u << j);
+        r.col[j] = 1u << j;
+    }
+    while (k) {
+        if (k & 1u) r = xs_compose(base, r);
+        base = xs_compose(base, base);
+        k >>= 1;
+    }
+    return r;
+}
+
 TT_HD float random_float(uint32_t& s) {
     return __uint_as_float(0x3f800000u | (xor_shift(s) >> 9)) - 1.0f;
 }

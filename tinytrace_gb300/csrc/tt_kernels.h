@@ -48,6 +48,7 @@ struct WfParams {
     float4* running;     // WH running per-pixel sums across chunks
     uint32_t P, WH;
     uint32_t chunk_sample0, chunk_spp, chunk_items;
+    XsJump chunk_jump;      // xor_shift advanced by 2 * chunk_sample0 draws
     uint32_t refill;        // a trace warp refills its idle lanes when fewer than this many hold a ray
     uint32_t trace_blocks;  // grid of the persistent trace kernel (host side)
     // learned radiance cache (cache_on = 0: off)

@@ -95,6 +95,21 @@ __device__ __forceinline__ float4 pack(f3 v, uint32_t w) { return make_float4(v.
 
 constexpr int REGEN_BLOCK = 512;
 
+// M^(2 s) for s = 0..64: the generator of sample chunk_sample0 + s of a pixel is its seed
+// advanced by chunk_jump and then by the entry of s (2 draws per earlier sample), 64 selects
+// per path instead of 2 (chunk_sample0 + s) xor_shift steps.
+struct XsJumpTable {
+    XsJump m[65];
+};
+constexpr XsJumpTable xs_jump_table() {
+    XsJumpTable t{};
+    XsJump two = xs_power(2u);
+    t.m[0] = xs_power(0u);
+    for (int s = 1; s < 65; ++s) t.m[s] = xs_compose(two, t.m[s - 1]);
+    return t;
+}
+__constant__ XsJumpTable c_xs_jump = xs_jump_table();
+
 __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_constant__ RenderParams p,
                                                                const __grid_constant__ WfParams w) {
     __shared__ uint32_t s_warp[REGEN_BLOCK / 32 + 1];
@@ -121,7 +136,9 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
         band_pixel(t, W, H, x, y);
         uint32_t sample = w.chunk_sample0 + s_local;
         uint32_t pg = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
-        for (uint32_t k = 0; k < 2u * sample; ++k) xor_shift(pg);
+        if (w.chunk_sample0) pg = xs_apply(w.chunk_jump, pg);
+        for (uint32_t r = s_local; r >= 64u; r -= 64u) pg = xs_apply(c_xs_jump.m[64], pg);  // chunks hold <= 64
+        pg = xs_apply(c_xs_jump.m[s_local & 63u], pg);
         f2 ndc = pixel_ndc(x, y, W, H, pg);
         f3 d = camera_ray_direction(c, ndc);
         if (w.ndc_mip) w.ndc_mip[s] = make_float2(ndc.x, ndc.y);
@@ -384,19 +401,24 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
             } else {
                 acc += em * thr;
             }
-            float density = 1.0f;
-            f3 wo = splat(0.0f);
-            int lobe = 0;
-            f3 bsdf = bsdf_sample(mc, lobes, wi, g, wo, density, lobe);
-            if (CACHE && w.spread_c > 0.0f) w.spread[s].z = density;
-            f3 new_dir = transform_to_basis(basis, wo);
-            thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
             uint32_t next = bounce + 1u;
-            uint32_t flags = (next == c.bounce_count ? F_TERM : F_LIVE) | train;
-            w.org[s] = pack(hit.world_position, next);
-            w.dir[s] = pack(new_dir, g);
-            w.thr[s] = pack(thr, __float_as_uint(t4.w));
-            w.acc[s] = pack(acc, flags);
+            if (next == c.bounce_count) {
+                // last vertex: the continuation ray would never be traced, so its BSDF sample
+                // (which changes only the generator and the throughput) is skipped
+                w.acc[s] = pack(acc, F_TERM | train);
+            } else {
+                float density = 1.0f;
+                f3 wo = splat(0.0f);
+                int lobe = 0;
+                f3 bsdf = bsdf_sample(mc, lobes, wi, g, wo, density, lobe);
+                if (CACHE && w.spread_c > 0.0f) w.spread[s].z = density;
+                f3 new_dir = transform_to_basis(basis, wo);
+                thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
+                w.org[s] = pack(hit.world_position, next);
+                w.dir[s] = pack(new_dir, g);
+                w.thr[s] = pack(thr, __float_as_uint(t4.w));
+                w.acc[s] = pack(acc, F_LIVE | train);
+            }
         }
     }
     __shared__ uint32_t s_warp[WF_BLOCK / 32 + 1];
@@ -519,6 +541,7 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
     check_cuda(cudaMemsetAsync(w.counters + CTRL_RECORDS, 0, 4, cs), "memset");
     for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
         w.chunk_sample0 = s0;
+        w.chunk_jump = xs_power(2ull * s0);
         w.chunk_spp = std::min(max_chunk, spp - s0);
         w.chunk_items = WH * w.chunk_spp;
         check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CHUNK_WORDS, cs), "memset");
@@ -582,6 +605,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
     check_cuda(cudaMemsetAsync(w.counters + CTRL_RECORDS, 0, 4, st), "memset");
     for (uint32_t s0 = 0; s0 < spp; s0 += max_chunk) {
         w.chunk_sample0 = s0;
+        w.chunk_jump = xs_power(2ull * s0);
         w.chunk_spp = std::min(max_chunk, spp - s0);
         w.chunk_items = WH * w.chunk_spp;
         check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CHUNK_WORDS, st), "memset");
