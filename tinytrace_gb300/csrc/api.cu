@@ -75,7 +75,7 @@ struct ImageRes {
 
 struct SceneRes {
     DeviceBuffer positions, indices, vertices, materials, meshes, instances, emissive, inst_xform, inst_bucket, light_prim;
-    DeviceBuffer tex_table, tex_data, srgb, light_alias;
+    DeviceBuffer tex_table, tex_data, srgb, light_alias, light_rec;
     BvhResult bvh;
     DevScene dev{};
     tt_scene_stats stats{};
@@ -939,6 +939,9 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.inst_bucket = s->inst_bucket.as<uint8_t>();
         ds.emissive_count = d->emissive_triangle_count;
         ds.instance_count = d->instance_count;
+        s->light_rec.alloc(16ull * LIGHT_RECORD * std::max<uint32_t>(d->emissive_triangle_count, 1u));
+        ds.light_rec = s->light_rec.as<float4>();
+        launch_light_records(ds, s->light_rec.as<float4>(), d->emissive_triangle_count, st);
         tt_scene_stats& stt = s->stats;
         stt.instance_count = d->instance_count;
         stt.emissive_count = d->emissive_triangle_count;
@@ -970,7 +973,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         stt.device_bytes = s->positions.bytes + s->indices.bytes + s->vertices.bytes + s->materials.bytes + s->meshes.bytes +
                            s->instances.bytes + s->emissive.bytes + s->inst_xform.bytes + s->inst_bucket.bytes + s->bvh.blas.bytes +
                            s->bvh.tris.bytes + s->bvh.tlas.bytes + s->bvh.flat_nodes_buf.bytes +
-                           s->bvh.flat_tris.bytes;
+                           s->bvh.flat_tris.bytes + s->light_rec.bytes;
         stt.max_stack = need_stack;
         Pool& p = ctx->pools[TT_LIFETIME_SCENE];
         p.scenes.push_back(std::move(s));
@@ -1008,6 +1011,7 @@ int32_t tt_scene_update_instances(tt_context* ctx, tt_handle scene, const tt_ins
             }
             check_cuda(cudaMemcpyAsync(s->inst_xform.ptr, xf.data(), 16ull * xf.size(), cudaMemcpyHostToDevice, st),
                        "instance rows");
+            launch_light_records(s->dev, s->light_rec.as<float4>(), s->dev.emissive_count, st);
             refit_scene_bvh(s->instances.as<tt_instance>(), st, s->bvh);  // synchronises the stream
             s->dev.tlas_bound = s->bvh.flat ? s->bvh.flat_bound : s->bvh.tlas_bound;
             s->host_instances.assign(instances, instances + count);

@@ -196,6 +196,47 @@ __global__ void math_kernel(int which, const float* x, uint64_t n, float* y) {
 }
 
 // ---------------------------------------------------------------- launchers
+// Light records (see LIGHT_RECORD): the world vertices, area and normal of each emissive
+// triangle with the operations sample_light applied per sample (instance transform of the
+// dequantised positions, cross product of the edges), the material's constant emission and its
+// emission-texture slots, so that a light sample reads one record instead of the triangle, its
+// instance and its material in turn.  `sc` must hold the emissive triangles, instances,
+// materials (texture masks in their padding) and light primitives.
+__global__ void light_records_kernel(const __grid_constant__ DevScene sc, float4* rec, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const tt_emissive_triangle* tri = sc.emissive + i;
+    uint32_t inst = tri->instance_index;
+    const tt_instance* in = sc.instances + inst;
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = in->transform[k];
+    f3 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        p[k] = mat43_point(m, f3{dequant_snorm16(tri->positions[k][0]), dequant_snorm16(tri->positions[k][1]),
+                                 dequant_snorm16(tri->positions[k][2])});
+    f3 e = cross(p[1] - p[0], p[2] - p[0]);
+    float area = fmx(0.00001f, 0.5f * length(e));
+    f3 nrm = normalize(e);
+    uint32_t mat = in->material_index;
+    f3 em = material_emissive(sc.materials + mat);
+    uint32_t mask = sc.materials[mat].padding & EMISSION_SLOTS;
+    const uint32_t* tc = reinterpret_cast<const uint32_t*>(tri->texture_coordinates);
+    float4* r = rec + (uint64_t)LIGHT_RECORD * i;
+    r[0] = make_float4(p[0].x, p[0].y, p[0].z, area);
+    r[1] = make_float4(p[1].x, p[1].y, p[1].z, __uint_as_float(inst));
+    r[2] = make_float4(p[2].x, p[2].y, p[2].z, __uint_as_float((uint32_t)tri->hash));
+    r[3] = make_float4(nrm.x, nrm.y, nrm.z, __uint_as_float(mask));
+    r[4] = make_float4(em.x, em.y, em.z, __uint_as_float(mat));
+    r[5] = make_float4(__uint_as_float(tc[0]), __uint_as_float(tc[1]), __uint_as_float(tc[2]),
+                       __uint_as_float(sc.light_prim[i]));
+}
+
+void launch_light_records(const DevScene& sc, float4* rec, uint32_t n, cudaStream_t st) {
+    if (n) light_records_kernel<<<(n + 255) / 256, 256, 0, st>>>(sc, rec, n);
+}
+
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st) {
     dim3 grid((p.c.screen_size[0] + TILE_W - 1) / TILE_W, (p.c.screen_size[1] + TILE_H - 1) / TILE_H);
     if (p.sc.textured) {

@@ -77,7 +77,14 @@ struct DevScene {
     uint32_t light_exact;        // TT_LIGHT_VISIBILITY_TRIANGLE: shadow rays test the sampled triangle itself
     uint32_t light_power;        // TT_LIGHT_SELECTION_POWER: lights picked through `light_alias`
     const float4* light_alias;   // per emissive triangle: (keep probability, alias index bits, pdf, 0)
+    const float4* light_rec;     // per emissive triangle: LIGHT_RECORD float4 (light_records_kernel)
 };
+// A light record: what light sampling derives from an emissive triangle, computed once per
+// scene and instance update.  float4 0..2: world vertices p0, p1, p2 with w = area, instance
+// bits, hash bits; 3: unit normal, emission-texture slots of the material; 4: the material's
+// constant emission, material index bits; 5: packed texture coordinates of the three corners,
+// primitive index bits.
+constexpr int LIGHT_RECORD = 6;
 
 struct Hit {
     int hit;

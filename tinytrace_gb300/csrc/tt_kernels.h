@@ -134,6 +134,7 @@ void launch_bsdf_sample(const tt_material_constants* m, const float4* samples, u
 void launch_trace(const DevScene& sc, const float4* rays, uint32_t n, uint32_t flags, uint4* hits,
                   uint32_t* err, cudaStream_t st);
 void launch_math(int which, const float* x, uint64_t n, float* y, cudaStream_t st);
+void launch_light_records(const DevScene& sc, float4* rec, uint32_t n, cudaStream_t st);
 void launch_texture_sample(const DevScene& sc, uint32_t index, const float* uvl, uint32_t n, float4* out,
                            cudaStream_t st);
 // Ray queries staged in the library's static device array (no device allocation).

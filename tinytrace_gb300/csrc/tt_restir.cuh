@@ -60,32 +60,20 @@ struct LightPoint {
 };
 template <bool TEX>
 __device__ __forceinline__ LightPoint light_point(const DevScene& sc, uint32_t light, float r1, float r2) {
-    const tt_emissive_triangle* tri = sc.emissive + light;
+    const float4* rec = sc.light_rec + (uint64_t)LIGHT_RECORD * light;
+    float4 q0 = __ldg(rec + 0), q1 = __ldg(rec + 1), q2 = __ldg(rec + 2), q3 = __ldg(rec + 3);
     LightPoint lp;
-    lp.instance = __ldg(&tri->instance_index);
-    const tt_instance* in = sc.instances + lp.instance;
-    float m[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) m[k] = __ldg(&in->transform[k]);
-    f3 p[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        p[k] = mat43_point(m, f3{dequant_snorm16(__ldg(&tri->positions[k][0])),
-                                 dequant_snorm16(__ldg(&tri->positions[k][1])),
-                                 dequant_snorm16(__ldg(&tri->positions[k][2]))});
-    f3 e = cross(p[1] - p[0], p[2] - p[0]);
-    lp.area = fmx(0.00001f, 0.5f * length(e));
-    lp.normal = normalize(e);
+    lp.instance = __float_as_uint(q1.w);
+    lp.area = q0.w;
+    lp.normal = f3{q3.x, q3.y, q3.z};
     f3 bary = sample_triangle(f2{r1, r2});
-    lp.pos = interp3(bary, p[0], p[1], p[2]);
+    lp.pos = interp3(bary, f3{q0.x, q0.y, q0.z}, f3{q1.x, q1.y, q1.z}, f3{q2.x, q2.y, q2.z});
     f2 uv = f2{0.0f, 0.0f};
     if (TEX) {
-        uint32_t tc[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) tc[k] = __ldg(reinterpret_cast<const uint32_t*>(&tri->texture_coordinates[k]));
-        uv = interp_uv(bary, tc[0], tc[1], tc[2]);
+        float4 q5 = __ldg(rec + 5);
+        uv = interp_uv(bary, __float_as_uint(q5.x), __float_as_uint(q5.y), __float_as_uint(q5.z));
     }
-    lp.emission = hit_emissive<TEX>(sc, sc.materials + __ldg(&in->material_index), uv, 4.0f);
+    lp.emission = light_emission<TEX>(sc, light, uv, 4.0f);
     return lp;
 }
 
@@ -136,7 +124,8 @@ __device__ __forceinline__ bool restir_visible(const DevScene& sc, f3 pos, const
     f3 dir = d / sqrtf(dot(d, d));
     Counters cnt{0u, 0u, 0u, 0u};
     Hit h = trace_closest<COUNT>(sc, pos, dir, SHADOW_TMIN, SHADOW_TMAX, false, stack, stride, err, cnt);
-    return h.hit && h.instance == lp.instance && h.prim == __ldg(sc.light_prim + light);
+    return h.hit && h.instance == lp.instance &&
+           h.prim == __float_as_uint(__ldg(&sc.light_rec[(uint64_t)LIGHT_RECORD * light + 5].w));
 }
 
 }  // namespace tt

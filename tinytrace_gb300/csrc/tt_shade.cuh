@@ -141,8 +141,11 @@ struct LightSample {
     float density;  // solid-angle density times the light selection probability
     uint32_t instance, hash;
     uint32_t prim;  // primitive of the light triangle in its instance's mesh (exact visibility)
+    uint32_t light; // emissive triangle index (its light record)
     f2 uv;          // texture coordinates of the light point (read by textured shading only)
 };
+// The light point reads the triangle's light record (world vertices, area and normal computed
+// once per scene by the same operations this function used to apply per sample).
 __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 position, const Basis& basis,
                                                     uint32_t& g) {
     uint32_t light = xor_shift(g) % sc.emissive_count;
@@ -153,29 +156,19 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 posit
         if (!(coin < e.x)) light = __float_as_uint(e.y);
         light_probability = __ldg(&sc.light_alias[light].z);
     }
-    const tt_emissive_triangle* tri = sc.emissive + light;
+    const float4* rec = sc.light_rec + (uint64_t)LIGHT_RECORD * light;
     f2 rnd = random_vec2(g);
     f3 bary = sample_triangle(rnd);
+    float4 r0 = __ldg(rec + 0), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2), r3 = __ldg(rec + 3), r5 = __ldg(rec + 5);
     LightSample ls;
-    ls.instance = __ldg(&tri->instance_index);
-    float m[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) m[k] = __ldg(&sc.instances[ls.instance].transform[k]);
-    f3 p[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        p[k] = mat43_point(m, f3{dequant_snorm16(__ldg(&tri->positions[k][0])),
-                                 dequant_snorm16(__ldg(&tri->positions[k][1])),
-                                 dequant_snorm16(__ldg(&tri->positions[k][2]))});
-    float area = fmx(0.00001f, 0.5f * length(cross(p[1] - p[0], p[2] - p[0])));
-    f3 lnormal = normalize(cross(p[1] - p[0], p[2] - p[0]));
-    f3 lpos = interp3(bary, p[0], p[1], p[2]);
-    uint32_t tc[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) tc[k] = __ldg(reinterpret_cast<const uint32_t*>(&tri->texture_coordinates[k]));
-    ls.uv = interp_uv(bary, tc[0], tc[1], tc[2]);
-    ls.hash = (uint32_t)__ldg(&tri->hash);
-    ls.prim = sc.light_exact ? __ldg(sc.light_prim + light) : 0xffffffffu;
+    ls.light = light;
+    ls.instance = __float_as_uint(r1.w);
+    float area = r0.w;
+    f3 lnormal = f3{r3.x, r3.y, r3.z};
+    f3 lpos = interp3(bary, f3{r0.x, r0.y, r0.z}, f3{r1.x, r1.y, r1.z}, f3{r2.x, r2.y, r2.z});
+    ls.uv = interp_uv(bary, __float_as_uint(r5.x), __float_as_uint(r5.y), __float_as_uint(r5.z));
+    ls.hash = __float_as_uint(r2.w);
+    ls.prim = sc.light_exact ? __float_as_uint(r5.w) : 0xffffffffu;
     f3 to_light = lpos - position;
     ls.wo = transform_from_basis(basis, to_light);
     float d2 = dot(to_light, to_light);
@@ -184,12 +177,25 @@ __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 posit
     return ls;
 }
 
+// Emission of a light point: the record's constant emission, or the material's emission
+// textures at `uv` when it has some (textured scenes).
+template <bool TEX>
+__device__ __forceinline__ f3 light_emission(const DevScene& sc, uint32_t light, f2 uv, float lod) {
+    const float4* rec = sc.light_rec + (uint64_t)LIGHT_RECORD * light;
+    float4 r4 = __ldg(rec + 4);
+    if (TEX) {
+        uint32_t mask = __float_as_uint(__ldg(&rec[3].w));
+        if (mask) return material_emissive_textured(sc, sc.materials + __float_as_uint(r4.w), mask, uv, lod);
+    }
+    return f3{r4.x, r4.y, r4.z};
+}
+
 // The contribution of integrate.glsl:186-192 when the light is visible (the light's emission
 // textures are sampled at mip level 4, integrate.glsl:188-189).
 template <bool TEX = false>
 __device__ __forceinline__ f3 light_contribution(const DevScene& sc, const LightSample& ls, const MatC& mat,
                                                  const Lobes& lobes, f3 wi) {
-    f3 emissive = hit_emissive<TEX>(sc, sc.materials + __ldg(&sc.instances[ls.instance].material_index), ls.uv, 4.0f);
+    f3 emissive = light_emission<TEX>(sc, ls.light, ls.uv, 4.0f);
     float bd = 0.0f;
     f3 bsdf = bsdf_evaluate(mat, lobes, wi, ls.wo, bd);
     return bsdf * emissive * fabsf(cos_theta(ls.wo)) / fmx(ls.density, PDF_EPSILON);
