@@ -96,7 +96,7 @@ struct WavefrontBuffers {
 // ReSTIR DI state kept between frames: two G-buffers and two final reservoir arrays
 // (current and previous frame), the initial and temporal reservoirs, the previous camera.
 struct RestirState {
-    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex;
+    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex, glob;
     uint64_t pixels = 0;
     uint32_t cur = 0;
     RestirHistory history{};
@@ -1259,6 +1259,7 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
             for (auto& b : R.final_res) b.alloc(32ull * WH);
             R.initial.alloc(32ull * WH);
             R.temporal.alloc(32ull * WH);
+            R.glob.alloc(16ull * LOBE_RECORD * WH);
             R.pixels = WH;
             R.history.valid = 0u;
         }
@@ -1276,6 +1277,7 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
             rp.gtex = R.gtex.as<float4>();
         }
         rp.gbuf = R.gbuf[R.cur].as<Surface>();
+        rp.glob = R.glob.as<float4>();
         rp.prev_gbuf = R.gbuf[R.cur ^ 1u].as<Surface>();
         rp.initial = R.initial.as<Reservoir>();
         rp.temporal = R.temporal.as<Reservoir>();

@@ -1,6 +1,7 @@
 // ReSTIR DI kernels (the passes described in tt_restir.cuh), one thread per pixel in 16 x 8
 // tiles; each pass reads and writes whole-frame arrays in HBM:
-//   G-buffer 64 B / pixel (current and previous frame), reservoirs 32 B / pixel
+//   G-buffer 64 B / pixel (current and previous frame), prepared lobes 96 B / pixel (current
+//   frame), reservoirs 32 B / pixel
 //   (initial, temporal, final; the final array of frame n is the history of frame n + 1).
 #include <cuda_runtime.h>
 
@@ -33,8 +34,8 @@ struct ShadingState {
     float mip;
 };
 template <bool TEX>
-__device__ __forceinline__ bool load_surface(const DevScene& sc, const Surface& s, const float4* gtex, uint64_t i,
-                                             ShadingState& st) {
+__device__ __forceinline__ bool load_surface(const DevScene& sc, const Surface& s, const float4* gtex,
+                                             const float4* glob, uint64_t i, ShadingState& st) {
     uint32_t mat = __float_as_uint(s.normal_mat.w);
     if (mat == NO_SURFACE) return false;
     st.pos = f3{s.pos_dist.x, s.pos_dist.y, s.pos_dist.z};
@@ -53,8 +54,7 @@ __device__ __forceinline__ bool load_surface(const DevScene& sc, const Surface& 
         st.mip = t.z;
     }
     st.mc = &hit_material<TEX>(sc, st.material, st.uv, st.mip, st.local);
-    uint32_t g = st.seed;
-    st.lobes = bsdf_prepare(*st.mc, st.wi, g);
+    st.lobes = load_lobes(glob + LOBE_RECORD * i);  // bsdf_prepare(*st.mc, st.wi, seed), stored by the G-buffer pass
     return true;
 }
 
@@ -68,7 +68,7 @@ __device__ __forceinline__ float target_of(const DevScene& sc, const ShadingStat
 
 template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
-                                                                  Surface* gbuf, float4* gtex) {
+                                                                  Surface* gbuf, float4* gtex, float4* glob) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     uint32_t x, y;
     const tt_constants& c = p.c;
@@ -104,13 +104,15 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
         s.normal_mat = make_float4(basis.normal.x, basis.normal.y, basis.normal.z, __uint_as_float(hit.material_index));
         s.tangent_inst = make_float4(basis.tangent.x, basis.tangent.y, basis.tangent.z, __uint_as_float(h.instance));
         s.wi_seed = make_float4(wi.x, wi.y, wi.z, __uint_as_float(g));
+        uint32_t gp = g;
+        store_lobes(glob + LOBE_RECORD * ((uint64_t)y * W + x), bsdf_prepare(mc, wi, gp));
     }
     gbuf[(uint64_t)y * W + x] = s;
 }
 
 template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_constant__ RenderParams p,
-                                                                  const Surface* gbuf, const float4* gtex,
+                                                                  const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   Reservoir* out, uint32_t candidates) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     uint32_t x, y;
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_c
     uint64_t i = (uint64_t)y * c.screen_size[0] + x;
     ShadingState st;
     Reservoir r = empty_reservoir();
-    if (load_surface<TEX>(sc, gbuf[i], gtex, i, st) && sc.emissive_count > 0) {
+    if (load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st) && sc.emissive_count > 0) {
         uint32_t g = jenkins_hash(st.seed + PASS_INITIAL);
         float inv_p_pick = (float)sc.emissive_count;
         float chosen = 0.0f;
@@ -198,7 +200,7 @@ __device__ __forceinline__ bool similar(const Surface& q, f3 normal, float dist)
 template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_constant__ RenderParams p,
                                                                    const __grid_constant__ RestirHistory hist,
-                                                                   const Surface* gbuf, const float4* gtex,
+                                                                   const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                    const Surface* prev_gbuf,
                                                                    const Reservoir* initial, const Reservoir* prev,
                                                                    Reservoir* out, float m_cap) {
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_
     Reservoir cur = initial[i];
     ShadingState st;
     uint32_t px, py;
-    if (!hist.valid || !load_surface<TEX>(sc, gbuf[i], gtex, i, st) || !reproject(hist, st.pos, W, H, px, py)) {
+    if (!hist.valid || !load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st) || !reproject(hist, st.pos, W, H, px, py)) {
         out[i] = cur;
         return;
     }
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_
 
 template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_constant__ RenderParams p,
-                                                                  const Surface* gbuf, const float4* gtex,
+                                                                  const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   const Reservoir* in,
                                                                   Reservoir* out, uint32_t neighbours, float radius) {
     uint32_t x, y;
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
     uint64_t i = (uint64_t)y * W + x;
     ShadingState st;
     Reservoir cur = in[i];
-    if (!load_surface<TEX>(sc, gbuf[i], gtex, i, st)) {
+    if (!load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st)) {
         out[i] = cur;
         return;
     }
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
 
 template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_constant__ RenderParams p,
-                                                                const Surface* gbuf, const float4* gtex,
+                                                                const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                 const Reservoir* res) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     uint32_t x, y;
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
     uint64_t i = (uint64_t)y * W + x;
     ShadingState st;
     f3 radiance;
-    if (!load_surface<TEX>(sc, gbuf[i], gtex, i, st)) {
+    if (!load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st)) {
         radiance = splat(1.0f);  // the white sky of integrate.glsl:272-276
     } else {
         radiance = hit_emissive<TEX>(sc, st.material, st.uv, st.mip);
@@ -305,13 +307,13 @@ template <bool TEX>
 static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {
     const tt_constants& c = p.c;
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
-    restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex);
-    restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.initial, rp.candidates);
-    restir_temporal_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.prev_gbuf, rp.initial,
-                                                           rp.prev, rp.temporal, rp.m_cap);
-    restir_spatial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.temporal, rp.final_out,
+    restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob);
+    restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
+    restir_temporal_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.glob, rp.prev_gbuf,
+                                                           rp.initial, rp.prev, rp.temporal, rp.m_cap);
+    restir_spatial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.temporal, rp.final_out,
                                                           rp.neighbours, rp.radius);
-    restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.final_out);
+    restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
 }
 
 void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {

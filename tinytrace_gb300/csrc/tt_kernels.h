@@ -116,9 +116,11 @@ struct RestirHistory {
 };
 struct Surface;
 struct Reservoir;
+constexpr int LOBE_RECORD = 6;  // float4 per pixel of RestirParams::glob
 struct RestirParams {
     Surface *gbuf, *prev_gbuf;
     float4* gtex;  // textured scenes: per pixel (u, v, mip level, 0) of the primary hit; else null
+    float4* glob;  // per pixel: the primary hit's prepared lobes (LOBE_RECORD float4)
     Reservoir *initial, *temporal, *final_out, *prev;
     RestirHistory history;
     uint32_t candidates, neighbours;

@@ -26,6 +26,7 @@
 // and the tests compare the images and reservoirs bit for bit.
 #pragma once
 
+#include "tt_kernels.h"
 #include "tt_shade.cuh"
 
 namespace tt {
@@ -51,6 +52,30 @@ struct Surface {
 };
 
 TT_HD float luminance(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+// The primary hit's prepared lobes (bsdf_prepare from the G-buffer's generator state), stored
+// by the G-buffer pass so that the later passes read them instead of preparing again.
+static_assert(sizeof(Lobes) == 16 * LOBE_RECORD, "Lobes is 24 floats");
+TT_HD void store_lobes(float4* dst, const Lobes& l) {
+    float v[4 * LOBE_RECORD];
+    memcpy(v, &l, sizeof(v));
+#pragma unroll
+    for (int k = 0; k < LOBE_RECORD; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+}
+TT_HD Lobes load_lobes(const float4* src) {
+    float v[4 * LOBE_RECORD];
+#pragma unroll
+    for (int k = 0; k < LOBE_RECORD; ++k) {
+        float4 q = src[k];
+        v[4 * k] = q.x;
+        v[4 * k + 1] = q.y;
+        v[4 * k + 2] = q.z;
+        v[4 * k + 3] = q.w;
+    }
+    Lobes l;
+    memcpy(&l, v, sizeof(v));
+    return l;
+}
 
 // World position, normal (one-sided, cross(p1-p0, p2-p0)), area and emission of a light point.
 struct LightPoint {
