@@ -141,16 +141,27 @@ TT_HD Reservoir empty_reservoir() {
     return r;
 }
 
-// Visibility of a light point: the closest hit along the shadow ray is its own triangle.
+// Visibility of a light point: the closest hit along the shadow ray is its own triangle.  The
+// traversal starts from the ray's hit on that triangle (seed_triangle_hit, computed as the
+// traversal computes it), so it only searches for a closer hit and stops at the first one:
+// the same answer as a full closest-hit query followed by the comparison.
 template <bool COUNT>
 __device__ __forceinline__ bool restir_visible(const DevScene& sc, f3 pos, const LightPoint& lp, uint32_t light,
                                                uint32_t* stack, int stride, uint32_t* err) {
     f3 d = lp.pos - pos;
     f3 dir = d / sqrtf(dot(d, d));
+    uint32_t prim = __float_as_uint(__ldg(&sc.light_rec[(uint64_t)LIGHT_RECORD * light + 5].w));
+    const tt_instance* in = sc.instances + lp.instance;
+    TraceState st;
+    trace_init(st, sc, pos, dir, SHADOW_TMIN, SHADOW_TMAX, false);
+    if (!st.have) return false;  // NaN direction or empty scene: the closest-hit query misses
+    if (!seed_triangle_hit(sc, lp.instance, prim, __ldg(&in->index_offset), __ldg(&in->vertex_offset), pos, dir,
+                           SHADOW_TMIN, SHADOW_TMAX, st.best, st.tbest))
+        return false;
     Counters cnt{0u, 0u, 0u, 0u};
-    Hit h = trace_closest<COUNT>(sc, pos, dir, SHADOW_TMIN, SHADOW_TMAX, false, stack, stride, err, cnt);
-    return h.hit && h.instance == lp.instance &&
-           h.prim == __float_as_uint(__ldg(&sc.light_rec[(uint64_t)LIGHT_RECORD * light + 5].w));
+    while (!trace_step<COUNT, ACCEL_ANY, true>(st, sc, stack, stride, err, cnt))
+        if (st.best.prim != prim || st.best.instance != lp.instance) return false;  // a closer hit occludes
+    return st.best.hit && st.best.instance == lp.instance && st.best.prim == prim;
 }
 
 }  // namespace tt

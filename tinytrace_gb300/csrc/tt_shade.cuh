@@ -211,6 +211,34 @@ __device__ __forceinline__ f3 light_contribution(const DevScene& sc, const Light
 // The hit is computed exactly as the traversal computes it (object ray of the instance, the
 // same watertight test on the same dequantised vertices), so a traversal seeded with it finds
 // the same closest hit as an unseeded one.
+// The hit of ray (o, d) on primitive `prim` of instance `inst` (no culling, t in [tmin, tmax])
+// exactly as the traversal computes it: the instance's object ray, the watertight test on the
+// dequantised snorm16 vertices.  On a hit, `best` and `tbest` hold it and the result is true.
+__device__ __forceinline__ bool seed_triangle_hit(const DevScene& sc, uint32_t inst, uint32_t prim,
+                                                  uint32_t index_offset, uint32_t vertex_offset, f3 o, f3 d,
+                                                  float tmin, float tmax, Hit& best, float& tbest) {
+    f3 oo, od;
+    uint32_t mesh;
+    instance_ray(sc, inst, o, d, oo, od, mesh);
+    if (!finite3(d) || !finite3(od)) return false;
+    f3 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int16_t* s = sc.positions + 3ull * (__ldg(sc.indices + index_offset + 3u * prim + k) + vertex_offset);
+        p[k] = f3{dequant_snorm16(__ldg(s + 0)), dequant_snorm16(__ldg(s + 1)), dequant_snorm16(__ldg(s + 2))};
+    }
+    float t, u, v;
+    if (!intersect_triangle(ray_precompute(oo, od), p[0], p[1], p[2], false, tmin, tmax, t, u, v)) return false;
+    best.hit = 1;
+    best.t = t;
+    best.u = u;
+    best.v = v;
+    best.instance = inst;
+    best.prim = prim;
+    tbest = t;
+    return true;
+}
+
 __device__ __forceinline__ int shadow_target(const DevScene& sc, uint32_t light_instance, uint32_t hash,
                                              uint32_t exact_prim, f3 o, f3 d, float tmin, float tmax, Hit& best,
                                              float& tbest) {
@@ -228,26 +256,7 @@ __device__ __forceinline__ int shadow_target(const DevScene& sc, uint32_t light_
         prim = hash >= r ? hash - r : hash + 0xffffu - r;
         if (prim >= tri_count) return 0;
     }
-    f3 oo, od;
-    uint32_t mesh;
-    instance_ray(sc, light_instance, o, d, oo, od, mesh);
-    if (!finite3(d) || !finite3(od)) return 0;
-    f3 p[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int16_t* s = sc.positions + 3ull * (__ldg(sc.indices + index_offset + 3u * prim + k) + vertex_offset);
-        p[k] = f3{dequant_snorm16(__ldg(s + 0)), dequant_snorm16(__ldg(s + 1)), dequant_snorm16(__ldg(s + 2))};
-    }
-    float t, u, v;
-    if (!intersect_triangle(ray_precompute(oo, od), p[0], p[1], p[2], false, tmin, tmax, t, u, v)) return 0;
-    best.hit = 1;
-    best.t = t;
-    best.u = u;
-    best.v = v;
-    best.instance = light_instance;
-    best.prim = prim;
-    tbest = t;
-    return 1;
+    return seed_triangle_hit(sc, light_instance, prim, index_offset, vertex_offset, o, d, tmin, tmax, best, tbest) ? 1 : 0;
 }
 
 // integrate.glsl:175-185: the closest shadow hit must be the sampled light triangle.
