@@ -330,7 +330,7 @@ def run_cache(a, device: int) -> dict:
     building and the Adam steps after the frame) and compared with the reference by the MSE of
     x / (1 + x) tonemapped images (robust to fireflies) and by the plain MSE; equal-error
     speed-up = (t_plain e_plain) / (t_cached e_cached).  The cache (path-spread rule c = 0.01
-    from the second vertex, 262,144 training paths, learning rate 1e-2) trains online for 128
+    from the second vertex, 65,536 training paths, learning rate 1e-2) trains online for 128
     frames of 4 spp before it is measured."""
     import ctypes
 
@@ -339,7 +339,7 @@ def run_cache(a, device: int) -> dict:
     from tinytrace_gb300.renderer import Config, Renderer
 
     W, H, depth = a.width, a.height, a.depth
-    out = {"reference_spp": 4096, "config": {"learning_rate": 1e-2, "train_paths_per_frame": 262144,
+    out = {"reference_spp": 4096, "config": {"learning_rate": 1e-2, "train_paths_per_frame": 65536,
                                              "terminate_depth": 1, "spread_threshold": 0.01},
            "warmup_frames": 128, "frames_averaged": 4, "scenes": {}}
     cases = [("textured_cornell", scenes.textured_cornell(),
@@ -379,7 +379,7 @@ def run_cache(a, device: int) -> dict:
             return ms, tm, mse
 
         plain = {spp: errors(spp) for spp in (4, 16)}
-        cfg = native.CacheConfig(1e-2, 262144, 1, 1, 0.01)
+        cfg = native.CacheConfig(1e-2, 65536, 1, 1, 0.01)
         check(lib.tt_cache_configure(ctx, ctypes.byref(cfg)))
         check(lib.tt_set_option(ctx, native.TT_OPTION_RADIANCE_CACHE, 1))
         for _ in range(128):

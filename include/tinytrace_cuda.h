@@ -379,7 +379,7 @@ int32_t tt_restir_download(tt_context* ctx, void* reservoirs, uint64_t bytes);
  * units, 3 outputs; queries are 12 floats: pos xyz, dir xyz, normal xyz, roughness, 0, 0. */
 #define TT_CACHE_WEIGHTS 16896u          /* 4 x 64 x 64 hidden weights + 8 x 64 output rows (3 used) */
 #define TT_CACHE_GRID_FLOATS 16777216u   /* 16 levels x 2^19 entries x 2 features */
-/* Defaults of a context that was never configured: {1e-2, 262144, 1, 1, 0.01}. */
+/* Defaults of a context that was never configured: {1e-2, 65536, 1, 1, 0.01}. */
 typedef struct tt_cache_config {
     float learning_rate;            /* Adam step size */
     uint32_t train_paths_per_frame; /* paths traced to full depth to produce training radiance */

@@ -112,7 +112,7 @@ struct CacheState {
     bool enabled = false;
     float last_loss = 0.0f;
     uint32_t last_pairs = 0;
-    tt_cache_config config{1e-2f, 262144u, 1u, 1u, 0.01f};
+    tt_cache_config config{1e-2f, 65536u, 1u, 1u, 0.01f};
     uint32_t step = 0;
     bool ready = false;
     CacheDevice dev() const {
