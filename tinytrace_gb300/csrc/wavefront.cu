@@ -126,7 +126,12 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
         w.acc[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     bool live = valid && (flags & F_LIVE);
-    bool need = valid && !live && *(volatile uint32_t*)&w.counters[0] < w.chunk_items;
+    // whether work items remain: one read of the shared counter per block (a stale value only
+    // makes some free slots draw item numbers past the chunk, which they skip)
+    __shared__ uint32_t s_next;
+    if (threadIdx.x == 0) s_next = *(volatile uint32_t*)&w.counters[0];
+    __syncthreads();
+    bool need = valid && !live && s_next < w.chunk_items;
     uint32_t item = block_append<REGEN_BLOCK>(&w.counters[0], need, s_warp);
     if (need && item < w.chunk_items) {
         const tt_constants& c = p.c;
