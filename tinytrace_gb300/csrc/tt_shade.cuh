@@ -144,8 +144,9 @@ struct LightSample {
     uint32_t light; // emissive triangle index (its light record)
     f2 uv;          // texture coordinates of the light point (read by textured shading only)
 };
-// The light point reads the triangle's light record (world vertices, area and normal computed
-// once per scene by the same operations this function used to apply per sample).
+// The triangle's world vertices, area and normal come from its light record, which
+// light_records_kernel computes once per scene with the operations of scene.glsl:114-136
+// (instance transform of the dequantised positions, cross product of the edges).
 __device__ __forceinline__ LightSample sample_light(const DevScene& sc, f3 position, const Basis& basis,
                                                     uint32_t& g) {
     uint32_t light = xor_shift(g) % sc.emissive_count;
