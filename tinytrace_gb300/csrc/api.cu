@@ -494,7 +494,7 @@ int32_t guarded(F&& f) {
 
 using namespace tt;
 
-constexpr uint32_t WAVEFRONT_DEFAULT_SLOTS = 1u << 21;
+constexpr uint32_t WAVEFRONT_DEFAULT_SLOTS = 1u << 23;
 constexpr uint32_t WAVEFRONT_MAX_CHUNK_SPP = 64;
 
 // Sizes (growing only) the wavefront pool for this frame and returns its device pointers.
@@ -1207,7 +1207,7 @@ int32_t tt_autotune(tt_context* ctx, tt_handle scene, const tt_constants* consta
         uint64_t items = (uint64_t)constants->screen_size[0] * constants->screen_size[1] *
                          std::min<uint32_t>(constants->sample_count, WAVEFRONT_MAX_CHUNK_SPP);
         std::vector<uint32_t> slots;
-        for (uint32_t s = 1u << 18; s <= (1u << 22); s <<= 1)
+        for (uint32_t s = 1u << 18; s <= (1u << 25); s <<= 1)
             if (s <= std::max<uint64_t>(items, 1u << 18)) slots.push_back(s);
         if (ctx->wavefront_slots == 0) ctx->wavefront_slots = WAVEFRONT_DEFAULT_SLOTS;
         tune(ctx->wavefront_slots, slots);
