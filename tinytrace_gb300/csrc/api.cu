@@ -494,7 +494,7 @@ int32_t guarded(F&& f) {
 
 using namespace tt;
 
-constexpr uint32_t WAVEFRONT_DEFAULT_SLOTS = 1u << 23;
+constexpr uint32_t WAVEFRONT_DEFAULT_SLOTS = 1u << 21;
 constexpr uint32_t WAVEFRONT_MAX_CHUNK_SPP = 64;
 
 // Sizes (growing only) the wavefront pool for this frame and returns its device pointers.
