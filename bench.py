@@ -650,7 +650,7 @@ def run_ours(a, dist: Dist):
     if not a.no_autotune and a.integrator == "wavefront" and not a.slots:
         t = r.autotune(sample_count=16)  # short 16-spp renders of the same frame, before the warm-up
         tuning = {"slots": t.slots, "refill_lanes": t.refill_lanes, "trace_blocks_per_sm": t.trace_blocks_per_sm,
-                  "renders": t.renders, "default_ms_8spp": t.default_ms, "tuned_ms_8spp": t.best_ms}
+                  "renders": t.renders, "tune_spp": 16, "default_ms": t.default_ms, "tuned_ms": t.best_ms}
     for _ in range(a.warmup):
         step()
     check(lib.tt_synchronize(ctx))
