@@ -926,6 +926,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             fail(TT_ERR_OVERFLOW, "scene BVH is too deep for the traversal stack (" +
                                       std::to_string(need_stack) + " entries needed)");
         DevScene& ds = s->dev;
+        ds.stack_need = (uint32_t)need_stack;
         ds.positions = s->positions.as<int16_t>();
         ds.indices = s->indices.as<uint32_t>();
         ds.vertices = s->vertices.as<tt_vertex>();

@@ -36,6 +36,9 @@ constexpr uint32_t STACK_MARKER = 0xffffffffu;
 #define TT_TRAVERSAL_STACK 64
 #endif
 constexpr int TRAVERSAL_STACK = TT_TRAVERSAL_STACK;  // entries per thread, in shared memory
+// The wavefront trace kernel also comes with this shorter stack, used for scenes that need no
+// more: less shared memory per block leaves more of the SM's L1 to cache nodes.
+constexpr int SHORT_TRAVERSAL_STACK = 48;
 constexpr uint32_t TRAVERSAL_ITERATION_LIMIT = 1u << 24;
 constexpr uint32_t ERR_STACK_OVERFLOW = 1u;
 constexpr uint32_t ERR_ITERATION_LIMIT = 2u;
@@ -70,6 +73,7 @@ struct DevScene {
     uint32_t has_tlas;
     float tlas_bound;  // max |coordinate| of the world boxes in `tlas`
     uint32_t flat;     // 1: `tlas`/`tris` hold the flat BVH
+    uint32_t stack_need;  // traversal stack entries the structure can need (3 per level + 1)
     const DevTexture* textures;  // texture table (null when the scene has no textures)
     const uint8_t* tex_data;     // all texture levels
     const float* srgb;           // 256-entry sRGB-to-linear table
@@ -271,10 +275,10 @@ TT_HD void trace_init(TraceState& st, const DevScene& sc, f3 o, f3 d, float tmin
     st.have = finite3(d) && sc.has_tlas != 0u;  // a NaN/inf direction or an empty scene misses
 }
 
-template <bool COUNT>
+template <bool COUNT, int STACK = TRAVERSAL_STACK>
 __device__ __forceinline__ bool trace_push(TraceState& st, uint32_t* stack, int stride, uint32_t* err,
                                            uint32_t v) {
-    if (st.sp >= TRAVERSAL_STACK) {
+    if (st.sp >= STACK) {
         atomicOr(err, ERR_STACK_OVERFLOW);
         return false;
     }
@@ -297,6 +301,7 @@ __device__ __forceinline__ void instance_ray(const DevScene& sc, uint32_t inst, 
 // Sorts the hit children of a node by entry distance and splits them into the nearest
 // internal child (the next node), the nearest leaf (the pending triangle range, when that is
 // free and `leaves` is set) and the rest, pushed farthest first.  Returns false on overflow.
+template <int STACK = TRAVERSAL_STACK>
 __device__ __forceinline__ bool visit_children(TraceState& st, int mask, const float* tn, const uint32_t* ch,
                                                bool leaves, uint32_t* stack, int stride, uint32_t* err) {
     float key[4];
@@ -332,7 +337,7 @@ __device__ __forceinline__ bool visit_children(TraceState& st, int mask, const f
         push[c] = valid && !take_leaf && !take_next;
         npush += push[c] ? 1 : 0;
     }
-    if (st.sp + npush > TRAVERSAL_STACK) {
+    if (st.sp + npush > STACK) {
         atomicOr(err, ERR_STACK_OVERFLOW);
         return false;
     }
@@ -359,7 +364,7 @@ __device__ __forceinline__ bool visit_children(TraceState& st, int mask, const f
 // rays (whose seeded tbest prunes most subtrees: shadow stage 18.8 -> 16.6 ms per frame of
 // the 1080p benchmark) and costs extension rays 4 % (81.2 -> 84.6 ms), so the trace kernel
 // enables it for shadow rays only.  Either order finds the same hit.
-template <bool COUNT, bool EARLY = false>
+template <bool COUNT, bool EARLY = false, int STACK = TRAVERSAL_STACK>
 __device__ __forceinline__ bool trace_step_flat(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
                                                 uint32_t* err, Counters& cnt) {
     if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {
@@ -436,18 +441,18 @@ __device__ __forceinline__ bool trace_step_flat(TraceState& st, const DevScene& 
     float tn[4];
     uint32_t ch[4];
     int mask = node_hits(sc.tlas, st.cur, st.nr, st.tmin, st.tbest, tn, ch);
-    return !visit_children(st, mask, tn, ch, true, stack, stride, err);
+    return !visit_children<STACK>(st, mask, tn, ch, true, stack, stride, err);
 }
 
 // ACCEL: ACCEL_ANY dispatches on the scene at run time; ACCEL_FLAT_ONLY and ACCEL_TWO_LEVEL_ONLY
 // compile one structure's step (the caller has checked sc.flat).
 constexpr int ACCEL_ANY = 0, ACCEL_FLAT_ONLY = 1, ACCEL_TWO_LEVEL_ONLY = 2;
 
-template <bool COUNT, int ACCEL = ACCEL_ANY, bool EARLY = false>
+template <bool COUNT, int ACCEL = ACCEL_ANY, bool EARLY = false, int STACK = TRAVERSAL_STACK>
 __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
                                            uint32_t* err, Counters& cnt) {
     if (ACCEL == ACCEL_FLAT_ONLY || (ACCEL == ACCEL_ANY && sc.flat))
-        return trace_step_flat<COUNT, EARLY>(st, sc, stack, stride, err, cnt);
+        return trace_step_flat<COUNT, EARLY, STACK>(st, sc, stack, stride, err, cnt);
     if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {
         atomicOr(err, ERR_ITERATION_LIMIT);
         return true;
@@ -500,7 +505,7 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
             st.have = false;
             return false;
         }
-        if (!trace_push<COUNT>(st, stack, stride, err, STACK_MARKER)) return true;
+        if (!trace_push<COUNT, STACK>(st, stack, stride, err, STACK_MARKER)) return true;
         st.rp = ray_precompute(oo, od);
         st.nr = node_ray(oo, od, 1.0f);
         st.in_blas = true;
@@ -514,7 +519,7 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
     float tn[4];
     uint32_t ch[4];
     int mask = node_hits(st.in_blas ? sc.blas : sc.tlas, st.cur, st.nr, st.tmin, st.tbest, tn, ch);
-    return !visit_children(st, mask, tn, ch, st.in_blas, stack, stride, err);
+    return !visit_children<STACK>(st, mask, tn, ch, st.in_blas, stack, stride, err);
 }
 
 // Closest hit, run to completion.
