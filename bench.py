@@ -10,7 +10,8 @@ kernel's (wf_trace_kernel: extension and shadow rays) algorithmic bytes per laun
 nodes, triangle records, object-ray set-ups, ray state; counted by the instrumented kernels
 on the same frame) to its mean CUDA-event launch duration and the measured HBM copy
 bandwidth; `traffic` is its DRAM bytes per launch from the committed ncu summary.
-`cpu_baseline` times the CPU oracle on a bounded sample of the same frame.
+`cpu_baseline` times the CPU oracle on a stratified row sample of the same frame, and
+`parity` compares those rows with the GPU's frame of the same Constants bit for bit.
 
 --impl reference times the reference path tracer's CPU restatement (the oracle: the
 reference itself is Rust + Vulkan/GLSL and cannot run on this machine) on the host cores.
@@ -50,7 +51,8 @@ def parse_args():
     p.add_argument("--instances", type=int, default=64)
     p.add_argument("--freq", type=int, default=28)
     p.add_argument("--lights", type=int, default=1000)
-    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the cpu_baseline sample")
+    p.add_argument("--cpu-row-stride", type=int, default=ROW_STRIDE,
+                   help="the CPU legs render every n-th row of the frame (stratified sample)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--integrator", default="wavefront", choices=["wavefront", "megakernel"])
     p.add_argument("--slots", type=int, default=0, help="wavefront paths in flight (0 = library default)")
@@ -162,6 +164,41 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def l2_copy_gbs(device: int) -> dict:
+    """Bandwidth of a plain device-to-device copy whose source and destination both stay in
+    L2 (copies of 4, 8, 16 and 32 MB; read + write bytes per copy): for each size ~0.3 s of
+    back-to-back copies first (clocks up, lines resident), then the best of 3 runs of 400
+    copies timed by CUDA events on torch's stream; the best size is kept.  The ceiling for a
+    kernel whose bytes L2 serves."""
+    import torch
+
+    best, at = 0.0, 0
+    with torch.cuda.device(device):
+        for mb in (4, 8, 16, 32):
+            n = (mb << 20) // 4
+            src = torch.ones(n, dtype=torch.float32, device="cuda")
+            dst = torch.empty_like(src)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 0.3:
+                for _ in range(100):
+                    dst.copy_(src)
+                torch.cuda.synchronize()
+            for _ in range(3):
+                e0.record()
+                for _ in range(400):
+                    dst.copy_(src)
+                e1.record()
+                torch.cuda.synchronize()
+                gbs = 2 * n * 4 * 400 / (e0.elapsed_time(e1) / 1e3) / 1e9
+                if gbs > best:
+                    best, at = gbs, mb
+            del src, dst
+        torch.cuda.empty_cache()
+    return {"gbs": best, "copy_mb": at, "how": "torch copy_ of an L2-resident buffer (4/8/16/32 MB, best of 3 x 400 "
+                                              "copies after 0.3 s of warm-up copies), read + write bytes, CUDA events"}
+
+
 # Algorithmic bytes per unit of traversal work (wf_trace_kernel): a BVH4 node is one 128-byte
 # record (six float4 planes + child references); a triangle test reads one 48-byte record; an
 # object-ray set-up reads the instance's three inverse rows and its mesh word (64 bytes); a
@@ -174,13 +211,21 @@ RAY_STATE_BYTES = 64
 PROFILE = ROOT / "profiles" / "wf_trace_kernel_icosphere_field_1080p.md"
 
 
-def ncu_traffic_per_launch() -> float | None:
+def ncu_traffic_per_launch(rays_per_launch: float) -> float | None:
     """dram__bytes_read.sum + dram__bytes_write.sum per wf_trace_kernel launch of this
-    workload (mean over one frame's launches), from the committed ncu summary."""
+    workload: the committed ncu summary's DRAM bytes per traced ray (captured on a small case
+    of the same frame: every trace launch of one 1-spp render) times this run's rays per
+    launch."""
     if not PROFILE.exists():
         return None
-    m = re.search(r"traffic_per_launch_bytes:\s*([0-9.eE+]+)", PROFILE.read_text())
-    return float(m.group(1)) if m else None
+    m = re.search(r"dram_bytes_per_ray:\s*([0-9.eE+]+)", PROFILE.read_text())
+    return float(m.group(1)) * rays_per_launch if m else None
+
+
+def traffic_source() -> str:
+    return ("ncu dram__bytes_read.sum + dram__bytes_write.sum per traced ray, every wf_trace_kernel launch of a "
+            "1-spp render of the same frame, scaled by this run's rays per launch "
+            "(profiles/wf_trace_kernel_icosphere_field_1080p.md)")
 
 
 def ncu_trace_metrics() -> dict | None:
@@ -207,66 +252,106 @@ def make_workload(a):
 
 _CPU_SCENES: dict = {}
 
+# The CPU legs render a stratified row sample of the frame: every ROW_STRIDE-th row from
+# ROW_STRIDE // 2 on (135 of the 1080 rows at the default stride of 8), the whole width, all
+# samples and bounces.  Both legs (cpu_baseline and --impl reference) render the same rows,
+# and the GPU's frame of the same Constants is compared with them bit for bit.
+ROW_STRIDE = 8
 
-def cpu_baseline(w, arrays, target_seconds: float) -> dict:
-    """The oracle (a scalar C++ restatement, OpenMP over pixels on every host core, tracing
-    through the flat BVH) on a centred band of rows of the same frame, same spp and depth.
-    The band is sized from a calibration run so that the timed part takes ~target_seconds."""
+
+def sample_rows(height: int, stride: int) -> list[int]:
+    return list(range(stride // 2, height, stride))
+
+
+def _oracle_scene(arrays):
     from oracle import oracle
-    from tinytrace_gb300.renderer import make_constants
 
     key = id(arrays)
     t0 = time.perf_counter()
     if key not in _CPU_SCENES:
         _CPU_SCENES[key] = oracle.OracleScene(arrays, flat=True)
-    orc = _CPU_SCENES[key]
-    build_s = time.perf_counter() - t0
+    return _CPU_SCENES[key], time.perf_counter() - t0
+
+
+def render_rows(w, arrays, rows: list[int], target: np.ndarray) -> float:
+    """The oracle (a scalar C++ restatement, OpenMP over the pixels of a row on every host
+    core, tracing through the flat BVH) renders `rows` of the frame's first render (frame
+    index 0, accumulated frame count 0) into `target`; returns the seconds it took."""
+    from tinytrace_gb300.renderer import make_constants
+
+    orc, _ = _oracle_scene(arrays)
     c = make_constants(w.camera, w.extent, w.config, 0, 0)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    for y in rows:
+        orc.render(c, target, rows=(y, y + 1), threads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(w, arrays, stride: int) -> tuple[dict, np.ndarray, list[int]]:
+    """Times the oracle on the stratified row sample of the frame; returns the baseline record,
+    the CPU image (only the sampled rows written) and the rows."""
+    _, build_s = _oracle_scene(arrays)
     W, H = w.extent
     spp = w.config.sample_count
+    rows = sample_rows(H, stride)
     target = np.zeros((H, W, 4), np.float32)
-    threads = os.cpu_count() or 1
-    # calibrate on a thin band, then size the band (whole rows) for ~target_seconds
-    y0 = H // 2 - 1
-    t0 = time.perf_counter()
-    orc.render(c, target, rows=(y0, y0 + 2), threads=threads)
-    dt = max(time.perf_counter() - t0, 1e-3)
-    rows = int(max(2, min(H, 2 * target_seconds / dt)))
-    y0 = max(0, H // 2 - rows // 2)
-    t0 = time.perf_counter()
-    orc.render(c, target, rows=(y0, y0 + rows), threads=threads)
-    dt = time.perf_counter() - t0
-    samples = rows * W * spp
-    return {"value": samples / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{rows} centred rows x {W} px of the {W}x{H} frame at {spp} spp, depth "
-                      f"{w.config.bounce_count} ({samples} samples, {dt:.1f} s; BVH build {build_s:.1f} s "
-                      f"excluded)"}
+    dt = render_rows(w, arrays, rows, target)
+    samples = len(rows) * W * spp
+    rec = {"value": samples / dt / 1e6, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+           "sample": f"{len(rows)} stratified rows (every {stride}th from row {stride // 2}) x {W} px of the "
+                     f"{W}x{H} frame at {spp} spp, depth {w.config.bounce_count} ({samples} samples, {dt:.1f} s; "
+                     f"flat BVH build {build_s:.1f} s excluded)"}
+    return rec, target, rows
+
+
+def row_parity(gpu: np.ndarray, cpu: np.ndarray, rows: list[int]) -> dict:
+    """Bit-for-bit comparison of the sampled rows (any NaN equals any NaN), plus the largest
+    relative difference of the radiance where they differ."""
+    g = np.ascontiguousarray(gpu[rows], np.float32)
+    c = np.ascontiguousarray(cpu[rows], np.float32)
+    same = (g.view(np.uint32) == c.view(np.uint32)) | (np.isnan(g) & np.isnan(c))
+    with np.errstate(all="ignore"):
+        rel = np.abs(g.astype(np.float64) - c) / np.maximum(np.abs(c.astype(np.float64)), 1e-30)
+    rel = np.where(same, 0.0, rel)
+    return {"rows": len(rows), "pixels": int(g.shape[0] * g.shape[1]), "values_compared": int(g.size),
+            "values_differing": int((~same).sum()), "max_rel_err": float(np.nanmax(rel)) if rel.size else 0.0,
+            "bit_exact": bool(same.all()), "frame": "frame index 0, accumulated frame count 0 (no accumulation)",
+            "tolerance": "bit for bit (NaN payloads aside); the north-star bar is 1e-4 relative"}
 
 
 def run_reference(a, dist: Dist):
+    """The reference arm: the oracle renders the stratified row sample of the frame once per
+    step (W untimed, K timed steps); `ms_per_step` is the measured time of one step and
+    `value` the samples of the K steps over their time."""
     if dist.rank != 0:
         return
     from tinytrace_gb300.renderer import SceneArrays
 
     w = make_workload(a)
     arrays = SceneArrays(w.scene)
-    per_step = max(2.0, min(20.0, 60.0 / max(1, a.steps + a.warmup)))
-    for _ in range(min(a.warmup, 1)):
-        cpu_baseline(w, arrays, per_step / 4)
-    vals = []
-    last = None
-    for _ in range(a.steps):
-        last = cpu_baseline(w, arrays, per_step)
-        vals.append(last["value"])
-    v = statistics.median(vals)
-    frame_samples = w.extent[0] * w.extent[1] * w.config.sample_count
+    _, build_s = _oracle_scene(arrays)
+    W, H = w.extent
+    rows = sample_rows(H, a.cpu_row_stride)
+    target = np.zeros((H, W, 4), np.float32)
+    for _ in range(a.warmup):
+        render_rows(w, arrays, rows, target)
+    times = [render_rows(w, arrays, rows, target) for _ in range(a.steps)]
+    samples = len(rows) * W * w.config.sample_count
+    v = samples * a.steps / sum(times) / 1e6
+    threads = os.cpu_count() or 1
     out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-           # one step is a bounded band of the frame; this is the whole frame at the measured rate
-           "ms_per_step": frame_samples / (v * 1e6) * 1e3 if v > 0 else None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic (seeded generator)", "impl": "reference",
-           "config": {"workload": w.name, "triangles": arrays.triangle_count, "resolution": list(w.extent),
-                      "spp": w.config.sample_count, "depth": w.config.bounce_count},
-           "cpu_baseline": {**last, "value": v},
+           "ms_per_step": sum(times) / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)", "impl": "reference",
+           "config": {"workload": w.name, "triangles": arrays.triangle_count, "resolution": [W, H],
+                      "spp": w.config.sample_count, "depth": w.config.bounce_count,
+                      "step": f"{len(rows)} stratified rows (every {a.cpu_row_stride}th) x {W} px, "
+                              f"{samples} samples"},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"{len(rows)} stratified rows (every {a.cpu_row_stride}th from row "
+                                      f"{a.cpu_row_stride // 2}) x {W} px of the {W}x{H} frame at "
+                                      f"{w.config.sample_count} spp per step ({samples} samples; flat BVH build "
+                                      f"{build_s:.1f} s before the first step)"},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "reference arm = the reference path tracer restated on the CPU (oracle/); the reference "
                    "itself (Rust + Vulkan ray queries) cannot run on this machine"}
@@ -735,18 +820,31 @@ def run_ours(a, dist: Dist):
         node_achieved = node_bytes / trace_s / 1e9
         rays_per_launch = cnt.rays / trace_launches
         default_workload = (W, H, spp, w.config.bounce_count) == (1920, 1080, 64, 8)
-        traffic = ncu_traffic_per_launch() if default_workload and a.accel != "two_level" else None
+        traffic = ncu_traffic_per_launch(rays_per_launch) if default_workload and a.accel != "two_level" else None
     else:  # the megakernel does everything in one launch
         bytes_per_launch, launch_s = trace_bytes, kernel_s
         achieved = trace_bytes / kernel_s / 1e9
         node_achieved = node_bytes / kernel_s / 1e9
         rays_per_launch, traffic = cnt.rays, None
 
+    l2 = None
+    if dist.rank == 0:
+        try:
+            l2 = l2_copy_gbs(device)
+        except Exception:  # torch absent or without CUDA: the L2 reference is left out
+            l2 = None
     out_line = None
     if dist.rank == 0:
-        cpu = None
+        cpu, parity = None, None
         if not a.no_cpu_baseline:
-            cpu = cpu_baseline(w, r.scene_arrays, a.cpu_seconds)
+            from tinytrace_gb300.renderer import make_constants
+
+            cpu, cpu_img, rows = cpu_baseline(w, r.scene_arrays, a.cpu_row_stride)
+            # the GPU's first frame of the same Constants (the image the timed steps render,
+            # without their accumulation), compared with the oracle's rows
+            c0 = make_constants(w.camera, w.extent, w.config, 0, 0)
+            check(lib.tt_render(ctx, r.scene, native.ptr(c0), r.render_target))
+            parity = row_parity(r.context.download(r.render_target, W, H), cpu_img, rows)
         stages = {name: {"ms_per_step": stage_ns[i] / a.steps / 1e6,
                          "launches_per_step": int(stage_launches[i]) / a.steps}
                   for i, name in enumerate(native.STAGE_NAMES) if stage_launches[i] > 0}
@@ -773,9 +871,17 @@ def run_ours(a, dist: Dist):
                          "bytes_per_unit": {"node": NODE_BYTES, "triangle_record": TRI_RECORD_BYTES,
                                             "instance_ray_setup": INSTANCE_RAY_BYTES, "ray_state": RAY_STATE_BYTES},
                          "node_fetch_gbs": node_achieved, "node_fetch_frac": node_achieved / peak,
+                         "rays_per_frame": int(cnt.rays), "rays_per_sample": cnt.rays / samples_per_step,
+                         "rays_per_s": cnt.rays / (total_s / a.steps),
+                         "trace_rays_per_s": cnt.rays / trace_s if trace_launches > 0 else None,
+                         "l2_copy": l2, "l2_frac": achieved / l2["gbs"] if l2 else None,
+                         "dram_gbs": traffic / launch_s / 1e9 if traffic else None,
+                         "dram_frac": traffic / launch_s / 1e9 / peak if traffic else None,
+                         "limiter": "latency of dependent L1/L2 node fetches and SIMT efficiency: the algorithmic "
+                                    "bytes are served mostly by L1/L2 (see dram_frac and l2_frac), so `frac` "
+                                    "measures them against the HBM copy ceiling, not DRAM traffic",
                          "ncu": ncu_trace_metrics(),
-                         "traffic_source": "ncu dram bytes per launch, full workload "
-                                           "(profiles/wf_trace_kernel_icosphere_field_1080p.md)"},
+                         "traffic_source": traffic_source()},
             "stages": stages,
             "counters": {"rays": cnt.rays, "blas_nodes": cnt.blas_nodes, "tlas_nodes": cnt.tlas_nodes,
                          "triangles": cnt.triangles, "instances": cnt.instances, "hits": cnt.hits,
@@ -788,6 +894,7 @@ def run_ours(a, dist: Dist):
             "gpu_launches_overflow": stage_overflow,
             "loop": "host-driven" if a.host_loop else "device-side while loop in one CUDA graph per render",
             "cpu_baseline": cpu,
+            "parity": parity,
         }
         t = native.Timings()
         check(lib.tt_timings_get(ctx, ctypes.byref(t)))

@@ -21,6 +21,7 @@
 #ifndef TINYTRACE_CUDA_H
 #define TINYTRACE_CUDA_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -187,6 +188,48 @@ typedef struct tt_scene_desc {
     uint32_t texture_count;
     uint32_t reserved;
 } tt_scene_desc;
+
+/* Compile-time checks of the byte layouts the ABI shares with the reference's #[repr(C)] types
+ * (every C or C++ translation unit that includes this header checks them): sizes and field
+ * offsets of Constants (src/lib.rs:234-250), MaterialConstants and ProcessedMaterial
+ * (src/asset/material.rs:186-231, 268-274), ProcessedVertex, ProcessedMesh and
+ * EmissiveTriangle (src/asset/mod.rs:44-73) and Instance (src/scene.rs:236-246). */
+#ifdef __cplusplus
+#define TT_LAYOUT_CHECK(cond, what) static_assert(cond, what)
+#else
+#define TT_LAYOUT_CHECK(cond, what) _Static_assert(cond, what)
+#endif
+TT_LAYOUT_CHECK(sizeof(tt_constants) == 368, "Constants is 368 bytes");
+TT_LAYOUT_CHECK(offsetof(tt_constants, inverse_proj) == 256, "Constants.inverse_proj at 256");
+TT_LAYOUT_CHECK(offsetof(tt_constants, camera_position) == 320, "Constants.camera_position at 320");
+TT_LAYOUT_CHECK(offsetof(tt_constants, frame_index) == 336, "Constants.frame_index at 336");
+TT_LAYOUT_CHECK(offsetof(tt_constants, sample_count) == 344, "Constants.sample_count at 344");
+TT_LAYOUT_CHECK(offsetof(tt_constants, screen_size) == 352, "Constants.screen_size at 352");
+TT_LAYOUT_CHECK(offsetof(tt_constants, tonemap) == 360, "Constants.tonemap at 360");
+TT_LAYOUT_CHECK(offsetof(tt_constants, light_sampling) == 364, "Constants.light_sampling at 364");
+TT_LAYOUT_CHECK(sizeof(tt_material_constants) == 192, "MaterialConstants is 192 bytes");
+TT_LAYOUT_CHECK(offsetof(tt_material_constants, geometry_normal) == 96, "geometry_normal at 96");
+TT_LAYOUT_CHECK(offsetof(tt_material_constants, base_weight) == 112, "base_weight at 112");
+TT_LAYOUT_CHECK(offsetof(tt_material_constants, specular_roughness) == 128, "specular_roughness at 128");
+TT_LAYOUT_CHECK(offsetof(tt_material_constants, coat_weight) == 152, "coat_weight at 152");
+TT_LAYOUT_CHECK(offsetof(tt_material_constants, emission_luminance) == 184, "emission_luminance at 184");
+TT_LAYOUT_CHECK(offsetof(tt_material_constants, geometry_opacity) == 188, "geometry_opacity at 188");
+TT_LAYOUT_CHECK(sizeof(tt_material) == 304, "ProcessedMaterial is 304 bytes");
+TT_LAYOUT_CHECK(offsetof(tt_material, textures) == 192, "ProcessedMaterial.textures at 192");
+TT_LAYOUT_CHECK(offsetof(tt_material, padding) == 300, "ProcessedMaterial.padding at 300");
+TT_LAYOUT_CHECK(sizeof(tt_vertex) == 8, "ProcessedVertex is 8 bytes");
+TT_LAYOUT_CHECK(offsetof(tt_vertex, tangent_frame) == 4, "ProcessedVertex.tangent_frame at 4");
+TT_LAYOUT_CHECK(sizeof(tt_mesh) == 32, "ProcessedMesh is 32 bytes");
+TT_LAYOUT_CHECK(offsetof(tt_mesh, vertex_offset) == 16, "ProcessedMesh.vertex_offset at 16");
+TT_LAYOUT_CHECK(offsetof(tt_mesh, index_count) == 28, "ProcessedMesh.index_count at 28");
+TT_LAYOUT_CHECK(sizeof(tt_instance) == 208, "Instance is 208 bytes");
+TT_LAYOUT_CHECK(offsetof(tt_instance, normal_transform) == 128, "Instance.normal_transform at 128");
+TT_LAYOUT_CHECK(offsetof(tt_instance, vertex_offset) == 192, "Instance.vertex_offset at 192");
+TT_LAYOUT_CHECK(offsetof(tt_instance, mesh_index) == 204, "Instance.mesh_index at 204");
+TT_LAYOUT_CHECK(sizeof(tt_emissive_triangle) == 36, "EmissiveTriangle is 36 bytes");
+TT_LAYOUT_CHECK(offsetof(tt_emissive_triangle, hash) == 18, "EmissiveTriangle.hash at 18");
+TT_LAYOUT_CHECK(offsetof(tt_emissive_triangle, texture_coordinates) == 20, "EmissiveTriangle.uv at 20");
+TT_LAYOUT_CHECK(offsetof(tt_emissive_triangle, instance_index) == 32, "EmissiveTriangle.instance_index at 32");
 
 /* src/lib.rs:228-232 Timings, in nanoseconds of device time */
 typedef struct tt_timings {
@@ -473,9 +516,12 @@ int32_t tt_trace_batch(tt_context* ctx, tt_handle scene, const float* rays, uint
  * tt_trace_batch; n above TT_TRACE_NOALLOC_MAX_RAYS is rejected with TT_ERR_INVALID_ARGUMENT
  * before any GPU work.  The first call on a device looks the array's device address up
  * (cudaGetSymbolAddress) with that device current; make that first call before any stream
- * capture.  Every call shares the array and leaves its contents behind (the error word is
- * cleared at the start of each call); calls whose GPU work overlaps (two contexts of one
- * device) race on it.  The call synchronises the context stream before it returns. */
+ * capture.  The address is kept until the process exits: after a device reset
+ * (cudaDeviceReset) the entry point must not be called on that device again.  Every call
+ * shares the array and leaves its contents behind (the error word is cleared at the start of
+ * each call); calls whose GPU work overlaps (two contexts of one device) race on it.  The call
+ * synchronises the context stream before it returns, and reports an error word left pending
+ * by an earlier asynchronous call on the context as tt_trace_batch does. */
 #define TT_TRACE_NOALLOC_MAX_RAYS 65536u
 int32_t tt_trace_batch_noalloc(tt_context* ctx, tt_handle scene, const float* rays, uint32_t n,
                                uint32_t flags, uint32_t* hits);

@@ -110,3 +110,38 @@ def test_handles_and_dtypes_roundtrip():
     c = np.zeros((), native.CONSTANTS_DTYPE)
     assert c.nbytes == 368
     assert native.NODE4_DTYPE.itemsize == 128 and native.TRI_RECORD_DTYPE.itemsize == 48
+
+
+def _compile_c(tmp_path, header_dir: Path, name: str) -> subprocess.CompletedProcess:
+    src = tmp_path / f"{name}.c"
+    src.write_text('#include "tinytrace_cuda.h"\nint main(void) { return 0; }\n')
+    return subprocess.run(["gcc", "-std=c11", "-Wall", "-pedantic", "-Werror", f"-I{header_dir}", "-c", str(src),
+                           "-o", str(tmp_path / f"{name}.o")], capture_output=True, text=True)
+
+
+def test_header_layout_checks_compile_as_c11(tmp_path):
+    """The header's _Static_assert layout checks (sizes and field offsets of the reference's
+    #[repr(C)] types) hold for a C11 compiler, and they catch a reordered field."""
+    ok = _compile_c(tmp_path, HEADER.parent, "ok")
+    assert ok.returncode == 0, ok.stderr
+    bad_dir = tmp_path / "bad"
+    bad_dir.mkdir()
+    text = HEADER.read_text()
+    swapped = text.replace("    uint32_t tonemap;\n    uint32_t light_sampling;\n",
+                           "    uint32_t light_sampling;\n    uint32_t tonemap;\n")
+    assert swapped != text
+    (bad_dir / "tinytrace_cuda.h").write_text(swapped)
+    bad = _compile_c(tmp_path, bad_dir, "bad")
+    assert bad.returncode != 0 and "Constants.tonemap at 360" in bad.stderr
+
+
+def test_rust_sys_crate_declares_every_function():
+    """rust/tinytrace_cuda_sys mirrors the header: every declared function and every #define
+    constant appear there (source-only crate: no Rust toolchain on this machine)."""
+    text = (ROOT / "rust" / "tinytrace_cuda_sys" / "src" / "lib.rs").read_text()
+    declared = set(re.findall(r"pub fn (tt_\w+)\(", text))
+    assert declared == header_functions()
+    consts = dict(re.findall(r"pub const (TT_\w+): \w+ = (\d+);", text))
+    for name, value in header_defines().items():
+        assert name in consts, name
+        assert int(consts[name]) == value, name

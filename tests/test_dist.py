@@ -65,6 +65,29 @@ def test_reference_arm_under_torchrun():
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
     assert line["higher_is_better"] is True and line["unit"] == "Msamples/s"
+    # one step renders the stratified rows; ms_per_step is that measured time, and value is the
+    # samples of the timed steps over it
+    rows = len(range(4, 24, 8))
+    assert "stratified rows" in line["config"]["step"]
+    samples = rows * 48 * 2
+    assert abs(line["value"] - samples / (line["ms_per_step"] / 1e3) / 1e6) <= 1e-6 * line["value"]
+
+
+def test_row_sample_and_parity_helpers():
+    import numpy as np
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    rows = bench.sample_rows(1080, 8)
+    assert rows[0] == 4 and rows[-1] == 1076 and len(rows) == 135
+    a = np.random.default_rng(0).random((32, 8, 4)).astype(np.float32)
+    b = a.copy()
+    b[4, 1, 2] = np.nextafter(b[4, 1, 2], np.float32(2))
+    b[12, 0, 0] = a[12, 0, 0] = np.nan
+    p = bench.row_parity(a, b, [4, 12, 20])
+    assert p["values_differing"] == 1 and not p["bit_exact"] and 0 < p["max_rel_err"] < 1e-6
+    assert bench.row_parity(a, a, [4, 12, 20])["bit_exact"]
 
 
 @pytest.mark.parametrize("world", [1])

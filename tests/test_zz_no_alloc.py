@@ -6,8 +6,9 @@ which an allocation's implicit device synchronisation would stall the frame.  Fo
 library stages rays, hits and the traversal error word in one static device array (at most
 TT_TRACE_NOALLOC_MAX_RAYS rays per call).  This file checks, through the C ABI, that the
 allocation-free entry point returns exactly the hits of the allocating one (tolerance zero,
-as in the other ray-query tests) on two calls in a row — the shared array keeps the previous
-call's contents — and that a batch above the maximum is refused before any GPU work.
+as in the other ray-query tests) on calls in a row — the shared array keeps the previous
+call's contents, and a smaller call after a larger one must return only its own hits — and
+that a batch above the maximum is refused before any GPU work.
 """
 import numpy as np
 import pytest
@@ -42,8 +43,10 @@ def test_noalloc_matches_allocating_entry_point(gpu_context):
     scene = ctx.create_scene(arrays)
     targets = arrays.instances["transform"][:, 12:15]
     rng = np.random.default_rng(21)
-    # two calls in a row: a small batch, then the largest accepted batch
-    for n, flags in ((5000, native.TT_TRACE_CULL_BACK_FACES), (native.TT_TRACE_NOALLOC_MAX_RAYS, 0)):
+    # calls in a row: a small batch, the largest accepted batch, then a smaller one again (the
+    # shared array still holds the larger call's rays and hits beyond its n)
+    for n, flags in ((5000, native.TT_TRACE_CULL_BACK_FACES), (native.TT_TRACE_NOALLOC_MAX_RAYS, 0),
+                     (3001, native.TT_TRACE_CULL_BACK_FACES)):
         rays = _rays(rng, n, targets)
         expected = _trace(ctx, ctx.lib.tt_trace_batch, scene, rays, flags)
         got = _trace(ctx, ctx.lib.tt_trace_batch_noalloc, scene, rays, flags)

@@ -163,6 +163,12 @@ struct tt_context {
 };
 
 namespace tt {
+void raise_device_error(uint32_t e) {
+    if (e & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
+    if (e & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
+    if (e & ERR_TENSOR_WAIT) fail(TT_ERR_TIMEOUT, "radiance-cache tensor-core wait limit reached");
+    if (e) fail(TT_ERR_DEVICE, "unknown device error bits " + std::to_string(e));
+}
 namespace {
 
 uint64_t make_handle(uint32_t lifetime, uint32_t kind, uint32_t epoch, uint32_t index) {
@@ -198,10 +204,7 @@ void use_device(tt_context* ctx) { check_cuda(cudaSetDevice(ctx->device), "cudaS
 void check_device_errors(tt_context* ctx) {
     if (!ctx->err_pending) return;
     ctx->err_pending = false;
-    uint32_t e = *ctx->err_host;
-    if (e & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
-    if (e & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
-    if (e & ERR_TENSOR_WAIT) fail(TT_ERR_TIMEOUT, "radiance-cache tensor-core wait limit reached");
+    raise_device_error(*ctx->err_host);
 }
 void sync(tt_context* ctx) {
     check_cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
@@ -1475,6 +1478,9 @@ int32_t tt_trace_batch_noalloc(tt_context* ctx, tt_handle scene, const float* ra
         use_device(ctx);
         SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
         trace_batch_noalloc(ctx->device, s->dev, rays, n, flags, hits, ctx->stream);
+        // the stream is synchronised: an error word still pending from an earlier asynchronous
+        // call on this context is reported here, as tt_trace_batch reports it
+        check_device_errors(ctx);
     });
 }
 

@@ -290,7 +290,9 @@ constexpr uint64_t NOALLOC_BYTES = NOALLOC_HITS_OFFSET + 32ull * TT_TRACE_NOALLO
 static __device__ __align__(256) unsigned char g_trace_scratch[NOALLOC_BYTES];
 
 // Device address of g_trace_scratch on `device`, looked up once per device with that device
-// current (in host code the symbol itself is only a host-side stand-in).
+// current (in host code the symbol itself is only a host-side stand-in).  The address is kept
+// for the life of the process: a device reset (cudaDeviceReset by the application or another
+// library) makes it stale, and tt_trace_batch_noalloc must not be called on that device again.
 static unsigned char* trace_scratch_address(int device) {
     constexpr int MAX_DEVICES = 64;
     static std::mutex mutex;
@@ -322,8 +324,7 @@ void trace_batch_noalloc(int device, const DevScene& sc, const float* rays_host,
     if (n) check_cuda(cudaMemcpyAsync(hits_host, hits, 32ull * n, cudaMemcpyDeviceToHost, st), "read hits");
     check_cuda(cudaMemcpyAsync(&err_value, err, 4, cudaMemcpyDeviceToHost, st), "read error word");
     check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-    if (err_value & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
-    if (err_value & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
+    raise_device_error(err_value);
 }
 
 }  // namespace tt

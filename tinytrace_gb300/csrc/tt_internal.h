@@ -19,6 +19,9 @@ struct Error {
 };
 [[noreturn]] void fail(int32_t code, const std::string& message);
 void check_cuda(cudaError_t e, const char* what);
+// Maps the bits of a device error word (ERR_* of tt_bvh.cuh) to a thrown status; returns when
+// no bit is set.  Every path that reads an error word back reports it through this function.
+void raise_device_error(uint32_t error_bits);
 
 // A device allocation owned by a resource.
 struct DeviceBuffer {
