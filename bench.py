@@ -359,15 +359,45 @@ def run_reference(a, dist: Dist):
 
 
 # ---------------------------------------------------------------- ReSTIR DI sample
-def run_restir(a, device: int) -> dict:
+# Algorithmic bytes per pixel of the ReSTIR passes (constant materials, uniform candidates),
+# for a pixel whose camera ray hits a surface; closest-hit traversal (the G-buffer's camera ray,
+# the visibility rays of the initial and shade passes) comes on top.  Records: G-buffer surface
+# 64 B, prepared lobes 96 B, reservoir 32 B, material constants 192 B, light record 64 B (the
+# four 16-byte rows a light point reads), hit reconstruction 262 B (instance 208, indices 12,
+# snorm16 positions 18, vertices 24), target pixel 16 B read + 16 B written.
+RESTIR_PASS_BYTES = {
+    "restir_gbuffer": 262 + 192 + 64 + 96,
+    "restir_initial": 64 + 96 + 192 + 32 * 64 + 32,
+    "restir_temporal": 64 + 96 + 192 + 64 + 32 + 32 + 2 * 64 + 32,
+    "restir_spatial": 64 + 96 + 192 + 32 + 64 + 5 * (64 + 32 + 64) + 32,
+    "restir_shade": 64 + 96 + 192 + 32 + 64 + 32,
+}
+RESTIR_PROFILE = ROOT / "profiles" / "restir_passes_restir_field_1080p.md"
+
+
+def restir_initial_flops_per_pixel() -> float | None:
+    """FP32 operations per pixel of the initial-candidate pass (FADD + FMUL + 2 x FFMA thread
+    instructions per pixel, measured by ncu on a small case of the same scene and camera; the
+    committed summary)."""
+    if not RESTIR_PROFILE.exists():
+        return None
+    m = re.search(r"initial_fp32_flops_per_pixel:\s*([0-9.eE+]+)", RESTIR_PROFILE.read_text())
+    return float(m.group(1)) if m else None
+
+
+def run_restir(a, device: int, sm_mhz: float | None) -> dict:
     """ReSTIR DI on the 2.1 M-triangle, 100 k-light scene: 1920x1080, 1 sample per pixel per frame,
     32 candidates, temporal reuse (M cap 20 x), 5 spatial neighbours in 30 px, a 60-frame orbit;
-    device time of the 60 frames by CUDA events on the context stream."""
+    device time of the 60 frames by CUDA events on the context stream.  Then the same orbit with
+    CUDA events around each pass (per-pass time, algorithmic bytes, the initial pass's FP32 rate
+    against the FP32 FMA peak at the sampled SM clock), and, at 960x540 over the orbit's first 12
+    frames, the oracle's time (cpu_baseline) and its images and reservoirs against the GPU's."""
     import ctypes
 
+    from oracle import oracle
     from tinytrace_gb300 import native, scenes
     from tinytrace_gb300.native import check
-    from tinytrace_gb300.renderer import Config, Renderer
+    from tinytrace_gb300.renderer import Config, Renderer, make_constants
 
     W, H, frames = a.width, a.height, 60
     r = Renderer((W, H), device=device)
@@ -397,12 +427,89 @@ def run_restir(a, device: int) -> dict:
     check(lib.tt_event_elapsed_ms(ctx, 2, 3, ctypes.byref(ms)))
     img = r.context.download(r.render_target, W, H)
     stats = r.context.scene_stats(r.scene)
+
+    # the same orbit with CUDA events around every pass
+    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 1))
+    r.restir_reset()
+    pass_ns = np.zeros(native.TT_STAGE_COUNT)
+    for f in range(frames):
+        r.camera = orbit(f)
+        check(lib.tt_flush_l2(ctx))
+        r.render_restir_to_target()
+        r.present()
+        stt = native.StageTimings()
+        check(lib.tt_stage_timings_get(ctx, ctypes.byref(stt)))
+        pass_ns += np.array(stt.ns[:], np.float64)
+    check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 0))
+    passes = {}
+    for name, stage in (("restir_gbuffer", native.TT_STAGE_RESTIR_GBUFFER),
+                        ("restir_initial", native.TT_STAGE_RESTIR_INITIAL),
+                        ("restir_temporal", native.TT_STAGE_RESTIR_TEMPORAL),
+                        ("restir_spatial", native.TT_STAGE_RESTIR_SPATIAL),
+                        ("restir_shade", native.TT_STAGE_RESTIR_SHADE)):
+        t = pass_ns[stage] / frames / 1e9
+        b = RESTIR_PASS_BYTES[name] * W * H
+        passes[name] = {"ms_per_frame": t * 1e3, "algorithmic_bytes_per_frame": b,
+                        "algorithmic_gbs": b / t / 1e9 if t > 0 else None}
     r.close()
+    peak, _ = measured_peaks()
+    t_init = pass_ns[native.TT_STAGE_RESTIR_INITIAL] / frames / 1e9
+    flops_px = restir_initial_flops_per_pixel()
+    mhz = sm_mhz or 2070.0
+    fp32_peak = 152 * 128 * 2 * mhz * 1e6 / 1e12  # TFLOP/s: SMs x FP32 lanes x FMA x clock
+    roofline = {"kernel": "restir_initial_kernel", "bound": "alu (FP32 BSDF evaluation of 32 candidates per pixel)",
+                "fp32_flops_per_pixel": flops_px,
+                "achieved_tflops": flops_px * W * H / t_init / 1e12 if flops_px and t_init > 0 else None,
+                "fp32_peak_tflops": fp32_peak,
+                "fp32_peak_source": f"nominal: 152 SMs x 128 FP32 lanes x 2 (FMA) x {mhz:.0f} MHz (sampled SM clock)",
+                "bytes_per_pixel": RESTIR_PASS_BYTES["restir_initial"],
+                "algorithmic_gbs": passes["restir_initial"]["algorithmic_gbs"], "hbm_peak_gbs": peak,
+                "flops_source": "ncu FP32 thread-instruction counts on a 480x270 frame of the same orbit "
+                                "(profiles/restir_passes_restir_field_1080p.md)"}
+    if roofline["achieved_tflops"] is not None:
+        roofline["frac"] = roofline["achieved_tflops"] / fp32_peak
+
+    # oracle: CPU time and bit-for-bit parity over the orbit's first frames at a quarter of the pixels
+    cw, chh, cframes = W // 2, H // 2, 12
+    rs = Renderer((cw, chh), device=device)
+    rs.set_scene(scene)
+    rs.set_config(Config(bounce_count=1, sample_count=1))
+    orc = oracle.OracleScene(rs.scene_arrays, flat=True)
+    R = oracle.OracleRestir(orc, cw, chh)
+    cpu = np.zeros((chh, cw, 4), np.float32)
+    cpu_s, differing, compared = 0.0, 0, 0
+    for f in range(cframes):
+        rs.camera = orbit(f)
+        c = make_constants(rs.camera, (cw, chh), rs.config(), rs.context.frame_index(), rs.accumulated_frame_count)
+        rs.render_restir_to_target()
+        t0 = time.perf_counter()
+        R.frame(c, cpu, threads=os.cpu_count() or 1)
+        cpu_s += time.perf_counter() - t0
+        for gpu_arr, cpu_arr in ((rs.context.download(rs.render_target, cw, chh), cpu),
+                                 (rs.restir_reservoirs(), R.reservoirs())):
+            g, k = np.ascontiguousarray(gpu_arr, np.float32), np.ascontiguousarray(cpu_arr, np.float32)
+            same = (g.view(np.uint32) == k.view(np.uint32)) | (np.isnan(g) & np.isnan(k))
+            differing += int((~same).sum())
+            compared += int(same.size)
+        rs.present()
+    rs.close()
+    cpu_rate = cw * chh * cframes / cpu_s / 1e6
+    gpu_rate = W * H * frames / (ms.value / 1e3) / 1e6
     return {"workload": f"restir_field_{stats.triangle_count}tri_{int(stats.emissive_count)}lights_{W}x{H}_60frames",
-            "ms_per_frame": ms.value / frames, "msamples_per_s": W * H * frames / (ms.value / 1e3) / 1e6,
+            "ms_per_frame": ms.value / frames, "msamples_per_s": gpu_rate,
             "candidates": 32, "temporal_m_cap": 20, "spatial_neighbours": 5, "spatial_radius_px": 30,
             "l2": "flushed before every frame", "image_mean": float(img[..., :3].mean()),
-            "image_finite": bool(np.isfinite(img).all())}
+            "image_finite": bool(np.isfinite(img).all()),
+            "passes": passes, "bytes_note": "algorithmic bytes per pixel whose camera ray hits a surface, "
+                                             "closest-hit traversal not included (an upper bound for sky pixels)",
+            "roofline": roofline,
+            "cpu_baseline": {"value": cpu_rate, "unit": "Msamples/s", "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"the oracle's ReSTIR frames at {cw}x{chh}, the orbit's first {cframes} "
+                                       f"frames, same scene and settings ({cpu_s:.1f} s)"},
+            "speedup_vs_cpu": gpu_rate / cpu_rate,
+            "parity": {"frames": cframes, "resolution": [cw, chh], "values_compared": compared,
+                       "values_differing": differing, "bit_exact": differing == 0,
+                       "compared": "images and final reservoirs of every frame"}}
 
 
 # ---------------------------------------------------------------- radiance-cache sample
@@ -906,7 +1013,7 @@ def run_ours(a, dist: Dist):
                 out_line["radiance_cache"] = {"error": f"{type(e).__name__}: {e}"}
         if not a.no_restir and dist.world == 1:
             try:
-                out_line["restir"] = run_restir(a, device)
+                out_line["restir"] = run_restir(a, device, clk.get("sm_mhz"))
             except Exception as e:
                 out_line["restir"] = {"error": f"{type(e).__name__}: {e}"}
         if not a.no_textured and dist.world == 1:

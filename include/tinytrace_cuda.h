@@ -249,8 +249,8 @@ typedef struct tt_scene_stats {
     uint64_t accel; /* TT_ACCEL_FLAT or TT_ACCEL_TWO_LEVEL */
 } tt_scene_stats;
 
-/* Device time per integrator stage of the last render, summed over its launches (with
- * TT_OPTION_STAGE_TIMING on).  Extends the integrate/post-process timestamps of
+/* Device time per integrator stage of the last render (tt_render or tt_render_restir), summed
+ * over its launches (with TT_OPTION_STAGE_TIMING on).  Extends the integrate/post-process timestamps of
  * src/lib.rs:149-193 (backend timing.rs:62-68) to the wavefront stages. */
 #define TT_STAGE_REGEN 0
 #define TT_STAGE_EXTEND 1  /* closest-hit trace of extension rays */
@@ -259,7 +259,13 @@ typedef struct tt_scene_stats {
 #define TT_STAGE_REDUCE 4
 #define TT_STAGE_MEGAKERNEL 5
 #define TT_STAGE_CACHE 6   /* radiance-cache queries of paths ending in the cache */
-#define TT_STAGE_COUNT 8
+#define TT_STAGE_CACHE_TRAIN 7      /* radiance-cache training after a cached frame (pairs + Adam steps) */
+#define TT_STAGE_RESTIR_GBUFFER 8   /* ReSTIR DI passes of tt_render_restir */
+#define TT_STAGE_RESTIR_INITIAL 9
+#define TT_STAGE_RESTIR_TEMPORAL 10
+#define TT_STAGE_RESTIR_SPATIAL 11
+#define TT_STAGE_RESTIR_SHADE 12
+#define TT_STAGE_COUNT 16
 typedef struct tt_stage_timings {
     uint64_t ns[TT_STAGE_COUNT];
     uint64_t launches[TT_STAGE_COUNT];
@@ -441,6 +447,12 @@ int32_t tt_cache_query(tt_context* ctx, const float* queries, uint32_t n, float*
 /* One Adam step on the mean relative L2 loss of n (query, target radiance) pairs; returns the
  * summed loss before the step. */
 int32_t tt_cache_train(tt_context* ctx, const float* queries, const float* targets, uint32_t n, float* loss);
+/* The gradients one tt_cache_train step would apply, without applying them (parameters and Adam
+ * state unchanged): weight_gradients (TT_CACHE_WEIGHTS floats) and grid_gradients
+ * (TT_CACHE_GRID_FLOATS floats, may be null) of the mean relative L2 loss of the n pairs, and
+ * the summed loss.  For checking the tensor-core backward pass against a reference. */
+int32_t tt_cache_gradients(tt_context* ctx, const float* queries, const float* targets, uint32_t n,
+                           float* weight_gradients, float* grid_gradients, float* loss);
 /* FP32 parameters: grid (TT_CACHE_GRID_FLOATS, may be null) and weights (TT_CACHE_WEIGHTS). */
 int32_t tt_cache_parameters(tt_context* ctx, float* grid, float* weights);
 typedef struct tt_cache_status {

@@ -72,7 +72,13 @@ pub const TT_STAGE_SHADOW: usize = 3;
 pub const TT_STAGE_REDUCE: usize = 4;
 pub const TT_STAGE_MEGAKERNEL: usize = 5;
 pub const TT_STAGE_CACHE: usize = 6;
-pub const TT_STAGE_COUNT: usize = 8;
+pub const TT_STAGE_CACHE_TRAIN: usize = 7;
+pub const TT_STAGE_RESTIR_GBUFFER: usize = 8;
+pub const TT_STAGE_RESTIR_INITIAL: usize = 9;
+pub const TT_STAGE_RESTIR_TEMPORAL: usize = 10;
+pub const TT_STAGE_RESTIR_SPATIAL: usize = 11;
+pub const TT_STAGE_RESTIR_SHADE: usize = 12;
+pub const TT_STAGE_COUNT: usize = 16;
 
 pub const TT_CACHE_WEIGHTS: u32 = 16896;
 pub const TT_CACHE_GRID_FLOATS: u32 = 16777216;
@@ -421,6 +427,8 @@ extern "C" {
     pub fn tt_cache_train(ctx: *mut tt_context, queries: *const f32, targets: *const f32, n: u32,
                           loss: *mut f32) -> i32;
     pub fn tt_cache_parameters(ctx: *mut tt_context, grid: *mut f32, weights: *mut f32) -> i32;
+    pub fn tt_cache_gradients(ctx: *mut tt_context, queries: *const f32, targets: *const f32, n: u32,
+                              weight_gradients: *mut f32, grid_gradients: *mut f32, loss: *mut f32) -> i32;
     pub fn tt_cache_status_get(ctx: *mut tt_context, out: *mut tt_cache_status) -> i32;
 
     // serving

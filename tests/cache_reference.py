@@ -98,3 +98,42 @@ def adam(p, g, m, v, step, lr):
     v = 0.99 * v + 0.01 * g * g
     c1, c2 = 1 - 0.9 ** step, 1 - 0.99 ** step
     return p - lr * (m / c1) / (np.sqrt(v / c2) + 1e-15), m, v
+
+
+GRAD_SCALE = 1.0 / 64.0  # the kernel scales the output gradient into FP16 range and undoes it at the end
+GRAD_CLAMP = 16384.0     # |dL/dy| per output before the mean's 1 / (3 n)
+
+
+def grads_fp16(q, target, grid, weights):
+    """The gradients of loss_and_grads computed with the training kernel's roundings: FP16
+    inputs, weights, hidden activations, output gradient (clamped, scaled by GRAD_SCALE) and
+    per-layer deltas; products accumulated in float64 here (FP32 on the tensor cores).
+    Returns (summed loss, weight gradients, grid gradients)."""
+    r = lambda a: a.astype(np.float16).astype(np.float64)  # noqa: E731
+    x = encode(q, grid)
+    ws, wo = split(weights.astype(np.float64))
+    h = [r(x)]
+    for w in ws:
+        h.append(r(np.maximum(h[-1] @ r(w).T, 0.0)))
+    y = h[-1] @ r(wo).T
+    n = len(q)
+    d = y - target
+    den = y * y + 0.01
+    loss = (d * d / den).sum()
+    g = r(np.clip(2.0 * d / den, -GRAD_CLAMP, GRAD_CLAMP) * GRAD_SCALE)
+    inv = 1.0 / (3.0 * n) / GRAD_SCALE
+    g_wo = (g.T @ h[-1]) * inv
+    grad = g @ r(wo)
+    g_ws = [None] * HIDDEN
+    for l in range(HIDDEN - 1, -1, -1):
+        delta = r(np.where(h[l + 1] > 0, grad, 0.0))
+        g_ws[l] = (delta.T @ h[l]) * inv
+        grad = delta @ r(ws[l])
+    g_w = np.concatenate([gw.ravel() for gw in g_ws] + [np.vstack([g_wo, np.zeros((OUT_ROWS - 3, WIDTH))]).ravel()])
+    g_grid = np.zeros(grid.shape)
+    gx = grad[:, :2 * LEVELS] * inv
+    for l in range(LEVELS):
+        idx, w = corners(q[:, 0:3], l)
+        for c in range(8):
+            np.add.at(g_grid[l], idx[:, c], w[:, c, None] * gx[:, 2 * l:2 * l + 2])
+    return loss, g_w, g_grid

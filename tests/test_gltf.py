@@ -165,13 +165,19 @@ def test_imported_scene_renders(tmp_path):
     assert np.isfinite(img).all() and img[..., :3].max() > 0.0
 
 
-REFERENCE_CORNELL = Path("/root/reference/scenes/cornell_box.gltf")
+REFERENCE_CORNELL = Path(__file__).resolve().parent / "golden" / "cornell_box.gltf"
+FIXTURE_SHA256 = {"cornell_box.gltf": "a15d11edadb3ff1c975bf22da50fa01b49075e48ae2507c1d8053abebe509012",
+                  "cornell_box.bin": "4bd62cf514d12da6801612a5b4b126967488715f634872c45a0c22f45f9cc5f1"}
 
 
-@pytest.mark.skipif(not REFERENCE_CORNELL.exists(), reason="the reference's fixture is not on this machine")
 def test_reference_cornell_fixture():
-    """The reference's own Cornell box, read where it lies (not copied), imports with its 32
-    triangles, its two emissive triangles of strength 40 and its metal material."""
+    """The reference's own Cornell box (scenes/cornell_box.gltf + .bin, committed unchanged by
+    tests/golden/copy_reference_gltf.py) imports with its 32 triangles, its two emissive
+    triangles of strength 40 and its metal material (src/asset/gltf.rs:50-122, 242-383)."""
+    import hashlib
+
+    for name, digest in FIXTURE_SHA256.items():
+        assert hashlib.sha256((REFERENCE_CORNELL.parent / name).read_bytes()).hexdigest() == digest, name
     imp = gltf.load(REFERENCE_CORNELL)
     arrays = SceneArrays(imp.scene)
     assert arrays.triangle_count == 32 and len(arrays.emissive) == 2

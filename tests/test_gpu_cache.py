@@ -5,7 +5,9 @@ are compared with the reference's FP16 emulation within 2e-3 of the output scale
 loss with the loss of that FP16 forward pass within 1e-3 relative, and the first Adam step
 (which moves every parameter with a nonzero gradient by exactly the learning rate, against the
 sign of its gradient) must agree in sign with the reference's float64 gradients on 98 % of the
-parameters whose gradient is above 1e-4 of the largest."""
+parameters whose gradient is above 1e-4 of the largest.  The gradient values of one step
+(tt_cache_gradients) are compared with a NumPy restatement of the kernel's FP16 roundings
+within 5e-3 relative L2 and with the float64 gradients within 5e-2 (weights) / 1e-1 (grid)."""
 import ctypes
 
 import numpy as np
@@ -82,6 +84,55 @@ def test_first_step_follows_the_reference_gradients(gpu_context):
         agree = np.sign(step[big]) == -np.sign(g[big])
         assert agree.mean() > 0.98, (name, agree.mean(), big.sum())
         assert np.allclose(np.abs(step[big]), 1e-2, rtol=1e-2, atol=1e-5), name
+
+
+def _gradients(ctx, q, t):
+    gw = np.zeros(native.TT_CACHE_WEIGHTS, np.float32)
+    gg = np.zeros(native.TT_CACHE_GRID_FLOATS, np.float32)
+    loss = ctypes.c_float()
+    check(ctx.lib.tt_cache_gradients(ctx.handle, native.ptr(q), native.ptr(t), len(q), native.ptr(gw),
+                                     native.ptr(gg), ctypes.byref(loss)))
+    return loss.value, gw.astype(np.float64), gg.astype(np.float64).reshape(cr.LEVELS, cr.TABLE, 2)
+
+
+def _rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+@pytest.mark.parametrize("train_steps", [0, 25])
+def test_gradient_values_match_the_reference(gpu_context, train_steps):
+    """The values (not only the signs) of one step's weight and grid gradients, at the initial
+    parameters and after 25 Adam steps, with a batch that ends in a partial tile: within 5e-3
+    (relative L2) of the NumPy restatement of the kernel's FP16 roundings, and within 5e-2
+    (weights) / 1e-1 (grid, four FP16 deltas deep) of the float64 gradients of the FP32 network;
+    99 % of the large weight gradients within 2 % of the FP16 restatement.  The parameters are
+    unchanged by the call."""
+    ctx = gpu_context
+    _configure(ctx, seed=13)
+    rng = np.random.default_rng(4)
+    for _ in range(train_steps):
+        qt = _queries(rng, 4096)
+        _train(ctx, qt, _field(qt))
+    grid0, w0 = _params(ctx)
+    q = _queries(rng, 2000)
+    t = _field(q)
+    loss, gw, gg = _gradients(ctx, q, t)
+    grid1, w1 = _params(ctx)
+    assert np.array_equal(w0, w1) and np.array_equal(grid0, grid1)
+    q64, t64, grid64, w64 = q.astype(np.float64), t.astype(np.float64), grid0.astype(np.float64), w0.astype(np.float64)
+    loss16, gw16, gg16 = cr.grads_fp16(q64, t64, grid64, w64)
+    _, gw64, gg64 = cr.loss_and_grads(q64, t64, grid64, w64)
+    assert abs(loss - loss16) <= 1e-3 * loss16, (loss, loss16)
+    errs = {"weights_fp16": _rel_l2(gw, gw16), "grid_fp16": _rel_l2(gg, gg16),
+            "weights_f64": _rel_l2(gw, gw64), "grid_f64": _rel_l2(gg, gg64)}
+    assert errs["weights_fp16"] <= 5e-3 and errs["grid_fp16"] <= 5e-3, errs
+    assert errs["weights_f64"] <= 5e-2 and errs["grid_f64"] <= 1e-1, errs
+    big = np.abs(gw16) > 1e-2 * np.abs(gw16).max()
+    close = np.abs(gw[big] - gw16[big]) <= 2e-2 * np.abs(gw16[big])
+    assert close.mean() >= 0.99, (close.mean(), errs)
+    # a second call gives the same gradients up to the order of the FP32 atomics
+    loss2, gw2, _ = _gradients(ctx, q, t)
+    assert _rel_l2(gw2, gw) <= 1e-5 and abs(loss2 - loss) <= 1e-5 * loss
 
 
 def test_queries_match_the_reference(gpu_context):

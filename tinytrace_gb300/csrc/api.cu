@@ -654,6 +654,26 @@ static void cache_train_after_frame(tt_context* ctx, const WfParams& w) {
     }
 }
 
+// The context's per-launch timer for the next render when TT_OPTION_STAGE_TIMING is on (its
+// events are created on first use), else null; either way the previous render's record is
+// dropped (count -1: the last render was not timed per stage).
+static StageTimer* begin_stage_timing(tt_context* ctx) {
+    StageTimer* timer = nullptr;
+    if (ctx->stage_timing) {
+        if (ctx->stage_events.empty()) {
+            ctx->stage_events.resize(2 * StageTimer::MAX_LAUNCHES);
+            for (auto& ev : ctx->stage_events) check_cuda(cudaEventCreate(&ev), "event");
+        }
+        timer = &ctx->stage_timer;
+        timer->events = ctx->stage_events.data();
+        timer->count = 0;
+        timer->overflow = false;
+        timer->open = false;
+    }
+    ctx->stage_timer.count = timer ? 0 : -1;
+    return timer;
+}
+
 static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c, tt_handle target, bool counted,
                         tt_traversal_counters* out) {
     require(ctx && c, "null argument");
@@ -678,19 +698,7 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     if (!s->dev.textured) w.ndc_mip = nullptr;
     bool cached = wavefront && ctx->cache.enabled && !counted;
     if (cached) cache_frame_buffers(ctx, *c, s->dev, w);
-    StageTimer* timer = nullptr;
-    if (ctx->stage_timing) {
-        if (ctx->stage_events.empty()) {
-            ctx->stage_events.resize(2 * StageTimer::MAX_LAUNCHES);
-            for (auto& ev : ctx->stage_events) check_cuda(cudaEventCreate(&ev), "event");
-        }
-        timer = &ctx->stage_timer;
-        timer->events = ctx->stage_events.data();
-        timer->count = 0;
-        timer->overflow = false;
-        timer->open = false;
-    }
-    ctx->stage_timer.count = timer ? 0 : -1;  // -1: the last render was not timed per stage
+    StageTimer* timer = begin_stage_timing(ctx);
     check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
     if (wavefront && ctx->graphs && !timer) {
         for (auto& cs : ctx->capture)
@@ -706,7 +714,11 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     check_cuda(cudaGetLastError(), "integrate launch");
     check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
     ctx->integrate_timed = true;
-    if (cached) cache_train_after_frame(ctx, w);
+    if (cached) {
+        stage_begin(timer, TT_STAGE_CACHE_TRAIN, ctx->stream);
+        cache_train_after_frame(ctx, w);
+        stage_end(timer, ctx->stream);
+    }
     fetch_error_word(ctx);
     if (counted) {
         unsigned long long h[8];
@@ -1293,8 +1305,9 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         rp.m_cap = R.config.temporal_m_cap * (float)R.config.candidates;
         rp.radius = R.config.spatial_radius;
         arm_error_word(ctx);
+        StageTimer* timer = begin_stage_timing(ctx);
         check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
-        render_restir(p, rp, ctx->stream);
+        render_restir(p, rp, ctx->stream, timer);
         check_cuda(cudaGetLastError(), "restir launch");
         check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");
         ctx->integrate_timed = true;
@@ -1366,6 +1379,35 @@ int32_t tt_cache_train(tt_context* ctx, const float* queries, const float* targe
         fetch_error_word(ctx);
         sync(ctx);
         if (loss) check_cuda(cudaMemcpy(loss, C.loss.ptr, 4, cudaMemcpyDeviceToHost), "loss");
+    });
+}
+
+int32_t tt_cache_gradients(tt_context* ctx, const float* queries, const float* targets, uint32_t n,
+                           float* weight_gradients, float* grid_gradients, float* loss) {
+    return guarded([&] {
+        require(ctx && weight_gradients && (n == 0 || (queries && targets)), "null argument");
+        use_device(ctx);
+        cache_ready(ctx);
+        CacheState& C = ctx->cache;
+        CacheDevice d = C.dev();
+        arm_error_word(ctx);
+        cache_clear_gradients(d, ctx->stream);
+        check_cuda(cudaMemsetAsync(C.loss.ptr, 0, 4, ctx->stream), "memset");
+        batch(ctx, queries, 48ull * n, targets, 12ull * n, nullptr, 0, [&](void* din, void* dex, void*) {
+            cache_gradients(d, static_cast<const CacheQuery*>(din), static_cast<const float*>(dex), n,
+                            ctx->err_word.as<uint32_t>(), ctx->stream);
+        });
+        fetch_error_word(ctx);
+        check_cuda(cudaMemcpyAsync(weight_gradients, C.w_grad.ptr, 4 * CACHE_PARAMS, cudaMemcpyDeviceToHost,
+                                   ctx->stream), "weight gradients");
+        if (grid_gradients)
+            check_cuda(cudaMemcpyAsync(grid_gradients, C.grid_grad.ptr, 4 * CACHE_GRID_PARAMS, cudaMemcpyDeviceToHost,
+                                       ctx->stream), "grid gradients");
+        float summed = 0.0f;
+        check_cuda(cudaMemcpyAsync(&summed, C.loss.ptr, 4, cudaMemcpyDeviceToHost, ctx->stream), "loss");
+        cache_clear_gradients(d, ctx->stream);  // the next training step starts from zero gradients
+        sync(ctx);
+        if (loss) *loss = summed;
     });
 }
 

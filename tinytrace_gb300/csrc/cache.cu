@@ -652,9 +652,11 @@ void cache_targets(const TrainRecord* rec, const uint32_t* rec_count, uint32_t c
     cache_targets_kernel<<<(cap + 255) / 256, 256, 0, st>>>(rec, rec_count, cap, final_radiance, q, t, count);
 }
 
-void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
-                      uint32_t step, uint32_t* err, cudaStream_t st) {
-    if (n == 0) return;
+// The training kernel's gradient pass: accumulates the gradients of the mean relative L2 loss
+// of n pairs into d.w_grad / d.grid_grad (which must start at zero) and the summed loss into
+// d.loss.
+static void cache_gradient_pass(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n,
+                                uint32_t* err, cudaStream_t st) {
     static bool attr[64] = {};  // per device: the shared-memory opt-in is a per-device function attribute
     int dev = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
@@ -668,6 +670,23 @@ void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* ta
     check_cuda(cudaMemsetAsync(d.loss, 0, 4, st), "memset");
     cache_train_tc_kernel<<<blocks, TC_THREADS, TT_SMEM, st>>>(q, target, n, d.grid, d.w16, d.w_grad, d.grid_grad,
                                                                d.loss, 1.0f / (3.0f * (float)n), err);
+}
+
+void cache_gradients(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, uint32_t* err,
+                     cudaStream_t st) {
+    if (n == 0) return;
+    cache_gradient_pass(d, q, target, n, err, st);
+}
+
+void cache_clear_gradients(const CacheDevice& d, cudaStream_t st) {
+    check_cuda(cudaMemsetAsync(d.grid_grad, 0, 4 * CACHE_GRID_PARAMS, st), "memset");
+    check_cuda(cudaMemsetAsync(d.w_grad, 0, 4 * CACHE_PARAMS, st), "memset");
+}
+
+void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
+                      uint32_t step, uint32_t* err, cudaStream_t st) {
+    if (n == 0) return;
+    cache_gradient_pass(d, q, target, n, err, st);
     float c1 = 1.0f - std::pow(0.9f, (float)step), c2 = 1.0f - std::pow(0.99f, (float)step);
     cache_adam_kernel<<<(CACHE_PARAMS + 255) / 256, 256, 0, st>>>(d.w, d.w_m, d.w_v, d.w_grad, d.w16, CACHE_PARAMS,
                                                                   lr, c1, c2);

@@ -304,21 +304,31 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
 }
 
 template <bool TEX>
-static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {
+static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer) {
     const tt_constants& c = p.c;
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
+    stage_begin(timer, TT_STAGE_RESTIR_GBUFFER, st);
     restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob);
+    stage_end(timer, st);
+    stage_begin(timer, TT_STAGE_RESTIR_INITIAL, st);
     restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
+    stage_end(timer, st);
+    stage_begin(timer, TT_STAGE_RESTIR_TEMPORAL, st);
     restir_temporal_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.glob, rp.prev_gbuf,
                                                            rp.initial, rp.prev, rp.temporal, rp.m_cap);
+    stage_end(timer, st);
+    stage_begin(timer, TT_STAGE_RESTIR_SPATIAL, st);
     restir_spatial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.temporal, rp.final_out,
                                                           rp.neighbours, rp.radius);
+    stage_end(timer, st);
+    stage_begin(timer, TT_STAGE_RESTIR_SHADE, st);
     restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
+    stage_end(timer, st);
 }
 
-void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st) {
-    if (p.sc.textured && rp.gtex) restir_passes<true>(p, rp, st);
-    else restir_passes<false>(p, rp, st);
+void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer) {
+    if (p.sc.textured && rp.gtex) restir_passes<true>(p, rp, st, timer);
+    else restir_passes<false>(p, rp, st, timer);
 }
 
 }  // namespace tt

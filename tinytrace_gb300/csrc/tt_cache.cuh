@@ -39,6 +39,12 @@ void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* o
 // One Adam step on n samples: gradients of the mean relative L2 loss.
 void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, float lr,
                       uint32_t step, uint32_t* err, cudaStream_t st);
+// The gradients of one training step without the Adam update: d.w_grad / d.grid_grad receive
+// the gradients of the mean relative L2 loss of the n pairs (they must start at zero; Adam
+// consumes them, cache_clear_gradients zeroes them), d.loss the summed loss.
+void cache_gradients(const CacheDevice& d, const CacheQuery* q, const float* target, uint32_t n, uint32_t* err,
+                     cudaStream_t st);
+void cache_clear_gradients(const CacheDevice& d, cudaStream_t st);
 void cache_init(const CacheDevice& d, uint32_t seed, cudaStream_t st);
 // Queries whose count is in device memory (at most max_n of them).
 void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,

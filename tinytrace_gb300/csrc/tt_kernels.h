@@ -126,7 +126,7 @@ struct RestirParams {
     uint32_t candidates, neighbours;
     float m_cap, radius;
 };
-void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st);
+void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer);
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out,
                     cudaStream_t st);
 void launch_bsdf_eval(const tt_material_constants* m, const float4* samples, uint32_t n,

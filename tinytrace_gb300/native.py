@@ -74,8 +74,15 @@ TT_STAGE_SHADE = 2
 TT_STAGE_SHADOW = 3
 TT_STAGE_REDUCE = 4
 TT_STAGE_MEGAKERNEL = 5
-TT_STAGE_COUNT = 8
-STAGE_NAMES = ("regen", "extend", "shade", "shadow", "reduce", "megakernel", "cache")
+TT_STAGE_RESTIR_GBUFFER = 8
+TT_STAGE_RESTIR_INITIAL = 9
+TT_STAGE_RESTIR_TEMPORAL = 10
+TT_STAGE_RESTIR_SPATIAL = 11
+TT_STAGE_RESTIR_SHADE = 12
+TT_STAGE_COUNT = 16
+TT_STAGE_CACHE_TRAIN = 7
+STAGE_NAMES = ("regen", "extend", "shade", "shadow", "reduce", "megakernel", "cache", "cache_train",
+               "restir_gbuffer", "restir_initial", "restir_temporal", "restir_spatial", "restir_shade")
 
 # ---------------------------------------------------------------- byte layouts (numpy)
 MATERIAL_CONSTANT_FIELDS = [
@@ -198,7 +205,8 @@ class SceneStats(ctypes.Structure):
 
 
 class StageTimings(ctypes.Structure):
-    _fields_ = [("ns", ctypes.c_uint64 * 8), ("launches", ctypes.c_uint64 * 8), ("overflow", ctypes.c_uint64)]
+    _fields_ = [("ns", ctypes.c_uint64 * TT_STAGE_COUNT), ("launches", ctypes.c_uint64 * TT_STAGE_COUNT),
+                ("overflow", ctypes.c_uint64)]
 
 
 class RestirConfig(ctypes.Structure):
@@ -270,6 +278,7 @@ SIGNATURES = {
     "tt_cache_query": (_I32, [_P, _P, _U32, _P]),
     "tt_cache_train": (_I32, [_P, _P, _P, _U32, _P]),
     "tt_cache_parameters": (_I32, [_P, _P, _P]),
+    "tt_cache_gradients": (_I32, [_P, _P, _P, ctypes.c_uint32, _P, _P, _P]),
     "tt_cache_status_get": (_I32, [_P, ctypes.POINTER(CacheStatus)]),
     "tt_restir_configure": (_I32, [_P, ctypes.POINTER(RestirConfig)]),
     "tt_restir_reset": (_I32, [_P]),
