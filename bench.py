@@ -64,10 +64,12 @@ def parse_args():
     p.add_argument("--no-textured", action="store_true", help="skip the textured-materials sample")
     p.add_argument("--no-ingest", action="store_true", help="skip the device mesh-ingest sample")
     p.add_argument("--no-light-selection", action="store_true", help="skip the light-selection sample")
-    p.add_argument("--serve-rates", default="2,8,32", help="Poisson arrival rates (requests/s) of the serving sample")
-    p.add_argument("--serve-requests", type=int, default=12, help="requests per arrival rate")
-    p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level"],
-                   help="acceleration structure (auto = flat up to 2^26 instanced triangles)")
+    p.add_argument("--serve-batch", type=int, default=64, help="requests of the serving sample's capacity run")
+    p.add_argument("--serve-requests", type=int, default=512,
+                   help="requests at 0.8 x capacity in the serving sample (a quarter as many at 0.5 x and 1.1 x)")
+    p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level", "wide"],
+                   help="acceleration structure (auto = flat up to 2^26 instanced triangles; wide = the flat BVH "
+                        "in the compressed 8-wide format)")
     return p.parse_args()
 
 
@@ -205,6 +207,7 @@ def l2_copy_gbs(device: int) -> dict:
 # traced ray reads its origin and direction (32 bytes) and writes its result (hit record or
 # radiance update, counted as 32 bytes).
 NODE_BYTES = 128
+WIDE_NODE_BYTES = 80  # compressed 8-wide node (TT_ACCEL_FLAT_WIDE)
 TRI_RECORD_BYTES = 48
 INSTANCE_RAY_BYTES = 64
 RAY_STATE_BYTES = 64
@@ -513,17 +516,41 @@ def run_restir(a, device: int, sm_mhz: float | None) -> dict:
 
 
 # ---------------------------------------------------------------- radiance-cache sample
+CACHE_SPP = (1, 2, 4, 8, 16, 32, 64)
+
+
+def time_at_error(points: list[dict], target: float) -> tuple[float | None, str]:
+    """Time at which an error-vs-time curve (points sorted by time, keys `ms` and `error`) reaches
+    `target`, interpolated linearly in log(time) against log(error) between the two points that
+    bracket it; (time of the cheapest point, "below") when the cheapest point is already below the
+    target, (None, "floor") when no point reaches it."""
+    pts = sorted(points, key=lambda p: p["ms"])
+    if pts[0]["error"] <= target:
+        return pts[0]["ms"], "below"
+    for p0, p1 in zip(pts, pts[1:]):
+        if p0["error"] >= target >= p1["error"]:
+            if p0["error"] == p1["error"]:
+                return p1["ms"], "interpolated"
+            f = np.log(target / p0["error"]) / np.log(p1["error"] / p0["error"])
+            return float(np.exp(np.log(p0["ms"]) + f * (np.log(p1["ms"]) - np.log(p0["ms"])))), "interpolated"
+    return None, "floor"
+
+
 def run_cache(a, device: int) -> dict:
     """Equal-error comparison of the learned radiance cache with the plain path tracer at
-    1920x1080, depth 8, on two scenes: the textured Cornell box (closed: every path bounces to
-    full depth) and the benchmark field (open, heavy-tailed lights).  Reference: the mean of 4
-    renders of 1024 spp.  Plain and cached frames at S spp (4 of each, different seeds) are
-    timed by CUDA events around the whole render call (for the cache: queries, training-pair
-    building and the Adam steps after the frame) and compared with the reference by the MSE of
-    x / (1 + x) tonemapped images (robust to fireflies) and by the plain MSE; equal-error
-    speed-up = (t_plain e_plain) / (t_cached e_cached).  The cache (path-spread rule c = 0.01
-    from the second vertex, 65,536 training paths, learning rate 1e-2) trains online for 128
-    frames of 4 spp before it is measured."""
+    1920x1080, depth 8, on the benchmark field (the 1M-triangle scene of the headline, open: most
+    camera paths end in the sky after one bounce) and on the textured Cornell box (closed).
+    Reference: the mean of 4 plain renders of 1024 spp.  Both arms render frames of 1, 2, 4, 8,
+    16, 32 and 64 spp, 4 frames each with their own seeds (frame index); each frame's device time
+    covers the whole render call (for the cache: its queries, the training pairs and the Adam
+    steps after the frame).  Error = the mean over pixels and channels of the squared difference
+    of tonemapped images, x / (1 + x): bounded per pixel, so that the fireflies of the log-normal
+    lights do not decide the comparison (the plain MSE is reported too).  Equal-error speed-up =
+    the plain arm's 16-spp time over the time at which the cached arm's error-vs-time curve
+    reaches the plain 16-spp error (log-log interpolation between its bracketing points).  The
+    cache (C5 configuration: learning rate 1e-2, 65,536 training paths per frame, paths end at the
+    first vertex after the primary hit whose path spread exceeds 0.01 of the primary's) trains
+    online for 128 frames of 4 spp before its curve is measured."""
     import ctypes
 
     from tinytrace_gb300 import native, scenes
@@ -531,12 +558,16 @@ def run_cache(a, device: int) -> dict:
     from tinytrace_gb300.renderer import Config, Renderer
 
     W, H, depth = a.width, a.height, a.depth
-    out = {"reference_spp": 4096, "config": {"learning_rate": 1e-2, "train_paths_per_frame": 65536,
-                                             "terminate_depth": 1, "spread_threshold": 0.01},
-           "warmup_frames": 128, "frames_averaged": 4, "scenes": {}}
-    cases = [("textured_cornell", scenes.textured_cornell(),
-              scenes.Camera.looking_at((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), fov=0.75)),
-             ("icosphere_field", make_workload(a).scene, make_workload(a).camera)]
+    cfg_c5 = (1e-2, 65536, 1, 1, 0.01)
+    out = {"reference_spp": 4096, "spp": list(CACHE_SPP), "frames_per_point": 4,
+           "error": "tonemapped MSE: mean of (x/(1+x) - ref/(1+ref))^2 over pixels and RGB",
+           "config": {"learning_rate": cfg_c5[0], "train_paths_per_frame": cfg_c5[1], "terminate_depth": cfg_c5[2],
+                      "spread_threshold": cfg_c5[4]},
+           "warmup_frames": 128, "scenes": {}}
+    w = make_workload(a)
+    cases = [("icosphere_field", w.scene, w.camera),
+             ("textured_cornell", scenes.textured_cornell(),
+              scenes.Camera.looking_at((0.0, 1.0, 3.4), (0.0, 1.0, 0.0), fov=0.75))]
     for name, scene, camera in cases:
         r = Renderer((W, H), device=device)
         r.set_scene(scene)
@@ -561,33 +592,47 @@ def run_cache(a, device: int) -> dict:
             ref += frame(1024)[0] / 4.0
         tref = ref / (1.0 + ref)
 
-        def errors(spp):
-            ms = tm = mse = 0.0
-            for _ in range(4):
-                img, t = frame(spp)
-                ms += t / 4.0
-                tm += float(np.mean((img / (1.0 + img) - tref) ** 2)) / 4.0
-                mse += float(np.mean((img - ref) ** 2)) / 4.0
-            return ms, tm, mse
+        def curve():
+            pts = []
+            for spp in CACHE_SPP:
+                ms = err = mse = 0.0
+                for _ in range(4):
+                    img, t = frame(spp)
+                    ms += t / 4.0
+                    err += float(np.mean((img / (1.0 + img) - tref) ** 2)) / 4.0
+                    mse += float(np.mean((img - ref) ** 2)) / 4.0
+                pts.append({"spp": spp, "ms": ms, "error": err, "mse": mse})
+            return pts
 
-        plain = {spp: errors(spp) for spp in (4, 16)}
-        cfg = native.CacheConfig(1e-2, 65536, 1, 1, 0.01)
+        plain = curve()
+        cfg = native.CacheConfig(*cfg_c5)
         check(lib.tt_cache_configure(ctx, ctypes.byref(cfg)))
         check(lib.tt_set_option(ctx, native.TT_OPTION_RADIANCE_CACHE, 1))
         for _ in range(128):
             frame(4)
-        rows = []
-        for spp in (4, 16):
-            ms, tm, mse = errors(spp)
-            pms, ptm, pmse = plain[spp]
-            rows.append({"spp": spp, "plain_ms": pms, "cached_ms": ms, "plain_tonemapped_mse": ptm,
-                         "cached_tonemapped_mse": tm, "plain_mse": pmse, "cached_mse": mse,
-                         "equal_error_speedup_tonemapped": (pms * ptm) / (ms * tm),
-                         "equal_error_speedup_mse": (pms * pmse) / (ms * mse)})
+        cached = curve()
+        # cost breakdown of one cached 16-spp frame (host-driven loop, CUDA events per launch)
+        check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 1))
+        frame(16)
+        stt = native.StageTimings()
+        check(lib.tt_stage_timings_get(ctx, ctypes.byref(stt)))
+        check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 0))
+        breakdown = {n: stt.ns[i] / 1e6 for i, n in enumerate(native.STAGE_NAMES) if stt.launches[i]}
         st = native.CacheStatus()
         check(lib.tt_cache_status_get(ctx, ctypes.byref(st)))
-        out["scenes"][name] = {"results": rows, "training": {"steps": int(st.steps), "pairs_last_frame": int(st.pairs),
-                                                             "last_loss": st.last_loss}}
+        p16 = next(p for p in plain if p["spp"] == 16)
+        c16 = next(p for p in cached if p["spp"] == 16)
+        t_cached, how = time_at_error(cached, p16["error"])
+        t_plain, how_p = time_at_error(plain, c16["error"])
+        out["scenes"][name] = {
+            "plain": plain, "cached": cached,
+            "target_error": p16["error"], "plain_ms_at_target": p16["ms"],
+            "cached_ms_at_target": t_cached, "cached_reaches_target": how,
+            "equal_rmse_speedup": p16["ms"] / t_cached if t_cached else None,
+            "plain_ms_at_cached_16spp_error": t_plain, "plain_reaches_cached_16spp_error": how_p,
+            "equal_rmse_speedup_at_cached_16spp": t_plain / c16["ms"] if t_plain else None,
+            "cached_16spp_breakdown_ms": breakdown,
+            "training": {"steps": int(st.steps), "pairs_last_frame": int(st.pairs), "last_loss": st.last_loss}}
         r.close()
     return out
 
@@ -759,13 +804,74 @@ def run_ingest(a, device: int) -> dict:
 SERVE_SCENES = [(1, 7), (4, 11), (16, 18), (64, 28), (128, 44)]  # (instances, frequency): 1e3 .. 5e6 triangles
 
 
-def run_serving(a, ctx) -> dict:
-    """Continuous batching under Poisson arrivals: requests with resolution side ~U{256..2048},
-    spp ~U{1..256}, depth 8, on scenes whose triangle count is drawn log-uniformly in
-    [1e3, 5e6] (nearest of five generated sizes); all scenes resident, HBM budget 150 GB."""
+def serve_requests(rng, pool, logs, n: int, first_frame: int):
+    """n requests of the C4 mix: square resolution with side ~U{256..2048} (steps of 16), spp
+    ~U{1..256}, depth 8, scene size log-uniform in [1e3, 5e6] triangles (nearest resident scene)."""
     from tinytrace_gb300 import scenes
-    from tinytrace_gb300.renderer import Config, SceneArrays, make_constants
+    from tinytrace_gb300.renderer import Config, make_constants
+
+    cam = scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0))
+    reqs = []
+    for k in range(n):
+        side = int(rng.integers(16, 129)) * 16
+        spp = int(rng.integers(1, 257))
+        scene = pool[int(np.argmin(np.abs(logs - rng.uniform(3.0, np.log10(5e6)))))][1]
+        c = make_constants(cam, (side, side), Config(bounce_count=8, sample_count=spp), first_frame + k, 0)
+        reqs.append((scene, c, side * side * spp))
+    return reqs
+
+
+def serve_run(ctx, reqs, rate: float | None, rng) -> dict:
+    """Submits `reqs` (Poisson arrivals at `rate` per second, or all at once when rate is None),
+    waits for all of them and returns latency percentiles and throughput.  Finished requests'
+    image buffers are released as the run goes."""
     from tinytrace_gb300.server import RenderServer
+
+    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=8) as srv:
+        t0 = time.perf_counter()
+        due = t0
+        ids, pending = [], []
+        gaps = rng.exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
+        for (scene, c, _), gap in zip(reqs, gaps):
+            due += gap
+            time.sleep(max(0.0, due - time.perf_counter()))
+            rid = srv.submit(scene, c)
+            ids.append(rid)
+            pending.append(rid)
+            still = []
+            for q in pending:
+                if srv.status(q)[0] >= 2:
+                    srv.release(q)
+                else:
+                    still.append(q)
+            pending = still
+        submit_end = time.perf_counter()
+        for q in ids:
+            srv.wait(q)
+            srv.release(q)
+        makespan = time.perf_counter() - t0
+        lat = np.array([srv.status(q)[1] for q in ids])
+        st = srv.stats()
+    samples = sum(n for _, _, n in reqs)
+    tenth = max(1, len(lat) // 10)
+    return {"requests": len(reqs), "arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()), "max_ms": float(lat.max()),
+            "first_tenth_mean_ms": float(lat[:tenth].mean()), "last_tenth_mean_ms": float(lat[-tenth:].mean()),
+            "completed_per_s": len(ids) / makespan, "offered_per_s": len(ids) / (submit_end - t0) if rate else None,
+            "throughput_msamples_s": samples / makespan / 1e6, "peak_inflight": int(st.peak_inflight),
+            "failed": int(st.failed), "makespan_s": makespan}
+
+
+def run_serving(a, ctx) -> dict:
+    """Continuous batching under the C4 request mix on five resident scenes (1e3 .. 5e6
+    triangles), HBM budget 150 GB, 8 execution slots.  First the server's capacity: a batch of
+    a.serve_batch requests submitted at once (completions per second over the makespan).  Then
+    Poisson arrivals at fractions of that capacity: a.serve_requests requests at 0.8 x capacity and
+    a quarter as many at 0.5 x and 1.1 x; a rate is sustained when its completions keep pace with
+    its arrivals (completed per second >= 0.95 x offered) and the latency does not grow over the
+    run (mean latency of the last tenth of the requests <= 1.5 x that of the first tenth)."""
+    from tinytrace_gb300 import scenes
+    from tinytrace_gb300.renderer import SceneArrays
 
     rng = np.random.default_rng(2024)
     pool = []
@@ -773,38 +879,29 @@ def run_serving(a, ctx) -> dict:
         arr = SceneArrays(scenes.icosphere_field(instances=inst, freq=freq, lights=max(4, min(1000, 16 * inst)),
                                                  seed=100 + inst))
         pool.append((arr.triangle_count, ctx.create_scene(arr)))
-    cam = scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0))
     logs = np.log10([t for t, _ in pool])
-    out = {"requests_per_rate": a.serve_requests, "scenes_triangles": [int(t) for t, _ in pool],
-           "hbm_budget_gb": 150, "max_inflight": 8, "rates": []}
-    for rate in [float(x) for x in a.serve_rates.split(",")]:
-        reqs = []
-        for k in range(a.serve_requests):
-            side = int(rng.integers(16, 129)) * 16
-            spp = int(rng.integers(1, 257))
-            scene = pool[int(np.argmin(np.abs(logs - rng.uniform(3.0, np.log10(5e6)))))][1]
-            c = make_constants(cam, (side, side), Config(bounce_count=8, sample_count=spp), k, 0)
-            reqs.append((scene, c, side * side * spp))
-        gaps = rng.exponential(1.0 / rate, len(reqs))
-        with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=8) as srv:
-            t0 = time.perf_counter()
-            ids = []
-            due = t0
-            for (scene, c, _), gap in zip(reqs, gaps):
-                due += gap
-                time.sleep(max(0.0, due - time.perf_counter()))
-                ids.append(srv.submit(scene, c))
-            for i in ids:
-                srv.wait(i)
-            makespan = time.perf_counter() - t0
-            lat = np.array([srv.status(i)[1] for i in ids])
-            st = srv.stats()
-        samples = sum(n for _, _, n in reqs)
-        out["rates"].append({"arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50)),
-                             "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-                             "throughput_msamples_s": samples / makespan / 1e6,
-                             "completed_per_s": len(ids) / makespan, "peak_inflight": int(st.peak_inflight),
-                             "failed": int(st.failed)})
+    out = {"scenes_triangles": [int(t) for t, _ in pool], "hbm_budget_gb": 150, "max_inflight": 8,
+           "mix": "side ~U{256..2048} step 16, spp ~U{1..256}, depth 8, scene log-uniform 1e3..5e6 triangles"}
+    serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng)  # warm-up: graphs, pool, caches
+    cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng)
+    mu = cap["completed_per_s"]
+    out["capacity"] = cap
+    out["capacity_per_s"] = mu
+    out["rates"] = []
+    frame = 10_000
+    for frac, n in ((0.5, max(32, a.serve_requests // 4)), (0.8, a.serve_requests), (1.1, max(32, a.serve_requests // 4))):
+        res = serve_run(ctx, serve_requests(rng, pool, logs, n, frame), frac * mu, rng)
+        frame += n
+        res["fraction_of_capacity"] = frac
+        res["sustained"] = bool(res["completed_per_s"] >= 0.95 * res["offered_per_s"]
+                                and res["last_tenth_mean_ms"] <= 1.5 * res["first_tenth_mean_ms"])
+        out["rates"].append(res)
+    sustained = [r for r in out["rates"] if r["sustained"]]
+    best = max(sustained, key=lambda r: r["arrival_rate_per_s"]) if sustained else None
+    out["sustainable_rate_per_s"] = best["arrival_rate_per_s"] if best else None
+    out["p50_ms_at_sustainable_rate"] = best["p50_ms"] if best else None
+    out["p99_ms_at_sustainable_rate"] = best["p99_ms"] if best else None
+    out["requests_at_sustainable_rate"] = best["requests"] if best else None
     return out
 
 
@@ -821,7 +918,8 @@ def run_ours(a, dist: Dist):
     integ = native.TT_INTEGRATOR_WAVEFRONT if a.integrator == "wavefront" else native.TT_INTEGRATOR_MEGAKERNEL
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_INTEGRATOR, integ))
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_WAVEFRONT_SLOTS, a.slots))
-    accel = {"auto": native.TT_ACCEL_AUTO, "flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL}
+    accel = {"auto": native.TT_ACCEL_AUTO, "flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL,
+             "wide": native.TT_ACCEL_FLAT_WIDE}
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_ACCEL, accel[a.accel]))
     r.set_scene(w.scene)
     r.camera = w.camera
@@ -912,7 +1010,8 @@ def run_ours(a, dist: Dist):
     cnt = native.TraversalCounters()
     c = r.constants()
     check(lib.tt_render_counted(ctx, r.scene, native.ptr(c), r.render_target, ctypes.byref(cnt)))
-    node_bytes = (cnt.blas_nodes + cnt.tlas_nodes) * NODE_BYTES
+    node_size = WIDE_NODE_BYTES if stats.accel == native.TT_ACCEL_FLAT_WIDE else NODE_BYTES
+    node_bytes = (cnt.blas_nodes + cnt.tlas_nodes) * node_size
     trace_bytes = (node_bytes + cnt.triangles * TRI_RECORD_BYTES + cnt.instances * INSTANCE_RAY_BYTES
                    + cnt.rays * RAY_STATE_BYTES)
     trace_stages = [native.TT_STAGE_EXTEND, native.TT_STAGE_SHADOW]
@@ -927,7 +1026,8 @@ def run_ours(a, dist: Dist):
         node_achieved = node_bytes / trace_s / 1e9
         rays_per_launch = cnt.rays / trace_launches
         default_workload = (W, H, spp, w.config.bounce_count) == (1920, 1080, 64, 8)
-        traffic = ncu_traffic_per_launch(rays_per_launch) if default_workload and a.accel != "two_level" else None
+        traffic = (ncu_traffic_per_launch(rays_per_launch)
+                   if default_workload and stats.accel == native.TT_ACCEL_FLAT else None)
     else:  # the megakernel does everything in one launch
         bytes_per_launch, launch_s = trace_bytes, kernel_s
         achieved = trace_bytes / kernel_s / 1e9
@@ -965,7 +1065,8 @@ def run_ours(a, dist: Dist):
                        "light_sampling": "next_event_estimation",
                        "l2": "flushed before every step (512 MiB memset, inside the timed region)",
                        "parallelism": f"replicas x{dist.world}", "integrator": a.integrator,
-                       "accel": "flat" if stats.accel == native.TT_ACCEL_FLAT else "two_level",
+                       "accel": {native.TT_ACCEL_FLAT: "flat", native.TT_ACCEL_FLAT_WIDE: "wide"}.get(
+                           int(stats.accel), "two_level"),
                        "autotune": tuning},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 368, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps},
@@ -975,7 +1076,7 @@ def run_ours(a, dist: Dist):
                          "kernel": "wf_trace_kernel" if trace_launches > 0 else "integrate_kernel",
                          "launches_per_step": trace_launches, "launch_ms": launch_s * 1e3,
                          "algorithmic_bytes_per_launch": bytes_per_launch, "rays_per_launch": rays_per_launch,
-                         "bytes_per_unit": {"node": NODE_BYTES, "triangle_record": TRI_RECORD_BYTES,
+                         "bytes_per_unit": {"node": node_size, "triangle_record": TRI_RECORD_BYTES,
                                             "instance_ray_setup": INSTANCE_RAY_BYTES, "ray_state": RAY_STATE_BYTES},
                          "node_fetch_gbs": node_achieved, "node_fetch_frac": node_achieved / peak,
                          "rays_per_frame": int(cnt.rays), "rays_per_sample": cnt.rays / samples_per_step,

@@ -87,6 +87,9 @@ extern "C" {
 #define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
 #define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */
 #define TT_ACCEL_TWO_LEVEL 2 /* per-mesh BLAS under a TLAS over instances */
+#define TT_ACCEL_FLAT_WIDE 3 /* the flat BVH in a compressed 8-wide format: 80-byte nodes with 8-bit child
+                                boxes relative to a per-node origin and power-of-two scales, children in
+                                slots by direction octant; rebuilt (not refitted) on instance updates */
 
 /* trace flags */
 #define TT_TRACE_CULL_BACK_FACES 1u
@@ -364,8 +367,8 @@ int32_t tt_emissive_extract(tt_context* ctx, const tt_emissive_source* source, t
                             uint64_t capacity, uint64_t* count);
 
 /* BVH arrays for node-for-node comparison: blas nodes (128 B each), triangle records
- * (48 B each), tlas nodes (128 B each; the flat BVH of a flat scene).  Sizes in bytes must
- * match tt_scene_stats. */
+ * (48 B each), tlas nodes (128 B each; the flat BVH of a flat scene, 80 B each in the
+ * compressed wide format).  Sizes in bytes must match tt_scene_stats. */
 int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint64_t blas_bytes,
                               void* tris, uint64_t tri_bytes, void* tlas, uint64_t tlas_bytes);
 

@@ -673,7 +673,8 @@ struct OracleSceneDesc {
 };
 
 // accel: 0 brute force, 1 two-level BVH, 2 flat BVH (the structure render() traces through;
-// both BVHs are built whenever accel != 0).
+// both BVHs are built whenever accel != 0), 3 the flat BVH plus its compressed 8-wide format
+// (render() traces through the flat BVH; the wide format is for comparison with the GPU build).
 void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
     OracleScene* s = new OracleScene();
     copy_in(s->positions, d->positions, d->position_count * 3u);
@@ -700,8 +701,9 @@ void* oracle_scene_create(const OracleSceneDesc* d, int accel, int leaf_max) {
     s->light_prim = r_light_prims(*s);
     s->light_alias = build_light_alias(*s);
     s->use_bvh = accel != 0;
-    s->flat = accel == 2;
+    s->flat = accel == 2 || accel == 3;
     if (s->use_bvh) s->bvh = build_scene_bvh(s->geom(), leaf_max);
+    if (accel == 3) build_wide_bvh(s->geom(), s->bvh);
     return s;
 }
 
@@ -715,7 +717,8 @@ void oracle_scene_set_light_exact(void* p, int exact) { static_cast<OracleScene*
 
 // BVH arrays for node-for-node comparison with the GPU build.
 void oracle_scene_bvh_info(void* p, uint64_t* out /* blas_nodes, tris, tlas_nodes, blas_levels, tlas_levels,
-                                                    flat_nodes, flat_tris, flat_levels */) {
+                                                    flat_nodes, flat_tris, flat_levels, wide_nodes,
+                                                    wide_tris, wide_levels */) {
     OracleScene* s = static_cast<OracleScene*>(p);
     out[0] = s->bvh.blas.size();
     out[1] = s->bvh.tris.size();
@@ -725,6 +728,14 @@ void oracle_scene_bvh_info(void* p, uint64_t* out /* blas_nodes, tris, tlas_node
     out[5] = s->bvh.flat.size();
     out[6] = s->bvh.flat_tris.size();
     out[7] = (uint64_t)s->bvh.flat_levels;
+    out[8] = s->bvh.wide.size();
+    out[9] = s->bvh.wide_tris.size();
+    out[10] = (uint64_t)s->bvh.wide_levels;
+}
+void oracle_scene_wide_copy(void* p, void* nodes, void* tris) {
+    OracleScene* s = static_cast<OracleScene*>(p);
+    if (nodes) std::memcpy(nodes, s->bvh.wide.data(), s->bvh.wide.size() * sizeof(Node8));
+    if (tris) std::memcpy(tris, s->bvh.wide_tris.data(), s->bvh.wide_tris.size() * sizeof(TriRecord));
 }
 void oracle_scene_flat_copy(void* p, void* nodes, void* tris) {
     OracleScene* s = static_cast<OracleScene*>(p);
@@ -740,7 +751,7 @@ void oracle_scene_bvh_copy(void* p, void* blas, void* tris, void* tlas) {
 
 // rays: n x 8 floats (origin xyz, tmin, direction xyz, tmax); hits: n x 8 words
 // (hit, t, u, v, instance, prim, 0, 0).  flags bit0 = cull back faces, bit1 = brute force,
-// bit2 = the flat BVH.
+// bit2 = the flat BVH, bit3 = the wide format of the flat BVH (scene created with accel 3).
 void oracle_trace_batch(void* p, const float* rays, uint32_t n, uint32_t flags, uint32_t* hits,
                         int threads) {
     OracleScene* s = static_cast<OracleScene*>(p);
@@ -754,6 +765,7 @@ void oracle_trace_batch(void* p, const float* rays, uint32_t n, uint32_t flags, 
         bool cull = flags & 1u;
         Geometry g = s->geom();
         Hit h = (flags & 2u) || !s->use_bvh ? trace_brute(g, o, d, r[3], r[7], cull)
+                : (flags & 8u)                  ? trace_wide(g, s->bvh, o, d, r[3], r[7], cull)
                 : (flags & 4u)                  ? trace_flat(g, s->bvh, o, d, r[3], r[7], cull)
                                                 : trace_bvh(g, s->bvh, o, d, r[3], r[7], cull);
         uint32_t* out = hits + 8 * i;
@@ -851,6 +863,7 @@ void oracle_scene_update_instances(void* p, const Instance* instances, uint32_t 
     if (count != s->instances.size()) return;
     std::memcpy(s->instances.data(), instances, sizeof(Instance) * count);
     if (s->use_bvh) refit_world_structures(s->geom(), s->bvh);
+    if (!s->bvh.wide.empty()) build_wide_bvh(s->geom(), s->bvh);  // quantised boxes: rebuilt, not refitted
     s->light_alias = build_light_alias(*s);
 }
 

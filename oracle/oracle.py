@@ -52,6 +52,7 @@ def load() -> ctypes.CDLL:
         lib.oracle_scene_bvh_info.argtypes = [_P, _P]
         lib.oracle_scene_bvh_copy.argtypes = [_P, _P, _P, _P]
         lib.oracle_scene_flat_copy.argtypes = [_P, _P, _P]
+        lib.oracle_scene_wide_copy.argtypes = [_P, _P, _P]
         lib.oracle_trace_batch.argtypes = [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_int]
         lib.oracle_render.argtypes = [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                       ctypes.c_uint32, ctypes.c_int]
@@ -83,9 +84,10 @@ def _p(a):
 class OracleScene:
     """CPU restatement of the scene (brute-force or LBVH ray queries)."""
 
-    def __init__(self, arrays, use_bvh: bool = True, leaf_max: int = 2, flat: bool = False):
+    def __init__(self, arrays, use_bvh: bool = True, leaf_max: int = 2, flat: bool = False, wide: bool = False):
         """use_bvh=False traces by brute force; otherwise render() traces through the
-        two-level BVH, or the flat one when `flat` (the hits are the same)."""
+        two-level BVH, or the flat one when `flat` (the hits are the same).  `wide` also builds
+        the compressed 8-wide format of the flat BVH (wide_bvh(), trace(..., wide=True))."""
         self.arrays = arrays  # keeps the borrowed arrays alive
         self._tex, ntex = _textures(arrays)
         d = OracleSceneDesc(_p(arrays.positions), len(arrays.positions), _p(arrays.indices), len(arrays.indices),
@@ -93,7 +95,8 @@ class OracleScene:
                             len(arrays.meshes), _p(arrays.meshes), _p(arrays.instances), len(arrays.instances),
                             len(arrays.emissive), _p(arrays.emissive), ctypes.addressof(self._tex), ntex, 0)
         self.lib = load()
-        self.handle = self.lib.oracle_scene_create(ctypes.byref(d), (2 if flat else 1) if use_bvh else 0, leaf_max)
+        accel = (3 if wide else (2 if flat else 1)) if use_bvh else 0
+        self.handle = self.lib.oracle_scene_create(ctypes.byref(d), accel, leaf_max)
 
     def __del__(self):
         try:
@@ -121,7 +124,7 @@ class OracleScene:
     def bvh(self):
         from tinytrace_gb300.native import NODE4_DTYPE, TRI_RECORD_DTYPE
 
-        info = np.zeros(8, np.uint64)
+        info = np.zeros(12, np.uint64)
         self.lib.oracle_scene_bvh_info(self.handle, _p(info))
         blas = np.zeros(int(info[0]), NODE4_DTYPE)
         tris = np.zeros(int(info[1]), TRI_RECORD_DTYPE)
@@ -132,12 +135,23 @@ class OracleScene:
     def flat_bvh(self):
         from tinytrace_gb300.native import NODE4_DTYPE, TRI_RECORD_DTYPE
 
-        info = np.zeros(8, np.uint64)
+        info = np.zeros(12, np.uint64)
         self.lib.oracle_scene_bvh_info(self.handle, _p(info))
         nodes = np.zeros(int(info[5]), NODE4_DTYPE)
         tris = np.zeros(int(info[6]), TRI_RECORD_DTYPE)
         self.lib.oracle_scene_flat_copy(self.handle, _p(nodes), _p(tris))
         return nodes, tris, int(info[7])
+
+    def wide_bvh(self):
+        """(80-byte wide nodes, triangle records in wide order, levels) of the flat structure."""
+        from tinytrace_gb300.native import NODE8_DTYPE, TRI_RECORD_DTYPE
+
+        info = np.zeros(12, np.uint64)
+        self.lib.oracle_scene_bvh_info(self.handle, _p(info))
+        nodes = np.zeros(int(info[8]), NODE8_DTYPE)
+        tris = np.zeros(int(info[9]), TRI_RECORD_DTYPE)
+        self.lib.oracle_scene_wide_copy(self.handle, _p(nodes), _p(tris))
+        return nodes, tris, int(info[10])
 
     def update_instances(self, instances: np.ndarray) -> None:
         """New instance transforms (the TLAS update); refits both world structures."""
@@ -145,10 +159,11 @@ class OracleScene:
         self.arrays.instances = inst
         self.lib.oracle_scene_update_instances(self.handle, _p(inst), len(inst))
 
-    def trace(self, rays: np.ndarray, cull: bool, brute: bool = False, threads: int = 0, flat: bool = False) -> np.ndarray:
+    def trace(self, rays: np.ndarray, cull: bool, brute: bool = False, threads: int = 0, flat: bool = False,
+              wide: bool = False) -> np.ndarray:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
         hits = np.zeros((len(rays), 8), np.uint32)
-        flags = (1 if cull else 0) | (2 if brute else 0) | (4 if flat else 0)
+        flags = (1 if cull else 0) | (2 if brute else 0) | (4 if flat else 0) | (8 if wide else 0)
         self.lib.oracle_trace_batch(self.handle, _p(rays), len(rays), flags, _p(hits), threads)
         return hits
 

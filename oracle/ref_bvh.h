@@ -138,13 +138,23 @@ inline void fill_node(Node4& nd, const Aabb* cbox, int count) {
     nd.count = (uint32_t)count;
 }
 
-// Build BVH4s over primitives grouped in segments (one BVH root per segment, node index =
-// segment index).  `segment` must be non-decreasing in primitive order.  `leaf_max` bounds
-// the primitives per leaf child; `leaf_by_prim` stores the primitive index instead of the
-// sorted position in leaf references (used for the instance level, where leaf_max == 1).
-inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<uint32_t>& segment,
-                           uint32_t segment_count, int leaf_max, bool leaf_by_prim) {
-    BvhBuild out;
+// Binary LBVH over primitives grouped in segments: Morton keys of the centroids normalised per
+// segment, stable sort, Karras hierarchy, exact bottom-up boxes; `roots` holds each segment's
+// root as a binary node reference (internal r < n - 1, leaf n - 1 + sorted position, -1 empty).
+struct BinaryBuild {
+    BinaryTree t;
+    std::vector<uint32_t> order;  // sorted position -> primitive index
+    std::vector<int> roots;
+    int ni = 0;
+    bool is_leaf(int r) const { return r >= ni; }
+    int nfirst(int r) const { return is_leaf(r) ? r - ni : t.first[r]; }
+    int ncount(int r) const { return is_leaf(r) ? 1 : t.last[r] - t.first[r] + 1; }
+    const Aabb& nbox(int r) const { return is_leaf(r) ? t.lbox[r - ni] : t.ibox[r]; }
+};
+
+inline BinaryBuild build_binary(const std::vector<Aabb>& prim_box, const std::vector<uint32_t>& segment,
+                                uint32_t segment_count) {
+    BinaryBuild out;
     const int n = (int)prim_box.size();
     // 1. centroid bounds per segment
     std::vector<Aabb> cb(segment_count, aabb_empty());
@@ -166,9 +176,10 @@ inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<
     std::vector<uint64_t> sk(n);
     for (int i = 0; i < n; ++i) sk[i] = key[order[i]];
     // 4. Karras hierarchy
-    BinaryTree t;
+    BinaryTree& t = out.t;
     t.n = n;
     int ni = n > 1 ? n - 1 : 0;
+    out.ni = ni;
     t.left.assign(ni, 0);
     t.right.assign(ni, 0);
     t.first.assign(ni, 0);
@@ -200,7 +211,6 @@ inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<
     t.lbox.resize(n);
     for (int i = 0; i < n; ++i) t.lbox[i] = prim_box[order[i]];
     t.ibox.assign(ni, aabb_empty());
-    std::vector<Aabb> memo(ni);
     std::vector<char> done(ni, 0);
     // iterative post-order
     {
@@ -220,22 +230,36 @@ inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<
             done[v] = 1;
         }
     }
-    auto is_leaf = [&](int r) { return r >= ni; };
-    auto nfirst = [&](int r) { return is_leaf(r) ? r - ni : t.first[r]; };
-    auto ncount = [&](int r) { return is_leaf(r) ? 1 : t.last[r] - t.first[r] + 1; };
-    auto nbox = [&](int r) { return is_leaf(r) ? t.lbox[r - ni] : t.ibox[r]; };
     // 6. segment roots: the node whose range equals the segment's sorted range
     std::vector<int> seg_first(segment_count, 0), seg_count(segment_count, 0);
     for (int i = 0; i < n; ++i) seg_count[segment[i]]++;
     for (uint32_t s = 1; s < segment_count; ++s) seg_first[s] = seg_first[s - 1] + seg_count[s - 1];
-    std::vector<int> level;  // binary node refs of the current BVH4 level (-1 = empty)
     for (uint32_t s = 0; s < segment_count; ++s) {
         int a = seg_first[s], b = a + seg_count[s] - 1;
-        if (seg_count[s] == 0) level.push_back(-1);
-        else if (seg_count[s] == 1) level.push_back(ni + a);
-        else if (t.first[a] == a && t.last[a] == b) level.push_back(a);
-        else level.push_back(b);
+        if (seg_count[s] == 0) out.roots.push_back(-1);
+        else if (seg_count[s] == 1) out.roots.push_back(ni + a);
+        else if (t.first[a] == a && t.last[a] == b) out.roots.push_back(a);
+        else out.roots.push_back(b);
     }
+    out.order = std::move(order);
+    return out;
+}
+
+// Build BVH4s over primitives grouped in segments (one BVH root per segment, node index =
+// segment index).  `segment` must be non-decreasing in primitive order.  `leaf_max` bounds
+// the primitives per leaf child; `leaf_by_prim` stores the primitive index instead of the
+// sorted position in leaf references (used for the instance level, where leaf_max == 1).
+inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<uint32_t>& segment,
+                           uint32_t segment_count, int leaf_max, bool leaf_by_prim) {
+    BvhBuild out;
+    BinaryBuild bb = build_binary(prim_box, segment, segment_count);
+    const BinaryTree& t = bb.t;
+    const std::vector<uint32_t>& order = bb.order;
+    auto is_leaf = [&](int r) { return bb.is_leaf(r); };
+    auto nfirst = [&](int r) { return bb.nfirst(r); };
+    auto ncount = [&](int r) { return bb.ncount(r); };
+    auto nbox = [&](int r) { return bb.nbox(r); };
+    std::vector<int> level = bb.roots;  // binary node refs of the current BVH4 level (-1 = empty)
     // 7. collapse to BVH4, level by level
     while (!level.empty()) {
         out.levels++;
@@ -296,6 +320,197 @@ inline BvhBuild build_bvh4(const std::vector<Aabb>& prim_box, const std::vector<
         level.swap(next);
     }
     out.order = order;
+    return out;
+}
+
+// ---------------------------------------------------------------- compressed 8-wide node (80 bytes)
+// A node of the flat structure's wide format (after the compressed wide BVHs of Ylitie, Karras &
+// Laine, HPG 2017): up to eight children whose boxes are quantised to 8 bits per plane relative
+// to the node's origin (its box's low corner) with one power-of-two scale per axis,
+//   plane = origin[a] + q * 2^(exponent[a] - 127),  q in 0..255,
+// rounded outwards (low planes down, high planes up), so that a decoded child box contains the
+// child's exact box.  Internal children are stored contiguously from `child_base` in slot order
+// (child of slot s: child_base + number of internal slots below s); the triangle records of the
+// leaf children are stored contiguously from `tri_base`, each leaf slot naming its first record
+// (meta bits 0..4, offset from tri_base) and its 1..3 records as a unary count (meta bits 5..7).
+// Children occupy slots by direction: slot s preferably holds the child lying farthest towards
+// the octant whose axis a is negative when bit a of s is set, so a ray whose direction has sign
+// bits o reaches the children roughly nearest first when it visits slots o ^ 0, o ^ 1, ... o ^ 7.
+struct Node8 {
+    float origin[3];
+    uint8_t exponent[3];  // biased exponents of the per-axis scales
+    uint8_t imask;        // bit s: slot s holds an internal child
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t meta[8];
+    uint8_t qlo_x[8], qhi_x[8], qlo_y[8], qhi_y[8], qlo_z[8], qhi_z[8];
+};
+static_assert(sizeof(Node8) == 80, "Node8 is 80 bytes");
+constexpr int WIDE_LEAF_MAX = 3;  // records per leaf child
+
+// Biased exponent e (scale 2^(e - 127), e in 1..254) of the smallest power-of-two scale whose 255
+// steps cover `extent`.
+inline uint8_t wide_exponent(float extent) {
+    float x = extent / 255.0f;
+    uint32_t bits = fbits(x);
+    uint32_t e = (bits >> 23) & 0xffu;
+    if (e == 0u) e = 1u;                               // zero or subnormal: the smallest normal scale
+    else if ((bits & 0x7fffffu) != 0u) e += 1u;        // round x up to a power of two
+    while (e < 254u && 255.0f * bitsf(e << 23) < extent) e += 1u;
+    return (uint8_t)(e > 254u ? 254u : e);
+}
+inline uint8_t wide_quantize_lo(float v, float origin, float scale) {
+    float q = std::floor((v - origin) / scale);
+    return (uint8_t)(q < 0.0f ? 0.0f : (q > 255.0f ? 255.0f : q));
+}
+inline uint8_t wide_quantize_hi(float v, float origin, float scale) {
+    float q = std::ceil((v - origin) / scale);
+    return (uint8_t)(q < 0.0f ? 0.0f : (q > 255.0f ? 255.0f : q));
+}
+
+// Slot assignment of `cnt` children with centroids `cc` in a node with centroid `pc`: the cost of
+// child c in slot s is the distance of its centroid along the octant direction of s
+// ((-1)^(bit a of s) per axis); pairs are taken greedily, cheapest first (ties: lower slot, then
+// lower child).  slot_of[c] receives the slot of child c.
+inline void wide_assign_slots(const v3* cc, v3 pc, int cnt, int* slot_of) {
+    float cost[8][8];
+    for (int c = 0; c < cnt; ++c) {
+        v3 d = cc[c] - pc;
+        for (int s = 0; s < 8; ++s) {
+            float sx = (s & 1) ? -d.x : d.x, sy = (s & 2) ? -d.y : d.y, sz = (s & 4) ? -d.z : d.z;
+            cost[c][s] = (sx + sy) + sz;
+        }
+    }
+    bool child_done[8] = {}, slot_used[8] = {};
+    for (int k = 0; k < cnt; ++k) {
+        int bc = -1, bs = -1;
+        float best = 0.0f;
+        for (int s = 0; s < 8; ++s) {
+            if (slot_used[s]) continue;
+            for (int c = 0; c < cnt; ++c) {
+                if (child_done[c]) continue;
+                if (bc < 0 || cost[c][s] < best) {
+                    bc = c;
+                    bs = s;
+                    best = cost[c][s];
+                }
+            }
+        }
+        child_done[bc] = true;
+        slot_used[bs] = true;
+        slot_of[bc] = bs;
+    }
+}
+
+struct WideBuild {
+    std::vector<Node8> nodes;
+    std::vector<uint32_t> tri_order;  // wide record position -> sorted position of the binary build
+    int levels = 0;
+};
+
+// The wide format over the binary LBVH of one segment, level by level from the root: each node
+// expands the largest-area internal child of its current children until it holds eight (subtrees
+// of at most WIDE_LEAF_MAX primitives are leaf children), assigns the children to slots, and
+// quantises their boxes; the next level lists the internal children of this level's nodes in
+// node order, each node's in slot order.
+inline WideBuild collapse_wide(const BinaryBuild& bb) {
+    WideBuild out;
+    std::vector<int> level = bb.roots;
+    uint32_t tri_next = 0;
+    auto leafish = [&](int r) { return bb.is_leaf(r) || bb.ncount(r) <= WIDE_LEAF_MAX; };
+    while (!level.empty()) {
+        out.levels++;
+        size_t base = out.nodes.size();
+        size_t next_base = base + level.size();
+        std::vector<int> next;
+        out.nodes.resize(base + level.size());
+        for (size_t li = 0; li < level.size(); ++li) {
+            Node8& nd = out.nodes[base + li];
+            std::memset(&nd, 0, sizeof(nd));
+            int r = level[li];
+            int ch[8];
+            int cnt = 0;
+            if (r < 0) {
+                cnt = 0;
+            } else if (leafish(r)) {
+                ch[0] = r;
+                cnt = 1;
+            } else {
+                ch[0] = bb.t.left[r];
+                ch[1] = bb.t.right[r];
+                cnt = 2;
+                while (cnt < 8) {
+                    int best = -1;
+                    float best_area = -1.0f;
+                    for (int c = 0; c < cnt; ++c) {
+                        if (leafish(ch[c])) continue;
+                        float a = aabb_half_area(bb.nbox(ch[c]));
+                        if (best < 0 || a > best_area) {
+                            best = c;
+                            best_area = a;
+                        }
+                    }
+                    if (best < 0) break;
+                    int v = ch[best];
+                    for (int c = cnt; c > best + 1; --c) ch[c] = ch[c - 1];
+                    ch[best] = bb.t.left[v];
+                    ch[best + 1] = bb.t.right[v];
+                    cnt++;
+                }
+            }
+            // node box, centroids, slots
+            Aabb box = aabb_empty();
+            v3 cc[8];
+            for (int c = 0; c < cnt; ++c) {
+                const Aabb& b = bb.nbox(ch[c]);
+                box = aabb_union(box, b);
+                cc[c] = (b.lo + b.hi) * 0.5f;
+            }
+            int slot_of[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            int child_at[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+            if (cnt > 0) {
+                wide_assign_slots(cc, (box.lo + box.hi) * 0.5f, cnt, slot_of);
+                for (int c = 0; c < cnt; ++c) child_at[slot_of[c]] = ch[c];
+            }
+            const float* lo = &box.lo.x;
+            const float* hi = &box.hi.x;
+            float scale[3];
+            for (int a = 0; a < 3; ++a) {
+                nd.origin[a] = cnt > 0 ? lo[a] : 0.0f;
+                nd.exponent[a] = cnt > 0 ? wide_exponent(hi[a] - lo[a]) : (uint8_t)127;
+                scale[a] = bitsf((uint32_t)nd.exponent[a] << 23);
+            }
+            nd.child_base = (uint32_t)(next_base + next.size());
+            nd.tri_base = tri_next;
+            uint32_t tri_off = 0;
+            for (int s = 0; s < 8; ++s) {
+                int v = child_at[s];
+                if (v < 0) {  // empty slot: an inverted box (never entered), meta 0
+                    nd.qlo_x[s] = nd.qlo_y[s] = nd.qlo_z[s] = 255;
+                    nd.qhi_x[s] = nd.qhi_y[s] = nd.qhi_z[s] = 0;
+                    continue;
+                }
+                const Aabb& b = bb.nbox(v);
+                nd.qlo_x[s] = wide_quantize_lo(b.lo.x, nd.origin[0], scale[0]);
+                nd.qhi_x[s] = wide_quantize_hi(b.hi.x, nd.origin[0], scale[0]);
+                nd.qlo_y[s] = wide_quantize_lo(b.lo.y, nd.origin[1], scale[1]);
+                nd.qhi_y[s] = wide_quantize_hi(b.hi.y, nd.origin[1], scale[1]);
+                nd.qlo_z[s] = wide_quantize_lo(b.lo.z, nd.origin[2], scale[2]);
+                nd.qhi_z[s] = wide_quantize_hi(b.hi.z, nd.origin[2], scale[2]);
+                if (leafish(v)) {
+                    uint32_t k = (uint32_t)bb.ncount(v), f = (uint32_t)bb.nfirst(v);
+                    nd.meta[s] = (uint8_t)(tri_off | (((1u << k) - 1u) << 5));
+                    for (uint32_t j = 0; j < k; ++j) out.tri_order.push_back(f + j);
+                    tri_off += k;
+                } else {
+                    nd.imask |= (uint8_t)(1u << s);
+                    next.push_back(v);
+                }
+            }
+            tri_next += tri_off;
+        }
+        level.swap(next);
+    }
     return out;
 }
 
@@ -478,6 +693,10 @@ struct SceneBvh {
     std::vector<TriRecord> flat_tris;
     int flat_levels = 0;
     float flat_bound = 0.0f;   // max |coordinate| of the triangle world boxes
+    // the same structure in the compressed 8-wide format (build_wide_bvh)
+    std::vector<Node8> wide;
+    std::vector<TriRecord> wide_tris;
+    int wide_levels = 0;
 };
 
 // The flat BVH: primitives are the (instance, triangle) pairs in instance order; a primitive's
@@ -516,6 +735,44 @@ inline void build_flat_bvh(const Geometry& g, int leaf_max, SceneBvh& s) {
     s.flat_levels = b.levels;
     s.flat_tris.resize(recs.size());
     for (size_t k = 0; k < recs.size(); ++k) s.flat_tris[k] = recs[b.order[k]];
+}
+
+// The flat structure in the compressed 8-wide format: the same primitives, boxes, records and
+// binary LBVH as build_flat_bvh, collapsed by collapse_wide; records in the wide order.
+inline void build_wide_bvh(const Geometry& g, SceneBvh& s) {
+    std::vector<Aabb> boxes;
+    std::vector<TriRecord> recs;
+    for (uint32_t i = 0; i < g.instance_count; ++i) {
+        const Instance& in = g.instances[i];
+        const Mesh& me = g.meshes[in.mesh_index];
+        uint32_t tris = me.index_count / 3u;
+        for (uint32_t p = 0; p < tris; ++p) {
+            v3 q[3];
+            triangle_object(g, in, p, q[0], q[1], q[2]);
+            v3 w0 = mat43_point(in.transform, q[0]), w1 = mat43_point(in.transform, q[1]),
+               w2 = mat43_point(in.transform, q[2]);
+            boxes.push_back(canon_box(aabb_point(aabb_point(Aabb{w0, w0}, w1), w2)));
+            TriRecord tr;
+            tr.v0[0] = q[0].x; tr.v0[1] = q[0].y; tr.v0[2] = q[0].z;
+            tr.v1[0] = q[1].x; tr.v1[1] = q[1].y; tr.v1[2] = q[1].z;
+            tr.v2[0] = q[2].x; tr.v2[1] = q[2].y; tr.v2[2] = q[2].z;
+            tr.prim = p;
+            tr.mesh = i;
+            tr.pad = 0;
+            recs.push_back(tr);
+        }
+    }
+    s.wide.clear();
+    s.wide_tris.clear();
+    s.wide_levels = 0;
+    if (boxes.empty()) return;
+    std::vector<uint32_t> seg(boxes.size(), 0u);
+    BinaryBuild bb = build_binary(boxes, seg, 1);
+    WideBuild w = collapse_wide(bb);
+    s.wide = std::move(w.nodes);
+    s.wide_levels = w.levels;
+    s.wide_tris.resize(w.tri_order.size());
+    for (size_t k = 0; k < w.tri_order.size(); ++k) s.wide_tris[k] = recs[bb.order[w.tri_order[k]]];
 }
 
 // BLAS over all meshes (segment = mesh) and TLAS over instances (leaf = instance index).
@@ -719,6 +976,81 @@ inline Hit trace_bvh(const Geometry& g, const SceneBvh& s, v3 o, v3 d, float tmi
                 trace_blas(s, in.mesh_index, inst, rp, nr, cull_back, tmin, best, tbest);
             } else {
                 stack[sp++] = ch;
+            }
+        }
+    }
+    return best;
+}
+
+// Conservative slab test of the eight children of a wide node: the decoded planes
+// origin + q 2^(e - 127) enter the slab distances as fma(q, 2^(e - 127) / d, fma(origin, 1/d,
+// -o/d -+ E)) (the margin E of node_ray); empty slots (neither internal nor leaf) never pass.
+inline int wide_node_hits(const Node8& nd, const NodeRay& r, float tmin, float tbest) {
+    const float ia[3] = {r.inv.x, r.inv.y, r.inv.z};
+    const uint8_t* qlo[3] = {nd.qlo_x, nd.qlo_y, nd.qlo_z};
+    const uint8_t* qhi[3] = {nd.qhi_x, nd.qhi_y, nd.qhi_z};
+    float step[3], base_near[3], base_far[3];
+    for (int a = 0; a < 3; ++a) {
+        step[a] = bitsf((uint32_t)nd.exponent[a] << 23) * ia[a];
+        base_near[a] = std::fmaf(nd.origin[a], ia[a], r.nob_near[a]);
+        base_far[a] = std::fmaf(nd.origin[a], ia[a], r.nob_far[a]);
+    }
+    int mask = 0;
+    for (int c = 0; c < 8; ++c) {
+        if (!((nd.imask >> c) & 1) && nd.meta[c] == 0) continue;
+        float tn = tmin, tf = tbest;
+        for (int a = 0; a < 3; ++a) {
+            float qn = (float)(r.near[a] ? qhi[a][c] : qlo[a][c]);
+            float qf = (float)(r.near[a] ? qlo[a][c] : qhi[a][c]);
+            tn = fmx(tn, std::fmaf(qn, step[a], base_near[a]));
+            tf = fmn(tf, std::fmaf(qf, step[a], base_far[a]));
+        }
+        if (tn <= tf) mask |= 1 << c;
+    }
+    return mask;
+}
+
+// Closest hit through the wide format of the flat structure (checks its decoding and layout; the
+// GPU traversal visits the same nodes in another order and finds the same hit).
+inline Hit trace_wide(const Geometry& g, const SceneBvh& s, v3 o, v3 d, float tmin, float tmax, bool cull_back) {
+    Hit best{0, 0.0f, 0.0f, 0.0f, 0u, 0u};
+    if (!finite3(d) || s.wide.empty()) return best;
+    float tbest = tmax;
+    NodeRay wr = node_ray(o, d, s.flat_bound);
+    uint32_t cur = 0xffffffffu;
+    bool skip = false;
+    RayPre rp{};
+    std::vector<uint32_t> stack;
+    stack.push_back(0u);
+    while (!stack.empty()) {
+        const Node8& nd = s.wide[stack.back()];
+        stack.pop_back();
+        int mask = wide_node_hits(nd, wr, tmin, tbest);
+        uint32_t rank = 0;
+        for (int c = 0; c < 8; ++c) {
+            bool internal = (nd.imask >> c) & 1;
+            if (internal && (mask >> c) & 1) stack.push_back(nd.child_base + rank);
+            rank += internal ? 1u : 0u;
+            if (internal || !((mask >> c) & 1)) continue;
+            uint32_t off = nd.meta[c] & 31u, units = nd.meta[c] >> 5;
+            for (uint32_t j = 0; units >> j; ++j) {
+                const TriRecord& tr = s.wide_tris[nd.tri_base + off + j];
+                if (tr.mesh != cur) {
+                    cur = tr.mesh;
+                    v3 oo, od;
+                    object_ray(g.instances[cur], o, d, oo, od);
+                    skip = !finite3(od);
+                    rp = ray_precompute(oo, od);
+                }
+                float t, u, v;
+                if (skip) continue;
+                if (!intersect_triangle(rp, v3{tr.v0[0], tr.v0[1], tr.v0[2]}, v3{tr.v1[0], tr.v1[1], tr.v1[2]},
+                                        v3{tr.v2[0], tr.v2[1], tr.v2[2]}, cull_back, tmin, tbest, t, u, v))
+                    continue;
+                if (closer(t, cur, tr.prim, best)) {
+                    best = Hit{1, t, u, v, cur, tr.prim};
+                    tbest = t;
+                }
             }
         }
     }

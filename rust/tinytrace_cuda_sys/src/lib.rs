@@ -55,6 +55,7 @@ pub const TT_LIGHT_SELECTION_POWER: u64 = 1;
 pub const TT_ACCEL_AUTO: u64 = 0;
 pub const TT_ACCEL_FLAT: u64 = 1;
 pub const TT_ACCEL_TWO_LEVEL: u64 = 2;
+pub const TT_ACCEL_FLAT_WIDE: u64 = 3;
 
 pub const TT_TRACE_CULL_BACK_FACES: u32 = 1;
 pub const TT_TRACE_NOALLOC_MAX_RAYS: u32 = 65536;

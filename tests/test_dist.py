@@ -90,6 +90,17 @@ def test_row_sample_and_parity_helpers():
     assert bench.row_parity(a, a, [4, 12, 20])["bit_exact"]
 
 
+def test_equal_error_interpolation():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    pts = [{"ms": 10.0, "error": 4e-3}, {"ms": 20.0, "error": 2e-3}, {"ms": 40.0, "error": 1e-3}]
+    t, how = bench.time_at_error(pts, 2.8284271247461903e-3)  # halfway in log-log between the first two
+    assert how == "interpolated" and abs(t - 14.142135623730951) < 1e-9
+    assert bench.time_at_error(pts, 5e-3) == (10.0, "below")
+    assert bench.time_at_error(pts, 5e-4) == (None, "floor")
+
+
 @pytest.mark.parametrize("world", [1])
 def test_single_process_dist_is_a_no_op(world, monkeypatch):
     monkeypatch.delenv("WORLD_SIZE", raising=False)

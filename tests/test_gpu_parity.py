@@ -66,7 +66,7 @@ def _gpu_bvh(ctx, scene):
     st = ctx.scene_stats(scene)
     blas = np.zeros(st.blas_nodes, NODE4_DTYPE)
     tris = np.zeros(st.triangle_count, TRI_RECORD_DTYPE)
-    tlas = np.zeros(st.tlas_nodes, NODE4_DTYPE)
+    tlas = np.zeros(st.tlas_nodes, native.NODE8_DTYPE if st.accel == native.TT_ACCEL_FLAT_WIDE else NODE4_DTYPE)
     check(ctx.lib.tt_scene_bvh_download(ctx.handle, scene, native.ptr(blas), blas.nbytes, native.ptr(tris),
                                         tris.nbytes, native.ptr(tlas), tlas.nbytes))
     return blas, tris, tlas, st
@@ -76,7 +76,7 @@ def _small_field():
     return scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11)
 
 
-ACCELS = {"flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL}
+ACCELS = {"flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL, "wide": native.TT_ACCEL_FLAT_WIDE}
 
 
 def _create_scene(ctx, arrays, accel):
@@ -87,15 +87,21 @@ def _create_scene(ctx, arrays, accel):
         check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_ACCEL, native.TT_ACCEL_AUTO))
 
 
-@pytest.mark.parametrize("accel", ["two_level", "flat"])
-@pytest.mark.parametrize("name", ["cornell", "field"])
+@pytest.mark.parametrize("accel", ["two_level", "flat", "wide"])
+@pytest.mark.parametrize("name", ["cornell", "field", "instanced"])
 def test_bvh_topology_bits(gpu_context, name, accel):
-    scene = scenes.cornell_box() if name == "cornell" else _small_field()
+    scene = {"cornell": scenes.cornell_box, "field": _small_field, "instanced": scenes.instanced_spheres}[name]()
     arrays = SceneArrays(scene)
     h = _create_scene(gpu_context, arrays, accel)
     blas, tris, tlas, st = _gpu_bvh(gpu_context, h)
-    orc = oracle.OracleScene(arrays)
-    if accel == "two_level":
+    orc = oracle.OracleScene(arrays, wide=accel == "wide")
+    if accel == "wide":
+        assert st.accel == native.TT_ACCEL_FLAT_WIDE
+        on, ot, ol = orc.wide_bvh()
+        assert st.blas_nodes == 0 and st.tlas_levels == ol
+        assert tris.tobytes() == ot.tobytes(), "wide triangle records differ"
+        assert tlas.tobytes() == on.tobytes(), "wide nodes differ"
+    elif accel == "two_level":
         assert st.accel == native.TT_ACCEL_TWO_LEVEL
         ob, ot, otl, bl, tl = orc.bvh()
         assert (st.blas_levels, st.tlas_levels) == (bl, tl)
@@ -126,7 +132,7 @@ def _random_rays(rng, n, center, spread):
     return rays
 
 
-@pytest.mark.parametrize("accel", ["two_level", "flat"])
+@pytest.mark.parametrize("accel", ["two_level", "flat", "wide"])
 @pytest.mark.parametrize("name", ["cornell", "field"])
 def test_closest_hit_matches_brute_force(gpu_context, name, accel):
     scene = scenes.cornell_box() if name == "cornell" else _small_field()
@@ -178,7 +184,7 @@ def _render_pair(ctx, w, frames=1, integrator="wavefront", slots=0, accel="flat"
     return gpu
 
 
-@pytest.mark.parametrize("accel", ["flat", "two_level"])
+@pytest.mark.parametrize("accel", ["flat", "two_level", "wide"])
 @pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
 def test_render_cornell_c1(gpu_context, integrator, accel):
     img = _render_pair(gpu_context, scenes.cornell_workload(), integrator=integrator, accel=accel)
@@ -192,7 +198,7 @@ def test_render_accumulation(gpu_context, integrator):
                  integrator=integrator)
 
 
-@pytest.mark.parametrize("accel", ["flat", "two_level"])
+@pytest.mark.parametrize("accel", ["flat", "two_level", "wide"])
 @pytest.mark.parametrize("integrator", ["wavefront", "megakernel"])
 def test_render_field_small(gpu_context, integrator, accel):
     w = scenes.Workload("field_small", _small_field(), scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0)),

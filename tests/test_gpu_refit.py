@@ -1,6 +1,6 @@
 """Instance updates on the GPU (tt_scene_update_instances) against the oracle: after moving the
-instances, the refitted world structure is byte-identical to the oracle's refit, closest hits
-equal brute force, and renders equal the oracle's."""
+instances, the refitted world structure (the rebuilt one for the compressed wide format) is
+byte-identical to the oracle's, closest hits equal brute force, and renders equal the oracle's."""
 import numpy as np
 import pytest
 
@@ -14,20 +14,20 @@ from tinytrace_gb300.renderer import Renderer, SceneArrays, make_constants
 
 pytestmark = pytest.mark.gpu
 
-ACCELS = {"flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL}
+ACCELS = {"flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL, "wide": native.TT_ACCEL_FLAT_WIDE}
 
 
 def _download(ctx, h):
     st = ctx.scene_stats(h)
     blas = np.zeros(st.blas_nodes, NODE4_DTYPE)
     tris = np.zeros(st.triangle_count, TRI_RECORD_DTYPE)
-    tlas = np.zeros(st.tlas_nodes, NODE4_DTYPE)
+    tlas = np.zeros(st.tlas_nodes, native.NODE8_DTYPE if st.accel == native.TT_ACCEL_FLAT_WIDE else NODE4_DTYPE)
     check(ctx.lib.tt_scene_bvh_download(ctx.handle, h, native.ptr(blas), blas.nbytes, native.ptr(tris), tris.nbytes,
                                         native.ptr(tlas), tlas.nbytes))
     return tlas
 
 
-@pytest.mark.parametrize("accel", ["flat", "two_level"])
+@pytest.mark.parametrize("accel", ["flat", "two_level", "wide"])
 def test_update_refits_like_the_oracle(gpu_context, accel):
     ctx = gpu_context
     arrays = SceneArrays(scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11))
@@ -36,14 +36,15 @@ def test_update_refits_like_the_oracle(gpu_context, accel):
         h = ctx.create_scene(arrays)
     finally:
         check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_ACCEL, native.TT_ACCEL_AUTO))
-    orc = oracle.OracleScene(SceneArrays.from_arrays(arrays.save(None)))
+    orc = oracle.OracleScene(SceneArrays.from_arrays(arrays.save(None)), wide=accel == "wide")
     rng = np.random.default_rng(8)
     for step in range(3):
         moved = moved_instances(arrays.instances, rng)
         check(ctx.lib.tt_scene_update_instances(ctx.handle, h, native.ptr(moved), len(moved)))
         orc.update_instances(moved)
         got = _download(ctx, h)
-        want = orc.flat_bvh()[0] if accel == "flat" else orc.bvh()[2]
+        want = {"flat": lambda: orc.flat_bvh()[0], "wide": lambda: orc.wide_bvh()[0],
+                "two_level": lambda: orc.bvh()[2]}[accel]()
         assert got.tobytes() == want.tobytes(), f"step {step}: refitted nodes differ"
         rays = _rays(rng, orc.arrays, 6000, 30.0)
         hits = np.zeros((len(rays), 8), np.uint32)

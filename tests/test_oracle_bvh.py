@@ -3,8 +3,9 @@
 The closed driver BVH of the reference's ray queries has no source, so the oracle carries
 a brute-force closest hit (every instance, every triangle, in object space) as ground truth
 and the project's own BVH4 construction, which the GPU build must reproduce byte for byte.
-These tests check that both oracle structures (two-level and flat) find exactly the brute
-force's hits, and that their node arrays are well-formed bounding hierarchies.
+These tests check that both oracle structures (two-level and flat) and the flat structure's
+compressed 8-wide format find exactly the brute force's hits, and that their node arrays are
+well-formed bounding hierarchies.
 """
 import numpy as np
 import pytest
@@ -157,6 +158,84 @@ def test_closest_hit_equals_brute_force(name, cull):
         got = orc.trace(rays, cull=cull, brute=False, flat=flat)
         diff = np.any(got != brute, axis=1)
         assert not diff.any(), f"flat={flat}: {diff.sum()} rays differ"
+    wide = oracle.OracleScene(arrays, wide=True).trace(rays, cull=cull, wide=True)
+    assert np.array_equal(wide, brute), f"wide format: {np.any(wide != brute, axis=1).sum()} rays differ"
+
+
+def _decoded(node):
+    """(8, 3) low and high planes of a wide node's child slots, decoded in float64."""
+    scale = np.ldexp(1.0, node["exponent"].astype(np.int64) - 127)
+    org = node["origin"].astype(np.float64)
+    lo = np.stack([node["qlo_x"], node["qlo_y"], node["qlo_z"]], 1).astype(np.float64) * scale + org
+    hi = np.stack([node["qhi_x"], node["qhi_y"], node["qhi_z"]], 1).astype(np.float64) * scale + org
+    return lo, hi
+
+
+@pytest.mark.parametrize("name", ["cornell", "field", "instanced"])
+def test_wide_bvh_structure(name):
+    """The compressed 8-wide format of the flat BVH: every (instance, triangle) record sits in
+    exactly one leaf slot (1..3 records, offsets within the node's record run), internal slots
+    address nodes of the next level, decoded child boxes contain their subtrees' triangles (the
+    quantisation rounds outwards) and empty slots carry inverted boxes."""
+    arrays = SceneArrays(_scene(name))
+    orc = oracle.OracleScene(arrays, wide=True)
+    nodes, tris, levels = orc.wide_bvh()
+    assert len(tris) == len(orc.flat_bvh()[1])
+    seen = np.zeros(len(tris), np.int32)
+    world = {}
+    for k, r in enumerate(tris):
+        inst = arrays.instances[int(r["mesh"])]
+        m = _instance_matrix(inst)
+        q = np.stack([r["v0"], r["v1"], r["v2"]]).astype(np.float64)
+        world[k] = (m[:3, :3] @ q.T).T + m[:3, 3]
+
+    def subtree_points(i):
+        nd = nodes[i]
+        pts = []
+        rank = 0
+        for s in range(8):
+            internal = (int(nd["imask"]) >> s) & 1
+            if internal:
+                pts.append(subtree_points(int(nd["child_base"]) + rank))
+                rank += 1
+            elif nd["meta"][s]:
+                off, units = int(nd["meta"][s]) & 31, int(nd["meta"][s]) >> 5
+                for j in range(bin(units).count("1")):
+                    pts.append(world[int(nd["tri_base"]) + off + j])
+        return np.concatenate(pts)
+
+    def visit(i, depth):
+        nd = nodes[i]
+        lo, hi = _decoded(nd)
+        rank = 0
+        deepest = depth
+        for s in range(8):
+            internal = (int(nd["imask"]) >> s) & 1
+            meta = int(nd["meta"][s])
+            if not internal and meta == 0:
+                assert np.all(lo[s] > hi[s]), "empty slots are inverted boxes"
+                continue
+            if internal:
+                child = int(nd["child_base"]) + rank
+                rank += 1
+                assert 0 < child < len(nodes)
+                pts = subtree_points(child)
+                deepest = max(deepest, visit(child, depth + 1))
+            else:
+                off, units = meta & 31, meta >> 5
+                assert units in (1, 3, 7) and off + bin(units).count("1") <= 24
+                pts = []
+                for j in range(bin(units).count("1")):
+                    seen[int(nd["tri_base"]) + off + j] += 1
+                    pts.append(world[int(nd["tri_base"]) + off + j])
+                pts = np.concatenate(pts)
+            slack = 1e-5 * (1.0 + np.abs(pts))
+            assert np.all(pts >= lo[s] - slack) and np.all(pts <= hi[s] + slack)
+        return deepest
+
+    depth = visit(0, 1)
+    assert np.all(seen == 1), "every record sits in exactly one leaf slot"
+    assert depth <= levels
 
 
 def test_empty_interval_misses():

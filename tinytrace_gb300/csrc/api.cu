@@ -82,6 +82,7 @@ struct SceneRes {
     std::vector<tt_instance> host_instances;  // for tt_scene_update_instances' checks
     std::vector<tt_emissive_triangle> host_emissive;  // to rebuild the light alias table on updates
     std::vector<tt_material> host_materials;
+    std::vector<tt_mesh> host_meshes;  // to rebuild the compressed wide structure on instance updates
     uint32_t material_count = 0;
 };
 
@@ -96,7 +97,7 @@ struct WavefrontBuffers {
 // ReSTIR DI state kept between frames: two G-buffers and two final reservoir arrays
 // (current and previous frame), the initial and temporal reservoirs, the previous camera.
 struct RestirState {
-    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex, glob;
+    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex, glob, queue, queue_count;
     uint64_t pixels = 0;
     uint32_t cur = 0;
     RestirHistory history{};
@@ -163,6 +164,14 @@ struct tt_context {
 };
 
 namespace tt {
+// Traversal stack entries (32-bit words) a structure can need: BVH4 nodes push at most 3 entries
+// per level (+1 for the instance marker of the two-level structure's transition); the wide format
+// pushes at most a node group and a triangle group (two words each) per level.
+uint64_t structure_stack_need(const BvhResult& b) {
+    if (b.flat && b.wide) return 4ull * b.flat_levels + 2ull;
+    if (b.flat) return 3ull * b.flat_levels + 1ull;
+    return 3ull * (b.blas_levels + b.tlas_levels) + 1ull;
+}
 void raise_device_error(uint32_t e) {
     if (e & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
     if (e & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
@@ -924,10 +933,13 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
                       d->instances, d->instance_count};
         uint64_t instanced = 0;
         for (uint32_t i = 0; i < d->instance_count; ++i) instanced += d->meshes[d->instances[i].mesh_index].index_count / 3u;
-        bool flat = ctx->accel == TT_ACCEL_FLAT || (ctx->accel == TT_ACCEL_AUTO && instanced <= FLAT_AUTO_MAX_TRIANGLES);
+        bool wide = ctx->accel == TT_ACCEL_FLAT_WIDE;
+        bool flat = wide || ctx->accel == TT_ACCEL_FLAT ||
+                    (ctx->accel == TT_ACCEL_AUTO && instanced <= FLAT_AUTO_MAX_TRIANGLES);
         if (flat && instanced >= (1ull << 27))
             fail(TT_ERR_OVERFLOW, "more than 2^27 instanced triangles for the flat BVH");
-        build_scene_bvh(bi, st, BLAS_LEAF_MAX, flat, s->bvh);
+        s->host_meshes.assign(d->meshes, d->meshes + d->mesh_count);
+        build_scene_bvh(bi, st, BLAS_LEAF_MAX, flat, wide, s->bvh);
         check_cuda(cudaEventRecord(e1, st), "event");
         check_cuda(cudaEventSynchronize(e1), "event");
         float ms = 0.0f;
@@ -935,8 +947,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         ctx->scene_build_ms = ms;
-        uint64_t need_stack = flat ? 3ull * s->bvh.flat_levels + 1ull
-                                   : 3ull * (s->bvh.blas_levels + s->bvh.tlas_levels) + 1ull;
+        uint64_t need_stack = structure_stack_need(s->bvh);
         if (need_stack > (uint64_t)TRAVERSAL_STACK)
             fail(TT_ERR_OVERFLOW, "scene BVH is too deep for the traversal stack (" +
                                       std::to_string(need_stack) + " entries needed)");
@@ -968,10 +979,11 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             ds.has_tlas = s->bvh.flat_nodes > 0 ? 1u : 0u;
             ds.tlas_bound = s->bvh.flat_bound;
             ds.flat = 1u;
+            ds.wide = wide ? 1u : 0u;
             stt.triangle_count = s->bvh.flat_tri_count;
             stt.tlas_nodes = s->bvh.flat_nodes;
             stt.tlas_levels = s->bvh.flat_levels;
-            stt.accel = TT_ACCEL_FLAT;
+            stt.accel = wide ? TT_ACCEL_FLAT_WIDE : TT_ACCEL_FLAT;
         } else {
             ds.blas = s->bvh.blas.as<uint4>();
             ds.tris = s->bvh.tris.as<float4>();
@@ -979,6 +991,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             ds.has_tlas = s->bvh.tlas_nodes > 0 ? 1u : 0u;
             ds.tlas_bound = s->bvh.tlas_bound;
             ds.flat = 0u;
+            ds.wide = 0u;
             stt.triangle_count = s->bvh.tri_count;
             stt.blas_nodes = s->bvh.blas_nodes;
             stt.tlas_nodes = s->bvh.tlas_nodes;
@@ -1028,7 +1041,27 @@ int32_t tt_scene_update_instances(tt_context* ctx, tt_handle scene, const tt_ins
             check_cuda(cudaMemcpyAsync(s->inst_xform.ptr, xf.data(), 16ull * xf.size(), cudaMemcpyHostToDevice, st),
                        "instance rows");
             launch_light_records(s->dev, s->light_rec.as<float4>(), s->dev.emissive_count, st);
-            refit_scene_bvh(s->instances.as<tt_instance>(), st, s->bvh);  // synchronises the stream
+            if (s->bvh.wide) {
+                // quantised child boxes cannot be refitted in place: the wide structure is rebuilt
+                // (same build as tt_scene_create, over the moved instances)
+                BvhResult nb;
+                BuildInput bi{s->positions.as<int16_t>(), s->indices.as<uint32_t>(), s->host_meshes.data(),
+                              (uint32_t)s->host_meshes.size(), instances, count};
+                build_scene_bvh(bi, st, BLAS_LEAF_MAX, true, true, nb);
+                uint64_t need = structure_stack_need(nb);
+                if (need > (uint64_t)TRAVERSAL_STACK)
+                    fail(TT_ERR_OVERFLOW, "updated BVH is too deep for the traversal stack (" + std::to_string(need) +
+                                              " entries needed); the scene keeps its previous structure");
+                s->bvh = std::move(nb);
+                s->dev.tris = s->bvh.flat_tris.as<float4>();
+                s->dev.tlas = s->bvh.flat_nodes_buf.as<uint4>();
+                s->dev.stack_need = (uint32_t)need;
+                s->stats.tlas_nodes = s->bvh.flat_nodes;
+                s->stats.tlas_levels = s->bvh.flat_levels;
+                s->stats.max_stack = need;
+            } else {
+                refit_scene_bvh(s->instances.as<tt_instance>(), st, s->bvh);  // synchronises the stream
+            }
             s->dev.tlas_bound = s->bvh.flat ? s->bvh.flat_bound : s->bvh.tlas_bound;
             s->host_instances.assign(instances, instances + count);
             // emitted powers follow the new world-space areas
@@ -1090,8 +1123,9 @@ int32_t tt_scene_bvh_download(tt_context* ctx, tt_handle scene, void* blas, uint
         use_device(ctx);
         SceneRes* s = lookup<SceneRes>(ctx, scene, KIND_SCENE);
         const tt_scene_stats& stt = s->stats;
+        uint64_t node_bytes = s->bvh.wide ? 80ull : 128ull;
         require(blas_bytes == stt.blas_nodes * 128ull && tri_bytes == stt.triangle_count * 48ull &&
-                    tlas_bytes == stt.tlas_nodes * 128ull,
+                    tlas_bytes == stt.tlas_nodes * node_bytes,
                 "byte counts must match tt_scene_stats");
         bool flat = s->bvh.flat;
         const void* src_tris = flat ? s->bvh.flat_tris.ptr : s->bvh.tris.ptr;
@@ -1173,7 +1207,8 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
             require(value <= 1, "stage timing is 0 or 1");
             ctx->stage_timing = value != 0;
         } else if (option == TT_OPTION_ACCEL) {
-            require(value == TT_ACCEL_AUTO || value == TT_ACCEL_FLAT || value == TT_ACCEL_TWO_LEVEL,
+            require(value == TT_ACCEL_AUTO || value == TT_ACCEL_FLAT || value == TT_ACCEL_TWO_LEVEL ||
+                        value == TT_ACCEL_FLAT_WIDE,
                     "unknown acceleration structure");
             ctx->accel = (uint32_t)value;
         } else {
@@ -1276,6 +1311,8 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
             R.initial.alloc(32ull * WH);
             R.temporal.alloc(32ull * WH);
             R.glob.alloc(16ull * LOBE_RECORD * WH);
+            R.queue.alloc(4ull * HIT_BUCKETS * WH);
+            R.queue_count.alloc(4ull * HIT_BUCKETS);
             R.pixels = WH;
             R.history.valid = 0u;
         }
@@ -1296,6 +1333,8 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         rp.glob = R.glob.as<float4>();
         rp.prev_gbuf = R.gbuf[R.cur ^ 1u].as<Surface>();
         rp.initial = R.initial.as<Reservoir>();
+        rp.queue = R.queue.as<uint32_t>();
+        rp.queue_count = R.queue_count.as<uint32_t>();
         rp.temporal = R.temporal.as<Reservoir>();
         rp.final_out = R.final_res[R.cur].as<Reservoir>();
         rp.prev = R.final_res[R.cur ^ 1u].as<Reservoir>();

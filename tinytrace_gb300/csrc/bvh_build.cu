@@ -580,12 +580,21 @@ struct Build4 {
     int* roots = nullptr;       // scratch, segment root binary refs
 };
 
-// Generic BVH4 build over primitive boxes grouped in non-decreasing segments.
-Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uint32_t n,
-                  uint32_t segs, int leaf_max, bool leaf_by_prim, const uint32_t* leaf_ids,
-                  DeviceBuffer& node_buf, Scratch& sc) {
+// Binary LBVH over primitive boxes grouped in non-decreasing segments: centroid bounds,
+// Morton keys, stable radix sort, Karras hierarchy, bottom-up boxes; each segment's root
+// binary reference in `roots` (device, -1 for an empty segment).
+struct Binary {
+    TreeView tv;
+    uint32_t* order = nullptr;  // sorted position -> primitive
+    float4* blo = nullptr;      // binary node boxes (internal r < ni, leaf ni + sorted position)
+    float4* bhi = nullptr;
+    int* roots = nullptr;
+};
+
+Binary build_binary(const float4* plo, const float4* phi, const uint32_t* seg, uint32_t n, uint32_t segs,
+                    Scratch& sc) {
     cudaStream_t st = sc.stream;
-    Build4 out;
+    Binary out;
     float* bounds = sc.get<float>(6ull * segs);
     uint32_t* seg_count = sc.get<uint32_t>(segs);
     init_bounds_kernel<<<grid_for(segs, 256), 256, 0, st>>>(bounds, seg_count, segs);
@@ -620,6 +629,24 @@ Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uin
                                                        blo, bhi, visits);
     out.blo = blo;
     out.bhi = bhi;
+    out.roots = sc.get<int>(segs);
+    segment_roots_kernel<<<grid_for(segs, 256), 256, 0, st>>>(seg_first, seg_count, segs, (int)n,
+                                                               first, last, out.roots);
+    out.tv = TreeView{(int)n, ni, left, right, first, last, blo, bhi};
+    return out;
+}
+
+// Generic BVH4 build over primitive boxes grouped in non-decreasing segments.
+Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uint32_t n,
+                  uint32_t segs, int leaf_max, bool leaf_by_prim, const uint32_t* leaf_ids,
+                  DeviceBuffer& node_buf, Scratch& sc) {
+    cudaStream_t st = sc.stream;
+    Build4 out;
+    Binary bin = build_binary(plo, phi, seg, n, segs, sc);
+    uint32_t* vals = bin.order;
+    out.order = vals;
+    out.blo = bin.blo;
+    out.bhi = bin.bhi;
     // collapse
     uint64_t cap = (uint64_t)n + segs + 1;
     node_buf.alloc(cap * 128ull);
@@ -627,12 +654,9 @@ Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uin
     int* lvl_b = sc.get<int>(cap);
     int* chosen = sc.get<int>(4 * cap);
     uint32_t* icount = sc.get<uint32_t>(cap + 1);
-    segment_roots_kernel<<<grid_for(segs, 256), 256, 0, st>>>(seg_first, seg_count, segs, (int)n,
-                                                               first, last, lvl_a);
-    int* roots = sc.get<int>(segs);
-    check_cuda(cudaMemcpyAsync(roots, lvl_a, sizeof(int) * segs, cudaMemcpyDeviceToDevice, st), "copy");
-    out.roots = roots;
-    TreeView tv{(int)n, ni, left, right, first, last, blo, bhi};
+    check_cuda(cudaMemcpyAsync(lvl_a, bin.roots, sizeof(int) * segs, cudaMemcpyDeviceToDevice, st), "copy");
+    out.roots = bin.roots;
+    TreeView tv = bin.tv;
     uint64_t base = 0;
     uint32_t L = segs;
     while (L > 0) {
@@ -657,25 +681,273 @@ Build4 build_bvh4(const float4* plo, const float4* phi, const uint32_t* seg, uin
     return out;
 }
 
+// ---------------------------------------------------------------- collapse to the compressed 8-wide format
+// The flat structure's wide format (oracle/ref_bvh.h collapse_wide restates it; the node arrays
+// must match byte for byte): level by level from the root, each node expands the largest-area
+// internal child until it holds eight children (subtrees of at most WIDE_LEAF_MAX primitives are
+// leaf children), assigns them to slots by octant direction, and quantises their boxes to 8 bits
+// per plane (outwards) relative to the node's low corner with a power-of-two scale per axis.
+// 80-byte node: origin xyz, biased exponents and the internal-slot mask; child base, triangle
+// base, eight meta bytes (leaf slot: offset | unary count << 5); qlo/qhi bytes per axis.
+#ifndef TT_WIDE_LEAF_MAX
+#define TT_WIDE_LEAF_MAX 3
+#endif
+constexpr int WIDE_LEAF_MAX = TT_WIDE_LEAF_MAX;
+
+__device__ __forceinline__ bool wide_leafish(const TreeView& t, int r) {
+    return t.is_leaf(r) || t.ncount(r) <= WIDE_LEAF_MAX;
+}
+
+__device__ __forceinline__ uint32_t wide_exponent(float extent) {
+    float x = extent / 255.0f;
+    uint32_t bits = __float_as_uint(x);
+    uint32_t e = (bits >> 23) & 0xffu;
+    if (e == 0u) e = 1u;
+    else if ((bits & 0x7fffffu) != 0u) e += 1u;
+    while (e < 254u && 255.0f * __uint_as_float(e << 23) < extent) e += 1u;
+    return e > 254u ? 254u : e;
+}
+__device__ __forceinline__ uint32_t wide_q(float q) { return (uint32_t)(q < 0.0f ? 0.0f : (q > 255.0f ? 255.0f : q)); }
+
+__global__ void wide_choose_kernel(TreeView t, const int* level, uint32_t L, int* slot_child, uint32_t* icount,
+                                   uint32_t* tcount) {
+    uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= L) return;
+    int r = level[li];
+    int ch[8];
+    int cnt = 0;
+    if (r >= 0) {
+        if (wide_leafish(t, r)) {
+            ch[0] = r;
+            cnt = 1;
+        } else {
+            ch[0] = t.left[r];
+            ch[1] = t.right[r];
+            cnt = 2;
+            while (cnt < 8) {
+                int best = -1;
+                float best_area = -1.0f;
+                for (int c = 0; c < cnt; ++c) {
+                    if (wide_leafish(t, ch[c])) continue;
+                    float a = t.half_area(ch[c]);
+                    if (best < 0 || a > best_area) {
+                        best = c;
+                        best_area = a;
+                    }
+                }
+                if (best < 0) break;
+                int v = ch[best];
+                for (int c = cnt; c > best + 1; --c) ch[c] = ch[c - 1];
+                ch[best] = t.left[v];
+                ch[best + 1] = t.right[v];
+                cnt++;
+            }
+        }
+    }
+    // node box and child centroids
+    float lo[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+    float hi[3] = {__int_as_float(0xff800000), __int_as_float(0xff800000), __int_as_float(0xff800000)};
+    float cc[8][3];
+    for (int c = 0; c < cnt; ++c) {
+        float4 l = t.blo[ch[c]], h = t.bhi[ch[c]];
+        lo[0] = fminf(lo[0], l.x); lo[1] = fminf(lo[1], l.y); lo[2] = fminf(lo[2], l.z);
+        hi[0] = fmaxf(hi[0], h.x); hi[1] = fmaxf(hi[1], h.y); hi[2] = fmaxf(hi[2], h.z);
+        cc[c][0] = (l.x + h.x) * 0.5f;
+        cc[c][1] = (l.y + h.y) * 0.5f;
+        cc[c][2] = (l.z + h.z) * 0.5f;
+    }
+    // slots: greedy cheapest (child, slot) pairs, cost = centroid offset along the slot's octant
+    float pc[3] = {(lo[0] + hi[0]) * 0.5f, (lo[1] + hi[1]) * 0.5f, (lo[2] + hi[2]) * 0.5f};
+    float cost[8][8];
+    for (int c = 0; c < cnt; ++c) {
+        float dx = cc[c][0] - pc[0], dy = cc[c][1] - pc[1], dz = cc[c][2] - pc[2];
+        for (int s = 0; s < 8; ++s) {
+            float sx = (s & 1) ? -dx : dx, sy = (s & 2) ? -dy : dy, sz = (s & 4) ? -dz : dz;
+            cost[c][s] = __fadd_rn(__fadd_rn(sx, sy), sz);
+        }
+    }
+    int child_at[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+    uint32_t child_done = 0u, slot_used = 0u;
+    for (int k = 0; k < cnt; ++k) {
+        int bc = -1, bs = -1;
+        float best = 0.0f;
+        for (int s = 0; s < 8; ++s) {
+            if ((slot_used >> s) & 1u) continue;
+            for (int c = 0; c < cnt; ++c) {
+                if ((child_done >> c) & 1u) continue;
+                if (bc < 0 || cost[c][s] < best) {
+                    bc = c;
+                    bs = s;
+                    best = cost[c][s];
+                }
+            }
+        }
+        child_done |= 1u << bc;
+        slot_used |= 1u << bs;
+        child_at[bs] = ch[bc];
+    }
+    uint32_t internal = 0, tris = 0;
+    for (int s = 0; s < 8; ++s) {
+        int v = child_at[s];
+        slot_child[8 * li + s] = v;
+        if (v < 0) continue;
+        if (wide_leafish(t, v)) tris += (uint32_t)t.ncount(v);
+        else internal++;
+    }
+    icount[li] = internal;
+    tcount[li] = tris;
+}
+
+__global__ void wide_emit_kernel(TreeView t, const int* level, uint32_t L, const int* slot_child,
+                                 const uint32_t* ioff, const uint32_t* toff, uint64_t next_base, uint32_t tri_level_base,
+                                 uint64_t node_base, uint4* nodes, int* next_level, uint32_t* tri_order) {
+    uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= L) return;
+    int child_at[8];
+    int cnt = 0;
+    float lo[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+    float hi[3] = {__int_as_float(0xff800000), __int_as_float(0xff800000), __int_as_float(0xff800000)};
+    for (int s = 0; s < 8; ++s) {
+        int v = slot_child[8 * li + s];
+        child_at[s] = v;
+        if (v < 0) continue;
+        cnt++;
+        float4 l = t.blo[v], h = t.bhi[v];
+        lo[0] = fminf(lo[0], l.x); lo[1] = fminf(lo[1], l.y); lo[2] = fminf(lo[2], l.z);
+        hi[0] = fmaxf(hi[0], h.x); hi[1] = fmaxf(hi[1], h.y); hi[2] = fmaxf(hi[2], h.z);
+    }
+    uint32_t w[20];
+    uint32_t e[3];
+    float scale[3], org[3];
+    for (int a = 0; a < 3; ++a) {
+        org[a] = cnt > 0 ? lo[a] : 0.0f;
+        e[a] = cnt > 0 ? wide_exponent(__fsub_rn(hi[a], lo[a])) : 127u;
+        scale[a] = __uint_as_float(e[a] << 23);
+        w[a] = __float_as_uint(org[a]);
+    }
+    uint32_t child_base = (uint32_t)(next_base + ioff[li]);
+    uint32_t tri_base = tri_level_base + toff[li];
+    uint32_t imask = 0u, meta[2] = {0u, 0u}, q[12] = {};
+    uint32_t tri_off = 0u, rank = 0u;
+    for (int s = 0; s < 8; ++s) {
+        int v = child_at[s];
+        uint32_t qb[6];
+        if (v < 0) {
+            qb[0] = qb[2] = qb[4] = 255u;  // lo planes
+            qb[1] = qb[3] = qb[5] = 0u;    // hi planes
+        } else {
+            float4 l = t.blo[v], h = t.bhi[v];
+            const float cl[3] = {l.x, l.y, l.z}, chh[3] = {h.x, h.y, h.z};
+            for (int a = 0; a < 3; ++a) {
+                qb[2 * a] = wide_q(floorf(__fdiv_rn(__fsub_rn(cl[a], org[a]), scale[a])));
+                qb[2 * a + 1] = wide_q(ceilf(__fdiv_rn(__fsub_rn(chh[a], org[a]), scale[a])));
+            }
+            if (wide_leafish(t, v)) {
+                uint32_t k = (uint32_t)t.ncount(v), f = (uint32_t)t.nfirst(v);
+                uint32_t m = tri_off | (((1u << k) - 1u) << 5);
+                meta[s >> 2] |= m << (8 * (s & 3));
+                for (uint32_t j = 0; j < k; ++j) tri_order[tri_base + tri_off + j] = f + j;
+                tri_off += k;
+            } else {
+                imask |= 1u << s;
+                next_level[ioff[li] + rank] = v;
+                rank++;
+            }
+        }
+        // q words: [qlo_x 0..3, qlo_x 4..7, qhi_x 0..3, qhi_x 4..7, qlo_y ..., qhi_z 4..7]
+        for (int a = 0; a < 3; ++a) {
+            q[4 * a + (s >> 2)] |= qb[2 * a] << (8 * (s & 3));
+            q[4 * a + 2 + (s >> 2)] |= qb[2 * a + 1] << (8 * (s & 3));
+        }
+    }
+    w[3] = e[0] | (e[1] << 8) | (e[2] << 16) | (imask << 24);
+    w[4] = child_base;
+    w[5] = tri_base;
+    w[6] = meta[0];
+    w[7] = meta[1];
+    for (int k = 0; k < 12; ++k) w[8 + k] = q[k];
+    uint4* nd = nodes + 5ull * (node_base + li);
+    for (int k = 0; k < 5; ++k) nd[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+}
+
+__global__ void gather_wide_records_kernel(const float4* in, const uint32_t* order, const uint32_t* tri_order,
+                                           uint32_t n, float4* out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t s = order[tri_order[i]];
+    out[3ull * i + 0] = in[3ull * s + 0];
+    out[3ull * i + 1] = in[3ull * s + 1];
+    out[3ull * i + 2] = in[3ull * s + 2];
+}
+
+struct Build8 {
+    uint64_t nodes = 0;
+    uint32_t levels = 0;
+    std::vector<uint64_t> level_start;
+};
+
+// The wide format of one segment's binary LBVH into `node_buf` (80-byte nodes); `tri_order`
+// (n entries) receives the sorted position of each wide triangle record.
+Build8 collapse_wide(const Binary& bin, uint32_t n, DeviceBuffer& node_buf, uint32_t* tri_order, Scratch& sc) {
+    cudaStream_t st = sc.stream;
+    Build8 out;
+    uint64_t cap = (uint64_t)n + 2;
+    node_buf.alloc(cap * 80ull);
+    int* lvl_a = sc.get<int>(cap);
+    int* lvl_b = sc.get<int>(cap);
+    int* slot_child = sc.get<int>(8 * cap);
+    uint32_t* icount = sc.get<uint32_t>(cap + 1);
+    uint32_t* tcount = sc.get<uint32_t>(cap + 1);
+    check_cuda(cudaMemcpyAsync(lvl_a, bin.roots, sizeof(int), cudaMemcpyDeviceToDevice, st), "copy");
+    uint64_t base = 0;
+    uint32_t L = 1, tri_level_base = 0;
+    while (L > 0) {
+        out.levels++;
+        out.level_start.push_back(base);
+        wide_choose_kernel<<<grid_for(L, 128), 128, 0, st>>>(bin.tv, lvl_a, L, slot_child, icount, tcount);
+        check_cuda(cudaMemsetAsync(icount + L, 0, 4, st), "memset");
+        check_cuda(cudaMemsetAsync(tcount + L, 0, 4, st), "memset");
+        exclusive_scan(icount, (uint64_t)L + 1, sc);
+        exclusive_scan(tcount, (uint64_t)L + 1, sc);
+        uint32_t totals[2] = {0u, 0u};
+        check_cuda(cudaMemcpyAsync(&totals[0], icount + L, 4, cudaMemcpyDeviceToHost, st), "copy");
+        check_cuda(cudaMemcpyAsync(&totals[1], tcount + L, 4, cudaMemcpyDeviceToHost, st), "copy");
+        check_cuda(cudaStreamSynchronize(st), "sync");
+        if (base + L + totals[0] > cap || (uint64_t)tri_level_base + totals[1] > n)
+            fail(TT_ERR_OVERFLOW, "wide bvh capacity exceeded");
+        wide_emit_kernel<<<grid_for(L, 128), 128, 0, st>>>(bin.tv, lvl_a, L, slot_child, icount, tcount, base + L,
+                                                           tri_level_base, base, node_buf.as<uint4>(), lvl_b,
+                                                           tri_order);
+        base += L;
+        tri_level_base += totals[1];
+        L = totals[0];
+        std::swap(lvl_a, lvl_b);
+    }
+    out.nodes = base;
+    out.level_start.push_back(base);
+    return out;
+}
+
 }  // namespace
 
 // Max |coordinate| of the root box of a built tree (the bound of the slab-test margins).
-static float root_bound(const Build4& b, cudaStream_t stream) {
+static float root_bound(const int* roots, const float4* blo, const float4* bhi, cudaStream_t stream) {
     int root = 0;
-    check_cuda(cudaMemcpyAsync(&root, b.roots, sizeof(int), cudaMemcpyDeviceToHost, stream), "root");
+    check_cuda(cudaMemcpyAsync(&root, roots, sizeof(int), cudaMemcpyDeviceToHost, stream), "root");
     check_cuda(cudaStreamSynchronize(stream), "sync");
     float4 rb[2];
-    check_cuda(cudaMemcpyAsync(&rb[0], b.blo + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
-    check_cuda(cudaMemcpyAsync(&rb[1], b.bhi + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
+    check_cuda(cudaMemcpyAsync(&rb[0], blo + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
+    check_cuda(cudaMemcpyAsync(&rb[1], bhi + root, 16, cudaMemcpyDeviceToHost, stream), "root box");
     check_cuda(cudaStreamSynchronize(stream), "sync");
     float bound = 0.0f;
     for (float v : {rb[0].x, rb[0].y, rb[0].z, rb[1].x, rb[1].y, rb[1].z}) bound = std::max(bound, std::fabs(v));
     return bound;
 }
 
-static void build_flat(const BuildInput& in, cudaStream_t stream, int leaf_max, BvhResult& out) {
+static void build_flat(const BuildInput& in, cudaStream_t stream, int leaf_max, bool wide, BvhResult& out) {
     Scratch sc(stream);
     out.flat = true;
+    out.wide = wide;
     std::vector<uint32_t> base(in.instance_count + 1, 0);
     for (uint32_t i = 0; i < in.instance_count; ++i)
         base[i + 1] = base[i] + in.meshes_host[in.instances_host[i].mesh_index].index_count / 3u;
@@ -701,12 +973,26 @@ static void build_flat(const BuildInput& in, cudaStream_t stream, int leaf_max, 
     float4* recs = sc.get<float4>(3ull * n);
     flat_prims_kernel<<<grid_for(n, 256), 256, 0, stream>>>(in.positions, in.indices, d_inst, d_base,
                                                              in.instance_count, n, plo, phi, seg, recs);
+    if (wide) {
+        Binary bin = build_binary(plo, phi, seg, n, 1, sc);
+        uint32_t* tri_order = sc.get<uint32_t>(n);
+        Build8 b = collapse_wide(bin, n, out.flat_nodes_buf, tri_order, sc);
+        out.flat_nodes = b.nodes;
+        out.flat_levels = b.levels;
+        out.flat_level_start = b.level_start;
+        gather_wide_records_kernel<<<grid_for(n, 256), 256, 0, stream>>>(recs, bin.order, tri_order, n,
+                                                                          out.flat_tris.as<float4>());
+        out.flat_bound = root_bound(bin.roots, bin.blo, bin.bhi, stream);
+        check_cuda(cudaStreamSynchronize(stream), "bvh build");
+        check_cuda(cudaGetLastError(), "bvh build kernels");
+        return;
+    }
     Build4 b = build_bvh4(plo, phi, seg, n, 1, leaf_max, false, nullptr, out.flat_nodes_buf, sc);
     out.flat_nodes = b.nodes;
     out.flat_levels = b.levels;
     out.flat_level_start = b.level_start;
     gather_records_kernel<<<grid_for(n, 256), 256, 0, stream>>>(recs, b.order, n, out.flat_tris.as<float4>());
-    out.flat_bound = root_bound(b, stream);
+    out.flat_bound = root_bound(b.roots, b.blo, b.bhi, stream);
     check_cuda(cudaStreamSynchronize(stream), "bvh build");
     check_cuda(cudaGetLastError(), "bvh build kernels");
 }
@@ -814,6 +1100,7 @@ static float root_node_bound(const DeviceBuffer& nodes, cudaStream_t stream) {
 }
 
 void refit_scene_bvh(const tt_instance* d_instances, cudaStream_t stream, BvhResult& b) {
+    if (b.wide) fail(TT_ERR_UNSUPPORTED, "the compressed wide format is rebuilt, not refitted");
     bool flat = b.flat;
     DeviceBuffer& nodes = flat ? b.flat_nodes_buf : b.tlas;
     const std::vector<uint64_t>& ls = flat ? b.flat_level_start : b.tlas_level_start;
@@ -831,9 +1118,9 @@ void refit_scene_bvh(const tt_instance* d_instances, cudaStream_t stream, BvhRes
     else b.tlas_bound = bound;
 }
 
-void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, BvhResult& out) {
+void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, bool wide, BvhResult& out) {
     if (flat) {
-        build_flat(in, stream, leaf_max, out);
+        build_flat(in, stream, leaf_max, wide, out);
         return;
     }
     Scratch sc(stream);
@@ -903,7 +1190,7 @@ void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bo
         out.tlas_nodes = tb.nodes;
         out.tlas_levels = tb.levels;
         out.tlas_level_start = tb.level_start;
-        out.tlas_bound = root_bound(tb, stream);  // bound of the world-space slab margins
+        out.tlas_bound = root_bound(tb.roots, tb.blo, tb.bhi, stream);  // bound of the world-space slab margins
     } else {
         out.tlas_nodes = 0;
         out.tlas_levels = 0;

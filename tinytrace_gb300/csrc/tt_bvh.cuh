@@ -30,6 +30,16 @@
 
 namespace tt {
 
+// Wide-format traversal variants (build-time switches): NEAREST descends into the nearest hit
+// internal child of each node before its siblings; FAST_DECODE folds the byte-to-float bias of the
+// quantised planes into the slab bases (one instruction less per plane, boxes one step looser).
+#ifndef TT_WIDE_NEAREST
+#define TT_WIDE_NEAREST 0
+#endif
+#ifndef TT_WIDE_FAST_DECODE
+#define TT_WIDE_FAST_DECODE 0
+#endif
+
 constexpr uint32_t CHILD_LEAF = 0x80000000u;
 constexpr uint32_t STACK_MARKER = 0xffffffffu;
 #ifndef TT_TRAVERSAL_STACK
@@ -73,6 +83,7 @@ struct DevScene {
     uint32_t has_tlas;
     float tlas_bound;  // max |coordinate| of the world boxes in `tlas`
     uint32_t flat;     // 1: `tlas`/`tris` hold the flat BVH
+    uint32_t wide;     // 1: the flat BVH is in the compressed 8-wide format (80-byte nodes in `tlas`)
     uint32_t stack_need;  // traversal stack entries the structure can need (3 per level + 1)
     const DevTexture* textures;  // texture table (null when the scene has no textures)
     const uint8_t* tex_data;     // all texture levels
@@ -249,6 +260,10 @@ struct TraceState {
     int sp;
     bool in_blas;  // two-level: inside an instance; flat: the object ray of `inst` is not finite
     bool have, cull;
+    // wide format: the node group being expanded (first child node, and hit slots in visiting
+    // order in bits 24..31 above the node's internal-slot mask) and the pending triangle group
+    // (first record, and the records still to test as a bit mask)
+    uint32_t ng_base, ng_bits, tg_base, tg_bits;
 };
 
 TT_HD void trace_init(TraceState& st, const DevScene& sc, f3 o, f3 d, float tmin, float tmax, bool cull) {
@@ -273,6 +288,18 @@ TT_HD void trace_init(TraceState& st, const DevScene& sc, f3 o, f3 d, float tmin
     st.tri_next = 0u;
     st.tri_left = 0u;
     st.have = finite3(d) && sc.has_tlas != 0u;  // a NaN/inf direction or an empty scene misses
+    // wide format: the root (node 0) as the only member of a group whose slots map to nodes 0..7
+    st.ng_base = 0u;
+    st.ng_bits = (st.have && !TT_WIDE_NEAREST) ? ((1u << (24u + st.nr.near)) | 0xffu) : 0u;  // NEAREST: `cur`
+    st.tg_base = 0u;
+    st.tg_bits = 0u;
+}
+
+// Makes the next trace_step finish with the current result (the ray traces nothing more).
+TT_HD void trace_stop(TraceState& st) {
+    st.have = false;
+    st.ng_bits = 0u;
+    st.tg_bits = 0u;
 }
 
 template <bool COUNT, int STACK = TRAVERSAL_STACK>
@@ -444,13 +471,210 @@ __device__ __forceinline__ bool trace_step_flat(TraceState& st, const DevScene& 
     return !visit_children<STACK>(st, mask, tn, ch, true, stack, stride, err);
 }
 
-// ACCEL: ACCEL_ANY dispatches on the scene at run time; ACCEL_FLAT_ONLY and ACCEL_TWO_LEVEL_ONLY
-// compile one structure's step (the caller has checked sc.flat).
-constexpr int ACCEL_ANY = 0, ACCEL_FLAT_ONLY = 1, ACCEL_TWO_LEVEL_ONLY = 2;
+// ---------------------------------------------------------------- compressed 8-wide format
+// Node (80 bytes, five 16-byte loads): origin xyz and, in the fourth word, the biased exponents
+// of the per-axis scales and the internal-slot mask; child base, triangle base and eight meta
+// bytes (a leaf slot's first record offset | unary record count << 5); then the child boxes as
+// bytes, per axis the eight low planes and the eight high planes.  A child plane is
+// origin + q 2^(exponent - 127); the slab distance enters as fma(q, 2^(e - 127) / d,
+// fma(origin, 1/d, -o/d -+ E)), conservative with the margin E of node_ray.
+//
+// Traversal (after Ylitie, Karras & Laine, HPG 2017): the hit internal children of a node form a
+// node group visited in the order the slots were assigned for the ray's direction octant (slot s
+// at position s ^ octant, lowest position first), the hit leaf children a triangle group (a mask
+// of records).  A step tests at most one record of the pending triangle group and visits at most
+// one node; the remainder of a node group, and a triangle group produced while another is
+// pending, wait on the stack as two-word entries (node groups have hit bits in 24..31, triangle
+// groups do not).
+
+// Byte k of `w` as a float plane coordinate: the bits 0x4b0000bb (byte bb of w below the exponent
+// of 2^23) are the float 2^23 + bb; minus 2^23 unless the caller folds the bias into its bases.
+__device__ __forceinline__ float wide_plane(uint32_t w, uint32_t k) {
+    float biased = __uint_as_float(__byte_perm(w, 0x4bu, 0x4550u | k));
+    return TT_WIDE_FAST_DECODE ? biased : biased - 8388608.0f;
+}
+// Bit i of the result is bit i ^ o of `m` (8 bits).
+__device__ __forceinline__ uint32_t permute_octant(uint32_t m, uint32_t o) {
+    if (o & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (o & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (o & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+    return m;
+}
+
+template <int STACK>
+__device__ __forceinline__ bool wide_push(TraceState& st, uint32_t* stack, int stride, uint32_t* err, uint32_t base,
+                                          uint32_t bits) {
+    if (2 * st.sp + 2 > STACK) {
+        atomicOr(err, ERR_STACK_OVERFLOW);
+        return false;
+    }
+    stack[(2 * st.sp) * stride] = base;
+    stack[(2 * st.sp + 1) * stride] = bits;
+    st.sp++;
+    return true;
+}
+
+template <bool COUNT, int STACK = TRAVERSAL_STACK>
+__device__ __forceinline__ bool trace_step_wide(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
+                                                uint32_t* err, Counters& cnt) {
+    if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {
+        atomicOr(err, ERR_ITERATION_LIMIT);
+        return true;
+    }
+    // 1. one record of the pending triangle group
+    if (st.tg_bits != 0u) {
+        uint32_t j = (uint32_t)(__ffs(st.tg_bits) - 1);
+        st.tg_bits &= st.tg_bits - 1u;
+        const float4* tr = sc.tris + 3ull * (st.tg_base + j);
+        float4 a = __ldg(tr + 0), b = __ldg(tr + 1), cc = __ldg(tr + 2);
+        uint32_t prim = __float_as_uint(a.w), inst = __float_as_uint(b.w);
+        if (inst != st.inst) {
+            f3 oo, od;
+            uint32_t mesh;
+            instance_ray(sc, inst, st.o, st.d, oo, od, mesh);
+            st.inst = inst;
+            st.in_blas = !finite3(od);
+            st.rp = ray_precompute(oo, od);
+            if (COUNT) cnt.instances++;
+        }
+        if (COUNT) cnt.triangles++;
+        float t, u, v;
+        bool better = !st.in_blas &&
+                      intersect_triangle(st.rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), st.cull, st.tmin,
+                                         st.tbest, t, u, v) &&
+                      closer(t, st.inst, prim, st.best);
+        st.best.hit = better ? 1 : st.best.hit;
+        st.best.t = better ? t : st.best.t;
+        st.best.u = better ? u : st.best.u;
+        st.best.v = better ? v : st.best.v;
+        st.best.instance = better ? st.inst : st.best.instance;
+        st.best.prim = better ? prim : st.best.prim;
+        st.tbest = better ? t : st.tbest;
+    }
+    // 2. the next node: the pending nearest child, else the next child of the node group, else
+    // the stack
+    uint32_t node;
+    if (TT_WIDE_NEAREST && st.have) {
+        node = st.cur;
+        st.have = false;
+    } else {
+        if ((st.ng_bits >> 24) == 0u) {
+            if (st.sp == 0) return st.tg_bits == 0u;
+            uint32_t base = stack[(2 * st.sp - 2) * stride], bits = stack[(2 * st.sp - 1) * stride];
+            if ((bits >> 24) == 0u) {  // a triangle group: it becomes pending once the current one is done
+                if (st.tg_bits != 0u) return false;
+                --st.sp;
+                st.tg_base = base;
+                st.tg_bits = bits;
+                return false;
+            }
+            --st.sp;
+            st.ng_base = base;
+            st.ng_bits = bits;
+        }
+        uint32_t pos = (uint32_t)(__ffs(st.ng_bits >> 24) - 1);
+        st.ng_bits &= ~(1u << (24u + pos));
+        uint32_t slot = pos ^ st.nr.near;
+        node = st.ng_base + (uint32_t)__popc(st.ng_bits & 0xffu & ((1u << slot) - 1u));
+        if (!TT_WIDE_NEAREST && (st.ng_bits >> 24) != 0u &&
+            !wide_push<STACK>(st, stack, stride, err, st.ng_base, st.ng_bits))
+            return true;
+    }
+    if (COUNT) cnt.tlas_nodes++;
+    const uint4* nd = sc.tlas + 5ull * node;
+    uint4 w0 = __ldg(nd + 0), w1 = __ldg(nd + 1), qx = __ldg(nd + 2), qy = __ldg(nd + 3), qz = __ldg(nd + 4);
+    const float ia[3] = {st.nr.inv.x, st.nr.inv.y, st.nr.inv.z};
+    const float nn[3] = {st.nr.nob_near.x, st.nr.nob_near.y, st.nr.nob_near.z};
+    const float nf[3] = {st.nr.nob_far.x, st.nr.nob_far.y, st.nr.nob_far.z};
+    const float org[3] = {__uint_as_float(w0.x), __uint_as_float(w0.y), __uint_as_float(w0.z)};
+    const uint4 q[3] = {qx, qy, qz};
+    float step[3], bn[3], bf[3];
+    uint32_t qn[3][2], qf[3][2];  // near / far plane bytes per axis, slots 0..3 and 4..7
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        step[a] = __uint_as_float(((w0.w >> (8 * a)) & 0xffu) << 23) * ia[a];
+        bn[a] = __fmaf_rn(org[a], ia[a], nn[a]);
+        bf[a] = __fmaf_rn(org[a], ia[a], nf[a]);
+        if (TT_WIDE_FAST_DECODE) {
+            // planes enter as the biased floats 2^23 + q: fold -2^23 step into the bases and widen
+            // them by one quantisation step, which covers the rounding of the folded bases
+            float big = step[a] * 8388608.0f, one = fabsf(step[a]);
+            bn[a] = (bn[a] - big) - one;
+            bf[a] = (bf[a] - big) + one;
+        }
+        bool neg = (st.nr.near >> a) & 1u;  // the near plane is the high one
+        qn[a][0] = neg ? q[a].z : q[a].x;
+        qn[a][1] = neg ? q[a].w : q[a].y;
+        qf[a][0] = neg ? q[a].x : q[a].z;
+        qf[a][1] = neg ? q[a].y : q[a].w;
+    }
+    const uint32_t imask = w0.w >> 24;
+    const uint32_t meta[2] = {w1.z, w1.w};
+    uint32_t hit = 0u, tmask = 0u;
+    float tnear[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        uint32_t h = c >> 2, k = c & 3;
+        float tn = fmx(fmx(__fmaf_rn(wide_plane(qn[0][h], k), step[0], bn[0]),
+                           __fmaf_rn(wide_plane(qn[1][h], k), step[1], bn[1])),
+                       fmx(__fmaf_rn(wide_plane(qn[2][h], k), step[2], bn[2]), st.tmin));
+        float tf = fmn(fmn(__fmaf_rn(wide_plane(qf[0][h], k), step[0], bf[0]),
+                           __fmaf_rn(wide_plane(qf[1][h], k), step[1], bf[1])),
+                       fmn(__fmaf_rn(wide_plane(qf[2][h], k), step[2], bf[2]), st.tbest));
+        tnear[c] = tn;
+        uint32_t m = (meta[h] >> (8 * k)) & 0xffu;
+        bool valid = ((imask >> c) & 1u) || m != 0u;
+        bool in = valid && tn <= tf;
+        hit |= in ? (1u << c) : 0u;
+        bool leaf = in && !((imask >> c) & 1u);
+        tmask |= leaf ? ((m >> 5) << (m & 31u)) : 0u;
+    }
+    uint32_t ihit = hit & imask;
+    if (TT_WIDE_NEAREST) {
+        // descend into the nearest internal child next; its hit siblings form the new node group
+        int best = -1;
+        float bt = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            bool take = ((ihit >> c) & 1u) && (best < 0 || tnear[c] < bt);
+            best = take ? c : best;
+            bt = take ? tnear[c] : bt;
+        }
+        if (best >= 0) {
+            uint32_t rest = ihit & ~(1u << best);
+            if (rest != 0u) {
+                if ((st.ng_bits >> 24) != 0u && !wide_push<STACK>(st, stack, stride, err, st.ng_base, st.ng_bits))
+                    return true;
+                st.ng_base = w1.x;
+                st.ng_bits = (permute_octant(rest, st.nr.near) << 24) | imask;
+            }
+            st.cur = w1.x + (uint32_t)__popc(imask & ((1u << best) - 1u));
+            st.have = true;
+        }
+    } else {
+        st.ng_base = w1.x;
+        st.ng_bits = (permute_octant(ihit, st.nr.near) << 24) | imask;
+    }
+    if (tmask != 0u) {
+        if (st.tg_bits == 0u) {
+            st.tg_base = w1.y;
+            st.tg_bits = tmask;
+        } else if (!wide_push<STACK>(st, stack, stride, err, w1.y, tmask)) {
+            return true;
+        }
+    }
+    return false;
+}
+
+// ACCEL: ACCEL_ANY dispatches on the scene at run time; ACCEL_FLAT_ONLY, ACCEL_TWO_LEVEL_ONLY and
+// ACCEL_WIDE_ONLY compile one structure's step (the caller has checked sc.flat and sc.wide).
+constexpr int ACCEL_ANY = 0, ACCEL_FLAT_ONLY = 1, ACCEL_TWO_LEVEL_ONLY = 2, ACCEL_WIDE_ONLY = 3;
 
 template <bool COUNT, int ACCEL = ACCEL_ANY, bool EARLY = false, int STACK = TRAVERSAL_STACK>
 __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
                                            uint32_t* err, Counters& cnt) {
+    if (ACCEL == ACCEL_WIDE_ONLY || (ACCEL == ACCEL_ANY && sc.wide))
+        return trace_step_wide<COUNT, STACK>(st, sc, stack, stride, err, cnt);
     if (ACCEL == ACCEL_FLAT_ONLY || (ACCEL == ACCEL_ANY && sc.flat))
         return trace_step_flat<COUNT, EARLY, STACK>(st, sc, stack, stride, err, cnt);
     if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {

@@ -47,9 +47,11 @@ struct BvhResult {
     uint32_t blas_levels = 0, tlas_levels = 0;
     float tlas_bound = 0.0f;  // max |coordinate| of the instance world boxes
     std::vector<uint64_t> tlas_level_start, flat_level_start;  // first node of each level (+ end)
-    // single-level BVH over the world boxes of every (instance, triangle) pair
+    // single-level BVH over the world boxes of every (instance, triangle) pair; `wide`: its nodes
+    // are in the compressed 8-wide format (80-byte nodes, records in the wide order)
     bool flat = false;
-    DeviceBuffer flat_nodes_buf;  // 128-byte BVH4 nodes
+    bool wide = false;
+    DeviceBuffer flat_nodes_buf;  // 128-byte BVH4 nodes (80-byte wide nodes when `wide`)
     DeviceBuffer flat_tris;       // 48-byte records: object-space vertices, primitive, instance
     uint64_t flat_nodes = 0, flat_tri_count = 0;
     uint32_t flat_levels = 0;
@@ -70,8 +72,9 @@ void set_last_error(const std::string& message);
 
 // Builds, on `stream`, either the two-level structure (BLAS with one root per mesh, node index
 // == mesh index, and TLAS with root 0) or, when `flat`, one BVH over the world boxes of all
-// (instance, triangle) pairs (root 0).
-void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, BvhResult& out);
+// (instance, triangle) pairs (root 0), in BVH4 nodes or, when `wide`, in the compressed 8-wide
+// format.
+void build_scene_bvh(const BuildInput& in, cudaStream_t stream, int leaf_max, bool flat, bool wide, BvhResult& out);
 
 // Refits the world-space structure (the flat BVH, or the TLAS) to new instance transforms
 // (device array `d_instances`), keeping its topology; updates the slab-margin bound.

@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                         uint32_t exact = __float_as_uint(w.pa0[slot].w);
                         int mode = shadow_target(sc, light, hash, exact, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX,
                                                  st.best, st.tbest);
-                        if (mode == 0) st.have = false;  // not visible: the first step finishes
+                        if (mode == 0) trace_stop(st);  // not visible: the first step finishes
                         seeded = mode == 1;
                         target_prim = st.best.prim;
                     }
@@ -494,7 +494,12 @@ template <bool SHADOW>
 // kernels always use the full stack.
 static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid, bool counted, cudaStream_t st) {
     bool short_stack = !counted && p.sc.stack_need <= (uint32_t)SHORT_TRAVERSAL_STACK;
-    if (p.sc.flat) {
+    if (p.sc.wide) {
+        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_WIDE_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+        else if (short_stack)
+            wf_trace_kernel<false, SHADOW, ACCEL_WIDE_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w);
+        else wf_trace_kernel<false, SHADOW, ACCEL_WIDE_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+    } else if (p.sc.flat) {
         if (counted) wf_trace_kernel<true, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
         else if (short_stack)
             wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w);

@@ -56,6 +56,7 @@ TT_OPTION_ACCEL = 3
 TT_ACCEL_AUTO = 0
 TT_ACCEL_FLAT = 1
 TT_ACCEL_TWO_LEVEL = 2
+TT_ACCEL_FLAT_WIDE = 3
 TT_OPTION_STAGE_TIMING = 4
 TT_OPTION_GRAPHS = 5
 TT_REQUEST_QUEUED = 0
@@ -133,6 +134,11 @@ CONSTANTS_DTYPE = np.dtype([("view", "<f4", (16,)), ("proj", "<f4", (16,)), ("pr
 NODE4_DTYPE = np.dtype([("box", "<f4", (6, 4)), ("child", "<u4", (4,)), ("count", "<u4"), ("pad", "<u4", (3,))])
 TRI_RECORD_DTYPE = np.dtype([("v0", "<f4", (3,)), ("prim", "<u4"), ("v1", "<f4", (3,)), ("mesh", "<u4"),
                              ("v2", "<f4", (3,)), ("pad", "<u4")])
+# compressed 8-wide node of the flat structure (TT_ACCEL_FLAT_WIDE), 80 bytes
+NODE8_DTYPE = np.dtype([("origin", "<f4", (3,)), ("exponent", "u1", (3,)), ("imask", "u1"), ("child_base", "<u4"),
+                        ("tri_base", "<u4"), ("meta", "u1", (8,)), ("qlo_x", "u1", (8,)), ("qhi_x", "u1", (8,)),
+                        ("qlo_y", "u1", (8,)), ("qhi_y", "u1", (8,)), ("qlo_z", "u1", (8,)), ("qhi_z", "u1", (8,))])
+assert NODE8_DTYPE.itemsize == 80
 
 assert MATERIAL_CONSTANTS_DTYPE.itemsize == 192
 assert MATERIAL_DTYPE.itemsize == 304

@@ -55,6 +55,13 @@ class RenderServer:
             raise native.TinytraceError(native.TT_ERR_DEVICE, self.lib.tt_last_error().decode())
         return self._outputs[request]
 
+    def release(self, request: int) -> np.ndarray | None:
+        """Drops the server's reference to a finished request's image buffer (returned)."""
+        st, _ = self.status(request)
+        if st < native.TT_REQUEST_DONE:
+            raise native.TinytraceError(native.TT_ERR_INVALID_ARGUMENT, "the request is still queued or running")
+        return self._outputs.pop(request, None)
+
     def stats(self) -> native.ServerStats:
         s = native.ServerStats()
         check(self.lib.tt_server_stats_get(self.handle, ctypes.byref(s)))
