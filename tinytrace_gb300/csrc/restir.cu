@@ -20,18 +20,29 @@ __device__ __forceinline__ bool pixel_of_thread(const tt_constants& c, uint32_t&
     return x < c.screen_size[0] && y < c.screen_size[1];
 }
 
-// Appends pred lanes of the calling (possibly partial) warp to a queue: one atomic per warp.
-__device__ __forceinline__ uint32_t queue_append(uint32_t* counter, bool pred) {
-    uint32_t active = __activemask();
-    uint32_t mask = __ballot_sync(active, pred);
-    uint32_t lane = threadIdx.x & 31u;
-    uint32_t base = 0u;
-    if (mask) {
-        uint32_t leader = (uint32_t)(__ffs(mask) - 1);
-        if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
-        base = __shfl_sync(active, base, leader);
+// Appends each thread's pixel to its bucket's queue (bucket == HIT_BUCKETS: to none).  Warp
+// ballots count the block's pixels per bucket in shared memory, and one thread per bucket takes
+// the block's range of the queue with a single global atomic, so the four counters see one
+// atomic per block instead of one per warp.  Every thread of the block must call it.
+__device__ __forceinline__ void block_queue_append(const RestirParams& rp, uint32_t bucket, uint32_t pixel,
+                                                   uint64_t WH) {
+    __shared__ uint32_t s_count[HIT_BUCKETS], s_base[HIT_BUCKETS];
+    if (threadIdx.x < HIT_BUCKETS) s_count[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t lane = threadIdx.x & 31u, pos = 0u;
+#pragma unroll
+    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
+        uint32_t mask = __ballot_sync(0xffffffffu, bucket == b);
+        uint32_t wbase = 0u;
+        if (lane == 0u && mask != 0u) wbase = atomicAdd(&s_count[b], (uint32_t)__popc(mask));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        if (bucket == b) pos = wbase + (uint32_t)__popc(mask & ((1u << lane) - 1u));
     }
-    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+    __syncthreads();
+    if (threadIdx.x < HIT_BUCKETS)
+        s_base[threadIdx.x] = s_count[threadIdx.x] ? atomicAdd(rp.queue_count + threadIdx.x, s_count[threadIdx.x]) : 0u;
+    __syncthreads();
+    if (bucket < HIT_BUCKETS) rp.queue[(uint64_t)bucket * WH + s_base[bucket] + pos] = pixel;
 }
 
 // Pixel of queue entry q: the bucket queues are concatenated in bucket order.
@@ -107,14 +118,13 @@ __device__ __forceinline__ float target_of(const DevScene& sc, const ShadingStat
     return luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
 }
 
+// The G-buffer pass for pixel (x, y); returns the material bucket of its primary hit, or
+// HIT_BUCKETS for a sky pixel (finished here).
 template <bool TEX>
-__global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
-                                                                  const __grid_constant__ RestirParams rp,
-                                                                  Surface* gbuf, float4* gtex, float4* glob) {
-    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
-    uint32_t x, y;
+__device__ __forceinline__ uint32_t gbuffer_pixel(const RenderParams& p, const RestirParams& rp, Surface* gbuf,
+                                                  float4* gtex, float4* glob, uint32_t x, uint32_t y,
+                                                  uint32_t* s_stack) {
     const tt_constants& c = p.c;
-    if (!pixel_of_thread(c, x, y)) return;
     const DevScene& sc = p.sc;
     uint32_t W = c.screen_size[0], H = c.screen_size[1];
     uint32_t g = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
@@ -129,11 +139,6 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     // surface pixels go to their material bucket's queue for the candidate and shade passes; sky
     // pixels are finished here: empty initial reservoir, the white sky (integrate.glsl:272-276)
     uint32_t bucket = h.hit ? (uint32_t)__ldg(sc.inst_bucket + h.instance) : HIT_BUCKETS;
-#pragma unroll
-    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
-        uint32_t pos = queue_append(&rp.queue_count[b], bucket == b);
-        if (bucket == b) rp.queue[(uint64_t)b * W * H + pos] = (uint32_t)i;
-    }
     if (!h.hit) {
         rp.initial[i] = empty_reservoir();
         write_target(p, i, splat(1.0f));
@@ -161,6 +166,21 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
         store_lobes(glob + LOBE_RECORD * ((uint64_t)y * W + x), bsdf_prepare(mc, wi, gp));
     }
     gbuf[(uint64_t)y * W + x] = s;
+    return bucket;
+}
+
+template <bool TEX>
+__global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
+                                                                  const __grid_constant__ RestirParams rp,
+                                                                  Surface* gbuf, float4* gtex, float4* glob) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
+    const tt_constants& c = p.c;
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    // threads outside the image take part in the block's queue append only
+    uint32_t bucket = HIT_BUCKETS;
+    if (pixel_of_thread(c, x, y)) bucket = gbuffer_pixel<TEX>(p, rp, gbuf, gtex, glob, x, y, s_stack);
+    block_queue_append(rp, bucket, y * W + x, (uint64_t)W * H);
 }
 
 template <bool TEX>
