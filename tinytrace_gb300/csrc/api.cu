@@ -1311,10 +1311,13 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
             R.initial.alloc(32ull * WH);
             R.temporal.alloc(32ull * WH);
             R.glob.alloc(16ull * LOBE_RECORD * WH);
-            R.queue.alloc(4ull * HIT_BUCKETS * WH);
-            R.queue_count.alloc(4ull * HIT_BUCKETS);
             R.pixels = WH;
             R.history.valid = 0u;
+        }
+        uint64_t tiles = (uint64_t)((img->width + 15u) / 16u) * ((img->height + 7u) / 8u);  // the passes' 16 x 8 tiles
+        if (R.queue_count.bytes < 4ull * tiles) {
+            R.queue.alloc(4ull * 128ull * tiles);
+            R.queue_count.alloc(4ull * tiles);
         }
         RenderParams p;
         p.sc = s->dev;

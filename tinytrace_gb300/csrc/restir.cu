@@ -20,44 +20,42 @@ __device__ __forceinline__ bool pixel_of_thread(const tt_constants& c, uint32_t&
     return x < c.screen_size[0] && y < c.screen_size[1];
 }
 
-// Appends each thread's pixel to its bucket's queue (bucket == HIT_BUCKETS: to none).  Warp
-// ballots count the block's pixels per bucket in shared memory, and one thread per bucket takes
-// the block's range of the queue with a single global atomic, so the four counters see one
-// atomic per block instead of one per warp.  Every thread of the block must call it.
-__device__ __forceinline__ void block_queue_append(const RestirParams& rp, uint32_t bucket, uint32_t pixel,
-                                                   uint64_t WH) {
-    __shared__ uint32_t s_count[HIT_BUCKETS], s_base[HIT_BUCKETS];
-    if (threadIdx.x < HIT_BUCKETS) s_count[threadIdx.x] = 0u;
-    __syncthreads();
-    uint32_t lane = threadIdx.x & 31u, pos = 0u;
+// Tile queues: the G-buffer block of each 16 x 8 tile lists the tile's surface pixels, sorted
+// by material bucket, in its own RT_BLOCK entries of `queue` and their number in
+// queue_count[tile] (no atomics), so that the candidate and shade blocks of the tile run only
+// warps of surface pixels whose lanes mostly share a lobe set.  Every thread of the block must
+// call it; bucket == HIT_BUCKETS lists nothing (sky pixels and threads outside the image).
+__device__ __forceinline__ void tile_queue_write(const RestirParams& rp, uint32_t bucket, uint32_t pixel) {
+    constexpr uint32_t WARPS = RT_BLOCK / 32;
+    __shared__ uint32_t s_wc[HIT_BUCKETS][WARPS];
+    uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, below = 0u;
 #pragma unroll
     for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
         uint32_t mask = __ballot_sync(0xffffffffu, bucket == b);
-        uint32_t wbase = 0u;
-        if (lane == 0u && mask != 0u) wbase = atomicAdd(&s_count[b], (uint32_t)__popc(mask));
-        wbase = __shfl_sync(0xffffffffu, wbase, 0);
-        if (bucket == b) pos = wbase + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+        if (lane == 0u) s_wc[b][warp] = (uint32_t)__popc(mask);
+        if (bucket == b) below = (uint32_t)__popc(mask & ((1u << lane) - 1u));
     }
     __syncthreads();
-    if (threadIdx.x < HIT_BUCKETS)
-        s_base[threadIdx.x] = s_count[threadIdx.x] ? atomicAdd(rp.queue_count + threadIdx.x, s_count[threadIdx.x]) : 0u;
-    __syncthreads();
-    if (bucket < HIT_BUCKETS) rp.queue[(uint64_t)bucket * WH + s_base[bucket] + pos] = pixel;
+    uint32_t pos = below, total = 0u;
+#pragma unroll
+    for (uint32_t b = 0; b < HIT_BUCKETS; ++b)
+#pragma unroll
+        for (uint32_t k = 0; k < WARPS; ++k) {
+            uint32_t n = s_wc[b][k];
+            pos += (b < bucket || (b == bucket && k < warp)) ? n : 0u;
+            total += n;
+        }
+    uint64_t tile = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x;
+    if (bucket < HIT_BUCKETS) rp.queue[tile * RT_BLOCK + pos] = pixel;
+    if (threadIdx.x == 0) rp.queue_count[tile] = total;
 }
 
-// Pixel of queue entry q: the bucket queues are concatenated in bucket order.
-__device__ __forceinline__ bool queued_pixel(const RestirParams& rp, uint32_t WH, uint32_t q, uint64_t& i) {
-    uint32_t start = 0u;
-#pragma unroll
-    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
-        uint32_t n = rp.queue_count[b];
-        if (q < start + n) {
-            i = rp.queue[(uint64_t)b * WH + (q - start)];
-            return true;
-        }
-        start += n;
-    }
-    return false;
+// Pixel of this thread in its tile's queue, or false (the tile has fewer surface pixels).
+__device__ __forceinline__ bool queued_pixel(const RestirParams& rp, uint64_t& i) {
+    uint64_t tile = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x;
+    if (threadIdx.x >= rp.queue_count[tile]) return false;
+    i = rp.queue[tile * RT_BLOCK + threadIdx.x];
+    return true;
 }
 
 // The accumulation rule of tt_render for one pixel of the target.
@@ -180,7 +178,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     // threads outside the image take part in the block's queue append only
     uint32_t bucket = HIT_BUCKETS;
     if (pixel_of_thread(c, x, y)) bucket = gbuffer_pixel<TEX>(p, rp, gbuf, gtex, glob, x, y, s_stack);
-    block_queue_append(rp, bucket, y * W + x, (uint64_t)W * H);
+    tile_queue_write(rp, bucket, y * W + x);
 }
 
 template <bool TEX>
@@ -191,7 +189,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_c
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     const tt_constants& c = p.c;
     uint64_t i = 0;
-    if (!queued_pixel(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i)) return;
+    if (!queued_pixel(rp, i)) return;
     const DevScene& sc = p.sc;
     ShadingState st;
     Reservoir r = empty_reservoir();
@@ -350,7 +348,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     const tt_constants& c = p.c;
     uint64_t i = 0;
-    if (!queued_pixel(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i)) return;
+    if (!queued_pixel(rp, i)) return;
     const DevScene& sc = p.sc;
     ShadingState st;
     f3 radiance;
@@ -373,14 +371,11 @@ template <bool TEX>
 static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer) {
     const tt_constants& c = p.c;
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
-    uint64_t WH = (uint64_t)c.screen_size[0] * c.screen_size[1];
-    unsigned qgrid = (unsigned)((WH + RT_BLOCK - 1) / RT_BLOCK);  // enough blocks for every pixel queued
-    check_cuda(cudaMemsetAsync(rp.queue_count, 0, 4ull * HIT_BUCKETS, st), "memset");
     stage_begin(timer, TT_STAGE_RESTIR_GBUFFER, st);
     restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_INITIAL, st);
-    restir_initial_kernel<TEX><<<qgrid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
+    restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_TEMPORAL, st);
     restir_temporal_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.glob, rp.prev_gbuf,
@@ -391,7 +386,7 @@ static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStr
                                                           rp.neighbours, rp.radius);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_SHADE, st);
-    restir_shade_kernel<TEX><<<qgrid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
+    restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
     stage_end(timer, st);
 }
 

@@ -48,12 +48,13 @@ class RenderServer:
         return st.value, lat.value
 
     def wait(self, request: int, timeout_ms: int = 600_000) -> np.ndarray:
-        """Blocks until the request is done; returns its image (raises if it failed)."""
+        """Blocks until the request is done; returns its image, or None once `release` dropped it
+        (raises if it failed)."""
         st = ctypes.c_int32()
         check(self.lib.tt_server_wait(self.handle, request, timeout_ms, ctypes.byref(st)))
         if st.value != native.TT_REQUEST_DONE:
             raise native.TinytraceError(native.TT_ERR_DEVICE, self.lib.tt_last_error().decode())
-        return self._outputs[request]
+        return self._outputs.get(request)
 
     def release(self, request: int) -> np.ndarray | None:
         """Drops the server's reference to a finished request's image buffer (returned)."""
