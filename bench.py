@@ -821,13 +821,16 @@ def serve_requests(rng, pool, logs, n: int, first_frame: int):
     return reqs
 
 
-def serve_run(ctx, reqs, rate: float | None, rng) -> dict:
+SERVE_INFLIGHT = 16  # requests rendered together per round
+
+
+def serve_run(ctx, reqs, rate: float | None, rng, pool_paths: int) -> dict:
     """Submits `reqs` (Poisson arrivals at `rate` per second, or all at once when rate is None),
     waits for all of them and returns latency percentiles and throughput.  Finished requests'
     image buffers are released as the run goes."""
     from tinytrace_gb300.server import RenderServer
 
-    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=8) as srv:
+    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=SERVE_INFLIGHT, pool_paths=pool_paths) as srv:
         t0 = time.perf_counter()
         due = t0
         ids, pending = [], []
@@ -859,19 +862,29 @@ def serve_run(ctx, reqs, rate: float | None, rng) -> dict:
             "first_tenth_mean_ms": float(lat[:tenth].mean()), "last_tenth_mean_ms": float(lat[-tenth:].mean()),
             "completed_per_s": len(ids) / makespan, "offered_per_s": len(ids) / (submit_end - t0) if rate else None,
             "throughput_msamples_s": samples / makespan / 1e6, "peak_inflight": int(st.peak_inflight),
-            "failed": int(st.failed), "makespan_s": makespan}
+            "failed": int(st.failed), "makespan_s": makespan,
+            "rounds": int(st.rounds), "mean_round_items": st.round_items / max(1, st.rounds),
+            "gpu_busy_frac": st.gpu_busy_ns / 1e9 / makespan,
+            "msamples_s_while_busy": samples / max(1e-9, st.gpu_busy_ns / 1e9) / 1e6,
+            "scheduler_s": {"admit": st.admit_ns / 1e9, "launch": st.launch_ns / 1e9,
+                            "copy_out": st.copy_out_ns / 1e9, "wait": st.wait_ns / 1e9}}
 
 
 def run_serving(a, ctx) -> dict:
     """Continuous batching under the C4 request mix on five resident scenes (1e3 .. 5e6
-    triangles), HBM budget 150 GB, 8 execution slots.  First the server's capacity: a batch of
+    triangles), HBM budget 150 GB, up to 16 requests rendered together per round through one
+    shared path pool whose size tt_autotune picks on a request of the mix (the 260k-triangle
+    scene at 1024 x 1024, 4 spp, depth 8).  First the server's capacity: a batch of
     a.serve_batch requests submitted at once (completions per second over the makespan).  Then
     Poisson arrivals at fractions of that capacity: a.serve_requests requests at 0.8 x capacity and
     a quarter as many at 0.5 x and 1.1 x; a rate is sustained when its completions keep pace with
     its arrivals (completed per second >= 0.95 x offered) and the latency does not grow over the
     run (mean latency of the last tenth of the requests <= 1.5 x that of the first tenth)."""
-    from tinytrace_gb300 import scenes
-    from tinytrace_gb300.renderer import SceneArrays
+    import ctypes
+
+    from tinytrace_gb300 import native, scenes
+    from tinytrace_gb300.native import check
+    from tinytrace_gb300.renderer import Config, SceneArrays, make_constants
 
     rng = np.random.default_rng(2024)
     pool = []
@@ -880,17 +893,26 @@ def run_serving(a, ctx) -> dict:
                                                  seed=100 + inst))
         pool.append((arr.triangle_count, ctx.create_scene(arr)))
     logs = np.log10([t for t, _ in pool])
-    out = {"scenes_triangles": [int(t) for t, _ in pool], "hbm_budget_gb": 150, "max_inflight": 8,
+    cam = scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0))
+    img = ctx.create_image(native.TT_LIFETIME_FRAME, 1024, 1024)
+    tune = native.TuneResult()
+    c = make_constants(cam, (1024, 1024), Config(bounce_count=8, sample_count=4), 0, 0)
+    check(ctx.lib.tt_autotune(ctx.handle, pool[2][1], native.ptr(c), img, ctypes.byref(tune)))
+    pool_paths = int(tune.slots)
+    out = {"scenes_triangles": [int(t) for t, _ in pool], "hbm_budget_gb": 150, "max_inflight": SERVE_INFLIGHT,
+           "pool_paths": pool_paths, "pool_tuning": {"tune_spp": 4, "default_ms": tune.default_ms,
+                                                     "tuned_ms": tune.best_ms, "renders": int(tune.renders)},
+           "round_items": 1 << 26,
            "mix": "side ~U{256..2048} step 16, spp ~U{1..256}, depth 8, scene log-uniform 1e3..5e6 triangles"}
-    serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng)  # warm-up: graphs, pool, caches
-    cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng)
+    serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng, pool_paths)  # warm-up: graphs, pool, caches
+    cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng, pool_paths)
     mu = cap["completed_per_s"]
     out["capacity"] = cap
     out["capacity_per_s"] = mu
     out["rates"] = []
     frame = 10_000
     for frac, n in ((0.5, max(32, a.serve_requests // 4)), (0.8, a.serve_requests), (1.1, max(32, a.serve_requests // 4))):
-        res = serve_run(ctx, serve_requests(rng, pool, logs, n, frame), frac * mu, rng)
+        res = serve_run(ctx, serve_requests(rng, pool, logs, n, frame), frac * mu, rng, pool_paths)
         frame += n
         res["fraction_of_capacity"] = frac
         res["sustained"] = bool(res["completed_per_s"] >= 0.95 * res["offered_per_s"]

@@ -470,21 +470,29 @@ int32_t tt_cache_status_get(tt_context* ctx, tt_cache_status* out);
  * Continuous-batching render server (no reference counterpart: the reference renders one frame
  * at a time on the caller's thread).  Scenes are created on the server's context beforehand and
  * stay resident; while a server lives, the caller neither clears the scene lifetime nor uses the
- * context from another thread.  Submitted requests (scene + constants) queue in arrival order; a
- * scheduler thread admits the head of the queue whenever an execution slot is free and its
- * device memory fits in the HBM budget next to the requests already in flight, runs it as one
- * CUDA graph (the wavefront integrator's device-side loop) on the slot's own stream, so that
- * admitted requests overlap on the device, copies the image into the caller's buffer and marks
- * the request done.  A request's image is the same, bit for bit, alone or among others. */
+ * context from another thread.  Submitted requests (scene + constants) queue in arrival order.
+ * A scheduler thread renders the admitted requests together in rounds: each round takes the
+ * next sample chunk of every admitted request (round_items work items in total, shared evenly)
+ * and traces them through one shared wavefront path pool and one set of persistent kernels
+ * (one CUDA graph launch per round).  Between rounds it retires finished requests, copying their
+ * images into the callers' buffers while the next round renders, and admits the head of the
+ * queue while the batch has room and the request's device memory fits in the HBM budget next to
+ * the requests already admitted.  A request's image is the same, bit for bit, alone or among
+ * others. */
 typedef struct tt_server tt_server;
 typedef struct tt_server_config {
-    uint64_t hbm_budget_bytes;  /* device memory in-flight requests may hold (0 = 150 GB) */
-    uint32_t max_inflight;      /* execution slots (0 = 8) */
-    uint32_t paths_per_request; /* wavefront paths in flight per request (0 = 2^20) */
+    uint64_t hbm_budget_bytes; /* device memory admitted requests may hold (0 = 150 GB); the
+                                  shared pool (236 bytes per path slot) is allocated once, apart */
+    uint32_t max_inflight;     /* requests rendered together (0 = 16, at most 64) */
+    uint32_t pool_paths;       /* path slots of the shared wavefront pool (0 = 2^21, at most 2^24) */
+    uint64_t round_items;      /* (pixel, sample) work items per round across the batch (0 = 2^26) */
 } tt_server_config;
 typedef struct tt_server_stats {
     uint64_t submitted, completed, failed, queued, inflight;
     uint64_t bytes_in_flight, peak_bytes_in_flight, peak_inflight;
+    /* rounds rendered, their work items, their device time (CUDA events around each round), and
+     * the scheduler thread's time admitting, launching, copying images out and waiting for rounds */
+    uint64_t rounds, round_items, gpu_busy_ns, admit_ns, launch_ns, copy_out_ns, wait_ns;
 } tt_server_stats;
 #define TT_REQUEST_QUEUED 0
 #define TT_REQUEST_RUNNING 1
@@ -494,7 +502,8 @@ int32_t tt_server_create(tt_context* ctx, const tt_server_config* config, tt_ser
 /* Finishes the queued and in-flight requests, then stops the scheduler. */
 int32_t tt_server_destroy(tt_server* server);
 /* host_rgba32f: width * height * 16 bytes, written when the request completes; it must stay
- * valid until then.  constants.sample_count and bounce_count must be at least 1. */
+ * valid until then.  constants.sample_count and bounce_count must be at least 1, bounce_count
+ * below 65536, and the image at most 4096 x 4096 pixels. */
 int32_t tt_server_submit(tt_server* server, tt_handle scene, const tt_constants* constants, float* host_rgba32f,
                          uint64_t bytes, uint64_t* request_id);
 /* Status (TT_REQUEST_*) and, once done, submit-to-completion latency in milliseconds. */

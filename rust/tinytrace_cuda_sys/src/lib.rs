@@ -358,7 +358,8 @@ pub struct tt_cache_status {
 pub struct tt_server_config {
     pub hbm_budget_bytes: u64,
     pub max_inflight: u32,
-    pub paths_per_request: u32,
+    pub pool_paths: u32,
+    pub round_items: u64,
 }
 
 #[repr(C)]
@@ -372,6 +373,13 @@ pub struct tt_server_stats {
     pub bytes_in_flight: u64,
     pub peak_bytes_in_flight: u64,
     pub peak_inflight: u64,
+    pub rounds: u64,
+    pub round_items: u64,
+    pub gpu_busy_ns: u64,
+    pub admit_ns: u64,
+    pub launch_ns: u64,
+    pub copy_out_ns: u64,
+    pub wait_ns: u64,
 }
 
 #[link(name = "tinytrace_cuda")]

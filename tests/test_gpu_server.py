@@ -1,6 +1,8 @@
-"""The continuous-batching server (tt_server_*) on the GPU: every request's image equals the same
-request rendered alone through tt_render (bit for bit), several requests are in flight at once,
-admission respects the HBM budget, and bad requests fail cleanly."""
+"""The continuous-batching server (tt_server_*) on the GPU: requests of different scenes,
+acceleration structures, resolutions, sample and bounce counts rendered together through the
+shared path pool, over many rounds, give each request's image exactly as tt_render gives it
+alone (bit for bit); several requests are in flight at once, admission respects the HBM budget,
+and bad requests fail cleanly."""
 import ctypes
 
 import numpy as np
@@ -27,21 +29,34 @@ def ctx():
 
 
 def _scenes():
+    field = SceneArrays(scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11))
+    field_cam = scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0))
     return {
-        "cornell": (SceneArrays(scenes.cornell_box()), scenes.cornell_workload().camera),
-        "field": (SceneArrays(scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11)),
-                  scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0))),
-        "instanced": (SceneArrays(scenes.instanced_spheres()), scenes.Camera.looking_at((0.0, 6.0, 40.0), (0, 0, 0))),
+        "cornell": (SceneArrays(scenes.cornell_box()), scenes.cornell_workload().camera, native.TT_ACCEL_AUTO),
+        "field": (field, field_cam, native.TT_ACCEL_AUTO),
+        "field_two_level": (field, field_cam, native.TT_ACCEL_TWO_LEVEL),
+        "field_wide": (field, field_cam, native.TT_ACCEL_FLAT_WIDE),
+        "instanced": (SceneArrays(scenes.instanced_spheres()), scenes.Camera.looking_at((0.0, 6.0, 40.0), (0, 0, 0)),
+                      native.TT_ACCEL_AUTO),
     }
 
 
+def _create(ctx, sc):
+    handles = {}
+    for name, (arrays, _, accel) in sc.items():
+        check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_ACCEL, accel))
+        handles[name] = ctx.create_scene(arrays)
+    check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_ACCEL, native.TT_ACCEL_AUTO))
+    return handles
+
+
 def _requests(rng, n):
-    names = ["cornell", "field", "instanced"]
+    names = ["cornell", "field", "instanced", "field_two_level", "field_wide"]
     out = []
     for k in range(n):
         w, h = int(rng.choice([40, 64, 96, 128])), int(rng.choice([24, 48, 72]))
         cfg = Config(bounce_count=int(rng.integers(2, 9)), sample_count=int(rng.integers(1, 13)))
-        out.append((names[k % 3], (w, h), cfg, int(rng.integers(0, 50))))
+        out.append((names[k % len(names)], (w, h), cfg, int(rng.integers(0, 50))))
     return out
 
 
@@ -52,14 +67,18 @@ def _alone(ctx, handle, constants):
     return ctx.download(img, w, h)
 
 
-def test_requests_in_the_mix_equal_alone(ctx):
+@pytest.mark.parametrize("round_items", [20_000, 0])
+def test_requests_in_the_mix_equal_alone(ctx, round_items):
+    """round_items 20,000: every request takes several rounds of a few samples per pixel, and the
+    requests that finish early are replaced by queued ones between rounds; 0: the default share
+    (each request's whole sample count in one round)."""
     sc = _scenes()
-    handles = {k: ctx.create_scene(a) for k, (a, _) in sc.items()}
+    handles = _create(ctx, sc)
     rng = np.random.default_rng(21)
-    reqs = _requests(rng, 12)
+    reqs = _requests(rng, 15)
     consts = [make_constants(sc[name][1], ext, cfg, frame, 0) for name, ext, cfg, frame in reqs]
     alone = [_alone(ctx, handles[name], c) for (name, _, _, _), c in zip(reqs, consts)]
-    with RenderServer(ctx, max_inflight=4, paths_per_request=1 << 14) as srv:
+    with RenderServer(ctx, max_inflight=4, pool_paths=1 << 14, round_items=round_items) as srv:
         ids = [srv.submit(handles[name], c) for (name, _, _, _), c in zip(reqs, consts)]
         imgs = [srv.wait(i) for i in ids]
         st = srv.stats()
@@ -75,22 +94,20 @@ def test_requests_in_the_mix_equal_alone(ctx):
         assert_same_bits(alone[k], oracle.OracleScene(sc[name][0]).render(consts[k]), f"oracle {k}")
 
 
-def _arena_bytes(w, h, spp, paths):
-    """Mirror of the server's arena layout (server.cu, layout_for)."""
+def _arena_bytes(w, h, spp, round_items=1 << 26):
+    """Mirror of the server's per-request arena (server.cu, arena_bytes): the per-sample radiance
+    of the largest chunk, running sums, image, error word."""
     wh = w * h
-    chunk = min(spp, 64)
-    items = wh * chunk
-    p = (min(paths, max(items, 1)) + 127) // 128 * 128
-    sizes = [16 * p] * 7 + [16 * 4 * p, 4 * 4 * p, 4 * p, 32 * p, 8 * p, 64, 16 * items, 16 * wh, 16 * wh]
-    return sum((s + 255) // 256 * 256 for s in sizes) + 256
+    chunk = max(1, min(round_items // wh, 64, spp))
+    return sum((s + 255) // 256 * 256 for s in (16 * chunk * wh, 16 * wh, 16 * wh)) + 256
 
 
 def test_budget_admits_one_at_a_time(ctx):
-    a, cam = _scenes()["cornell"]
+    a, cam, _ = _scenes()["cornell"]
     h = ctx.create_scene(a)
     c = make_constants(cam, (64, 48), Config(bounce_count=4, sample_count=4), 0, 0)
-    need = _arena_bytes(64, 48, 4, 4096)
-    with RenderServer(ctx, hbm_budget_bytes=int(need * 1.5), max_inflight=4, paths_per_request=4096) as srv:
+    need = _arena_bytes(64, 48, 4)
+    with RenderServer(ctx, hbm_budget_bytes=int(need * 1.5), max_inflight=4, pool_paths=4096) as srv:
         ids = [srv.submit(h, c) for _ in range(5)]
         imgs = [srv.wait(i) for i in ids]
         st = srv.stats()
@@ -100,10 +117,11 @@ def test_budget_admits_one_at_a_time(ctx):
 
 
 def test_request_larger_than_budget_fails(ctx):
-    a, cam = _scenes()["cornell"]
+    a, cam, _ = _scenes()["cornell"]
     h = ctx.create_scene(a)
     c = make_constants(cam, (64, 48), Config(bounce_count=4, sample_count=4), 0, 0)
-    with RenderServer(ctx, hbm_budget_bytes=1 << 20, max_inflight=2) as srv:
+    assert _arena_bytes(64, 48, 4) > 1 << 16
+    with RenderServer(ctx, hbm_budget_bytes=1 << 16, max_inflight=2) as srv:
         rid = srv.submit(h, c)
         st = ctypes.c_int32()
         assert ctx.lib.tt_server_wait(srv.handle, rid, 60_000, ctypes.byref(st)) == native.TT_OK
@@ -112,7 +130,7 @@ def test_request_larger_than_budget_fails(ctx):
 
 
 def test_bad_requests(ctx):
-    a, cam = _scenes()["cornell"]
+    a, cam, _ = _scenes()["cornell"]
     h = ctx.create_scene(a)
     c = make_constants(cam, (32, 16), Config(bounce_count=2, sample_count=1), 0, 0)
     with RenderServer(ctx, max_inflight=1) as srv:

@@ -67,13 +67,21 @@ def test_textured_render_bits(gpu_context, mode):
 
 
 def test_textured_server_request(gpu_context):
+    """A textured and an untextured request rendered in the same rounds (the batch then shades
+    with texture sampling on for both)."""
     ctx = gpu_context
     arrays = SceneArrays(scenes.textured_cornell())
     h = ctx.create_scene(arrays)
+    plain = SceneArrays(scenes.cornell_box())
+    hp = ctx.create_scene(plain)
     c = make_constants(CAMERA, (40, 32), Config(bounce_count=4, sample_count=3), 3, 0)
-    with RenderServer(ctx, max_inflight=2, paths_per_request=1 << 12) as srv:
-        img = srv.wait(srv.submit(h, c))
+    cp = make_constants(scenes.cornell_workload().camera, (48, 24), Config(bounce_count=3, sample_count=5), 1, 0)
+    with RenderServer(ctx, max_inflight=2, pool_paths=1 << 12, round_items=2000) as srv:
+        ids = [srv.submit(h, c), srv.submit(hp, cp)]
+        img, img_plain = (srv.wait(i) for i in ids)
+        assert srv.stats().peak_inflight == 2
     assert_same_bits(img, oracle.OracleScene(SceneArrays.from_arrays(arrays.save(None))).render(c), "server")
+    assert_same_bits(img_plain, oracle.OracleScene(plain).render(cp), "untextured in the textured batch")
 
 
 def test_textured_scene_rejects(gpu_context):

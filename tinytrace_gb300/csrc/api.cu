@@ -97,7 +97,7 @@ struct WavefrontBuffers {
 // ReSTIR DI state kept between frames: two G-buffers and two final reservoir arrays
 // (current and previous frame), the initial and temporal reservoirs, the previous camera.
 struct RestirState {
-    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex, glob, queue, queue_count;
+    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex, glob;
     uint64_t pixels = 0;
     uint32_t cur = 0;
     RestirHistory history{};
@@ -1314,11 +1314,6 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
             R.pixels = WH;
             R.history.valid = 0u;
         }
-        uint64_t tiles = (uint64_t)((img->width + 15u) / 16u) * ((img->height + 7u) / 8u);  // the passes' 16 x 8 tiles
-        if (R.queue_count.bytes < 4ull * tiles) {
-            R.queue.alloc(4ull * 128ull * tiles);
-            R.queue_count.alloc(4ull * tiles);
-        }
         RenderParams p;
         p.sc = s->dev;
         p.sc.light_power = ctx->light_selection == TT_LIGHT_SELECTION_POWER ? 1u : 0u;
@@ -1336,8 +1331,6 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         rp.glob = R.glob.as<float4>();
         rp.prev_gbuf = R.gbuf[R.cur ^ 1u].as<Surface>();
         rp.initial = R.initial.as<Reservoir>();
-        rp.queue = R.queue.as<uint32_t>();
-        rp.queue_count = R.queue_count.as<uint32_t>();
         rp.temporal = R.temporal.as<Reservoir>();
         rp.final_out = R.final_res[R.cur].as<Reservoir>();
         rp.prev = R.final_res[R.cur ^ 1u].as<Reservoir>();

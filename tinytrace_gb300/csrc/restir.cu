@@ -20,56 +20,6 @@ __device__ __forceinline__ bool pixel_of_thread(const tt_constants& c, uint32_t&
     return x < c.screen_size[0] && y < c.screen_size[1];
 }
 
-// Tile queues: the G-buffer block of each 16 x 8 tile lists the tile's surface pixels, sorted
-// by material bucket, in its own RT_BLOCK entries of `queue` and their number in
-// queue_count[tile] (no atomics), so that the candidate and shade blocks of the tile run only
-// warps of surface pixels whose lanes mostly share a lobe set.  Every thread of the block must
-// call it; bucket == HIT_BUCKETS lists nothing (sky pixels and threads outside the image).
-__device__ __forceinline__ void tile_queue_write(const RestirParams& rp, uint32_t bucket, uint32_t pixel) {
-    constexpr uint32_t WARPS = RT_BLOCK / 32;
-    __shared__ uint32_t s_wc[HIT_BUCKETS][WARPS];
-    uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, below = 0u;
-#pragma unroll
-    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
-        uint32_t mask = __ballot_sync(0xffffffffu, bucket == b);
-        if (lane == 0u) s_wc[b][warp] = (uint32_t)__popc(mask);
-        if (bucket == b) below = (uint32_t)__popc(mask & ((1u << lane) - 1u));
-    }
-    __syncthreads();
-    uint32_t pos = below, total = 0u;
-#pragma unroll
-    for (uint32_t b = 0; b < HIT_BUCKETS; ++b)
-#pragma unroll
-        for (uint32_t k = 0; k < WARPS; ++k) {
-            uint32_t n = s_wc[b][k];
-            pos += (b < bucket || (b == bucket && k < warp)) ? n : 0u;
-            total += n;
-        }
-    uint64_t tile = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x;
-    if (bucket < HIT_BUCKETS) rp.queue[tile * RT_BLOCK + pos] = pixel;
-    if (threadIdx.x == 0) rp.queue_count[tile] = total;
-}
-
-// Pixel of this thread in its tile's queue, or false (the tile has fewer surface pixels).
-__device__ __forceinline__ bool queued_pixel(const RestirParams& rp, uint64_t& i) {
-    uint64_t tile = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x;
-    if (threadIdx.x >= rp.queue_count[tile]) return false;
-    i = rp.queue[tile * RT_BLOCK + threadIdx.x];
-    return true;
-}
-
-// The accumulation rule of tt_render for one pixel of the target.
-__device__ __forceinline__ void write_target(const RenderParams& p, uint64_t i, f3 radiance) {
-    const tt_constants& c = p.c;
-    float4* tp = p.target + i;
-    if (c.accumulated_frame_count != 0) {
-        float4 prev = *tp;
-        radiance = (f3{prev.x, prev.y, prev.z} * (float)(c.accumulated_frame_count - 1u) + radiance) /
-                   (float)c.accumulated_frame_count;
-    }
-    *tp = make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
-}
-
 // Rebuilds the pixel's shading state from its G-buffer record.
 struct ShadingState {
     f3 pos, wi;
@@ -116,13 +66,13 @@ __device__ __forceinline__ float target_of(const DevScene& sc, const ShadingStat
     return luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
 }
 
-// The G-buffer pass for pixel (x, y); returns the material bucket of its primary hit, or
-// HIT_BUCKETS for a sky pixel (finished here).
 template <bool TEX>
-__device__ __forceinline__ uint32_t gbuffer_pixel(const RenderParams& p, const RestirParams& rp, Surface* gbuf,
-                                                  float4* gtex, float4* glob, uint32_t x, uint32_t y,
-                                                  uint32_t* s_stack) {
+__global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
+                                                                  Surface* gbuf, float4* gtex, float4* glob) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
     const tt_constants& c = p.c;
+    if (!pixel_of_thread(c, x, y)) return;
     const DevScene& sc = p.sc;
     uint32_t W = c.screen_size[0], H = c.screen_size[1];
     uint32_t g = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
@@ -133,13 +83,7 @@ __device__ __forceinline__ uint32_t gbuffer_pixel(const RenderParams& p, const R
     Hit h = trace_closest<false>(sc, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true, s_stack + threadIdx.x, RT_BLOCK,
                                  p.err, cnt);
     Surface s;
-    uint64_t i = (uint64_t)y * W + x;
-    // surface pixels go to their material bucket's queue for the candidate and shade passes; sky
-    // pixels are finished here: empty initial reservoir, the white sky (integrate.glsl:272-276)
-    uint32_t bucket = h.hit ? (uint32_t)__ldg(sc.inst_bucket + h.instance) : HIT_BUCKETS;
     if (!h.hit) {
-        rp.initial[i] = empty_reservoir();
-        write_target(p, i, splat(1.0f));
         s.pos_dist = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         s.normal_mat = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(NO_SURFACE));
         s.tangent_inst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -164,33 +108,18 @@ __device__ __forceinline__ uint32_t gbuffer_pixel(const RenderParams& p, const R
         store_lobes(glob + LOBE_RECORD * ((uint64_t)y * W + x), bsdf_prepare(mc, wi, gp));
     }
     gbuf[(uint64_t)y * W + x] = s;
-    return bucket;
-}
-
-template <bool TEX>
-__global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
-                                                                  const __grid_constant__ RestirParams rp,
-                                                                  Surface* gbuf, float4* gtex, float4* glob) {
-    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
-    uint32_t x, y;
-    const tt_constants& c = p.c;
-    uint32_t W = c.screen_size[0], H = c.screen_size[1];
-    // threads outside the image take part in the block's queue append only
-    uint32_t bucket = HIT_BUCKETS;
-    if (pixel_of_thread(c, x, y)) bucket = gbuffer_pixel<TEX>(p, rp, gbuf, gtex, glob, x, y, s_stack);
-    tile_queue_write(rp, bucket, y * W + x);
 }
 
 template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_constant__ RenderParams p,
-                                                                  const __grid_constant__ RestirParams rp,
                                                                   const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   Reservoir* out, uint32_t candidates) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
     const tt_constants& c = p.c;
-    uint64_t i = 0;
-    if (!queued_pixel(rp, i)) return;
+    if (!pixel_of_thread(c, x, y)) return;
     const DevScene& sc = p.sc;
+    uint64_t i = (uint64_t)y * c.screen_size[0] + x;
     ShadingState st;
     Reservoir r = empty_reservoir();
     if (load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st) && sc.emissive_count > 0) {
@@ -342,14 +271,15 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
 
 template <bool TEX>
 __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_constant__ RenderParams p,
-                                                                const __grid_constant__ RestirParams rp,
                                                                 const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                 const Reservoir* res) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
     const tt_constants& c = p.c;
-    uint64_t i = 0;
-    if (!queued_pixel(rp, i)) return;
+    if (!pixel_of_thread(c, x, y)) return;
     const DevScene& sc = p.sc;
+    uint32_t W = c.screen_size[0];
+    uint64_t i = (uint64_t)y * W + x;
     ShadingState st;
     f3 radiance;
     if (!load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st)) {
@@ -364,7 +294,13 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
                 radiance += contrib * r.W;
         }
     }
-    write_target(p, i, radiance);
+    float4* tp = p.target + i;
+    if (c.accumulated_frame_count != 0) {
+        float4 prev = *tp;
+        radiance = (f3{prev.x, prev.y, prev.z} * (float)(c.accumulated_frame_count - 1u) + radiance) /
+                   (float)c.accumulated_frame_count;
+    }
+    *tp = make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
 }
 
 template <bool TEX>
@@ -372,10 +308,10 @@ static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStr
     const tt_constants& c = p.c;
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
     stage_begin(timer, TT_STAGE_RESTIR_GBUFFER, st);
-    restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob);
+    restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_INITIAL, st);
-    restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
+    restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_TEMPORAL, st);
     restir_temporal_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.glob, rp.prev_gbuf,
@@ -386,7 +322,7 @@ static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStr
                                                           rp.neighbours, rp.radius);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_SHADE, st);
-    restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
+    restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
     stage_end(timer, st);
 }
 

@@ -1,13 +1,22 @@
 // Continuous-batching render server (tt_server_*): requests of any scene, resolution and
-// sample count are admitted from an arrival-order queue whenever an execution slot and enough
-// of the HBM budget are free, and run concurrently, each as one CUDA graph on its own stream.
+// sample count share one wavefront path pool and one set of persistent kernels.
+//
+// The scheduler thread works in rounds.  A round takes the next sample chunk of every admitted
+// request (up to round_items work items in total, split evenly across the requests and capped
+// at 64 samples per pixel), lays the chunks end to end as the work items of one shared-pool
+// wavefront loop (regen, extend, shade, shadow in a device-side while loop) and finishes with
+// the per-request reductions; the whole round is one launch of a CUDA graph instantiated once
+// per server.  Between rounds the scheduler retires finished requests (their images are copied
+// out while the next round runs) and admits queued ones in arrival order while the batch has
+// room and their device memory fits in the HBM budget, so requests that arrive while others
+// render join the batch at the next round boundary.
 //
 // Per request the device holds one stream-ordered arena (allocated from a server-owned memory
-// pool on the slot's stream and freed on it after the image is copied out): the wavefront path
-// pool, its queues, the per-sample radiance of one sample chunk, the running pixel sums and the
-// render target.  The admission test uses the arena's exact size, so the budget bounds what is
-// in flight.  Requests share nothing mutable on the device, which makes every image identical
-// to the same request rendered alone.
+// pool): the per-sample radiance of its largest chunk, the running pixel sums, the image and
+// its error word; the admission test uses the arena's exact size.  A path carries its request
+// in its slot state, and every kernel reads that request's Constants, scene and buffers, so a
+// request's image is the same, bit for bit, alone or among others (the reduction adds each
+// pixel's samples in sample order whatever the chunking).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,70 +45,38 @@ using Clock = std::chrono::steady_clock;
 namespace {
 
 constexpr uint64_t DEFAULT_BUDGET = 150ull << 30;
-constexpr uint32_t DEFAULT_INFLIGHT = 8;
-constexpr uint32_t DEFAULT_PATHS = 1u << 20;
+constexpr uint32_t DEFAULT_INFLIGHT = 16;
+constexpr uint32_t DEFAULT_PATHS = 1u << 21;
+constexpr uint64_t DEFAULT_ROUND_ITEMS = 1ull << 26;
 constexpr uint32_t MAX_CHUNK_SPP = 64;
+constexpr uint64_t MAX_PIXELS = 1ull << 24;  // per request: 4096 x 4096
+
+uint64_t align256(uint64_t b) { return (b + 255u) / 256u * 256u; }
 
 struct Request {
     uint64_t id = 0;
     DevScene sc{};
     tt_constants c{};
     float* host = nullptr;
-    uint64_t bytes = 0, arena_bytes = 0;
+    uint64_t bytes = 0, arena_bytes = 0, WH = 0;
+    uint32_t chunk_cap = 0;  // samples per pixel the arena's per-sample buffer holds
+    uint32_t done_spp = 0;
     Clock::time_point submitted, finished;
     int32_t status = TT_REQUEST_QUEUED;
     std::string error;
+    // device arena: samples (chunk_cap x WH), running sums, image, error word
+    char* arena = nullptr;
+    float4 *samples = nullptr, *running = nullptr, *target = nullptr;
+    uint32_t* err = nullptr;
+    // this round
+    uint32_t chunk_spp = 0;
+    bool last = false;
 };
 
-// Byte offsets of one request's arrays inside its arena (256-byte aligned).
-struct Layout {
-    uint32_t P = 0, chunk_spp = 0;
-    uint64_t WH = 0, items = 0;
-    uint64_t org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, ndc_mip, counters, samples, running, target,
-        total;
-};
-
-Layout layout_for(const tt_constants& c, uint32_t paths) {
-    Layout L;
-    L.WH = (uint64_t)c.screen_size[0] * c.screen_size[1];
-    L.chunk_spp = std::min<uint32_t>(c.sample_count, MAX_CHUNK_SPP);
-    L.items = L.WH * L.chunk_spp;
-    uint64_t P = std::min<uint64_t>(paths, std::max<uint64_t>(L.items, 1));
-    L.P = (uint32_t)((P + 127u) / 128u * 128u);
-    uint64_t at = 0;
-    auto take = [&](uint64_t bytes) {
-        uint64_t o = at;
-        at += (bytes + 255u) / 256u * 256u;
-        return o;
-    };
-    L.org = take(16ull * L.P);
-    L.dir = take(16ull * L.P);
-    L.thr = take(16ull * L.P);
-    L.acc = take(16ull * L.P);
-    L.pa1 = take(16ull * L.P);
-    L.pa0 = take(16ull * L.P);
-    L.pe = take(16ull * L.P);
-    L.hit = take(16ull * HIT_BUCKETS * L.P);
-    L.hslot = take(4ull * HIT_BUCKETS * L.P);
-    L.active = take(4ull * L.P);
-    L.shadow = take(32ull * L.P);
-    L.ndc_mip = take(8ull * L.P);
-    L.counters = take(4ull * CTRL_WORDS);
-    L.samples = take(16ull * L.items);
-    L.running = take(16ull * L.WH);
-    L.target = take(16ull * L.WH);
-    L.total = at + 256u;  // + the error word
-    return L;
-}
-
-struct Slot {
-    cudaStream_t stream = nullptr, capture = nullptr, body = nullptr;
-    cudaEvent_t done = nullptr;
-    uint32_t* err_dev = nullptr;   // in the arena's last 256 bytes
-    uint32_t* err_host = nullptr;  // pinned
-    float* staging = nullptr;      // pinned copy of the target
-    uint64_t staging_bytes = 0;
-    Request* req = nullptr;
+// A pinned host buffer the image of a finished request is copied into during its last round.
+struct Staging {
+    float* ptr = nullptr;
+    uint64_t bytes = 0;
 };
 
 }  // namespace
@@ -107,14 +84,26 @@ struct Slot {
 struct tt_server {
     int device = 0;
     tt_context* ctx = nullptr;
-    uint64_t budget = DEFAULT_BUDGET;
-    uint32_t paths = DEFAULT_PATHS;
-    int trace_blocks = 0;
+    uint64_t budget = DEFAULT_BUDGET, round_items = DEFAULT_ROUND_ITEMS;
+    uint32_t max_live = DEFAULT_INFLIGHT, paths = DEFAULT_PATHS;
+    cudaStream_t stream = nullptr, capture = nullptr, body = nullptr;
+    cudaEvent_t round_start = nullptr, round_done = nullptr;
     cudaMemPool_t pool = nullptr;
-    std::vector<Slot> slots;
+    // the shared path pool and the round tables (device), their pinned host mirrors
+    DeviceBuffer org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, counters, ndc_mip;
+    DeviceBuffer d_reqs, d_scenes, d_round, d_batch_err;
+    BatchRequest* h_reqs = nullptr;
+    DevScene* h_scenes = nullptr;
+    BatchRound* h_round = nullptr;
+    uint32_t* h_err = nullptr;  // BATCH_MAX_REQUESTS request error words + the batch word
+    WfParams w{};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // without / with texture sampling
+    std::vector<Staging> staging_free;
+    uint64_t round_items_now = 0;
+
     std::mutex mu;
-    std::condition_variable cv;      // submissions and stop (scheduler side)
-    std::condition_variable done_cv; // completions (waiter side)
+    std::condition_variable cv;       // submissions and stop (scheduler side)
+    std::condition_variable done_cv;  // completions (waiter side)
     std::deque<Request*> queue;
     std::map<uint64_t, std::unique_ptr<Request>> requests;
     uint64_t next_id = 1;
@@ -122,157 +111,288 @@ struct tt_server {
     tt_server_stats stats{};
     std::thread worker;
 
-    void launch(Slot& s, Request& r);
-    void finish(Slot& s, cudaError_t q);
+    void create_pool();
+    void admit(std::vector<Request*>& live);
+    void launch_round(std::vector<Request*>& live);
+    Staging take_staging(uint64_t bytes);
+    void retire(Request* r, int32_t status, const std::string& error);
     void run();
 };
 
-// Enqueues request r on slot s: arena, error word, the graph, the image and error read-back.
-void tt_server::launch(Slot& s, Request& r) {
-    Layout L = layout_for(r.c, paths);
-    char* arena = nullptr;
-    check_cuda(cudaMallocFromPoolAsync((void**)&arena, L.total, pool, s.stream), "arena");
-    s.err_dev = reinterpret_cast<uint32_t*>(arena + L.total - 256u);
-    uint64_t image = 16ull * L.WH;
-    if (s.staging_bytes < image) {
-        if (s.staging) cudaFreeHost(s.staging);
-        s.staging = nullptr;
-        check_cuda(cudaMallocHost((void**)&s.staging, image), "staging");
-        s.staging_bytes = image;
-    }
-    WfParams w{};
-    w.org = reinterpret_cast<float4*>(arena + L.org);
-    w.dir = reinterpret_cast<float4*>(arena + L.dir);
-    w.thr = reinterpret_cast<float4*>(arena + L.thr);
-    w.acc = reinterpret_cast<float4*>(arena + L.acc);
-    w.pa1 = reinterpret_cast<float4*>(arena + L.pa1);
-    w.pa0 = reinterpret_cast<float4*>(arena + L.pa0);
-    w.pe = reinterpret_cast<float4*>(arena + L.pe);
-    w.hit = reinterpret_cast<uint4*>(arena + L.hit);
-    w.hslot = reinterpret_cast<uint32_t*>(arena + L.hslot);
-    w.active = reinterpret_cast<uint32_t*>(arena + L.active);
-    w.shadow = reinterpret_cast<float4*>(arena + L.shadow);
-    w.counters = reinterpret_cast<uint32_t*>(arena + L.counters);
-    w.samples = reinterpret_cast<float4*>(arena + L.samples);
-    w.running = reinterpret_cast<float4*>(arena + L.running);
-    w.ndc_mip = r.sc.textured ? reinterpret_cast<float2*>(arena + L.ndc_mip) : nullptr;
-    w.P = L.P;
-    w.chunk_spp = L.chunk_spp;
+void tt_server::create_pool() {
+    uint64_t P = (paths + 127u) / 128u * 128u;
+    org.alloc(16 * P);
+    dir.alloc(16 * P);
+    thr.alloc(16 * P);
+    acc.alloc(16 * P);
+    pa1.alloc(16 * P);
+    pa0.alloc(16 * P);
+    pe.alloc(16 * P);
+    hit.alloc(16ull * HIT_BUCKETS * P);
+    hslot.alloc(4ull * HIT_BUCKETS * P);
+    active.alloc(4 * P);
+    shadow.alloc(32 * P);
+    counters.alloc(4ull * CTRL_WORDS);
+    ndc_mip.alloc(8 * P);
+    d_reqs.alloc(sizeof(BatchRequest) * BATCH_MAX_REQUESTS);
+    d_scenes.alloc(sizeof(DevScene) * BATCH_MAX_REQUESTS);
+    d_round.alloc(sizeof(BatchRound));
+    d_batch_err.alloc(256);
+    check_cuda(cudaMemset(d_reqs.ptr, 0, d_reqs.bytes), "memset");
+    check_cuda(cudaMemset(d_scenes.ptr, 0, d_scenes.bytes), "memset");
+    check_cuda(cudaMallocHost((void**)&h_reqs, sizeof(BatchRequest) * BATCH_MAX_REQUESTS), "cudaMallocHost");
+    check_cuda(cudaMallocHost((void**)&h_scenes, sizeof(DevScene) * BATCH_MAX_REQUESTS), "cudaMallocHost");
+    check_cuda(cudaMallocHost((void**)&h_round, sizeof(BatchRound)), "cudaMallocHost");
+    check_cuda(cudaMallocHost((void**)&h_err, 4ull * (BATCH_MAX_REQUESTS + 1)), "cudaMallocHost");
+    std::memset(h_reqs, 0, sizeof(BatchRequest) * BATCH_MAX_REQUESTS);
+    w = WfParams{};
+    w.org = org.as<float4>();
+    w.dir = dir.as<float4>();
+    w.thr = thr.as<float4>();
+    w.acc = acc.as<float4>();
+    w.pa1 = pa1.as<float4>();
+    w.pa0 = pa0.as<float4>();
+    w.pe = pe.as<float4>();
+    w.hit = hit.as<uint4>();
+    w.hslot = hslot.as<uint32_t>();
+    w.active = active.as<uint32_t>();
+    w.shadow = shadow.as<float4>();
+    w.counters = counters.as<uint32_t>();
+    w.ndc_mip = ndc_mip.as<float2>();
+    w.P = (uint32_t)P;
     w.refill = 20;
-    w.trace_blocks = (uint32_t)trace_blocks;
-    RenderParams p{};
-    p.sc = r.sc;
-    p.c = r.c;
-    p.target = reinterpret_cast<float4*>(arena + L.target);
-    p.err = s.err_dev;
-    p.counters = nullptr;
-    try {
-        check_cuda(cudaMemsetAsync(s.err_dev, 0, 4, s.stream), "memset");
-        render_wavefront_graph(p, w, false, s.stream, s.capture, s.body);
-        check_cuda(cudaMemcpyAsync(s.staging, p.target, image, cudaMemcpyDeviceToHost, s.stream), "image");
-        check_cuda(cudaMemcpyAsync(s.err_host, s.err_dev, 4, cudaMemcpyDeviceToHost, s.stream), "error word");
-    } catch (...) {
-        cudaFreeAsync(arena, s.stream);
-        throw;
-    }
-    check_cuda(cudaFreeAsync(arena, s.stream), "arena free");
-    check_cuda(cudaEventRecord(s.done, s.stream), "event");
 }
 
-// Completion of slot s (its event fired, or failed with q): error word, image copy-out, stats.
-void tt_server::finish(Slot& s, cudaError_t q) {
-    Request& r = *s.req;
-    int32_t status = TT_REQUEST_DONE;
-    std::string error;
-    if (q != cudaSuccess) {
-        status = TT_REQUEST_FAILED;
-        error = std::string("device error: ") + cudaGetErrorString(q);
-    } else if (*s.err_host & ERR_STACK_OVERFLOW) {
-        status = TT_REQUEST_FAILED;
-        error = "traversal stack overflow";
-    } else if (*s.err_host & ERR_ITERATION_LIMIT) {
-        status = TT_REQUEST_FAILED;
-        error = "iteration limit reached";
-    } else {
-        std::memcpy(r.host, s.staging, r.bytes);
-    }
+Staging tt_server::take_staging(uint64_t bytes) {
+    for (size_t k = 0; k < staging_free.size(); ++k)
+        if (staging_free[k].bytes >= bytes) {
+            Staging s = staging_free[k];
+            staging_free.erase(staging_free.begin() + (long)k);
+            return s;
+        }
+    Staging s;
+    check_cuda(cudaMallocHost((void**)&s.ptr, bytes), "cudaMallocHost");
+    s.bytes = bytes;
+    return s;
+}
+
+// Final status of r; frees its arena (stream-ordered after the work already enqueued).
+void tt_server::retire(Request* r, int32_t status, const std::string& error) {
+    if (r->arena) cudaFreeAsync(r->arena, stream);
+    r->arena = nullptr;
     std::lock_guard<std::mutex> lk(mu);
-    r.finished = Clock::now();
-    r.status = status;
-    r.error = error;
+    r->finished = Clock::now();
+    r->status = status;
+    r->error = error;
     stats.inflight--;
-    stats.bytes_in_flight -= r.arena_bytes;
+    stats.bytes_in_flight -= r->arena_bytes;
     if (status == TT_REQUEST_DONE) stats.completed++;
     else stats.failed++;
-    s.req = nullptr;
     done_cv.notify_all();
+}
+
+// Moves queued requests into the batch in arrival order while it has room and the budget allows.
+void tt_server::admit(std::vector<Request*>& live) {
+    std::vector<Request*> in;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        while (!queue.empty()) {
+            Request* head = queue.front();
+            if (head->arena_bytes > budget) {  // can never fit
+                queue.pop_front();
+                head->status = TT_REQUEST_FAILED;
+                head->error = "request needs more device memory than the HBM budget";
+                head->finished = Clock::now();
+                stats.queued--;
+                stats.failed++;
+                done_cv.notify_all();
+                continue;
+            }
+            if (live.size() + in.size() >= max_live || stats.bytes_in_flight + head->arena_bytes > budget) break;
+            queue.pop_front();
+            head->status = TT_REQUEST_RUNNING;
+            stats.queued--;
+            stats.inflight++;
+            stats.bytes_in_flight += head->arena_bytes;
+            stats.peak_inflight = std::max(stats.peak_inflight, stats.inflight);
+            stats.peak_bytes_in_flight = std::max(stats.peak_bytes_in_flight, stats.bytes_in_flight);
+            in.push_back(head);
+        }
+    }
+    for (Request* r : in) {
+        try {
+            check_cuda(cudaMallocFromPoolAsync((void**)&r->arena, r->arena_bytes, pool, stream), "arena");
+            uint64_t at = 0;
+            r->samples = reinterpret_cast<float4*>(r->arena + at);
+            at += align256(16ull * r->chunk_cap * r->WH);
+            r->running = reinterpret_cast<float4*>(r->arena + at);
+            at += align256(16ull * r->WH);
+            r->target = reinterpret_cast<float4*>(r->arena + at);
+            at += align256(16ull * r->WH);
+            r->err = reinterpret_cast<uint32_t*>(r->arena + at);
+            check_cuda(cudaMemsetAsync(r->err, 0, 4, stream), "memset");
+            live.push_back(r);
+        } catch (const Error& e) {
+            retire(r, TT_REQUEST_FAILED, e.message);
+        }
+    }
+}
+
+// Enqueues one round over the batch: tables, the graph, the error words, and the images of the
+// requests whose last chunk this is (into pinned staging, `outs`).
+void tt_server::launch_round(std::vector<Request*>& live) {
+    uint32_t n = (uint32_t)live.size();
+    uint64_t share = std::max<uint64_t>(1, round_items / n);
+    uint64_t items = 0, pixels = 0;
+    uint32_t max_bounce = 1;
+    bool tex = false;
+    for (uint32_t k = 0; k < n; ++k) {
+        Request& r = *live[k];
+        uint32_t left = r.c.sample_count - r.done_spp;
+        uint32_t fair = (uint32_t)std::max<uint64_t>(1, share / r.WH);
+        r.chunk_spp = std::min({r.chunk_cap, left, fair});
+        r.last = r.chunk_spp == left;
+        BatchRequest& b = h_reqs[k];
+        b.c = r.c;
+        b.chunk_jump = xs_power(2ull * r.done_spp);
+        b.samples = r.samples;
+        b.running = r.running;
+        b.target = r.target;
+        b.err = r.err;
+        b.scene = k;
+        b.WH = (uint32_t)r.WH;
+        b.item_base = (uint32_t)items;
+        b.pixel_base = (uint32_t)pixels;
+        b.chunk_sample0 = r.done_spp;
+        b.chunk_spp = r.chunk_spp;
+        b.chunk_items = (uint32_t)(r.WH * r.chunk_spp);
+        b.last = r.last ? 1u : 0u;
+        h_scenes[k] = r.sc;
+        items += b.chunk_items;
+        pixels += r.WH;
+        max_bounce = std::max(max_bounce, r.c.bounce_count);
+        tex = tex || r.sc.textured != 0u;
+    }
+    h_round->nreq = n;
+    h_round->items = (uint32_t)items;
+    h_round->pixels = (uint32_t)pixels;
+    h_round->limit = (uint32_t)std::min<uint64_t>(2ull * (items / w.P + 1u) * (max_bounce + 2u) + 16u, 0x7fffffffu);
+    round_items_now = items;
+    BatchParams bp{d_reqs.as<BatchRequest>(), d_scenes.as<DevScene>(), d_round.as<BatchRound>()};
+    cudaGraphExec_t& g = graph[tex ? 1 : 0];
+    if (!g) g = build_batch_graph(w, bp, tex, d_batch_err.as<uint32_t>(), capture, body);
+    check_cuda(cudaEventRecord(round_start, stream), "event");
+    check_cuda(cudaMemcpyAsync(d_reqs.ptr, h_reqs, sizeof(BatchRequest) * n, cudaMemcpyHostToDevice, stream), "table");
+    check_cuda(cudaMemcpyAsync(d_scenes.ptr, h_scenes, sizeof(DevScene) * n, cudaMemcpyHostToDevice, stream), "scenes");
+    check_cuda(cudaMemcpyAsync(d_round.ptr, h_round, sizeof(BatchRound), cudaMemcpyHostToDevice, stream), "round");
+    check_cuda(cudaMemsetAsync(d_batch_err.ptr, 0, 4, stream), "memset");
+    check_cuda(cudaGraphLaunch(g, stream), "cudaGraphLaunch");
+    for (uint32_t k = 0; k < n; ++k)
+        check_cuda(cudaMemcpyAsync(h_err + k, live[k]->err, 4, cudaMemcpyDeviceToHost, stream), "error word");
+    check_cuda(cudaMemcpyAsync(h_err + BATCH_MAX_REQUESTS, d_batch_err.ptr, 4, cudaMemcpyDeviceToHost, stream),
+               "error word");
 }
 
 void tt_server::run() {
     cudaSetDevice(device);
+    std::vector<Request*> live;
+    // finished requests of the previous round: image in pinned staging, copied out while the
+    // next round renders
+    std::vector<std::pair<Request*, Staging>> copy_out;
+    auto ns_since = [](Clock::time_point t0) {
+        return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
+    };
+    uint64_t t_admit = 0, t_launch = 0, t_copy = 0, t_wait = 0, busy = 0;
     while (true) {
-        bool progressed = false;
-        for (Slot& s : slots) {
-            if (!s.req) continue;
-            cudaError_t q = cudaEventQuery(s.done);
-            if (q == cudaErrorNotReady) continue;
-            finish(s, q);
-            progressed = true;
+        Clock::time_point t0 = Clock::now();
+        try {
+            admit(live);
+        } catch (const Error&) {
         }
-        // admit the head of the queue while a slot and the budget allow (arrival order)
-        while (true) {
-            Request* r = nullptr;
-            Slot* slot = nullptr;
+        t_admit += ns_since(t0);
+        t0 = Clock::now();
+        bool launched = false;
+        std::vector<std::pair<Request*, Staging>> finishing;
+        if (!live.empty()) {
+            try {
+                launch_round(live);
+                for (Request* r : live)
+                    if (r->last) {
+                        Staging s = take_staging(r->bytes);
+                        check_cuda(cudaMemcpyAsync(s.ptr, r->target, r->bytes, cudaMemcpyDeviceToHost, stream),
+                                   "image");
+                        finishing.emplace_back(r, s);
+                    }
+                check_cuda(cudaEventRecord(round_done, stream), "event");
+                launched = true;
+            } catch (const Error& e) {
+                for (auto& f : finishing) staging_free.push_back(f.second);
+                finishing.clear();
+                cudaStreamSynchronize(stream);
+                for (Request* r : live) retire(r, TT_REQUEST_FAILED, e.message);
+                live.clear();
+            }
+        }
+        t_launch += ns_since(t0);
+        t0 = Clock::now();
+        for (auto& [r, s] : copy_out) {
+            std::memcpy(r->host, s.ptr, r->bytes);
+            staging_free.push_back(s);
+            retire(r, TT_REQUEST_DONE, "");
+        }
+        copy_out.clear();
+        t_copy += ns_since(t0);
+        if (launched) {
+            t0 = Clock::now();
+            cudaError_t q = cudaEventSynchronize(round_done);
+            t_wait += ns_since(t0);
+            float ms = 0.0f;
+            if (q == cudaSuccess && cudaEventElapsedTime(&ms, round_start, round_done) == cudaSuccess)
+                busy += (uint64_t)((double)ms * 1e6);
             {
                 std::lock_guard<std::mutex> lk(mu);
-                if (queue.empty()) break;
-                Request* head = queue.front();
-                if (head->arena_bytes > budget) {  // can never fit
-                    queue.pop_front();
-                    head->status = TT_REQUEST_FAILED;
-                    head->error = "request needs more device memory than the HBM budget";
-                    head->finished = Clock::now();
-                    stats.queued--;
-                    stats.failed++;
-                    done_cv.notify_all();
-                    progressed = true;
+                stats.rounds++;
+                stats.round_items += round_items_now;
+                stats.gpu_busy_ns = busy;
+                stats.admit_ns = t_admit;
+                stats.launch_ns = t_launch;
+                stats.copy_out_ns = t_copy;
+                stats.wait_ns = t_wait;
+            }
+            uint32_t batch_err = q == cudaSuccess ? h_err[BATCH_MAX_REQUESTS] : 0u;
+            std::vector<Request*> still;
+            for (size_t k = 0; k < live.size(); ++k) {
+                Request* r = live[k];
+                std::string error;
+                if (q != cudaSuccess) error = std::string("device error: ") + cudaGetErrorString(q);
+                else if (batch_err & ERR_ITERATION_LIMIT) error = "iteration limit reached";
+                else if (h_err[k] & ERR_STACK_OVERFLOW) error = "traversal stack overflow";
+                else if (h_err[k] & ERR_ITERATION_LIMIT) error = "iteration limit reached";
+                auto f = std::find_if(finishing.begin(), finishing.end(), [&](auto& e) { return e.first == r; });
+                if (!error.empty()) {
+                    if (f != finishing.end()) {
+                        staging_free.push_back(f->second);
+                        finishing.erase(f);
+                    }
+                    retire(r, TT_REQUEST_FAILED, error);
                     continue;
                 }
-                for (Slot& s : slots)
-                    if (!s.req) {
-                        slot = &s;
-                        break;
-                    }
-                if (!slot || stats.bytes_in_flight + head->arena_bytes > budget) break;
-                queue.pop_front();
-                r = head;
-                r->status = TT_REQUEST_RUNNING;
-                slot->req = r;
-                stats.queued--;
-                stats.inflight++;
-                stats.bytes_in_flight += r->arena_bytes;
-                stats.peak_inflight = std::max(stats.peak_inflight, stats.inflight);
-                stats.peak_bytes_in_flight = std::max(stats.peak_bytes_in_flight, stats.bytes_in_flight);
+                r->done_spp += r->chunk_spp;
+                if (f == finishing.end()) still.push_back(r);
+                else if (r->arena) {
+                    cudaFreeAsync(r->arena, stream);  // the image is in staging
+                    r->arena = nullptr;
+                }
             }
-            progressed = true;
-            try {
-                launch(*slot, *r);
-            } catch (const Error& e) {
-                std::lock_guard<std::mutex> lk(mu);
-                r->status = TT_REQUEST_FAILED;
-                r->error = e.message;
-                r->finished = Clock::now();
-                stats.inflight--;
-                stats.bytes_in_flight -= r->arena_bytes;
-                stats.failed++;
-                slot->req = nullptr;
-                done_cv.notify_all();
-            }
+            live.swap(still);
+            copy_out.swap(finishing);
+            continue;
         }
         std::unique_lock<std::mutex> lk(mu);
-        bool busy = stats.inflight > 0 || !queue.empty();
-        if (stop && !busy) break;
-        if (!progressed) cv.wait_for(lk, std::chrono::microseconds(busy ? 50 : 2000));
+        if (copy_out.empty() && live.empty()) {
+            if (stop && queue.empty()) break;
+            if (queue.empty()) cv.wait_for(lk, std::chrono::milliseconds(2));
+        }
     }
 }
 
@@ -296,6 +416,9 @@ int32_t server_guarded(F&& f) {
 void need(bool cond, const char* msg) {
     if (!cond) fail(TT_ERR_INVALID_ARGUMENT, msg);
 }
+uint64_t arena_bytes(uint64_t WH, uint32_t chunk_cap) {
+    return align256(16ull * chunk_cap * WH) + 2 * align256(16ull * WH) + 256u;
+}
 }  // namespace
 
 extern "C" {
@@ -307,17 +430,15 @@ int32_t tt_server_create(tt_context* ctx, const tt_server_config* config, tt_ser
         srv->ctx = ctx;
         srv->device = context_device(ctx);
         check_cuda(cudaSetDevice(srv->device), "cudaSetDevice");
-        uint32_t inflight = DEFAULT_INFLIGHT;
         if (config) {
             if (config->hbm_budget_bytes) srv->budget = config->hbm_budget_bytes;
-            if (config->max_inflight) inflight = config->max_inflight;
-            if (config->paths_per_request) srv->paths = config->paths_per_request;
+            if (config->max_inflight) srv->max_live = config->max_inflight;
+            if (config->pool_paths) srv->paths = config->pool_paths;
+            if (config->round_items) srv->round_items = config->round_items;
         }
-        need(inflight <= 64, "max_inflight above 64");
-        need(srv->paths <= (1u << 24), "paths_per_request above 2^24");
-        int sms = 0, per_sm = 0;
-        trace_occupancy(&sms, &per_sm);
-        srv->trace_blocks = std::max(1, sms * per_sm);
+        need(srv->max_live <= BATCH_MAX_REQUESTS, "max_inflight above 64");
+        need(srv->paths <= (1u << 24), "pool_paths above 2^24");
+        need(srv->round_items >= 1 && srv->round_items <= (1ull << 30), "round_items must be in [1, 2^30]");
         cudaMemPoolProps props{};
         props.allocType = cudaMemAllocationTypePinned;
         props.location.type = cudaMemLocationTypeDevice;
@@ -325,14 +446,12 @@ int32_t tt_server_create(tt_context* ctx, const tt_server_config* config, tt_ser
         check_cuda(cudaMemPoolCreate(&srv->pool, &props), "cudaMemPoolCreate");
         uint64_t keep = srv->budget;  // keep freed arenas cached up to the budget
         check_cuda(cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep), "pool attribute");
-        srv->slots.resize(inflight);
-        for (Slot& s : srv->slots) {
-            check_cuda(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "stream");
-            check_cuda(cudaStreamCreateWithFlags(&s.capture, cudaStreamNonBlocking), "stream");
-            check_cuda(cudaStreamCreateWithFlags(&s.body, cudaStreamNonBlocking), "stream");
-            check_cuda(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "event");
-            check_cuda(cudaMallocHost((void**)&s.err_host, 16), "cudaMallocHost");
-        }
+        check_cuda(cudaStreamCreateWithFlags(&srv->stream, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaStreamCreateWithFlags(&srv->capture, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaStreamCreateWithFlags(&srv->body, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaEventCreate(&srv->round_start), "event");
+        check_cuda(cudaEventCreate(&srv->round_done), "event");
+        srv->create_pool();
         tt_server* raw = srv.get();
         srv->worker = std::thread([raw] { raw->run(); });
         *out = srv.release();
@@ -349,15 +468,19 @@ int32_t tt_server_destroy(tt_server* server) {
         server->cv.notify_all();
         if (server->worker.joinable()) server->worker.join();
         cudaSetDevice(server->device);
-        for (Slot& s : server->slots) {
-            cudaStreamSynchronize(s.stream);
-            cudaStreamDestroy(s.stream);
-            cudaStreamDestroy(s.capture);
-            cudaStreamDestroy(s.body);
-            cudaEventDestroy(s.done);
-            cudaFreeHost(s.err_host);
-            if (s.staging) cudaFreeHost(s.staging);
-        }
+        cudaStreamSynchronize(server->stream);
+        for (cudaGraphExec_t g : server->graph)
+            if (g) cudaGraphExecDestroy(g);
+        cudaStreamDestroy(server->stream);
+        cudaStreamDestroy(server->capture);
+        cudaStreamDestroy(server->body);
+        cudaEventDestroy(server->round_start);
+        cudaEventDestroy(server->round_done);
+        cudaFreeHost(server->h_reqs);
+        cudaFreeHost(server->h_scenes);
+        cudaFreeHost(server->h_round);
+        cudaFreeHost(server->h_err);
+        for (Staging& s : server->staging_free) cudaFreeHost(s.ptr);
         if (server->pool) cudaMemPoolDestroy(server->pool);
         delete server;
     });
@@ -368,14 +491,19 @@ int32_t tt_server_submit(tt_server* server, tt_handle scene, const tt_constants*
     return server_guarded([&] {
         need(server && constants && host_rgba32f && request_id, "null argument");
         need(constants->sample_count >= 1 && constants->bounce_count >= 1, "sample_count and bounce_count must be >= 1");
+        need(constants->bounce_count < (1u << BATCH_BOUNCE_BITS), "bounce_count must be below 65536");
         uint64_t WH = (uint64_t)constants->screen_size[0] * constants->screen_size[1];
         need(WH > 0 && bytes == 16ull * WH, "byte count must equal width * height * 16");
+        need(WH <= MAX_PIXELS, "more than 4096 x 4096 pixels");
         auto r = std::make_unique<Request>();
         r->sc = scene_view(server->ctx, scene);  // validates the handle on the caller's thread
         r->c = *constants;
         r->host = host_rgba32f;
         r->bytes = bytes;
-        r->arena_bytes = layout_for(*constants, server->paths).total;
+        r->WH = WH;
+        r->chunk_cap = (uint32_t)std::clamp<uint64_t>(server->round_items / WH, 1,
+                                                      std::min<uint32_t>(MAX_CHUNK_SPP, constants->sample_count));
+        r->arena_bytes = arena_bytes(WH, r->chunk_cap);
         r->submitted = Clock::now();
         {
             std::lock_guard<std::mutex> lk(server->mu);
@@ -431,4 +559,3 @@ int32_t tt_server_stats_get(tt_server* server, tt_server_stats* out) {
 }
 
 }  // extern "C"
-

@@ -69,6 +69,42 @@ struct WfParams {
 };
 // SM count and resident blocks per SM of the persistent trace kernel.
 void trace_occupancy(int* sms, int* blocks_per_sm);
+
+// Shared-pool rendering of several requests (the render server): one round renders the next
+// sample chunk of every request in the batch through one path pool.  The round's work items
+// are the requests' chunk items laid end to end (request r owns [item_base, item_base +
+// chunk_items)); a path slot carries its request in bits 16..23 of org.w (the bounce count
+// keeps bits 0..15).  Each request keeps its own Constants, scene, per-sample radiance,
+// running sums, image and error word, so its image is the one it gets rendered alone.
+constexpr uint32_t BATCH_MAX_REQUESTS = 64;
+constexpr uint32_t BATCH_BOUNCE_BITS = 16;
+struct BatchRequest {
+    tt_constants c;
+    XsJump chunk_jump;   // xor_shift advanced by 2 * chunk_sample0 draws
+    float4* samples;     // chunk_spp x WH per-sample radiance of the round's chunk (band order)
+    float4* running;     // WH running per-pixel sums across chunks
+    float4* target;      // WH image
+    uint32_t* err;       // the request's ERR_* word
+    uint32_t scene;      // index into the round's scene table
+    uint32_t WH, item_base, pixel_base;
+    uint32_t chunk_sample0, chunk_spp, chunk_items, last;  // last: the chunk ends the request
+};
+// Round header in device memory (read by the graph's kernels, so that one instantiated graph
+// serves every round): request count, total work items, total pixels, iteration limit.
+struct BatchRound {
+    uint32_t nreq, items, pixels, limit;
+};
+struct BatchParams {
+    const BatchRequest* reqs;  // BATCH_MAX_REQUESTS entries
+    const DevScene* scenes;    // BATCH_MAX_REQUESTS entries
+    const BatchRound* round;
+};
+// Instantiates the graph of one shared-pool round: while (paths are live) { regen, extend,
+// shade, shadow }, then the per-request reductions.  `w` holds the pool (no radiance cache);
+// `tex`: some scene of the batch samples textures (w.ndc_mip allocated).  Launch it after the
+// request table, the scene table and the round header are in place.
+cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, uint32_t* batch_err,
+                                  cudaStream_t cs, cudaStream_t body_stream);
 // Optional per-launch timing: a pair of CUDA events recorded on the launching stream around
 // each integrator launch, tagged with its TT_STAGE_*.  `events` holds 2 * MAX_LAUNCHES events
 // owned by the context; launches past MAX_LAUNCHES are not recorded (overflow).
@@ -122,12 +158,6 @@ struct RestirParams {
     float4* gtex;  // textured scenes: per pixel (u, v, mip level, 0) of the primary hit; else null
     float4* glob;  // per pixel: the primary hit's prepared lobes (LOBE_RECORD float4)
     Reservoir *initial, *temporal, *final_out, *prev;
-    // per 16 x 8 tile (row-major tile order): the tile's pixels whose camera ray hit a surface,
-    // sorted by material bucket, in the tile's 128 entries of `queue`, their number in
-    // queue_count[tile]; the candidate and shade passes run over them (sky pixels are finished
-    // by the G-buffer pass)
-    uint32_t* queue;
-    uint32_t* queue_count;
     RestirHistory history;
     uint32_t candidates, neighbours;
     float m_cap, radius;

@@ -110,48 +110,91 @@ constexpr XsJumpTable xs_jump_table() {
 }
 __constant__ XsJumpTable c_xs_jump = xs_jump_table();
 
+// The camera ray of sample chunk_sample0 + s_local of pixel t (band order) into slot s.
+__device__ __forceinline__ void regen_path(const WfParams& w, const tt_constants& c, const XsJump& chunk_jump,
+                                           uint32_t chunk_sample0, uint32_t WH, uint32_t item, uint32_t s,
+                                           uint32_t org_w) {
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    uint32_t s_local = item / WH, t = item - s_local * WH;
+    uint32_t x, y;
+    band_pixel(t, W, H, x, y);
+    uint32_t pg = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
+    if (chunk_sample0) pg = xs_apply(chunk_jump, pg);
+    for (uint32_t r = s_local; r >= 64u; r -= 64u) pg = xs_apply(c_xs_jump.m[64], pg);  // chunks hold <= 64
+    pg = xs_apply(c_xs_jump.m[s_local & 63u], pg);
+    f2 ndc = pixel_ndc(x, y, W, H, pg);
+    f3 d = camera_ray_direction(c, ndc);
+    if (w.ndc_mip) w.ndc_mip[s] = make_float2(ndc.x, ndc.y);
+    w.org[s] = make_float4(c.camera_position[0], c.camera_position[1], c.camera_position[2], __uint_as_float(org_w));
+    w.dir[s] = pack(d, pg);
+    w.thr[s] = pack(splat(1.0f), item);
+}
+
+// Index of the last of the n ascending `base` entries that is <= v (base[0] == 0 <= v).
+__device__ __forceinline__ uint32_t last_at_most(const uint32_t* base, uint32_t n, uint32_t v) {
+    uint32_t lo = 0u, hi = n;  // base[lo] <= v < base[hi] (base[n] = infinity)
+    while (hi - lo > 1u) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// MULTI: a shared-pool round (BatchParams); the work items of every request of the round are
+// drawn from one counter, and a finished path's radiance goes to its own request's buffer.
+template <bool MULTI>
 __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_constant__ RenderParams p,
-                                                               const __grid_constant__ WfParams w) {
+                                                               const __grid_constant__ WfParams w,
+                                                               const __grid_constant__ BatchParams b) {
     __shared__ uint32_t s_warp[REGEN_BLOCK / 32 + 1];
+    __shared__ uint32_t s_base[MULTI ? BATCH_MAX_REQUESTS : 1];
+    __shared__ uint32_t s_next, s_nreq, s_total;
     uint32_t s = blockIdx.x * REGEN_BLOCK + threadIdx.x;
     bool valid = s < w.P;
     float4 a = valid ? w.acc[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint32_t flags = __float_as_uint(a.w);
     if (valid && (flags & F_TERM)) {
         uint32_t item = __float_as_uint(w.thr[s].w);
-        w.samples[item] = make_float4(a.x, a.y, a.z, 0.0f);
-        if (flags & F_TRAIN)
-            w.train_final[((uint64_t)w.chunk_sample0 * w.WH + item) / w.train_stride] = make_float4(a.x, a.y, a.z, 0.0f);
+        if (MULTI) {
+            uint32_t r = (__float_as_uint(w.org[s].w) >> BATCH_BOUNCE_BITS) & 0xffu;
+            b.reqs[r].samples[item] = make_float4(a.x, a.y, a.z, 0.0f);
+        } else {
+            w.samples[item] = make_float4(a.x, a.y, a.z, 0.0f);
+            if (flags & F_TRAIN)
+                w.train_final[((uint64_t)w.chunk_sample0 * w.WH + item) / w.train_stride] =
+                    make_float4(a.x, a.y, a.z, 0.0f);
+        }
         flags = 0u;
         w.acc[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     bool live = valid && (flags & F_LIVE);
     // whether work items remain: one read of the shared counter per block (a stale value only
     // makes some free slots draw item numbers past the chunk, which they skip)
-    __shared__ uint32_t s_next;
-    if (threadIdx.x == 0) s_next = *(volatile uint32_t*)&w.counters[0];
+    if (threadIdx.x == 0) {
+        s_next = *(volatile uint32_t*)&w.counters[0];
+        if (MULTI) {
+            s_nreq = b.round->nreq;
+            s_total = b.round->items;
+        }
+    }
+    if (MULTI && threadIdx.x < BATCH_MAX_REQUESTS) s_base[threadIdx.x] = b.reqs[threadIdx.x].item_base;
     __syncthreads();
-    bool need = valid && !live && s_next < w.chunk_items;
+    uint32_t total = MULTI ? s_total : w.chunk_items;
+    bool need = valid && !live && s_next < total;
     uint32_t item = block_append<REGEN_BLOCK>(&w.counters[0], need, s_warp);
-    if (need && item < w.chunk_items) {
-        const tt_constants& c = p.c;
-        uint32_t W = c.screen_size[0], H = c.screen_size[1];
-        uint32_t s_local = item / w.WH, t = item - s_local * w.WH;
-        uint32_t x, y;
-        band_pixel(t, W, H, x, y);
-        uint32_t pg = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
-        if (w.chunk_sample0) pg = xs_apply(w.chunk_jump, pg);
-        for (uint32_t r = s_local; r >= 64u; r -= 64u) pg = xs_apply(c_xs_jump.m[64], pg);  // chunks hold <= 64
-        pg = xs_apply(c_xs_jump.m[s_local & 63u], pg);
-        f2 ndc = pixel_ndc(x, y, W, H, pg);
-        f3 d = camera_ray_direction(c, ndc);
-        if (w.ndc_mip) w.ndc_mip[s] = make_float2(ndc.x, ndc.y);
-        w.org[s] = make_float4(c.camera_position[0], c.camera_position[1], c.camera_position[2], __uint_as_float(0u));
-        w.dir[s] = pack(d, pg);
-        w.thr[s] = pack(splat(1.0f), item);
-        bool train = w.cache_on && ((uint64_t)w.chunk_sample0 * w.WH + item) % w.train_stride == 0u;
-        if (w.cache_on) w.spread[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        w.acc[s] = pack(splat(0.0f), F_LIVE | (train ? F_TRAIN : 0u));
+    if (need && item < total) {
+        if (MULTI) {
+            uint32_t r = last_at_most(s_base, s_nreq, item);
+            const BatchRequest& R = b.reqs[r];
+            regen_path(w, R.c, R.chunk_jump, R.chunk_sample0, R.WH, item - s_base[r], s, r << BATCH_BOUNCE_BITS);
+            w.acc[s] = pack(splat(0.0f), F_LIVE);
+        } else {
+            regen_path(w, p.c, w.chunk_jump, w.chunk_sample0, w.WH, item, s, 0u);
+            bool train = w.cache_on && ((uint64_t)w.chunk_sample0 * w.WH + item) % w.train_stride == 0u;
+            if (w.cache_on) w.spread[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            w.acc[s] = pack(splat(0.0f), F_LIVE | (train ? F_TRAIN : 0u));
+        }
         live = true;
     }
     uint32_t q = block_append<REGEN_BLOCK>(&w.counters[1], live, s_warp);
@@ -169,12 +212,17 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
 #endif
 constexpr int TR_BLOCK = 128;
 
-template <bool COUNT, bool SHADOW, int ACCEL, int STACK = TRAVERSAL_STACK>
+// MULTI: a shared-pool round; each lane traces in the scene of its ray's request and reports
+// traversal errors to that request's error word.
+template <bool COUNT, bool SHADOW, int ACCEL, int STACK = TRAVERSAL_STACK, bool MULTI = false>
 __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel(const __grid_constant__ RenderParams p,
-                                                                const __grid_constant__ WfParams w) {
+                                                                const __grid_constant__ WfParams w,
+                                                                const __grid_constant__ BatchParams b) {
     __shared__ uint32_t s_stack[STACK * TR_BLOCK];
     uint32_t* stack = s_stack + threadIdx.x;
-    const DevScene& sc = p.sc;
+    uint32_t lane_req = 0u, lane_scene = 0u;  // MULTI: request and scene of the lane's ray
+#define TT_SC (MULTI ? b.scenes[lane_scene] : p.sc)
+#define TT_ERR (MULTI ? b.reqs[lane_req].err : p.err)
     const uint32_t n = SHADOW ? w.counters[2] : w.counters[1];
     uint32_t* head = &w.counters[SHADOW ? 4 : 3];
     TraceState st;
@@ -198,22 +246,29 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                 if (idle && my < n) {
                     item = my;
                     float4 o, d;
+                    uint32_t org_w;
                     if (SHADOW) {
                         o = w.shadow[2ull * item];
                         d = w.shadow[2ull * item + 1];
                         slot = __float_as_uint(o.w);
                         light = __float_as_uint(d.w);
+                        org_w = MULTI ? __float_as_uint(w.org[slot].w) : 0u;
                     } else {
                         slot = w.active[item];
                         o = w.org[slot];
                         d = w.dir[slot];
+                        org_w = __float_as_uint(o.w);
                     }
-                    trace_init(st, sc, xyz(o), xyz(d), SHADOW ? SHADOW_TMIN : EXTENSION_TMIN,
+                    if (MULTI) {
+                        lane_req = (org_w >> BATCH_BOUNCE_BITS) & 0xffu;
+                        lane_scene = b.reqs[lane_req].scene;
+                    }
+                    trace_init(st, TT_SC, xyz(o), xyz(d), SHADOW ? SHADOW_TMIN : EXTENSION_TMIN,
                                SHADOW ? SHADOW_TMAX : EXTENSION_TMAX, !SHADOW);
                     if (SHADOW) {
                         uint32_t hash = __float_as_uint(w.pa1[slot].w) >> 16;
                         uint32_t exact = __float_as_uint(w.pa0[slot].w);
-                        int mode = shadow_target(sc, light, hash, exact, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX,
+                        int mode = shadow_target(TT_SC, light, hash, exact, xyz(o), xyz(d), SHADOW_TMIN, SHADOW_TMAX,
                                                  st.best, st.tbest);
                         if (mode == 0) trace_stop(st);  // not visible: the first step finishes
                         seeded = mode == 1;
@@ -228,7 +283,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
         if (!__any_sync(0xffffffffu, active)) break;
         while (true) {
             bool fin = false;
-            if (active && (trace_step<COUNT, ACCEL, SHADOW, STACK>(st, sc, stack, TR_BLOCK, p.err, cnt) ||
+            if (active && (trace_step<COUNT, ACCEL, SHADOW, STACK>(st, TT_SC, stack, TR_BLOCK, TT_ERR, cnt) ||
                            (SHADOW && seeded && (st.best.prim != target_prim || st.best.instance != light)))) {
                 fin = true;
                 active = false;
@@ -239,7 +294,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                     float4 a1 = w.pa1[slot];
                     uint32_t pflags = __float_as_uint(a1.w);
                     float4 a0 = w.pa0[slot];
-                    bool vis = light_visible(sc, h, light, pflags >> 16, __float_as_uint(a0.w));
+                    bool vis = light_visible(TT_SC, h, light, pflags >> 16, __float_as_uint(a0.w));
                     float4 a4 = w.acc[slot];
                     f3 acc = xyz(a4);
                     acc += vis ? xyz(a1) : xyz(a0);
@@ -250,7 +305,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                 // hits go to the compacted shading queue; a miss adds the sky (integrate.glsl:272-276)
                 // one queue per material bucket, so that the shade stage's warps share lobe sets
                 bool is_hit = fin && h.hit;
-                uint32_t bucket = is_hit ? (uint32_t)__ldg(sc.inst_bucket + h.instance) : 0u;
+                uint32_t bucket = is_hit ? (uint32_t)__ldg(TT_SC.inst_bucket + h.instance) : 0u;
                 uint32_t pos = 0u;
 #pragma unroll
                 for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
@@ -289,13 +344,17 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
         }
     }
 }
+#undef TT_SC
+#undef TT_ERR
 
 #ifndef TT_SHADE_MIN_BLOCKS
 #define TT_SHADE_MIN_BLOCKS 6
 #endif
-template <bool CACHE, bool TEX>
+// MULTI: a shared-pool round; each path shades with its request's Constants and scene.
+template <bool CACHE, bool TEX, bool MULTI = false>
 __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel(const __grid_constant__ RenderParams p,
-                                                            const __grid_constant__ WfParams w) {
+                                                            const __grid_constant__ WfParams w,
+                                                            const __grid_constant__ BatchParams b) {
     // thread q shades entry q of the bucket queues laid end to end
     uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
     uint64_t at = 0;
@@ -316,13 +375,15 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
     f3 rec_thr = splat(0.0f), rec_before = splat(0.0f);
     uint32_t rec_path = 0;
     if (have) {
-        const tt_constants& c = p.c;
-        const DevScene& sc = p.sc;
         s = w.hslot[at];
         uint4 hv = w.hit[at];
         float4 o4 = w.org[s], d4 = w.dir[s], t4 = w.thr[s], a4 = w.acc[s];
+        uint32_t ow = __float_as_uint(o4.w);
+        uint32_t req = MULTI ? (ow >> BATCH_BOUNCE_BITS) & 0xffu : 0u;
+        const tt_constants& c = MULTI ? b.reqs[req].c : p.c;
+        const DevScene& sc = MULTI ? b.scenes[b.reqs[req].scene] : p.sc;
         f3 thr = xyz(t4), acc = xyz(a4), ray_dir = xyz(d4);
-        uint32_t g = __float_as_uint(d4.w), bounce = __float_as_uint(o4.w);
+        uint32_t g = __float_as_uint(d4.w), bounce = MULTI ? ow & ((1u << BATCH_BOUNCE_BITS) - 1u) : ow;
         uint32_t train = __float_as_uint(a4.w) & F_TRAIN;
         ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
         float mip_level = 1.0f;
@@ -420,7 +481,7 @@ __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel
                 if (CACHE && w.spread_c > 0.0f) w.spread[s].z = density;
                 f3 new_dir = transform_to_basis(basis, wo);
                 thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
-                w.org[s] = pack(hit.world_position, next);
+                w.org[s] = pack(hit.world_position, MULTI ? next | (req << BATCH_BOUNCE_BITS) : next);
                 w.dir[s] = pack(new_dir, g);
                 w.thr[s] = pack(thr, __float_as_uint(t4.w));
                 w.acc[s] = pack(acc, F_LIVE | train);
@@ -466,26 +527,46 @@ __global__ void wf_cache_apply_kernel(const __grid_constant__ WfParams w) {
 
 // Per pixel: samples of this chunk added in sample order to the running sum; after the last
 // chunk, divide by the sample count and apply the frame accumulation (integrate.glsl:338-346).
-__global__ void wf_reduce_kernel(const __grid_constant__ RenderParams p, const __grid_constant__ WfParams w,
-                                 int last) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= w.WH) return;
-    const tt_constants& c = p.c;
-    f3 acc = w.chunk_sample0 == 0u ? splat(0.0f) : xyz(w.running[t]);
-    for (uint32_t sl = 0; sl < w.chunk_spp; ++sl) acc += xyz(w.samples[(uint64_t)sl * w.WH + t]);
+__device__ __forceinline__ void reduce_pixel(const tt_constants& c, uint32_t WH, uint32_t chunk_sample0,
+                                             uint32_t chunk_spp, const float4* samples, float4* running,
+                                             float4* target, bool last, uint32_t t) {
+    f3 acc = chunk_sample0 == 0u ? splat(0.0f) : xyz(running[t]);
+    for (uint32_t sl = 0; sl < chunk_spp; ++sl) acc += xyz(samples[(uint64_t)sl * WH + t]);
     if (!last) {
-        w.running[t] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+        running[t] = make_float4(acc.x, acc.y, acc.z, 0.0f);
         return;
     }
     uint32_t x, y;
     band_pixel(t, c.screen_size[0], c.screen_size[1], x, y);
     acc = acc / (float)c.sample_count;
-    float4* tp = p.target + (uint64_t)y * c.screen_size[0] + x;
+    float4* tp = target + (uint64_t)y * c.screen_size[0] + x;
     if (c.accumulated_frame_count != 0) {
         float4 prev = *tp;
         acc = (xyz(prev) * (float)(c.accumulated_frame_count - 1u) + acc) / (float)c.accumulated_frame_count;
     }
     *tp = make_float4(acc.x, acc.y, acc.z, 1.0f);
+}
+
+__global__ void wf_reduce_kernel(const __grid_constant__ RenderParams p, const __grid_constant__ WfParams w,
+                                 int last) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= w.WH) return;
+    reduce_pixel(p.c, w.WH, w.chunk_sample0, w.chunk_spp, w.samples, w.running, p.target, last != 0, t);
+}
+
+// The reductions of a shared-pool round: the requests' pixels laid end to end (request r owns
+// [pixel_base, pixel_base + WH)), grid-stride over all of them.
+__global__ void __launch_bounds__(256) wf_reduce_batch_kernel(const __grid_constant__ BatchParams b) {
+    __shared__ uint32_t s_base[BATCH_MAX_REQUESTS];
+    if (threadIdx.x < BATCH_MAX_REQUESTS) s_base[threadIdx.x] = b.reqs[threadIdx.x].pixel_base;
+    __syncthreads();
+    uint32_t nreq = b.round->nreq, total = b.round->pixels;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        uint32_t r = last_at_most(s_base, nreq, g);
+        const BatchRequest& R = b.reqs[r];
+        reduce_pixel(R.c, R.WH, R.chunk_sample0, R.chunk_spp, R.samples, R.running, R.target, R.last != 0u,
+                     g - s_base[r]);
+    }
 }
 
 template <bool SHADOW>
@@ -495,31 +576,31 @@ template <bool SHADOW>
 static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid, bool counted, cudaStream_t st) {
     bool short_stack = !counted && p.sc.stack_need <= (uint32_t)SHORT_TRAVERSAL_STACK;
     if (p.sc.wide) {
-        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_WIDE_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_WIDE_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
         else if (short_stack)
-            wf_trace_kernel<false, SHADOW, ACCEL_WIDE_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w);
-        else wf_trace_kernel<false, SHADOW, ACCEL_WIDE_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+            wf_trace_kernel<false, SHADOW, ACCEL_WIDE_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
+        else wf_trace_kernel<false, SHADOW, ACCEL_WIDE_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
     } else if (p.sc.flat) {
-        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
         else if (short_stack)
-            wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w);
-        else wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+            wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
+        else wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
     } else {
-        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_TWO_LEVEL_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+        if (counted) wf_trace_kernel<true, SHADOW, ACCEL_TWO_LEVEL_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
         else if (short_stack)
-            wf_trace_kernel<false, SHADOW, ACCEL_TWO_LEVEL_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w);
-        else wf_trace_kernel<false, SHADOW, ACCEL_TWO_LEVEL_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w);
+            wf_trace_kernel<false, SHADOW, ACCEL_TWO_LEVEL_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
+        else wf_trace_kernel<false, SHADOW, ACCEL_TWO_LEVEL_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
     }
 }
 
 static void launch_shade(const RenderParams& p, const WfParams& w, unsigned grid, cudaStream_t st) {
     bool tex = p.sc.textured != 0u;
     if (w.cache_on) {
-        if (tex) wf_shade_kernel<true, true><<<grid, WF_BLOCK, 0, st>>>(p, w);
-        else wf_shade_kernel<true, false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+        if (tex) wf_shade_kernel<true, true><<<grid, WF_BLOCK, 0, st>>>(p, w, BatchParams{});
+        else wf_shade_kernel<true, false><<<grid, WF_BLOCK, 0, st>>>(p, w, BatchParams{});
     } else {
-        if (tex) wf_shade_kernel<false, true><<<grid, WF_BLOCK, 0, st>>>(p, w);
-        else wf_shade_kernel<false, false><<<grid, WF_BLOCK, 0, st>>>(p, w);
+        if (tex) wf_shade_kernel<false, true><<<grid, WF_BLOCK, 0, st>>>(p, w, BatchParams{});
+        else wf_shade_kernel<false, false><<<grid, WF_BLOCK, 0, st>>>(p, w, BatchParams{});
     }
 }
 
@@ -529,6 +610,17 @@ __global__ void wf_control_kernel(uint32_t* counters, cudaGraphConditionalHandle
                                   uint32_t* err) {
     uint32_t n = counters[1];
     uint32_t it = ++counters[CTRL_ITERATION];
+    bool more = n > 0u && it < limit;
+    if (n > 0u && it >= limit) atomicOr(err, ERR_ITERATION_LIMIT);
+    cudaGraphSetConditional(handle, more ? 1u : 0u);
+}
+
+// The same control for a shared-pool round, whose iteration limit is in the round header.
+__global__ void wf_control_batch_kernel(uint32_t* counters, cudaGraphConditionalHandle handle,
+                                        const BatchRound* round, uint32_t* err) {
+    uint32_t n = counters[1];
+    uint32_t it = ++counters[CTRL_ITERATION];
+    uint32_t limit = round->limit;
     bool more = n > 0u && it < limit;
     if (n > 0u && it >= limit) atomicOr(err, ERR_ITERATION_LIMIT);
     cudaGraphSetConditional(handle, more ? 1u : 0u);
@@ -586,7 +678,7 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
         uint64_t rounds = (uint64_t)w.chunk_items / w.P + 1u;
         uint32_t limit = (uint32_t)std::min<uint64_t>(2ull * rounds * (c.bounce_count + 2u) + 16u, 0x7fffffffu);
         check_cuda(cudaMemsetAsync(w.counters + 1, 0, 4ull * (WF_COUNTERS - 1), body_stream), "memset");
-        wf_regen_kernel<<<regen_grid, REGEN_BLOCK, 0, body_stream>>>(p, w);
+        wf_regen_kernel<false><<<regen_grid, REGEN_BLOCK, 0, body_stream>>>(p, w, BatchParams{});
         wf_control_kernel<<<1, 1, 0, body_stream>>>(w.counters, handle, limit, p.err);
         launch_trace<false>(p, w, tgrid, counted, body_stream);
         launch_shade(p, w, shade_grid, body_stream);
@@ -611,6 +703,61 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
     check_cuda(e, "cudaGraphLaunch");
 }
 
+cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, uint32_t* batch_err,
+                                  cudaStream_t cs, cudaStream_t body_stream) {
+    RenderParams p{};  // the shared-pool kernels read only its batch error word
+    p.err = batch_err;
+    unsigned regen_grid = (w.P + REGEN_BLOCK - 1) / REGEN_BLOCK;
+    unsigned shade_grid = (w.P + WF_BLOCK - 1) / WF_BLOCK;
+    int sms = 0, dev = 0, ext_per_sm = 0, shadow_per_sm = 0;
+    check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+    auto ext = wf_trace_kernel<false, false, ACCEL_ANY, TRAVERSAL_STACK, true>;
+    auto shadow = wf_trace_kernel<false, true, ACCEL_ANY, TRAVERSAL_STACK, true>;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, ext, TR_BLOCK, 0), "occupancy");
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shadow_per_sm, shadow, TR_BLOCK, 0), "occupancy");
+    unsigned ext_grid = (unsigned)std::max(1, sms * ext_per_sm), shadow_grid = (unsigned)std::max(1, sms * shadow_per_sm);
+    cudaGraph_t g = nullptr;
+    check_cuda(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+    check_cuda(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "capture");
+    check_cuda(cudaMemsetAsync(w.acc, 0, 16ull * w.P, cs), "memset");  // every slot starts free
+    check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CTRL_WORDS, cs), "memset");
+    cudaStreamCaptureStatus status;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    check_cuda(cudaStreamGetCaptureInfo(cs, &status, nullptr, &cg, &deps, nullptr, &ndeps), "capture info");
+    cudaGraphConditionalHandle handle;
+    check_cuda(cudaGraphConditionalHandleCreate(&handle, cg, 1u, cudaGraphCondAssignDefault), "conditional handle");
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop;
+    check_cuda(cudaGraphAddNode(&loop, cg, deps, nullptr, ndeps, &cp), "conditional node");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    check_cuda(cudaStreamBeginCaptureToGraph(body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+               "body capture");
+    check_cuda(cudaMemsetAsync(w.counters + 1, 0, 4ull * (WF_COUNTERS - 1), body_stream), "memset");
+    wf_regen_kernel<true><<<regen_grid, REGEN_BLOCK, 0, body_stream>>>(p, w, b);
+    wf_control_batch_kernel<<<1, 1, 0, body_stream>>>(w.counters, handle, b.round, batch_err);
+    ext<<<ext_grid, TR_BLOCK, 0, body_stream>>>(p, w, b);
+    if (tex) wf_shade_kernel<false, true, true><<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w, b);
+    else wf_shade_kernel<false, false, true><<<shade_grid, WF_BLOCK, 0, body_stream>>>(p, w, b);
+    shadow<<<shadow_grid, TR_BLOCK, 0, body_stream>>>(p, w, b);
+    check_cuda(cudaStreamEndCapture(body_stream, &body), "body capture end");
+    check_cuda(cudaStreamUpdateCaptureDependencies(cs, &loop, nullptr, 1, cudaStreamSetCaptureDependencies),
+               "capture dependencies");
+    wf_reduce_batch_kernel<<<(unsigned)(4 * sms), 256, 0, cs>>>(b);
+    check_cuda(cudaStreamEndCapture(cs, &g), "capture end");
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    check_cuda(e, "cudaGraphInstantiate");
+    return exec;
+}
+
 void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
                       StageTimer* timer) {
     const tt_constants& c = p.c;
@@ -631,7 +778,7 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
         while (true) {
             check_cuda(cudaMemsetAsync(w.counters + 1, 0, 4ull * (WF_COUNTERS - 1), st), "memset");
             stage_begin(timer, TT_STAGE_REGEN, st);
-            wf_regen_kernel<<<regen_grid, REGEN_BLOCK, 0, st>>>(p, w);
+            wf_regen_kernel<false><<<regen_grid, REGEN_BLOCK, 0, st>>>(p, w, BatchParams{});
             stage_end(timer, st);
             check_cuda(cudaMemcpyAsync(host_count, w.counters + 1, 4, cudaMemcpyDeviceToHost, st), "count");
             check_cuda(cudaStreamSynchronize(st), "sync");

@@ -237,12 +237,14 @@ class TuneResult(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
-                ("paths_per_request", ctypes.c_uint32)]
+                ("pool_paths", ctypes.c_uint32), ("round_items", ctypes.c_uint64)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "queued", "inflight",
-                                               "bytes_in_flight", "peak_bytes_in_flight", "peak_inflight")]
+                                               "bytes_in_flight", "peak_bytes_in_flight", "peak_inflight",
+                                               "rounds", "round_items", "gpu_busy_ns", "admit_ns", "launch_ns",
+                                               "copy_out_ns", "wait_ns")]
 
 
 class TraversalCounters(ctypes.Structure):

@@ -2,8 +2,9 @@
 
 Scenes are created on the server's Context first and stay resident; `submit` queues a
 request (scene, Constants, a host RGBA32F buffer the image lands in) and returns its id; the
-library's scheduler thread admits requests in arrival order as execution slots and HBM budget
-free up and runs them concurrently on the device.
+library's scheduler thread admits requests in arrival order as room in the batch and HBM budget
+free up, and renders the admitted requests together, round by round, through one shared
+wavefront path pool.
 """
 from __future__ import annotations
 
@@ -18,10 +19,10 @@ from .renderer import Context, SceneArrays
 
 class RenderServer:
     def __init__(self, context: Context, hbm_budget_bytes: int = 0, max_inflight: int = 0,
-                 paths_per_request: int = 0):
+                 pool_paths: int = 0, round_items: int = 0):
         self.context = context
         self.lib = context.lib
-        cfg = native.ServerConfig(hbm_budget_bytes, max_inflight, paths_per_request)
+        cfg = native.ServerConfig(hbm_budget_bytes, max_inflight, pool_paths, round_items)
         h = ctypes.c_void_p()
         check(self.lib.tt_server_create(context.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h
