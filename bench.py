@@ -64,7 +64,7 @@ def parse_args():
     p.add_argument("--no-textured", action="store_true", help="skip the textured-materials sample")
     p.add_argument("--no-ingest", action="store_true", help="skip the device mesh-ingest sample")
     p.add_argument("--no-light-selection", action="store_true", help="skip the light-selection sample")
-    p.add_argument("--serve-batch", type=int, default=64, help="requests of the serving sample's capacity run")
+    p.add_argument("--serve-batch", type=int, default=96, help="requests of the serving sample's capacity run")
     p.add_argument("--serve-requests", type=int, default=512,
                    help="requests at 0.8 x capacity in the serving sample (a quarter as many at 0.5 x and 1.1 x)")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level", "wide"],
@@ -875,7 +875,8 @@ def run_serving(a, ctx) -> dict:
     triangles), HBM budget 150 GB, up to 16 requests rendered together per round through one
     shared path pool whose size tt_autotune picks on a request of the mix (the 260k-triangle
     scene at 1024 x 1024, 4 spp, depth 8).  First the server's capacity: a batch of
-    a.serve_batch requests submitted at once (completions per second over the makespan).  Then
+    a.serve_batch requests submitted at once gives the saturated sample throughput, which over
+    the mix's mean request size gives requests per second.  Then
     Poisson arrivals at fractions of that capacity: a.serve_requests requests at 0.8 x capacity and
     a quarter as many at 0.5 x and 1.1 x; a rate is sustained when its completions keep pace with
     its arrivals (completed per second >= 0.95 x offered) and the latency does not grow over the
@@ -906,8 +907,14 @@ def run_serving(a, ctx) -> dict:
            "mix": "side ~U{256..2048} step 16, spp ~U{1..256}, depth 8, scene log-uniform 1e3..5e6 triangles"}
     serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng, pool_paths)  # warm-up: graphs, pool, caches
     cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng, pool_paths)
-    mu = cap["completed_per_s"]
+    # capacity in requests per second: the sample throughput of the saturated server over the mix's
+    # mean request size (E[side^2] E[spp], side = 16 k with k ~ U{16..128}, spp ~ U{1..256}), not
+    # the completion rate of one finite batch, whose few large requests decide its makespan
+    k = np.arange(16, 129, dtype=np.float64)
+    mean_samples = float(np.mean((16.0 * k) ** 2)) * 128.5
+    mu = cap["throughput_msamples_s"] * 1e6 / mean_samples
     out["capacity"] = cap
+    out["mean_request_msamples"] = mean_samples / 1e6
     out["capacity_per_s"] = mu
     out["rates"] = []
     frame = 10_000

@@ -18,7 +18,7 @@ namespace tt {
 
 constexpr int TILE_W = 16, TILE_H = 8, BLOCK = TILE_W * TILE_H;
 
-template <bool COUNT, bool TEX>
+template <bool COUNT, bool TEX, int ACCEL>
 __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant__ RenderParams p) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * BLOCK];
     const tt_constants& c = p.c;
@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
             float mip_level = 1.0f;  // integrate.glsl:215-216
             for (uint32_t bounce = 0; bounce < c.bounce_count; ++bounce) {
                 if (COUNT) rays++;
-                Hit h = trace_closest<COUNT>(sc, ray_org, ray_dir, EXTENSION_TMIN, EXTENSION_TMAX, true,
+                Hit h = trace_closest<COUNT, ACCEL>(sc, ray_org, ray_dir, EXTENSION_TMIN, EXTENSION_TMAX, true,
                                              stack, BLOCK, p.err, cnt);
                 if (!h.hit) {
                     path_acc += splat(1.0f) * thr;
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
                 if (nee) {
                     if (COUNT) rays++;
                     LightSample ls = sample_light(sc, hit.world_position, basis, g);
-                    Hit hs = trace_closest<COUNT>(sc, hit.world_position, ls.dir, SHADOW_TMIN, SHADOW_TMAX, false,
+                    Hit hs = trace_closest<COUNT, ACCEL>(sc, hit.world_position, ls.dir, SHADOW_TMIN, SHADOW_TMAX, false,
                                                   stack, BLOCK, p.err, cnt);
                     f3 direct = light_visible(sc, hs, ls.instance, ls.hash, ls.prim) ? light_contribution<TEX>(sc, ls, mc, lobes, wi)
                                                                            : splat(0.0f);
@@ -162,6 +162,7 @@ __global__ void bsdf_sample_kernel(const MatC* m, const float4* samples, uint32_
     results[3 * i + 1] = make_float4(wo.x, wo.y, wo.z, (float)lobe);
     results[3 * i + 2] = make_float4(__uint_as_float(g), 0.0f, 0.0f, 0.0f);
 }
+template <int ACCEL>
 __global__ void __launch_bounds__(BLOCK) trace_kernel(DevScene sc, const float4* rays, uint32_t n,
                                                       uint32_t flags, uint4* hits, uint32_t* err) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * BLOCK];
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(BLOCK) trace_kernel(DevScene sc, const float4*
     if (i >= n) return;
     float4 a = rays[2 * i], b = rays[2 * i + 1];
     Counters cnt{0u, 0u, 0u, 0u};
-    Hit h = trace_closest<false>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, a.w, b.w,
+    Hit h = trace_closest<false, ACCEL>(sc, f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, a.w, b.w,
                                  (flags & TT_TRACE_CULL_BACK_FACES) != 0u, s_stack + threadIdx.x,
                                  BLOCK, err, cnt);
     if (h.hit) {
@@ -239,13 +240,16 @@ void launch_light_records(const DevScene& sc, float4* rec, uint32_t n, cudaStrea
 
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st) {
     dim3 grid((p.c.screen_size[0] + TILE_W - 1) / TILE_W, (p.c.screen_size[1] + TILE_H - 1) / TILE_H);
-    if (p.sc.textured) {
-        if (counted) integrate_kernel<true, true><<<grid, BLOCK, 0, st>>>(p);
-        else integrate_kernel<false, true><<<grid, BLOCK, 0, st>>>(p);
-    } else {
-        if (counted) integrate_kernel<true, false><<<grid, BLOCK, 0, st>>>(p);
-        else integrate_kernel<false, false><<<grid, BLOCK, 0, st>>>(p);
-    }
+    dispatch_accel(p.sc, [&](auto accel) {
+        constexpr int A = decltype(accel)::value;
+        if (p.sc.textured) {
+            if (counted) integrate_kernel<true, true, A><<<grid, BLOCK, 0, st>>>(p);
+            else integrate_kernel<false, true, A><<<grid, BLOCK, 0, st>>>(p);
+        } else {
+            if (counted) integrate_kernel<true, false, A><<<grid, BLOCK, 0, st>>>(p);
+            else integrate_kernel<false, false, A><<<grid, BLOCK, 0, st>>>(p);
+        }
+    });
 }
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out, cudaStream_t st) {
     if (n == 0) return;
@@ -259,7 +263,10 @@ void launch_bsdf_sample(const MatC* m, const float4* s, uint32_t n, float4* r, c
 }
 void launch_trace(const DevScene& sc, const float4* rays, uint32_t n, uint32_t flags, uint4* hits,
                   uint32_t* err, cudaStream_t st) {
-    if (n) trace_kernel<<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(sc, rays, n, flags, hits, err);
+    if (n)
+        dispatch_accel(sc, [&](auto accel) {
+            trace_kernel<decltype(accel)::value><<<(n + BLOCK - 1) / BLOCK, BLOCK, 0, st>>>(sc, rays, n, flags, hits, err);
+        });
 }
 // textureLod of one texture at (u, v, lod) triples, for parity tests of the decoders and filter.
 __global__ void texture_sample_kernel(DevScene sc, uint32_t index, const float* uvl, uint32_t n, float4* out) {

@@ -66,7 +66,7 @@ __device__ __forceinline__ float target_of(const DevScene& sc, const ShadingStat
     return luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
 }
 
-template <bool TEX>
+template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
                                                                   Surface* gbuf, float4* gtex, float4* glob) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     f3 dir = camera_ray_direction(c, ndc);
     f3 org = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
     Counters cnt{0u, 0u, 0u, 0u};
-    Hit h = trace_closest<false>(sc, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true, s_stack + threadIdx.x, RT_BLOCK,
+    Hit h = trace_closest<false, ACCEL>(sc, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true, s_stack + threadIdx.x, RT_BLOCK,
                                  p.err, cnt);
     Surface s;
     if (!h.hit) {
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     gbuf[(uint64_t)y * W + x] = s;
 }
 
-template <bool TEX>
+template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_constant__ RenderParams p,
                                                                   const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   Reservoir* out, uint32_t candidates) {
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_c
         r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
         if (r.W > 0.0f) {
             LightPoint lp = light_point<TEX>(sc, r.light, r.r1, r.r2);
-            if (!restir_visible<false>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err)) r.W = 0.0f;
+            if (!restir_visible<false, ACCEL>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err)) r.W = 0.0f;
         }
     }
     out[i] = r;
@@ -197,7 +197,7 @@ __device__ __forceinline__ bool similar(const Surface& q, f3 normal, float dist)
     return dot(n, normal) > 0.90630779f && fabsf(q.pos_dist.w - dist) <= 0.1f * dist;
 }
 
-template <bool TEX>
+template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_constant__ RenderParams p,
                                                                    const __grid_constant__ RestirHistory hist,
                                                                    const Surface* gbuf, const float4* gtex, const float4* glob,
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_
     out[i] = r;
 }
 
-template <bool TEX>
+template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_constant__ RenderParams p,
                                                                   const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   const Reservoir* in,
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
     out[i] = r;
 }
 
-template <bool TEX>
+template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_constant__ RenderParams p,
                                                                 const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                 const Reservoir* res) {
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
         if (r.light != NO_LIGHT && r.W > 0.0f) {
             LightPoint lp = light_point<TEX>(sc, r.light, r.r1, r.r2);
             f3 contrib = restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp);
-            if (restir_visible<false>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err))
+            if (restir_visible<false, ACCEL>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err))
                 radiance += contrib * r.W;
         }
     }
@@ -303,32 +303,34 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
     *tp = make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
 }
 
-template <bool TEX>
+template <bool TEX, int ACCEL>
 static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer) {
     const tt_constants& c = p.c;
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
     stage_begin(timer, TT_STAGE_RESTIR_GBUFFER, st);
-    restir_gbuffer_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob);
+    restir_gbuffer_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_INITIAL, st);
-    restir_initial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
+    restir_initial_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_TEMPORAL, st);
-    restir_temporal_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.glob, rp.prev_gbuf,
+    restir_temporal_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.glob, rp.prev_gbuf,
                                                            rp.initial, rp.prev, rp.temporal, rp.m_cap);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_SPATIAL, st);
-    restir_spatial_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.temporal, rp.final_out,
+    restir_spatial_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.temporal, rp.final_out,
                                                           rp.neighbours, rp.radius);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_SHADE, st);
-    restir_shade_kernel<TEX><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
+    restir_shade_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
     stage_end(timer, st);
 }
 
 void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer) {
-    if (p.sc.textured && rp.gtex) restir_passes<true>(p, rp, st, timer);
-    else restir_passes<false>(p, rp, st, timer);
+    dispatch_accel(p.sc, [&](auto accel) {
+        if (p.sc.textured && rp.gtex) restir_passes<true, decltype(accel)::value>(p, rp, st, timer);
+        else restir_passes<false, decltype(accel)::value>(p, rp, st, timer);
+    });
 }
 
 }  // namespace tt

@@ -667,15 +667,18 @@ __device__ __forceinline__ bool trace_step_wide(TraceState& st, const DevScene& 
 }
 
 // ACCEL: ACCEL_ANY dispatches on the scene at run time; ACCEL_FLAT_ONLY, ACCEL_TWO_LEVEL_ONLY and
-// ACCEL_WIDE_ONLY compile one structure's step (the caller has checked sc.flat and sc.wide).
-constexpr int ACCEL_ANY = 0, ACCEL_FLAT_ONLY = 1, ACCEL_TWO_LEVEL_ONLY = 2, ACCEL_WIDE_ONLY = 3;
+// ACCEL_WIDE_ONLY compile one structure's step (the caller has checked sc.flat and sc.wide);
+// ACCEL_NO_WIDE dispatches between the flat and the two-level step (no scene is wide).  Kernels
+// compile the variant they need: every step compiled into a loop enlarges it, and a loop that
+// holds all three ran the ReSTIR passes measurably slower on flat scenes.
+constexpr int ACCEL_ANY = 0, ACCEL_FLAT_ONLY = 1, ACCEL_TWO_LEVEL_ONLY = 2, ACCEL_WIDE_ONLY = 3, ACCEL_NO_WIDE = 4;
 
 template <bool COUNT, int ACCEL = ACCEL_ANY, bool EARLY = false, int STACK = TRAVERSAL_STACK>
 __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, uint32_t* stack, int stride,
                                            uint32_t* err, Counters& cnt) {
     if (ACCEL == ACCEL_WIDE_ONLY || (ACCEL == ACCEL_ANY && sc.wide))
         return trace_step_wide<COUNT, STACK>(st, sc, stack, stride, err, cnt);
-    if (ACCEL == ACCEL_FLAT_ONLY || (ACCEL == ACCEL_ANY && sc.flat))
+    if (ACCEL == ACCEL_FLAT_ONLY || ((ACCEL == ACCEL_ANY || ACCEL == ACCEL_NO_WIDE) && sc.flat))
         return trace_step_flat<COUNT, EARLY, STACK>(st, sc, stack, stride, err, cnt);
     if (++st.iterations > TRAVERSAL_ITERATION_LIMIT) {
         atomicOr(err, ERR_ITERATION_LIMIT);
@@ -747,12 +750,12 @@ __device__ __forceinline__ bool trace_step(TraceState& st, const DevScene& sc, u
 }
 
 // Closest hit, run to completion.
-template <bool COUNT>
+template <bool COUNT, int ACCEL = ACCEL_ANY>
 __device__ __forceinline__ Hit trace_closest(const DevScene& sc, f3 o, f3 d, float tmin, float tmax, bool cull,
                                              uint32_t* stack, int stride, uint32_t* err, Counters& cnt) {
     TraceState st;
     trace_init(st, sc, o, d, tmin, tmax, cull);
-    while (!trace_step<COUNT>(st, sc, stack, stride, err, cnt)) {
+    while (!trace_step<COUNT, ACCEL>(st, sc, stack, stride, err, cnt)) {
     }
     return st.best;
 }

@@ -4,10 +4,20 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "../../include/tinytrace_cuda.h"
 #include "tt_bvh.cuh"
 
 namespace tt {
+
+// Calls f with the traversal variant of scene sc (ACCEL_*) as a compile-time constant.
+template <class F>
+inline void dispatch_accel(const DevScene& sc, F&& f) {
+    if (sc.wide) f(std::integral_constant<int, ACCEL_WIDE_ONLY>{});
+    else if (sc.flat) f(std::integral_constant<int, ACCEL_FLAT_ONLY>{});
+    else f(std::integral_constant<int, ACCEL_TWO_LEVEL_ONLY>{});
+}
 
 struct RenderParams {
     DevScene sc;
@@ -101,9 +111,10 @@ struct BatchParams {
 };
 // Instantiates the graph of one shared-pool round: while (paths are live) { regen, extend,
 // shade, shadow }, then the per-request reductions.  `w` holds the pool (no radiance cache);
-// `tex`: some scene of the batch samples textures (w.ndc_mip allocated).  Launch it after the
-// request table, the scene table and the round header are in place.
-cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, uint32_t* batch_err,
+// `tex`: some scene of the batch samples textures (w.ndc_mip allocated); `wide`: some scene of
+// the batch has the compressed wide structure (its traversal step is compiled in only then).
+// Launch it after the request table, the scene table and the round header are in place.
+cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, bool wide, uint32_t* batch_err,
                                   cudaStream_t cs, cudaStream_t body_stream);
 // Optional per-launch timing: a pair of CUDA events recorded on the launching stream around
 // each integrator launch, tagged with its TT_STAGE_*.  `events` holds 2 * MAX_LAUNCHES events

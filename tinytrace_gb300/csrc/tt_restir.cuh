@@ -145,7 +145,7 @@ TT_HD Reservoir empty_reservoir() {
 // traversal starts from the ray's hit on that triangle (seed_triangle_hit, computed as the
 // traversal computes it), so it only searches for a closer hit and stops at the first one:
 // the same answer as a full closest-hit query followed by the comparison.
-template <bool COUNT>
+template <bool COUNT, int ACCEL = ACCEL_ANY>
 __device__ __forceinline__ bool restir_visible(const DevScene& sc, f3 pos, const LightPoint& lp, uint32_t light,
                                                uint32_t* stack, int stride, uint32_t* err) {
     f3 d = lp.pos - pos;
@@ -159,7 +159,7 @@ __device__ __forceinline__ bool restir_visible(const DevScene& sc, f3 pos, const
                            SHADOW_TMIN, SHADOW_TMAX, st.best, st.tbest))
         return false;
     Counters cnt{0u, 0u, 0u, 0u};
-    while (!trace_step<COUNT, ACCEL_ANY, true>(st, sc, stack, stride, err, cnt))
+    while (!trace_step<COUNT, ACCEL, true>(st, sc, stack, stride, err, cnt))
         if (st.best.prim != prim || st.best.instance != lp.instance) return false;  // a closer hit occludes
     return st.best.hit && st.best.instance == lp.instance && st.best.prim == prim;
 }
