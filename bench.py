@@ -64,6 +64,7 @@ def parse_args():
     p.add_argument("--no-textured", action="store_true", help="skip the textured-materials sample")
     p.add_argument("--no-ingest", action="store_true", help="skip the device mesh-ingest sample")
     p.add_argument("--no-light-selection", action="store_true", help="skip the light-selection sample")
+    p.add_argument("--no-closed", action="store_true", help="skip the closed-scene (Cornell box) sample")
     p.add_argument("--serve-batch", type=int, default=96, help="requests of the serving sample's capacity run")
     p.add_argument("--serve-requests", type=int, default=512,
                    help="requests at 0.8 x capacity in the serving sample (a quarter as many at 0.5 x and 1.1 x)")
@@ -684,6 +685,54 @@ def run_textured(a, device: int) -> dict:
     return out
 
 
+# ---------------------------------------------------------------- closed-scene sample
+def run_closed(a, device: int) -> dict:
+    """The per-bounce cost the open benchmark field hides: most of its camera paths leave the
+    scene after one bounce (about 1.5 traced rays per sample), while in the closed Cornell box
+    of the CPU-runnable configuration every path bounces to full depth.  The box at the
+    headline's 1920x1080 and depth 8, 16 spp, autotuned pool: device time (CUDA events, L2
+    flushed before each of 3 frames after 3 warm-up frames), Msamples/s, and traced rays per
+    sample and per second from an instrumented render of the same frame."""
+    import ctypes
+
+    from tinytrace_gb300 import native, scenes
+    from tinytrace_gb300.native import check
+    from tinytrace_gb300.renderer import Config, Renderer
+
+    W, H, spp, frames = a.width, a.height, 16, 3
+    w = scenes.cornell_workload()
+    r = Renderer((W, H), device=device)
+    r.set_scene(w.scene)
+    r.camera = w.camera
+    r.set_config(Config(bounce_count=a.depth, sample_count=spp))
+    lib, ctx = r.context.lib, r.context.handle
+    tune = r.autotune(sample_count=4)
+    for _ in range(3):
+        r.render_to_target()
+        r.present()
+    total = 0.0
+    for _ in range(frames):
+        check(lib.tt_flush_l2(ctx))
+        check(lib.tt_synchronize(ctx))
+        check(lib.tt_event_record(ctx, 6))
+        r.render_to_target()
+        check(lib.tt_event_record(ctx, 7))
+        ms = ctypes.c_float()
+        check(lib.tt_event_elapsed_ms(ctx, 6, 7, ctypes.byref(ms)))
+        total += ms.value
+        r.present()
+    cnt = native.TraversalCounters()
+    c = r.constants()
+    check(lib.tt_render_counted(ctx, r.scene, native.ptr(c), r.render_target, ctypes.byref(cnt)))
+    r.close()
+    samples = W * H * spp
+    ms = total / frames
+    return {"workload": f"cornell_box_{W}x{H}_{spp}spp_d{a.depth}", "ms_per_frame": ms,
+            "msamples_per_s": samples / (ms / 1e3) / 1e6, "rays_per_sample": cnt.rays / samples,
+            "rays_per_s": cnt.rays / (ms / 1e3), "nodes_per_ray": (cnt.blas_nodes + cnt.tlas_nodes) / max(1, cnt.rays),
+            "pool_slots": int(tune.slots), "l2": "flushed before every frame"}
+
+
 # ---------------------------------------------------------------- light-selection sample
 def run_light_selection(a, device: int) -> dict:
     """Power-proportional light selection (TT_LIGHT_SELECTION_POWER, an alias table over the
@@ -870,6 +919,42 @@ def serve_run(ctx, reqs, rate: float | None, rng, pool_paths: int) -> dict:
                             "copy_out": st.copy_out_ns / 1e9, "wait": st.wait_ns / 1e9}}
 
 
+def serve_one_request(ctx, scene, cam, pool_paths: int) -> dict:
+    """The cost of the shared-pool kernels: one 1920x1080, 64-spp, depth-8 request on the 1M-
+    triangle scene, alone, rendered by tt_render (the single-request kernels; CUDA events) and
+    by the server (device time of its rounds from tt_server_stats), same pool size."""
+    import ctypes
+
+    from tinytrace_gb300 import native
+    from tinytrace_gb300.native import check
+    from tinytrace_gb300.renderer import Config, make_constants
+    from tinytrace_gb300.server import RenderServer
+
+    lib, h = ctx.lib, ctx.handle
+    c = make_constants(cam, (1920, 1080), Config(bounce_count=8, sample_count=64), 7, 0)
+    img = ctx.create_image(native.TT_LIFETIME_FRAME, 1920, 1080)
+    check(lib.tt_set_option(h, native.TT_OPTION_WAVEFRONT_SLOTS, pool_paths))
+    for _ in range(2):
+        check(lib.tt_render(h, scene, native.ptr(c), img))
+    check(lib.tt_synchronize(h))
+    check(lib.tt_event_record(h, 6))
+    check(lib.tt_render(h, scene, native.ptr(c), img))
+    check(lib.tt_event_record(h, 7))
+    ms = ctypes.c_float()
+    check(lib.tt_event_elapsed_ms(h, 6, 7, ctypes.byref(ms)))
+    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=SERVE_INFLIGHT, pool_paths=pool_paths) as srv:
+        srv.wait(srv.submit(scene, c))
+        busy0, rounds0 = srv.stats().gpu_busy_ns, srv.stats().rounds
+        t0 = time.perf_counter()
+        srv.wait(srv.submit(scene, c))
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    server_ms = (st.gpu_busy_ns - busy0) / 1e6
+    return {"request": "1920x1080, 64 spp, depth 8, 1,004,520 triangles", "tt_render_ms": ms.value,
+            "server_gpu_ms": server_ms, "server_rounds": int(st.rounds - rounds0), "server_wall_ms": wall * 1e3,
+            "server_over_tt_render": server_ms / ms.value}
+
+
 def run_serving(a, ctx) -> dict:
     """Continuous batching under the C4 request mix on five resident scenes (1e3 .. 5e6
     triangles), HBM budget 150 GB, up to 16 requests rendered together per round through one
@@ -906,6 +991,7 @@ def run_serving(a, ctx) -> dict:
            "round_items": 1 << 26,
            "mix": "side ~U{256..2048} step 16, spp ~U{1..256}, depth 8, scene log-uniform 1e3..5e6 triangles"}
     serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng, pool_paths)  # warm-up: graphs, pool, caches
+    out["one_request"] = serve_one_request(ctx, pool[3][1], cam, pool_paths)
     cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng, pool_paths)
     # capacity in requests per second: the sample throughput of the saturated server over the mix's
     # mean request size (E[side^2] E[spp], side = 16 k with k ~ U{16..128}, spp ~ U{1..256}), not
@@ -1151,6 +1237,11 @@ def run_ours(a, dist: Dist):
                 out_line["textured"] = run_textured(a, device)
             except Exception as e:
                 out_line["textured"] = {"error": f"{type(e).__name__}: {e}"}
+        if not a.no_closed and dist.world == 1:
+            try:
+                out_line["closed_scene"] = run_closed(a, device)
+            except Exception as e:
+                out_line["closed_scene"] = {"error": f"{type(e).__name__}: {e}"}
         if not a.no_light_selection and dist.world == 1:
             try:
                 out_line["light_selection"] = run_light_selection(a, device)

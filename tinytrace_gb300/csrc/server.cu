@@ -97,7 +97,7 @@ struct tt_server {
     BatchRound* h_round = nullptr;
     uint32_t* h_err = nullptr;  // BATCH_MAX_REQUESTS request error words + the batch word
     WfParams w{};
-    cudaGraphExec_t graph[2][2] = {};  // [texture sampling][some scene wide]
+    cudaGraphExec_t graph[2][3][2] = {};  // [texture sampling][BATCH_* structures][short stacks]
     std::vector<Staging> staging_free;
     uint64_t round_items_now = 0;
 
@@ -245,7 +245,7 @@ void tt_server::launch_round(std::vector<Request*>& live) {
     uint64_t share = std::max<uint64_t>(1, round_items / n);
     uint64_t items = 0, pixels = 0;
     uint32_t max_bounce = 1;
-    bool tex = false, wide = false;
+    bool tex = false, wide = false, two_level = false, short_stack = true;
     for (uint32_t k = 0; k < n; ++k) {
         Request& r = *live[k];
         uint32_t left = r.c.sample_count - r.done_spp;
@@ -273,6 +273,8 @@ void tt_server::launch_round(std::vector<Request*>& live) {
         max_bounce = std::max(max_bounce, r.c.bounce_count);
         tex = tex || r.sc.textured != 0u;
         wide = wide || r.sc.wide != 0u;
+        two_level = two_level || r.sc.flat == 0u;
+        short_stack = short_stack && r.sc.stack_need <= (uint32_t)SHORT_TRAVERSAL_STACK;
     }
     h_round->nreq = n;
     h_round->items = (uint32_t)items;
@@ -280,8 +282,10 @@ void tt_server::launch_round(std::vector<Request*>& live) {
     h_round->limit = (uint32_t)std::min<uint64_t>(2ull * (items / w.P + 1u) * (max_bounce + 2u) + 16u, 0x7fffffffu);
     round_items_now = items;
     BatchParams bp{d_reqs.as<BatchRequest>(), d_scenes.as<DevScene>(), d_round.as<BatchRound>()};
-    cudaGraphExec_t& g = graph[tex ? 1 : 0][wide ? 1 : 0];
-    if (!g) g = build_batch_graph(w, bp, tex, wide, d_batch_err.as<uint32_t>(), capture, body);
+    int structures = wide ? BATCH_ANY : (two_level ? BATCH_NO_WIDE : BATCH_FLAT);
+    short_stack = short_stack && !wide;
+    cudaGraphExec_t& g = graph[tex ? 1 : 0][structures][short_stack ? 1 : 0];
+    if (!g) g = build_batch_graph(w, bp, tex, structures, short_stack, d_batch_err.as<uint32_t>(), capture, body);
     check_cuda(cudaEventRecord(round_start, stream), "event");
     check_cuda(cudaMemcpyAsync(d_reqs.ptr, h_reqs, sizeof(BatchRequest) * n, cudaMemcpyHostToDevice, stream), "table");
     check_cuda(cudaMemcpyAsync(d_scenes.ptr, h_scenes, sizeof(DevScene) * n, cudaMemcpyHostToDevice, stream), "scenes");
@@ -470,9 +474,10 @@ int32_t tt_server_destroy(tt_server* server) {
         if (server->worker.joinable()) server->worker.join();
         cudaSetDevice(server->device);
         cudaStreamSynchronize(server->stream);
-        for (auto& row : server->graph)
-            for (cudaGraphExec_t g : row)
-                if (g) cudaGraphExecDestroy(g);
+        for (auto& by_tex : server->graph)
+            for (auto& by_structures : by_tex)
+                for (cudaGraphExec_t g : by_structures)
+                    if (g) cudaGraphExecDestroy(g);
         cudaStreamDestroy(server->stream);
         cudaStreamDestroy(server->capture);
         cudaStreamDestroy(server->body);

@@ -111,11 +111,14 @@ struct BatchParams {
 };
 // Instantiates the graph of one shared-pool round: while (paths are live) { regen, extend,
 // shade, shadow }, then the per-request reductions.  `w` holds the pool (no radiance cache);
-// `tex`: some scene of the batch samples textures (w.ndc_mip allocated); `wide`: some scene of
-// the batch has the compressed wide structure (its traversal step is compiled in only then).
-// Launch it after the request table, the scene table and the round header are in place.
-cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, bool wide, uint32_t* batch_err,
-                                  cudaStream_t cs, cudaStream_t body_stream);
+// `tex`: some scene of the batch samples textures (w.ndc_mip allocated); `structures`: the
+// acceleration structures of the batch's scenes (BATCH_*: only their traversal steps are
+// compiled into the trace kernel); `short_stack`: every scene needs at most
+// SHORT_TRAVERSAL_STACK entries (not used with wide structures).  Launch it after the request
+// table, the scene table and the round header are in place.
+constexpr int BATCH_FLAT = 0, BATCH_NO_WIDE = 1, BATCH_ANY = 2;
+cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, int structures,
+                                  bool short_stack, uint32_t* batch_err, cudaStream_t cs, cudaStream_t body_stream);
 // Optional per-launch timing: a pair of CUDA events recorded on the launching stream around
 // each integrator launch, tagged with its TT_STAGE_*.  `events` holds 2 * MAX_LAUNCHES events
 // owned by the context; launches past MAX_LAUNCHES are not recorded (overflow).

@@ -703,7 +703,7 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
     check_cuda(e, "cudaGraphLaunch");
 }
 
-template <int ACCEL>
+template <int ACCEL, int STACK>
 static cudaGraphExec_t batch_graph(const WfParams& w, const BatchParams& b, bool tex, uint32_t* batch_err,
                                    cudaStream_t cs, cudaStream_t body_stream) {
     RenderParams p{};  // the shared-pool kernels read only its batch error word
@@ -713,8 +713,8 @@ static cudaGraphExec_t batch_graph(const WfParams& w, const BatchParams& b, bool
     int sms = 0, dev = 0, ext_per_sm = 0, shadow_per_sm = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
-    auto ext = wf_trace_kernel<false, false, ACCEL, TRAVERSAL_STACK, true>;
-    auto shadow = wf_trace_kernel<false, true, ACCEL, TRAVERSAL_STACK, true>;
+    auto ext = wf_trace_kernel<false, false, ACCEL, STACK, true>;
+    auto shadow = wf_trace_kernel<false, true, ACCEL, STACK, true>;
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, ext, TR_BLOCK, 0), "occupancy");
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shadow_per_sm, shadow, TR_BLOCK, 0), "occupancy");
     unsigned ext_grid = (unsigned)std::max(1, sms * ext_per_sm), shadow_grid = (unsigned)std::max(1, sms * shadow_per_sm);
@@ -759,10 +759,15 @@ static cudaGraphExec_t batch_graph(const WfParams& w, const BatchParams& b, bool
     return exec;
 }
 
-cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, bool wide, uint32_t* batch_err,
-                                  cudaStream_t cs, cudaStream_t body_stream) {
-    return wide ? batch_graph<ACCEL_ANY>(w, b, tex, batch_err, cs, body_stream)
-                : batch_graph<ACCEL_NO_WIDE>(w, b, tex, batch_err, cs, body_stream);
+cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool tex, int structures,
+                                  bool short_stack, uint32_t* batch_err, cudaStream_t cs, cudaStream_t body_stream) {
+    if (structures == BATCH_FLAT)
+        return short_stack ? batch_graph<ACCEL_FLAT_ONLY, SHORT_TRAVERSAL_STACK>(w, b, tex, batch_err, cs, body_stream)
+                           : batch_graph<ACCEL_FLAT_ONLY, TRAVERSAL_STACK>(w, b, tex, batch_err, cs, body_stream);
+    if (structures == BATCH_NO_WIDE)
+        return short_stack ? batch_graph<ACCEL_NO_WIDE, SHORT_TRAVERSAL_STACK>(w, b, tex, batch_err, cs, body_stream)
+                           : batch_graph<ACCEL_NO_WIDE, TRAVERSAL_STACK>(w, b, tex, batch_err, cs, body_stream);
+    return batch_graph<ACCEL_ANY, TRAVERSAL_STACK>(w, b, tex, batch_err, cs, body_stream);
 }
 
 void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
