@@ -9,7 +9,7 @@
 //      per-segment centroid bounds (float atomics);
 //   2. 30-bit Morton codes of the centroids, normalised per segment, prefixed by the segment
 //      (mesh) index: key = segment << 30 | morton;
-//   3. stable LSD radix sort of (key, primitive) in 8-bit digits;
+//   3. stable onesweep LSD radix sort of (key, primitive) in 8-bit digits;
 //   4. Karras (2012) binary radix tree over the sorted keys (index tie-break for duplicates);
 //      each segment's primitives form exactly one subtree;
 //   5. bottom-up box refit with one atomic visit counter per node;
@@ -115,62 +115,178 @@ void exclusive_scan(uint32_t* data, uint64_t n, Scratch& sc) {
 }
 
 // ---------------------------------------------------------------- radix sort (u64 key, u32 value)
-__global__ void radix_hist_kernel(const uint64_t* keys, uint32_t n, int shift, uint32_t* hist,
-                                  uint32_t nblocks) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0u;
+// Onesweep LSD radix sort (after Adinets & Merrill 2022), 8-bit digits: one up-front pass counts
+// the keys of every digit position, a small kernel turns the counts into each digit's global
+// offsets, and then one kernel per digit position ranks and scatters the keys.  That kernel
+// takes tiles of SORT_ITEMS x SORT_THREADS keys in the order its blocks claim them (an atomic
+// tile counter, so every predecessor of a tile belongs to a block that is already running),
+// ranks its keys stably per digit (warp match over SORT_ITEMS rounds of SORT_THREADS
+// consecutive keys), publishes its per-digit counts, and finds each digit's exclusive prefix
+// over the preceding tiles by decoupled look-back: it adds predecessors' published counts until
+// it meets a published inclusive prefix, then publishes its own inclusive prefix.  A status word
+// holds a 2-bit flag over a 30-bit value; the look-back wait is bounded (SORT_WAIT_LIMIT polls,
+// then ERR_SORT_WAIT and the pass goes on with a wrong prefix, reported after the sort).
+constexpr int SORT_ITEMS = 8;
+constexpr uint32_t SORT_TILE = SORT_THREADS * SORT_ITEMS;
+constexpr int SORT_MAX_PASSES = 8;
+constexpr uint32_t SORT_FLAG_AGGREGATE = 1u << 30, SORT_FLAG_INCLUSIVE = 2u << 30;
+constexpr uint32_t SORT_VALUE_MASK = (1u << 30) - 1u, SORT_FLAG_MASK = 3u << 30;
+constexpr uint32_t SORT_WAIT_LIMIT = 1u << 24;
+constexpr uint32_t ERR_SORT_WAIT = 1u;
+
+// counts[p][d]: keys whose digit p (bits 8p..8p+7) is d, for passes p < passes.
+__global__ void __launch_bounds__(SORT_THREADS) sort_count_kernel(const uint64_t* keys, uint32_t n, int passes,
+                                                                  uint32_t* counts) {
+    __shared__ uint32_t h[SORT_MAX_PASSES][256];
+    for (int p = 0; p < passes; ++p) h[p][threadIdx.x] = 0u;
     __syncthreads();
-    uint32_t i = blockIdx.x * SORT_THREADS + threadIdx.x;
-    if (i < n) atomicAdd(&h[(uint32_t)(keys[i] >> shift) & 0xffu], 1u);
+    for (uint32_t i = blockIdx.x * SORT_THREADS + threadIdx.x; i < n; i += gridDim.x * SORT_THREADS) {
+        uint64_t k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(uint32_t)(k >> (8 * p)) & 0xffu], 1u);
+    }
     __syncthreads();
-    hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+    for (int p = 0; p < passes; ++p)
+        if (h[p][threadIdx.x]) atomicAdd(&counts[p * 256 + threadIdx.x], h[p][threadIdx.x]);
 }
-__global__ void radix_scatter_kernel(const uint64_t* kin, const uint32_t* vin, uint64_t* kout,
-                                     uint32_t* vout, const uint32_t* offsets, uint32_t n,
-                                     int shift, uint32_t nblocks) {
-    __shared__ uint32_t wh[SORT_WARPS][256];
-    for (int w = 0; w < SORT_WARPS; ++w) wh[w][threadIdx.x] = 0u;
-    __syncthreads();
-    uint32_t i = blockIdx.x * SORT_THREADS + threadIdx.x;
-    bool valid = i < n;
-    uint64_t key = valid ? kin[i] : 0ull;
-    uint32_t digit = valid ? ((uint32_t)(key >> shift) & 0xffu) : 256u;
+
+// offsets[p][d] = sum of counts[p][d'] for d' < d (one block of 256 threads per pass).
+__global__ void __launch_bounds__(256) sort_offsets_kernel(const uint32_t* counts, uint32_t* offsets) {
+    __shared__ uint32_t w[8];
+    uint32_t c = counts[blockIdx.x * 256 + threadIdx.x];
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t peers = __match_any_sync(0xffffffffu, digit);
-    uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-    int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) wh[warp][digit] = __popc(peers);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) w[warp] = incl;
     __syncthreads();
-    {
-        uint32_t run = 0;
+    uint32_t before = 0u;
+    for (int k = 0; k < warp; ++k) before += w[k];
+    offsets[blockIdx.x * 256 + threadIdx.x] = before + incl - c;
+}
+
+// One digit pass: kin/vin -> kout/vout by digit `pass`.  status holds (tiles x 256) words and
+// *tile_counter 0 at launch.
+__global__ void __launch_bounds__(SORT_THREADS) sort_pass_kernel(const uint64_t* kin, const uint32_t* vin,
+                                                                 uint64_t* kout, uint32_t* vout, uint32_t n,
+                                                                 int pass, const uint32_t* offsets,
+                                                                 uint32_t* status, uint32_t* tile_counter,
+                                                                 uint32_t* err) {
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_warp[SORT_WARPS][256];
+    __shared__ uint32_t s_run[256];
+    const uint32_t t = threadIdx.x;
+    const int lane = t & 31, warp = t >> 5;
+    if (t == 0) s_tile = atomicAdd(tile_counter, 1u);
+    s_run[t] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = (uint64_t)tile * SORT_TILE;
+    const int shift = 8 * pass;
+    uint64_t key[SORT_ITEMS];
+    uint32_t val[SORT_ITEMS], digit[SORT_ITEMS], off[SORT_ITEMS];
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; ++k) {
+        uint64_t i = base + (uint64_t)k * SORT_THREADS + t;
+        bool valid = i < n;
+        key[k] = valid ? kin[i] : 0ull;
+        val[k] = valid ? vin[i] : 0u;
+        digit[k] = valid ? ((uint32_t)(key[k] >> shift) & 0xffu) : 256u;
+    }
+    // stable ranks inside the tile: round k covers keys k * SORT_THREADS .. + SORT_THREADS - 1
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; ++k) {
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; ++w) s_warp[w][t] = 0u;
+        __syncthreads();
+        uint32_t peers = __match_any_sync(0xffffffffu, digit[k]);
+        uint32_t rank = (uint32_t)__popc(peers & ((1u << lane) - 1u));
+        if (digit[k] < 256u && lane == __ffs(peers) - 1) s_warp[warp][digit[k]] = (uint32_t)__popc(peers);
+        __syncthreads();
+        uint32_t run = s_run[t];
+#pragma unroll
         for (int w = 0; w < SORT_WARPS; ++w) {
-            uint32_t c = wh[w][threadIdx.x];
-            wh[w][threadIdx.x] = run;
+            uint32_t c = s_warp[w][t];
+            s_warp[w][t] = run;
             run += c;
         }
+        s_run[t] = run;
+        __syncthreads();
+        off[k] = digit[k] < 256u ? s_warp[warp][digit[k]] + rank : 0u;
+        __syncthreads();
     }
+    // decoupled look-back, one digit per thread
+    const uint32_t count = s_run[t];
+    uint32_t* mine = status + (uint64_t)tile * 256 + t;
+    uint32_t excl = 0u;
+    if (tile == 0) {
+        atomicExch(mine, SORT_FLAG_INCLUSIVE | count);
+    } else {
+        atomicExch(mine, SORT_FLAG_AGGREGATE | count);
+        uint32_t j = tile - 1u, polls = 0u;
+        while (true) {
+            uint32_t v = __ldcv(status + (uint64_t)j * 256 + t);
+            uint32_t flag = v & SORT_FLAG_MASK;
+            if (flag == 0u) {
+                if (++polls > SORT_WAIT_LIMIT) {
+                    atomicOr(err, ERR_SORT_WAIT);
+                    break;
+                }
+                continue;
+            }
+            excl += v & SORT_VALUE_MASK;
+            if (flag == SORT_FLAG_INCLUSIVE || j == 0u) break;
+            --j;
+        }
+        atomicExch(mine, SORT_FLAG_INCLUSIVE | ((excl + count) & SORT_VALUE_MASK));
+    }
+    __syncthreads();  // every s_run read above is done
+    s_run[t] = offsets[pass * 256 + t] + excl;
     __syncthreads();
-    if (valid) {
-        uint32_t pos = offsets[(uint64_t)digit * nblocks + blockIdx.x] + wh[warp][digit] + rank;
-        kout[pos] = key;
-        vout[pos] = vin[i];
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; ++k) {
+        uint32_t pos = digit[k] < 256u ? s_run[digit[k]] + off[k] : n;
+        if (pos < n) {  // always, unless a look-back wait ran out (reported by ERR_SORT_WAIT)
+            kout[pos] = key[k];
+            vout[pos] = val[k];
+        }
     }
 }
-// Stable sort of (keys, vals) by the low `bits` bits of the keys. Result in keys/vals.
+
+// Stable sort of (keys, vals) by the low `bits` bits of the keys (bits <= 64). Result in
+// keys/vals.  Synchronises the stream once, to report a look-back wait that ran out.
 void radix_sort(uint64_t*& keys, uint32_t*& vals, uint32_t n, int bits, Scratch& sc) {
     if (n <= 1) return;
-    uint32_t nblocks = grid_for(n, SORT_THREADS);
+    if (n > SORT_VALUE_MASK) fail(TT_ERR_OVERFLOW, "more than 2^30 keys for the radix sort");
+    const int passes = (bits + 7) / 8;
+    const uint32_t tiles = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
     uint64_t* k2 = sc.get<uint64_t>(n);
     uint32_t* v2 = sc.get<uint32_t>(n);
-    uint32_t* hist = sc.get<uint32_t>((uint64_t)256 * nblocks);
-    for (int shift = 0; shift < bits; shift += 8) {
-        radix_hist_kernel<<<nblocks, SORT_THREADS, 0, sc.stream>>>(keys, n, shift, hist, nblocks);
-        exclusive_scan(hist, (uint64_t)256 * nblocks, sc);
-        radix_scatter_kernel<<<nblocks, SORT_THREADS, 0, sc.stream>>>(keys, vals, k2, v2, hist, n,
-                                                                     shift, nblocks);
+    // counts, offsets, per-pass tile counters and the error word in one zeroed block; the
+    // status words of a pass (tiles x 256) are cleared before it
+    const uint64_t words = 2ull * SORT_MAX_PASSES * 256 + SORT_MAX_PASSES + 1;
+    uint32_t* w = sc.get<uint32_t>(words);
+    check_cuda(cudaMemsetAsync(w, 0, 4ull * words, sc.stream), "memset");
+    uint32_t* counts = w;
+    uint32_t* offsets = counts + SORT_MAX_PASSES * 256;
+    uint32_t* tile_counter = offsets + SORT_MAX_PASSES * 256;
+    uint32_t* err = tile_counter + SORT_MAX_PASSES;
+    uint32_t* status = sc.get<uint32_t>((uint64_t)tiles * 256);
+    sort_count_kernel<<<std::min<unsigned>(tiles, 1024u), SORT_THREADS, 0, sc.stream>>>(keys, n, passes, counts);
+    sort_offsets_kernel<<<passes, 256, 0, sc.stream>>>(counts, offsets);
+    for (int p = 0; p < passes; ++p) {
+        check_cuda(cudaMemsetAsync(status, 0, 4ull * tiles * 256, sc.stream), "memset");
+        sort_pass_kernel<<<tiles, SORT_THREADS, 0, sc.stream>>>(keys, vals, k2, v2, n, p, offsets, status,
+                                                                 tile_counter + p, err);
         std::swap(keys, k2);
         std::swap(vals, v2);
     }
+    uint32_t host_err = 0;
+    check_cuda(cudaMemcpyAsync(&host_err, err, 4, cudaMemcpyDeviceToHost, sc.stream), "sort error word");
+    check_cuda(cudaStreamSynchronize(sc.stream), "cudaStreamSynchronize");
+    if (host_err) fail(TT_ERR_TIMEOUT, "radix sort: a look-back wait ran out");
 }
 
 // ---------------------------------------------------------------- float atomics
