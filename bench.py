@@ -66,6 +66,7 @@ def parse_args():
     p.add_argument("--no-light-selection", action="store_true", help="skip the light-selection sample")
     p.add_argument("--no-closed", action="store_true", help="skip the closed-scene (Cornell box) sample")
     p.add_argument("--serve-batch", type=int, default=96, help="requests of the serving sample's capacity run")
+    p.add_argument("--serve-inflight", type=int, default=SERVE_INFLIGHT, help="requests the server renders together")
     p.add_argument("--serve-requests", type=int, default=512,
                    help="requests at 0.8 x capacity in the serving sample (a quarter as many at 0.5 x and 1.1 x)")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level", "wide"],
@@ -873,13 +874,14 @@ def serve_requests(rng, pool, logs, n: int, first_frame: int):
 SERVE_INFLIGHT = 16  # requests rendered together per round
 
 
-def serve_run(ctx, reqs, rate: float | None, rng, pool_paths: int) -> dict:
+def serve_run(ctx, reqs, rate: float | None, rng, pool_paths: int, capacity_msamples_s: float | None = None,
+              inflight: int = 16) -> dict:
     """Submits `reqs` (Poisson arrivals at `rate` per second, or all at once when rate is None),
     waits for all of them and returns latency percentiles and throughput.  Finished requests'
     image buffers are released as the run goes."""
     from tinytrace_gb300.server import RenderServer
 
-    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=SERVE_INFLIGHT, pool_paths=pool_paths) as srv:
+    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=inflight, pool_paths=pool_paths) as srv:
         t0 = time.perf_counter()
         due = t0
         ids, pending = [], []
@@ -906,6 +908,18 @@ def serve_run(ctx, reqs, rate: float | None, rng, pool_paths: int) -> dict:
         st = srv.stats()
     samples = sum(n for _, _, n in reqs)
     tenth = max(1, len(lat) // 10)
+    # latency against request size: percentiles of the smaller and the larger half (by samples),
+    # and of the slowdown, latency over the request's service time at the saturated throughput
+    size = np.array([n for _, _, n in reqs], np.float64)
+    small = size <= np.median(size)
+    by_size = {"smaller_half_p50_ms": float(np.percentile(lat[small], 50)),
+               "smaller_half_p99_ms": float(np.percentile(lat[small], 99)),
+               "larger_half_p50_ms": float(np.percentile(lat[~small], 50)),
+               "larger_half_p99_ms": float(np.percentile(lat[~small], 99))}
+    if capacity_msamples_s:
+        slow = lat / (size / (capacity_msamples_s * 1e3))
+        by_size["slowdown_p50"] = float(np.percentile(slow, 50))
+        by_size["slowdown_p99"] = float(np.percentile(slow, 99))
     return {"requests": len(reqs), "arrival_rate_per_s": rate, "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()), "max_ms": float(lat.max()),
             "first_tenth_mean_ms": float(lat[:tenth].mean()), "last_tenth_mean_ms": float(lat[-tenth:].mean()),
@@ -916,7 +930,8 @@ def serve_run(ctx, reqs, rate: float | None, rng, pool_paths: int) -> dict:
             "gpu_busy_frac": st.gpu_busy_ns / 1e9 / makespan,
             "msamples_s_while_busy": samples / max(1e-9, st.gpu_busy_ns / 1e9) / 1e6,
             "scheduler_s": {"admit": st.admit_ns / 1e9, "launch": st.launch_ns / 1e9,
-                            "copy_out": st.copy_out_ns / 1e9, "wait": st.wait_ns / 1e9}}
+                            "copy_out": st.copy_out_ns / 1e9, "wait": st.wait_ns / 1e9},
+            "latency_by_size": by_size}
 
 
 def serve_one_request(ctx, scene, cam, pool_paths: int) -> dict:
@@ -942,7 +957,7 @@ def serve_one_request(ctx, scene, cam, pool_paths: int) -> dict:
     check(lib.tt_event_record(h, 7))
     ms = ctypes.c_float()
     check(lib.tt_event_elapsed_ms(h, 6, 7, ctypes.byref(ms)))
-    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=SERVE_INFLIGHT, pool_paths=pool_paths) as srv:
+    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=1, pool_paths=pool_paths) as srv:
         srv.wait(srv.submit(scene, c))
         busy0, rounds0 = srv.stats().gpu_busy_ns, srv.stats().rounds
         t0 = time.perf_counter()
@@ -985,14 +1000,15 @@ def run_serving(a, ctx) -> dict:
     c = make_constants(cam, (1024, 1024), Config(bounce_count=8, sample_count=4), 0, 0)
     check(ctx.lib.tt_autotune(ctx.handle, pool[2][1], native.ptr(c), img, ctypes.byref(tune)))
     pool_paths = int(tune.slots)
-    out = {"scenes_triangles": [int(t) for t, _ in pool], "hbm_budget_gb": 150, "max_inflight": SERVE_INFLIGHT,
+    out = {"scenes_triangles": [int(t) for t, _ in pool], "hbm_budget_gb": 150, "max_inflight": a.serve_inflight,
            "pool_paths": pool_paths, "pool_tuning": {"tune_spp": 4, "default_ms": tune.default_ms,
                                                      "tuned_ms": tune.best_ms, "renders": int(tune.renders)},
            "round_items": 1 << 26,
            "mix": "side ~U{256..2048} step 16, spp ~U{1..256}, depth 8, scene log-uniform 1e3..5e6 triangles"}
-    serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng, pool_paths)  # warm-up: graphs, pool, caches
+    serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng, pool_paths, None, a.serve_inflight)  # warm-up
     out["one_request"] = serve_one_request(ctx, pool[3][1], cam, pool_paths)
-    cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng, pool_paths)
+    cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng, pool_paths, None,
+                    a.serve_inflight)
     # capacity in requests per second: the sample throughput of the saturated server over the mix's
     # mean request size (E[side^2] E[spp], side = 16 k with k ~ U{16..128}, spp ~ U{1..256}), not
     # the completion rate of one finite batch, whose few large requests decide its makespan
@@ -1005,7 +1021,8 @@ def run_serving(a, ctx) -> dict:
     out["rates"] = []
     frame = 10_000
     for frac, n in ((0.5, max(32, a.serve_requests // 4)), (0.8, a.serve_requests), (1.1, max(32, a.serve_requests // 4))):
-        res = serve_run(ctx, serve_requests(rng, pool, logs, n, frame), frac * mu, rng, pool_paths)
+        res = serve_run(ctx, serve_requests(rng, pool, logs, n, frame), frac * mu, rng, pool_paths,
+                        cap["throughput_msamples_s"], a.serve_inflight)
         frame += n
         res["fraction_of_capacity"] = frac
         res["sustained"] = bool(res["completed_per_s"] >= 0.95 * res["offered_per_s"]
@@ -1017,6 +1034,7 @@ def run_serving(a, ctx) -> dict:
     out["p50_ms_at_sustainable_rate"] = best["p50_ms"] if best else None
     out["p99_ms_at_sustainable_rate"] = best["p99_ms"] if best else None
     out["requests_at_sustainable_rate"] = best["requests"] if best else None
+    out["latency_by_size_at_sustainable_rate"] = best["latency_by_size"] if best else None
     return out
 
 
