@@ -97,7 +97,7 @@ struct WavefrontBuffers {
 // ReSTIR DI state kept between frames: two G-buffers and two final reservoir arrays
 // (current and previous frame), the initial and temporal reservoirs, the previous camera.
 struct RestirState {
-    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex, glob;
+    DeviceBuffer gbuf[2], final_res[2], initial, temporal, gtex, glob, queue, queue_count;
     uint64_t pixels = 0;
     uint32_t cur = 0;
     RestirHistory history{};
@@ -1311,6 +1311,8 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
             R.initial.alloc(32ull * WH);
             R.temporal.alloc(32ull * WH);
             R.glob.alloc(16ull * LOBE_RECORD * WH);
+            R.queue.alloc(4ull * HIT_BUCKETS * WH);
+            R.queue_count.alloc(4ull * HIT_BUCKETS);
             R.pixels = WH;
             R.history.valid = 0u;
         }
@@ -1331,6 +1333,8 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         rp.glob = R.glob.as<float4>();
         rp.prev_gbuf = R.gbuf[R.cur ^ 1u].as<Surface>();
         rp.initial = R.initial.as<Reservoir>();
+        rp.queue = R.queue.as<uint32_t>();
+        rp.queue_count = R.queue_count.as<uint32_t>();
         rp.temporal = R.temporal.as<Reservoir>();
         rp.final_out = R.final_res[R.cur].as<Reservoir>();
         rp.prev = R.final_res[R.cur ^ 1u].as<Reservoir>();

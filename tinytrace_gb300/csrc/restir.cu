@@ -20,6 +20,58 @@ __device__ __forceinline__ bool pixel_of_thread(const tt_constants& c, uint32_t&
     return x < c.screen_size[0] && y < c.screen_size[1];
 }
 
+// Appends each thread's pixel to its bucket's queue (bucket == HIT_BUCKETS: to none).  Warp
+// ballots count the block's pixels per bucket in shared memory, and one thread per bucket takes
+// the block's range of the queue with a single global atomic, so the four counters see one
+// atomic per block instead of one per warp.  Every thread of the block must call it.
+__device__ __forceinline__ void block_queue_append(const RestirParams& rp, uint32_t bucket, uint32_t pixel,
+                                                   uint64_t WH) {
+    __shared__ uint32_t s_count[HIT_BUCKETS], s_base[HIT_BUCKETS];
+    if (threadIdx.x < HIT_BUCKETS) s_count[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t lane = threadIdx.x & 31u, pos = 0u;
+#pragma unroll
+    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
+        uint32_t mask = __ballot_sync(0xffffffffu, bucket == b);
+        uint32_t wbase = 0u;
+        if (lane == 0u && mask != 0u) wbase = atomicAdd(&s_count[b], (uint32_t)__popc(mask));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        if (bucket == b) pos = wbase + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+    }
+    __syncthreads();
+    if (threadIdx.x < HIT_BUCKETS)
+        s_base[threadIdx.x] = s_count[threadIdx.x] ? atomicAdd(rp.queue_count + threadIdx.x, s_count[threadIdx.x]) : 0u;
+    __syncthreads();
+    if (bucket < HIT_BUCKETS) rp.queue[(uint64_t)bucket * WH + s_base[bucket] + pos] = pixel;
+}
+
+// Pixel of queue entry q: the bucket queues are concatenated in bucket order.
+__device__ __forceinline__ bool queued_pixel(const RestirParams& rp, uint32_t WH, uint32_t q, uint64_t& i) {
+    uint32_t start = 0u;
+#pragma unroll
+    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
+        uint32_t n = rp.queue_count[b];
+        if (q < start + n) {
+            i = rp.queue[(uint64_t)b * WH + (q - start)];
+            return true;
+        }
+        start += n;
+    }
+    return false;
+}
+
+// The accumulation rule of tt_render for one pixel of the target.
+__device__ __forceinline__ void write_target(const RenderParams& p, uint64_t i, f3 radiance) {
+    const tt_constants& c = p.c;
+    float4* tp = p.target + i;
+    if (c.accumulated_frame_count != 0) {
+        float4 prev = *tp;
+        radiance = (f3{prev.x, prev.y, prev.z} * (float)(c.accumulated_frame_count - 1u) + radiance) /
+                   (float)c.accumulated_frame_count;
+    }
+    *tp = make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
+}
+
 // Rebuilds the pixel's shading state from its G-buffer record.
 struct ShadingState {
     f3 pos, wi;
@@ -66,13 +118,13 @@ __device__ __forceinline__ float target_of(const DevScene& sc, const ShadingStat
     return luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
 }
 
+// The G-buffer pass for pixel (x, y); returns the material bucket of its primary hit, or
+// HIT_BUCKETS for a sky pixel (finished here).
 template <bool TEX, int ACCEL>
-__global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
-                                                                  Surface* gbuf, float4* gtex, float4* glob) {
-    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
-    uint32_t x, y;
+__device__ __forceinline__ uint32_t gbuffer_pixel(const RenderParams& p, const RestirParams& rp, Surface* gbuf,
+                                                  float4* gtex, float4* glob, uint32_t x, uint32_t y,
+                                                  uint32_t* s_stack) {
     const tt_constants& c = p.c;
-    if (!pixel_of_thread(c, x, y)) return;
     const DevScene& sc = p.sc;
     uint32_t W = c.screen_size[0], H = c.screen_size[1];
     uint32_t g = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
@@ -83,7 +135,13 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     Hit h = trace_closest<false, ACCEL>(sc, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true, s_stack + threadIdx.x, RT_BLOCK,
                                  p.err, cnt);
     Surface s;
+    uint64_t i = (uint64_t)y * W + x;
+    // surface pixels go to their material bucket's queue for the candidate and shade passes; sky
+    // pixels are finished here: empty initial reservoir, the white sky (integrate.glsl:272-276)
+    uint32_t bucket = h.hit ? (uint32_t)__ldg(sc.inst_bucket + h.instance) : HIT_BUCKETS;
     if (!h.hit) {
+        rp.initial[i] = empty_reservoir();
+        write_target(p, i, splat(1.0f));
         s.pos_dist = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         s.normal_mat = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(NO_SURFACE));
         s.tangent_inst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -108,18 +166,33 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
         store_lobes(glob + LOBE_RECORD * ((uint64_t)y * W + x), bsdf_prepare(mc, wi, gp));
     }
     gbuf[(uint64_t)y * W + x] = s;
+    return bucket;
+}
+
+template <bool TEX, int ACCEL>
+__global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
+                                                                  const __grid_constant__ RestirParams rp,
+                                                                  Surface* gbuf, float4* gtex, float4* glob) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    uint32_t x, y;
+    const tt_constants& c = p.c;
+    uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    // threads outside the image take part in the block's queue append only
+    uint32_t bucket = HIT_BUCKETS;
+    if (pixel_of_thread(c, x, y)) bucket = gbuffer_pixel<TEX, ACCEL>(p, rp, gbuf, gtex, glob, x, y, s_stack);
+    block_queue_append(rp, bucket, y * W + x, (uint64_t)W * H);
 }
 
 template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_constant__ RenderParams p,
+                                                                  const __grid_constant__ RestirParams rp,
                                                                   const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   Reservoir* out, uint32_t candidates) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
-    uint32_t x, y;
     const tt_constants& c = p.c;
-    if (!pixel_of_thread(c, x, y)) return;
+    uint64_t i = 0;
+    if (!queued_pixel(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i)) return;
     const DevScene& sc = p.sc;
-    uint64_t i = (uint64_t)y * c.screen_size[0] + x;
     ShadingState st;
     Reservoir r = empty_reservoir();
     if (load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st) && sc.emissive_count > 0) {
@@ -271,15 +344,14 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
 
 template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_constant__ RenderParams p,
+                                                                const __grid_constant__ RestirParams rp,
                                                                 const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                 const Reservoir* res) {
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
-    uint32_t x, y;
     const tt_constants& c = p.c;
-    if (!pixel_of_thread(c, x, y)) return;
+    uint64_t i = 0;
+    if (!queued_pixel(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i)) return;
     const DevScene& sc = p.sc;
-    uint32_t W = c.screen_size[0];
-    uint64_t i = (uint64_t)y * W + x;
     ShadingState st;
     f3 radiance;
     if (!load_surface<TEX>(sc, gbuf[i], gtex, glob, i, st)) {
@@ -294,24 +366,22 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_con
                 radiance += contrib * r.W;
         }
     }
-    float4* tp = p.target + i;
-    if (c.accumulated_frame_count != 0) {
-        float4 prev = *tp;
-        radiance = (f3{prev.x, prev.y, prev.z} * (float)(c.accumulated_frame_count - 1u) + radiance) /
-                   (float)c.accumulated_frame_count;
-    }
-    *tp = make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
+    write_target(p, i, radiance);
 }
 
 template <bool TEX, int ACCEL>
 static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer) {
     const tt_constants& c = p.c;
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
+    uint64_t WH = (uint64_t)c.screen_size[0] * c.screen_size[1];
+    unsigned qgrid = (unsigned)((WH + RT_BLOCK - 1) / RT_BLOCK);  // enough blocks for every pixel queued
+    check_cuda(cudaMemsetAsync(rp.queue_count, 0, 4ull * HIT_BUCKETS, st), "memset");
     stage_begin(timer, TT_STAGE_RESTIR_GBUFFER, st);
-    restir_gbuffer_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob);
+    restir_gbuffer_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_INITIAL, st);
-    restir_initial_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.initial, rp.candidates);
+    restir_initial_kernel<TEX, ACCEL><<<qgrid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.initial,
+                                                                 rp.candidates);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_TEMPORAL, st);
     restir_temporal_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.history, rp.gbuf, rp.gtex, rp.glob, rp.prev_gbuf,
@@ -322,7 +392,7 @@ static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStr
                                                           rp.neighbours, rp.radius);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_SHADE, st);
-    restir_shade_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
+    restir_shade_kernel<TEX, ACCEL><<<qgrid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.final_out);
     stage_end(timer, st);
 }
 

@@ -172,6 +172,12 @@ struct RestirParams {
     float4* gtex;  // textured scenes: per pixel (u, v, mip level, 0) of the primary hit; else null
     float4* glob;  // per pixel: the primary hit's prepared lobes (LOBE_RECORD float4)
     Reservoir *initial, *temporal, *final_out, *prev;
+    // pixels whose camera ray hit a surface, one queue of pixel indices per material bucket
+    // (HIT_BUCKETS x width * height) with its length in queue_count[bucket]; the candidate and
+    // shade passes run over the queues laid end to end, so that a warp's pixels share a lobe set
+    // (sky pixels are finished by the G-buffer pass)
+    uint32_t* queue;
+    uint32_t* queue_count;
     RestirHistory history;
     uint32_t candidates, neighbours;
     float m_cap, radius;
