@@ -1,5 +1,7 @@
 """The learned radiance cache's CUDA kernels against the NumPy reference (GPU required).
 
+The kernels read the hash-grid features as FP16 copies of the FP32 parameters (rounded to
+nearest), so the FP16 emulations below encode with the parameters rounded the same way.
 Tolerances: queries and training run FP16-in / FP32-accumulate on the tensor cores, so queries
 are compared with the reference's FP16 emulation within 2e-3 of the output scale, the reported
 loss with the loss of that FP16 forward pass within 1e-3 relative, and the first Adam step
@@ -23,6 +25,11 @@ pytestmark = pytest.mark.gpu
 def _configure(ctx, seed=3, lr=1e-2):
     cfg = native.CacheConfig(lr, 65536, 2, seed)
     check(ctx.lib.tt_cache_configure(ctx.handle, ctypes.byref(cfg)))
+
+
+def _f16(grid):
+    """The FP16 grid features the kernels read, as float64."""
+    return grid.astype(np.float16).astype(np.float64)
 
 
 def _params(ctx):
@@ -75,7 +82,7 @@ def test_first_step_follows_the_reference_gradients(gpu_context):
     grid1, w1 = _params(ctx)
     ref_loss, g_w, g_grid = cr.loss_and_grads(q.astype(np.float64), t.astype(np.float64), grid0.astype(np.float64),
                                               w0.astype(np.float64))
-    y16, _ = cr.forward(cr.encode(q.astype(np.float64), grid0.astype(np.float64)), w0, fp16=True)
+    y16, _ = cr.forward(cr.encode(q.astype(np.float64), _f16(grid0)), w0, fp16=True)
     loss16 = float((((y16 - t) ** 2) / (y16 * y16 + 0.01)).sum())
     assert abs(loss - loss16) <= 1e-3 * loss16, (loss, loss16, ref_loss)
     for before, after, g, name in ((w0, w1, g_w, "weights"), (grid0.ravel(), grid1.ravel(), g_grid.ravel(), "grid")):
@@ -120,7 +127,7 @@ def test_gradient_values_match_the_reference(gpu_context, train_steps):
     grid1, w1 = _params(ctx)
     assert np.array_equal(w0, w1) and np.array_equal(grid0, grid1)
     q64, t64, grid64, w64 = q.astype(np.float64), t.astype(np.float64), grid0.astype(np.float64), w0.astype(np.float64)
-    loss16, gw16, gg16 = cr.grads_fp16(q64, t64, grid64, w64)
+    loss16, gw16, gg16 = cr.grads_fp16(q64, t64, _f16(grid0), w64)
     _, gw64, gg64 = cr.loss_and_grads(q64, t64, grid64, w64)
     assert abs(loss - loss16) <= 1e-3 * loss16, (loss, loss16)
     errs = {"weights_fp16": _rel_l2(gw, gw16), "grid_fp16": _rel_l2(gg, gg16),
@@ -145,9 +152,9 @@ def test_queries_match_the_reference(gpu_context):
     grid, w = _params(ctx)
     q = _queries(rng, 3000)
     got = _query(ctx, q)
-    x = cr.encode(q.astype(np.float64), grid.astype(np.float64))
+    x = cr.encode(q.astype(np.float64), _f16(grid))
     want16, _ = cr.forward(x, w, fp16=True)
-    want32, _ = cr.forward(x, w, fp16=False)
+    want32, _ = cr.forward(cr.encode(q.astype(np.float64), grid.astype(np.float64)), w, fp16=False)
     scale = np.abs(want32).max()
     assert scale > 0.1
     assert np.abs(got - want16).max() <= 2e-3 * scale + 1e-4, np.abs(got - want16).max() / scale
@@ -282,7 +289,7 @@ def test_large_query_batch(gpu_context):
     got = _query(ctx, q)
     assert np.isfinite(got).all()
     pick = rng.choice(len(q), 2000, replace=False)
-    x = cr.encode(q[pick].astype(np.float64), grid.astype(np.float64))
+    x = cr.encode(q[pick].astype(np.float64), _f16(grid))
     want16, _ = cr.forward(x, w, fp16=True)
     scale = np.abs(want16).max()
     assert np.abs(got[pick] - want16).max() <= 2e-3 * scale + 1e-4

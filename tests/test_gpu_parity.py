@@ -76,6 +76,25 @@ def _small_field():
     return scenes.icosphere_field(instances=6, freq=8, lights=40, seed=11)
 
 
+def _duplicate_keys():
+    """Equal Morton codes in bulk: 2,100 copies of one small triangle and 400 random ones in one
+    mesh, placed three times with the same transform, so the flat build sorts 7,500 keys (four
+    2,048-key tiles of the onesweep sort) of which 6,300 are equal and must keep primitive
+    order."""
+    from tinytrace_gb300.asset import Model, Node, Scene
+    rng = np.random.default_rng(7)
+    tri = np.array([[0.1, 0.2, 0.3], [0.12, 0.2, 0.3], [0.1, 0.23, 0.31]], np.float32)
+    rand = rng.uniform(-1.0, 1.0, (400, 3, 3)).astype(np.float32)
+    pos = np.concatenate([np.tile(tri, (2100, 1)), rand.reshape(-1, 3)])
+    idx = np.arange(len(pos), dtype=np.uint32)
+    s = Scene()
+    m = s.insert_mesh(pos, None, idx)
+    mat = s.insert_material(scenes.lambertian((0.5, 0.5, 0.5)))
+    for _ in range(3):
+        s.root.children.append(Node(models=[Model(m, mat)]))
+    return s
+
+
 ACCELS = {"flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL, "wide": native.TT_ACCEL_FLAT_WIDE}
 
 
@@ -88,9 +107,10 @@ def _create_scene(ctx, arrays, accel):
 
 
 @pytest.mark.parametrize("accel", ["two_level", "flat", "wide"])
-@pytest.mark.parametrize("name", ["cornell", "field", "instanced"])
+@pytest.mark.parametrize("name", ["cornell", "field", "instanced", "duplicates"])
 def test_bvh_topology_bits(gpu_context, name, accel):
-    scene = {"cornell": scenes.cornell_box, "field": _small_field, "instanced": scenes.instanced_spheres}[name]()
+    scene = {"cornell": scenes.cornell_box, "field": _small_field, "instanced": scenes.instanced_spheres,
+             "duplicates": _duplicate_keys}[name]()
     arrays = SceneArrays(scene)
     h = _create_scene(gpu_context, arrays, accel)
     blas, tris, tlas, st = _gpu_bvh(gpu_context, h)

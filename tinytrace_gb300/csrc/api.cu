@@ -107,7 +107,7 @@ struct RestirState {
 // Learned radiance cache: device parameters, the configuration and the integrator's buffers
 // (queued queries, training records and pairs).
 struct CacheState {
-    DeviceBuffer grid, grid_m, grid_v, grid_grad, w, w_m, w_v, w_grad, w16, loss;
+    DeviceBuffer grid, grid_m, grid_v, grid_grad, w, w_m, w_v, w_grad, w16, loss, grid16;
     DeviceBuffer cq, cq_slot, cq_out, rec, train_final, tq, tt, tcount, spread;
     uint64_t cq_cap = 0, rec_cap = 0, final_cap = 0;
     bool enabled = false;
@@ -119,7 +119,7 @@ struct CacheState {
     CacheDevice dev() const {
         return CacheDevice{grid.as<float>(), grid_m.as<float>(), grid_v.as<float>(), grid_grad.as<float>(),
                            w.as<float>(), w_m.as<float>(), w_v.as<float>(), w_grad.as<float>(), w16.as<__half>(),
-                           loss.as<float>()};
+                           loss.as<float>(), grid16.as<__half>()};
     }
 };
 
@@ -584,6 +584,7 @@ static void cache_ready(tt_context* ctx) {
     CacheState& C = ctx->cache;
     if (C.ready) return;
     C.grid.alloc(4 * CACHE_GRID_PARAMS);
+    C.grid16.alloc(2 * CACHE_GRID_PARAMS);
     C.grid_m.alloc(4 * CACHE_GRID_PARAMS);
     C.grid_v.alloc(4 * CACHE_GRID_PARAMS);
     C.grid_grad.alloc(4 * CACHE_GRID_PARAMS);
@@ -640,7 +641,7 @@ static void cache_frame_buffers(tt_context* ctx, const tt_constants& c, const De
     w.cq_out = C.cq_out.as<float>();
     w.rec = C.rec.as<TrainRecord>();
     w.train_final = C.train_final.as<float4>();
-    w.cache_grid = C.grid.as<float>();
+    w.cache_grid = C.grid16.as<__half>();
     w.cache_w16 = C.w16.as<__half>();
 }
 

@@ -148,7 +148,7 @@ __device__ __forceinline__ uint32_t pack_half2(float a, float b) {
 // The 64 FP16 inputs of one query written straight into row `row` of the A operand, 16 bytes
 // (8 inputs) at a time: the grid features of levels 4c..4c+3 (float2 gathers of the 8 corners),
 // then direction, normal, roughness and zero padding.  Same values as encode().
-__device__ __forceinline__ void encode_row(const CacheQuery& q, const float* grid, uint8_t* a, uint32_t row) {
+__device__ __forceinline__ void encode_row(const CacheQuery& q, const __half* grid16, uint8_t* a, uint32_t row) {
     float3 p = make_float3(fminf(fmaxf(q.pos[0], 0.0f), 1.0f), fminf(fmaxf(q.pos[1], 0.0f), 1.0f),
                            fminf(fmaxf(q.pos[2], 0.0f), 1.0f));
 #pragma unroll 1
@@ -160,11 +160,12 @@ __device__ __forceinline__ void encode_row(const CacheQuery& q, const float* gri
             uint32_t idx[8];
             float w[8];
             grid_corners(p, l, idx, w);
-            const float2* g = reinterpret_cast<const float2*>(grid + 2ull * CACHE_TABLE * l);
+            const uint32_t* g = reinterpret_cast<const uint32_t*>(grid16 + 2ull * CACHE_TABLE * l);
             float f0 = 0.0f, f1 = 0.0f;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                float2 v = __ldg(g + idx[k]);
+                uint32_t bits = __ldg(g + idx[k]);
+                float2 v = __half22float2(*reinterpret_cast<const __half2*>(&bits));
                 f0 += w[k] * v.x;
                 f1 += w[k] * v.y;
             }
@@ -198,7 +199,7 @@ __device__ __forceinline__ void store_relu16(uint8_t* a, uint32_t row, uint32_t 
 
 // out[i] = MLP(encode(q[i])) for n queries (n = min(n, *count) when count is given).
 __global__ void __launch_bounds__(TC_THREADS) cache_infer_tc_kernel(const CacheQuery* q, uint32_t n,
-                                                                    const uint32_t* count, const float* grid,
+                                                                    const uint32_t* count, const __half* grid16,
                                                                     const __half* w16, float* out, uint32_t* err) {
     extern __shared__ uint8_t tc_smem_raw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023u) & ~uintptr_t(1023));
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(TC_THREADS) cache_infer_tc_kernel(const CacheQ
     const uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
     for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         uint32_t i = tile * TC_ROWS + tid;
-        if (i < n) encode_row(q[i], grid, s_a, tid);
+        if (i < n) encode_row(q[i], grid16, s_a, tid);
         else zero_row(s_a, tid);
         for (int layer = 0; layer <= CACHE_HIDDEN_LAYERS && ok; ++layer) {
             const bool last = layer == CACHE_HIDDEN_LAYERS;
@@ -351,7 +352,7 @@ __device__ __forceinline__ void mma_chain(uint32_t tmem_col, uint32_t a, uint32_
 }
 
 __global__ void __launch_bounds__(TC_THREADS) cache_train_tc_kernel(const CacheQuery* q, const float* target, uint32_t n,
-                                                                    const float* grid, const __half* w16,
+                                                                    const __half* grid16, const __half* w16,
                                                                     float* w_grad, float* grid_grad, float* loss,
                                                                     float inv_count, uint32_t* err) {
     inv_count = inv_count / TT_GRAD_SCALE;  // the output gradient was scaled by TT_GRAD_SCALE
@@ -425,7 +426,7 @@ __global__ void __launch_bounds__(TC_THREADS) cache_train_tc_kernel(const CacheQ
         const bool valid = i < n;
         const bool acc = done_tiles > 0;
         uint8_t* h0 = sm + TT_OFF_H;
-        if (valid) encode_row(q[i], grid, h0, tid);
+        if (valid) encode_row(q[i], grid16, h0, tid);
         else zero_row(h0, tid);
         // forward
         for (int l = 0; l < CACHE_HIDDEN_LAYERS && ok; ++l) {
@@ -584,9 +585,13 @@ __device__ __forceinline__ float hash_uniform(uint64_t i, uint32_t seed) {
     h ^= h >> 16;
     return (float)(h >> 8) * (1.0f / 16777216.0f);  // [0, 1)
 }
-__global__ void cache_init_kernel(float* grid, float* w, __half* w16, uint32_t seed) {
+__global__ void cache_init_kernel(float* grid, __half* grid16, float* w, __half* w16, uint32_t seed) {
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i < CACHE_GRID_PARAMS) grid[i] = (hash_uniform(i, seed) * 2.0f - 1.0f) * 1e-4f;
+    if (i < CACHE_GRID_PARAMS) {
+        float x = (hash_uniform(i, seed) * 2.0f - 1.0f) * 1e-4f;
+        grid[i] = x;
+        grid16[i] = __float2half_rn(x);
+    }
     if (i < CACHE_PARAMS) {
         float bound = sqrtf(6.0f / (i < CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH ? 128.0f : 67.0f));
         bool unused = i >= CACHE_HIDDEN_LAYERS * CACHE_WIDTH * CACHE_WIDTH &&
@@ -597,7 +602,7 @@ __global__ void cache_init_kernel(float* grid, float* w, __half* w16, uint32_t s
     }
 }
 
-static void launch_infer(const CacheQuery* q, uint32_t n, const uint32_t* count, const float* grid,
+static void launch_infer(const CacheQuery* q, uint32_t n, const uint32_t* count, const __half* grid16,
                          const __half* w16, float* out, uint32_t* err, cudaStream_t st) {
     if (n == 0) return;
     static bool attr[64] = {};  // per device: the shared-memory opt-in is a per-device function attribute
@@ -610,16 +615,16 @@ static void launch_infer(const CacheQuery* q, uint32_t n, const uint32_t* count,
     }
     uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
     uint32_t blocks = std::min<uint32_t>(tiles, 152u * 4u);
-    cache_infer_tc_kernel<<<blocks, TC_THREADS, TC_SMEM, st>>>(q, n, count, grid, w16, out, err);
+    cache_infer_tc_kernel<<<blocks, TC_THREADS, TC_SMEM, st>>>(q, n, count, grid16, w16, out, err);
 }
 
 void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* out, uint32_t* err, cudaStream_t st) {
-    launch_infer(q, n, nullptr, d.grid, d.w16, out, err, st);
+    launch_infer(q, n, nullptr, d.grid16, d.w16, out, err, st);
 }
 
-void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,
+void cache_infer_queue(const __half* grid16, const __half* w16, const CacheQuery* q, const uint32_t* count,
                        uint32_t max_n, float* out, uint32_t* err, cudaStream_t st) {
-    launch_infer(q, max_n, count, grid, w16, out, err, st);
+    launch_infer(q, max_n, count, grid16, w16, out, err, st);
 }
 
 // Training pairs of the frame's records: target = (final - before) / throughput, kept when the
@@ -668,7 +673,7 @@ static void cache_gradient_pass(const CacheDevice& d, const CacheQuery* q, const
     uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
     uint32_t blocks = std::min<uint32_t>(tiles, 152u);
     check_cuda(cudaMemsetAsync(d.loss, 0, 4, st), "memset");
-    cache_train_tc_kernel<<<blocks, TC_THREADS, TT_SMEM, st>>>(q, target, n, d.grid, d.w16, d.w_grad, d.grid_grad,
+    cache_train_tc_kernel<<<blocks, TC_THREADS, TT_SMEM, st>>>(q, target, n, d.grid16, d.w16, d.w_grad, d.grid_grad,
                                                                d.loss, 1.0f / (3.0f * (float)n), err);
 }
 
@@ -691,11 +696,12 @@ void cache_train_step(const CacheDevice& d, const CacheQuery* q, const float* ta
     cache_adam_kernel<<<(CACHE_PARAMS + 255) / 256, 256, 0, st>>>(d.w, d.w_m, d.w_v, d.w_grad, d.w16, CACHE_PARAMS,
                                                                   lr, c1, c2);
     cache_adam_kernel<<<(unsigned)((CACHE_GRID_PARAMS + 255) / 256), 256, 0, st>>>(
-        d.grid, d.grid_m, d.grid_v, d.grid_grad, nullptr, CACHE_GRID_PARAMS, lr, c1, c2);
+        d.grid, d.grid_m, d.grid_v, d.grid_grad, d.grid16, CACHE_GRID_PARAMS, lr, c1, c2);
 }
 
 void cache_init(const CacheDevice& d, uint32_t seed, cudaStream_t st) {
-    cache_init_kernel<<<(unsigned)((CACHE_GRID_PARAMS + 255) / 256), 256, 0, st>>>(d.grid, d.w, d.w16, seed);
+    cache_init_kernel<<<(unsigned)((CACHE_GRID_PARAMS + 255) / 256), 256, 0, st>>>(d.grid, d.grid16, d.w, d.w16,
+                                                                                   seed);
     check_cuda(cudaMemsetAsync(d.grid_m, 0, 4 * CACHE_GRID_PARAMS, st), "memset");
     check_cuda(cudaMemsetAsync(d.grid_v, 0, 4 * CACHE_GRID_PARAMS, st), "memset");
     check_cuda(cudaMemsetAsync(d.grid_grad, 0, 4 * CACHE_GRID_PARAMS, st), "memset");

@@ -26,12 +26,14 @@ struct CacheQuery {
 };
 static_assert(sizeof(CacheQuery) == 48, "48-byte cache queries");
 
-// Device state: FP32 parameters and Adam moments, FP16 copies for inference, gradients.
+// Device state: FP32 parameters and Adam moments, FP16 copies that the queries and the training
+// forward pass read (grid features: two FP16 values per entry, one 32-bit load), gradients.
 struct CacheDevice {
     float *grid, *grid_m, *grid_v, *grid_grad;  // CACHE_GRID_PARAMS each
     float *w, *w_m, *w_v, *w_grad;              // CACHE_PARAMS each
     __half* w16;                                // CACHE_PARAMS
     float* loss;                                // [0]: summed loss of the last step
+    __half* grid16;                             // CACHE_GRID_PARAMS
 };
 
 // err: device error word (ERR_TENSOR_WAIT), may be null.
@@ -47,7 +49,7 @@ void cache_gradients(const CacheDevice& d, const CacheQuery* q, const float* tar
 void cache_clear_gradients(const CacheDevice& d, cudaStream_t st);
 void cache_init(const CacheDevice& d, uint32_t seed, cudaStream_t st);
 // Queries whose count is in device memory (at most max_n of them).
-void cache_infer_queue(const float* grid, const __half* w16, const CacheQuery* q, const uint32_t* count,
+void cache_infer_queue(const __half* grid16, const __half* w16, const CacheQuery* q, const uint32_t* count,
                        uint32_t max_n, float* out, uint32_t* err, cudaStream_t st);
 struct TrainRecord;
 void cache_targets(const TrainRecord* rec, const uint32_t* rec_count, uint32_t cap, const float4* final_radiance,

@@ -71,7 +71,7 @@ struct WfParams {
     float* cq_out;          // their radiance (3 P)
     TrainRecord* rec;       // training records of the frame (rec_cap)
     float4* train_final;    // final radiance of each training path
-    const float* cache_grid;
+    const __half* cache_grid;   // FP16 grid features (two per entry)
     const __half* cache_w16;
     // textured scenes: per slot, the primary ray's ndc (written by regen) and then the mip
     // level of the path (x, written at bounce 0); null without textures
