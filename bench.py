@@ -67,6 +67,8 @@ def parse_args():
     p.add_argument("--no-closed", action="store_true", help="skip the closed-scene (Cornell box) sample")
     p.add_argument("--serve-batch", type=int, default=96, help="requests of the serving sample's capacity run")
     p.add_argument("--serve-inflight", type=int, default=SERVE_INFLIGHT, help="requests the server renders together")
+    p.add_argument("--serve-policy", default="fair", choices=["fair", "smallest_first"],
+                   help="server scheduling policy (TT_SERVER_POLICY_*)")
     p.add_argument("--serve-requests", type=int, default=512,
                    help="requests at 0.8 x capacity in the serving sample (a quarter as many at 0.5 x and 1.1 x)")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level", "wide"],
@@ -875,13 +877,14 @@ SERVE_INFLIGHT = 16  # requests rendered together per round
 
 
 def serve_run(ctx, reqs, rate: float | None, rng, pool_paths: int, capacity_msamples_s: float | None = None,
-              inflight: int = 16) -> dict:
+              inflight: int = 16, policy: int = 0) -> dict:
     """Submits `reqs` (Poisson arrivals at `rate` per second, or all at once when rate is None),
     waits for all of them and returns latency percentiles and throughput.  Finished requests'
     image buffers are released as the run goes."""
     from tinytrace_gb300.server import RenderServer
 
-    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=inflight, pool_paths=pool_paths) as srv:
+    with RenderServer(ctx, hbm_budget_bytes=150 << 30, max_inflight=inflight, pool_paths=pool_paths,
+                      policy=policy) as srv:
         t0 = time.perf_counter()
         due = t0
         ids, pending = [], []
@@ -1001,14 +1004,18 @@ def run_serving(a, ctx) -> dict:
     check(ctx.lib.tt_autotune(ctx.handle, pool[2][1], native.ptr(c), img, ctypes.byref(tune)))
     pool_paths = int(tune.slots)
     out = {"scenes_triangles": [int(t) for t, _ in pool], "hbm_budget_gb": 150, "max_inflight": a.serve_inflight,
+           "policy": a.serve_policy,
            "pool_paths": pool_paths, "pool_tuning": {"tune_spp": 4, "default_ms": tune.default_ms,
                                                      "tuned_ms": tune.best_ms, "renders": int(tune.renders)},
            "round_items": 1 << 26,
            "mix": "side ~U{256..2048} step 16, spp ~U{1..256}, depth 8, scene log-uniform 1e3..5e6 triangles"}
-    serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng, pool_paths, None, a.serve_inflight)  # warm-up
+    policy = {"fair": native.TT_SERVER_POLICY_FAIR, "smallest_first": native.TT_SERVER_POLICY_SMALLEST_FIRST}[
+        a.serve_policy]
+    serve_run(ctx, serve_requests(rng, pool, logs, 8, 0), None, rng, pool_paths, None, a.serve_inflight,
+              policy)  # warm-up
     out["one_request"] = serve_one_request(ctx, pool[3][1], cam, pool_paths)
     cap = serve_run(ctx, serve_requests(rng, pool, logs, a.serve_batch, 100), None, rng, pool_paths, None,
-                    a.serve_inflight)
+                    a.serve_inflight, policy)
     # capacity in requests per second: the sample throughput of the saturated server over the mix's
     # mean request size (E[side^2] E[spp], side = 16 k with k ~ U{16..128}, spp ~ U{1..256}), not
     # the completion rate of one finite batch, whose few large requests decide its makespan
@@ -1022,7 +1029,7 @@ def run_serving(a, ctx) -> dict:
     frame = 10_000
     for frac, n in ((0.5, max(32, a.serve_requests // 4)), (0.8, a.serve_requests), (1.1, max(32, a.serve_requests // 4))):
         res = serve_run(ctx, serve_requests(rng, pool, logs, n, frame), frac * mu, rng, pool_paths,
-                        cap["throughput_msamples_s"], a.serve_inflight)
+                        cap["throughput_msamples_s"], a.serve_inflight, policy)
         frame += n
         res["fraction_of_capacity"] = frac
         res["sustained"] = bool(res["completed_per_s"] >= 0.95 * res["offered_per_s"]

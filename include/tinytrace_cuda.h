@@ -486,7 +486,15 @@ typedef struct tt_server_config {
     uint32_t max_inflight;     /* requests rendered together (0 = 16, at most 64) */
     uint32_t pool_paths;       /* path slots of the shared wavefront pool (0 = 2^21, at most 2^24) */
     uint64_t round_items;      /* (pixel, sample) work items per round across the batch (0 = 2^26) */
+    uint32_t policy;           /* TT_SERVER_POLICY_* */
+    uint32_t reserved;         /* 0 */
 } tt_server_config;
+/* FAIR: queued requests are admitted in arrival order and every request of the batch gets an
+ * equal share of each round's work items.  SMALLEST_FIRST: the queued request with the fewest
+ * samples is admitted first, and each round serves the requests with the least remaining work
+ * first (full chunks until the round's work items are spent; the rest wait for a later round). */
+#define TT_SERVER_POLICY_FAIR 0u
+#define TT_SERVER_POLICY_SMALLEST_FIRST 1u
 typedef struct tt_server_stats {
     uint64_t submitted, completed, failed, queued, inflight;
     uint64_t bytes_in_flight, peak_bytes_in_flight, peak_inflight;

@@ -57,6 +57,8 @@ pub const TT_ACCEL_FLAT: u64 = 1;
 pub const TT_ACCEL_TWO_LEVEL: u64 = 2;
 pub const TT_ACCEL_FLAT_WIDE: u64 = 3;
 
+pub const TT_SERVER_POLICY_FAIR: u32 = 0;
+pub const TT_SERVER_POLICY_SMALLEST_FIRST: u32 = 1;
 pub const TT_TRACE_CULL_BACK_FACES: u32 = 1;
 pub const TT_TRACE_NOALLOC_MAX_RAYS: u32 = 65536;
 
@@ -360,6 +362,8 @@ pub struct tt_server_config {
     pub max_inflight: u32,
     pub pool_paths: u32,
     pub round_items: u64,
+    pub policy: u32,
+    pub reserved: u32,
 }
 
 #[repr(C)]

@@ -67,18 +67,20 @@ def _alone(ctx, handle, constants):
     return ctx.download(img, w, h)
 
 
-@pytest.mark.parametrize("round_items", [20_000, 0])
-def test_requests_in_the_mix_equal_alone(ctx, round_items):
+@pytest.mark.parametrize("round_items,policy", [(20_000, native.TT_SERVER_POLICY_FAIR), (0, native.TT_SERVER_POLICY_FAIR),
+                                               (20_000, native.TT_SERVER_POLICY_SMALLEST_FIRST)])
+def test_requests_in_the_mix_equal_alone(ctx, round_items, policy):
     """round_items 20,000: every request takes several rounds of a few samples per pixel, and the
     requests that finish early are replaced by queued ones between rounds; 0: the default share
-    (each request's whole sample count in one round)."""
+    (each request's whole sample count in one round); smallest first: requests are admitted and
+    served out of arrival order, some of them left out of some rounds."""
     sc = _scenes()
     handles = _create(ctx, sc)
     rng = np.random.default_rng(21)
     reqs = _requests(rng, 15)
     consts = [make_constants(sc[name][1], ext, cfg, frame, 0) for name, ext, cfg, frame in reqs]
     alone = [_alone(ctx, handles[name], c) for (name, _, _, _), c in zip(reqs, consts)]
-    with RenderServer(ctx, max_inflight=4, pool_paths=1 << 14, round_items=round_items) as srv:
+    with RenderServer(ctx, max_inflight=4, pool_paths=1 << 14, round_items=round_items, policy=policy) as srv:
         ids = [srv.submit(handles[name], c) for (name, _, _, _), c in zip(reqs, consts)]
         imgs = [srv.wait(i) for i in ids]
         st = srv.stats()

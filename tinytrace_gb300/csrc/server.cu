@@ -85,7 +85,7 @@ struct tt_server {
     int device = 0;
     tt_context* ctx = nullptr;
     uint64_t budget = DEFAULT_BUDGET, round_items = DEFAULT_ROUND_ITEMS;
-    uint32_t max_live = DEFAULT_INFLIGHT, paths = DEFAULT_PATHS;
+    uint32_t max_live = DEFAULT_INFLIGHT, paths = DEFAULT_PATHS, policy = TT_SERVER_POLICY_FAIR;
     cudaStream_t stream = nullptr, capture = nullptr, body = nullptr;
     cudaEvent_t round_start = nullptr, round_done = nullptr;
     cudaMemPool_t pool = nullptr;
@@ -100,6 +100,7 @@ struct tt_server {
     cudaGraphExec_t graph[2][3][2] = {};  // [texture sampling][BATCH_* structures][short stacks]
     std::vector<Staging> staging_free;
     uint64_t round_items_now = 0;
+    uint32_t round_n = 0;  // requests in the last round: live[0 .. round_n)
 
     std::mutex mu;
     std::condition_variable cv;       // submissions and stop (scheduler side)
@@ -197,9 +198,15 @@ void tt_server::admit(std::vector<Request*>& live) {
     {
         std::lock_guard<std::mutex> lk(mu);
         while (!queue.empty()) {
-            Request* head = queue.front();
+            auto pick = queue.begin();
+            if (policy == TT_SERVER_POLICY_SMALLEST_FIRST)  // fewest samples, then arrival order
+                pick = std::min_element(queue.begin(), queue.end(), [](const Request* a, const Request* b) {
+                    uint64_t sa = a->WH * a->c.sample_count, sb = b->WH * b->c.sample_count;
+                    return sa != sb ? sa < sb : a->id < b->id;
+                });
+            Request* head = *pick;
             if (head->arena_bytes > budget) {  // can never fit
-                queue.pop_front();
+                queue.erase(pick);
                 head->status = TT_REQUEST_FAILED;
                 head->error = "request needs more device memory than the HBM budget";
                 head->finished = Clock::now();
@@ -209,7 +216,7 @@ void tt_server::admit(std::vector<Request*>& live) {
                 continue;
             }
             if (live.size() + in.size() >= max_live || stats.bytes_in_flight + head->arena_bytes > budget) break;
-            queue.pop_front();
+            queue.erase(pick);
             head->status = TT_REQUEST_RUNNING;
             stats.queued--;
             stats.inflight++;
@@ -242,15 +249,39 @@ void tt_server::admit(std::vector<Request*>& live) {
 // requests whose last chunk this is (into pinned staging, `outs`).
 void tt_server::launch_round(std::vector<Request*>& live) {
     uint32_t n = (uint32_t)live.size();
-    uint64_t share = std::max<uint64_t>(1, round_items / n);
+    if (policy == TT_SERVER_POLICY_SMALLEST_FIRST) {
+        // least remaining work first: full chunks until the round's items are spent (the first
+        // request always gets one); the requests left out wait, after the served ones in `live`
+        std::stable_sort(live.begin(), live.end(), [](const Request* a, const Request* b) {
+            return a->WH * (a->c.sample_count - a->done_spp) < b->WH * (b->c.sample_count - b->done_spp);
+        });
+        uint64_t room = round_items;
+        uint32_t served = 0;
+        for (Request* r : live) {
+            uint32_t left = r->c.sample_count - r->done_spp;
+            uint64_t fit = room / r->WH;
+            uint32_t spp = (uint32_t)std::min<uint64_t>(std::min(r->chunk_cap, left), served == 0 ? std::max<uint64_t>(fit, 1) : fit);
+            r->chunk_spp = spp;
+            if (spp == 0) break;
+            room -= std::min<uint64_t>(room, (uint64_t)spp * r->WH);
+            ++served;
+        }
+        n = served;
+    } else {
+        uint64_t share = std::max<uint64_t>(1, round_items / n);
+        for (Request* r : live) {
+            uint32_t left = r->c.sample_count - r->done_spp;
+            uint32_t fair = (uint32_t)std::max<uint64_t>(1, share / r->WH);
+            r->chunk_spp = std::min({r->chunk_cap, left, fair});
+        }
+    }
+    round_n = n;
     uint64_t items = 0, pixels = 0;
     uint32_t max_bounce = 1;
     bool tex = false, wide = false, two_level = false, short_stack = true;
     for (uint32_t k = 0; k < n; ++k) {
         Request& r = *live[k];
         uint32_t left = r.c.sample_count - r.done_spp;
-        uint32_t fair = (uint32_t)std::max<uint64_t>(1, share / r.WH);
-        r.chunk_spp = std::min({r.chunk_cap, left, fair});
         r.last = r.chunk_spp == left;
         BatchRequest& b = h_reqs[k];
         b.c = r.c;
@@ -321,8 +352,8 @@ void tt_server::run() {
         if (!live.empty()) {
             try {
                 launch_round(live);
-                for (Request* r : live)
-                    if (r->last) {
+                for (uint32_t k = 0; k < round_n; ++k)
+                    if (Request* r = live[k]; r->last) {
                         Staging s = take_staging(r->bytes);
                         check_cuda(cudaMemcpyAsync(s.ptr, r->target, r->bytes, cudaMemcpyDeviceToHost, stream),
                                    "image");
@@ -368,6 +399,10 @@ void tt_server::run() {
             std::vector<Request*> still;
             for (size_t k = 0; k < live.size(); ++k) {
                 Request* r = live[k];
+                if (k >= round_n) {  // not served this round
+                    still.push_back(r);
+                    continue;
+                }
                 std::string error;
                 if (q != cudaSuccess) error = std::string("device error: ") + cudaGetErrorString(q);
                 else if (batch_err & ERR_ITERATION_LIMIT) error = "iteration limit reached";
@@ -440,7 +475,10 @@ int32_t tt_server_create(tt_context* ctx, const tt_server_config* config, tt_ser
             if (config->max_inflight) srv->max_live = config->max_inflight;
             if (config->pool_paths) srv->paths = config->pool_paths;
             if (config->round_items) srv->round_items = config->round_items;
+            srv->policy = config->policy;
         }
+        need(srv->policy == TT_SERVER_POLICY_FAIR || srv->policy == TT_SERVER_POLICY_SMALLEST_FIRST,
+             "unknown server policy");
         need(srv->max_live <= BATCH_MAX_REQUESTS, "max_inflight above 64");
         need(srv->paths <= (1u << 24), "pool_paths above 2^24");
         need(srv->round_items >= 1 && srv->round_items <= (1ull << 30), "round_items must be in [1, 2^30]");

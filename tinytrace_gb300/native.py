@@ -59,6 +59,8 @@ TT_ACCEL_TWO_LEVEL = 2
 TT_ACCEL_FLAT_WIDE = 3
 TT_OPTION_STAGE_TIMING = 4
 TT_OPTION_GRAPHS = 5
+TT_SERVER_POLICY_FAIR = 0
+TT_SERVER_POLICY_SMALLEST_FIRST = 1
 TT_REQUEST_QUEUED = 0
 TT_REQUEST_RUNNING = 1
 TT_REQUEST_DONE = 2
@@ -237,7 +239,8 @@ class TuneResult(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
-                ("pool_paths", ctypes.c_uint32), ("round_items", ctypes.c_uint64)]
+                ("pool_paths", ctypes.c_uint32), ("round_items", ctypes.c_uint64), ("policy", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class ServerStats(ctypes.Structure):

@@ -19,10 +19,10 @@ from .renderer import Context, SceneArrays
 
 class RenderServer:
     def __init__(self, context: Context, hbm_budget_bytes: int = 0, max_inflight: int = 0,
-                 pool_paths: int = 0, round_items: int = 0):
+                 pool_paths: int = 0, round_items: int = 0, policy: int = native.TT_SERVER_POLICY_FAIR):
         self.context = context
         self.lib = context.lib
-        cfg = native.ServerConfig(hbm_budget_bytes, max_inflight, pool_paths, round_items)
+        cfg = native.ServerConfig(hbm_budget_bytes, max_inflight, pool_paths, round_items, policy, 0)
         h = ctypes.c_void_p()
         check(self.lib.tt_server_create(context.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h
