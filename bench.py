@@ -67,7 +67,7 @@ def parse_args():
     p.add_argument("--no-closed", action="store_true", help="skip the closed-scene (Cornell box) sample")
     p.add_argument("--serve-batch", type=int, default=96, help="requests of the serving sample's capacity run")
     p.add_argument("--serve-inflight", type=int, default=SERVE_INFLIGHT, help="requests the server renders together")
-    p.add_argument("--serve-policy", default="fair", choices=["fair", "smallest_first"],
+    p.add_argument("--serve-policy", default="smallest_first", choices=["fair", "smallest_first"],
                    help="server scheduling policy (TT_SERVER_POLICY_*)")
     p.add_argument("--serve-requests", type=int, default=512,
                    help="requests at 0.8 x capacity in the serving sample (a quarter as many at 0.5 x and 1.1 x)")
@@ -975,7 +975,8 @@ def serve_one_request(ctx, scene, cam, pool_paths: int) -> dict:
 
 def run_serving(a, ctx) -> dict:
     """Continuous batching under the C4 request mix on five resident scenes (1e3 .. 5e6
-    triangles), HBM budget 150 GB, up to 16 requests rendered together per round through one
+    triangles), HBM budget 150 GB, smallest-first scheduling (a.serve_policy), up to 16 requests
+    rendered together per round through one
     shared path pool whose size tt_autotune picks on a request of the mix (the 260k-triangle
     scene at 1024 x 1024, 4 spp, depth 8).  First the server's capacity: a batch of
     a.serve_batch requests submitted at once gives the saturated sample throughput, which over
