@@ -475,10 +475,10 @@ int32_t tt_cache_status_get(tt_context* ctx, tt_cache_status* out);
  * next sample chunk of every admitted request (round_items work items in total, shared evenly)
  * and traces them through one shared wavefront path pool and one set of persistent kernels
  * (one CUDA graph launch per round).  Between rounds it retires finished requests, copying their
- * images into the callers' buffers while the next round renders, and admits the head of the
- * queue while the batch has room and the request's device memory fits in the HBM budget next to
- * the requests already admitted.  A request's image is the same, bit for bit, alone or among
- * others. */
+ * images into the callers' buffers while the next round renders, and admits queued requests
+ * (in arrival order, or smallest first: TT_SERVER_POLICY_*) while the batch has room and the
+ * request's device memory fits in the HBM budget next to the requests already admitted.  A
+ * request's image is the same, bit for bit, alone or among others. */
 typedef struct tt_server tt_server;
 typedef struct tt_server_config {
     uint64_t hbm_budget_bytes; /* device memory admitted requests may hold (0 = 150 GB); the

@@ -1,15 +1,16 @@
 // Continuous-batching render server (tt_server_*): requests of any scene, resolution and
 // sample count share one wavefront path pool and one set of persistent kernels.
 //
-// The scheduler thread works in rounds.  A round takes the next sample chunk of every admitted
-// request (up to round_items work items in total, split evenly across the requests and capped
-// at 64 samples per pixel), lays the chunks end to end as the work items of one shared-pool
+// The scheduler thread works in rounds.  A round takes the next sample chunk of the admitted
+// requests (up to round_items work items in total, capped at 64 samples per pixel per request:
+// split evenly across the requests under the fair policy, given to the requests with the least
+// remaining work first under the smallest-first policy), lays the chunks end to end as the work items of one shared-pool
 // wavefront loop (regen, extend, shade, shadow in a device-side while loop) and finishes with
 // the per-request reductions; the whole round is one launch of a CUDA graph instantiated once
 // per server.  Between rounds the scheduler retires finished requests (their images are copied
-// out while the next round runs) and admits queued ones in arrival order while the batch has
-// room and their device memory fits in the HBM budget, so requests that arrive while others
-// render join the batch at the next round boundary.
+// out while the next round runs) and admits queued ones (in arrival order, or the smallest
+// first) while the batch has room and their device memory fits in the HBM budget, so requests
+// that arrive while others render join the batch at the next round boundary.
 //
 // Per request the device holds one stream-ordered arena (allocated from a server-owned memory
 // pool): the per-sample radiance of its largest chunk, the running pixel sums, the image and
