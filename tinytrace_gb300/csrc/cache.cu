@@ -62,7 +62,7 @@ __device__ __forceinline__ void grid_corners(const float3& p, int l, uint32_t* i
 }
 
 // ---------------------------------------------------------------- inference (tcgen05 tensor cores)
-// A warpgroup of 128 threads owns 128 queries at a time (thread t: query row t).  Per layer the
+// One CTA of 128 threads owns 128 queries at a time (thread t: query row t).  Per layer the
 // activations A (128 x 64 FP16) and the layer's weights B (64 x 64 FP16, [out][in]) sit in
 // shared memory in the canonical K-major layout without swizzling: 8-row x 16-byte core
 // matrices, the 8 core matrices of a row group 128 bytes apart along K (leading byte offset)
@@ -83,6 +83,8 @@ constexpr uint32_t TC_WOUT_BYTES = TC_OUT_N * CACHE_WIDTH * 2;     // 2 KB
 constexpr uint32_t TC_A_BYTES = TC_ROWS * CACHE_WIDTH * 2;         // 16 KB
 constexpr uint32_t TC_OFF_WOUT = CACHE_HIDDEN_LAYERS * TC_W_BYTES;
 constexpr uint32_t TC_OFF_A = TC_OFF_WOUT + TC_WOUT_BYTES;
+constexpr uint32_t TC_OFF_BAR = TC_OFF_A + TC_A_BYTES;
+constexpr uint32_t TC_SMEM = TC_OFF_BAR + 16 + 1024;  // + alignment slack
 
 // Byte offset of element (row, k) of a 64-wide K-major operand in the core-matrix layout.
 __device__ __forceinline__ uint32_t core_offset(uint32_t row, uint32_t k) {
@@ -196,40 +198,25 @@ __device__ __forceinline__ void store_relu16(uint8_t* a, uint32_t row, uint32_t 
 }
 
 // out[i] = MLP(encode(q[i])) for n queries (n = min(n, *count) when count is given).
-// Two warpgroups per CTA share the weights in shared memory and each run the inference loop on
-// their own tiles (tile index 2 * blockIdx.x + warpgroup, grid-strided) with their own
-// activation tile, mbarrier and 64 TMEM columns, synchronising on their own named barrier, so
-// one warpgroup's hash-grid gathers overlap the other's MMAs and an SM holds 24 warps (three
-// CTAs of 68 KB) instead of 16.  A warp reads the TMEM lanes of its quadrant (warp % 4).
-constexpr int TC2_THREADS = 256;
-constexpr uint32_t TC2_TMEM_COLS = 2 * TC_TMEM_COLS;
-constexpr uint32_t TC2_OFF_BAR = TC_OFF_A + 2 * TC_A_BYTES;  // two mbarriers, TMEM address, failure flags
-constexpr uint32_t TC2_SMEM = TC2_OFF_BAR + 32 + 1024;      // + alignment slack
-__device__ __forceinline__ void group_sync(uint32_t group) {
-    if (group == 0u) asm volatile("bar.sync 1, 128;\n" ::: "memory");
-    else asm volatile("bar.sync 2, 128;\n" ::: "memory");
-}
-__global__ void __launch_bounds__(TC2_THREADS) cache_infer_tc_kernel(const CacheQuery* q, uint32_t n,
-                                                                     const uint32_t* count, const __half* grid16,
-                                                                     const __half* w16, float* out, uint32_t* err) {
+__global__ void __launch_bounds__(TC_THREADS) cache_infer_tc_kernel(const CacheQuery* q, uint32_t n,
+                                                                    const uint32_t* count, const __half* grid16,
+                                                                    const __half* w16, float* out, uint32_t* err) {
     extern __shared__ uint8_t tc_smem_raw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023u) & ~uintptr_t(1023));
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(sm + TC2_OFF_BAR);            // [2]
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + TC2_OFF_BAR + 16);
-    volatile uint32_t* s_fail = reinterpret_cast<volatile uint32_t*>(sm + TC2_OFF_BAR + 24);  // [2]
+    uint8_t* s_a = sm + TC_OFF_A;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(sm + TC_OFF_BAR);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(sm + TC_OFF_BAR + 8);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t group = tid >> 7, row = tid & 127u;
-    uint8_t* s_a = sm + TC_OFF_A + group * TC_A_BYTES;
     if (count) n = min(n, *count);
 
     // weights into the core-matrix layout: hidden layers [n][k], then 16 output rows (3..15 zero)
-    for (uint32_t c = tid; c < CACHE_HIDDEN_LAYERS * CACHE_WIDTH * 8u; c += TC2_THREADS) {
+    for (uint32_t c = tid; c < CACHE_HIDDEN_LAYERS * CACHE_WIDTH * 8u; c += TC_THREADS) {
         uint32_t layer = c / (CACHE_WIDTH * 8u), r = (c / 8u) % CACHE_WIDTH, j = c % 8u;
         uint4 v = reinterpret_cast<const uint4*>(w16 + (uint64_t)layer * CACHE_WIDTH * CACHE_WIDTH +
                                                  (uint64_t)r * CACHE_WIDTH)[j];
         *reinterpret_cast<uint4*>(sm + layer * TC_W_BYTES + core_offset(r, 8u * j)) = v;
     }
-    for (uint32_t c = tid; c < TC_OUT_N * 8u; c += TC2_THREADS) {
+    for (uint32_t c = tid; c < TC_OUT_N * 8u; c += TC_THREADS) {
         uint32_t r = c / 8u, j = c % 8u;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (r < (uint32_t)CACHE_OUT_ROWS)
@@ -239,14 +226,11 @@ __global__ void __launch_bounds__(TC2_THREADS) cache_infer_tc_kernel(const Cache
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(s_bar)) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(s_bar + 1)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-        s_fail[0] = 0u;
-        s_fail[1] = 0u;
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(s_tmem)),
-                     "r"(TC2_TMEM_COLS)
+                     "r"(TC_TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
@@ -254,24 +238,24 @@ __global__ void __launch_bounds__(TC2_THREADS) cache_infer_tc_kernel(const Cache
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *s_tmem + group * TC_TMEM_COLS;  // this warpgroup's 64 columns
-    const uint32_t bar = smem_u32(s_bar + group);
+    const uint32_t tmem = *s_tmem;
+    const uint32_t bar = smem_u32(s_bar);
     const uint32_t a_addr = smem_u32(s_a), w_addr = smem_u32(sm);
-    const uint32_t lane_taddr = tmem + ((32u * (warp & 3u)) << 16);
+    const uint32_t lane_taddr = tmem + ((32u * warp) << 16);
     uint32_t phase = 0;
     bool ok = true;
     const uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
-    for (uint32_t tile = 2u * blockIdx.x + group; tile < tiles && ok; tile += 2u * gridDim.x) {
-        uint32_t i = tile * TC_ROWS + row;
-        if (i < n) encode_row(q[i], grid16, s_a, row);
-        else zero_row(s_a, row);
+    for (uint32_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        uint32_t i = tile * TC_ROWS + tid;
+        if (i < n) encode_row(q[i], grid16, s_a, tid);
+        else zero_row(s_a, tid);
         for (int layer = 0; layer <= CACHE_HIDDEN_LAYERS && ok; ++layer) {
             const bool last = layer == CACHE_HIDDEN_LAYERS;
             fence_async_smem();
             tc_fence_before();
-            group_sync(group);
+            __syncthreads();
             tc_fence_after();
-            if (row == 0) {
+            if (tid == 0) {
                 uint32_t b_addr = last ? w_addr + TC_OFF_WOUT : w_addr + (uint32_t)layer * TC_W_BYTES;
                 uint32_t idesc = mma_idesc(last ? TC_OUT_N : (uint32_t)CACHE_WIDTH);
 #pragma unroll
@@ -279,9 +263,7 @@ __global__ void __launch_bounds__(TC2_THREADS) cache_infer_tc_kernel(const Cache
                     mma_f16(tmem, smem_desc(a_addr + 256u * kk), smem_desc(b_addr + 256u * kk), idesc, kk);
                 mma_commit(bar);
             }
-            if (!bar_wait(bar, phase)) s_fail[group] = 1u;
-            group_sync(group);  // one verdict for the whole warpgroup
-            ok = s_fail[group] == 0u;
+            ok = __syncthreads_and(bar_wait(bar, phase) ? 1 : 0) != 0;  // one verdict for the whole CTA
             phase ^= 1u;
             tc_fence_after();
             if (!ok) break;
@@ -291,7 +273,7 @@ __global__ void __launch_bounds__(TC2_THREADS) cache_infer_tc_kernel(const Cache
                     float v[16];
                     tmem_ld16(lane_taddr + (uint32_t)c, v);
                     tmem_ld_wait();
-                    store_relu16(s_a, row, (uint32_t)c, v);
+                    store_relu16(s_a, tid, (uint32_t)c, v);
                 }
             } else {
                 float v[16];
@@ -306,13 +288,13 @@ __global__ void __launch_bounds__(TC2_THREADS) cache_infer_tc_kernel(const Cache
         }
     }
     if (!ok && err) atomicOr(err, ERR_TENSOR_WAIT);
-    // every MMA of this warpgroup was waited for (or the wait ran out and nothing more was issued)
+    // every MMA of this CTA was waited for (or the wait ran out and nothing more was issued)
     tc_fence_before();
     __syncthreads();
     if (!ok) bar_wait(bar, phase ^ 1u);  // one more bounded wait for the last commit in flight
     tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*s_tmem), "r"(TC2_TMEM_COLS)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS)
                      : "memory");
 }
 
@@ -627,13 +609,13 @@ static void launch_infer(const CacheQuery* q, uint32_t n, const uint32_t* count,
     int dev = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= 64 || !attr[dev]) {
-        check_cuda(cudaFuncSetAttribute(cache_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC2_SMEM),
+        check_cuda(cudaFuncSetAttribute(cache_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM),
                    "infer smem");
         if (dev >= 0 && dev < 64) attr[dev] = true;
     }
     uint32_t tiles = (n + TC_ROWS - 1u) / TC_ROWS;
-    uint32_t blocks = std::min<uint32_t>((tiles + 1u) / 2u, 152u * 3u);  // two tiles at a time, 3 CTAs per SM
-    cache_infer_tc_kernel<<<blocks, TC2_THREADS, TC2_SMEM, st>>>(q, n, count, grid16, w16, out, err);
+    uint32_t blocks = std::min<uint32_t>(tiles, 152u * 4u);
+    cache_infer_tc_kernel<<<blocks, TC_THREADS, TC_SMEM, st>>>(q, n, count, grid16, w16, out, err);
 }
 
 void cache_infer(const CacheDevice& d, const CacheQuery* q, uint32_t n, float* out, uint32_t* err, cudaStream_t st) {
