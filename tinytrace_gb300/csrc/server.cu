@@ -246,8 +246,10 @@ void tt_server::admit(std::vector<Request*>& live) {
     }
 }
 
-// Enqueues one round over the batch: tables, the graph, the error words, and the images of the
-// requests whose last chunk this is (into pinned staging, `outs`).
+// Enqueues one round: picks each request's chunk by the policy (the round serves live[0 ..
+// round_n)), uploads the request table, the scene table and the round header, launches the
+// graph and reads the error words back; run() adds the image copies of the requests whose last
+// chunk this is.
 void tt_server::launch_round(std::vector<Request*>& live) {
     uint32_t n = (uint32_t)live.size();
     if (policy == TT_SERVER_POLICY_SMALLEST_FIRST) {
