@@ -491,8 +491,9 @@ typedef struct tt_server_config {
 } tt_server_config;
 /* FAIR: queued requests are admitted in arrival order and every request of the batch gets an
  * equal share of each round's work items.  SMALLEST_FIRST: the queued request with the fewest
- * samples is admitted first, and each round serves the requests with the least remaining work
- * first (full chunks until the round's work items are spent; the rest wait for a later round). */
+ * samples is admitted first; each round serves the oldest admitted request with up to a quarter
+ * of its work items (so that large requests keep progressing) and then the requests with the
+ * least remaining work (full chunks until the round's work items are spent; the rest wait). */
 #define TT_SERVER_POLICY_FAIR 0u
 #define TT_SERVER_POLICY_SMALLEST_FIRST 1u
 typedef struct tt_server_stats {

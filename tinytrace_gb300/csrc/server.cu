@@ -253,16 +253,21 @@ void tt_server::admit(std::vector<Request*>& live) {
 void tt_server::launch_round(std::vector<Request*>& live) {
     uint32_t n = (uint32_t)live.size();
     if (policy == TT_SERVER_POLICY_SMALLEST_FIRST) {
-        // least remaining work first: full chunks until the round's items are spent (the first
-        // request always gets one); the requests left out wait, after the served ones in `live`
-        std::stable_sort(live.begin(), live.end(), [](const Request* a, const Request* b) {
+        // the oldest request first, with up to a quarter of the round's items (so the largest
+        // requests keep progressing), then least remaining work first: full chunks until the
+        // round's items are spent; the requests left out wait, after the served ones in `live`
+        auto oldest = std::min_element(live.begin(), live.end(), [](const Request* a, const Request* b) {
+            return a->id < b->id;
+        });
+        std::iter_swap(live.begin(), oldest);
+        std::stable_sort(live.begin() + 1, live.end(), [](const Request* a, const Request* b) {
             return a->WH * (a->c.sample_count - a->done_spp) < b->WH * (b->c.sample_count - b->done_spp);
         });
         uint64_t room = round_items;
         uint32_t served = 0;
         for (Request* r : live) {
             uint32_t left = r->c.sample_count - r->done_spp;
-            uint64_t fit = room / r->WH;
+            uint64_t fit = (served == 0 ? round_items / 4u : room) / r->WH;
             uint32_t spp = (uint32_t)std::min<uint64_t>(std::min(r->chunk_cap, left), served == 0 ? std::max<uint64_t>(fit, 1) : fit);
             r->chunk_spp = spp;
             if (spp == 0) break;
