@@ -50,6 +50,35 @@ def test_restir_frames_match_oracle(gpu_context, name):
     r.close()
 
 
+@pytest.mark.parametrize("accel", ["two_level", "wide"])
+def test_restir_structures_match_oracle(gpu_context, accel):
+    """The ReSTIR passes compiled for the two-level and the compressed wide structure (each
+    scene's passes use the traversal of its own structure): the field's frames as above."""
+    from tinytrace_gb300 import native
+    from tinytrace_gb300.native import check
+
+    make, center, radius, height, extent = CASES["field"]
+    r = Renderer(extent)
+    value = {"two_level": native.TT_ACCEL_TWO_LEVEL, "wide": native.TT_ACCEL_FLAT_WIDE}[accel]
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_ACCEL, value))
+    r.set_scene(make())
+    assert r.context.scene_stats(r.scene).accel == value
+    r.set_config(Config(bounce_count=1, sample_count=1))
+    orc = oracle.OracleScene(r.scene_arrays)
+    R = oracle.OracleRestir(orc, *extent)
+    cpu = np.zeros((extent[1], extent[0], 4), np.float32)
+    for f in range(3):
+        r.camera = _orbit(center, radius, height, f)
+        c = make_constants(r.camera, extent, r.config(), r.context.frame_index(), r.accumulated_frame_count)
+        r.render_restir_to_target()
+        gpu = r.context.download(r.render_target, *extent)
+        R.frame(c, cpu)
+        assert_same_bits(gpu, cpu, f"{accel} frame {f} image")
+        assert_same_bits(r.restir_reservoirs(), R.reservoirs(), f"{accel} frame {f} reservoirs")
+        r.present()
+    r.close()
+
+
 def test_restir_config_and_reset(gpu_context):
     make, center, radius, height, extent = CASES["cornell"]
     r = Renderer(extent)
