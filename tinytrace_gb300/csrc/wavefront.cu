@@ -80,6 +80,37 @@ __device__ __forceinline__ uint32_t block_append(uint32_t* counter, bool pred, u
     return pos;
 }
 
+// Block-aggregated append of two kinds: threads with `first` get consecutive positions at the
+// start of the block's range, threads with `second` the positions after them (one atomicAdd per
+// block on `counter`).  Every thread of the block must call it; `s_warp` holds 2 BLOCK / 32 + 2
+// words.
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_append2(uint32_t* counter, bool first, bool second, uint32_t* s_warp) {
+    constexpr int WARPS = BLOCK / 32;
+    uint32_t ma = __ballot_sync(0xffffffffu, first), mb = __ballot_sync(0xffffffffu, second);
+    int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
+    if (lane == 0) {
+        s_warp[warp] = (uint32_t)__popc(ma);
+        s_warp[WARPS + warp] = (uint32_t)__popc(mb);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t sum = 0u;
+        for (int k = 0; k < 2 * WARPS; ++k) {  // the first kind's counts, then the second kind's
+            uint32_t c = s_warp[k];
+            s_warp[k] = sum;
+            sum += c;
+        }
+        s_warp[2 * WARPS] = sum ? atomicAdd(counter, sum) : 0u;
+    }
+    __syncthreads();
+    uint32_t below = lane_mask_lt();
+    uint32_t pos = s_warp[2 * WARPS] + (first ? s_warp[warp] + (uint32_t)__popc(ma & below)
+                                              : s_warp[WARPS + warp] + (uint32_t)__popc(mb & below));
+    __syncthreads();
+    return pos;
+}
+
 // Pixel of band-ordered index t: bands of 8 rows, column-major inside a band, so a warp's 32
 // consecutive items cover a 4 x 8 pixel block (coherent camera rays).
 __device__ __forceinline__ void band_pixel(uint32_t t, uint32_t W, uint32_t H, uint32_t& x, uint32_t& y) {
@@ -148,6 +179,7 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
                                                                const __grid_constant__ WfParams w,
                                                                const __grid_constant__ BatchParams b) {
     __shared__ uint32_t s_warp[REGEN_BLOCK / 32 + 1];
+    __shared__ uint32_t s_warp2[2 * (REGEN_BLOCK / 32) + 2];
     __shared__ uint32_t s_base[MULTI ? BATCH_MAX_REQUESTS : 1];
     __shared__ uint32_t s_next, s_nreq, s_total;
     uint32_t s = blockIdx.x * REGEN_BLOCK + threadIdx.x;
@@ -183,7 +215,8 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
     uint32_t total = MULTI ? s_total : w.chunk_items;
     bool need = valid && !live && s_next < total;
     uint32_t item = block_append<REGEN_BLOCK>(&w.counters[0], need, s_warp);
-    if (need && item < total) {
+    bool fresh = need && item < total;
+    if (fresh) {
         if (MULTI) {
             uint32_t r = last_at_most(s_base, s_nreq, item);
             const BatchRequest& R = b.reqs[r];
@@ -197,7 +230,10 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
         }
         live = true;
     }
-    uint32_t q = block_append<REGEN_BLOCK>(&w.counters[1], live, s_warp);
+    // the block's new camera rays first, then its continuing paths: trace warps fetch runs of
+    // coherent camera rays (consecutive work items of neighbouring pixels) apart from the
+    // scattered secondary rays
+    uint32_t q = block_append2<REGEN_BLOCK>(&w.counters[1], fresh, live && !fresh, s_warp2);
     if (live) w.active[q] = s;
 }
 
