@@ -471,6 +471,127 @@ __device__ __forceinline__ bool trace_step_flat(TraceState& st, const DevScene& 
     return !visit_children<STACK>(st, mask, tn, ch, true, stack, stride, err);
 }
 
+// Closest-hit traversal of the flat BVH by a whole warp, for coherent rays (camera rays of
+// neighbouring pixels).  The warp walks one stack of (node or leaf reference, lane mask) entries
+// in shared memory: every lane in an entry's mask tests the node's children (or the leaf's
+// records) against its own ray with its own closest distance so far, and a child is pushed with
+// the mask of the lanes whose ray enters it, farthest first by the entry distances of the lowest
+// such lane.  A lane therefore tests every node and record its ray would test traced alone
+// (and possibly more, with a larger closest distance at the time), so it finds the same closest
+// hit, while each node is fetched once for the warp and all lanes run the same instructions.
+// Every lane of the warp must call it; lanes with !valid take no part.  `stack` holds
+// PACKET_STACK entries; overflow and the iteration limit set ERR_* bits and end the traversal.
+constexpr int PACKET_STACK = 64;
+__device__ __forceinline__ Hit packet_trace_flat(const DevScene& sc, f3 o, f3 d, bool valid, float tmin, float tmax,
+                                                 bool cull, uint2* stack, uint32_t* err) {
+    const uint32_t lane = threadIdx.x & 31u;
+    Hit best;
+    best.hit = 0;
+    best.t = best.u = best.v = 0.0f;
+    best.instance = best.prim = 0u;
+    float tbest = tmax;
+    const NodeRay nr = node_ray(o, d, sc.tlas_bound);
+    RayPre rp = ray_precompute(o, d);
+    uint32_t inst = 0xffffffffu;  // the instance whose object ray `rp` holds
+    bool inst_bad = false;        // that object ray is not finite
+    bool have = valid && finite3(d) && sc.has_tlas != 0u;
+    uint32_t root = __ballot_sync(0xffffffffu, have);
+    int sp = 0;
+    if (root) {
+        if (lane == 0u) stack[0] = make_uint2(0u, root);
+        sp = 1;
+    }
+    __syncwarp();
+    uint32_t iterations = 0u;
+    while (sp > 0) {
+        if (++iterations > TRAVERSAL_ITERATION_LIMIT) {
+            if (lane == 0u) atomicOr(err, ERR_ITERATION_LIMIT);
+            break;
+        }
+        const uint2 e = stack[sp - 1];
+        --sp;
+        __syncwarp();  // every lane has read the entry before lane 0 writes over it
+        const bool mine = (e.y >> lane) & 1u;
+        if (e.x & CHILD_LEAF) {
+            const uint32_t first = leaf_first(e.x), count = leaf_count(e.x);
+            for (uint32_t k = 0; k < count; ++k) {
+                const float4* tr = sc.tris + 3ull * (first + k);
+                float4 a = __ldg(tr + 0), b = __ldg(tr + 1), cc = __ldg(tr + 2);
+                if (mine) {
+                    uint32_t prim = __float_as_uint(a.w), in = __float_as_uint(b.w);
+                    if (in != inst) {
+                        f3 oo, od;
+                        uint32_t mesh;
+                        instance_ray(sc, in, o, d, oo, od, mesh);
+                        inst = in;
+                        inst_bad = !finite3(od);
+                        rp = ray_precompute(oo, od);
+                    }
+                    float t, u, v;
+                    bool better = !inst_bad &&
+                                  intersect_triangle(rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), cull, tmin, tbest,
+                                                     t, u, v) &&
+                                  closer(t, inst, prim, best);
+                    if (better) {
+                        best.hit = 1;
+                        best.t = t;
+                        best.u = u;
+                        best.v = v;
+                        best.instance = inst;
+                        best.prim = prim;
+                        tbest = t;
+                    }
+                }
+            }
+            continue;
+        }
+        float tn[4];
+        uint32_t ch[4];
+        const int hm = node_hits(sc.tlas, e.x, nr, tmin, tbest, tn, ch) & (mine ? 0xf : 0);
+        uint32_t cm[4], any = 0u;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            cm[c] = __ballot_sync(0xffffffffu, (hm >> c) & 1);
+            any |= cm[c];
+        }
+        if (!any) continue;
+        const int rep = __ffs(any) - 1;
+        // the entered children, farthest first (a sorting network on lane-uniform keys; children
+        // no lane enters sort last with key -inf and are not pushed)
+        float key[4];
+        uint2 ent[4];
+        int npush = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float k = __shfl_sync(0xffffffffu, tn[c], rep);
+            key[c] = cm[c] ? k : __int_as_float(0xff800000);
+            ent[c] = make_uint2(ch[c], cm[c]);
+            npush += cm[c] ? 1 : 0;
+        }
+#define TT_DESC(i, j)                                               \
+    {                                                               \
+        bool sw = key[j] > key[i];                                  \
+        float k0 = sw ? key[j] : key[i], k1 = sw ? key[i] : key[j]; \
+        uint2 e0 = sw ? ent[j] : ent[i], e1 = sw ? ent[i] : ent[j]; \
+        key[i] = k0; key[j] = k1; ent[i] = e0; ent[j] = e1;         \
+    }
+        TT_DESC(0, 1) TT_DESC(2, 3) TT_DESC(0, 2) TT_DESC(1, 3) TT_DESC(1, 2)
+#undef TT_DESC
+        if (sp + npush > PACKET_STACK) {
+            if (lane == 0u) atomicOr(err, ERR_STACK_OVERFLOW);
+            break;
+        }
+        if (lane == 0u) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (i < npush) stack[sp + i] = ent[i];
+        }
+        sp += npush;
+        __syncwarp();
+    }
+    return best;
+}
+
 // ---------------------------------------------------------------- compressed 8-wide format
 // Node (80 bytes, five 16-byte loads): origin xyz and, in the fourth word, the biased exponents
 // of the per-axis scales and the internal-slot mask; child base, triangle base and eight meta

@@ -30,11 +30,15 @@ struct RenderParams {
 // Wavefront integrator (wavefront.cu): device pointers of the slot pool and queues.
 constexpr uint32_t HIT_BUCKETS = 4;                // shading queues, one per material bucket
 constexpr uint32_t CACHE_QUEUE = 5 + HIT_BUCKETS;  // counters word: queued radiance-cache queries
-constexpr uint32_t WF_COUNTERS = 6 + HIT_BUCKETS;  // words cleared every iteration: [1, WF_COUNTERS)
+constexpr uint32_t WF_CAMERA = 6 + HIT_BUCKETS;    // counters word: camera rays in the active queue
+constexpr uint32_t WF_CONTINUING = 7 + HIT_BUCKETS;  // counters word: continuing paths in the active queue
+constexpr uint32_t WF_PACKET_HEAD = 8 + HIT_BUCKETS;  // counters word: next camera ray of the packet phase
+constexpr uint32_t WF_COUNTERS = 9 + HIT_BUCKETS;  // words cleared every iteration: [1, WF_COUNTERS)
 constexpr uint32_t CTRL_RECORDS = 14;              // training records of the frame (cleared per frame)
 constexpr uint32_t CTRL_ITERATION = 15;            // iteration count of the device-side loop
 constexpr uint32_t CTRL_WORDS = 16;                // words of WfParams::counters
 constexpr uint32_t CHUNK_WORDS = 14;               // words cleared per sample chunk: [0, CHUNK_WORDS)
+static_assert(WF_COUNTERS <= CHUNK_WORDS && CHUNK_WORDS <= CTRL_RECORDS, "counter words overlap");
 
 struct CacheQuery;
 // A vertex of a training path: its query, the throughput arriving at it and the path radiance
@@ -50,10 +54,11 @@ struct WfParams {
     float4 *org, *dir, *thr, *acc, *pa1, *pa0, *pe;
     uint4* hit;          // shading queues: hit records, HIT_BUCKETS x P
     uint32_t* hslot;     // shading queues: slots, HIT_BUCKETS x P
-    uint32_t* active;
+    uint32_t* active;    // P entries: camera rays from the front, continuing paths from the back
     float4* shadow;
     uint32_t* counters;  // [0] next work item, [1] active paths, [2] shadow rays, [3]/[4] trace queue heads,
-                         // [5 + b] length of shading queue b
+                         // [5 + b] length of shading queue b, [WF_CAMERA] / [WF_CONTINUING] the two parts
+                         // of the active paths
     float4* samples;     // chunk_spp x WH per-sample radiance (band order)
     float4* running;     // WH running per-pixel sums across chunks
     uint32_t P, WH;

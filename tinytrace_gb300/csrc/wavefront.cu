@@ -80,14 +80,16 @@ __device__ __forceinline__ uint32_t block_append(uint32_t* counter, bool pred, u
     return pos;
 }
 
-// Block-aggregated append of two kinds: threads with `first` get consecutive positions at the
-// start of the block's range, threads with `second` the positions after them (one atomicAdd per
-// block on `counter`).  Every thread of the block must call it; `s_warp` holds 2 BLOCK / 32 + 2
-// words.
+// Block-aggregated append to the two parts of the active queue: threads with `camera` get
+// positions from counters[WF_CAMERA] (the block's camera rays consecutive, in thread order),
+// threads with `continuing` from counters[WF_CONTINUING]; counters[1] counts both.  One atomic
+// per block and counter.  Every thread of the block must call it; `s_warp` holds
+// 2 BLOCK / 32 + 3 words.
 template <int BLOCK>
-__device__ __forceinline__ uint32_t block_append2(uint32_t* counter, bool first, bool second, uint32_t* s_warp) {
+__device__ __forceinline__ uint32_t block_append_split(uint32_t* counters, bool camera, bool continuing,
+                                                       uint32_t* s_warp) {
     constexpr int WARPS = BLOCK / 32;
-    uint32_t ma = __ballot_sync(0xffffffffu, first), mb = __ballot_sync(0xffffffffu, second);
+    uint32_t ma = __ballot_sync(0xffffffffu, camera), mb = __ballot_sync(0xffffffffu, continuing);
     int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
     if (lane == 0) {
         s_warp[warp] = (uint32_t)__popc(ma);
@@ -95,20 +97,30 @@ __device__ __forceinline__ uint32_t block_append2(uint32_t* counter, bool first,
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t sum = 0u;
-        for (int k = 0; k < 2 * WARPS; ++k) {  // the first kind's counts, then the second kind's
-            uint32_t c = s_warp[k];
-            s_warp[k] = sum;
-            sum += c;
+        uint32_t sa = 0u, sb = 0u;
+        for (int k = 0; k < WARPS; ++k) {
+            uint32_t ca = s_warp[k], cb = s_warp[WARPS + k];
+            s_warp[k] = sa;
+            s_warp[WARPS + k] = sb;
+            sa += ca;
+            sb += cb;
         }
-        s_warp[2 * WARPS] = sum ? atomicAdd(counter, sum) : 0u;
+        s_warp[2 * WARPS] = sa ? atomicAdd(&counters[WF_CAMERA], sa) : 0u;
+        s_warp[2 * WARPS + 1] = sb ? atomicAdd(&counters[WF_CONTINUING], sb) : 0u;
+        if (sa + sb) atomicAdd(&counters[1], sa + sb);
     }
     __syncthreads();
     uint32_t below = lane_mask_lt();
-    uint32_t pos = s_warp[2 * WARPS] + (first ? s_warp[warp] + (uint32_t)__popc(ma & below)
-                                              : s_warp[WARPS + warp] + (uint32_t)__popc(mb & below));
+    uint32_t pos = camera ? s_warp[2 * WARPS] + s_warp[warp] + (uint32_t)__popc(ma & below)
+                          : s_warp[2 * WARPS + 1] + s_warp[WARPS + warp] + (uint32_t)__popc(mb & below);
     __syncthreads();
     return pos;
+}
+
+// Slot of active-queue entry i when the camera rays (n_camera of them, from the front) and the
+// continuing paths (from the back) are taken as one sequence.
+__device__ __forceinline__ uint32_t active_slot(const WfParams& w, uint32_t n_camera, uint32_t i) {
+    return i < n_camera ? w.active[i] : w.active[w.P - 1u - (i - n_camera)];
 }
 
 // Pixel of band-ordered index t: bands of 8 rows, column-major inside a band, so a warp's 32
@@ -179,7 +191,7 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
                                                                const __grid_constant__ WfParams w,
                                                                const __grid_constant__ BatchParams b) {
     __shared__ uint32_t s_warp[REGEN_BLOCK / 32 + 1];
-    __shared__ uint32_t s_warp2[2 * (REGEN_BLOCK / 32) + 2];
+    __shared__ uint32_t s_warp2[2 * (REGEN_BLOCK / 32) + 3];
     __shared__ uint32_t s_base[MULTI ? BATCH_MAX_REQUESTS : 1];
     __shared__ uint32_t s_next, s_nreq, s_total;
     uint32_t s = blockIdx.x * REGEN_BLOCK + threadIdx.x;
@@ -230,11 +242,12 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
         }
         live = true;
     }
-    // the block's new camera rays first, then its continuing paths: trace warps fetch runs of
-    // coherent camera rays (consecutive work items of neighbouring pixels) apart from the
-    // scattered secondary rays
-    uint32_t q = block_append2<REGEN_BLOCK>(&w.counters[1], fresh, live && !fresh, s_warp2);
-    if (live) w.active[q] = s;
+    // new camera rays to the front of the active queue, continuing paths to its back: trace warps
+    // take runs of coherent camera rays (consecutive work items of neighbouring pixels) apart
+    // from the scattered secondary rays
+    uint32_t q = block_append_split<REGEN_BLOCK>(w.counters, fresh, live && !fresh, s_warp2);
+    if (fresh) w.active[q] = s;
+    else if (live) w.active[w.P - 1u - q] = s;
 }
 
 // Extension and shadow rays: persistent warps with per-lane refill.  Each lane traces one ray
@@ -248,18 +261,71 @@ __global__ void __launch_bounds__(REGEN_BLOCK) wf_regen_kernel(const __grid_cons
 #endif
 constexpr int TR_BLOCK = 128;
 
+// The end of an extension ray (fin): a hit goes to the shading queue of its material bucket,
+// so that the shade stage's warps share lobe sets; a miss adds the sky (integrate.glsl:272-276)
+// and ends the path.  Every lane of the warp must call it.
+__device__ __forceinline__ bool extension_result(const WfParams& w, const DevScene& sc, uint32_t slot, bool fin,
+                                                 const Hit& h) {
+    bool is_hit = fin && h.hit;
+    uint32_t bucket = is_hit ? (uint32_t)__ldg(sc.inst_bucket + h.instance) : 0u;
+    uint32_t pos = 0u;
+#pragma unroll
+    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
+        uint32_t pb = warp_append(&w.counters[5 + b], is_hit && bucket == b);
+        pos = bucket == b ? pb : pos;
+    }
+    if (is_hit) {
+        uint64_t at = (uint64_t)bucket * w.P + pos;
+        w.hslot[at] = slot;
+        w.hit[at] = make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim);
+    } else if (fin) {
+        f3 thr = xyz(w.thr[slot]);
+        float4 a4 = w.acc[slot];
+        f3 acc = xyz(a4);
+        acc += splat(1.0f) * thr;
+        w.acc[slot] = pack(acc, F_TERM | (__float_as_uint(a4.w) & F_TRAIN));
+    }
+    return is_hit;
+}
+
 // MULTI: a shared-pool round; each lane traces in the scene of its ray's request and reports
 // traversal errors to that request's error word.
 template <bool COUNT, bool SHADOW, int ACCEL, int STACK = TRAVERSAL_STACK, bool MULTI = false>
 __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel(const __grid_constant__ RenderParams p,
                                                                 const __grid_constant__ WfParams w,
                                                                 const __grid_constant__ BatchParams b) {
+    // PACKET: the camera rays go first, 32 at a time, through the warp-wide traversal of the flat
+    // BVH; the per-lane loop below then takes the continuing paths only
+    constexpr bool PACKET = !SHADOW && !COUNT && !MULTI && ACCEL == ACCEL_FLAT_ONLY;
     __shared__ uint32_t s_stack[STACK * TR_BLOCK];
+    __shared__ uint2 s_packet[PACKET ? TR_BLOCK / 32 : 1][PACKET ? PACKET_STACK : 1];
     uint32_t* stack = s_stack + threadIdx.x;
     uint32_t lane_req = 0u, lane_scene = 0u;  // MULTI: request and scene of the lane's ray
 #define TT_SC (MULTI ? b.scenes[lane_scene] : p.sc)
 #define TT_ERR (MULTI ? b.reqs[lane_req].err : p.err)
-    const uint32_t n = SHADOW ? w.counters[2] : w.counters[1];
+    const uint32_t n_camera = SHADOW ? 0u : w.counters[WF_CAMERA];
+    if (PACKET) {
+        uint32_t* phead = &w.counters[WF_PACKET_HEAD];
+        uint2* pstack = s_packet[threadIdx.x >> 5];
+        const uint32_t lane = threadIdx.x & 31u;
+        while (true) {
+            uint32_t base = 0u;
+            if (lane == 0u) base = atomicAdd(phead, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n_camera) break;
+            uint32_t i = base + lane;
+            bool valid = i < n_camera;
+            uint32_t pslot = valid ? w.active[i] : 0u;
+            float4 o = valid ? w.org[pslot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float4 d = valid ? w.dir[pslot] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+            Hit h = packet_trace_flat(p.sc, xyz(o), xyz(d), valid, EXTENSION_TMIN, EXTENSION_TMAX, true, pstack, p.err);
+            extension_result(w, p.sc, pslot, valid, h);
+        }
+    }
+    // the per-lane loop's queue: shadow rays, or the active paths (camera rays, unless the packet
+    // phase took them, then the continuing paths)
+    const uint32_t skip = PACKET ? n_camera : 0u;
+    const uint32_t n = SHADOW ? w.counters[2] : w.counters[WF_CAMERA] + w.counters[WF_CONTINUING] - skip;
     uint32_t* head = &w.counters[SHADOW ? 4 : 3];
     TraceState st;
     uint32_t item = 0, slot = 0, light = 0, target_prim = 0;
@@ -290,7 +356,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                         light = __float_as_uint(d.w);
                         org_w = MULTI ? __float_as_uint(w.org[slot].w) : 0u;
                     } else {
-                        slot = w.active[item];
+                        slot = active_slot(w, n_camera, skip + item);
                         o = w.org[slot];
                         d = w.dir[slot];
                         org_w = __float_as_uint(o.w);
@@ -338,28 +404,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                     w.acc[slot] = make_float4(acc.x, acc.y, acc.z, a4.w);
                 }
             } else {
-                // hits go to the compacted shading queue; a miss adds the sky (integrate.glsl:272-276)
-                // one queue per material bucket, so that the shade stage's warps share lobe sets
-                bool is_hit = fin && h.hit;
-                uint32_t bucket = is_hit ? (uint32_t)__ldg(TT_SC.inst_bucket + h.instance) : 0u;
-                uint32_t pos = 0u;
-#pragma unroll
-                for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
-                    uint32_t pb = warp_append(&w.counters[5 + b], is_hit && bucket == b);
-                    pos = bucket == b ? pb : pos;
-                }
-                if (is_hit) {
-                    uint64_t at = (uint64_t)bucket * w.P + pos;
-                    w.hslot[at] = slot;
-                    w.hit[at] = make_uint4(__float_as_uint(h.u), __float_as_uint(h.v), h.instance, h.prim);
-                    if (COUNT) hits++;
-                } else if (fin) {
-                    f3 thr = xyz(w.thr[slot]);
-                    float4 a4 = w.acc[slot];
-                    f3 acc = xyz(a4);
-                    acc += splat(1.0f) * thr;
-                    w.acc[slot] = pack(acc, F_TERM | (__float_as_uint(a4.w) & F_TRAIN));
-                }
+                if (extension_result(w, TT_SC, slot, fin, h) && COUNT) hits++;
             }
             uint32_t am = __ballot_sync(0xffffffffu, active);
             if (COUNT && (threadIdx.x & 31u) == 0u) {
