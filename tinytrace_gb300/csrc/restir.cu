@@ -122,18 +122,12 @@ __device__ __forceinline__ float target_of(const DevScene& sc, const ShadingStat
 // HIT_BUCKETS for a sky pixel (finished here).
 template <bool TEX, int ACCEL>
 __device__ __forceinline__ uint32_t gbuffer_pixel(const RenderParams& p, const RestirParams& rp, Surface* gbuf,
-                                                  float4* gtex, float4* glob, uint32_t x, uint32_t y,
-                                                  uint32_t* s_stack) {
+                                                  float4* gtex, float4* glob, uint32_t x, uint32_t y, uint32_t g,
+                                                  f2 ndc, f3 dir, const Hit& h) {
     const tt_constants& c = p.c;
     const DevScene& sc = p.sc;
-    uint32_t W = c.screen_size[0], H = c.screen_size[1];
-    uint32_t g = jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index));
-    f2 ndc = pixel_ndc(x, y, W, H, g);
-    f3 dir = camera_ray_direction(c, ndc);
+    uint32_t W = c.screen_size[0];
     f3 org = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
-    Counters cnt{0u, 0u, 0u, 0u};
-    Hit h = trace_closest<false, ACCEL>(sc, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true, s_stack + threadIdx.x, RT_BLOCK,
-                                 p.err, cnt);
     Surface s;
     uint64_t i = (uint64_t)y * W + x;
     // surface pixels go to their material bucket's queue for the candidate and shade passes; sky
@@ -173,13 +167,30 @@ template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
                                                                   const __grid_constant__ RestirParams rp,
                                                                   Surface* gbuf, float4* gtex, float4* glob) {
-    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    // the flat BVH: the warp's camera rays (a 16 x 2 pixel strip) traced as one packet
+    constexpr bool PACKET = ACCEL == ACCEL_FLAT_ONLY;
+    __shared__ uint32_t s_stack[PACKET ? 1 : TRAVERSAL_STACK * RT_BLOCK];
+    __shared__ uint2 s_packet[PACKET ? RT_BLOCK / 32 : 1][PACKET ? PACKET_STACK : 1];
     uint32_t x, y;
     const tt_constants& c = p.c;
     uint32_t W = c.screen_size[0], H = c.screen_size[1];
+    const bool inside = pixel_of_thread(c, x, y);
+    uint32_t g = inside ? jenkins_hash((x + y * W) ^ jenkins_hash(c.frame_index)) : 0u;
+    f2 ndc = inside ? pixel_ndc(x, y, W, H, g) : f2{0.0f, 0.0f};
+    f3 dir = inside ? camera_ray_direction(c, ndc) : f3{0.0f, 0.0f, 1.0f};
+    f3 org = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
+    Hit h;
+    if (PACKET) {
+        h = packet_trace_flat(p.sc, org, dir, inside, EXTENSION_TMIN, EXTENSION_TMAX, true, s_packet[threadIdx.x >> 5],
+                              p.err);
+    } else if (inside) {
+        Counters cnt{0u, 0u, 0u, 0u};
+        h = trace_closest<false, ACCEL>(p.sc, org, dir, EXTENSION_TMIN, EXTENSION_TMAX, true, s_stack + threadIdx.x,
+                                        RT_BLOCK, p.err, cnt);
+    }
     // threads outside the image take part in the block's queue append only
     uint32_t bucket = HIT_BUCKETS;
-    if (pixel_of_thread(c, x, y)) bucket = gbuffer_pixel<TEX, ACCEL>(p, rp, gbuf, gtex, glob, x, y, s_stack);
+    if (inside) bucket = gbuffer_pixel<TEX, ACCEL>(p, rp, gbuf, gtex, glob, x, y, g, ndc, dir, h);
     block_queue_append(rp, bucket, y * W + x, (uint64_t)W * H);
 }
 
