@@ -71,10 +71,18 @@ def parse_args():
                    help="server scheduling policy (TT_SERVER_POLICY_*)")
     p.add_argument("--serve-requests", type=int, default=512,
                    help="requests at 0.8 x capacity in the serving sample (a quarter as many at 0.5 x and 1.1 x)")
+    p.add_argument("--primary", default="raster", choices=["raster", "traverse"],
+                   help="camera-ray hits of flat BVH4 scenes: rasterised keys (TT_PRIMARY_RASTER) or traversal")
     p.add_argument("--accel", default="auto", choices=["auto", "flat", "two_level", "wide"],
                    help="acceleration structure (auto = flat up to 2^26 instanced triangles; wide = the flat BVH "
                         "in the compressed 8-wide format)")
     return p.parse_args()
+
+
+def scan_launches(n: int, per_block: int = 4096) -> int:
+    """Kernels of the library's exclusive u32 scan over n values (1024 threads x 4 per block)."""
+    blocks = (n + per_block - 1) // per_block
+    return 1 if blocks <= 1 else 2 + scan_launches(blocks, per_block)
 
 
 # ---------------------------------------------------------------- distributed helpers
@@ -1062,6 +1070,8 @@ def run_ours(a, dist: Dist):
     accel = {"auto": native.TT_ACCEL_AUTO, "flat": native.TT_ACCEL_FLAT, "two_level": native.TT_ACCEL_TWO_LEVEL,
              "wide": native.TT_ACCEL_FLAT_WIDE}
     check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_ACCEL, accel[a.accel]))
+    primary = {"raster": native.TT_PRIMARY_RASTER, "traverse": native.TT_PRIMARY_TRAVERSE}
+    check(r.context.lib.tt_set_option(r.context.handle, native.TT_OPTION_PRIMARY_VISIBILITY, primary[a.primary]))
     r.set_scene(w.scene)
     r.camera = w.camera
     r.set_config(w.config)
@@ -1122,10 +1132,13 @@ def run_ours(a, dist: Dist):
     check(lib.tt_set_option(ctx, native.TT_OPTION_STAGE_TIMING, 0))
     regen_per_step = int(stage_launches[native.TT_STAGE_REGEN]) // a.steps
     reduce_per_step = int(stage_launches[native.TT_STAGE_REDUCE]) // a.steps
+    primary_per_step = int(stage_launches[native.TT_STAGE_PRIMARY]) // a.steps
     if a.host_loop or a.integrator != "wavefront":
         launches_per_step = int(stage_launches.sum()) // a.steps
     else:  # graph loop: regen, control, extend, shade and shadow every iteration, then the reduction
-        launches_per_step = 5 * regen_per_step + reduce_per_step
+        launches_per_step = 5 * regen_per_step + reduce_per_step + primary_per_step
+    if primary_per_step:  # the timed set-up counts once: instance, rectangle, scan and finish kernels
+        launches_per_step += 2 + scan_launches(int(stats.triangle_count) + 1)
 
     # end to end through the public API: render_to_texture into pinned host memory
     host = ctypes.c_void_p()
@@ -1208,6 +1221,7 @@ def run_ours(a, dist: Dist):
                        "parallelism": f"replicas x{dist.world}", "integrator": a.integrator,
                        "accel": {native.TT_ACCEL_FLAT: "flat", native.TT_ACCEL_FLAT_WIDE: "wide"}.get(
                            int(stats.accel), "two_level"),
+                       "primary_visibility": a.primary if stats.accel == native.TT_ACCEL_FLAT else "traverse",
                        "autotune": tuning},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 368, "d2h_bytes_per_step": nbytes,
                     "steps": e2e_steps},

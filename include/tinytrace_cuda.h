@@ -83,6 +83,13 @@ extern "C" {
                                           through an alias table built at scene creation (Vose's method in
                                           double precision); draws: random_uint(count), then one float for
                                           the alias coin; the density uses the light's own probability */
+#define TT_OPTION_PRIMARY_VISIBILITY 11 /* TT_PRIMARY_*: how the wavefront integrator finds camera-ray hits */
+#define TT_PRIMARY_TRAVERSE 0  /* camera rays traverse the BVH like every other ray */
+#define TT_PRIMARY_RASTER 1    /* flat BVH4 scenes (TT_ACCEL_FLAT): before each sample chunk, every triangle is
+                                  bounded on the screen and the chunk's samples in its rectangle are tested
+                                  against it with the traversal's ray/triangle test; the smallest (t, instance,
+                                  primitive) of each sample is the traversal's closest hit, bit for bit
+                                  (default; the other structures traverse) */
 /* acceleration structures (tt_set_option TT_OPTION_ACCEL; tt_scene_stats.accel) */
 #define TT_ACCEL_AUTO 0      /* flat up to 2^26 instanced triangles, two-level above */
 #define TT_ACCEL_FLAT 1      /* one BVH over the world boxes of all (instance, triangle) pairs */
@@ -268,6 +275,7 @@ typedef struct tt_scene_stats {
 #define TT_STAGE_RESTIR_TEMPORAL 10
 #define TT_STAGE_RESTIR_SPATIAL 11
 #define TT_STAGE_RESTIR_SHADE 12
+#define TT_STAGE_PRIMARY 13         /* rasterised primary visibility (TT_PRIMARY_RASTER): bounds and keys */
 #define TT_STAGE_COUNT 16
 typedef struct tt_stage_timings {
     uint64_t ns[TT_STAGE_COUNT];

@@ -52,6 +52,9 @@ pub const TT_LIGHT_VISIBILITY_TRIANGLE: u64 = 1;
 pub const TT_OPTION_LIGHT_SELECTION: u32 = 10;
 pub const TT_LIGHT_SELECTION_UNIFORM: u64 = 0;
 pub const TT_LIGHT_SELECTION_POWER: u64 = 1;
+pub const TT_OPTION_PRIMARY_VISIBILITY: u32 = 11;
+pub const TT_PRIMARY_TRAVERSE: u64 = 0;
+pub const TT_PRIMARY_RASTER: u64 = 1;
 pub const TT_ACCEL_AUTO: u64 = 0;
 pub const TT_ACCEL_FLAT: u64 = 1;
 pub const TT_ACCEL_TWO_LEVEL: u64 = 2;
@@ -81,6 +84,7 @@ pub const TT_STAGE_RESTIR_INITIAL: usize = 9;
 pub const TT_STAGE_RESTIR_TEMPORAL: usize = 10;
 pub const TT_STAGE_RESTIR_SPATIAL: usize = 11;
 pub const TT_STAGE_RESTIR_SHADE: usize = 12;
+pub const TT_STAGE_PRIMARY: usize = 13;
 pub const TT_STAGE_COUNT: usize = 16;
 
 pub const TT_CACHE_WEIGHTS: u32 = 16896;

@@ -18,7 +18,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libtinytrace_cuda.so"
-SOURCES = ["api.cu", "bvh_build.cu", "integrate.cu", "wavefront.cu", "server.cu", "restir.cu", "cache.cu", "ingest.cu"]
+SOURCES = ["api.cu", "bvh_build.cu", "integrate.cu", "wavefront.cu", "primary.cu", "server.cu", "restir.cu", "cache.cu",
+           "ingest.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3",

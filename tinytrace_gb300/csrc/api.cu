@@ -94,6 +94,13 @@ struct WavefrontBuffers {
     uint32_t pixels = 0;
 };
 
+// Rasterised primary visibility (primary.cu): per-record rectangles and pair counts, per-instance
+// bounds and the closest-hit keys of one sample chunk, grown on demand.
+struct PrimaryState {
+    DeviceBuffer key, rect, count, inst, flags;  // flags: total (8 bytes), ok (4 bytes)
+    uint64_t key_items = 0, records = 0, instances = 0;
+};
+
 // ReSTIR DI state kept between frames: two G-buffers and two final reservoir arrays
 // (current and previous frame), the initial and temporal reservoirs, the previous camera.
 struct RestirState {
@@ -153,6 +160,8 @@ struct tt_context {
     bool graphs = true;
     uint32_t light_visibility = TT_LIGHT_VISIBILITY_HASH;  // TT_OPTION_LIGHT_VISIBILITY
     uint32_t light_selection = TT_LIGHT_SELECTION_UNIFORM; // TT_OPTION_LIGHT_SELECTION
+    uint32_t primary = TT_PRIMARY_RASTER;                   // TT_OPTION_PRIMARY_VISIBILITY
+    tt::PrimaryState prim;
     uint32_t refill_lanes = 20;       // TT_OPTION_REFILL_LANES
     uint32_t trace_blocks_per_sm = 0; // TT_OPTION_TRACE_BLOCKS_PER_SM (0 = as many as fit)
     int occupancy_sms = 0, occupancy_blocks = 0;
@@ -176,6 +185,7 @@ void raise_device_error(uint32_t e) {
     if (e & ERR_STACK_OVERFLOW) fail(TT_ERR_OVERFLOW, "traversal stack overflow");
     if (e & ERR_ITERATION_LIMIT) fail(TT_ERR_TIMEOUT, "traversal iteration limit reached");
     if (e & ERR_TENSOR_WAIT) fail(TT_ERR_TIMEOUT, "radiance-cache tensor-core wait limit reached");
+    if (e & ERR_PRIMARY_MISMATCH) fail(TT_ERR_DEVICE, "a rasterised camera-ray hit failed its ray/triangle test");
     if (e) fail(TT_ERR_DEVICE, "unknown device error bits " + std::to_string(e));
 }
 namespace {
@@ -568,6 +578,35 @@ static WfParams wavefront_buffers(tt_context* ctx, const tt_constants& c) {
     return w;
 }
 
+// Rasterised primary visibility buffers for a frame of `c` on scene `sc` (grown on demand).
+static void primary_buffers(tt_context* ctx, const tt_constants& c, const DevScene& sc, uint32_t chunk_spp,
+                            PrimaryParams& v) {
+    PrimaryState& S = ctx->prim;
+    uint64_t items = (uint64_t)c.screen_size[0] * c.screen_size[1] * chunk_spp;
+    if (items > S.key_items) {
+        S.key.alloc(8ull * items);
+        S.key_items = items;
+    }
+    if ((uint64_t)sc.tri_count + 1 > S.records) {
+        S.rect.alloc(16ull * sc.tri_count);
+        S.count.alloc(4ull * (sc.tri_count + 1ull));
+        S.records = (uint64_t)sc.tri_count + 1;
+    }
+    if (sc.instance_count > S.instances) {
+        S.inst.alloc(sizeof(PrimaryInstance) * (uint64_t)sc.instance_count);
+        S.instances = sc.instance_count;
+    }
+    if (!S.flags.ptr) S.flags.alloc(16);
+    v.key = S.key.as<unsigned long long>();
+    v.rect = S.rect.as<float4>();
+    v.count = S.count.as<uint32_t>();
+    v.total = S.flags.as<unsigned long long>();
+    v.ok = reinterpret_cast<uint32_t*>(S.flags.as<unsigned char>() + 8);
+    v.inst = S.inst.as<PrimaryInstance>();
+    v.records = sc.tri_count;
+    v.raster_blocks = std::max(1, ctx->occupancy_sms) * 8;
+}
+
 namespace tt {
 void set_last_error(const std::string& message) { g_last_error = message; }
 DevScene scene_view(tt_context* ctx, tt_handle scene) {
@@ -708,14 +747,30 @@ static void render_impl(tt_context* ctx, tt_handle scene, const tt_constants* c,
     if (!s->dev.textured) w.ndc_mip = nullptr;
     bool cached = wavefront && ctx->cache.enabled && !counted;
     if (cached) cache_frame_buffers(ctx, *c, s->dev, w);
+    // camera rays from rasterised keys: flat BVH4 scenes with a regular camera (instrumented
+    // renders too, so that their counters describe the same work)
+    PrimaryParams pv{};
+    const PrimaryParams* prim = nullptr;
+    if (wavefront && ctx->primary == TT_PRIMARY_RASTER && s->dev.tri_record && s->dev.tri_count > 0 &&
+        primary_camera(*c, pv)) {
+        primary_buffers(ctx, *c, s->dev, w.chunk_spp, pv);
+        w.vis = pv.key;
+        w.vis_ok = pv.ok;
+        prim = &pv;
+    }
     StageTimer* timer = begin_stage_timing(ctx);
     check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
+    if (prim) {
+        stage_begin(timer, TT_STAGE_PRIMARY, ctx->stream);
+        primary_setup(p, pv, ctx->stream);
+        stage_end(timer, ctx->stream);
+    }
     if (wavefront && ctx->graphs && !timer) {
         for (auto& cs : ctx->capture)
             if (!cs) check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
-        render_wavefront_graph(p, w, counted, ctx->stream, ctx->capture[0], ctx->capture[1]);
+        render_wavefront_graph(p, w, counted, ctx->stream, ctx->capture[0], ctx->capture[1], prim);
     } else if (wavefront) {
-        render_wavefront(p, w, ctx->err_host + 1, counted, ctx->stream, timer);
+        render_wavefront(p, w, ctx->err_host + 1, counted, ctx->stream, timer, prim);
     } else {
         stage_begin(timer, TT_STAGE_MEGAKERNEL, ctx->stream);
         launch_integrate(p, counted, ctx->stream);
@@ -981,6 +1036,9 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             ds.tlas_bound = s->bvh.flat_bound;
             ds.flat = 1u;
             ds.wide = wide ? 1u : 0u;
+            ds.tri_base = wide ? nullptr : s->bvh.flat_tri_base.as<uint32_t>();
+            ds.tri_record = wide ? nullptr : s->bvh.flat_tri_record.as<uint32_t>();
+            ds.tri_count = wide ? 0u : (uint32_t)s->bvh.flat_tri_count;
             stt.triangle_count = s->bvh.flat_tri_count;
             stt.tlas_nodes = s->bvh.flat_nodes;
             stt.tlas_levels = s->bvh.flat_levels;
@@ -1198,6 +1256,9 @@ int32_t tt_set_option(tt_context* ctx, uint32_t option, uint64_t value) {
         } else if (option == TT_OPTION_LIGHT_SELECTION) {
             require(value == TT_LIGHT_SELECTION_UNIFORM || value == TT_LIGHT_SELECTION_POWER, "unknown light selection");
             ctx->light_selection = (uint32_t)value;
+        } else if (option == TT_OPTION_PRIMARY_VISIBILITY) {
+            require(value == TT_PRIMARY_TRAVERSE || value == TT_PRIMARY_RASTER, "unknown primary visibility");
+            ctx->primary = (uint32_t)value;
         } else if (option == TT_OPTION_RADIANCE_CACHE) {
             require(value <= 1, "radiance cache is 0 or 1");
             ctx->cache.enabled = value != 0;

@@ -672,6 +672,14 @@ __global__ void gather_records_kernel(const float4* in, const uint32_t* order, u
     out[3ull * i + 2] = in[3ull * s + 2];
 }
 
+// tri_record[tri_base[instance] + primitive] = record, over the records in leaf order.
+__global__ void tri_record_kernel(const float4* recs, const uint32_t* tri_base, uint32_t n, uint32_t* tri_record) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t prim = __float_as_uint(recs[3ull * i].w), inst = __float_as_uint(recs[3ull * i + 1].w);
+    tri_record[tri_base[inst] + prim] = i;
+}
+
 __global__ void segment_boxes_kernel(const int* roots, uint32_t segs, const float4* blo,
                                      const float4* bhi, float4* slo, float4* shi) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1108,6 +1116,12 @@ static void build_flat(const BuildInput& in, cudaStream_t stream, int leaf_max, 
     out.flat_levels = b.levels;
     out.flat_level_start = b.level_start;
     gather_records_kernel<<<grid_for(n, 256), 256, 0, stream>>>(recs, b.order, n, out.flat_tris.as<float4>());
+    out.flat_tri_base.alloc(4ull * (in.instance_count + 1));
+    out.flat_tri_record.alloc(4ull * n);
+    check_cuda(cudaMemcpyAsync(out.flat_tri_base.ptr, base.data(), 4ull * (in.instance_count + 1),
+                               cudaMemcpyHostToDevice, stream), "triangle bases");
+    tri_record_kernel<<<grid_for(n, 256), 256, 0, stream>>>(out.flat_tris.as<float4>(), out.flat_tri_base.as<uint32_t>(),
+                                                            n, out.flat_tri_record.as<uint32_t>());
     out.flat_bound = root_bound(b.roots, b.blo, b.bhi, stream);
     check_cuda(cudaStreamSynchronize(stream), "bvh build");
     check_cuda(cudaGetLastError(), "bvh build kernels");

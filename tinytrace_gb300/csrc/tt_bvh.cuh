@@ -53,6 +53,7 @@ constexpr uint32_t TRAVERSAL_ITERATION_LIMIT = 1u << 24;
 constexpr uint32_t ERR_STACK_OVERFLOW = 1u;
 constexpr uint32_t ERR_ITERATION_LIMIT = 2u;
 constexpr uint32_t ERR_TENSOR_WAIT = 4u;  // a tensor-core completion wait ran out (cache queries)
+constexpr uint32_t ERR_PRIMARY_MISMATCH = 8u;  // a camera ray's rasterised closest hit failed its own ray test
 
 TT_HD uint32_t leaf_first(uint32_t r) { return r & 0x07ffffffu; }
 TT_HD uint32_t leaf_count(uint32_t r) { return ((r >> 27) & 0xfu) + 1u; }
@@ -93,6 +94,12 @@ struct DevScene {
     uint32_t light_power;        // TT_LIGHT_SELECTION_POWER: lights picked through `light_alias`
     const float4* light_alias;   // per emissive triangle: (keep probability, alias index bits, pdf, 0)
     const float4* light_rec;     // per emissive triangle: LIGHT_RECORD float4 (light_records_kernel)
+    // flat BVH4 scenes: the scene triangle index of (instance, primitive) is tri_base[instance] +
+    // primitive (so it orders hits as the closest-hit tie-break does), tri_record maps it to its
+    // record in `tris`; null for the other structures
+    const uint32_t* tri_base;    // instance_count + 1 entries
+    const uint32_t* tri_record;  // tri_count entries
+    uint32_t tri_count;          // records in `tris` (flat BVH4 scenes)
 };
 // A light record: what light sampling derives from an emissive triangle, computed once per
 // scene and instance update.  float4 0..2: world vertices p0, p1, p2 with w = area, instance

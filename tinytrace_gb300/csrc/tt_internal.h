@@ -56,6 +56,9 @@ struct BvhResult {
     uint64_t flat_nodes = 0, flat_tri_count = 0;
     uint32_t flat_levels = 0;
     float flat_bound = 0.0f;      // max |coordinate| of the triangle world boxes
+    // flat BVH4 only: first scene triangle index of each instance (instance_count + 1 entries)
+    // and the record of each scene triangle index (flat_tri_count entries)
+    DeviceBuffer flat_tri_base, flat_tri_record;
 };
 
 struct BuildInput {

@@ -81,6 +81,10 @@ struct WfParams {
     // textured scenes: per slot, the primary ray's ndc (written by regen) and then the mip
     // level of the path (x, written at bounce 0); null without textures
     float2* ndc_mip;
+    // rasterised primary visibility (primary.cu): the closest-hit key of every camera ray of the
+    // chunk, indexed by work item; null, or *vis_ok == 0, when the camera rays are traversed
+    const unsigned long long* vis;
+    const uint32_t* vis_ok;
 };
 // SM count and resident blocks per SM of the persistent trace kernel.
 void trace_occupancy(int* sms, int* blocks_per_sm);
@@ -151,15 +155,52 @@ inline void stage_end(StageTimer* t, cudaStream_t st) {
     t->open = false;
 }
 
+// Primary visibility by rasterisation (primary.cu).  Every camera ray of a frame starts at the
+// camera position, so the triangles it can hit are found the way a rasteriser finds them: each
+// triangle record of a flat BVH4 scene is bounded on the screen (its projection, widened by a
+// margin that covers the rounding of the camera rays and of the ray/triangle test, clipped
+// where no camera ray can reach it, back faces dropped), and every sample of every pixel in that
+// rectangle is tested against it with the traversal's own ray/triangle test.  The smallest
+// (t, scene triangle index) key of each sample is its closest hit: the traversal's result, since
+// that key orders hits exactly as the closest-hit rule does (smallest t, then the smaller
+// (instance, primitive)).  The extension kernel then rebuilds each camera ray's hit from its key
+// with one ray/triangle test instead of a traversal.
+struct PrimaryInstance {
+    double oo[3];    // the camera position in object space, as instance_ray computes it (float)
+    double ci[9];    // (object-from-world 3x3 * B)^-1, row-major: object-space offset -> lambda (ndc, 1)
+    double margin;   // screen margin in pixels (grows with the matrix's condition number)
+    uint32_t ok;     // 0: no bound (the instance's records cover the whole screen)
+};
+struct PrimaryParams {
+    unsigned long long* key;     // chunk_spp x WH keys (t bits << 32 | scene triangle index), ~0: no hit
+    float4* rect;                // per record: pixel-position rectangle x0, y0, x1, y1 (x0 > x1: none)
+    uint32_t* count;             // records + 1: pixels of each rectangle, then their exclusive prefix
+    unsigned long long* total;   // pixel-record pairs of the frame
+    uint32_t* ok;                // 1 when the keys are complete (the extension kernel reads them)
+    PrimaryInstance* inst;       // per instance
+    double B[9];                 // row-major: (ndc.x, ndc.y, 1) -> world direction of the camera ray
+    double lambda_clip;          // no camera ray hits where lambda < lambda_clip
+    double pixel_scale;          // pixels per radian of direction error, an upper bound
+    uint32_t records;
+    int raster_blocks;           // grid of the persistent raster kernel
+};
+// Camera terms of `c` for primary visibility; false when the camera's ray map is singular.
+bool primary_camera(const tt_constants& c, PrimaryParams& v);
+// Per frame, on `st`: instance bounds, record rectangles, their prefix and the ok flag.
+void primary_setup(const RenderParams& p, const PrimaryParams& v, cudaStream_t st);
+// Per sample chunk (w.chunk_sample0, w.chunk_spp, w.chunk_jump): clears and fills the keys.
+void primary_chunk(const RenderParams& p, const PrimaryParams& v, const WfParams& w, cudaStream_t st);
+
 // Renders with the wavefront integrator; w.chunk_spp is the largest chunk of samples the
-// buffers hold.  Synchronises `st` once per iteration to read the active-path count.
+// buffers hold.  Synchronises `st` once per iteration to read the active-path count.  `prim`:
+// rasterised primary visibility (w.vis points to its keys), or null.
 void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
-                      StageTimer* timer);
+                      StageTimer* timer, const PrimaryParams* prim);
 // The same loop with no host synchronisation: each sample chunk's iterations run as a
 // device-side while loop (a conditional node) of one CUDA graph, captured on `cs` and
 // `body_stream` and launched on `st`.
 void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cudaStream_t st, cudaStream_t cs,
-                            cudaStream_t body_stream);
+                            cudaStream_t body_stream, const PrimaryParams* prim);
 void launch_integrate(const RenderParams& p, bool counted, cudaStream_t st);
 
 // ReSTIR DI (restir.cu): the previous frame's camera and the frame's buffers.

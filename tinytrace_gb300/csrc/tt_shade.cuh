@@ -14,11 +14,14 @@ constexpr float EXTENSION_TMIN = 1.0e-3f, EXTENSION_TMAX = 1000.0f;  // integrat
 constexpr float SHADOW_TMIN = 1.0e-3f, SHADOW_TMAX = 10000.0f;       // integrate.glsl:168-172
 
 // integrate.glsl:129-132 (the two draws come from the pixel generator)
+TT_HD f2 pixel_ndc_from_draws(uint32_t px, uint32_t py, uint32_t W, uint32_t H, float ox, float oy) {
+    f2 off = f2{ox - 0.5f, oy - 0.5f};
+    return f2{(((float)px + off.x) / (float)W) * 2.0f - 1.0f, (((float)py + off.y) / (float)H) * 2.0f - 1.0f};
+}
 TT_HD f2 pixel_ndc(uint32_t px, uint32_t py, uint32_t W, uint32_t H, uint32_t& pixel_gen) {
     float ox = random_float(pixel_gen);
     float oy = random_float(pixel_gen);
-    f2 off = f2{ox - 0.5f, oy - 0.5f};
-    return f2{(((float)px + off.x) / (float)W) * 2.0f - 1.0f, (((float)py + off.y) / (float)H) * 2.0f - 1.0f};
+    return pixel_ndc_from_draws(px, py, W, H, ox, oy);
 }
 
 // integrate.glsl:17-20

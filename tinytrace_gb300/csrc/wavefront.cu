@@ -288,15 +288,55 @@ __device__ __forceinline__ bool extension_result(const WfParams& w, const DevSce
     return is_hit;
 }
 
+// The closest hit of the camera ray in `slot` from its rasterised key (primary.cu): the record
+// of the key's scene triangle, tested with the ray's own set-up, gives the t, u, v the traversal
+// would report.  A key that this test does not confirm sets ERR_PRIMARY_MISMATCH.
+__device__ __forceinline__ Hit primary_hit(const WfParams& w, const DevScene& sc, uint32_t slot, bool valid,
+                                           uint32_t* err) {
+    Hit h;
+    h.hit = 0;
+    h.t = h.u = h.v = 0.0f;
+    h.instance = h.prim = 0u;
+    if (!valid) return h;
+    const unsigned long long key = w.vis[__float_as_uint(w.thr[slot].w)];
+    if (key == ~0ull) return h;
+    const uint32_t rec = __ldg(sc.tri_record + (uint32_t)key);
+    const float4 a = __ldg(sc.tris + 3ull * rec), b = __ldg(sc.tris + 3ull * rec + 1), c = __ldg(sc.tris + 3ull * rec + 2);
+    const uint32_t inst = __float_as_uint(b.w);
+    f3 oo, od;
+    uint32_t mesh;
+    instance_ray(sc, inst, xyz(w.org[slot]), xyz(w.dir[slot]), oo, od, mesh);
+    RayPre rp = ray_precompute(oo, od);
+    float t, u, v;
+    bool ok = finite3(od) &&
+              intersect_triangle(rp, tri_vertex(a), tri_vertex(b), tri_vertex(c), true, EXTENSION_TMIN, EXTENSION_TMAX,
+                                 t, u, v) &&
+              __float_as_uint(t) == (uint32_t)(key >> 32);
+    if (!ok) {
+        atomicOr(err, ERR_PRIMARY_MISMATCH);
+        return h;
+    }
+    h.hit = 1;
+    h.t = t;
+    h.u = u;
+    h.v = v;
+    h.instance = inst;
+    h.prim = __float_as_uint(a.w);
+    return h;
+}
+
 // MULTI: a shared-pool round; each lane traces in the scene of its ray's request and reports
 // traversal errors to that request's error word.
 template <bool COUNT, bool SHADOW, int ACCEL, int STACK = TRAVERSAL_STACK, bool MULTI = false>
 __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel(const __grid_constant__ RenderParams p,
                                                                 const __grid_constant__ WfParams w,
                                                                 const __grid_constant__ BatchParams b) {
-    // PACKET: the camera rays go first, 32 at a time, through the warp-wide traversal of the flat
-    // BVH; the per-lane loop below then takes the continuing paths only
-    constexpr bool PACKET = !SHADOW && !COUNT && !MULTI && ACCEL == ACCEL_FLAT_ONLY;
+    // CAMERA: the camera rays go first, 32 at a time per warp: from their rasterised closest hits
+    // when the chunk has them (w.vis), else, in the uninstrumented kernel (PACKET), through the
+    // warp-wide traversal of the flat BVH; the per-lane loop below then takes the continuing
+    // paths only
+    constexpr bool CAMERA = !SHADOW && !MULTI && ACCEL == ACCEL_FLAT_ONLY;
+    constexpr bool PACKET = CAMERA && !COUNT;
     __shared__ uint32_t s_stack[STACK * TR_BLOCK];
     __shared__ uint2 s_packet[PACKET ? TR_BLOCK / 32 : 1][PACKET ? PACKET_STACK : 1];
     uint32_t* stack = s_stack + threadIdx.x;
@@ -304,9 +344,12 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
 #define TT_SC (MULTI ? b.scenes[lane_scene] : p.sc)
 #define TT_ERR (MULTI ? b.reqs[lane_req].err : p.err)
     const uint32_t n_camera = SHADOW ? 0u : w.counters[WF_CAMERA];
-    if (PACKET) {
+    Counters cnt{0u, 0u, 0u, 0u};
+    uint32_t rays = 0, hits = 0;
+    const bool raster = CAMERA && w.vis != nullptr && *w.vis_ok != 0u;
+    const bool camera_phase = raster || PACKET;
+    if (CAMERA && camera_phase) {
         uint32_t* phead = &w.counters[WF_PACKET_HEAD];
-        uint2* pstack = s_packet[threadIdx.x >> 5];
         const uint32_t lane = threadIdx.x & 31u;
         while (true) {
             uint32_t base = 0u;
@@ -316,15 +359,26 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
             uint32_t i = base + lane;
             bool valid = i < n_camera;
             uint32_t pslot = valid ? w.active[i] : 0u;
-            float4 o = valid ? w.org[pslot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            float4 d = valid ? w.dir[pslot] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-            Hit h = packet_trace_flat(p.sc, xyz(o), xyz(d), valid, EXTENSION_TMIN, EXTENSION_TMAX, true, pstack, p.err);
-            extension_result(w, p.sc, pslot, valid, h);
+            Hit h{};
+            if (raster) {
+                h = primary_hit(w, p.sc, pslot, valid, p.err);
+                if (COUNT && valid) {  // one record test and one object-ray set-up per hit
+                    rays++;
+                    cnt.triangles += h.hit ? 1u : 0u;
+                    cnt.instances += h.hit ? 1u : 0u;
+                }
+            } else if constexpr (PACKET) {
+                float4 o = valid ? w.org[pslot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                float4 d = valid ? w.dir[pslot] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+                h = packet_trace_flat(p.sc, xyz(o), xyz(d), valid, EXTENSION_TMIN, EXTENSION_TMAX, true,
+                                      s_packet[threadIdx.x >> 5], p.err);
+            }
+            if (extension_result(w, p.sc, pslot, valid, h) && COUNT) hits++;
         }
     }
-    // the per-lane loop's queue: shadow rays, or the active paths (camera rays, unless the packet
+    // the per-lane loop's queue: shadow rays, or the active paths (camera rays, unless the camera
     // phase took them, then the continuing paths)
-    const uint32_t skip = PACKET ? n_camera : 0u;
+    const uint32_t skip = camera_phase ? n_camera : 0u;
     const uint32_t n = SHADOW ? w.counters[2] : w.counters[WF_CAMERA] + w.counters[WF_CONTINUING] - skip;
     uint32_t* head = &w.counters[SHADOW ? 4 : 3];
     TraceState st;
@@ -332,8 +386,6 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
     bool active = false;
     bool seeded = false;  // shadow ray seeded with its light triangle: any change of the closest hit occludes
     bool drained = false;  // warp-uniform: the queue has no more rays
-    Counters cnt{0u, 0u, 0u, 0u};
-    uint32_t rays = 0, hits = 0;
     unsigned long long warp_steps = 0, lane_steps = 0;  // step-level lane occupancy (instrumented kernel)
     while (true) {
         if (!drained) {
@@ -717,7 +769,7 @@ void trace_occupancy(int* sms, int* blocks_per_sm) {
 }
 
 void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cudaStream_t st, cudaStream_t cs,
-                            cudaStream_t body_stream) {
+                            cudaStream_t body_stream, const PrimaryParams* prim) {
     const tt_constants& c = p.c;
     uint32_t WH = c.screen_size[0] * c.screen_size[1];
     uint32_t spp = c.sample_count;
@@ -738,6 +790,7 @@ void render_wavefront_graph(const RenderParams& p, WfParams w, bool counted, cud
         w.chunk_items = WH * w.chunk_spp;
         check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CHUNK_WORDS, cs), "memset");
         check_cuda(cudaMemsetAsync(w.counters + CTRL_ITERATION, 0, 4, cs), "memset");
+        if (prim) primary_chunk(p, *prim, w, cs);
         // while (paths are live) { regen; extend; shade; shadow }
         cudaStreamCaptureStatus status;
         cudaGraph_t cg = nullptr;
@@ -852,7 +905,7 @@ cudaGraphExec_t build_batch_graph(const WfParams& w, const BatchParams& b, bool 
 }
 
 void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, bool counted, cudaStream_t st,
-                      StageTimer* timer) {
+                      StageTimer* timer, const PrimaryParams* prim) {
     const tt_constants& c = p.c;
     uint32_t WH = c.screen_size[0] * c.screen_size[1];
     uint32_t spp = c.sample_count;
@@ -868,6 +921,11 @@ void render_wavefront(const RenderParams& p, WfParams w, uint32_t* host_count, b
         w.chunk_spp = std::min(max_chunk, spp - s0);
         w.chunk_items = WH * w.chunk_spp;
         check_cuda(cudaMemsetAsync(w.counters, 0, 4ull * CHUNK_WORDS, st), "memset");
+        if (prim) {
+            stage_begin(timer, TT_STAGE_PRIMARY, st);
+            primary_chunk(p, *prim, w, st);
+            stage_end(timer, st);
+        }
         while (true) {
             check_cuda(cudaMemsetAsync(w.counters + 1, 0, 4ull * (WF_COUNTERS - 1), st), "memset");
             stage_begin(timer, TT_STAGE_REGEN, st);

@@ -41,6 +41,9 @@ TT_LIGHT_VISIBILITY_TRIANGLE = 1
 TT_OPTION_LIGHT_SELECTION = 10
 TT_LIGHT_SELECTION_UNIFORM = 0
 TT_LIGHT_SELECTION_POWER = 1
+TT_OPTION_PRIMARY_VISIBILITY = 11
+TT_PRIMARY_TRAVERSE = 0
+TT_PRIMARY_RASTER = 1
 TT_TEXTURE_BC1_SRGB = 1
 TT_TEXTURE_BC5_UNORM = 2
 TT_TEXTURE_R8_UNORM = 3
@@ -82,10 +85,11 @@ TT_STAGE_RESTIR_INITIAL = 9
 TT_STAGE_RESTIR_TEMPORAL = 10
 TT_STAGE_RESTIR_SPATIAL = 11
 TT_STAGE_RESTIR_SHADE = 12
+TT_STAGE_PRIMARY = 13
 TT_STAGE_COUNT = 16
 TT_STAGE_CACHE_TRAIN = 7
 STAGE_NAMES = ("regen", "extend", "shade", "shadow", "reduce", "megakernel", "cache", "cache_train",
-               "restir_gbuffer", "restir_initial", "restir_temporal", "restir_spatial", "restir_shade")
+               "restir_gbuffer", "restir_initial", "restir_temporal", "restir_spatial", "restir_shade", "primary")
 
 # ---------------------------------------------------------------- byte layouts (numpy)
 MATERIAL_CONSTANT_FIELDS = [
