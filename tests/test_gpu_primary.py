@@ -140,3 +140,36 @@ def test_primary_option_rejects_unknown(gpu_context):
     lib, hd = gpu_context.lib, gpu_context.handle
     assert lib.tt_set_option(hd, native.TT_OPTION_PRIMARY_VISIBILITY, 2) == native.TT_ERR_INVALID_ARGUMENT
     check(lib.tt_set_option(hd, native.TT_OPTION_PRIMARY_VISIBILITY, native.TT_PRIMARY_RASTER))
+
+
+def test_primary_raster_restir_frames(gpu_context):
+    """ReSTIR's G-buffer pass takes its camera-ray hits from one sample of rasterised keys per
+    pixel: images and reservoirs equal the traversed frames and the oracle's, with the camera
+    moving inside the Cornell box (walls crossing the camera plane)."""
+    extent = (48, 36)
+    frames = {}
+    for mode in ("raster", "traverse"):
+        r = Renderer(extent)
+        lib, hd = r.context.lib, r.context.handle
+        check(lib.tt_set_option(hd, native.TT_OPTION_ACCEL, native.TT_ACCEL_FLAT))
+        check(lib.tt_set_option(hd, native.TT_OPTION_PRIMARY_VISIBILITY, MODES[mode]))
+        r.set_scene(scenes.cornell_box())
+        r.set_config(Config(bounce_count=1, sample_count=1))
+        orc = oracle.OracleScene(r.scene_arrays)
+        R = oracle.OracleRestir(orc, *extent)
+        cpu = np.zeros((extent[1], extent[0], 4), np.float32)
+        out = []
+        for f in range(4):
+            r.camera = Camera.looking_at((0.1 * f, 1.0, 0.6), (0.3, 0.8 - 0.05 * f, -1.0))
+            c = make_constants(r.camera, extent, r.config(), r.context.frame_index(), r.accumulated_frame_count)
+            r.render_restir_to_target()
+            gpu = r.context.download(r.render_target, *extent)
+            R.frame(c, cpu)
+            assert_same_bits(gpu, cpu, f"restir {mode} frame {f} image")
+            assert_same_bits(r.restir_reservoirs(), R.reservoirs(), f"restir {mode} frame {f} reservoirs")
+            out.append(gpu.copy())
+            r.present()
+        frames[mode] = out
+        r.close()
+    for f, (a, b) in enumerate(zip(frames["raster"], frames["traverse"])):
+        assert_same_bits(a, b, f"restir frame {f}: raster vs traversal")

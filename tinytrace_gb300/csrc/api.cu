@@ -97,7 +97,7 @@ struct WavefrontBuffers {
 // Rasterised primary visibility (primary.cu): per-record rectangles and pair counts, per-instance
 // bounds and the closest-hit keys of one sample chunk, grown on demand.
 struct PrimaryState {
-    DeviceBuffer key, rect, count, inst, flags;  // flags: total (8 bytes), ok (4 bytes)
+    DeviceBuffer key, rect, edge, count, inst, flags;  // flags: total (8 bytes), ok (4 bytes)
     uint64_t key_items = 0, records = 0, instances = 0;
 };
 
@@ -589,6 +589,7 @@ static void primary_buffers(tt_context* ctx, const tt_constants& c, const DevSce
     }
     if ((uint64_t)sc.tri_count + 1 > S.records) {
         S.rect.alloc(16ull * sc.tri_count);
+        S.edge.alloc(48ull * sc.tri_count);
         S.count.alloc(4ull * (sc.tri_count + 1ull));
         S.records = (uint64_t)sc.tri_count + 1;
     }
@@ -599,6 +600,7 @@ static void primary_buffers(tt_context* ctx, const tt_constants& c, const DevSce
     if (!S.flags.ptr) S.flags.alloc(16);
     v.key = S.key.as<unsigned long long>();
     v.rect = S.rect.as<float4>();
+    v.edge = S.edge.as<float4>();
     v.count = S.count.as<uint32_t>();
     v.total = S.flags.as<unsigned long long>();
     v.ok = reinterpret_cast<uint32_t*>(S.flags.as<unsigned char>() + 8);
@@ -1405,9 +1407,28 @@ int32_t tt_render_restir(tt_context* ctx, tt_handle scene, const tt_constants* c
         rp.neighbours = R.config.spatial_neighbours;
         rp.m_cap = R.config.temporal_m_cap * (float)R.config.candidates;
         rp.radius = R.config.spatial_radius;
+        // the camera rays' hits from rasterised keys (one sample per pixel: the path tracer's
+        // first sample) on flat BVH4 scenes
+        PrimaryParams pv{};
+        bool raster = ctx->primary == TT_PRIMARY_RASTER && s->dev.tri_record && s->dev.tri_count > 0 &&
+                      primary_camera(*constants, pv);
+        if (raster) {
+            if (ctx->occupancy_sms == 0) trace_occupancy(&ctx->occupancy_sms, &ctx->occupancy_blocks);
+            primary_buffers(ctx, *constants, s->dev, 1u, pv);
+        }
+        rp.vis = raster ? pv.key : nullptr;
+        rp.vis_ok = raster ? pv.ok : nullptr;
         arm_error_word(ctx);
         StageTimer* timer = begin_stage_timing(ctx);
         check_cuda(cudaEventRecord(ctx->ev_integrate[0], ctx->stream), "event");
+        if (raster) {
+            WfParams chunk{};  // sample 0 of the frame: chunk_sample0 = 0, one sample
+            chunk.chunk_spp = 1u;
+            stage_begin(timer, TT_STAGE_PRIMARY, ctx->stream);
+            primary_setup(p, pv, ctx->stream);
+            primary_chunk(p, pv, chunk, ctx->stream);
+            stage_end(timer, ctx->stream);
+        }
         render_restir(p, rp, ctx->stream, timer);
         check_cuda(cudaGetLastError(), "restir launch");
         check_cuda(cudaEventRecord(ctx->ev_integrate[1], ctx->stream), "event");

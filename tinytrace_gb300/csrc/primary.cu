@@ -40,10 +40,16 @@ namespace {
 
 constexpr double BASE_MARGIN_PX = 0.05;
 constexpr double COND_MARGIN = 2.0e-6;
-constexpr double BACKFACE_COS = 1.0e-4;
-constexpr double MAX_PROJECTION_COND = 1.0e8;  // beyond this the double projection is not trusted
+constexpr double PROJ_MARGIN = 2.0e-6;  // float bound: per unit condition number of C, per pixel of width
+constexpr float BACKFACE_COS = 1.0e-3f;
+constexpr float EDGE_EVAL_MARGIN = 1.0e-3f;  // pixels: rounding of an edge function's evaluation
+constexpr float EDGE_MAX_COORD = 1.0e5f;     // edge functions only for vertices within this many pixels
+constexpr double MAX_PROJECTION_COND = 1.0e6;  // beyond this the float bound is not used
 constexpr unsigned long long PAIR_LIMIT = 1ull << 31;
 constexpr int RASTER_BLOCK = 256;
+constexpr int RASTER_WARPS = RASTER_BLOCK / 32;
+constexpr int SAMPLE_GROUP = 8;
+constexpr int QUEUE_CAP = 32 + 32 * SAMPLE_GROUP;  // < 32 left over + one group's entries
 
 __host__ __device__ inline void mul3(const double* a, const double* b, double* out) {  // row-major
     for (int i = 0; i < 3; ++i)
@@ -73,12 +79,11 @@ __host__ __device__ inline double frobenius(const double* m) {
     return sqrt(s);
 }
 
-// Index of pixel (x, y) in the band order of the integrator's work items (the inverse of
-// band_pixel: bands of 8 rows, column by column within a band).
-__device__ __forceinline__ uint32_t band_index(uint32_t x, uint32_t y, uint32_t W, uint32_t H) {
-    uint32_t band = y / 8u;
-    uint32_t rows = min(8u, H - 8u * band);
-    return band * 8u * W + x * rows + (y - 8u * band);
+__device__ __forceinline__ f3 xyz3(float4 v) { return f3{v.x, v.y, v.z}; }
+__device__ __forceinline__ uint32_t lanes_below() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
 }
 
 // The pixels whose samples can fall in the pixel-position rectangle [lo, hi] (pixel p covers
@@ -88,8 +93,13 @@ __device__ __forceinline__ void pixel_span(float lo, float hi, uint32_t n, int& 
     b = min((int)n - 1, (int)floorf(hi + 0.5f));
 }
 
+// Per instance, in double precision: the projection C^-1 = (X B)^-1 and the margin.  The margin
+// adds to BASE_MARGIN_PX the direction error an ill-conditioned X adds to the float rays
+// (COND_MARGIN x cond(X) x pixels per radian) and the error of evaluating the projection in float
+// (PROJ_MARGIN x cond(C) x the screen width: |delta v| / |v| <= 5 eps cond(C) for v = C^-1 q with
+// rounded C^-1 and q, ndc = v.xy / v.z then errs by at most ~17 eps cond(C) on screen).
 __global__ void primary_instance_kernel(const __grid_constant__ DevScene sc, f3 camera,
-                                        const __grid_constant__ PrimaryParams v) {
+                                        const __grid_constant__ PrimaryParams v, uint32_t W, uint32_t H) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= sc.instance_count) return;
     f3 oo, od;
@@ -100,103 +110,174 @@ __global__ void primary_instance_kernel(const __grid_constant__ DevScene sc, f3 
     double X[9] = {r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
     double C[9], Ci[9], Xi[9];
     mul3(X, v.B, C);
-    bool ok = inverse3(C, Ci) && inverse3(X, Xi) && finite3(oo) &&
-              frobenius(C) * frobenius(Ci) < MAX_PROJECTION_COND;
+    bool ok = inverse3(C, Ci) && inverse3(X, Xi) && finite3(oo);
+    double cond_c = ok ? frobenius(C) * frobenius(Ci) : 0.0;
+    ok = ok && cond_c < MAX_PROJECTION_COND;
+    double margin = BASE_MARGIN_PX + COND_MARGIN * frobenius(X) * frobenius(Xi) * v.pixel_scale +
+                    PROJ_MARGIN * cond_c * (double)max(W, H);
     PrimaryInstance& I = v.inst[i];
     I.oo[0] = oo.x;
     I.oo[1] = oo.y;
     I.oo[2] = oo.z;
-    for (int k = 0; k < 9; ++k) I.ci[k] = ok ? Ci[k] : 0.0;
-    double margin = BASE_MARGIN_PX + COND_MARGIN * frobenius(X) * frobenius(Xi) * v.pixel_scale;
-    I.margin = margin;
-    I.ok = ok && isfinite(margin) ? 1u : 0u;
+    for (int k = 0; k < 9; ++k) I.ci[k] = ok ? (float)Ci[k] : 0.0f;
+    I.margin = __double2float_ru(margin);
+    I.ok = ok && isfinite(margin) && margin < 1.0e6 ? 1u : 0u;
+    I.pad[0] = I.pad[1] = 0.0f;
 }
 
 struct P3 {
     double x, y, l;  // C^-1 (p - oo): lambda (ndc.x, ndc.y, 1)
 };
 
+// The rare records that cross lambda_clip: clipped (Sutherland-Hodgman against one plane) and
+// projected in double precision; false when nothing is left.
+__device__ __noinline__ bool clipped_bounds(const PrimaryInstance& I, float4 va, float4 vb, float4 vc, double lc,
+                                            double W, double H, double& xlo, double& ylo, double& xhi, double& yhi) {
+    P3 p[3];
+    const float4 vtx[3] = {va, vb, vc};
+    for (int k = 0; k < 3; ++k) {
+        double q[3] = {(double)vtx[k].x - I.oo[0], (double)vtx[k].y - I.oo[1], (double)vtx[k].z - I.oo[2]};
+        const float* m = I.ci;
+        p[k].x = (double)m[0] * q[0] + (double)m[1] * q[1] + (double)m[2] * q[2];
+        p[k].y = (double)m[3] * q[0] + (double)m[4] * q[1] + (double)m[5] * q[2];
+        p[k].l = (double)m[6] * q[0] + (double)m[7] * q[1] + (double)m[8] * q[2];
+    }
+    P3 poly[4];
+    int np = 0;
+    for (int k = 0; k < 3; ++k) {
+        const P3& s = p[k];
+        const P3& e = p[(k + 1) % 3];
+        bool sin = s.l >= lc, ein = e.l >= lc;
+        if (sin) poly[np++] = s;
+        if (sin != ein) {
+            double f = (lc - s.l) / (e.l - s.l);
+            poly[np++] = P3{s.x + (e.x - s.x) * f, s.y + (e.y - s.y) * f, lc};
+        }
+    }
+    if (np == 0) return false;
+    xlo = ylo = INFINITY;
+    xhi = yhi = -INFINITY;
+    for (int k = 0; k < np; ++k) {
+        double l = fmax(poly[k].l, lc);
+        double px = (poly[k].x / l + 1.0) * 0.5 * W;
+        double py = (poly[k].y / l + 1.0) * 0.5 * H;
+        xlo = fmin(xlo, px);
+        xhi = fmax(xhi, px);
+        ylo = fmin(ylo, py);
+        yhi = fmax(yhi, py);
+    }
+    if (!(isfinite(xlo) && isfinite(xhi) && isfinite(ylo) && isfinite(yhi))) {
+        xlo = ylo = -4.0;
+        xhi = W + 4.0;
+        yhi = H + 4.0;
+    }
+    return true;
+}
+
+// Per record: the pixel-position rectangle (widened by the instance's margin), its pixel count,
+// and, for records wholly in front of lambda_clip, the three edge functions of the projected
+// triangle moved out by the margin (a sample outside them cannot hit the record).  float
+// arithmetic; the margin covers its rounding.
 __global__ void primary_rect_kernel(const __grid_constant__ DevScene sc, const __grid_constant__ PrimaryParams v,
                                     uint32_t W, uint32_t H) {
     uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t cnt = 0u;
     float4 rect = make_float4(1.0f, 1.0f, 0.0f, 0.0f);
+    const float4 pass = make_float4(0.0f, 0.0f, 1.0f, 0.0f);  // an edge function every sample passes
+    float4 edge[3] = {pass, pass, pass};
     if (r < v.records) {
-        float4 a = sc.tris[3ull * r], b = sc.tris[3ull * r + 1], c = sc.tris[3ull * r + 2];
-        const PrimaryInstance& I = v.inst[__float_as_uint(b.w)];
+        const float4 va = sc.tris[3ull * r], vb = sc.tris[3ull * r + 1], vc = sc.tris[3ull * r + 2];
+        const PrimaryInstance& I = v.inst[__float_as_uint(vb.w)];
+        const float Wf = (float)W, Hf = (float)H;
         bool any = false;
-        double xlo = 0.0, ylo = 0.0, xhi = 0.0, yhi = 0.0;
+        float xlo = 0.0f, ylo = 0.0f, xhi = 0.0f, yhi = 0.0f;
         if (!I.ok) {
             any = true;
-            xlo = ylo = -4.0;
-            xhi = (double)W + 4.0;
-            yhi = (double)H + 4.0;
+            xlo = ylo = -4.0f;
+            xhi = Wf + 4.0f;
+            yhi = Hf + 4.0f;
         } else {
-            double q[3][3] = {{a.x - I.oo[0], a.y - I.oo[1], a.z - I.oo[2]},
-                              {b.x - I.oo[0], b.y - I.oo[1], b.z - I.oo[2]},
-                              {c.x - I.oo[0], c.y - I.oo[1], c.z - I.oo[2]}};
-            double e1[3] = {q[1][0] - q[0][0], q[1][1] - q[0][1], q[1][2] - q[0][2]};
-            double e2[3] = {q[2][0] - q[0][0], q[2][1] - q[0][1], q[2][2] - q[0][2]};
-            double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-            // front faces have their normal towards the ray origin: dot(n, oo - p0) > 0
-            double facing = -(n[0] * q[0][0] + n[1] * q[0][1] + n[2] * q[0][2]);
-            double scale = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) *
-                           sqrt(q[0][0] * q[0][0] + q[0][1] * q[0][1] + q[0][2] * q[0][2]);
-            bool back = facing < -BACKFACE_COS * scale;
+            const f3 oo = f3{I.oo[0], I.oo[1], I.oo[2]};
+            f3 a = xyz3(va), b = xyz3(vb), c = xyz3(vc);
+            // back faces (extension rays cull them): object-space vertices are within the unit
+            // cube, so each edge's float difference errs by at most 1e-7 per unit of length
+            f3 e1 = b - a, e2 = c - a, q0 = a - oo;
+            f3 n = cross(e1, e2);
+            float l1 = length(e1), l2 = length(e2);
+            float nerr = 1.0e-7f * (l1 + l2) + 2.4e-7f * l1 * l2;
+            // front faces have their normal towards the ray origin, dot(n, oo - a) > 0
+            bool back = dot(n, q0) > (BACKFACE_COS * length(n) + 4.0f * nerr) * length(q0);
             if (!back) {
-                P3 p[3];
+                const float* m = I.ci;
+                f3 q[3] = {q0, b - oo, c - oo};
+                float px[3], py[3], pl[3];
+#pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    const double* m = I.ci;
-                    p[k].x = m[0] * q[k][0] + m[1] * q[k][1] + m[2] * q[k][2];
-                    p[k].y = m[3] * q[k][0] + m[4] * q[k][1] + m[5] * q[k][2];
-                    p[k].l = m[6] * q[k][0] + m[7] * q[k][1] + m[8] * q[k][2];
+                    px[k] = m[0] * q[k].x + m[1] * q[k].y + m[2] * q[k].z;
+                    py[k] = m[3] * q[k].x + m[4] * q[k].y + m[5] * q[k].z;
+                    pl[k] = m[6] * q[k].x + m[7] * q[k].y + m[8] * q[k].z;
                 }
-                // clip to lambda >= lambda_clip (Sutherland-Hodgman against one plane)
-                P3 poly[4];
-                int np = 0;
-                const double lc = v.lambda_clip;
-                for (int k = 0; k < 3; ++k) {
-                    const P3& s = p[k];
-                    const P3& e = p[(k + 1) % 3];
-                    bool sin = s.l >= lc, ein = e.l >= lc;
-                    if (sin) poly[np++] = s;
-                    if (sin != ein) {
-                        double f = (lc - s.l) / (e.l - s.l);
-                        poly[np++] = P3{s.x + (e.x - s.x) * f, s.y + (e.y - s.y) * f, lc};
+                const float lc = (float)v.lambda_clip;
+                if (pl[0] >= lc && pl[1] >= lc && pl[2] >= lc) {
+                    float sx[3], sy[3];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        sx[k] = (px[k] / pl[k] + 1.0f) * (0.5f * Wf);
+                        sy[k] = (py[k] / pl[k] + 1.0f) * (0.5f * Hf);
                     }
-                }
-                if (np > 0) {
                     any = true;
-                    xlo = ylo = INFINITY;
-                    xhi = yhi = -INFINITY;
-                    for (int k = 0; k < np; ++k) {
-                        double l = fmax(poly[k].l, lc);
-                        double px = (poly[k].x / l + 1.0) * 0.5 * (double)W;
-                        double py = (poly[k].y / l + 1.0) * 0.5 * (double)H;
-                        xlo = fmin(xlo, px);
-                        xhi = fmax(xhi, px);
-                        ylo = fmin(ylo, py);
-                        yhi = fmax(yhi, py);
-                    }
-                    if (!(isfinite(xlo) && isfinite(xhi) && isfinite(ylo) && isfinite(yhi))) {
-                        xlo = ylo = -4.0;
-                        xhi = (double)W + 4.0;
-                        yhi = (double)H + 4.0;
+                    xlo = fminf(fminf(sx[0], sx[1]), sx[2]);
+                    xhi = fmaxf(fmaxf(sx[0], sx[1]), sx[2]);
+                    ylo = fminf(fminf(sy[0], sy[1]), sy[2]);
+                    yhi = fmaxf(fmaxf(sy[0], sy[1]), sy[2]);
+                    float big = fmaxf(fmaxf(fabsf(xlo), fabsf(xhi)), fmaxf(fabsf(ylo), fabsf(yhi)));
+                    if (!isfinite(big)) {
+                        xlo = ylo = -4.0f;
+                        xhi = Wf + 4.0f;
+                        yhi = Hf + 4.0f;
+                    } else if (big < EDGE_MAX_COORD) {
+                        float area = (sx[1] - sx[0]) * (sy[2] - sy[0]) - (sy[1] - sy[0]) * (sx[2] - sx[0]);
+                        float em = I.margin + EDGE_EVAL_MARGIN + 4.0e-7f * big;
+                        float4 ed[3];
+                        bool usable = fabsf(area) > 1.0e-4f;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            const int k1 = k == 2 ? 0 : k + 1;
+                            float dx = sx[k1] - sx[k], dy = sy[k1] - sy[k];
+                            float len = sqrtf(dx * dx + dy * dy);
+                            usable = usable && len > 1.0e-2f;
+                            float s = (area > 0.0f ? 1.0f : -1.0f) / fmaxf(len, 1.0e-2f);
+                            float na = -dy * s, nb = dx * s;  // unit normal towards the inside
+                            ed[k] = make_float4(na, nb, em - (na * sx[k] + nb * sy[k]), 0.0f);
+                        }
+                        if (usable) {
+                            edge[0] = ed[0];
+                            edge[1] = ed[1];
+                            edge[2] = ed[2];
+                        }
                     }
                     xlo -= I.margin;
                     ylo -= I.margin;
                     xhi += I.margin;
                     yhi += I.margin;
+                } else if (pl[0] >= lc || pl[1] >= lc || pl[2] >= lc) {
+                    double dxlo, dylo, dxhi, dyhi;
+                    if (clipped_bounds(I, va, vb, vc, v.lambda_clip, W, H, dxlo, dylo, dxhi, dyhi)) {
+                        any = true;
+                        xlo = __double2float_rd(fmax(dxlo, -1.0e9) - I.margin);
+                        ylo = __double2float_rd(fmax(dylo, -1.0e9) - I.margin);
+                        xhi = __double2float_ru(fmin(dxhi, 1.0e9) + I.margin);
+                        yhi = __double2float_ru(fmin(dyhi, 1.0e9) + I.margin);
+                    }
                 }
             }
         }
         if (any) {
-            xlo = fmin(fmax(xlo, -4.0), (double)W + 4.0);
-            xhi = fmin(fmax(xhi, -4.0), (double)W + 4.0);
-            ylo = fmin(fmax(ylo, -4.0), (double)H + 4.0);
-            yhi = fmin(fmax(yhi, -4.0), (double)H + 4.0);
-            float4 f = make_float4(__double2float_rd(xlo), __double2float_rd(ylo), __double2float_ru(xhi),
-                                   __double2float_ru(yhi));
+            xlo = fminf(fmaxf(xlo, -4.0f), Wf + 4.0f);
+            xhi = fminf(fmaxf(xhi, -4.0f), Wf + 4.0f);
+            ylo = fminf(fmaxf(ylo, -4.0f), Hf + 4.0f);
+            yhi = fminf(fmaxf(yhi, -4.0f), Hf + 4.0f);
+            float4 f = make_float4(xlo, ylo, xhi, yhi);
             int x0, x1, y0, y1;
             pixel_span(f.x, f.z, W, x0, x1);
             pixel_span(f.y, f.w, H, y0, y1);
@@ -207,6 +288,9 @@ __global__ void primary_rect_kernel(const __grid_constant__ DevScene sc, const _
             }
         }
         v.rect[r] = rect;
+        v.edge[3ull * r] = edge[0];
+        v.edge[3ull * r + 1] = edge[1];
+        v.edge[3ull * r + 2] = edge[2];
     }
     if (r <= v.records) v.count[r] = cnt;  // count[records] = 0: the exclusive prefix ends with the total
     unsigned long long sum = cnt;
@@ -218,12 +302,21 @@ __global__ void primary_finish_kernel(const __grid_constant__ PrimaryParams v) {
     *v.ok = *v.total < PAIR_LIMIT ? 1u : 0u;
 }
 
-// One thread per pixel-record pair (grid-stride): every sample of the chunk in the pixel whose
-// position lies in the record's rectangle is tested against the record.
+__device__ __forceinline__ bool inside_edge(float4 e, float px, float py) {
+    return __fmaf_rn(e.x, px, __fmaf_rn(e.y, py, e.z)) >= 0.0f;
+}
+
+// Each warp takes 32 pixel-record pairs at a time, one per lane.  A lane draws its pixel's
+// samples in order (the draws of pixel_ndc) and queues those whose position passes the record's
+// rectangle and edge functions; the warp then tests queued samples 32 at a time, every lane busy,
+// with the traversal's ray set-up and ray/triangle test, reading the pair from its lane.  A
+// queue entry is the lane (5 bits), the sample (6 bits) and the two draws' mantissas (23 bits
+// each).
 __global__ void __launch_bounds__(RASTER_BLOCK) primary_raster_kernel(const __grid_constant__ RenderParams p,
                                                                       const __grid_constant__ PrimaryParams v,
                                                                       uint32_t chunk_sample0, uint32_t chunk_spp,
                                                                       const __grid_constant__ XsJump jump) {
+    __shared__ unsigned long long s_queue[RASTER_WARPS][QUEUE_CAP];
     if (*v.ok == 0u) return;
     const tt_constants& c = p.c;
     const DevScene& sc = p.sc;
@@ -232,46 +325,101 @@ __global__ void __launch_bounds__(RASTER_BLOCK) primary_raster_kernel(const __gr
     const uint32_t total = v.count[v.records];
     const uint32_t frame_hash = jenkins_hash(c.frame_index);
     const f3 camera = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
-        uint32_t lo = 0u, hi = v.records;  // count[lo] <= k < count[hi]
-        while (hi - lo > 1u) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (__ldg(v.count + mid) <= k) lo = mid;
-            else hi = mid;
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned long long* queue = s_queue[threadIdx.x >> 5];
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+
+    // tests queue entry `e` (have: the lane holds one) of the pair of lane e & 31; every lane calls
+    auto test = [&](unsigned long long e, bool have, uint32_t rec, uint32_t x, uint32_t y, uint32_t t, uint32_t tri) {
+        const uint32_t owner = (uint32_t)e & 31u;
+        const uint32_t orec = __shfl_sync(0xffffffffu, rec, owner), ox_ = __shfl_sync(0xffffffffu, x, owner),
+                       oy_ = __shfl_sync(0xffffffffu, y, owner), ot = __shfl_sync(0xffffffffu, t, owner),
+                       otri = __shfl_sync(0xffffffffu, tri, owner);
+        if (!have) return;
+        const uint32_t s = (uint32_t)(e >> 5) & 63u;
+        const float ox = mantissa_float((uint32_t)(e >> 11) & 0x7fffffu), oy = mantissa_float((uint32_t)(e >> 34) & 0x7fffffu);
+        f3 d = camera_ray_direction(c, pixel_ndc_from_draws(ox_, oy_, W, H, ox, oy));
+        if (!finite3(d)) return;
+        const float4 a = __ldg(sc.tris + 3ull * orec), b = __ldg(sc.tris + 3ull * orec + 1),
+                     cc = __ldg(sc.tris + 3ull * orec + 2);
+        f3 oo, od;
+        uint32_t mesh;
+        instance_ray(sc, __float_as_uint(b.w), camera, d, oo, od, mesh);
+        if (!finite3(od)) return;
+        RayPre rp = ray_precompute(oo, od);
+        float th, u, w;
+        if (!intersect_triangle(rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), true, EXTENSION_TMIN, EXTENSION_TMAX,
+                                th, u, w))
+            return;
+        unsigned long long key = ((unsigned long long)__float_as_uint(th) << 32) | otri;
+        unsigned long long* dst = v.key + (uint64_t)s * WH + ot;
+        if (key < *dst) atomicMin(dst, key);
+    };
+
+    for (uint32_t base = warp * 32u; base < total; base += warps * 32u) {
+        const uint32_t k = base + lane;
+        const bool valid = k < total;
+        uint32_t rec = 0u, x = 0u, y = 0u, t = 0u, tri = 0u, pg = 0u;
+        float4 rect = make_float4(1.0f, 1.0f, 0.0f, 0.0f), e0 = rect, e1 = rect, e2 = rect;
+        if (valid) {
+            uint32_t lo = 0u, hi = v.records;  // count[lo] <= k < count[hi]
+            while (hi - lo > 1u) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (__ldg(v.count + mid) <= k) lo = mid;
+                else hi = mid;
+            }
+            rec = lo;
+            rect = v.rect[rec];
+            e0 = v.edge[3ull * rec];
+            e1 = v.edge[3ull * rec + 1];
+            e2 = v.edge[3ull * rec + 2];
+            int x0, x1, y0, y1;
+            pixel_span(rect.x, rect.z, W, x0, x1);
+            pixel_span(rect.y, rect.w, H, y0, y1);
+            const uint32_t bw = (uint32_t)(x1 - x0 + 1);
+            const uint32_t j = k - __ldg(v.count + rec);
+            x = (uint32_t)x0 + j % bw;
+            y = (uint32_t)y0 + j / bw;
+            t = band_index(x, y, W, H);
+            const uint32_t prim = __float_as_uint(__ldg(sc.tris + 3ull * rec).w);
+            const uint32_t inst = __float_as_uint(__ldg(sc.tris + 3ull * rec + 1).w);
+            tri = __ldg(sc.tri_base + inst) + prim;
+            pg = jenkins_hash((x + y * W) ^ frame_hash);
+            if (chunk_sample0) pg = xs_apply(jump, pg);
         }
-        const float4 rect = v.rect[lo];
-        int x0, x1, y0, y1;
-        pixel_span(rect.x, rect.z, W, x0, x1);
-        pixel_span(rect.y, rect.w, H, y0, y1);
-        const uint32_t bw = (uint32_t)(x1 - x0 + 1);
-        const uint32_t j = k - __ldg(v.count + lo);
-        const uint32_t x = (uint32_t)x0 + j % bw, y = (uint32_t)y0 + j / bw;
-        const float4 a = __ldg(sc.tris + 3ull * lo), b = __ldg(sc.tris + 3ull * lo + 1), cc = __ldg(sc.tris + 3ull * lo + 2);
-        const uint32_t prim = __float_as_uint(a.w), inst = __float_as_uint(b.w);
-        const unsigned long long tri = (unsigned long long)(__ldg(sc.tri_base + inst) + prim);
-        unsigned long long* dst = v.key + band_index(x, y, W, H);
-        uint32_t pg = jenkins_hash((x + y * W) ^ frame_hash);
-        if (chunk_sample0) pg = xs_apply(jump, pg);
-        for (uint32_t s = 0; s < chunk_spp; ++s, dst += WH) {
-            // the draws of pixel_ndc: the sample's generator ends two steps on, at the next sample's
-            float ox = random_float(pg);
-            float oy = random_float(pg);
-            float px = (float)x + (ox - 0.5f), py = (float)y + (oy - 0.5f);
-            if (px < rect.x || px > rect.z || py < rect.y || py > rect.w) continue;
-            f3 d = camera_ray_direction(c, pixel_ndc_from_draws(x, y, W, H, ox, oy));
-            if (!finite3(d)) continue;
-            f3 oo, od;
-            uint32_t mesh;
-            instance_ray(sc, inst, camera, d, oo, od, mesh);
-            if (!finite3(od)) continue;
-            RayPre rp = ray_precompute(oo, od);
-            float t, u, w;
-            if (!intersect_triangle(rp, tri_vertex(a), tri_vertex(b), tri_vertex(cc), true, EXTENSION_TMIN,
-                                    EXTENSION_TMAX, t, u, w))
-                continue;
-            unsigned long long key = ((unsigned long long)__float_as_uint(t) << 32) | tri;
-            if (key < *dst) atomicMin(dst, key);
+        uint32_t queued = 0u;  // warp-uniform
+        for (uint32_t s0 = 0; s0 < chunk_spp; s0 += SAMPLE_GROUP) {
+#pragma unroll
+            for (uint32_t j = 0; j < (uint32_t)SAMPLE_GROUP; ++j) {
+                const uint32_t s = s0 + j;
+                bool in = false;
+                uint32_t mx = 0u, my = 0u;
+                if (valid && s < chunk_spp) {
+                    // the draws of pixel_ndc: the generator ends two steps on, at the next sample's
+                    mx = random_mantissa(pg);
+                    my = random_mantissa(pg);
+                    const float px = (float)x + (mantissa_float(mx) - 0.5f), py = (float)y + (mantissa_float(my) - 0.5f);
+                    in = px >= rect.x && px <= rect.z && py >= rect.y && py <= rect.w && inside_edge(e0, px, py) &&
+                         inside_edge(e1, px, py) && inside_edge(e2, px, py);
+                }
+                const uint32_t m = __ballot_sync(0xffffffffu, in);
+                if (in)
+                    queue[queued + __popc(m & lanes_below())] =
+                        lane | (s << 5) | ((unsigned long long)mx << 11) | ((unsigned long long)my << 34);
+                queued += __popc(m);
+            }
+            __syncwarp();
+            while (queued >= 32u) {
+                queued -= 32u;
+                test(queue[queued + lane], true, rec, x, y, t, tri);
+            }
+            __syncwarp();
         }
+        if (queued) {
+            const bool have = lane < queued;
+            test(have ? queue[lane] : 0ull, have, rec, x, y, t, tri);
+        }
+        __syncwarp();
     }
 }
 
@@ -316,7 +464,8 @@ void primary_setup(const RenderParams& p, const PrimaryParams& v, cudaStream_t s
     f3 camera = f3{p.c.camera_position[0], p.c.camera_position[1], p.c.camera_position[2]};
     check_cuda(cudaMemsetAsync(v.total, 0, 8, st), "memset");
     if (sc.instance_count)
-        primary_instance_kernel<<<(sc.instance_count + 127) / 128, 128, 0, st>>>(sc, camera, v);
+        primary_instance_kernel<<<(sc.instance_count + 127) / 128, 128, 0, st>>>(sc, camera, v, p.c.screen_size[0],
+                                                                                p.c.screen_size[1]);
     primary_rect_kernel<<<(unsigned)((v.records + 1ull + 255) / 256), 256, 0, st>>>(sc, v, p.c.screen_size[0],
                                                                                    p.c.screen_size[1]);
     check_cuda(cudaGetLastError(), "primary bounds");

@@ -167,7 +167,8 @@ template <bool TEX, int ACCEL>
 __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_constant__ RenderParams p,
                                                                   const __grid_constant__ RestirParams rp,
                                                                   Surface* gbuf, float4* gtex, float4* glob) {
-    // the flat BVH: the warp's camera rays (a 16 x 2 pixel strip) traced as one packet
+    // the flat BVH: the camera rays' hits from their rasterised keys, or the warp's camera rays (a
+    // 16 x 2 pixel strip) traced as one packet
     constexpr bool PACKET = ACCEL == ACCEL_FLAT_ONLY;
     __shared__ uint32_t s_stack[PACKET ? 1 : TRAVERSAL_STACK * RT_BLOCK];
     __shared__ uint2 s_packet[PACKET ? RT_BLOCK / 32 : 1][PACKET ? PACKET_STACK : 1];
@@ -179,8 +180,10 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     f2 ndc = inside ? pixel_ndc(x, y, W, H, g) : f2{0.0f, 0.0f};
     f3 dir = inside ? camera_ray_direction(c, ndc) : f3{0.0f, 0.0f, 1.0f};
     f3 org = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
-    Hit h;
-    if (PACKET) {
+    Hit h{};
+    if (PACKET && rp.vis != nullptr && *rp.vis_ok != 0u) {
+        if (inside) h = primary_resolve(p.sc, rp.vis[band_index(x, y, W, H)], org, dir, p.err);
+    } else if (PACKET) {
         h = packet_trace_flat(p.sc, org, dir, inside, EXTENSION_TMIN, EXTENSION_TMAX, true, s_packet[threadIdx.x >> 5],
                               p.err);
     } else if (inside) {

@@ -275,9 +275,10 @@ __host__ __device__ constexpr XsJump xs_power(uint64_t k) {  // M^k by squaring
     return r;
 }
 
-TT_HD float random_float(uint32_t& s) {
-    return __uint_as_float(0x3f800000u | (xor_shift(s) >> 9)) - 1.0f;
-}
+// random_float split in two: the 23 mantissa bits a step draws, and the float in [0, 1) they give
+TT_HD uint32_t random_mantissa(uint32_t& s) { return xor_shift(s) >> 9; }
+TT_HD float mantissa_float(uint32_t m) { return __uint_as_float(0x3f800000u | m) - 1.0f; }
+TT_HD float random_float(uint32_t& s) { return mantissa_float(random_mantissa(s)); }
 TT_HD f2 random_vec2(uint32_t& s) {
     float a = random_float(s);
     float b = random_float(s);

@@ -166,14 +166,17 @@ inline void stage_end(StageTimer* t, cudaStream_t st) {
 // (instance, primitive)).  The extension kernel then rebuilds each camera ray's hit from its key
 // with one ray/triangle test instead of a traversal.
 struct PrimaryInstance {
-    double oo[3];    // the camera position in object space, as instance_ray computes it (float)
-    double ci[9];    // (object-from-world 3x3 * B)^-1, row-major: object-space offset -> lambda (ndc, 1)
-    double margin;   // screen margin in pixels (grows with the matrix's condition number)
+    float oo[3];     // the camera position in object space, as instance_ray computes it
+    float ci[9];     // (object-from-world 3x3 * B)^-1, row-major: object-space offset -> lambda (ndc, 1)
+    float margin;    // screen margin in pixels (rounding of the rays, the ray/triangle test and the bound)
     uint32_t ok;     // 0: no bound (the instance's records cover the whole screen)
+    float pad[2];
 };
 struct PrimaryParams {
     unsigned long long* key;     // chunk_spp x WH keys (t bits << 32 | scene triangle index), ~0: no hit
     float4* rect;                // per record: pixel-position rectangle x0, y0, x1, y1 (x0 > x1: none)
+    float4* edge;                // per record: 3 edge functions (a, b, c, 0); a sample at pixel position
+                                 // (x, y) can hit the record only where a x + b y + c >= 0 for all three
     uint32_t* count;             // records + 1: pixels of each rectangle, then their exclusive prefix
     unsigned long long* total;   // pixel-record pairs of the frame
     uint32_t* ok;                // 1 when the keys are complete (the extension kernel reads them)
@@ -227,6 +230,10 @@ struct RestirParams {
     RestirHistory history;
     uint32_t candidates, neighbours;
     float m_cap, radius;
+    // rasterised primary visibility of the frame's camera rays (one sample per pixel, keys in band
+    // order); null, or *vis_ok == 0, when the G-buffer pass traces them
+    const unsigned long long* vis;
+    const uint32_t* vis_ok;
 };
 void render_restir(const RenderParams& p, const RestirParams& rp, cudaStream_t st, StageTimer* timer);
 void launch_tonemap(const float4* in, uint64_t n, uint32_t tonemap, uint32_t format, void* out,

@@ -31,6 +31,49 @@ TT_HD f3 camera_ray_direction(const tt_constants& c, f2 ndc) {
     return normalize(f3{wd.x, wd.y, wd.z});
 }
 
+// Index of pixel (x, y) in the band order of the wavefront integrator's work items (bands of 8
+// rows, column by column within a band): the index of rasterised primary-visibility keys.
+TT_HD uint32_t band_index(uint32_t x, uint32_t y, uint32_t W, uint32_t H) {
+    uint32_t band = y / 8u;
+    uint32_t rows = H - 8u * band < 8u ? H - 8u * band : 8u;
+    return band * 8u * W + x * rows + (y - 8u * band);
+}
+
+// The closest hit of the camera ray (o, d) from its rasterised primary-visibility key (t bits <<
+// 32 | scene triangle index, ~0: no hit; primary.cu): the key's record, tested with the ray's own
+// set-up, gives the t, u, v the traversal reports.  A key the test does not confirm sets
+// ERR_PRIMARY_MISMATCH and counts as a miss.
+__device__ __forceinline__ Hit primary_resolve(const DevScene& sc, unsigned long long key, f3 o, f3 d, uint32_t* err) {
+    Hit h;
+    h.hit = 0;
+    h.t = h.u = h.v = 0.0f;
+    h.instance = h.prim = 0u;
+    if (key == ~0ull) return h;
+    const uint32_t rec = __ldg(sc.tri_record + (uint32_t)key);
+    const float4 a = __ldg(sc.tris + 3ull * rec), b = __ldg(sc.tris + 3ull * rec + 1), c = __ldg(sc.tris + 3ull * rec + 2);
+    const uint32_t inst = __float_as_uint(b.w);
+    f3 oo, od;
+    uint32_t mesh;
+    instance_ray(sc, inst, o, d, oo, od, mesh);
+    RayPre rp = ray_precompute(oo, od);
+    float t, u, v;
+    bool ok = finite3(od) &&
+              intersect_triangle(rp, tri_vertex(a), tri_vertex(b), tri_vertex(c), true, EXTENSION_TMIN, EXTENSION_TMAX,
+                                 t, u, v) &&
+              __float_as_uint(t) == (uint32_t)(key >> 32);
+    if (!ok) {
+        atomicOr(err, ERR_PRIMARY_MISMATCH);
+        return h;
+    }
+    h.hit = 1;
+    h.t = t;
+    h.u = u;
+    h.v = v;
+    h.instance = inst;
+    h.prim = __float_as_uint(a.w);
+    return h;
+}
+
 struct ShadeHit {
     f3 world_position;
     Basis tangent_space;

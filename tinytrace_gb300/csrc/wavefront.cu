@@ -288,41 +288,11 @@ __device__ __forceinline__ bool extension_result(const WfParams& w, const DevSce
     return is_hit;
 }
 
-// The closest hit of the camera ray in `slot` from its rasterised key (primary.cu): the record
-// of the key's scene triangle, tested with the ray's own set-up, gives the t, u, v the traversal
-// would report.  A key that this test does not confirm sets ERR_PRIMARY_MISMATCH.
+// The closest hit of the camera ray in `slot` from the chunk's rasterised key of its work item.
 __device__ __forceinline__ Hit primary_hit(const WfParams& w, const DevScene& sc, uint32_t slot, bool valid,
                                            uint32_t* err) {
-    Hit h;
-    h.hit = 0;
-    h.t = h.u = h.v = 0.0f;
-    h.instance = h.prim = 0u;
-    if (!valid) return h;
-    const unsigned long long key = w.vis[__float_as_uint(w.thr[slot].w)];
-    if (key == ~0ull) return h;
-    const uint32_t rec = __ldg(sc.tri_record + (uint32_t)key);
-    const float4 a = __ldg(sc.tris + 3ull * rec), b = __ldg(sc.tris + 3ull * rec + 1), c = __ldg(sc.tris + 3ull * rec + 2);
-    const uint32_t inst = __float_as_uint(b.w);
-    f3 oo, od;
-    uint32_t mesh;
-    instance_ray(sc, inst, xyz(w.org[slot]), xyz(w.dir[slot]), oo, od, mesh);
-    RayPre rp = ray_precompute(oo, od);
-    float t, u, v;
-    bool ok = finite3(od) &&
-              intersect_triangle(rp, tri_vertex(a), tri_vertex(b), tri_vertex(c), true, EXTENSION_TMIN, EXTENSION_TMAX,
-                                 t, u, v) &&
-              __float_as_uint(t) == (uint32_t)(key >> 32);
-    if (!ok) {
-        atomicOr(err, ERR_PRIMARY_MISMATCH);
-        return h;
-    }
-    h.hit = 1;
-    h.t = t;
-    h.u = u;
-    h.v = v;
-    h.instance = inst;
-    h.prim = __float_as_uint(a.w);
-    return h;
+    if (!valid) return primary_resolve(sc, ~0ull, splat(0.0f), splat(0.0f), err);
+    return primary_resolve(sc, w.vis[__float_as_uint(w.thr[slot].w)], xyz(w.org[slot]), xyz(w.dir[slot]), err);
 }
 
 // MULTI: a shared-pool round; each lane traces in the scene of its ray's request and reports
