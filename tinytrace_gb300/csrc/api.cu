@@ -619,6 +619,7 @@ DevScene scene_view(tt_context* ctx, tt_handle scene) {
     return d;
 }
 int context_device(tt_context* ctx) { return ctx->device; }
+bool context_primary_raster(tt_context* ctx) { return ctx->primary == TT_PRIMARY_RASTER; }
 }  // namespace tt
 
 static void cache_ready(tt_context* ctx) {

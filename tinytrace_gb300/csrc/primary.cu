@@ -423,7 +423,18 @@ __global__ void __launch_bounds__(RASTER_BLOCK) primary_raster_kernel(const __gr
     }
 }
 
+__global__ void primary_round_keys_kernel(const BatchRequest* reqs, BatchRound* round) {
+    uint32_t keys = round->keys;
+    for (uint32_t r = 0; r < round->nreq && keys; ++r) keys = reqs[r].vis_ok != nullptr && *reqs[r].vis_ok != 0u;
+    round->keys = keys ? 1u : 0u;
+}
+
 }  // namespace
+
+void primary_round_keys(const BatchRequest* reqs, BatchRound* round, cudaStream_t st) {
+    primary_round_keys_kernel<<<1, 1, 0, st>>>(reqs, round);
+    check_cuda(cudaGetLastError(), "primary round keys");
+}
 
 bool primary_camera(const tt_constants& c, PrimaryParams& v) {
     const float* IP = c.inverse_proj;

@@ -38,6 +38,7 @@
 namespace tt {
 DevScene scene_view(tt_context* ctx, tt_handle scene);
 int context_device(tt_context* ctx);
+bool context_primary_raster(tt_context* ctx);
 }  // namespace tt
 
 using namespace tt;
@@ -93,6 +94,12 @@ struct tt_server {
     // the shared path pool and the round tables (device), their pinned host mirrors
     DeviceBuffer org, dir, thr, acc, pa1, pa0, pe, hit, hslot, active, shadow, counters, ndc_mip;
     DeviceBuffer d_reqs, d_scenes, d_round, d_batch_err;
+    // rasterised camera-ray keys of flat-BVH4 rounds: one key per work item of the round, and the
+    // per-request bound buffers (reused request after request) with per-request total/ok words
+    DeviceBuffer keys, prim_rect, prim_edge, prim_count, prim_inst, prim_flags;
+    uint64_t key_items = 0, prim_records = 0, prim_instances = 0;
+    int occupancy_sms = 0;
+    bool primary = true;  // the context's TT_OPTION_PRIMARY_VISIBILITY at creation is TT_PRIMARY_RASTER
     BatchRequest* h_reqs = nullptr;
     DevScene* h_scenes = nullptr;
     BatchRound* h_round = nullptr;
@@ -326,9 +333,74 @@ void tt_server::launch_round(std::vector<Request*>& live) {
     cudaGraphExec_t& g = graph[tex ? 1 : 0][structures][short_stack ? 1 : 0];
     if (!g) g = build_batch_graph(w, bp, tex, structures, short_stack, d_batch_err.as<uint32_t>(), capture, body);
     check_cuda(cudaEventRecord(round_start, stream), "event");
+    // flat-BVH4 rounds: each request's camera-ray keys for its chunk, at its items in the round
+    h_round->keys = 0u;
+    if (structures == BATCH_FLAT && primary) {
+        uint64_t recs = 0, insts = 0;
+        for (uint32_t k = 0; k < n; ++k) {
+            recs = std::max<uint64_t>(recs, live[k]->sc.tri_count);
+            insts = std::max<uint64_t>(insts, live[k]->sc.instance_count);
+        }
+        if (items > key_items) {
+            keys.alloc(8ull * items);
+            key_items = items;
+        }
+        if (recs + 1 > prim_records) {
+            prim_rect.alloc(16ull * recs);
+            prim_edge.alloc(48ull * recs);
+            prim_count.alloc(4ull * (recs + 1));
+            prim_records = recs + 1;
+        }
+        if (insts > prim_instances) {
+            prim_inst.alloc(sizeof(PrimaryInstance) * insts);
+            prim_instances = insts;
+        }
+        if (!prim_flags.ptr) prim_flags.alloc(16ull * BATCH_MAX_REQUESTS);
+        if (occupancy_sms == 0)
+            check_cuda(cudaDeviceGetAttribute(&occupancy_sms, cudaDevAttrMultiProcessorCount, device), "sm count");
+        bool all = n > 0;
+        for (uint32_t k = 0; k < n; ++k) {
+            Request& r = *live[k];
+            BatchRequest& b = h_reqs[k];
+            PrimaryParams v{};
+            if (!(r.sc.tri_record && r.sc.tri_count > 0 && primary_camera(r.c, v))) {
+                b.vis = nullptr;
+                b.vis_ok = nullptr;
+                all = false;
+                continue;
+            }
+            v.key = keys.as<unsigned long long>() + b.item_base;
+            v.rect = prim_rect.as<float4>();
+            v.edge = prim_edge.as<float4>();
+            v.count = prim_count.as<uint32_t>();
+            v.total = reinterpret_cast<unsigned long long*>(prim_flags.as<unsigned char>() + 16ull * k);
+            v.ok = reinterpret_cast<uint32_t*>(prim_flags.as<unsigned char>() + 16ull * k + 8);
+            v.inst = prim_inst.as<PrimaryInstance>();
+            v.records = r.sc.tri_count;
+            v.raster_blocks = std::max(1, occupancy_sms) * 8;
+            RenderParams rp{};
+            rp.sc = r.sc;
+            rp.c = r.c;
+            WfParams chunk{};
+            chunk.chunk_sample0 = b.chunk_sample0;
+            chunk.chunk_spp = b.chunk_spp;
+            chunk.chunk_jump = b.chunk_jump;
+            primary_setup(rp, v, stream);
+            primary_chunk(rp, v, chunk, stream);
+            b.vis = v.key;
+            b.vis_ok = v.ok;
+        }
+        h_round->keys = all ? 1u : 0u;
+    } else {
+        for (uint32_t k = 0; k < n; ++k) {
+            h_reqs[k].vis = nullptr;
+            h_reqs[k].vis_ok = nullptr;
+        }
+    }
     check_cuda(cudaMemcpyAsync(d_reqs.ptr, h_reqs, sizeof(BatchRequest) * n, cudaMemcpyHostToDevice, stream), "table");
     check_cuda(cudaMemcpyAsync(d_scenes.ptr, h_scenes, sizeof(DevScene) * n, cudaMemcpyHostToDevice, stream), "scenes");
     check_cuda(cudaMemcpyAsync(d_round.ptr, h_round, sizeof(BatchRound), cudaMemcpyHostToDevice, stream), "round");
+    if (h_round->keys) primary_round_keys(d_reqs.as<BatchRequest>(), d_round.as<BatchRound>(), stream);
     check_cuda(cudaMemsetAsync(d_batch_err.ptr, 0, 4, stream), "memset");
     check_cuda(cudaGraphLaunch(g, stream), "cudaGraphLaunch");
     for (uint32_t k = 0; k < n; ++k)
@@ -477,6 +549,7 @@ int32_t tt_server_create(tt_context* ctx, const tt_server_config* config, tt_ser
         auto srv = std::make_unique<tt_server>();
         srv->ctx = ctx;
         srv->device = context_device(ctx);
+        srv->primary = context_primary_raster(ctx);
         check_cuda(cudaSetDevice(srv->device), "cudaSetDevice");
         if (config) {
             if (config->hbm_budget_bytes) srv->budget = config->hbm_budget_bytes;

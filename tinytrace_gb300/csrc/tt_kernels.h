@@ -107,11 +107,16 @@ struct BatchRequest {
     uint32_t scene;      // index into the round's scene table
     uint32_t WH, item_base, pixel_base;
     uint32_t chunk_sample0, chunk_spp, chunk_items, last;  // last: the chunk ends the request
+    // rasterised camera-ray keys of the request's chunk (indexed by its work item) and their ok
+    // word; null when the request's camera rays are traversed
+    const unsigned long long* vis;
+    const uint32_t* vis_ok;
 };
 // Round header in device memory (read by the graph's kernels, so that one instantiated graph
 // serves every round): request count, total work items, total pixels, iteration limit.
 struct BatchRound {
     uint32_t nreq, items, pixels, limit;
+    uint32_t keys;  // 1: every request of the round has complete camera-ray keys
 };
 struct BatchParams {
     const BatchRequest* reqs;  // BATCH_MAX_REQUESTS entries
@@ -193,6 +198,8 @@ bool primary_camera(const tt_constants& c, PrimaryParams& v);
 void primary_setup(const RenderParams& p, const PrimaryParams& v, cudaStream_t st);
 // Per sample chunk (w.chunk_sample0, w.chunk_spp, w.chunk_jump): clears and fills the keys.
 void primary_chunk(const RenderParams& p, const PrimaryParams& v, const WfParams& w, cudaStream_t st);
+// Shared-pool rounds: round->keys stays 1 only if every request's ok word is 1 (one thread).
+void primary_round_keys(const BatchRequest* reqs, BatchRound* round, cudaStream_t st);
 
 // Renders with the wavefront integrator; w.chunk_spp is the largest chunk of samples the
 // buffers hold.  Synchronises `st` once per iteration to read the active-path count.  `prim`:

@@ -297,7 +297,8 @@ __device__ __forceinline__ Hit primary_hit(const WfParams& w, const DevScene& sc
 
 // MULTI: a shared-pool round; each lane traces in the scene of its ray's request and reports
 // traversal errors to that request's error word.
-template <bool COUNT, bool SHADOW, int ACCEL, int STACK = TRAVERSAL_STACK, bool MULTI = false>
+// KEYS: the flat-BVH extension kernel of renders with rasterised camera-ray keys (no packet code).
+template <bool COUNT, bool SHADOW, int ACCEL, int STACK = TRAVERSAL_STACK, bool MULTI = false, bool KEYS = false>
 __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel(const __grid_constant__ RenderParams p,
                                                                 const __grid_constant__ WfParams w,
                                                                 const __grid_constant__ BatchParams b) {
@@ -305,8 +306,8 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
     // when the chunk has them (w.vis), else, in the uninstrumented kernel (PACKET), through the
     // warp-wide traversal of the flat BVH; the per-lane loop below then takes the continuing
     // paths only
-    constexpr bool CAMERA = !SHADOW && !MULTI && ACCEL == ACCEL_FLAT_ONLY;
-    constexpr bool PACKET = CAMERA && !COUNT;
+    constexpr bool CAMERA = !SHADOW && ACCEL == ACCEL_FLAT_ONLY && (!MULTI || KEYS);
+    constexpr bool PACKET = CAMERA && !COUNT && !KEYS;
     __shared__ uint32_t s_stack[STACK * TR_BLOCK];
     __shared__ uint2 s_packet[PACKET ? TR_BLOCK / 32 : 1][PACKET ? PACKET_STACK : 1];
     uint32_t* stack = s_stack + threadIdx.x;
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
     const uint32_t n_camera = SHADOW ? 0u : w.counters[WF_CAMERA];
     Counters cnt{0u, 0u, 0u, 0u};
     uint32_t rays = 0, hits = 0;
-    const bool raster = CAMERA && w.vis != nullptr && *w.vis_ok != 0u;
+    const bool raster = CAMERA && (MULTI ? b.round->keys != 0u : w.vis != nullptr && *w.vis_ok != 0u);
     const bool camera_phase = raster || PACKET;
     if (CAMERA && camera_phase) {
         uint32_t* phead = &w.counters[WF_PACKET_HEAD];
@@ -330,7 +331,13 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
             bool valid = i < n_camera;
             uint32_t pslot = valid ? w.active[i] : 0u;
             Hit h{};
-            if (raster) {
+            if (MULTI && raster) {  // the key of the ray's request, indexed by its item in that request
+                const uint32_t req = valid ? (__float_as_uint(w.org[pslot].w) >> BATCH_BOUNCE_BITS) & 0xffu : 0u;
+                const BatchRequest& R = b.reqs[req];
+                h = valid ? primary_resolve(b.scenes[R.scene], R.vis[__float_as_uint(w.thr[pslot].w)],
+                                            xyz(w.org[pslot]), xyz(w.dir[pslot]), R.err)
+                          : Hit{};
+            } else if (raster) {
                 h = primary_hit(w, p.sc, pslot, valid, p.err);
                 if (COUNT && valid) {  // one record test and one object-ray set-up per hit
                     rays++;
@@ -343,7 +350,12 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
                 h = packet_trace_flat(p.sc, xyz(o), xyz(d), valid, EXTENSION_TMIN, EXTENSION_TMAX, true,
                                       s_packet[threadIdx.x >> 5], p.err);
             }
-            if (extension_result(w, p.sc, pslot, valid, h) && COUNT) hits++;
+            if (MULTI) {
+                const uint32_t req = valid ? (__float_as_uint(w.org[pslot].w) >> BATCH_BOUNCE_BITS) & 0xffu : 0u;
+                extension_result(w, b.scenes[b.reqs[req].scene], pslot, valid, h);
+            } else if (extension_result(w, p.sc, pslot, valid, h) && COUNT) {
+                hits++;
+            }
         }
     }
     // the per-lane loop's queue: shadow rays, or the active paths (camera rays, unless the camera
@@ -685,6 +697,11 @@ static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid
         else wf_trace_kernel<false, SHADOW, ACCEL_WIDE_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
     } else if (p.sc.flat) {
         if (counted) wf_trace_kernel<true, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
+        else if (!SHADOW && w.vis && short_stack)
+            wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY, SHORT_TRAVERSAL_STACK, false, true>
+                <<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
+        else if (!SHADOW && w.vis)
+            wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY, TRAVERSAL_STACK, false, true><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
         else if (short_stack)
             wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY, SHORT_TRAVERSAL_STACK><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
         else wf_trace_kernel<false, SHADOW, ACCEL_FLAT_ONLY><<<grid, TR_BLOCK, 0, st>>>(p, w, BatchParams{});
@@ -817,7 +834,7 @@ static cudaGraphExec_t batch_graph(const WfParams& w, const BatchParams& b, bool
     int sms = 0, dev = 0, ext_per_sm = 0, shadow_per_sm = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
-    auto ext = wf_trace_kernel<false, false, ACCEL, STACK, true>;
+    auto ext = wf_trace_kernel<false, false, ACCEL, STACK, true, ACCEL == ACCEL_FLAT_ONLY>;
     auto shadow = wf_trace_kernel<false, true, ACCEL, STACK, true>;
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ext_per_sm, ext, TR_BLOCK, 0), "occupancy");
     check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shadow_per_sm, shadow, TR_BLOCK, 0), "occupancy");
