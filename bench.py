@@ -1089,9 +1089,12 @@ def run_ours(a, dist: Dist):
     check(lib.tt_set_option(ctx, native.TT_OPTION_GRAPHS, 0 if a.host_loop else 1))
     tuning = None
     if not a.no_autotune and a.integrator == "wavefront" and not a.slots:
-        t = r.autotune(sample_count=16)  # short 16-spp renders of the same frame, before the warm-up
+        # renders of the same frame at its own sample count (up to 64, one sample chunk), before the
+        # warm-up: shorter tuning renders rank pools that the full frame ranks otherwise
+        tune_spp = min(spp, 64)
+        t = r.autotune(sample_count=tune_spp)
         tuning = {"slots": t.slots, "refill_lanes": t.refill_lanes, "trace_blocks_per_sm": t.trace_blocks_per_sm,
-                  "renders": t.renders, "tune_spp": 16, "default_ms": t.default_ms, "tuned_ms": t.best_ms}
+                  "renders": t.renders, "tune_spp": tune_spp, "default_ms": t.default_ms, "tuned_ms": t.best_ms}
     for _ in range(a.warmup):
         step()
     check(lib.tt_synchronize(ctx))
@@ -1137,8 +1140,8 @@ def run_ours(a, dist: Dist):
         launches_per_step = int(stage_launches.sum()) // a.steps
     else:  # graph loop: regen, control, extend, shade and shadow every iteration, then the reduction
         launches_per_step = 5 * regen_per_step + reduce_per_step + primary_per_step
-    if primary_per_step:  # the timed set-up counts once: instance, rectangle, scan and finish kernels
-        launches_per_step += 2 + scan_launches(int(stats.triangle_count) + 1)
+    if primary_per_step:  # the timed set-up counts once: instance, rectangle, two scans, listing and finish kernels
+        launches_per_step += 4 + 2 * scan_launches(int(stats.triangle_count) + 1)
 
     # end to end through the public API: render_to_texture into pinned host memory
     host = ctypes.c_void_p()

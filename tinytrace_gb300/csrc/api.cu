@@ -97,7 +97,7 @@ struct WavefrontBuffers {
 // Rasterised primary visibility (primary.cu): per-record rectangles and pair counts, per-instance
 // bounds and the closest-hit keys of one sample chunk, grown on demand.
 struct PrimaryState {
-    DeviceBuffer key, rect, edge, count, inst, flags;  // flags: total (8 bytes), ok (4 bytes)
+    DeviceBuffer key, rect, edge, count, live_pos, live_rec, live_first, inst, flags;  // flags: total, ok, live_n, next
     uint64_t key_items = 0, records = 0, instances = 0;
 };
 
@@ -591,22 +591,30 @@ static void primary_buffers(tt_context* ctx, const tt_constants& c, const DevSce
         S.rect.alloc(16ull * sc.tri_count);
         S.edge.alloc(48ull * sc.tri_count);
         S.count.alloc(4ull * (sc.tri_count + 1ull));
+        S.live_pos.alloc(4ull * (sc.tri_count + 1ull));
+        S.live_rec.alloc(4ull * sc.tri_count);
+        S.live_first.alloc(4ull * (sc.tri_count + 1ull));
         S.records = (uint64_t)sc.tri_count + 1;
     }
     if (sc.instance_count > S.instances) {
         S.inst.alloc(sizeof(PrimaryInstance) * (uint64_t)sc.instance_count);
         S.instances = sc.instance_count;
     }
-    if (!S.flags.ptr) S.flags.alloc(16);
+    if (!S.flags.ptr) S.flags.alloc(32);
     v.key = S.key.as<unsigned long long>();
     v.rect = S.rect.as<float4>();
     v.edge = S.edge.as<float4>();
     v.count = S.count.as<uint32_t>();
+    v.live_pos = S.live_pos.as<uint32_t>();
+    v.live_rec = S.live_rec.as<uint32_t>();
+    v.live_first = S.live_first.as<uint32_t>();
     v.total = S.flags.as<unsigned long long>();
     v.ok = reinterpret_cast<uint32_t*>(S.flags.as<unsigned char>() + 8);
+    v.live_n = reinterpret_cast<uint32_t*>(S.flags.as<unsigned char>() + 12);
+    v.next = reinterpret_cast<uint32_t*>(S.flags.as<unsigned char>() + 16);
     v.inst = S.inst.as<PrimaryInstance>();
     v.records = sc.tri_count;
-    v.raster_blocks = std::max(1, ctx->occupancy_sms) * 8;
+    v.sms = std::max(1, ctx->occupancy_sms);
 }
 
 namespace tt {

@@ -302,6 +302,29 @@ __global__ void primary_finish_kernel(const __grid_constant__ PrimaryParams v) {
     *v.ok = *v.total < PAIR_LIMIT ? 1u : 0u;
 }
 
+// The records with pixels, listed densely (after the scan of the counts): each has at least one
+// pair, so the 32 pairs a warp takes lie in at most 32 consecutive listed records.
+__global__ void primary_live_flag_kernel(const __grid_constant__ PrimaryParams v) {
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > v.records) return;
+    v.live_pos[r] = r < v.records && v.count[r + 1] > v.count[r] ? 1u : 0u;
+}
+__global__ void primary_live_scatter_kernel(const __grid_constant__ PrimaryParams v) {
+    uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > v.records) return;
+    if (r == v.records) {
+        const uint32_t n = v.live_pos[r];
+        *v.live_n = n;
+        v.live_first[n] = v.count[r];
+        return;
+    }
+    if (v.count[r + 1] > v.count[r]) {
+        const uint32_t i = v.live_pos[r];
+        v.live_rec[i] = r;
+        v.live_first[i] = v.count[r];
+    }
+}
+
 __device__ __forceinline__ bool inside_edge(float4 e, float px, float py) {
     return __fmaf_rn(e.x, px, __fmaf_rn(e.y, py, e.z)) >= 0.0f;
 }
@@ -315,19 +338,20 @@ __device__ __forceinline__ bool inside_edge(float4 e, float px, float py) {
 __global__ void __launch_bounds__(RASTER_BLOCK) primary_raster_kernel(const __grid_constant__ RenderParams p,
                                                                       const __grid_constant__ PrimaryParams v,
                                                                       uint32_t chunk_sample0, uint32_t chunk_spp,
-                                                                      const __grid_constant__ XsJump jump) {
+                                                                      const __grid_constant__ XsJump jump,
+                                                                      uint32_t range_pairs) {
     __shared__ unsigned long long s_queue[RASTER_WARPS][QUEUE_CAP];
     if (*v.ok == 0u) return;
     const tt_constants& c = p.c;
     const DevScene& sc = p.sc;
     const uint32_t W = c.screen_size[0], H = c.screen_size[1];
     const uint64_t WH = (uint64_t)W * H;
-    const uint32_t total = v.count[v.records];
+    const uint32_t live = *v.live_n;
+    const uint32_t total = v.live_first[live];
     const uint32_t frame_hash = jenkins_hash(c.frame_index);
     const f3 camera = f3{c.camera_position[0], c.camera_position[1], c.camera_position[2]};
     const uint32_t lane = threadIdx.x & 31u;
     unsigned long long* queue = s_queue[threadIdx.x >> 5];
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
 
     // tests queue entry `e` (have: the lane holds one) of the pair of lane e & 31; every lane calls
     auto test = [&](unsigned long long e, bool have, uint32_t rec, uint32_t x, uint32_t y, uint32_t t, uint32_t tri) {
@@ -356,70 +380,106 @@ __global__ void __launch_bounds__(RASTER_BLOCK) primary_raster_kernel(const __gr
         if (key < *dst) atomicMin(dst, key);
     };
 
-    for (uint32_t base = warp * 32u; base < total; base += warps * 32u) {
-        const uint32_t k = base + lane;
-        const bool valid = k < total;
-        uint32_t rec = 0u, x = 0u, y = 0u, t = 0u, tri = 0u, pg = 0u;
-        float4 rect = make_float4(1.0f, 1.0f, 0.0f, 0.0f), e0 = rect, e1 = rect, e2 = rect;
-        if (valid) {
-            uint32_t lo = 0u, hi = v.records;  // count[lo] <= k < count[hi]
+    // warps claim ranges of pairs (a multiple of 32: about six ranges per warp of the wave, at most
+    // range_pairs, fewer when the pairs carry more samples, so that the last ranges end
+    // together) and take them 32 at a time: one search for the range's first listed record, then
+    // each batch's first record follows from the previous batch's last
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t share = (uint32_t)(((uint64_t)total / (6ull * warps) + 31ull) & ~31ull);
+    const uint32_t range = share < 128u ? 128u : (share > range_pairs ? range_pairs : share);
+    while (true) {
+        uint32_t begin = 0u;
+        if (lane == 0u) begin = atomicAdd(v.next, range);
+        begin = __shfl_sync(0xffffffffu, begin, 0);
+        if (begin >= total) break;
+        const uint32_t end = total - begin > range ? begin + range : total;
+        uint32_t r0 = 0u;
+        if (lane == 0u) {
+            uint32_t lo = 0u, hi = live;  // live_first[lo] <= begin < live_first[hi]
             while (hi - lo > 1u) {
                 uint32_t mid = (lo + hi) >> 1;
-                if (__ldg(v.count + mid) <= k) lo = mid;
+                if (__ldg(v.live_first + mid) <= begin) lo = mid;
                 else hi = mid;
             }
-            rec = lo;
-            rect = v.rect[rec];
-            e0 = v.edge[3ull * rec];
-            e1 = v.edge[3ull * rec + 1];
-            e2 = v.edge[3ull * rec + 2];
-            int x0, x1, y0, y1;
-            pixel_span(rect.x, rect.z, W, x0, x1);
-            pixel_span(rect.y, rect.w, H, y0, y1);
-            const uint32_t bw = (uint32_t)(x1 - x0 + 1);
-            const uint32_t j = k - __ldg(v.count + rec);
-            x = (uint32_t)x0 + j % bw;
-            y = (uint32_t)y0 + j / bw;
-            t = band_index(x, y, W, H);
-            const uint32_t prim = __float_as_uint(__ldg(sc.tris + 3ull * rec).w);
-            const uint32_t inst = __float_as_uint(__ldg(sc.tris + 3ull * rec + 1).w);
-            tri = __ldg(sc.tri_base + inst) + prim;
-            pg = jenkins_hash((x + y * W) ^ frame_hash);
-            if (chunk_sample0) pg = xs_apply(jump, pg);
+            r0 = lo;
         }
-        uint32_t queued = 0u;  // warp-uniform
-        for (uint32_t s0 = 0; s0 < chunk_spp; s0 += SAMPLE_GROUP) {
-#pragma unroll
-            for (uint32_t j = 0; j < (uint32_t)SAMPLE_GROUP; ++j) {
-                const uint32_t s = s0 + j;
-                bool in = false;
-                uint32_t mx = 0u, my = 0u;
-                if (valid && s < chunk_spp) {
-                    // the draws of pixel_ndc: the generator ends two steps on, at the next sample's
-                    mx = random_mantissa(pg);
-                    my = random_mantissa(pg);
-                    const float px = (float)x + (mantissa_float(mx) - 0.5f), py = (float)y + (mantissa_float(my) - 0.5f);
-                    in = px >= rect.x && px <= rect.z && py >= rect.y && py <= rect.w && inside_edge(e0, px, py) &&
-                         inside_edge(e1, px, py) && inside_edge(e2, px, py);
+        r0 = __shfl_sync(0xffffffffu, r0, 0);
+        for (uint32_t base = begin; base < end; base += 32u) {
+            const uint32_t k = base + lane;
+            const bool valid = k < end;
+            uint32_t rec = 0u, x = 0u, y = 0u, t = 0u, tri = 0u, pg = 0u;
+            float4 rect = make_float4(1.0f, 1.0f, 0.0f, 0.0f), e0 = rect, e1 = rect, e2 = rect;
+            // each lane's listed record within the 32 from r0 (the record of pair `base`):
+            // live_first[r0 + i] >= base + i for i >= 1, so pair base + 31 lies before r0 + 32
+            const uint32_t window = r0 + lane < live ? __ldg(v.live_first + r0 + lane) : 0xffffffffu;
+            uint32_t wlo = 0u, whi = 32u;  // window[wlo] <= k < window[whi] (window[32] > base + 31)
+    #pragma unroll
+            for (int step = 0; step < 5; ++step) {
+                const uint32_t mid = (wlo + whi) >> 1;
+                const uint32_t wv = __shfl_sync(0xffffffffu, window, mid);
+                if (wv <= k) wlo = mid;
+                else whi = mid;
+            }
+            const uint32_t first = __shfl_sync(0xffffffffu, window, wlo);
+            if (valid) {
+                rec = __ldg(v.live_rec + r0 + wlo);
+                rect = v.rect[rec];
+                e0 = v.edge[3ull * rec];
+                e1 = v.edge[3ull * rec + 1];
+                e2 = v.edge[3ull * rec + 2];
+                int x0, x1, y0, y1;
+                pixel_span(rect.x, rect.z, W, x0, x1);
+                pixel_span(rect.y, rect.w, H, y0, y1);
+                const uint32_t bw = (uint32_t)(x1 - x0 + 1);
+                const uint32_t j = k - first;
+                x = (uint32_t)x0 + j % bw;
+                y = (uint32_t)y0 + j / bw;
+                t = band_index(x, y, W, H);
+                const uint32_t prim = __float_as_uint(__ldg(sc.tris + 3ull * rec).w);
+                const uint32_t inst = __float_as_uint(__ldg(sc.tris + 3ull * rec + 1).w);
+                tri = __ldg(sc.tri_base + inst) + prim;
+                pg = jenkins_hash((x + y * W) ^ frame_hash);
+                if (chunk_sample0) pg = xs_apply(jump, pg);
+            }
+            uint32_t queued = 0u;  // warp-uniform
+            for (uint32_t s0 = 0; s0 < chunk_spp; s0 += SAMPLE_GROUP) {
+    #pragma unroll
+                for (uint32_t j = 0; j < (uint32_t)SAMPLE_GROUP; ++j) {
+                    const uint32_t s = s0 + j;
+                    bool in = false;
+                    uint32_t mx = 0u, my = 0u;
+                    if (valid && s < chunk_spp) {
+                        // the draws of pixel_ndc: the generator ends two steps on, at the next sample's
+                        mx = random_mantissa(pg);
+                        my = random_mantissa(pg);
+                        const float px = (float)x + (mantissa_float(mx) - 0.5f), py = (float)y + (mantissa_float(my) - 0.5f);
+                        in = px >= rect.x && px <= rect.z && py >= rect.y && py <= rect.w && inside_edge(e0, px, py) &&
+                             inside_edge(e1, px, py) && inside_edge(e2, px, py);
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, in);
+                    if (in)
+                        queue[queued + __popc(m & lanes_below())] =
+                            lane | (s << 5) | ((unsigned long long)mx << 11) | ((unsigned long long)my << 34);
+                    queued += __popc(m);
                 }
-                const uint32_t m = __ballot_sync(0xffffffffu, in);
-                if (in)
-                    queue[queued + __popc(m & lanes_below())] =
-                        lane | (s << 5) | ((unsigned long long)mx << 11) | ((unsigned long long)my << 34);
-                queued += __popc(m);
+                __syncwarp();
+                while (queued >= 32u) {
+                    queued -= 32u;
+                    test(queue[queued + lane], true, rec, x, y, t, tri);
+                }
+                __syncwarp();
+            }
+            if (queued) {
+                const bool have = lane < queued;
+                test(have ? queue[lane] : 0ull, have, rec, x, y, t, tri);
             }
             __syncwarp();
-            while (queued >= 32u) {
-                queued -= 32u;
-                test(queue[queued + lane], true, rec, x, y, t, tri);
-            }
-            __syncwarp();
+            // the record of pair base + 32: lane 31's record, or the next one if that starts there
+            const uint32_t last = r0 + __shfl_sync(0xffffffffu, wlo, 31);
+            uint32_t next = last;
+            if (lane == 0u && last + 1u < live && __ldg(v.live_first + last + 1u) <= base + 32u) next = last + 1u;
+            r0 = __shfl_sync(0xffffffffu, next, 0);
         }
-        if (queued) {
-            const bool have = lane < queued;
-            test(have ? queue[lane] : 0ull, have, rec, x, y, t, tri);
-        }
-        __syncwarp();
     }
 }
 
@@ -481,6 +541,10 @@ void primary_setup(const RenderParams& p, const PrimaryParams& v, cudaStream_t s
                                                                                    p.c.screen_size[1]);
     check_cuda(cudaGetLastError(), "primary bounds");
     exclusive_scan_u32(v.count, (uint64_t)v.records + 1, st);
+    const unsigned g = (unsigned)((v.records + 1ull + 255) / 256);
+    primary_live_flag_kernel<<<g, 256, 0, st>>>(v);
+    exclusive_scan_u32(v.live_pos, (uint64_t)v.records + 1, st);
+    primary_live_scatter_kernel<<<g, 256, 0, st>>>(v);
     primary_finish_kernel<<<1, 1, 0, st>>>(v);
     check_cuda(cudaGetLastError(), "primary finish");
 }
@@ -488,9 +552,15 @@ void primary_setup(const RenderParams& p, const PrimaryParams& v, cudaStream_t s
 void primary_chunk(const RenderParams& p, const PrimaryParams& v, const WfParams& w, cudaStream_t st) {
     uint64_t WH = (uint64_t)p.c.screen_size[0] * p.c.screen_size[1];
     check_cuda(cudaMemsetAsync(v.key, 0xff, 8ull * WH * w.chunk_spp, st), "memset");
+    check_cuda(cudaMemsetAsync(v.next, 0, 4, st), "memset");
+    // one wave of resident blocks; ranges of at most 512 / spp batches (8..128)
+    int occupancy = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occupancy, primary_raster_kernel, RASTER_BLOCK, 0),
+               "occupancy");
+    const uint32_t batches = std::min<uint32_t>(128u, std::max<uint32_t>(8u, 512u / std::max(w.chunk_spp, 1u)));
     if (v.records)
-        primary_raster_kernel<<<v.raster_blocks, RASTER_BLOCK, 0, st>>>(p, v, w.chunk_sample0, w.chunk_spp,
-                                                                        w.chunk_jump);
+        primary_raster_kernel<<<v.sms * std::max(occupancy, 1), RASTER_BLOCK, 0, st>>>(
+            p, v, w.chunk_sample0, w.chunk_spp, w.chunk_jump, 32u * batches);
     check_cuda(cudaGetLastError(), "primary raster");
 }
 

@@ -96,7 +96,8 @@ struct tt_server {
     DeviceBuffer d_reqs, d_scenes, d_round, d_batch_err;
     // rasterised camera-ray keys of flat-BVH4 rounds: one key per work item of the round, and the
     // per-request bound buffers (reused request after request) with per-request total/ok words
-    DeviceBuffer keys, prim_rect, prim_edge, prim_count, prim_inst, prim_flags;
+    DeviceBuffer keys, prim_rect, prim_edge, prim_count, prim_live_pos, prim_live_rec, prim_live_first, prim_inst,
+        prim_flags;
     uint64_t key_items = 0, prim_records = 0, prim_instances = 0;
     int occupancy_sms = 0;
     bool primary = true;  // the context's TT_OPTION_PRIMARY_VISIBILITY at creation is TT_PRIMARY_RASTER
@@ -349,13 +350,16 @@ void tt_server::launch_round(std::vector<Request*>& live) {
             prim_rect.alloc(16ull * recs);
             prim_edge.alloc(48ull * recs);
             prim_count.alloc(4ull * (recs + 1));
+            prim_live_pos.alloc(4ull * (recs + 1));
+            prim_live_rec.alloc(4ull * recs);
+            prim_live_first.alloc(4ull * (recs + 1));
             prim_records = recs + 1;
         }
         if (insts > prim_instances) {
             prim_inst.alloc(sizeof(PrimaryInstance) * insts);
             prim_instances = insts;
         }
-        if (!prim_flags.ptr) prim_flags.alloc(16ull * BATCH_MAX_REQUESTS);
+        if (!prim_flags.ptr) prim_flags.alloc(32ull * BATCH_MAX_REQUESTS);
         if (occupancy_sms == 0)
             check_cuda(cudaDeviceGetAttribute(&occupancy_sms, cudaDevAttrMultiProcessorCount, device), "sm count");
         bool all = n > 0;
@@ -373,11 +377,16 @@ void tt_server::launch_round(std::vector<Request*>& live) {
             v.rect = prim_rect.as<float4>();
             v.edge = prim_edge.as<float4>();
             v.count = prim_count.as<uint32_t>();
-            v.total = reinterpret_cast<unsigned long long*>(prim_flags.as<unsigned char>() + 16ull * k);
-            v.ok = reinterpret_cast<uint32_t*>(prim_flags.as<unsigned char>() + 16ull * k + 8);
+            v.live_pos = prim_live_pos.as<uint32_t>();
+            v.live_rec = prim_live_rec.as<uint32_t>();
+            v.live_first = prim_live_first.as<uint32_t>();
+            v.total = reinterpret_cast<unsigned long long*>(prim_flags.as<unsigned char>() + 32ull * k);
+            v.ok = reinterpret_cast<uint32_t*>(prim_flags.as<unsigned char>() + 32ull * k + 8);
+            v.live_n = reinterpret_cast<uint32_t*>(prim_flags.as<unsigned char>() + 32ull * k + 12);
+            v.next = reinterpret_cast<uint32_t*>(prim_flags.as<unsigned char>() + 32ull * k + 16);
             v.inst = prim_inst.as<PrimaryInstance>();
             v.records = r.sc.tri_count;
-            v.raster_blocks = std::max(1, occupancy_sms) * 8;
+            v.sms = std::max(1, occupancy_sms);
             RenderParams rp{};
             rp.sc = r.sc;
             rp.c = r.c;

@@ -183,14 +183,19 @@ struct PrimaryParams {
     float4* edge;                // per record: 3 edge functions (a, b, c, 0); a sample at pixel position
                                  // (x, y) can hit the record only where a x + b y + c >= 0 for all three
     uint32_t* count;             // records + 1: pixels of each rectangle, then their exclusive prefix
+    uint32_t* live_pos;          // records + 1: 1 per record with pixels, then their exclusive prefix
+    uint32_t* live_rec;          // per record with pixels (in record order): its record
+    uint32_t* live_first;        // per record with pixels: its first pair; then the total pairs
     unsigned long long* total;   // pixel-record pairs of the frame
     uint32_t* ok;                // 1 when the keys are complete (the extension kernel reads them)
+    uint32_t* live_n;            // records with pixels
+    uint32_t* next;              // first pair of the next range the key pass hands out
     PrimaryInstance* inst;       // per instance
     double B[9];                 // row-major: (ndc.x, ndc.y, 1) -> world direction of the camera ray
     double lambda_clip;          // no camera ray hits where lambda < lambda_clip
     double pixel_scale;          // pixels per radian of direction error, an upper bound
     uint32_t records;
-    int raster_blocks;           // grid of the persistent raster kernel
+    int sms;                     // multiprocessors (the key pass runs one wave of resident blocks)
 };
 // Camera terms of `c` for primary visibility; false when the camera's ray map is singular.
 bool primary_camera(const tt_constants& c, PrimaryParams& v);
