@@ -96,6 +96,30 @@ def test_requests_in_the_mix_equal_alone(ctx, round_items, policy):
         assert_same_bits(alone[k], oracle.OracleScene(sc[name][0]).render(consts[k]), f"oracle {k}")
 
 
+@pytest.mark.parametrize("primary", [native.TT_PRIMARY_RASTER, native.TT_PRIMARY_TRAVERSE])
+def test_flat_rounds_with_camera_keys(ctx, primary):
+    """Rounds whose scenes are all flat BVH4 take camera-ray hits from per-request rasterised
+    keys (TT_PRIMARY_RASTER, the context's setting when the server is created) or traverse them;
+    the images are tt_render's either way, over rounds that carry several requests' chunks."""
+    sc = {k: v for k, v in _scenes().items() if k in ("cornell", "field", "instanced")}
+    handles = _create(ctx, sc)
+    rng = np.random.default_rng(5)
+    reqs = [r for r in _requests(rng, 12) if r[0] in sc]
+    consts = [make_constants(sc[name][1], ext, cfg, frame, 0) for name, ext, cfg, frame in reqs]
+    alone = [_alone(ctx, handles[name], c) for (name, _, _, _), c in zip(reqs, consts)]
+    check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_PRIMARY_VISIBILITY, primary))
+    try:
+        with RenderServer(ctx, max_inflight=4, pool_paths=1 << 14, round_items=30_000) as srv:
+            ids = [srv.submit(handles[name], c) for (name, _, _, _), c in zip(reqs, consts)]
+            imgs = [srv.wait(i) for i in ids]
+            st = srv.stats()
+    finally:
+        check(ctx.lib.tt_set_option(ctx.handle, native.TT_OPTION_PRIMARY_VISIBILITY, native.TT_PRIMARY_RASTER))
+    assert st.completed == len(reqs) and st.failed == 0 and st.peak_inflight >= 2
+    for k, (a, b) in enumerate(zip(alone, imgs)):
+        assert_same_bits(b, a, f"request {k} {reqs[k]}")
+
+
 def _arena_bytes(w, h, spp, round_items=1 << 26):
     """Mirror of the server's per-request arena (server.cu, arena_bytes): the per-sample radiance
     of the largest chunk, running sums, image, error word."""
