@@ -17,6 +17,12 @@
 namespace tt {
 
 constexpr int RT_TILE_X = 16, RT_TILE_Y = 8, RT_BLOCK = RT_TILE_X * RT_TILE_Y;
+// resident blocks per SM the candidate, reuse and shading passes are compiled for (a register cap
+// of 102): 5 blocks took the 1080p frame from 5.55 to 5.31 ms against the uncapped 105 registers
+// (4 blocks)
+#ifndef TT_RESTIR_MIN_BLOCKS
+#define TT_RESTIR_MIN_BLOCKS 5
+#endif
 constexpr uint32_t PASS_INITIAL = 1u, PASS_TEMPORAL = 2u, PASS_SPATIAL = 3u;
 
 __device__ __forceinline__ bool pixel_of_thread(const tt_constants& c, uint32_t& x, uint32_t& y) {
@@ -203,7 +209,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
 }
 
 template <bool TEX, int ACCEL>
-__global__ void __launch_bounds__(RT_BLOCK) restir_initial_kernel(const __grid_constant__ RenderParams p,
+__global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_initial_kernel(const __grid_constant__ RenderParams p,
                                                                   const __grid_constant__ RestirParams rp,
                                                                   const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   Reservoir* out, uint32_t candidates) {
@@ -290,7 +296,7 @@ __device__ __forceinline__ bool similar(const Surface& q, f3 normal, float dist)
 }
 
 template <bool TEX, int ACCEL>
-__global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_constant__ RenderParams p,
+__global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_temporal_kernel(const __grid_constant__ RenderParams p,
                                                                    const __grid_constant__ RestirHistory hist,
                                                                    const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                    const Surface* prev_gbuf,
@@ -325,7 +331,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_temporal_kernel(const __grid_
 }
 
 template <bool TEX, int ACCEL>
-__global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_constant__ RenderParams p,
+__global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_spatial_kernel(const __grid_constant__ RenderParams p,
                                                                   const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                   const Reservoir* in,
                                                                   Reservoir* out, uint32_t neighbours, float radius) {
@@ -362,7 +368,7 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_spatial_kernel(const __grid_c
 }
 
 template <bool TEX, int ACCEL>
-__global__ void __launch_bounds__(RT_BLOCK) restir_shade_kernel(const __grid_constant__ RenderParams p,
+__global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_shade_kernel(const __grid_constant__ RenderParams p,
                                                                 const __grid_constant__ RestirParams rp,
                                                                 const Surface* gbuf, const float4* gtex, const float4* glob,
                                                                 const Reservoir* res) {

@@ -462,8 +462,10 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
 #undef TT_SC
 #undef TT_ERR
 
+// 8 resident blocks (64 registers, 32 warps per SM): shade 20.6 -> 19.5 ms per 1080p frame against
+// 6 blocks (80 registers), despite more spilling; 10 and 12 blocks gave 19.6 and 19.8 ms
 #ifndef TT_SHADE_MIN_BLOCKS
-#define TT_SHADE_MIN_BLOCKS 6
+#define TT_SHADE_MIN_BLOCKS 8
 #endif
 // MULTI: a shared-pool round; each path shades with its request's Constants and scene.
 template <bool CACHE, bool TEX, bool MULTI = false>
