@@ -985,8 +985,8 @@ def run_serving(a, ctx) -> dict:
     """Continuous batching under the C4 request mix on five resident scenes (1e3 .. 5e6
     triangles), HBM budget 150 GB, smallest-first scheduling (a.serve_policy), up to 16 requests
     rendered together per round through one
-    shared path pool whose size tt_autotune picks on a request of the mix (the 260k-triangle
-    scene at 1024 x 1024, 4 spp, depth 8).  First the server's capacity: a batch of
+    shared path pool whose size tt_autotune picks on a render as large as a round (the
+    260k-triangle scene at 2048 x 2048, 16 spp, depth 8).  First the server's capacity: a batch of
     a.serve_batch requests submitted at once gives the saturated sample throughput, which over
     the mix's mean request size gives requests per second.  Then
     Poisson arrivals at fractions of that capacity: a.serve_requests requests at 0.8 x capacity and
@@ -1007,15 +1007,18 @@ def run_serving(a, ctx) -> dict:
         pool.append((arr.triangle_count, ctx.create_scene(arr)))
     logs = np.log10([t for t, _ in pool])
     cam = scenes.Camera.looking_at((0.0, 10.0, 95.0), (0, 0, 0))
-    img = ctx.create_image(native.TT_LIFETIME_FRAME, 1024, 1024)
+    # tuned on a render as large as a round (2048 x 2048 x 16 spp = 2^26 work items), so that the
+    # pool sizes a round needs are among the candidates and the ranking is not decided by noise
+    img = ctx.create_image(native.TT_LIFETIME_FRAME, 2048, 2048)
     tune = native.TuneResult()
-    c = make_constants(cam, (1024, 1024), Config(bounce_count=8, sample_count=4), 0, 0)
+    c = make_constants(cam, (2048, 2048), Config(bounce_count=8, sample_count=16), 0, 0)
     check(ctx.lib.tt_autotune(ctx.handle, pool[2][1], native.ptr(c), img, ctypes.byref(tune)))
     pool_paths = int(tune.slots)
     out = {"scenes_triangles": [int(t) for t, _ in pool], "hbm_budget_gb": 150, "max_inflight": a.serve_inflight,
            "policy": a.serve_policy,
-           "pool_paths": pool_paths, "pool_tuning": {"tune_spp": 4, "default_ms": tune.default_ms,
-                                                     "tuned_ms": tune.best_ms, "renders": int(tune.renders)},
+           "pool_paths": pool_paths, "pool_tuning": {"extent": [2048, 2048], "tune_spp": 16,
+                                                     "default_ms": tune.default_ms, "tuned_ms": tune.best_ms,
+                                                     "renders": int(tune.renders)},
            "round_items": 1 << 26,
            "mix": "side ~U{256..2048} step 16, spp ~U{1..256}, depth 8, scene log-uniform 1e3..5e6 triangles"}
     policy = {"fair": native.TT_SERVER_POLICY_FAIR, "smallest_first": native.TT_SERVER_POLICY_SMALLEST_FIRST}[
