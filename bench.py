@@ -332,7 +332,7 @@ def row_parity(gpu: np.ndarray, cpu: np.ndarray, rows: list[int]) -> dict:
     return {"rows": len(rows), "pixels": int(g.shape[0] * g.shape[1]), "values_compared": int(g.size),
             "values_differing": int((~same).sum()), "max_rel_err": float(np.nanmax(rel)) if rel.size else 0.0,
             "bit_exact": bool(same.all()), "frame": "frame index 0, accumulated frame count 0 (no accumulation)",
-            "tolerance": "bit for bit (NaN payloads aside); the north-star bar is 1e-4 relative"}
+            "tolerance": "bit for bit (NaN payloads aside); the parity bar is 1e-4 relative per pixel"}
 
 
 def run_reference(a, dist: Dist):
