@@ -10,22 +10,31 @@
 // (tri_base[instance] + primitive) orders as (instance, primitive), so the smallest key is the
 // hit the traversal's closest-hit rule selects, whatever the order of the tests.
 //
-// The rectangle is conservative:
+// The bound of a record is conservative:
 //   * the sample's direction is d = normalize(B (ndc.x, ndc.y, 1)) with B from the inverse
 //     projection and view matrices (camera_ray_direction), so in an instance's object space a
 //     point p on a camera ray satisfies C^-1 (p - oo) = lambda (ndc.x, ndc.y, 1), C = X B (X the
 //     object-from-world 3x3), lambda = t / |B (ndc, 1)| > 0: the record's vertices, mapped this
-//     way in double precision, project to the ndc the rays through them have;
+//     way, project to the ndc of the rays through them (C^-1 per instance in double precision,
+//     the per-record projection in float; records that cross lambda_clip in double);
 //   * oo is the float origin instance_ray computes, so the bound and the test share the origin;
-//   * the rectangle is widened by BASE_MARGIN_PX (the float rounding of the camera ray and of the
-//     ray/triangle test is ~1e-3 pixel) plus COND_MARGIN x the condition number of X x the pixels
-//     per radian of the camera (the direction error an ill-conditioned instance matrix can add);
+//   * the pixel-position rectangle and the three edge functions of the projected triangle are
+//     widened by a margin: BASE_MARGIN_PX (the float rounding of the camera ray and of the
+//     ray/triangle test is ~1e-3 pixel), plus COND_MARGIN x cond(X) x the camera's pixels per
+//     radian (the direction error an ill-conditioned instance matrix adds to the float
+//     object-space ray), plus PROJ_MARGIN x cond(C) x the screen width (the float projection
+//     errs by at most ~17 eps cond(C) in ndc on screen); the edge functions also carry their own
+//     evaluation error;
 //   * parts of a record with lambda < lambda_clip (half the least lambda of a hit at tmin) are
-//     clipped away, so records that cross the camera plane keep a finite rectangle;
-//   * records facing away from the camera beyond a cosine of BACKFACE_COS are dropped (extension
-//     rays cull back faces, and such a record yields det < 0 for every camera ray);
-//   * an instance whose matrices are singular or non-finite has no bound: its records cover the
-//     whole screen.
+//     clipped away, so records that cross the camera plane keep a finite rectangle (and no edge
+//     functions);
+//   * records facing away from the camera beyond a cosine of BACKFACE_COS plus the rounding
+//     bound of their normal are dropped (extension rays cull back faces, and such a record
+//     yields det < 0 for every camera ray);
+//   * an instance whose matrices are singular, non-finite or too badly conditioned has no
+//     bound: its records cover the whole screen.
+// The key pass runs over (record, pixel) pairs of the records with pixels, listed densely;
+// samples that pass a record's rectangle and edges are queued per warp and tested 32 at a time.
 // If the frame's pixel-record pairs exceed PAIR_LIMIT the keys are not built (ok = 0) and the
 // extension kernel traverses the camera rays instead.
 #include <algorithm>
