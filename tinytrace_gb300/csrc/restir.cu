@@ -18,8 +18,8 @@ namespace tt {
 
 constexpr int RT_TILE_X = 16, RT_TILE_Y = 8, RT_BLOCK = RT_TILE_X * RT_TILE_Y;
 // resident blocks per SM the candidate, reuse and shading passes are compiled for (a register cap
-// of 80): the 1080p frame took 5.55 ms uncapped (105 registers, 4 blocks), 5.26 ms at 5 blocks
-// and 5.15 ms at 6, despite some spilling
+// of 80): the 1080p frame took 5.55 ms uncapped (105 registers, 4 blocks), 5.26 ms at 5 blocks,
+// 5.15 ms at 6 despite some spilling, and 5.33 ms at 7
 #ifndef TT_RESTIR_MIN_BLOCKS
 #define TT_RESTIR_MIN_BLOCKS 6
 #endif
