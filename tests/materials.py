@@ -5,6 +5,10 @@ from tinytrace_gb300.asset import Material
 
 
 def material_suite(seed: int = 3, count: int = 24) -> list:
+    return [m.constants() for m in material_objects(seed, count)]
+
+
+def material_objects(seed: int = 3, count: int = 24) -> list:
     rng = np.random.default_rng(seed)
     mats = [
         Material(),  # reference defaults: dielectric base + specular
@@ -43,7 +47,7 @@ def material_suite(seed: int = 3, count: int = 24) -> list:
             fuzz_color=tuple(rng.uniform(0.5, 1.0, 3)),
             fuzz_roughness=float(rng.uniform()),
         ))
-    return [m.constants() for m in mats]
+    return mats
 
 
 def random_directions(rng, n: int) -> np.ndarray:

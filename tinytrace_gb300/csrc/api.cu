@@ -244,25 +244,20 @@ void upload(DeviceBuffer& b, const T* host, uint64_t count, cudaStream_t st) {
     if (count) check_cuda(cudaMemcpyAsync(b.ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
 }
 
-// Which shading code a material runs: the OpenPBR lobes that can carry weight, NEE eligibility
-// (integrate.glsl:293-295) and emission.  Hits on materials with equal signatures share one
-// shading queue of the wavefront integrator.
+// Which shading code a material runs: the OpenPBR lobes that can carry weight (lobe_set_of,
+// bits 0-5), NEE eligibility (integrate.glsl:293-295) and emission.  Hits on materials with
+// equal signatures share one shading queue of the wavefront integrator.
 uint32_t shading_signature(const tt_material_constants& m) {
-    uint32_t sig = 0u;
-    if (m.fuzz_weight > 0.0f) sig |= 1u;
-    if (m.coat_weight > 0.0f) sig |= 2u;
-    if (m.base_metalness > 0.0f) sig |= 4u;
-    if (m.base_metalness < 1.0f && m.specular_weight > 0.0f) sig |= 8u;
-    if (m.base_metalness < 1.0f && m.transmission_weight > 0.0f) sig |= 16u;
-    if (m.base_metalness < 1.0f && m.transmission_weight < 1.0f) sig |= 32u;
+    uint32_t sig = lobe_set_of(m);
     if (m.specular_roughness > 0.15f) sig |= 64u;
     if (m.emission_luminance > 0.0f) sig |= 128u;
     return sig;
 }
 
 // Shading-queue bucket per instance: the HIT_BUCKETS - 1 signatures covering the most
-// instanced triangles get their own bucket, all others share the last one.
-std::vector<uint8_t> instance_buckets(const tt_scene_desc* d) {
+// instanced triangles get their own bucket, all others share the last one.  `lobes` receives
+// byte b = the union of the lobe sets of bucket b's signatures (the shade kernel's variant).
+std::vector<uint8_t> instance_buckets(const tt_scene_desc* d, uint32_t& lobes) {
     std::map<uint32_t, uint64_t> weight;
     std::vector<uint32_t> sig(d->instance_count);
     for (uint32_t i = 0; i < d->instance_count; ++i) {
@@ -276,7 +271,11 @@ std::vector<uint8_t> instance_buckets(const tt_scene_desc* d) {
     std::map<uint32_t, uint8_t> bucket;
     for (size_t k = 0; k < order.size(); ++k) bucket[order[k].second] = (uint8_t)std::min<size_t>(k, HIT_BUCKETS - 1);
     std::vector<uint8_t> out(std::max<uint32_t>(d->instance_count, 1), 0);
-    for (uint32_t i = 0; i < d->instance_count; ++i) out[i] = bucket[sig[i]];
+    lobes = 0u;
+    for (uint32_t i = 0; i < d->instance_count; ++i) {
+        out[i] = bucket[sig[i]];
+        lobes |= (sig[i] & LOBE_SET_ALL) << (8u * out[i]);
+    }
     return out;
 }
 
@@ -994,7 +993,8 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
             xf[4ull * i + 3] = v;
         }
         upload(s->inst_xform, xf.data(), xf.size(), st);
-        std::vector<uint8_t> buckets = instance_buckets(d);
+        uint32_t bucket_lobes = 0u;
+        std::vector<uint8_t> buckets = instance_buckets(d, bucket_lobes);
         upload(s->inst_bucket, buckets.data(), buckets.size(), st);
         BuildInput bi{s->positions.as<int16_t>(), s->indices.as<uint32_t>(), d->meshes, d->mesh_count,
                       d->instances, d->instance_count};
@@ -1031,6 +1031,7 @@ int32_t tt_scene_create(tt_context* ctx, const tt_scene_desc* d, tt_handle* out)
         ds.emissive = s->emissive.as<tt_emissive_triangle>();
         ds.inst_xform = s->inst_xform.as<float4>();
         ds.inst_bucket = s->inst_bucket.as<uint8_t>();
+        ds.bucket_lobes = bucket_lobes;
         ds.emissive_count = d->emissive_triangle_count;
         ds.instance_count = d->instance_count;
         s->light_rec.alloc(16ull * LIGHT_RECORD * std::max<uint32_t>(d->emissive_triangle_count, 1u));

@@ -467,24 +467,55 @@ struct Lobes {
     float probs[LOBE_COUNT];
 };
 
+// Lobe sets: bit i stands for lobe i.  A material can carry weight in lobe i only where the
+// albedo condition of bsdf_prepare holds for it (lobe_set_of); elsewhere the lobe's albedo is
+// zero, so its probability is zero (or NaN), it is never evaluated and never sampled.  The BSDF
+// functions below take the lobe set LS their callers' materials fall into and compile the lobes
+// outside it away: for every material whose lobe_set_of is a subset of LS they compute exactly
+// what the six-lobe code computes (same operations, same generator draws).
+constexpr uint32_t LOBE_SET_ALL = (1u << LOBE_COUNT) - 1u;
+constexpr uint32_t LOBE_SET_DIELECTRIC = (1u << SPEC_BRDF) | (1u << DIFFUSE);  // opaque, no coat or fuzz
+constexpr uint32_t LOBE_SET_METAL = 1u << METAL;                               // fully metallic
+constexpr uint32_t LOBE_SET_BASE = LOBE_SET_DIELECTRIC | LOBE_SET_METAL;        // partly metallic
+
+// The lobes whose albedo bsdf_prepare computes for material m (the conditions of bsdf.glsl:39-59).
+__host__ __device__ inline uint32_t lobe_set_of(const MatC& m) {
+    bool fully_metallic = m.base_metalness == 1.0f;
+    uint32_t set = 0u;
+    if (m.fuzz_weight > 0.0f) set |= 1u << FUZZ;
+    if (m.coat_weight > 0.0f) set |= 1u << COAT;
+    if (m.base_metalness > 0.0f) set |= 1u << METAL;
+    if (!fully_metallic) set |= 1u << SPEC_BRDF;
+    if (!fully_metallic && m.transmission_weight > 0.0f) set |= 1u << SPEC_BTDF;
+    if (!fully_metallic && m.transmission_weight != 1.0f) set |= 1u << DIFFUSE;
+    return set;
+}
+
+template <uint32_t LS, int LOBE>
+TT_HD constexpr bool has_lobe() { return (LS >> LOBE) & 1u; }
+
 // lobe_weights + lobe_probabilities (bsdf.glsl:33-120).  Albedos are needed only here.
+template <uint32_t LS = LOBE_SET_ALL>
 TT_HD Lobes bsdf_prepare(const MatC& m, f3 wi, uint32_t& g) {
     Lobes l;
     f3 alb[LOBE_COUNT];
     bool fully_metallic = m.base_metalness == 1.0f;
     bool fully_transmissive = m.transmission_weight == 1.0f;
-    alb[FUZZ] = m.fuzz_weight > 0.0f ? fuzz_brdf_albedo(m, wi) : splat(0.0f);
-    alb[COAT] = m.coat_weight > 0.0f ? coat_brdf_albedo(m, wi, g) : splat(0.0f);
-    alb[METAL] = m.base_metalness > 0.0f ? metal_brdf_albedo(m, wi, g) : splat(0.0f);
-    alb[SPEC_BRDF] = !fully_metallic ? specular_brdf_albedo(m, wi, g) : splat(0.0f);
-    alb[SPEC_BTDF] = !fully_metallic && m.transmission_weight > 0.0f ? specular_btdf_albedo(m, wi, g) : splat(0.0f);
-    alb[DIFFUSE] = !fully_metallic && !fully_transmissive ? diffuse_brdf_albedo(m, wi) : splat(0.0f);
+    alb[FUZZ] = has_lobe<LS, FUZZ>() && m.fuzz_weight > 0.0f ? fuzz_brdf_albedo(m, wi) : splat(0.0f);
+    alb[COAT] = has_lobe<LS, COAT>() && m.coat_weight > 0.0f ? coat_brdf_albedo(m, wi, g) : splat(0.0f);
+    alb[METAL] = has_lobe<LS, METAL>() && m.base_metalness > 0.0f ? metal_brdf_albedo(m, wi, g) : splat(0.0f);
+    alb[SPEC_BRDF] = has_lobe<LS, SPEC_BRDF>() && !fully_metallic ? specular_brdf_albedo(m, wi, g) : splat(0.0f);
+    alb[SPEC_BTDF] = has_lobe<LS, SPEC_BTDF>() && !fully_metallic && m.transmission_weight > 0.0f
+                         ? specular_btdf_albedo(m, wi, g)
+                         : splat(0.0f);
+    alb[DIFFUSE] = has_lobe<LS, DIFFUSE>() && !fully_metallic && !fully_transmissive ? diffuse_brdf_albedo(m, wi)
+                                                                                      : splat(0.0f);
 
     l.weights[FUZZ] = splat(m.fuzz_weight);
     f3 coated_base_weight = mix3(splat(1.0f), 1.0f - alb[FUZZ], m.fuzz_weight);
     l.weights[COAT] = coated_base_weight * m.coat_weight;
     f3 base_darkening = splat(1.0f);
-    if (m.coat_weight > 0.0f && m.coat_darkening > 0.0f) {
+    if (has_lobe<LS, COAT>() && m.coat_weight > 0.0f && m.coat_darkening > 0.0f) {
         float fresnel_weight = saturate(m.specular_weight * fresnel_at_normal_incident(specular_ior(m)));
         float dielectric_roughness = mixf(1.0f, m.specular_roughness, fresnel_weight);
         float base_roughness = mixf(dielectric_roughness, m.specular_roughness, m.base_metalness);
@@ -517,16 +548,20 @@ TT_HD Lobes bsdf_prepare(const MatC& m, f3 wi, uint32_t& g) {
     return l;
 }
 
+template <uint32_t LS = LOBE_SET_ALL>
 TT_HD f3 bsdf_evaluate_lobes(const MatC& m, const Lobes& l, f3 wi, f3 wo, int skip, float* dens) {
     f3 b = splat(0.0f);
-    if (skip != FUZZ && l.probs[FUZZ] > 0.0f) b += l.weights[FUZZ] * fuzz_brdf_evaluate(m, wi, wo, dens[FUZZ]);
-    if (skip != COAT && l.probs[COAT] > 0.0f) b += l.weights[COAT] * coat_brdf_evaluate(m, wi, wo, dens[COAT]);
-    if (skip != METAL && l.probs[METAL] > 0.0f) b += l.weights[METAL] * metal_brdf_evaluate(m, wi, wo, dens[METAL]);
-    if (skip != SPEC_BRDF && l.probs[SPEC_BRDF] > 0.0f)
+    if (has_lobe<LS, FUZZ>() && skip != FUZZ && l.probs[FUZZ] > 0.0f)
+        b += l.weights[FUZZ] * fuzz_brdf_evaluate(m, wi, wo, dens[FUZZ]);
+    if (has_lobe<LS, COAT>() && skip != COAT && l.probs[COAT] > 0.0f)
+        b += l.weights[COAT] * coat_brdf_evaluate(m, wi, wo, dens[COAT]);
+    if (has_lobe<LS, METAL>() && skip != METAL && l.probs[METAL] > 0.0f)
+        b += l.weights[METAL] * metal_brdf_evaluate(m, wi, wo, dens[METAL]);
+    if (has_lobe<LS, SPEC_BRDF>() && skip != SPEC_BRDF && l.probs[SPEC_BRDF] > 0.0f)
         b += l.weights[SPEC_BRDF] * specular_brdf_evaluate(m, wi, wo, dens[SPEC_BRDF]);
-    if (skip != DIFFUSE && l.probs[DIFFUSE] > 0.0f)
+    if (has_lobe<LS, DIFFUSE>() && skip != DIFFUSE && l.probs[DIFFUSE] > 0.0f)
         b += l.weights[DIFFUSE] * diffuse_brdf_evaluate(m, wi, wo, dens[DIFFUSE]);
-    if (skip != SPEC_BTDF && l.probs[SPEC_BTDF] > 0.0f)
+    if (has_lobe<LS, SPEC_BTDF>() && skip != SPEC_BTDF && l.probs[SPEC_BTDF] > 0.0f)
         b += l.weights[SPEC_BTDF] * specular_btdf_evaluate(m, wi, wo, dens[SPEC_BTDF]);
     return b;
 }
@@ -536,13 +571,18 @@ TT_HD float bsdf_total_pdf(const Lobes& l, const float* dens) {
     for (int i = 0; i < LOBE_COUNT; ++i) d += l.probs[i] * dens[i];
     return d;
 }
+template <uint32_t LS = LOBE_SET_ALL>
 TT_HD f3 bsdf_evaluate(const MatC& m, const Lobes& l, f3 wi, f3 wo, float& density) {
     float dens[LOBE_COUNT] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    f3 b = bsdf_evaluate_lobes(m, l, wi, wo, -1, dens);
+    f3 b = bsdf_evaluate_lobes<LS>(m, l, wi, wo, -1, dens);
     density = bsdf_total_pdf(l, dens);
     return b;
 }
+// A lobe outside LS has probability zero (or NaN) and is never the sampled one: its case below
+// is unreachable and compiled away.
+template <uint32_t LS = LOBE_SET_ALL>
 TT_HD f3 bsdf_sample(const MatC& m, const Lobes& l, f3 wi, uint32_t& g, f3& wo, float& density, int& sampled) {
+    static_assert(LS == LOBE_SET_ALL || (LS & ~LOBE_SET_BASE) == 0u, "lobe sets: all six, or within metal + dielectric");
     float rnd = random_float(g);
     float acc = 0.0f;
     int lobe = -1;
@@ -558,16 +598,24 @@ TT_HD f3 bsdf_sample(const MatC& m, const Lobes& l, f3 wi, uint32_t& g, f3& wo, 
     }
     float lobe_density = 0.0f;
     f3 lobe_bsdf = splat(0.0f);
-    switch (lobe) {
-        case FUZZ: lobe_bsdf = fuzz_brdf_sample(m, wi, g, wo, lobe_density); break;
-        case COAT: lobe_bsdf = coat_brdf_sample(m, wi, g, wo, lobe_density); break;
-        case METAL: lobe_bsdf = metal_brdf_sample(m, wi, g, wo, lobe_density); break;
-        case SPEC_BRDF: lobe_bsdf = specular_brdf_sample(m, wi, g, wo, lobe_density); break;
-        case SPEC_BTDF: lobe_bsdf = specular_btdf_sample(m, wi, g, wo, lobe_density); break;
-        default: lobe_bsdf = diffuse_brdf_sample(m, wi, g, wo, lobe_density); break;
+    if (LS == LOBE_SET_ALL) {
+        switch (lobe) {
+            case FUZZ: lobe_bsdf = fuzz_brdf_sample(m, wi, g, wo, lobe_density); break;
+            case COAT: lobe_bsdf = coat_brdf_sample(m, wi, g, wo, lobe_density); break;
+            case METAL: lobe_bsdf = metal_brdf_sample(m, wi, g, wo, lobe_density); break;
+            case SPEC_BRDF: lobe_bsdf = specular_brdf_sample(m, wi, g, wo, lobe_density); break;
+            case SPEC_BTDF: lobe_bsdf = specular_btdf_sample(m, wi, g, wo, lobe_density); break;
+            default: lobe_bsdf = diffuse_brdf_sample(m, wi, g, wo, lobe_density); break;
+        }
+    } else if (has_lobe<LS, METAL>() && (LS == LOBE_SET_METAL || lobe == METAL)) {
+        lobe_bsdf = metal_brdf_sample(m, wi, g, wo, lobe_density);
+    } else if (has_lobe<LS, SPEC_BRDF>() && lobe == SPEC_BRDF) {
+        lobe_bsdf = specular_brdf_sample(m, wi, g, wo, lobe_density);
+    } else if (has_lobe<LS, DIFFUSE>()) {
+        lobe_bsdf = diffuse_brdf_sample(m, wi, g, wo, lobe_density);
     }
     float dens[LOBE_COUNT] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    f3 b = bsdf_evaluate_lobes(m, l, wi, wo, lobe, dens);
+    f3 b = bsdf_evaluate_lobes<LS>(m, l, wi, wo, lobe, dens);
     f3 w = splat(0.0f);
 #pragma unroll
     for (int i = 0; i < LOBE_COUNT; ++i) {  // unrolled selects keep both arrays in registers

@@ -79,6 +79,7 @@ struct DevScene {
     const uint4* tlas;        // 8 x uint4 per node: the TLAS, or the flat BVH
     const float4* inst_xform; // 4 x float4 per instance: inverse rows 0..2, (mesh, material, index_offset, vertex_offset)
     const uint8_t* inst_bucket;  // shading-queue bucket of each instance's material (wavefront integrator)
+    uint32_t bucket_lobes;       // byte b: the union of the lobe sets (lobe_set_of) of bucket b's materials
     uint32_t emissive_count;
     uint32_t instance_count;
     uint32_t has_tlas;

@@ -29,6 +29,7 @@ struct RenderParams {
 
 // Wavefront integrator (wavefront.cu): device pointers of the slot pool and queues.
 constexpr uint32_t HIT_BUCKETS = 4;                // shading queues, one per material bucket
+static_assert(HIT_BUCKETS <= 4, "DevScene::bucket_lobes holds one byte per bucket");
 constexpr uint32_t CACHE_QUEUE = 5 + HIT_BUCKETS;  // counters word: queued radiance-cache queries
 constexpr uint32_t WF_CAMERA = 6 + HIT_BUCKETS;    // counters word: camera rays in the active queue
 constexpr uint32_t WF_CONTINUING = 7 + HIT_BUCKETS;  // counters word: continuing paths in the active queue

@@ -239,12 +239,12 @@ __device__ __forceinline__ f3 light_emission(const DevScene& sc, uint32_t light,
 
 // The contribution of integrate.glsl:186-192 when the light is visible (the light's emission
 // textures are sampled at mip level 4, integrate.glsl:188-189).
-template <bool TEX = false>
+template <bool TEX = false, uint32_t LS = LOBE_SET_ALL>
 __device__ __forceinline__ f3 light_contribution(const DevScene& sc, const LightSample& ls, const MatC& mat,
                                                  const Lobes& lobes, f3 wi) {
     f3 emissive = light_emission<TEX>(sc, ls.light, ls.uv, 4.0f);
     float bd = 0.0f;
-    f3 bsdf = bsdf_evaluate(mat, lobes, wi, ls.wo, bd);
+    f3 bsdf = bsdf_evaluate<LS>(mat, lobes, wi, ls.wo, bd);
     return bsdf * emissive * fabsf(cos_theta(ls.wo)) / fmx(ls.density, PDF_EPSILON);
 }
 

@@ -467,144 +467,184 @@ __global__ void __launch_bounds__(TR_BLOCK, TT_TRACE_MIN_BLOCKS) wf_trace_kernel
 #ifndef TT_SHADE_MIN_BLOCKS
 #define TT_SHADE_MIN_BLOCKS 8
 #endif
+// What the shading of one hit leaves for the block's appends (shadow ray, cache query, training record).
+struct ShadeOut {
+    bool want_shadow = false, want_cache = false, want_record = false;
+    uint32_t s = 0, light = 0;
+    f3 sh_org = splat(0.0f), sh_dir = splat(0.0f);
+    float qv[12];  // radiance-cache query of this vertex (cache or training record)
+    f3 rec_thr = splat(0.0f), rec_before = splat(0.0f);
+    uint32_t rec_path = 0;
+};
+
+// The shading of the hit at queue entry `at`, with the BSDF compiled for lobe set LS: every
+// material of the hit's bucket has its lobe set within LS, so the result is the six-lobe code's.
+template <bool CACHE, bool TEX, bool MULTI, uint32_t LS>
+__device__ __forceinline__ void shade_hit(const RenderParams& p, const WfParams& w, const BatchParams& b, uint64_t at,
+                                          ShadeOut& o) {
+    uint32_t s = w.hslot[at];
+    o.s = s;
+    uint4 hv = w.hit[at];
+    float4 o4 = w.org[s], d4 = w.dir[s], t4 = w.thr[s], a4 = w.acc[s];
+    uint32_t ow = __float_as_uint(o4.w);
+    uint32_t req = MULTI ? (ow >> BATCH_BOUNCE_BITS) & 0xffu : 0u;
+    const tt_constants& c = MULTI ? b.reqs[req].c : p.c;
+    const DevScene& sc = MULTI ? b.scenes[b.reqs[req].scene] : p.sc;
+    f3 thr = xyz(t4), acc = xyz(a4), ray_dir = xyz(d4);
+    uint32_t g = __float_as_uint(d4.w), bounce = MULTI ? ow & ((1u << BATCH_BOUNCE_BITS) - 1u) : ow;
+    uint32_t train = __float_as_uint(a4.w) & F_TRAIN;
+    ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
+    float mip_level = 1.0f;
+    if (TEX) {
+        float2 nm = w.ndc_mip[s];
+        if (bounce == 0u) {
+            mip_level = primary_mip_level(c, hit, xyz(o4), f2{nm.x, nm.y});
+            w.ndc_mip[s] = make_float2(mip_level, nm.y);
+        } else {
+            mip_level = nm.x;
+        }
+    }
+    const tt_material* material = sc.materials + hit.material_index;
+    MatC local;
+    const MatC& mc = hit_material<TEX>(sc, material, hit.uv, mip_level, local);
+    Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
+    {
+        if (CACHE) {
+            float ib = 0.5f / w.cache_bound;
+            o.qv[0] = hit.world_position.x * ib + 0.5f;
+            o.qv[1] = hit.world_position.y * ib + 0.5f;
+            o.qv[2] = hit.world_position.z * ib + 0.5f;
+            o.qv[3] = -ray_dir.x;
+            o.qv[4] = -ray_dir.y;
+            o.qv[5] = -ray_dir.z;
+            o.qv[6] = basis.normal.x;
+            o.qv[7] = basis.normal.y;
+            o.qv[8] = basis.normal.z;
+            o.qv[9] = mc.specular_roughness;
+            o.qv[10] = o.qv[11] = 0.0f;
+            if (w.spread_c > 0.0f) {
+                // path spread (neural radiance caching, Mueller et al. 2021, section 4):
+                // a += sqrt(d^2 / (p |cos|)) per vertex after the first, a0 from a uniform
+                // sphere pdf at the first; the path ends in the cache once a > c a0
+                float4 sp = w.spread[s];
+                f3 seg = hit.world_position - xyz(o4);
+                float d2 = dot(seg, seg);
+                float cs = fmaxf(fabsf(dot(basis.normal, ray_dir)), 1e-4f);
+                if (bounce == 0u) sp.y = sqrtf(d2 / (4.0f * PI * cs));
+                else sp.x += sqrtf(d2 / (fmaxf(sp.z, 1e-20f) * cs));
+                w.spread[s] = sp;
+                o.want_cache = !train && bounce >= w.cache_depth && sp.x > w.spread_c * sp.y;
+            } else {
+                o.want_cache = !train && bounce == w.cache_depth;
+            }
+            o.want_record = train != 0u;
+            o.rec_thr = thr;
+            o.rec_before = acc;
+            o.rec_path = (uint32_t)(((uint64_t)w.chunk_sample0 * w.WH + __float_as_uint(t4.w)) / w.train_stride);
+        }
+    }
+    if (o.want_cache) {  // the path ends in the cache: its radiance comes from the query
+        w.acc[s] = pack(acc, F_CACHE);
+    } else {
+        f3 wi = transform_from_basis(basis, -ray_dir);
+        Lobes lobes = bsdf_prepare<LS>(mc, wi, g);
+        bool nee = c.light_sampling == LIGHT_SAMPLING_NEE && sc.emissive_count > 0 && mc.specular_roughness > 0.15f;
+        f3 em = hit_emissive<TEX>(sc, material, hit.uv, mip_level);
+        if (nee) {
+            LightSample ls = sample_light(sc, hit.world_position, basis, g);
+            f3 contrib = light_contribution<TEX, LS>(sc, ls, mc, lobes, wi);
+            f3 a1 = thr * contrib, a0 = thr * splat(0.0f);
+            // When the visible and the occluded update have the same bits (the light faces
+            // away, or the BSDF is zero towards it) the shadow ray cannot change the result:
+            // apply the update here, in the order the shadow stage would, and trace nothing.
+            bool same = __float_as_uint(a1.x) == __float_as_uint(a0.x) &&
+                        __float_as_uint(a1.y) == __float_as_uint(a0.y) &&
+                        __float_as_uint(a1.z) == __float_as_uint(a0.z);
+            if (same) {
+                acc += a1;
+                if (bounce == 0u) acc += em * thr;
+            } else {
+                uint32_t pflags = (bounce == 0u ? 1u : 0u) | (ls.hash << 16);
+                w.pa1[s] = pack(a1, pflags);
+                w.pa0[s] = pack(a0, ls.prim);
+                w.pe[s] = pack(em * thr, 0u);
+                o.want_shadow = true;
+                o.light = ls.instance;
+                o.sh_org = hit.world_position;
+                o.sh_dir = ls.dir;
+            }
+        } else {
+            acc += em * thr;
+        }
+        uint32_t next = bounce + 1u;
+        if (next == c.bounce_count) {
+            // last vertex: the continuation ray would never be traced, so its BSDF sample
+            // (which changes only the generator and the throughput) is skipped
+            w.acc[s] = pack(acc, F_TERM | train);
+        } else {
+            float density = 1.0f;
+            f3 wo = splat(0.0f);
+            int lobe = 0;
+            f3 bsdf = bsdf_sample<LS>(mc, lobes, wi, g, wo, density, lobe);
+            if (CACHE && w.spread_c > 0.0f) w.spread[s].z = density;
+            f3 new_dir = transform_to_basis(basis, wo);
+            thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
+            w.org[s] = pack(hit.world_position, MULTI ? next | (req << BATCH_BOUNCE_BITS) : next);
+            w.dir[s] = pack(new_dir, g);
+            w.thr[s] = pack(thr, __float_as_uint(t4.w));
+            w.acc[s] = pack(acc, F_LIVE | train);
+        }
+    }
+}
+
 // MULTI: a shared-pool round; each path shades with its request's Constants and scene.
+// Single-request, untextured scenes: each bucket's queue starts on a block boundary, so a block
+// shades one bucket, and the block runs the shading compiled for the smallest lobe set covering
+// the bucket's materials (opaque dielectric, fully metallic, the two, or all six lobes).  The
+// variants leave out the code of lobes that carry no weight, and the registers it needs.
+// Textured materials can take metalness or transmission from a texel; they and shared-pool
+// rounds (whose buckets mix the requests' scenes) shade with all six lobes.
 template <bool CACHE, bool TEX, bool MULTI = false>
 __global__ void __launch_bounds__(WF_BLOCK, TT_SHADE_MIN_BLOCKS) wf_shade_kernel(const __grid_constant__ RenderParams p,
                                                             const __grid_constant__ WfParams w,
                                                             const __grid_constant__ BatchParams b) {
-    // thread q shades entry q of the bucket queues laid end to end
+    constexpr bool VARIANTS = !TEX && !MULTI;
+    // thread q shades entry q of the bucket queues laid end to end (VARIANTS: each queue padded
+    // to a multiple of the block)
     uint32_t q = blockIdx.x * WF_BLOCK + threadIdx.x;
     uint64_t at = 0;
-    uint32_t start = 0;
+    uint32_t start = 0, bucket = HIT_BUCKETS;
     bool have = false;
 #pragma unroll
-    for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
-        uint32_t cnt = w.counters[5 + b];
+    for (uint32_t k = 0; k < HIT_BUCKETS; ++k) {
+        uint32_t cnt = w.counters[5 + k];
+        uint32_t span = VARIANTS ? (cnt + WF_BLOCK - 1u) / WF_BLOCK * WF_BLOCK : cnt;
         bool in = !have && q >= start && q < start + cnt;
-        at = in ? (uint64_t)b * w.P + (q - start) : at;
+        bucket = bucket == HIT_BUCKETS && q >= start && q < start + span ? k : bucket;
+        at = in ? (uint64_t)k * w.P + (q - start) : at;
         have = have || in;
-        start += cnt;
+        start += span;
     }
-    bool want_shadow = false, want_cache = false, want_record = false;
-    uint32_t s = 0, light = 0;
-    f3 sh_org = splat(0.0f), sh_dir = splat(0.0f);
-    float qv[12];          // radiance-cache query of this vertex (cache or training record)
-    f3 rec_thr = splat(0.0f), rec_before = splat(0.0f);
-    uint32_t rec_path = 0;
-    if (have) {
-        s = w.hslot[at];
-        uint4 hv = w.hit[at];
-        float4 o4 = w.org[s], d4 = w.dir[s], t4 = w.thr[s], a4 = w.acc[s];
-        uint32_t ow = __float_as_uint(o4.w);
-        uint32_t req = MULTI ? (ow >> BATCH_BOUNCE_BITS) & 0xffu : 0u;
-        const tt_constants& c = MULTI ? b.reqs[req].c : p.c;
-        const DevScene& sc = MULTI ? b.scenes[b.reqs[req].scene] : p.sc;
-        f3 thr = xyz(t4), acc = xyz(a4), ray_dir = xyz(d4);
-        uint32_t g = __float_as_uint(d4.w), bounce = MULTI ? ow & ((1u << BATCH_BOUNCE_BITS) - 1u) : ow;
-        uint32_t train = __float_as_uint(a4.w) & F_TRAIN;
-        ShadeHit hit = get_ray_hit(sc, hv.z, hv.w, __uint_as_float(hv.x), __uint_as_float(hv.y));
-        float mip_level = 1.0f;
-        if (TEX) {
-            float2 nm = w.ndc_mip[s];
-            if (bounce == 0u) {
-                mip_level = primary_mip_level(c, hit, xyz(o4), f2{nm.x, nm.y});
-                w.ndc_mip[s] = make_float2(mip_level, nm.y);
-            } else {
-                mip_level = nm.x;
-            }
-        }
-        const tt_material* material = sc.materials + hit.material_index;
-        MatC local;
-        const MatC& mc = hit_material<TEX>(sc, material, hit.uv, mip_level, local);
-        Basis basis = create_surface_basis(hit.tangent_space, col3(mc.geometry_normal));
-        {
-            if (CACHE) {
-                float ib = 0.5f / w.cache_bound;
-                qv[0] = hit.world_position.x * ib + 0.5f;
-                qv[1] = hit.world_position.y * ib + 0.5f;
-                qv[2] = hit.world_position.z * ib + 0.5f;
-                qv[3] = -ray_dir.x;
-                qv[4] = -ray_dir.y;
-                qv[5] = -ray_dir.z;
-                qv[6] = basis.normal.x;
-                qv[7] = basis.normal.y;
-                qv[8] = basis.normal.z;
-                qv[9] = mc.specular_roughness;
-                qv[10] = qv[11] = 0.0f;
-                if (w.spread_c > 0.0f) {
-                    // path spread (neural radiance caching, Mueller et al. 2021, section 4):
-                    // a += sqrt(d^2 / (p |cos|)) per vertex after the first, a0 from a uniform
-                    // sphere pdf at the first; the path ends in the cache once a > c a0
-                    float4 sp = w.spread[s];
-                    f3 seg = hit.world_position - xyz(o4);
-                    float d2 = dot(seg, seg);
-                    float cs = fmaxf(fabsf(dot(basis.normal, ray_dir)), 1e-4f);
-                    if (bounce == 0u) sp.y = sqrtf(d2 / (4.0f * PI * cs));
-                    else sp.x += sqrtf(d2 / (fmaxf(sp.z, 1e-20f) * cs));
-                    w.spread[s] = sp;
-                    want_cache = !train && bounce >= w.cache_depth && sp.x > w.spread_c * sp.y;
-                } else {
-                    want_cache = !train && bounce == w.cache_depth;
-                }
-                want_record = train != 0u;
-                rec_thr = thr;
-                rec_before = acc;
-                rec_path = (uint32_t)(((uint64_t)w.chunk_sample0 * w.WH + __float_as_uint(t4.w)) / w.train_stride);
-            }
-        }
-        if (want_cache) {  // the path ends in the cache: its radiance comes from the query
-            w.acc[s] = pack(acc, F_CACHE);
+    ShadeOut o;
+    if (VARIANTS) {
+        uint32_t ls = bucket < HIT_BUCKETS ? (p.sc.bucket_lobes >> (8u * bucket)) & LOBE_SET_ALL : LOBE_SET_ALL;
+        if (!have) {
+        } else if ((ls & ~LOBE_SET_METAL) == 0u) {
+            shade_hit<CACHE, TEX, MULTI, LOBE_SET_METAL>(p, w, b, at, o);
+        } else if ((ls & ~LOBE_SET_DIELECTRIC) == 0u) {
+            shade_hit<CACHE, TEX, MULTI, LOBE_SET_DIELECTRIC>(p, w, b, at, o);
+        } else if ((ls & ~LOBE_SET_BASE) == 0u) {
+            shade_hit<CACHE, TEX, MULTI, LOBE_SET_BASE>(p, w, b, at, o);
         } else {
-            f3 wi = transform_from_basis(basis, -ray_dir);
-            Lobes lobes = bsdf_prepare(mc, wi, g);
-            bool nee = c.light_sampling == LIGHT_SAMPLING_NEE && sc.emissive_count > 0 && mc.specular_roughness > 0.15f;
-            f3 em = hit_emissive<TEX>(sc, material, hit.uv, mip_level);
-            if (nee) {
-                LightSample ls = sample_light(sc, hit.world_position, basis, g);
-                f3 contrib = light_contribution<TEX>(sc, ls, mc, lobes, wi);
-                f3 a1 = thr * contrib, a0 = thr * splat(0.0f);
-                // When the visible and the occluded update have the same bits (the light faces
-                // away, or the BSDF is zero towards it) the shadow ray cannot change the result:
-                // apply the update here, in the order the shadow stage would, and trace nothing.
-                bool same = __float_as_uint(a1.x) == __float_as_uint(a0.x) &&
-                            __float_as_uint(a1.y) == __float_as_uint(a0.y) &&
-                            __float_as_uint(a1.z) == __float_as_uint(a0.z);
-                if (same) {
-                    acc += a1;
-                    if (bounce == 0u) acc += em * thr;
-                } else {
-                    uint32_t pflags = (bounce == 0u ? 1u : 0u) | (ls.hash << 16);
-                    w.pa1[s] = pack(a1, pflags);
-                    w.pa0[s] = pack(a0, ls.prim);
-                    w.pe[s] = pack(em * thr, 0u);
-                    want_shadow = true;
-                    light = ls.instance;
-                    sh_org = hit.world_position;
-                    sh_dir = ls.dir;
-                }
-            } else {
-                acc += em * thr;
-            }
-            uint32_t next = bounce + 1u;
-            if (next == c.bounce_count) {
-                // last vertex: the continuation ray would never be traced, so its BSDF sample
-                // (which changes only the generator and the throughput) is skipped
-                w.acc[s] = pack(acc, F_TERM | train);
-            } else {
-                float density = 1.0f;
-                f3 wo = splat(0.0f);
-                int lobe = 0;
-                f3 bsdf = bsdf_sample(mc, lobes, wi, g, wo, density, lobe);
-                if (CACHE && w.spread_c > 0.0f) w.spread[s].z = density;
-                f3 new_dir = transform_to_basis(basis, wo);
-                thr *= bsdf / fmx(density, PDF_EPSILON) * fabsf(cos_theta(wo));
-                w.org[s] = pack(hit.world_position, MULTI ? next | (req << BATCH_BOUNCE_BITS) : next);
-                w.dir[s] = pack(new_dir, g);
-                w.thr[s] = pack(thr, __float_as_uint(t4.w));
-                w.acc[s] = pack(acc, F_LIVE | train);
-            }
+            shade_hit<CACHE, TEX, MULTI, LOBE_SET_ALL>(p, w, b, at, o);
         }
+    } else if (have) {
+        shade_hit<CACHE, TEX, MULTI, LOBE_SET_ALL>(p, w, b, at, o);
     }
+    const bool want_shadow = o.want_shadow, want_cache = o.want_cache, want_record = o.want_record;
+    const uint32_t s = o.s, light = o.light, rec_path = o.rec_path;
+    const f3 sh_org = o.sh_org, sh_dir = o.sh_dir, rec_thr = o.rec_thr, rec_before = o.rec_before;
+    const float* qv = o.qv;
     __shared__ uint32_t s_warp[WF_BLOCK / 32 + 1];
     uint32_t e = block_append<WF_BLOCK>(&w.counters[2], want_shadow, s_warp);
     if (want_shadow) {
@@ -715,8 +755,10 @@ static void launch_trace(const RenderParams& p, const WfParams& w, unsigned grid
     }
 }
 
+// `grid` covers the hits; each bucket's queue can be padded to a block boundary (one more block each).
 static void launch_shade(const RenderParams& p, const WfParams& w, unsigned grid, cudaStream_t st) {
     bool tex = p.sc.textured != 0u;
+    grid += HIT_BUCKETS;
     if (w.cache_on) {
         if (tex) wf_shade_kernel<true, true><<<grid, WF_BLOCK, 0, st>>>(p, w, BatchParams{});
         else wf_shade_kernel<true, false><<<grid, WF_BLOCK, 0, st>>>(p, w, BatchParams{});
