@@ -1,4 +1,5 @@
-"""Seeded OpenPBR material constants covering every lobe, for the BSDF parity tests."""
+"""Seeded OpenPBR material constants covering every lobe, for the BSDF parity tests, and a scene
+of spheres in those materials for the render parity tests."""
 import numpy as np
 
 from tinytrace_gb300.asset import Material
@@ -75,4 +76,38 @@ def sample_samples(rng, n: int) -> np.ndarray:
     wi[: 3 * n // 4, 2] = np.abs(wi[: 3 * n // 4, 2])
     s[:, 0:3] = wi
     s[:, 3] = rng.integers(1, 2**32, n, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    return s
+
+
+def material_spheres():
+    """Spheres in every material of the BSDF suite (coat, fuzz, glass, partly transmissive,
+    anisotropic, random mixtures) plus, carrying the most triangles, fully metallic, opaque
+    dielectric and half-metallic spheres: the three largest hit buckets (the wavefront shade
+    kernel's, ReSTIR's candidate pass's) then run the metal, dielectric and metal + dielectric
+    lobe sets, and the bucket that takes all other materials runs all six lobes."""
+    from tinytrace_gb300 import scenes
+    from tinytrace_gb300.asset import Model, Node
+    from tinytrace_gb300.asset import Scene as AssetScene
+
+    s = AssetScene()
+    light = s.insert_material(Material(emission_luminance=12.0, emission_color=(1.0, 0.95, 0.9)))
+    lq = scenes._quad((-3, 5, -3), (3, 5, -3), (3, 5, 3), (-3, 5, 3))  # facing -y, onto the spheres
+    s.root.children.append(Node(models=[Model(s.insert_mesh(lq[0], lq[3], lq[1], lq[2]), light)]))
+    floor = s.insert_material(Material(base_color=(0.6, 0.6, 0.55), specular_roughness=0.5))
+    g = scenes._quad((-8, -0.5, 8), (8, -0.5, 8), (8, -0.5, -8), (-8, -0.5, -8))
+    s.root.children.append(Node(models=[Model(s.insert_mesh(g[0], g[3], g[1], g[2]), floor)]))
+    big_pts, big_tris = scenes.geodesic_sphere(8)
+    small_pts, small_tris = scenes.geodesic_sphere(3)
+    big = s.insert_mesh(big_pts.astype(np.float32), None, big_tris)
+    small = s.insert_mesh(small_pts.astype(np.float32), None, small_tris)
+    mats = [(Material(base_metalness=1.0, specular_roughness=0.4, base_color=(0.9, 0.7, 0.4)), 4),
+            (Material(base_color=(0.3, 0.5, 0.8), specular_roughness=0.5), 3),
+            (Material(base_metalness=0.5, specular_roughness=0.45), 2)]
+    mats += [(m, 1) for m in material_objects()]
+    spheres = [(s.insert_material(m), big if n > 1 else small) for m, n in mats for _ in range(n)]
+    for i, (mat, mesh) in enumerate(spheres):
+        t = np.eye(4)
+        t[:3, :3] *= 0.42
+        t[:3, 3] = (-3.0 + (i % 7), 0.0, -3.0 + (i // 7))
+        s.root.children.append(Node(transform=t, models=[Model(mesh, mat)]))
     return s

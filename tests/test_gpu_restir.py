@@ -1,10 +1,11 @@
 """ReSTIR DI on the GPU (tt_render_restir) against the CPU oracle, bit for bit: images and the
 final reservoirs of every frame, with a moving camera (temporal reprojection), on scenes with
-few and with many lights and with textured materials and lights."""
+few and with many lights, with textured materials and lights, and with every lobe combination."""
 import numpy as np
 import pytest
 
 from conftest import assert_same_bits
+from materials import material_spheres
 from oracle import oracle
 from tinytrace_gb300 import scenes
 from tinytrace_gb300.camera import Camera
@@ -25,6 +26,8 @@ CASES = {
               (96, 54)),
     "instanced": (lambda: scenes.instanced_spheres(), (0.0, 0.0, 0.0), 40.0, 6.0, (80, 60)),
     "textured": (lambda: scenes.textured_cornell(), (0.0, 1.0, 0.0), 3.4, 1.0, (64, 48)),
+    # every lobe combination of the BSDF suite; the candidate pass runs each bucket's lobe set
+    "materials": (material_spheres, (0.0, 0.0, -0.5), 5.0, 3.0, (80, 60)),
 }
 
 

@@ -56,17 +56,23 @@ __device__ __forceinline__ void block_queue_append(const RestirParams& rp, uint3
     if (bucket < HIT_BUCKETS) rp.queue[(uint64_t)bucket * WH + s_base[bucket] + pos] = pixel;
 }
 
-// Pixel of queue entry q: the bucket queues are concatenated in bucket order.
-__device__ __forceinline__ bool queued_pixel(const RestirParams& rp, uint32_t WH, uint32_t q, uint64_t& i) {
+// Pixel of queue entry q: the bucket queues are concatenated in bucket order; with PAD each
+// queue starts on a block boundary, so that a block holds one bucket's pixels.  `bucket`
+// receives the bucket of a queued pixel.
+template <bool PAD = false>
+__device__ __forceinline__ bool queued_pixel(const RestirParams& rp, uint32_t WH, uint32_t q, uint64_t& i,
+                                             uint32_t& bucket) {
     uint32_t start = 0u;
 #pragma unroll
     for (uint32_t b = 0; b < HIT_BUCKETS; ++b) {
         uint32_t n = rp.queue_count[b];
         if (q < start + n) {
             i = rp.queue[(uint64_t)b * WH + (q - start)];
+            bucket = b;
             return true;
         }
-        start += n;
+        start += PAD ? (n + RT_BLOCK - 1u) / RT_BLOCK * RT_BLOCK : n;
+        if (q < start) return false;  // the padding after bucket b's queue
     }
     return false;
 }
@@ -208,15 +214,12 @@ __global__ void __launch_bounds__(RT_BLOCK) restir_gbuffer_kernel(const __grid_c
     block_queue_append(rp, bucket, y * W + x, (uint64_t)W * H);
 }
 
-template <bool TEX, int ACCEL>
-__global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_initial_kernel(const __grid_constant__ RenderParams p,
-                                                                  const __grid_constant__ RestirParams rp,
-                                                                  const Surface* gbuf, const float4* gtex, const float4* glob,
-                                                                  Reservoir* out, uint32_t candidates) {
-    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
-    const tt_constants& c = p.c;
-    uint64_t i = 0;
-    if (!queued_pixel(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i)) return;
+// Candidate generation for queued pixel i, with the BSDF compiled for lobe set LS (the lobe sets
+// of all materials of the pixel's bucket lie within LS, so the result is the six-lobe code's).
+template <bool TEX, int ACCEL, uint32_t LS>
+__device__ __forceinline__ Reservoir initial_pixel(const RenderParams& p, const Surface* gbuf, const float4* gtex,
+                                                   const float4* glob, uint64_t i, uint32_t candidates,
+                                                   uint32_t* stack) {
     const DevScene& sc = p.sc;
     ShadingState st;
     Reservoir r = empty_reservoir();
@@ -236,16 +239,43 @@ __global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_initial
             float r1 = random_float(g);
             float r2 = random_float(g);
             LightPoint lp = light_point<TEX>(sc, light, r1, r2);
-            float ph = luminance(restir_contribution(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
+            float ph = luminance(restir_contribution<LS>(*st.mc, st.lobes, st.basis, st.wi, st.pos, lp));
             float w = ph * (inv_p * lp.area);  // p^ / p, p = pick probability / area
             if (reservoir_update(r, light, r1, r2, w, 1.0f, g)) chosen = ph;
         }
         r.W = chosen > 0.0f ? r.w_sum / (r.M * chosen) : 0.0f;
         if (r.W > 0.0f) {
             LightPoint lp = light_point<TEX>(sc, r.light, r.r1, r.r2);
-            if (!restir_visible<false, ACCEL>(sc, st.pos, lp, r.light, s_stack + threadIdx.x, RT_BLOCK, p.err)) r.W = 0.0f;
+            if (!restir_visible<false, ACCEL>(sc, st.pos, lp, r.light, stack, RT_BLOCK, p.err)) r.W = 0.0f;
         }
     }
+    return r;
+}
+
+// Untextured scenes: the bucket queues are padded to block boundaries and each block evaluates
+// its candidates with the BSDF of its bucket's lobe set (metal, opaque dielectric, the two, or
+// all six lobes), which leaves the absent lobes' code and registers out of the candidate loop.
+// Textured materials can take metalness or transmission from a texel: they use all six lobes.
+template <bool TEX, int ACCEL>
+__global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_initial_kernel(const __grid_constant__ RenderParams p,
+                                                                  const __grid_constant__ RestirParams rp,
+                                                                  const Surface* gbuf, const float4* gtex, const float4* glob,
+                                                                  Reservoir* out, uint32_t candidates) {
+    __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
+    const tt_constants& c = p.c;
+    uint64_t i = 0;
+    uint32_t bucket = 0;
+    if (!queued_pixel<!TEX>(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i, bucket))
+        return;
+    uint32_t* stack = s_stack + threadIdx.x;
+    Reservoir r;
+    uint32_t ls = TEX ? LOBE_SET_ALL : (p.sc.bucket_lobes >> (8u * bucket)) & LOBE_SET_ALL;
+    if ((ls & ~LOBE_SET_METAL) == 0u) r = initial_pixel<TEX, ACCEL, LOBE_SET_METAL>(p, gbuf, gtex, glob, i, candidates, stack);
+    else if ((ls & ~LOBE_SET_DIELECTRIC) == 0u)
+        r = initial_pixel<TEX, ACCEL, LOBE_SET_DIELECTRIC>(p, gbuf, gtex, glob, i, candidates, stack);
+    else if ((ls & ~LOBE_SET_BASE) == 0u)
+        r = initial_pixel<TEX, ACCEL, LOBE_SET_BASE>(p, gbuf, gtex, glob, i, candidates, stack);
+    else r = initial_pixel<TEX, ACCEL, LOBE_SET_ALL>(p, gbuf, gtex, glob, i, candidates, stack);
     out[i] = r;
 }
 
@@ -375,7 +405,8 @@ __global__ void __launch_bounds__(RT_BLOCK, TT_RESTIR_MIN_BLOCKS) restir_shade_k
     __shared__ uint32_t s_stack[TRAVERSAL_STACK * RT_BLOCK];
     const tt_constants& c = p.c;
     uint64_t i = 0;
-    if (!queued_pixel(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i)) return;
+    uint32_t bucket = 0;
+    if (!queued_pixel(rp, c.screen_size[0] * c.screen_size[1], blockIdx.x * RT_BLOCK + threadIdx.x, i, bucket)) return;
     const DevScene& sc = p.sc;
     ShadingState st;
     f3 radiance;
@@ -400,12 +431,13 @@ static void restir_passes(const RenderParams& p, const RestirParams& rp, cudaStr
     dim3 grid((c.screen_size[0] + RT_TILE_X - 1) / RT_TILE_X, (c.screen_size[1] + RT_TILE_Y - 1) / RT_TILE_Y);
     uint64_t WH = (uint64_t)c.screen_size[0] * c.screen_size[1];
     unsigned qgrid = (unsigned)((WH + RT_BLOCK - 1) / RT_BLOCK);  // enough blocks for every pixel queued
+    unsigned padded_qgrid = qgrid + HIT_BUCKETS;                       // and for each queue padded to a block
     check_cuda(cudaMemsetAsync(rp.queue_count, 0, 4ull * HIT_BUCKETS, st), "memset");
     stage_begin(timer, TT_STAGE_RESTIR_GBUFFER, st);
     restir_gbuffer_kernel<TEX, ACCEL><<<grid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_INITIAL, st);
-    restir_initial_kernel<TEX, ACCEL><<<qgrid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.initial,
+    restir_initial_kernel<TEX, ACCEL><<<padded_qgrid, RT_BLOCK, 0, st>>>(p, rp, rp.gbuf, rp.gtex, rp.glob, rp.initial,
                                                                  rp.candidates);
     stage_end(timer, st);
     stage_begin(timer, TT_STAGE_RESTIR_TEMPORAL, st);

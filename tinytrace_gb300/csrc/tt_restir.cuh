@@ -102,7 +102,9 @@ __device__ __forceinline__ LightPoint light_point(const DevScene& sc, uint32_t l
     return lp;
 }
 
-// Unshadowed contribution f * Le * |cos| * cosL / d^2 of light point lp at the surface.
+// Unshadowed contribution f * Le * |cos| * cosL / d^2 of light point lp at the surface (the
+// surface's material has its lobe set within LS).
+template <uint32_t LS = LOBE_SET_ALL>
 __device__ __forceinline__ f3 restir_contribution(const MatC& mc, const Lobes& lobes, const Basis& basis, f3 wi,
                                                   f3 pos, const LightPoint& lp) {
     f3 d = lp.pos - pos;
@@ -112,7 +114,7 @@ __device__ __forceinline__ f3 restir_contribution(const MatC& mc, const Lobes& l
     if (!(cos_light > 0.0f) || !(d2 > 0.0f)) return splat(0.0f);
     f3 wo = transform_from_basis(basis, d);
     float density = 0.0f;
-    f3 f = bsdf_evaluate(mc, lobes, wi, wo, density);
+    f3 f = bsdf_evaluate<LS>(mc, lobes, wi, wo, density);
     return f * lp.emission * (fabsf(cos_theta(wo)) * cos_light / d2);
 }
 
