@@ -190,3 +190,48 @@ def test_suite_outputs_are_finite():
         smp = _sample(m, wi, _seeds(rng, n))
         assert np.isfinite(smp[:, 0:8]).all()
         assert (smp[:, 3] >= 0).all()
+
+
+# Lobe indices of the BSDF (bsdf.glsl:15-31): fuzz, coat, metal, specular BRDF, specular BTDF,
+# diffuse.
+FUZZ, COAT, METAL, SPEC_BRDF, SPEC_BTDF, DIFFUSE = range(6)
+
+
+def _lobe_set(m) -> int:
+    """The lobes whose albedo bsdf_prepare computes (bsdf.glsl:39-59), as the device's
+    tt_bsdf.cuh: lobe_set_of states them: outside this set a lobe's albedo is zero."""
+    f32 = np.float32
+    fully_metallic = m["base_metalness"] == f32(1.0)
+    s = 0
+    if m["fuzz_weight"] > 0:
+        s |= 1 << FUZZ
+    if m["coat_weight"] > 0:
+        s |= 1 << COAT
+    if m["base_metalness"] > 0:
+        s |= 1 << METAL
+    if not fully_metallic:
+        s |= 1 << SPEC_BRDF
+    if not fully_metallic and m["transmission_weight"] > 0:
+        s |= 1 << SPEC_BTDF
+    if not fully_metallic and m["transmission_weight"] != f32(1.0):
+        s |= 1 << DIFFUSE
+    return s
+
+
+def test_sampled_lobes_lie_in_the_lobe_set():
+    """The shading kernels compile the BSDF per lobe set and leave out the lobes outside a
+    material's set, which is exact only if such a lobe is never chosen: over the suite's 33
+    materials and both hemispheres, the oracle samples no lobe outside lobe_set_of, and each
+    sampled lobe index is one the set allows."""
+    rng = np.random.default_rng(17)
+    seen = set()
+    for m in material_suite():
+        allowed = _lobe_set(m)
+        n = 4000
+        wi = random_directions(rng, n)
+        smp = _sample(m, wi, _seeds(rng, n))
+        lobes = smp[:, 7].astype(np.int64)
+        picked = lobes[lobes >= 0]
+        assert all((allowed >> int(k)) & 1 for k in np.unique(picked)), (allowed, np.unique(picked))
+        seen.update(int(k) for k in np.unique(picked))
+    assert seen == set(range(6))  # every lobe is sampled somewhere in the suite
